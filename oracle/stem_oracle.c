@@ -1,0 +1,1218 @@
+/*
+ * ORACLE -- test infrastructure only (see stem_oracle.h).
+ *
+ * Plain-C restatement of simulated_tem's imaging hot path.  Every function
+ * names the reference lines it follows.  Compiled with -O2 -ffp-contract=off so
+ * that the left-to-right double arithmetic of the reference is kept.
+ */
+#include "stem_oracle.h"
+
+#include <float.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* PI of Lib_DynamicalTwoBeamImaging.f90:55 and Lib_DiffractionConditions.f90:21. */
+static const double PI = 3.141592653589790;
+/* Lib_RelativisticElectrons.f90:9-14. */
+static const double ME = 0.056856301036;
+static const double EC = 1.0;
+static const double CL = 2997.92458;
+static const double HP = 4.135667696;
+#define HBAR (HP / (2 * 3.14159265390))
+/* huge(1.0): the default-kind (single precision) largest value. */
+static const double HUGE1 = (double)FLT_MAX;
+
+#define A(m, i, j) ((m)[((i)-1) + 3 * ((j)-1)])
+
+/* ------------------------------------------------------------------------ */
+/* small linear algebra                                                     */
+/* ------------------------------------------------------------------------ */
+
+/* gfortran's NORM2: scaled sum of squares. */
+double oc_norm2(const double* v) {
+  double scale = 0.0, res = 1.0;
+  for (int i = 0; i < 3; ++i) {
+    if (v[i] != 0.0) {
+      double ax = fabs(v[i]);
+      if (scale < ax) {
+        double val = scale / ax;
+        res = 1.0 + res * val * val;
+        scale = ax;
+      } else {
+        double val = ax / scale;
+        res += val * val;
+      }
+    }
+  }
+  return sqrt(res) * scale;
+}
+
+/* determinant3Mat (Lib_SimpleSupercells.f90:1240-1256). */
+double oc_det3(const double* M) {
+  double dd[9];
+  dd[0] = A(M, 1, 1) * (A(M, 2, 2) * A(M, 3, 3) - A(M, 2, 3) * A(M, 3, 2));
+  dd[1] = A(M, 1, 2) * (A(M, 2, 3) * A(M, 3, 1) - A(M, 2, 1) * A(M, 3, 3));
+  dd[2] = A(M, 1, 3) * (A(M, 2, 1) * A(M, 3, 2) - A(M, 2, 2) * A(M, 3, 1));
+  dd[3] = A(M, 2, 1) * (A(M, 3, 2) * A(M, 1, 3) - A(M, 3, 3) * A(M, 1, 2));
+  dd[4] = A(M, 2, 2) * (A(M, 3, 3) * A(M, 1, 1) - A(M, 3, 1) * A(M, 1, 3));
+  dd[5] = A(M, 2, 3) * (A(M, 3, 1) * A(M, 1, 2) - A(M, 3, 2) * A(M, 1, 1));
+  dd[6] = A(M, 3, 1) * (A(M, 1, 2) * A(M, 2, 3) - A(M, 1, 3) * A(M, 2, 2));
+  dd[7] = A(M, 3, 2) * (A(M, 1, 3) * A(M, 2, 1) - A(M, 1, 1) * A(M, 2, 3));
+  dd[8] = A(M, 3, 3) * (A(M, 1, 1) * A(M, 2, 2) - A(M, 1, 2) * A(M, 2, 1));
+  double s = 0.0;
+  for (int i = 0; i < 9; ++i) s += dd[i];
+  return (1.0 / 3.0) * s;
+}
+
+/* inverse3Mat (Lib_SimpleSupercells.f90:1205-1236). */
+void oc_inv3(const double* M, double* N) {
+  double idd = oc_det3(M);
+  if (fabs(idd) < DBL_MIN) {
+    memset(N, 0, 9 * sizeof(double));
+    N[0] = N[4] = N[8] = 1.0;
+    return;
+  }
+  idd = 1.0 / idd;
+  A(N, 1, 1) = (A(M, 2, 2) * A(M, 3, 3) - A(M, 2, 3) * A(M, 3, 2)) * idd;
+  A(N, 2, 1) = (A(M, 2, 3) * A(M, 3, 1) - A(M, 2, 1) * A(M, 3, 3)) * idd;
+  A(N, 3, 1) = (A(M, 2, 1) * A(M, 3, 2) - A(M, 2, 2) * A(M, 3, 1)) * idd;
+  A(N, 1, 2) = (A(M, 1, 3) * A(M, 3, 2) - A(M, 1, 2) * A(M, 3, 3)) * idd;
+  A(N, 2, 2) = (A(M, 1, 1) * A(M, 3, 3) - A(M, 1, 3) * A(M, 3, 1)) * idd;
+  A(N, 3, 2) = (A(M, 1, 2) * A(M, 3, 1) - A(M, 1, 1) * A(M, 3, 2)) * idd;
+  A(N, 1, 3) = (A(M, 1, 2) * A(M, 2, 3) - A(M, 1, 3) * A(M, 2, 2)) * idd;
+  A(N, 2, 3) = (A(M, 1, 3) * A(M, 2, 1) - A(M, 1, 1) * A(M, 2, 3)) * idd;
+  A(N, 3, 3) = (A(M, 1, 1) * A(M, 2, 2) - A(M, 1, 2) * A(M, 2, 1)) * idd;
+}
+
+/* matmul of two 3x3 matrices, k ascending. */
+static void mat_mul(const double* a, const double* b, double* c) {
+  double t[9];
+  for (int j = 1; j <= 3; ++j)
+    for (int i = 1; i <= 3; ++i) {
+      double s = 0.0;
+      for (int k = 1; k <= 3; ++k) s += A(a, i, k) * A(b, k, j);
+      A(t, i, j) = s;
+    }
+  memcpy(c, t, sizeof t);
+}
+
+static void transpose3(const double* a, double* t) {
+  for (int i = 1; i <= 3; ++i)
+    for (int j = 1; j <= 3; ++j) A(t, i, j) = A(a, j, i);
+}
+
+/* y(1:3) = m(1:3,1)*v(1) + m(1:3,2)*v(2) + m(1:3,3)*v(3) */
+static void mat_vec(const double* m, const double* v, double* y) {
+  double t[3];
+  for (int i = 1; i <= 3; ++i) t[i - 1] = A(m, i, 1) * v[0] + A(m, i, 2) * v[1] + A(m, i, 3) * v[2];
+  y[0] = t[0];
+  y[1] = t[1];
+  y[2] = t[2];
+}
+
+static void identity3(double* m) {
+  memset(m, 0, 9 * sizeof(double));
+  m[0] = m[4] = m[8] = 1.0;
+}
+
+static int imod(int a, int n) { /* Fortran mod: sign of a */
+  return a % n;
+}
+
+/* ------------------------------------------------------------------------ */
+/* SimpleSupercell                                                          */
+/* ------------------------------------------------------------------------ */
+
+/* SimpleSupercell_ctor0 (Lib_SimpleSupercells.f90:183-196). */
+void oc_super_ctor(oc_super* s, const double* a, int Nx, int Ny, int Nz) {
+  memcpy(s->a, a, 9 * sizeof(double));
+  s->Nx = Nx;
+  s->Ny = Ny;
+  s->Nz = Nz;
+  oc_inv3(s->a, s->ia);
+}
+
+/* cellToRealSpace2 (Lib_SimpleSupercells.f90:338-345). */
+static void cell_to_real_i(const oc_super* s, int ix, int iy, int iz, double* y) {
+  for (int i = 1; i <= 3; ++i)
+    y[i - 1] = A(s->a, i, 1) * (double)ix + A(s->a, i, 2) * (double)iy + A(s->a, i, 3) * (double)iz;
+}
+
+/* realSpaceToCell0 (Lib_SimpleSupercells.f90:348-356). */
+static void real_to_cell(const oc_super* s, const double* y, double* x) { mat_vec(s->ia, y, x); }
+
+/* pointInSupercell0 (Lib_SimpleSupercells.f90:1063-1102). */
+static int point_in_super(const oc_super* s, const double* x) {
+  int ix = (int)floor(A(s->ia, 1, 1) * x[0] + A(s->ia, 1, 2) * x[1] + A(s->ia, 1, 3) * x[2]);
+  int is = (ix == imod(ix + (s->Nx << 8), s->Nx));
+  int iy = (int)floor(A(s->ia, 2, 1) * x[0] + A(s->ia, 2, 2) * x[1] + A(s->ia, 2, 3) * x[2]);
+  is = is && (iy == imod(iy + (s->Ny << 8), s->Ny));
+  int iz = (int)floor(A(s->ia, 3, 1) * x[0] + A(s->ia, 3, 2) * x[1] + A(s->ia, 3, 3) * x[2]);
+  is = is && (iz == imod(iz + (s->Nz << 8), s->Nz));
+  return is;
+}
+
+/* wrapPBC0 (Lib_SimpleSupercells.f90:992-1023). */
+void oc_wrap_pbc(const oc_super* s, const double* y, double* yp) {
+  double xx[3];
+  real_to_cell(s, y, xx);
+  int N[3] = {s->Nx, s->Ny, s->Nz};
+  for (int d = 0; d < 3; ++d) {
+    int ii = (int)floor(xx[d]);
+    xx[d] = xx[d] - ii;
+    ii = imod(ii + (N[d] << 8), N[d]);
+    xx[d] = (ii + xx[d]);
+  }
+  mat_vec(s->a, xx, yp);
+}
+
+static double cell_side_length(const oc_super* s, int i) { return oc_norm2(&s->a[3 * (i - 1)]); }
+
+/* getSuperCellSideLength0 (Lib_SimpleSupercells.f90:862-876). */
+static double super_side_length(const oc_super* s, int i) {
+  int N = (i == 1) ? s->Nx : (i == 2) ? s->Ny : s->Nz;
+  return oc_norm2(&s->a[3 * (i - 1)]) * N;
+}
+
+/* getSuperA (Lib_SimpleSupercells.f90:851-860). */
+static void super_a(const oc_super* s, double* a) {
+  for (int i = 0; i < 3; ++i) {
+    a[i] = s->a[i] * s->Nx;
+    a[3 + i] = s->a[3 + i] * s->Ny;
+    a[6 + i] = s->a[6 + i] * s->Nz;
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Lib_RelativisticElectrons / Lib_DiffractionConditions                    */
+/* ------------------------------------------------------------------------ */
+
+/* wavelength (Lib_RelativisticElectrons.f90:25-38). */
+double oc_wavelength(double V) {
+  if (V <= 0) return 0.0;
+  double lambda = 2 * ME * EC * V * (1 + EC * V / (2 * ME * CL * CL));
+  return HP / sqrt(lambda);
+}
+
+/* velocity (Lib_RelativisticElectrons.f90:40-50). */
+double oc_velocity(double V) {
+  double u = 1 + EC * V / (ME * CL * CL);
+  return CL * sqrt(1 - 1 / (u * u));
+}
+
+/* getReciprocalLatticeVectors (Lib_DiffractionConditions.f90:1630-1640). */
+static void reciprocal(const double* A_cell, double* B) {
+  double t[9];
+  transpose3(A_cell, t);
+  oc_inv3(t, B);
+  for (int i = 0; i < 9; ++i) B[i] = 2 * PI * B[i];
+}
+
+/* reflection1 (Lib_DiffractionConditions.f90:1656-1667). */
+static void reflection(const double* B, const double* hkl, double* g) {
+  double t[3];
+  for (int i = 1; i <= 3; ++i) t[i - 1] = A(B, i, 1) * hkl[0] + A(B, i, 2) * hkl[1] + A(B, i, 3) * hkl[2];
+  memcpy(g, t, sizeof t);
+}
+
+/* energyToLengthDeviationParameter (Lib_DiffractionConditions.f90:1194-1204). */
+static double energy_to_length_sg(double v, double eps) { return -eps / (2 * PI * HBAR * v); }
+
+/* energy_deviation_parameter (Lib_DiffractionConditions.f90:1265-1299). */
+static double energy_deviation_parameter(double v, const double* khat, const double* g) {
+  const double HBAR2ON2M = HBAR * HBAR / (2 * ME);
+  double cst = 2 * ME * v / HBAR;
+  double eps = khat[0] * g[0] + khat[1] * g[1] + khat[2] * g[2];
+  eps = cst * eps;
+  eps = eps + g[0] * g[0] + g[1] * g[1] + g[2] * g[2];
+  return eps * HBAR2ON2M;
+}
+
+/* intensityAtDepthZ (Lib_DiffractionConditions.f90:1209-1259). */
+double oc_intensity_at_depth(double xi0, double xig, double sg, double z) {
+  double b0 = PI / xi0, bg = PI / xig, aa = 2 * PI * sg;
+  double dd = sqrt(aa * aa / 4 + bg * bg);
+  double l1 = (b0 + aa / 2) + dd, l2 = (b0 + aa / 2) - dd;
+  double re = cos(l1 * z) - cos(l2 * z), im = sin(l1 * z) - sin(l2 * z);
+  double s = bg / (2 * dd);
+  re *= s;
+  im *= s;
+  return re * re + im * im;
+}
+
+static void cross3(const double* x, const double* y, double* z) {
+  z[0] = x[1] * y[2] - x[2] * y[1];
+  z[1] = x[2] * y[0] - x[0] * y[2];
+  z[2] = x[0] * y[1] - x[1] * y[0];
+}
+
+/* rotateToStandardFrame0 (Lib_DiffractionConditions.f90:65-108). */
+void oc_rotate_to_standard_frame(const double* z0, const double* A_cell, const double* hkl, double* U) {
+  double BB[9], gg[3], zz[3], xx[3], yy[3];
+  reciprocal(A_cell, BB);
+  reflection(BB, hkl, gg);
+  for (int i = 1; i <= 3; ++i) {
+    double s = 0.0;
+    for (int k = 1; k <= 3; ++k) s += A(A_cell, i, k) * z0[k - 1];
+    zz[i - 1] = s;
+  }
+  double nz = oc_norm2(zz);
+  for (int i = 0; i < 3; ++i) zz[i] = zz[i] / nz;
+  double gz = 0.0;
+  for (int i = 0; i < 3; ++i) gz += gg[i] * zz[i];
+  for (int i = 0; i < 3; ++i) xx[i] = gg[i] - gz * zz[i];
+  double nx = oc_norm2(xx);
+  for (int i = 0; i < 3; ++i) xx[i] = xx[i] / nx;
+  cross3(zz, xx, yy);
+  for (int j = 1; j <= 3; ++j) {
+    A(U, 1, j) = xx[j - 1];
+    A(U, 2, j) = yy[j - 1];
+    A(U, 3, j) = zz[j - 1];
+  }
+}
+
+/* findTransformedSupercell (Lib_DiffractionConditions.f90:996-1189): the
+ * cuboid D, the offset delta and the 27 periodic replicas. */
+static void find_transformed_supercell(const double* A_super, const double* R, double* D_super, double* delta,
+                                       int* uvw, int* nuvw, const double* foil) {
+  double dd[3] = {foil[0], foil[1], foil[2]}, xx[3];
+  memset(D_super, 0, 9 * sizeof(double));
+  A(D_super, 1, 1) = dd[0];
+  A(D_super, 2, 2) = dd[1];
+  A(D_super, 3, 3) = dd[2];
+  xx[0] = xx[1] = xx[2] = 0.5;
+  mat_vec(A_super, xx, xx);
+  mat_vec(R, xx, xx);
+  for (int i = 0; i < 3; ++i) delta[i] = dd[i] / 2 - xx[i];
+  int n = 0;
+  for (int iz = -1; iz <= 1; ++iz)
+    for (int iy = -1; iy <= 1; ++iy)
+      for (int ix = -1; ix <= 1; ++ix) {
+        uvw[3 * n + 0] = ix;
+        uvw[3 * n + 1] = iy;
+        uvw[3 * n + 2] = iz;
+        ++n;
+      }
+  *nuvw = n;
+}
+
+/* ------------------------------------------------------------------------ */
+/* DynamicalTwoBeamImaging                                                  */
+/* ------------------------------------------------------------------------ */
+
+/* DynamicalTwoBeamImaging_ctor0 / _null (Lib_DynamicalTwoBeamImaging.f90:125-178). */
+void oc_d2bi_ctor(oc_d2bi* t, const oc_super* super, double a0, const double* k, const double* g, double E,
+                  int mxy, int mzz) {
+  memset(t, 0, sizeof *t);
+  t->super = *super;
+  double id[9];
+  identity3(id);
+  oc_super_ctor(&t->gksuper, id, 1, 1, 1);
+  t->a0 = a0;
+  t->xi0 = 103.9;
+  t->xig = 207.5;
+  t->useDensityField = 1;
+  for (int i = 0; i < 9; ++i) t->a_cell[i] = a0 * id[i];
+  t->sg = NAN;
+  t->nuvw = 1;
+  identity3(t->R);
+  identity3(t->U);
+  t->test = 0;
+  memcpy(t->k, k, 3 * sizeof(double));
+  memcpy(t->g, g, 3 * sizeof(double));
+  t->E = E;
+  t->mxy = mxy;
+  t->mzz = mzz;
+}
+
+void oc_set_conventional_unit_cell(oc_d2bi* t, const double* a_cell) { memcpy(t->a_cell, a_cell, 9 * sizeof(double)); }
+
+/* setVoxelSupercellSize2 (Lib_DynamicalTwoBeamImaging.f90:349-430) for
+ * cuboidSides with all three entries nonzero (the d2bi path). */
+int oc_set_voxel_supercell_size(oc_d2bi* t, const double* cs) {
+  double hkl[3] = {(double)lround(t->g[0]), (double)lround(t->g[1]), (double)lround(t->g[2])};
+  oc_rotate_to_standard_frame(t->k, t->a_cell, hkl, t->U);
+  if (cs[0] == 0 || cs[1] == 0 || cs[2] == 0) return OC_ERR_ARG;
+  memcpy(t->voxelSupercellDimensions, cs, 3 * sizeof(double));
+  return OC_OK;
+}
+
+void oc_set_deviation_parameter(oc_d2bi* t, double sg) { t->sg = sg; }
+void oc_set_extinction_distances(oc_d2bi* t, double xi0, double xig) {
+  t->xi0 = xi0;
+  t->xig = xig;
+}
+void oc_set_use_density_field(oc_d2bi* t, int is) { t->useDensityField = is; }
+
+/* getAperture (Lib_DynamicalTwoBeamImaging.f90:1137-1155). */
+void oc_get_aperture(const oc_d2bi* t, const double* beamTilt, double* g) {
+  double b[9], RU[9];
+  reciprocal(t->a_cell, b);
+  reflection(b, t->g, g);
+  mat_mul(t->R, t->U, RU);
+  if (beamTilt) mat_mul(beamTilt, RU, RU);
+  mat_vec(RU, g, g);
+}
+
+/* getDeviationParameter (Lib_DynamicalTwoBeamImaging.f90:292-307). */
+double oc_get_deviation_parameter(const oc_d2bi* t, const double* g) {
+  if (!g) return t->sg;
+  double modk = 2 * PI / oc_wavelength(t->E * 1000);
+  double vv = HBAR * modk / ME;
+  const double khat[3] = {0.0, 0.0, 1.0};
+  double eps = energy_deviation_parameter(vv, khat, g);
+  return energy_to_length_sg(vv, eps);
+}
+
+/* gksuper from D_super (Lib_DynamicalTwoBeamImaging.f90:775-784, 1086-1096). */
+static void build_gksuper(oc_d2bi* t, double* D) {
+  int Nx = t->mxy, Ny = t->mxy, Nz = t->mzz;
+  int nx = (int)lround(t->mxy * A(D, 1, 1) / t->a0);
+  int ny = (int)lround(t->mxy * A(D, 2, 2) / t->a0);
+  int nz = (int)lround(t->mzz * A(D, 3, 3) / t->a0);
+  if (nx > Nx) Nx = nx;
+  if (ny > Ny) Ny = ny;
+  if (nz > Nz) Nz = nz;
+  A(D, 1, 1) = A(D, 1, 1) / Nx;
+  A(D, 2, 2) = A(D, 2, 2) / Ny;
+  A(D, 3, 3) = A(D, 3, 3) / Nz;
+  oc_super_ctor(&t->gksuper, D, Nx, Ny, Nz);
+}
+
+static void tilt_about_y(double theta, double* R) {
+  double c = cos(theta), s = sin(theta);
+  /* reshape((/cos,0,-sin, 0,1,0, sin,0,cos/),(/3,3/)) */
+  R[0] = c;
+  R[1] = 0.0;
+  R[2] = -s;
+  R[3] = 0.0;
+  R[4] = 1.0;
+  R[5] = 0.0;
+  R[6] = s;
+  R[7] = 0.0;
+  R[8] = c;
+}
+
+/* setSupercellTilt0 (Lib_DynamicalTwoBeamImaging.f90:567-792). */
+void oc_set_supercell_tilt0(oc_d2bi* t) {
+  double hkl[3] = {(double)lround(t->g[0]), (double)lround(t->g[1]), (double)lround(t->g[2])};
+  oc_rotate_to_standard_frame(t->k, t->a_cell, hkl, t->U);
+  double a_cell0[9], b_cell[9], gg[3], a_cell[9];
+  mat_mul(t->U, t->a_cell, a_cell0);
+  reciprocal(a_cell0, b_cell);
+  reflection(b_cell, t->g, gg);
+  double modg = oc_norm2(gg);
+  double modk = 2 * PI / oc_wavelength(t->E * 1000);
+  double vv = HBAR * modk / ME;
+  const double khat[3] = {0.0, 0.0, 1.0};
+  double eps = energy_deviation_parameter(vv, khat, gg);
+  if (isnan(t->sg)) {
+    t->sg = energy_to_length_sg(vv, eps);
+    identity3(t->R);
+  } else {
+    double aa = 2 * PI * t->sg + HBAR * modg * modg / (2 * ME * vv);
+    double cc = gg[0] * gg[0] + gg[2] * gg[2];
+    double bb = cc - aa * aa;
+    if (bb < 0) {
+      t->sg = energy_to_length_sg(vv, eps);
+      identity3(t->R);
+    } else {
+      bb = sqrt(bb);
+      cc = 1 / cc;
+      double th[4], sgs[4];
+      th[0] = acos(-(gg[2] * aa + gg[0] * bb) * cc);
+      th[1] = acos(-(gg[2] * aa - gg[0] * bb) * cc);
+      th[2] = -th[0];
+      th[3] = -th[1];
+      for (int i = 0; i < 4; ++i) {
+        double g2[3];
+        tilt_about_y(th[i], t->R);
+        mat_mul(t->R, a_cell0, a_cell);
+        reciprocal(a_cell, b_cell);
+        reflection(b_cell, t->g, g2);
+        sgs[i] = energy_to_length_sg(vv, energy_deviation_parameter(vv, khat, g2));
+      }
+      for (int i = 0; i < 4; ++i)
+        if (fabs(th[i]) * 2 > PI) sgs[i] = HUGE1;
+      /* minloc of |sg - sg_i|: first minimum wins */
+      int best = 0;
+      double bestv = fabs(t->sg - sgs[0]);
+      for (int i = 1; i < 4; ++i) {
+        double v = fabs(t->sg - sgs[i]);
+        if (v < bestv) {
+          bestv = v;
+          best = i;
+        }
+      }
+      tilt_about_y(th[best], t->R);
+    }
+    mat_mul(t->R, a_cell0, a_cell);
+    reciprocal(a_cell, b_cell);
+    reflection(b_cell, t->g, gg);
+    eps = energy_deviation_parameter(vv, khat, gg);
+    t->sg = energy_to_length_sg(vv, eps);
+  }
+  double RU[9], a_sup[9], D[9];
+  mat_mul(t->R, t->U, RU);
+  super_a(&t->super, a_sup);
+  find_transformed_supercell(a_sup, RU, D, t->delta, t->uvw, &t->nuvw, t->voxelSupercellDimensions);
+  build_gksuper(t, D);
+  oc_get_aperture(t, NULL, gg);
+  t->sg = oc_get_deviation_parameter(t, gg);
+}
+
+/* setSupercellTilt2 (Lib_DynamicalTwoBeamImaging.f90:1048-1122). */
+void oc_set_supercell_tilt2(oc_d2bi* t, const double* U, const double* R) {
+  memcpy(t->U, U, 9 * sizeof(double));
+  memcpy(t->R, R, 9 * sizeof(double));
+  double a_sup[9], RU[9], D[9], gg[3];
+  super_a(&t->super, a_sup);
+  mat_mul(t->R, t->U, RU);
+  find_transformed_supercell(a_sup, RU, D, t->delta, t->uvw, &t->nuvw, t->voxelSupercellDimensions);
+  build_gksuper(t, D);
+  oc_get_aperture(t, NULL, gg);
+  t->sg = oc_get_deviation_parameter(t, gg);
+}
+
+/* findImageParameters (Lib_DynamicalTwoBeamImaging.f90:450-482). */
+void oc_find_image_parameters(const oc_d2bi* t, double* aperpx, double* xmax, double* modg, int* Mx, int* My,
+                              int* Mz) {
+  double b[9], gg[3];
+  reciprocal(t->a_cell, b);
+  reflection(b, t->g, gg);
+  *modg = oc_norm2(gg);
+  for (int i = 1; i <= 3; ++i) xmax[i - 1] = super_side_length(&t->gksuper, i);
+  *Mx = t->gksuper.Nx;
+  *My = t->gksuper.Ny;
+  *Mz = t->gksuper.Nz;
+  *aperpx = sqrt(xmax[0] * xmax[1] / (double)((*Mx) * (*My)));
+}
+
+/* estimateMaxCountPerCell1 (Lib_LinkCell3D.f90:320-349). */
+static int estimate_max_count_per_cell(double nCells, int nTotal) {
+  double rho = nTotal / nCells;
+  double pp = exp(-rho), psum = pp;
+  for (int kk = 1; kk <= nTotal; ++kk) {
+    if (psum >= 0.99) return kk;
+    pp = pp * rho / kk;
+    psum = psum + pp;
+  }
+  return nTotal;
+}
+
+/* FactoriseParallel0 for the process counts a single GPU replaces
+ * (Lib_FactoriseParallel.f90:33-88). */
+static int factorise_parallel(int Ai, int Bi, int N, int* C, int* D) {
+  double Ad = Ai, Bd = Bi;
+  switch (N) {
+    case 1: *C = 1; *D = 1; return OC_OK;
+    case 2: if (Ad >= Bd) { *C = 2; *D = 1; } else { *C = 1; *D = 2; } return OC_OK;
+    case 3: if (Ad >= Bd) { *C = 3; *D = 1; } else { *C = 1; *D = 3; } return OC_OK;
+    case 4:
+      if (Ad >= 2 * Bd) { *C = 4; *D = 1; }
+      else if (Bd >= 2 * Ad) { *C = 1; *D = 4; }
+      else { *C = 2; *D = 2; }
+      return OC_OK;
+    default: return OC_ERR_ARG;
+  }
+}
+
+/* Prologue of computeD2BI_img (Lib_DynamicalTwoBeamImaging.f90:1635-1852). */
+int oc_image_geometry(const oc_d2bi* t, int64_t nAtoms, int nProcs, int jj, double precAngle, int nPrec,
+                      oc_geom* G, double* aa) {
+  memset(G, 0, sizeof *G);
+  double aperpx, xmax[3], modg;
+  int Mx, My, Mz;
+  oc_find_image_parameters(t, &aperpx, xmax, &modg, &Mx, &My, &Mz);
+  double costheta = 1.0, sintheta = 0.0;
+  if (nPrec > 1) {
+    costheta = cos(precAngle);
+    sintheta = sin(precAngle);
+  }
+  double sigma = t->a0 / 2;
+  G->sigma = sigma;
+  G->i2s2 = 1 / (2 * sigma * sigma);
+  double cmin = cell_side_length(&t->gksuper, 1), c2 = cell_side_length(&t->gksuper, 2);
+  if (c2 < cmin) cmin = c2;
+  int deltaM = (int)ceil(3 * sigma / cmin);
+  int nMax = estimate_max_count_per_cell((double)Mx * My * Mz, (int)nAtoms) * deltaM * deltaM;
+  int Cx, Cy;
+  if (factorise_parallel(Mx, My, nProcs, &Cx, &Cy) != OC_OK) return OC_ERR_ARG;
+  int Dx = (int)ceilf((float)Mx / (float)Cx);
+  int Dy = (int)ceilf((float)My / (float)Cy);
+  int Ex = (int)floorf((float)Dx / (float)deltaM + 2.0f);
+  int Ey = (int)floorf((float)Dy / (float)deltaM + 2.0f);
+  int Ez = (int)floorf((float)Mz / (float)deltaM);
+  if (Ex < 3) Ex = 3;
+  if (Ey < 3) Ey = 3;
+  if (Ez < 3) Ez = 3;
+  double a_col[9];
+  const double* a_vox = t->gksuper.a;
+  for (int i = 0; i < 3; ++i) {
+    a_col[i] = (Dx + 2 * deltaM) * a_vox[i] / Ex;
+    a_col[3 + i] = (Dy + 2 * deltaM) * a_vox[3 + i] / Ey;
+    a_col[6 + i] = Mz * a_vox[6 + i] / Ez;
+  }
+  oc_super lc;
+  oc_super_ctor(&lc, a_col, Ex, Ey, Ez);
+
+  G->Mx = Mx;
+  G->My = My;
+  G->Mz = Mz;
+  G->Ex = Ex;
+  G->Ey = Ey;
+  G->Ez = Ez;
+  G->deltaM = deltaM;
+  G->nMax0 = nMax;
+  memcpy(G->a_col, lc.a, sizeof lc.a);
+  memcpy(G->ia_col, lc.ia, sizeof lc.ia);
+  memcpy(G->a_vox, a_vox, 9 * sizeof(double));
+  G->deltaz = xmax[2] / Mz;
+  G->bg = (PI / t->xig);
+  G->b0 = (PI / t->xi0);
+  G->cut2 = (3 * sigma) * (3 * sigma);
+  G->useDensity = t->useDensityField;
+
+  /* precession (:1805-1831); nApp = 1 and its aperture offset is zero */
+  for (int prec = 1; prec <= nPrec; ++prec) {
+    double gg[3];
+    if (prec == 1) {
+      oc_get_aperture(t, NULL, gg);
+    } else {
+      double phi = (prec - 1) * 2 * PI / (nPrec - 1);
+      double ux = sin(phi), uy = cos(phi), BT[9];
+      A(BT, 1, 1) = costheta + ux * ux * (1 - costheta);
+      A(BT, 1, 2) = ux * uy * (1 - costheta);
+      A(BT, 1, 3) = uy * sintheta;
+      A(BT, 2, 1) = ux * uy * (1 - costheta);
+      A(BT, 2, 2) = costheta + uy * uy * (1 - costheta);
+      A(BT, 2, 3) = -ux * sintheta;
+      A(BT, 3, 1) = -uy * sintheta;
+      A(BT, 3, 2) = ux * sintheta;
+      A(BT, 3, 3) = costheta;
+      oc_get_aperture(t, BT, gg);
+    }
+    double z[3] = {0.0, 0.0, 0.0};
+    for (int i = 0; i < 3; ++i) z[i] = gg[i] + z[i];
+    double sg = oc_get_deviation_parameter(t, z);
+    aa[prec - 1] = (2 * PI * sg);
+  }
+
+  /* patch jj (:1843-1852) */
+  int jy = jj / Cx, jx = jj - jy * Cx;
+  double p0[3], p1[3];
+  cell_to_real_i(&t->gksuper, jx * Dx, jy * Dy, 0, p0);
+  cell_to_real_i(&lc, 1, 1, 0, p1);
+  for (int i = 0; i < 3; ++i) G->lc_delta[i] = p0[i] - p1[i];
+  G->ix0 = jx * Dx;
+  G->ix1 = ((jx + 1) * Dx < Mx) ? (jx + 1) * Dx : Mx;
+  G->iy0 = jy * Dy;
+  G->iy1 = ((jy + 1) * Dy < My) ? (jy + 1) * Dy : My;
+
+  /* findGdotR's transform (:1220-1240): RU, replicas, untilted aperture */
+  mat_mul(t->R, t->U, G->RU);
+  memcpy(G->delta, t->delta, sizeof t->delta);
+  G->nuvw = t->nuvw;
+  for (int nn = 0; nn < t->nuvw; ++nn) {
+    double sv[9];
+    super_a(&t->super, sv);
+    for (int i = 0; i < 3; ++i)
+      G->Ruvw[3 * nn + i] = t->uvw[3 * nn + 0] * sv[i] + t->uvw[3 * nn + 1] * sv[3 + i] + t->uvw[3 * nn + 2] * sv[6 + i];
+  }
+  oc_get_aperture(t, NULL, G->g);
+  return OC_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* LinkCell3D                                                               */
+/* ------------------------------------------------------------------------ */
+
+typedef struct {
+  int n, cap;
+  int* indx;
+  double* x; /* 3 per entry */
+} lc_cell;
+
+typedef struct {
+  oc_super s;
+  int nMax0;
+  int maxCount;
+  lc_cell* c;
+} lc3d;
+
+/* LinkCell3D_ctor1 / Cell_ctor0 (Lib_LinkCell3D.f90:237-259, 288-301). */
+static int lc_ctor(lc3d* L, const oc_super* s, int nMax0) {
+  L->s = *s;
+  L->nMax0 = nMax0;
+  L->maxCount = 0;
+  size_t nc = (size_t)s->Nx * s->Ny * s->Nz;
+  L->c = (lc_cell*)calloc(nc, sizeof(lc_cell));
+  if (!L->c) return OC_ERR_ALLOC;
+  for (size_t i = 0; i < nc; ++i) {
+    L->c[i].cap = nMax0;
+    if (nMax0 > 0) {
+      L->c[i].indx = (int*)malloc(sizeof(int) * nMax0);
+      L->c[i].x = (double*)malloc(sizeof(double) * 3 * nMax0);
+      if (!L->c[i].indx || !L->c[i].x) return OC_ERR_ALLOC;
+    }
+  }
+  return OC_OK;
+}
+
+static void lc_delete(lc3d* L) {
+  if (!L->c) return;
+  size_t nc = (size_t)L->s.Nx * L->s.Ny * L->s.Nz;
+  for (size_t i = 0; i < nc; ++i) {
+    free(L->c[i].indx);
+    free(L->c[i].x);
+  }
+  free(L->c);
+  L->c = NULL;
+}
+
+/* clear0 (Lib_LinkCell3D.f90:576-590). */
+static void lc_clear(lc3d* L) {
+  size_t nc = (size_t)L->s.Nx * L->s.Ny * L->s.Nz;
+  for (size_t i = 0; i < nc; ++i) L->c[i].n = 0;
+  L->maxCount = 0;
+}
+
+static lc_cell* lc_at(lc3d* L, int ix, int iy, int iz) {
+  return &L->c[(size_t)ix + (size_t)L->s.Nx * ((size_t)iy + (size_t)L->s.Ny * iz)];
+}
+
+/* add0 with doubleCell (Lib_LinkCell3D.f90:691-748, 388-410). */
+static int lc_add(lc3d* L, int id, const double* x) {
+  double yy[3], zz[3];
+  real_to_cell(&L->s, x, yy);
+  for (int i = 0; i < 3; ++i) zz[i] = yy[i] - floor(yy[i]);
+  int ix = imod((int)floor(yy[0]) + (L->s.Nx << 4), L->s.Nx);
+  int iy = imod((int)floor(yy[1]) + (L->s.Ny << 4), L->s.Ny);
+  int iz = imod((int)floor(yy[2]) + (L->s.Nz << 4), L->s.Nz);
+  lc_cell* c = lc_at(L, ix, iy, iz);
+  int nn = c->n + 1;
+  if (nn > c->cap) {
+    if (c->cap == 16 * L->nMax0) return OC_ERR_CAPACITY;
+    int nc = (c->cap == 0) ? 2 : ((2 * c->cap > 2) ? 2 * c->cap : 2);
+    int* ni = (int*)realloc(c->indx, sizeof(int) * nc);
+    if (!ni) return OC_ERR_ALLOC;
+    c->indx = ni;
+    double* nx = (double*)realloc(c->x, sizeof(double) * 3 * nc);
+    if (!nx) return OC_ERR_ALLOC;
+    c->x = nx;
+    c->cap = nc;
+  }
+  c->n = nn;
+  c->indx[nn - 1] = id;
+  memcpy(&c->x[3 * (nn - 1)], zz, sizeof zz);
+  if (nn > L->maxCount) L->maxCount = nn;
+  return OC_OK;
+}
+
+/* neighbourList1b (Lib_LinkCell3D.f90:1515-1605); also returns the real-space
+ * separations when dxo is non-null (the neighbourList0a layout). */
+static int lc_neighbours(const lc3d* L, const double* x, double sigma, int* id, double* r2, double* dxo,
+                         int64_t* ntests) {
+  int Nx = L->s.Nx, Ny = L->s.Ny, Nz = L->s.Nz;
+  const double* a = L->s.a;
+  double zi[3];
+  real_to_cell(&L->s, x, zi);
+  int ix = imod((int)floor(zi[0]) + 16 * Nx, Nx);
+  int iy = imod((int)floor(zi[1]) + 16 * Ny, Ny);
+  int iz = imod((int)floor(zi[2]) + 16 * Nz, Nz);
+  zi[0] = zi[0] - ix;
+  zi[1] = zi[1] - iy;
+  zi[2] = zi[2] - iz;
+  int n = 0;
+  int64_t tests = 0;
+  for (int kz = -1; kz <= 1; ++kz) {
+    int jz = imod(iz + Nz + kz, Nz);
+    double dzi3 = kz - zi[2];
+    for (int ky = -1; ky <= 1; ++ky) {
+      int jy = imod(iy + Ny + ky, Ny);
+      double dzi2 = ky - zi[1];
+      for (int kx = -1; kx <= 1; ++kx) {
+        int jx = imod(ix + Nx + kx, Nx);
+        double dzi1 = kx - zi[0];
+        const lc_cell* c = &L->c[(size_t)jx + (size_t)Nx * ((size_t)jy + (size_t)Ny * jz)];
+        tests += c->n;
+        for (int jk = 0; jk < c->n; ++jk) {
+          double dzj1 = c->x[3 * jk + 0] + dzi1;
+          double dzj2 = c->x[3 * jk + 1] + dzi2;
+          double dzj3 = c->x[3 * jk + 2] + dzi3;
+          double d0 = A(a, 1, 1) * dzj1 + A(a, 1, 2) * dzj2 + A(a, 1, 3) * dzj3;
+          double d1 = A(a, 2, 1) * dzj1 + A(a, 2, 2) * dzj2 + A(a, 2, 3) * dzj3;
+          double d2 = A(a, 3, 1) * dzj1 + A(a, 3, 2) * dzj2 + A(a, 3, 3) * dzj3;
+          double dd = d0 * d0 + d1 * d1 + d2 * d2;
+          if (dd <= sigma * sigma) {
+            id[n] = c->indx[jk];
+            r2[n] = dd;
+            if (dxo) {
+              dxo[3 * n + 0] = d0;
+              dxo[3 * n + 1] = d1;
+              dxo[3 * n + 2] = d2;
+            }
+            ++n;
+          }
+        }
+      }
+    }
+  }
+  if (ntests) *ntests += tests;
+  return n;
+}
+
+static int lc_max_27(const lc3d* L) {
+  /* upper bound on the neighbour count of any point: 27 x largest cell */
+  size_t nc = (size_t)L->s.Nx * L->s.Ny * L->s.Nz;
+  int m = 0;
+  for (size_t i = 0; i < nc; ++i)
+    if (L->c[i].n > m) m = L->c[i].n;
+  return 27 * (m > 0 ? m : 1);
+}
+
+int oc_neighbour_list(const oc_super* lc, const double* pts, int npts, int nMax0, const double* query,
+                      double cutoff, int* ids, double* dx, double* r2, int maxn, int* max_count) {
+  lc3d L;
+  if (lc_ctor(&L, lc, nMax0) != OC_OK) return -OC_ERR_ALLOC;
+  for (int i = 0; i < npts; ++i) {
+    int rc = lc_add(&L, i + 1, &pts[3 * i]);
+    if (rc != OC_OK) {
+      lc_delete(&L);
+      return -rc;
+    }
+  }
+  int need = lc_max_27(&L);
+  int* tid = (int*)malloc(sizeof(int) * need);
+  double* tr2 = (double*)malloc(sizeof(double) * need);
+  double* tdx = (double*)malloc(sizeof(double) * 3 * need);
+  int n = lc_neighbours(&L, query, cutoff, tid, tr2, tdx, NULL);
+  for (int i = 0; i < n && i < maxn; ++i) {
+    ids[i] = tid[i];
+    r2[i] = tr2[i];
+    memcpy(&dx[3 * i], &tdx[3 * i], 3 * sizeof(double));
+  }
+  if (max_count) *max_count = L.maxCount;
+  free(tid);
+  free(tr2);
+  free(tdx);
+  lc_delete(&L);
+  return n;
+}
+
+/* ------------------------------------------------------------------------ */
+/* findGdotR and the voxel loops                                            */
+/* ------------------------------------------------------------------------ */
+
+/* findGdotR (Lib_DynamicalTwoBeamImaging.f90:1160-1265): rotate the 27
+ * replicas, keep atoms inside the link-cell box, bin them and record g.y. */
+static int find_gdotr(const oc_geom* G, const double* x, int64_t ldx, int64_t nAtoms, lc3d* L, double** gdotr,
+                      int64_t* nkept) {
+  lc_clear(L);
+  int64_t cap = (int64_t)(nAtoms * 1.5) + 1, ii = 0;
+  double* gd = (double*)malloc(sizeof(double) * cap);
+  if (!gd) return OC_ERR_ALLOC;
+  for (int nn = 0; nn < G->nuvw; ++nn) {
+    const double* Ruvw = &G->Ruvw[3 * nn];
+    for (int64_t jj = 0; jj < nAtoms; ++jj) {
+      double yy[3], zz[3];
+      const double* xa = &x[jj * ldx];
+      for (int i = 0; i < 3; ++i) yy[i] = xa[i] + Ruvw[i];
+      mat_vec(G->RU, yy, yy);
+      for (int i = 0; i < 3; ++i) yy[i] = yy[i] + G->delta[i];
+      for (int i = 0; i < 3; ++i) zz[i] = yy[i] - G->lc_delta[i];
+      if (point_in_super(&L->s, zz)) {
+        ii = ii + 1;
+        if (ii > cap) {
+          double* ng = (double*)realloc(gd, sizeof(double) * cap * 2);
+          if (!ng) {
+            free(gd);
+            return OC_ERR_ALLOC;
+          }
+          gd = ng;
+          cap *= 2;
+        }
+        int rc = lc_add(L, (int)ii, zz);
+        if (rc != OC_OK) {
+          free(gd);
+          return rc;
+        }
+        gd[ii - 1] = G->g[0] * yy[0] + G->g[1] * yy[1] + G->g[2] * yy[2];
+      }
+    }
+  }
+  *gdotr = gd;
+  *nkept = ii;
+  return OC_OK;
+}
+
+/* convertScaledRangeToRho (Lib_DynamicalTwoBeamImaging.f90:1973-1994). */
+static double scaled_range_to_rho(double r2_min, double sig) {
+  if (r2_min < sig * sig) return 1.0;
+  if (r2_min > 4 * sig * sig) return 0.0;
+  double xx = (sqrt(r2_min) / sig - 1.0);
+  return 1 - xx * xx * xx * (10 - 15 * xx + 6 * xx * xx);
+}
+
+/* dynamicalTwoBeamIntegrationColumn_phaserho (Lib_DynamicalTwoBeamImaging.f90:2316-2480). */
+double oc_integrate_column(double a, double b0, double bg, double dz, const double* x, const double* rho, int nz) {
+  double phi0r = 1.0, phi0i = 0.0, phigr = 0.0, phigi = 0.0;
+  for (int ii = 0; ii <= nz - 2; ii += 2) {
+    double c0[3], ca[3], cgr[3], cgi[3];
+    for (int s = 0; s < 3; ++s) {
+      int k = ii + s;
+      c0[s] = b0 * rho[k];
+      ca[s] = b0 * rho[k] + a;
+      cgr[s] = bg * rho[k] * x[2 * k];
+      cgi[s] = bg * rho[k] * x[2 * k + 1];
+    }
+    double d0r, d0i, dgr, dgi;
+    /* step 1 at ii */
+    d0r = -c0[0] * phi0i - cgi[0] * phigr - cgr[0] * phigi;
+    d0i = c0[0] * phi0r + cgr[0] * phigr - cgi[0] * phigi;
+    dgr = cgi[0] * phi0r - cgr[0] * phi0i - ca[0] * phigi;
+    dgi = cgr[0] * phi0r + cgi[0] * phi0i + ca[0] * phigr;
+    double p0r2 = phi0r, p0i2 = phi0i, pgr2 = phigr, pgi2 = phigi;
+    double p0r1 = phi0r + d0r * dz / 3, p0i1 = phi0i + d0i * dz / 3;
+    double pgr1 = phigr + dgr * dz / 3, pgi1 = phigi + dgi * dz / 3;
+    phi0r = phi0r + d0r * dz;
+    phi0i = phi0i + d0i * dz;
+    phigr = phigr + dgr * dz;
+    phigi = phigi + dgi * dz;
+    /* step 2 at ii+1 */
+    d0r = -c0[1] * phi0i - cgi[1] * phigr - cgr[1] * phigi;
+    d0i = c0[1] * phi0r + cgr[1] * phigr - cgi[1] * phigi;
+    dgr = cgi[1] * phi0r - cgr[1] * phi0i - ca[1] * phigi;
+    dgi = cgr[1] * phi0r + cgi[1] * phi0i + ca[1] * phigr;
+    phi0r = p0r2 + d0r * dz;
+    phi0i = p0i2 + d0i * dz;
+    phigr = pgr2 + dgr * dz;
+    phigi = pgi2 + dgi * dz;
+    p0r1 = p0r1 + d0r * 2 * dz / 3;
+    p0i1 = p0i1 + d0i * 2 * dz / 3;
+    pgr1 = pgr1 + dgr * 2 * dz / 3;
+    pgi1 = pgi1 + dgi * 2 * dz / 3;
+    /* step 3 at ii+1 */
+    d0r = -c0[1] * phi0i - cgi[1] * phigr - cgr[1] * phigi;
+    d0i = c0[1] * phi0r + cgr[1] * phigr - cgi[1] * phigi;
+    dgr = cgi[1] * phi0r - cgr[1] * phi0i - ca[1] * phigi;
+    dgi = cgr[1] * phi0r + cgi[1] * phi0i + ca[1] * phigr;
+    phi0r = p0r2 + d0r * 2 * dz;
+    phi0i = p0i2 + d0i * 2 * dz;
+    phigr = pgr2 + dgr * 2 * dz;
+    phigi = pgi2 + dgi * 2 * dz;
+    p0r1 = p0r1 + d0r * 2 * dz / 3;
+    p0i1 = p0i1 + d0i * 2 * dz / 3;
+    pgr1 = pgr1 + dgr * 2 * dz / 3;
+    pgi1 = pgi1 + dgi * 2 * dz / 3;
+    /* step 4 at ii+2 */
+    d0r = -c0[2] * phi0i - cgi[2] * phigr - cgr[2] * phigi;
+    d0i = c0[2] * phi0r + cgr[2] * phigr - cgi[2] * phigi;
+    dgr = cgi[2] * phi0r - cgr[2] * phi0i - ca[2] * phigi;
+    dgi = cgr[2] * phi0r + cgi[2] * phi0i + ca[2] * phigr;
+    phi0r = p0r1 + d0r * dz / 3;
+    phi0i = p0i1 + d0i * dz / 3;
+    phigr = pgr1 + dgr * dz / 3;
+    phigi = pgi1 + dgi * dz / 3;
+    double phimag = phi0r * phi0r + phi0i * phi0i + phigr * phigr + phigi * phigi;
+    phimag = 1 / sqrt(phimag);
+    phi0r = phi0r * phimag;
+    phi0i = phi0i * phimag;
+    phigr = phigr * phimag;
+    phigi = phigi * phimag;
+  }
+  return phigr * phigr + phigi * phigi;
+}
+
+/* Voxel loop of one pixel column (:1877-1900). */
+static void column_field(const oc_geom* G, const lc3d* L, const double* gdotr, int ix, int iy, double* xf,
+                         double* rho, int* id, double* r2, oc_stats* st) {
+  oc_super gk;
+  gk.Nx = G->Mx;
+  gk.Ny = G->My;
+  gk.Nz = G->Mz;
+  memcpy(gk.a, G->a_vox, sizeof gk.a);
+  for (int iz = 0; iz < G->Mz; ++iz) {
+    double xx[3];
+    cell_to_real_i(&gk, ix, iy, iz, xx);
+    for (int i = 0; i < 3; ++i) xx[i] = xx[i] - G->lc_delta[i];
+    int64_t tests = 0;
+    int nn = lc_neighbours(L, xx, 3 * G->sigma, id, r2, NULL, &tests);
+    double r2_min = HUGE1, sr = 0.0, si = 0.0;
+    for (int kk = 0; kk < nn; ++kk) {
+      if (r2[kk] < r2_min) r2_min = r2[kk];
+      double w = exp(-r2[kk] * G->i2s2), s, c;
+      sincos(gdotr[id[kk] - 1], &s, &c);
+      sr = sr + w * c;
+      si = si + w * s;
+    }
+    if (G->useDensity) rho[iz] = scaled_range_to_rho(r2_min, G->sigma);
+    double ww = hypot(sr, si);
+    ww = 1 / (1.0e-16 > ww ? 1.0e-16 : ww);
+    xf[2 * iz] = sr * ww;
+    xf[2 * iz + 1] = si * ww;
+    if (st) {
+      st->n_tests += tests;
+      st->n_accepted += nn;
+      st->n_voxels += 1;
+    }
+  }
+  xf[2 * G->Mz] = xf[0];
+  xf[2 * G->Mz + 1] = xf[1];
+  rho[G->Mz] = rho[0];
+}
+
+int oc_patch_image_rows(const oc_geom* G, const double* aa, int nPrec, const double* x, int64_t ldx, int64_t nAtoms,
+                        int iy_lo, int iy_hi, double* img, oc_stats* stats, int nthreads) {
+  oc_super lcs;
+  lcs.Nx = G->Ex;
+  lcs.Ny = G->Ey;
+  lcs.Nz = G->Ez;
+  memcpy(lcs.a, G->a_col, sizeof lcs.a);
+  memcpy(lcs.ia, G->ia_col, sizeof lcs.ia);
+  lc3d L;
+  int rc = lc_ctor(&L, &lcs, G->nMax0);
+  if (rc != OC_OK) return rc;
+  double* gdotr = NULL;
+  int64_t nkept = 0;
+  rc = find_gdotr(G, x, ldx, nAtoms, &L, &gdotr, &nkept);
+  if (rc != OC_OK) {
+    lc_delete(&L);
+    return rc;
+  }
+  int need = lc_max_27(&L);
+  if (iy_lo < G->iy0) iy_lo = G->iy0;
+  if (iy_hi > G->iy1) iy_hi = G->iy1;
+  int64_t tests = 0, acc = 0, vox = 0;
+  int err = 0;
+#ifdef _OPENMP
+  if (nthreads < 1) nthreads = 1;
+#pragma omp parallel num_threads(nthreads) reduction(+ : tests, acc, vox)
+#endif
+  {
+    double* xf = (double*)malloc(sizeof(double) * 2 * (G->Mz + 1));
+    double* rho = (double*)malloc(sizeof(double) * (G->Mz + 1));
+    int* id = (int*)malloc(sizeof(int) * need);
+    double* r2 = (double*)malloc(sizeof(double) * need);
+    if (!xf || !rho || !id || !r2) {
+      err = 1;
+    } else {
+      for (int i = 0; i <= G->Mz; ++i) rho[i] = 1.0;
+      oc_stats st;
+      memset(&st, 0, sizeof st);
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 1)
+#endif
+      for (int iy = iy_lo; iy < iy_hi; ++iy) {
+        for (int ix = G->ix0; ix < G->ix1; ++ix) {
+          column_field(G, &L, gdotr, ix, iy, xf, rho, id, r2, &st);
+          double acc_px = img[(size_t)ix + (size_t)G->Mx * iy];
+          for (int p = 0; p < nPrec; ++p)
+            acc_px = acc_px + oc_integrate_column(aa[p], G->b0, G->bg, G->deltaz, xf, rho, G->Mz);
+          img[(size_t)ix + (size_t)G->Mx * iy] = acc_px;
+        }
+      }
+      tests += st.n_tests;
+      acc += st.n_accepted;
+      vox += st.n_voxels;
+    }
+    free(xf);
+    free(rho);
+    free(id);
+    free(r2);
+  }
+  (void)nthreads;
+  if (stats) {
+    stats->n_kept += nkept;
+    stats->n_tests += tests;
+    stats->n_accepted += acc;
+    stats->n_voxels += vox;
+    if (L.maxCount > stats->max_cell_count) stats->max_cell_count = L.maxCount;
+  }
+  free(gdotr);
+  lc_delete(&L);
+  return err ? OC_ERR_ALLOC : OC_OK;
+}
+
+int oc_patch_image(const oc_geom* G, const double* aa, int nPrec, const double* x, int64_t ldx, int64_t nAtoms,
+                   double* img, oc_stats* stats, int nthreads) {
+  return oc_patch_image_rows(G, aa, nPrec, x, ldx, nAtoms, G->iy0, G->iy1, img, stats, nthreads);
+}
+
+/* computeD2BI_img with one process (Lib_DynamicalTwoBeamImaging.f90:1563-1998). */
+int oc_compute_d2bi_img(const oc_d2bi* t, const double* x, int64_t ldx, int64_t nAtoms, double precAngle, int nPrec,
+                        double* img, oc_stats* stats, int nthreads) {
+  if (nPrec < 1) return OC_ERR_ARG;
+  oc_geom G;
+  double* aa = (double*)malloc(sizeof(double) * nPrec);
+  int rc = oc_image_geometry(t, nAtoms, 1, 0, precAngle, nPrec, &G, aa);
+  if (rc != OC_OK) {
+    free(aa);
+    return rc;
+  }
+  memset(img, 0, sizeof(double) * (size_t)G.Mx * G.My);
+  if (stats) memset(stats, 0, sizeof *stats);
+  rc = oc_patch_image(&G, aa, nPrec, x, ldx, nAtoms, img, stats, nthreads);
+  for (size_t i = 0; i < (size_t)G.Mx * G.My; ++i) img[i] = img[i] / (double)(1 * nPrec);
+  free(aa);
+  return rc;
+}
+
+/* ------------------------------------------------------------------------ */
+/* d2bi                                                                     */
+/* ------------------------------------------------------------------------ */
+
+/* src/d2bi.f90:782-789, 856-866, 983-991, 1145-1268, 1352-1381 for one
+ * diffraction condition and tomography step nn. */
+int oc_d2bi_setup(const oc_args* args, double* x, int64_t ldx, int64_t nAtoms, int nn, oc_d2bi* t,
+                  double* aperpx_out) {
+  double a0in[3] = {args->a0in, args->a0in, args->a0in};
+  double a0 = (a0in[0] + a0in[1] + a0in[2]) / 3;
+  const double* a_super = args->a_super;
+  int Mx = (int)floor(args->M[0] * oc_norm2(&a_super[0]) / a0);
+  int My = (int)floor(args->M[0] * oc_norm2(&a_super[3]) / a0);
+  int Mz = (int)floor(args->M[1] * oc_norm2(&a_super[6]) / a0);
+  if (Mx < 3) Mx = 3;
+  if (My < 3) My = 3;
+  if (Mz < 3) Mz = 3;
+  double a_vox[9];
+  for (int i = 0; i < 3; ++i) {
+    a_vox[i] = a_super[i] / Mx;
+    a_vox[3 + i] = a_super[3 + i] / My;
+    a_vox[6 + i] = a_super[6 + i] / Mz;
+  }
+  oc_super super;
+  oc_super_ctor(&super, a_vox, Mx, My, Mz);
+  for (int64_t i = 0; i < nAtoms; ++i) oc_wrap_pbc(&super, &x[i * ldx], &x[i * ldx]);
+
+  double a_cell[9];
+  identity3(a_cell);
+  for (int i = 0; i < 9; ++i) a_cell[i] = a0 * a_cell[i];
+
+  double d[3];
+  if (args->haveD) {
+    memcpy(d, args->d0, sizeof d);
+  } else {
+    double rot[9], xmin[3] = {HUGE1, HUGE1, HUGE1}, xmax[3] = {-HUGE1, -HUGE1, -HUGE1};
+    oc_rotate_to_standard_frame(args->k, a_cell, args->g, rot);
+    for (int64_t i = 0; i < nAtoms; ++i) {
+      double yy[3];
+      mat_vec(rot, &x[i * ldx], yy);
+      for (int k = 0; k < 3; ++k) {
+        if (yy[k] < xmin[k]) xmin[k] = yy[k];
+        if (yy[k] > xmax[k]) xmax[k] = yy[k];
+      }
+    }
+    for (int k = 0; k < 3; ++k) d[k] = xmax[k] - xmin[k];
+  }
+  oc_d2bi_ctor(t, &super, a0, args->k, args->g, args->V, args->M[0], args->M[1]);
+  oc_set_conventional_unit_cell(t, a_cell);
+  int rc = oc_set_voxel_supercell_size(t, d);
+  if (rc != OC_OK) return rc;
+  if (args->tilt_mode == 1) {
+    oc_set_deviation_parameter(t, args->sg);
+    oc_set_supercell_tilt0(t);
+  } else if (args->tilt_mode == 2) {
+    double U[9];
+    if (args->haveU)
+      memcpy(U, args->U, sizeof U);
+    else
+      identity3(U);
+    oc_set_supercell_tilt2(t, U, args->R);
+  } else {
+    oc_set_deviation_parameter(t, 0.0);
+    oc_set_supercell_tilt0(t);
+  }
+  double U0[9], R0[9];
+  memcpy(U0, t->U, sizeof U0);
+  memcpy(R0, t->R, sizeof R0);
+  oc_set_extinction_distances(t, args->xi0, args->xig);
+  double aperpx, xm[3], modg;
+  int mx, my, mz;
+  oc_find_image_parameters(t, &aperpx, xm, &modg, &mx, &my, &mz);
+  oc_set_use_density_field(t, args->useDensity);
+  if (args->nTomo > 1) {
+    double theta = args->tomoAngle - 2 * args->tomoAngle * nn / (args->nTomo - 1);
+    theta = theta * 3.141592654 / 180.0;
+    double R[9] = {1.0, 0.0, 0.0, 0.0, cos(theta), sin(theta), 0.0, -sin(theta), cos(theta)};
+    mat_mul(R, R0, R);
+    oc_set_supercell_tilt2(t, U0, R);
+  }
+  if (aperpx_out) *aperpx_out = aperpx;
+  return OC_OK;
+}
+
+/* gaussianBlurImage (src/d2bi.f90:1543-1624). */
+void oc_gaussian_blur(const double* f_in, int Nx, int Ny, double t, double* f_out) {
+  int Nk = (int)ceil(t * 5);
+  if (Nk < 5) Nk = 5;
+  double* kernel = (double*)malloc(sizeof(double) * (Nk + 1));
+  double i2s2 = 1 / (2 * t * t);
+  kernel[0] = 1.0;
+  for (int ix = 1; ix <= Nk; ++ix) kernel[ix] = exp(-(ix * ix * i2s2));
+  double* f_stripe = (double*)malloc(sizeof(double) * Ny);
+  double* w_stripe = (double*)malloc(sizeof(double) * Nx);
+  for (int iy = 0; iy < Ny; ++iy) {
+    for (int ix = 0; ix < Nx; ++ix) {
+      double wf = 0.0, ws = 0.0;
+      int lo = ix - Nk > 0 ? ix - Nk : 0, hi = ix + Nk < Nx - 1 ? ix + Nk : Nx - 1;
+      for (int jj = lo; jj <= hi; ++jj) {
+        double ww = kernel[abs(jj - ix)];
+        wf = wf + ww * f_in[(size_t)jj + (size_t)Nx * iy];
+        ws = ws + ww;
+      }
+      f_out[(size_t)ix + (size_t)Nx * iy] = wf;
+      if (iy == 0) w_stripe[ix] = 1 / ws;
+    }
+  }
+  for (int ix = 0; ix < Nx; ++ix) {
+    for (int iy = 0; iy < Ny; ++iy) f_stripe[iy] = f_out[(size_t)ix + (size_t)Nx * iy];
+    for (int iy = 0; iy < Ny; ++iy) {
+      double wf = 0.0, ws = 0.0;
+      int lo = iy - Nk > 0 ? iy - Nk : 0, hi = iy + Nk < Ny - 1 ? iy + Nk : Ny - 1;
+      for (int jj = lo; jj <= hi; ++jj) {
+        double ww = kernel[abs(jj - iy)];
+        wf = wf + ww * f_stripe[jj];
+        ws = ws + ww;
+      }
+      f_out[(size_t)ix + (size_t)Nx * iy] = wf * w_stripe[ix] / (ws);
+    }
+  }
+  free(kernel);
+  free(f_stripe);
+  free(w_stripe);
+}
+
+/* write_greyscale_png(normalise=.true.) levels (Lib_Png.f90:117-181) and the
+ * C writer's clamp and truncation (Lib_Greyscale.c:234-241). */
+void oc_png_levels(const double* img, int Nx, int Ny, uint16_t* levels) {
+  const double ONE = 1.0 - 1.0 / 65536;
+  double mn = img[0], mx = img[0];
+  for (size_t i = 0; i < (size_t)Nx * Ny; ++i) {
+    if (img[i] < mn) mn = img[i];
+    if (img[i] > mx) mx = img[i];
+  }
+  double aa, bb;
+  if (mx - mn < 1.0e-16) {
+    aa = 0.0;
+    bb = 0.5;
+  } else {
+    aa = ONE / (mx - mn);
+    bb = -aa * mn;
+  }
+  for (int y = 0; y < Ny; ++y)
+    for (int x = 0; x < Nx; ++x) {
+      float f = (float)(aa * img[(size_t)x + (size_t)Nx * y] + bb);
+      if (f > 0.999984741) {
+        f = 0.999984741f;
+      } else if (f < 0.0) {
+        f = 0.0f;
+      }
+      int i = (int)(f * 65536);
+      levels[(size_t)y * Nx + x] = (uint16_t)i;
+    }
+}

@@ -1,0 +1,217 @@
+"""ORACLE -- test infrastructure only.
+
+ctypes binding of ``libstem_oracle.so``, the plain-C restatement of the
+reference's imaging path (``stem_oracle.c``).  Only the tests, the smoke check
+and the CPU-baseline leg of the benchmark import this module, always as the
+checker; the product path never does.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libstem_oracle.so")
+
+_d = ctypes.c_double
+_i = ctypes.c_int
+_i64 = ctypes.c_int64
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+
+
+class Super(ctypes.Structure):
+    _fields_ = [("Nx", _i), ("Ny", _i), ("Nz", _i), ("a", _d * 9), ("ia", _d * 9)]
+
+
+class D2BI(ctypes.Structure):
+    _fields_ = [("k", _d * 3), ("g", _d * 3), ("a0", _d), ("super", Super), ("sg", _d), ("mxy", _i), ("mzz", _i),
+                ("xi0", _d), ("xig", _d), ("E", _d), ("useDensityField", _i), ("gksuper", Super), ("delta", _d * 3),
+                ("foilThickness", _d), ("voxelSupercellDimensions", _d * 3), ("nuvw", _i), ("uvw", _i * 375),
+                ("a_cell", _d * 9), ("U", _d * 9), ("R", _d * 9), ("test", _i)]
+
+
+class Geom(ctypes.Structure):
+    _fields_ = [("Mx", _i), ("My", _i), ("Mz", _i), ("ix0", _i), ("ix1", _i), ("iy0", _i), ("iy1", _i),
+                ("Ex", _i), ("Ey", _i), ("Ez", _i), ("deltaM", _i), ("nMax0", _i), ("nuvw", _i),
+                ("RU", _d * 9), ("delta", _d * 3), ("Ruvw", _d * 81), ("lc_delta", _d * 3), ("a_col", _d * 9),
+                ("ia_col", _d * 9), ("a_vox", _d * 9), ("g", _d * 3), ("sigma", _d), ("cut2", _d), ("i2s2", _d),
+                ("deltaz", _d), ("b0", _d), ("bg", _d), ("useDensity", _i)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("n_kept", _i64), ("n_tests", _i64), ("n_accepted", _i64), ("n_voxels", _i64),
+                ("max_cell_count", _i)]
+
+
+class Args(ctypes.Structure):
+    _fields_ = [("a_super", _d * 9), ("a0in", _d), ("k", _d * 3), ("g", _d * 3), ("V", _d), ("M", _i * 2),
+                ("tilt_mode", _i), ("sg", _d), ("haveU", _i), ("U", _d * 9), ("R", _d * 9), ("haveD", _i),
+                ("d0", _d * 3), ("xi0", _d), ("xig", _d), ("useDensity", _i), ("nPrec", _i), ("precAngle", _d),
+                ("nTomo", _i), ("tomoAngle", _d), ("dark", _i)]
+
+
+_lib = None
+
+
+def build():
+    """Compile the oracle with its Makefile (gcc only)."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = ctypes.CDLL(LIB_PATH)
+        L.oc_norm2.restype = _d
+        L.oc_wavelength.restype = _d
+        L.oc_velocity.restype = _d
+        L.oc_intensity_at_depth.restype = _d
+        L.oc_integrate_column.restype = _d
+        L.oc_get_deviation_parameter.restype = _d
+        for name in ("oc_image_geometry", "oc_patch_image", "oc_patch_image_rows", "oc_compute_d2bi_img",
+                     "oc_neighbour_list", "oc_d2bi_setup"):
+            getattr(L, name).restype = _i
+        _lib = L
+    return _lib
+
+
+def _dptr(a):
+    return a.ctypes.data_as(_dp)
+
+
+def _mat(m):
+    """3x3 numpy (row i, column j) -> column-major ctypes array."""
+    m = np.asarray(m, dtype=np.float64)
+    return (_d * 9)(*m.T.reshape(-1))
+
+
+def make_args(a_super, a0, k, g, V=200.0, M=(4, 4), sg=None, R=None, U=None, d=None, xi0=103.889565,
+              xig=207.533203, density=False, nPrec=1, precAngle=0.005, nTomo=1, tomoAngle=20.0, dark=True):
+    """d2bi command-line arguments for one diffraction condition (src/d2bi.f90:48-100 defaults)."""
+    a = Args()
+    a.a_super[:] = list(np.asarray(a_super, dtype=np.float64).T.reshape(-1))
+    a.a0in = a0
+    a.k[:] = list(map(float, k))
+    a.g[:] = list(map(float, g))
+    a.V = V
+    a.M[:] = list(M)
+    if R is not None:
+        a.tilt_mode = 2
+        a.R[:] = list(np.asarray(R, dtype=np.float64).T.reshape(-1))
+        if U is not None:
+            a.haveU = 1
+            a.U[:] = list(np.asarray(U, dtype=np.float64).T.reshape(-1))
+    elif sg is not None:
+        a.tilt_mode = 1
+        a.sg = sg
+    else:
+        a.tilt_mode = 0
+    if d is not None:
+        a.haveD = 1
+        a.d0[:] = list(map(float, d))
+    a.xi0, a.xig = xi0, xig
+    a.useDensity = int(bool(density))
+    a.nPrec, a.precAngle = nPrec, precAngle
+    a.nTomo, a.tomoAngle = nTomo, tomoAngle
+    a.dark = int(bool(dark))
+    return a
+
+
+def setup(args, pos, nn=0):
+    """wrapPBC the atoms and set up the imaging state; returns (state, wrapped x (N,3), aperpx)."""
+    x = np.ascontiguousarray(pos, dtype=np.float64).copy()
+    t = D2BI()
+    aperpx = _d()
+    rc = lib().oc_d2bi_setup(ctypes.byref(args), _dptr(x), _i64(3), _i64(x.shape[0]), _i(nn), ctypes.byref(t),
+                             ctypes.byref(aperpx))
+    if rc != 0:
+        raise RuntimeError("oracle setup failed: %d" % rc)
+    return t, x, aperpx.value
+
+
+def geometry(state, n_atoms, nPrec=1, precAngle=0.005, nProcs=1, jj=0):
+    G = Geom()
+    aa = np.zeros(max(nPrec, 1))
+    rc = lib().oc_image_geometry(ctypes.byref(state), _i64(n_atoms), _i(nProcs), _i(jj), _d(precAngle), _i(nPrec),
+                                 ctypes.byref(G), _dptr(aa))
+    if rc != 0:
+        raise RuntimeError("oracle geometry failed: %d" % rc)
+    return G, aa
+
+
+def patch_image(G, aa, x, img=None, rows=None, nthreads=1):
+    """Sum over precession of |phi_g|^2 for the pixels of the patch (column-major (Mx, My) in a numpy (Mx, My) array
+    stored Fortran-order); returns (img, stats)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    if img is None:
+        img = np.zeros((G.Mx, G.My), order="F")
+    st = Stats()
+    aa = np.ascontiguousarray(aa, dtype=np.float64)
+    if rows is None:
+        rc = lib().oc_patch_image(ctypes.byref(G), _dptr(aa), _i(len(aa)), _dptr(x), _i64(3), _i64(x.shape[0]),
+                                  _dptr(img), ctypes.byref(st), _i(nthreads))
+    else:
+        rc = lib().oc_patch_image_rows(ctypes.byref(G), _dptr(aa), _i(len(aa)), _dptr(x), _i64(3),
+                                       _i64(x.shape[0]), _i(rows[0]), _i(rows[1]), _dptr(img), ctypes.byref(st),
+                                       _i(nthreads))
+    if rc != 0:
+        raise RuntimeError("oracle image failed: %d" % rc)
+    return img, st
+
+
+def compute_d2bi_img(state, x, nPrec=1, precAngle=0.005, nthreads=1):
+    """computeD2BI_img: the precession-averaged dark-field image (Mx, My)."""
+    Mx, My = state.gksuper.Nx, state.gksuper.Ny
+    img = np.zeros((Mx, My), order="F")
+    st = Stats()
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    rc = lib().oc_compute_d2bi_img(ctypes.byref(state), _dptr(x), _i64(3), _i64(x.shape[0]), _d(precAngle),
+                                   _i(nPrec), _dptr(img), ctypes.byref(st), _i(nthreads))
+    if rc != 0:
+        raise RuntimeError("oracle computeD2BI_img failed: %d" % rc)
+    return img, st
+
+
+def integrate_column(a, b0, bg, dz, field, rho):
+    f = np.ascontiguousarray(np.stack([field.real, field.imag], axis=-1).reshape(-1))
+    r = np.ascontiguousarray(rho, dtype=np.float64)
+    return lib().oc_integrate_column(_d(a), _d(b0), _d(bg), _d(dz), _dptr(f), _dptr(r), _i(len(rho) - 1))
+
+
+def gaussian_blur(img, t):
+    img = np.asfortranarray(img, dtype=np.float64)
+    out = np.zeros_like(img, order="F")
+    lib().oc_gaussian_blur(_dptr(img), _i(img.shape[0]), _i(img.shape[1]), _d(t), _dptr(out))
+    return out
+
+
+def png_levels(img):
+    img = np.asfortranarray(img, dtype=np.float64)
+    Nx, Ny = img.shape
+    lv = np.zeros((Ny, Nx), dtype=np.uint16)
+    lib().oc_png_levels(_dptr(img), _i(Nx), _i(Ny), lv.ctypes.data_as(ctypes.POINTER(ctypes.c_uint16)))
+    return lv
+
+
+def neighbour_list(a_cell, cells, nmax0, points, query, cutoff):
+    s = Super()
+    s.Nx, s.Ny, s.Nz = cells
+    s.a[:] = list(np.asarray(a_cell, dtype=np.float64).T.reshape(-1))
+    L = lib()
+    L.oc_inv3(s.a, s.ia)
+    pts = np.ascontiguousarray(points, dtype=np.float64)
+    q = np.ascontiguousarray(query, dtype=np.float64)
+    maxn = len(points)
+    ids = np.zeros(maxn, dtype=np.int32)
+    dx = np.zeros((maxn, 3))
+    r2 = np.zeros(maxn)
+    mc = _i()
+    n = L.oc_neighbour_list(ctypes.byref(s), _dptr(pts), _i(len(pts)), _i(nmax0), _dptr(q), _d(cutoff),
+                            ids.ctypes.data_as(_ip), _dptr(dx), _dptr(r2), _i(maxn), ctypes.byref(mc))
+    if n < 0:
+        raise RuntimeError("oracle neighbour list failed: %d" % -n)
+    return ids[:n], dx[:n], r2[:n], mc.value
