@@ -1,0 +1,360 @@
+"""Benchmark of the d2bi imaging hot path on GB300.
+
+Workload: the 1.2M-atom bcc Fe cell (100 x 100 x 60 cells, screw dislocation
+along z through the centre, 20 voids of radius U(5, 15) A, jitter 0.05 A,
+seeded), g = [110], k = [001], s_g = 0.01 1/A, M = 4,4, 200 kV: a 566 x 566
+image with 240 voxels per column.  One step = one image: link-cell binning
+(findGdotR), voxel phase field and column integration, FP32 arithmetic with
+FP64 cell assignment and FP64 g.r reduction.
+
+  value  images/s with the atoms resident in HBM (st_image_device), each step
+         timed with CUDA events on the launching stream, L2 flushed between
+         steps (a 512 MB write), untimed.
+  e2e    the same through st_image, the C-ABI call a Fortran or C host makes,
+         from pinned host buffers: the H2D copy of the atoms and the D2H copy
+         of the image are inside the timed region.
+  also   the plain FP64 GPU path (images/s) and max |dI| FP32 vs FP64.
+
+``--impl reference`` times the reference's algorithm on the host cores: the
+reference (Fortran) cannot be built here, so the oracle's C restatement runs,
+with all host threads, on a bounded band of pixel rows of the same image,
+extrapolated to whole images.
+
+Under torchrun with N > 1 every rank images its own copy of the workload
+(independent images: replicas, no collective on the data path); value is the
+total images/s over all ranks.
+"""
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "images/s at 1.2M atoms: batched FP32 vs plain FP64 GPU at ≤1e-4 max |ΔI|"
+WORKLOAD = "bcc Fe 100x100x60 cells (1.2M atoms), screw + 20 voids, g=[110] k=[001] s_g=0.01, M=4,4, 200 kV"
+
+
+def workload():
+    from simulated_tem_gb300 import imaging, synth
+    cell = synth.screw_cell_1p2m()
+    t, x, aperpx = imaging.d2bi_condition(cell.a_super, synth.A0_FE, (0, 0, 1), (1, 1, 0), cell.pos, sg=0.01,
+                                          xi0=103.9, xig=207.5, V=200.0, M=(4, 4))
+    return cell, t, x, aperpx
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if len(r) > 8 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 8 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows if len(r) > 8 for i in range(4) if r[5 + i] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def measure_fp32_peak():
+    from simulated_tem_gb300 import _lib
+    out = (ctypes.c_double * 4)()
+    rc = _lib.peaks_lib().stp_measure_peaks(out)
+    if rc != 0:
+        return None
+    return {"fp32_tflops": out[0], "fp64_tflops": out[1], "mufu_ex2_gops": out[2], "mufu_sin_gops": out[3]}
+
+
+def run_gpu(args):
+    import torch
+
+    from simulated_tem_gb300 import _lib, imaging
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    cell, t, x, aperpx = workload()
+    G, aa = t.image_geometry(len(x))
+    n_prec = len(aa)
+    ctx = imaging.Context(local)
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+    d_x = torch.from_numpy(np.ascontiguousarray(x)).cuda()
+    d_img = torch.zeros((G.My, G.Mx), dtype=torch.float64, device="cuda")
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    flags = _lib.ST_FLAG_FP32 | _lib.ST_FLAG_AVERAGE
+
+    def step(f=flags):
+        ctx.image_device(G, d_x.data_ptr(), len(x), aa, f, d_img.data_ptr(), stream=sptr)
+
+    # counters for the roofline (one untimed image with statistics)
+    step(flags | _lib.ST_FLAG_STATS)
+    st = ctx.stats()
+    n_acc, n_kept = st.n_accepted, st.n_kept
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    col_ms = []
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            flush.fill_(float(i))
+            ev[i][0].record(stream)
+            step()
+            ev[i][1].record(stream)
+            col_ms.append(ctx.stats().ms_column)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    ms = float(np.mean(step_ms))
+    if ws > 1:
+        tmax = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(tmax, op=torch.distributed.ReduceOp.MAX)
+        ms = float(tmax.item())
+    value = ws * 1000.0 / ms
+    img32 = d_img.cpu().numpy().T.copy()
+
+    # end to end through st_image from pinned host memory
+    h_x = torch.from_numpy(np.ascontiguousarray(x)).pin_memory()
+    h_img = torch.zeros((G.My, G.Mx), dtype=torch.float64).pin_memory()
+    geom_ptr = ctypes.byref(G)
+    L = _lib.lib()
+    aa_c = np.ascontiguousarray(aa)
+    x_ptr = ctypes.cast(h_x.data_ptr(), _lib._dp)
+    img_ptr = ctypes.cast(h_img.data_ptr(), _lib._dp)
+
+    def e2e_step():
+        rc = L.st_image(ctx.handle, geom_ptr, x_ptr, 3, len(x), aa_c.ctypes.data_as(_lib._dp), n_prec, flags, img_ptr)
+        _lib.check(rc, ctx.handle)
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    e2e_ms = []
+    for i in range(args.steps):
+        flush.fill_(float(i))
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        e2e_step()
+        e2e_ms.append((time.perf_counter() - t1) * 1e3)
+    e2e_value = ws * 1000.0 / float(np.mean(e2e_ms))
+
+    # plain FP64 GPU path on the same image
+    step(_lib.ST_FLAG_AVERAGE)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    step(_lib.ST_FLAG_AVERAGE)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    fp64_ms = e0.elapsed_time(e1)
+    img64 = d_img.cpu().numpy().T.copy()
+    d = img32 - img64
+
+    peaks = measure_fp32_peak()
+    V = (G.ix1 - G.ix0) * (G.iy1 - G.iy0) * G.Mz
+    c_tests = reference_candidate_tests(ctx, G, x)
+    flops = 8.0 * c_tests + 6.0 * n_acc + 20.0 * V + 165.0 * (G.Mz // 2) * (G.Mx * G.My) * n_prec
+    col_avg = float(np.mean(col_ms))
+    achieved = flops / (col_avg * 1e-3) / 1e12
+    roof = {"bound": "fp32", "kernel": "k_column_fp32", "achieved": achieved,
+            "peak": peaks["fp32_tflops"] if peaks else None, "unit": "TFLOP/s",
+            "frac": achieved / peaks["fp32_tflops"] if peaks else None,
+            "peak_source": "measured live: FP32 FMA-pipe microbenchmark (libstem_peaks.so) on this GPU",
+            "traffic": None,
+            "algorithmic": {"flops_per_image": flops, "c_tests": c_tests, "accepted_pairs": n_acc,
+                            "voxels": V, "kept_atoms": n_kept, "kernel_ms": col_avg,
+                            "formula": "8*C_tests + 6*accepted + 20*V + 165*(Mz/2)*Mx*My*nPrec"}}
+    line = {"metric": METRIC, "value": value, "unit": "images/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded bcc Fe cell, no dataset)",
+            "config": {"workload": WORKLOAD, "atoms": len(x), "image": [G.Mx, G.My, G.Mz], "n_prec": n_prec,
+                       "path": "FP32 deposition + integration, FP64 binning and g.r mod 1",
+                       "l2": "flushed between steps (512 MB write)", "parallelism": "replicas%d" % ws},
+            "e2e": {"value": e2e_value, "unit": "images/s", "h2d_bytes_per_step": int(x.nbytes),
+                    "d2h_bytes_per_step": int(G.Mx * G.My * 8)},
+            "fp64": {"value": 1000.0 / fp64_ms, "unit": "images/s", "ms": fp64_ms},
+            "accuracy": {"max_abs_dI_fp32_vs_fp64": float(np.abs(d).max()),
+                         "rms_dI_fp32_vs_fp64": float(np.sqrt((d ** 2).mean()))},
+            "gpu_launches": args.steps * launches_per_image(n_prec, fp32=True, average=True),
+            "roofline": roof, "peaks": peaks, "wall_s": wall, "clocks": clk.summary()}
+    if rank == 0:
+        if ws == 1 and not args.no_cpu:
+            line["cpu_baseline"] = cpu_baseline(x_state=(cell, t, x), rows=args.cpu_rows)
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def launches_per_image(n_prec, fp32, average):
+    width = 16 if fp32 else 4
+    passes = (n_prec + width - 1) // width
+    return 6 + passes + (1 if average else 0)  # transform, 3 scans, place, finalize; columns; epilogue
+
+
+def reference_candidate_tests(ctx, G, x):
+    """C_tests of the reference algorithm: every voxel tests every atom of the 27
+    link cells around its home cell (Lib_LinkCell3D.f90:1562-1601).  Computed
+    from the per-cell atom counts of the binning and the voxels' home cells."""
+    # home cells per axis, as the library computes them
+    def homes(n, a_vox, lcd, ia, N):
+        i = np.arange(n, dtype=np.float64)
+        zi = ia * (a_vox * i - lcd)
+        return np.mod(np.floor(zi).astype(np.int64) + 16 * N, N)
+    hx = homes(G.Mx, G.a_vox[0], G.lc_delta[0], G.ia_col[0], G.Ex)[G.ix0:G.ix1]
+    hy = homes(G.My, G.a_vox[4], G.lc_delta[1], G.ia_col[4], G.Ey)[G.iy0:G.iy1]
+    hz = homes(G.Mz, G.a_vox[8], G.lc_delta[2], G.ia_col[8], G.Ez)
+
+    def weight(h, N):
+        nv = np.bincount(h, minlength=N).astype(np.float64)
+        return nv + np.roll(nv, 1) + np.roll(nv, -1)  # voxels whose home is c-1, c or c+1 (periodic)
+    wx, wy, wz = weight(hx, G.Ex), weight(hy, G.Ey), weight(hz, G.Ez)
+    cnt = _bin_counts(G, x).reshape(G.Ez, G.Ey, G.Ex).astype(np.float64)
+    return float(np.einsum("zyx,x,y,z->", cnt, wx, wy, wz))
+
+
+def _bin_counts(G, x):
+    """Per-cell atom counts of findGdotR for geometry G, recounted in numpy for the
+    flop accounting (a boundary atom may land in a neighbouring cell here; the
+    count is used for the roofline only)."""
+    RU = np.array(list(G.RU)).reshape(3, 3, order="F")
+    delta = np.array(list(G.delta))
+    lcd = np.array(list(G.lc_delta))
+    ia = np.array([G.ia_col[0], G.ia_col[4], G.ia_col[8]])
+    N = np.array([G.Ex, G.Ey, G.Ez])
+    counts = np.zeros(G.Ex * G.Ey * G.Ez, dtype=np.int64)
+    for n in range(G.nuvw):
+        R = np.array(list(G.Ruvw)[3 * n:3 * n + 3])
+        y = (x + R) @ RU.T + delta
+        c = (y - lcd) * ia
+        ok = np.all((c >= 0) & (c < N), axis=1)
+        ci = np.floor(c[ok]).astype(np.int64)
+        lin = ci[:, 0] + G.Ex * (ci[:, 1] + G.Ey * ci[:, 2])
+        counts += np.bincount(lin, minlength=len(counts))
+    return counts
+
+
+def cpu_baseline(x_state=None, rows=48, threads=None):
+    """The oracle (C restatement of the reference) on all host cores, on a band of
+    pixel rows of the same image; extrapolated to whole images."""
+    from oracle import stem_oracle as O
+    from simulated_tem_gb300 import synth
+    cell, _, _ = x_state if x_state else (synth.screw_cell_1p2m(), None, None)
+    threads = threads or os.cpu_count() or 1
+    args = O.make_args(cell.a_super, synth.A0_FE, (0, 0, 1), (1, 1, 0), sg=0.01, xi0=103.9, xig=207.5)
+    so, xo, _ = O.setup(args, cell.pos)
+    G, aa = O.geometry(so, len(xo))
+    mid = (G.iy0 + G.iy1) // 2
+    r1 = max(1, rows // 4)
+    t0 = time.perf_counter()
+    O.patch_image(G, aa, xo, rows=(mid, mid + r1), nthreads=threads)
+    ta = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    O.patch_image(G, aa, xo, rows=(mid, mid + rows), nthreads=threads)
+    tb = time.perf_counter() - t0
+    per_row = max((tb - ta) / (rows - r1), 1e-9)
+    t_bin = max(ta - r1 * per_row, 0.0)
+    t_img = t_bin + per_row * (G.iy1 - G.iy0)
+    return {"value": 1.0 / t_img, "unit": "images/s", "cores": threads, "kind": "port",
+            "sample": "oracle C restatement of computeD2BI_img, binning + %d pixel rows of %d (566 columns each, "
+                      "240 voxels deep), extrapolated: %.2f s per image (binning %.2f s)" % (rows, G.iy1 - G.iy0,
+                                                                                            t_img, t_bin),
+            "seconds_measured": ta + tb}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import stem_oracle as O
+    O.build() if not os.path.exists(O.LIB_PATH) else None
+    cell, t, x, _ = workload()
+    vals = []
+    for i in range(args.warmup + args.steps):
+        cb = cpu_baseline(x_state=(cell, t, x), rows=args.cpu_rows)
+        if i >= args.warmup:
+            vals.append(1.0 / cb["value"])
+    s_per_img = float(np.mean(vals))
+    value = 1.0 / s_per_img
+    cb["value"] = value
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "images/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": s_per_img * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded bcc Fe cell)",
+            "config": {"workload": WORKLOAD, "atoms": len(x),
+                       "note": "reference Fortran is not buildable here (no Fortran compiler on either machine); "
+                               "the oracle C restatement of its algorithm runs on all host cores"},
+            "cpu_baseline": cb,
+            "e2e": {"value": value, "unit": "images/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=60)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-rows", type=int, default=48)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

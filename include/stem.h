@@ -1,0 +1,125 @@
+/*
+ * libstem -- GB300 (sm_103a) imaging hot path of simulated_tem's d2bi.
+ *
+ * C ABI: plain pointers and sizes, no C++ or torch types, callable from the
+ * reference's Fortran host through iso_c_binding.  Every entry point returns
+ * ST_OK (0) or an ST_ERR_* code; st_last_error() gives the message.
+ *
+ * Reference interfaces these calls replace (paths are within the reference
+ * project):
+ *   st_image   -- the patch loop of computeD2BI_img,
+ *                 src/Lib_DynamicalTwoBeamImaging.f90:1842-1946 (findGdotR,
+ *                 the link-cell neighbour sums of :1877-1895 and the column
+ *                 integrator dynamicalTwoBeamIntegrationColumn_phaserho
+ *                 :2316-2480).  The geometry and precession set-up before it
+ *                 (:1635-1836) and the MPI_Reduce and average after it
+ *                 (:1950-1951) stay with the caller, exactly as in the
+ *                 reference; ST_FLAG_AVERAGE / ST_FLAG_BRIGHT fold the
+ *                 single-process average and the bright-field flip of
+ *                 src/d2bi.f90:1396 into the call for callers without MPI.
+ *   st_blur    -- gaussianBlurImage, src/d2bi.f90:1543-1624 (private to the
+ *                 d2bi program, applied to the PNG output only).
+ *   st_create / st_destroy -- no counterpart: the library keeps its device
+ *                 buffers across calls (tomography steps, conditions).
+ *
+ * Matrices are 3x3 column-major, as Fortran stores them: m(i,j) is
+ * m[(i-1) + 3*(j-1)].  Images are column-major (0:Mx-1, 0:My-1).
+ */
+#ifndef STEM_H
+#define STEM_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ST_OK 0
+#define ST_ERR_ARG 1      /* invalid argument or unsupported geometry */
+#define ST_ERR_CAPACITY 2 /* a link cell holds more than 16 x nMax0 atoms (the reference stops there) */
+#define ST_ERR_CUDA 3     /* CUDA runtime error */
+#define ST_ERR_TIMEOUT 4  /* a bounded device wait ran out */
+#define ST_ERR_ALLOC 5    /* device or host allocation failed */
+
+/* flags */
+#define ST_FLAG_FP32 0x1    /* FP32 deposition and integration; FP64 binning and g.r reduction */
+#define ST_FLAG_AVERAGE 0x2 /* divide by nPrec (the reference's average after MPI_Reduce) */
+#define ST_FLAG_BRIGHT 0x4  /* with ST_FLAG_AVERAGE: return 1 - I (bright field) */
+#define ST_FLAG_STATS 0x8   /* count candidate tests and accepted pairs (st_get_stats) */
+
+typedef struct st_ctx st_ctx;
+
+/* Per-image geometry: what computeD2BI_img has computed when it enters its
+ * patch loop (Lib_DynamicalTwoBeamImaging.f90:1635-1852). */
+typedef struct st_geom {
+  /* findGdotR transform y = RU (x + Ruvw[n]) + delta, kept if y - lc_delta
+   * lies in the link-cell box; phase g . y (:1160-1265) */
+  double RU[9];       /* matmul(R, U), no beam tilt: precession changes only aa */
+  double delta[3];
+  int32_t nuvw;       /* periodic replicas, <= 27 */
+  int32_t pad0;
+  double Ruvw[81];    /* replica translations uvw(1)*A1 + uvw(2)*A2 + uvw(3)*A3 */
+  double g[3];        /* aperture g-vector (includes 2 pi), getAperture(this) */
+  /* link cells (:1753-1773) */
+  double a_col[9];    /* link-cell vectors a_column */
+  double ia_col[9];   /* inverse3Mat(a_column) */
+  int32_t Ex, Ey, Ez;
+  int32_t nMax0;      /* link-cell capacity estimate (:1681) */
+  double lc_delta[3]; /* offset of the link-cell box for this patch (:1852) */
+  /* voxels */
+  double a_vox[9];    /* getA(gksuper) */
+  int32_t Mx, My, Mz;
+  int32_t ix0, ix1, iy0, iy1; /* pixel window of the patch, half open */
+  int32_t useDensity;
+  /* physics */
+  double sigma;       /* a0 / 2 */
+  double deltaz;      /* xmax(3) / Mz */
+  double b0, bg;      /* pi / xi0, pi / xig */
+} st_geom;
+
+typedef struct st_stats {
+  int64_t n_atoms;     /* input atoms */
+  int64_t n_kept;      /* atoms binned into link cells (all replicas) */
+  int64_t n_tests;     /* candidate pairs tested (ST_FLAG_STATS) */
+  int64_t n_accepted;  /* pairs with r^2 <= (3 sigma)^2 (ST_FLAG_STATS) */
+  int64_t n_voxels;    /* voxels of the patch */
+  int32_t max_cell_count;
+  int32_t n_prec;
+  double ms_bin;       /* device time of the binning kernels (ms) */
+  double ms_column;    /* device time of the column kernel (ms) */
+} st_stats;
+
+/* Context on CUDA device `device` (made current for the calls). */
+int st_create(st_ctx** ctx, int device);
+void st_destroy(st_ctx* ctx);
+const char* st_last_error(const st_ctx* ctx);
+
+/* One image from host buffers (synchronous).
+ *   x    : atom positions, Fortran x(ldx, nAtoms); only x(1:3, :) is read (ldx >= 3)
+ *   aa   : 2 pi s_g for each precession angle, aa(1:nPrec) (:1808-1831)
+ *   img  : Mx x My doubles, column-major, fully overwritten: the patch window
+ *          holds sum_prec |phi_g|^2 (or the average / bright field by flags),
+ *          every other pixel is 0 -- the reference's d2big2 before MPI_Reduce. */
+int st_image(st_ctx* ctx, const st_geom* geom, const double* x, int64_t ldx, int64_t nAtoms, const double* aa,
+             int32_t nPrec, int32_t flags, double* img);
+
+/* Same with x and img in device memory, on `stream` (a cudaStream_t, or 0 for
+ * the context's stream).  Returns after the image is complete. */
+int st_image_device(st_ctx* ctx, const st_geom* geom, const double* d_x, int64_t ldx, int64_t nAtoms,
+                    const double* aa, int32_t nPrec, int32_t flags, double* d_img, void* stream);
+
+/* Gaussian blur of width t pixels (src/d2bi.f90:1543-1624) from host buffers;
+ * in and out are nx x ny doubles, column-major; out is overwritten. */
+int st_blur(st_ctx* ctx, const double* in, int32_t nx, int32_t ny, double t, double* out);
+
+/* Same in device memory, on `stream` (0: the context's stream). */
+int st_blur_device(st_ctx* ctx, const double* d_in, int32_t nx, int32_t ny, double t, double* d_out, void* stream);
+
+/* Counters and kernel times of the last st_image / st_image_device call. */
+int st_get_stats(const st_ctx* ctx, st_stats* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,74 @@
+/*
+ * libstem host mirror -- the reference's Fortran host-side set-up of one
+ * image, restated in C++ behind a C ABI.
+ *
+ * In the reference these routines stay in Fortran and a Fortran caller of
+ * libstem keeps them; they are here because neither machine of this build has
+ * a Fortran compiler, and they give C, C++ and Python callers the reference's
+ * DynamicalTwoBeamImaging type API (src/Lib_DynamicalTwoBeamImaging.f90:31-48)
+ * on top of st_image.  Each function names the routine it mirrors.
+ * Matrices are 3x3 column-major.
+ */
+#ifndef STEM_HOST_H
+#define STEM_HOST_H
+
+#include <stdint.h>
+
+#include "stem.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct st_d2bi st_d2bi; /* type(DynamicalTwoBeamImaging) */
+
+/* DynamicalTwoBeamImaging_ctor0 (Lib_DynamicalTwoBeamImaging.f90:145-166):
+ * super = SimpleSupercell(a_vox, Nx, Ny, Nz) of the input cell, a0, beam k
+ * [uvw], reflection g [hkl], voltage E (keV), voxel subdivisions mxy, mzz. */
+int st_d2bi_create(st_d2bi** h, const double* a_vox, int32_t Nx, int32_t Ny, int32_t Nz, double a0, const double* k,
+                   const double* g, double E, int32_t mxy, int32_t mzz);
+void st_d2bi_destroy(st_d2bi* h);
+/* setConventionalUnitCell (:433-441) */
+int st_d2bi_set_conventional_unit_cell(st_d2bi* h, const double* a_cell);
+/* setVoxelSupercellSize2 (:349-430); all three sides must be nonzero */
+int st_d2bi_set_voxel_supercell_size(st_d2bi* h, const double* cuboid_sides);
+/* setDeviationParameter (:267-274) */
+int st_d2bi_set_deviation_parameter(st_d2bi* h, double sg);
+/* setSupercellTilt0 (:567-792) */
+int st_d2bi_set_supercell_tilt0(st_d2bi* h);
+/* setSupercellTilt2 (:1048-1122) */
+int st_d2bi_set_supercell_tilt2(st_d2bi* h, const double* U, const double* R);
+/* setExtinctionDistances (:337-345) */
+int st_d2bi_set_extinction_distances(st_d2bi* h, double xi0, double xig);
+/* setUseDensityField2 (:1127-1134) */
+int st_d2bi_set_use_density_field(st_d2bi* h, int32_t use);
+/* findImageParameters (:450-482) */
+int st_d2bi_find_image_parameters(const st_d2bi* h, double* aperpx, double* xmax, double* modg, int32_t* Mx,
+                                  int32_t* My, int32_t* Mz);
+/* getRotation (:254-263) */
+int st_d2bi_get_rotation(const st_d2bi* h, double* U, double* R);
+/* getDeviationParameter without g (:292-307) */
+double st_d2bi_get_deviation_parameter(const st_d2bi* h);
+/* The prologue of computeD2BI_img (:1635-1852) for process `rank` of
+ * `nprocs` and patch jj: the st_image geometry and aa(1:nPrec). */
+int st_d2bi_image_geometry(const st_d2bi* h, int64_t nAtoms, int32_t nprocs, int32_t jj, double precAngle,
+                           int32_t nPrec, st_geom* geom, double* aa);
+/* computeD2BI_img (:1563-1998) on one process through st_image: the
+ * precession-averaged dark-field image (Mx x My, column-major). */
+int st_d2bi_compute_img(const st_d2bi* h, st_ctx* ctx, const double* x, int64_t ldx, int64_t nAtoms,
+                        double precAngle, int32_t nPrec, int32_t flags, double* img);
+
+/* d2bi program helpers (src/d2bi.f90) */
+/* wrapPBC of the atoms read from file (:856-866); x is (ldx, n), in place */
+int st_wrap_pbc(const double* a_vox, int32_t Nx, int32_t Ny, int32_t Nz, double* x, int64_t ldx, int64_t n);
+/* atom extents after rotateToStandardFrame(k, a_cell, g) (:1201-1223) */
+int st_atom_extents(const double* k, const double* g, const double* a_cell, const double* x, int64_t ldx, int64_t n,
+                    double* d);
+/* tomography tilt R = Rx(theta) R0 for step nn of nTomo (:1365-1372) */
+int st_tomography_tilt(double tomoAngle, int32_t nn, int32_t nTomo, const double* R0, double* R);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -316,7 +316,7 @@ void oc_d2bi_ctor(oc_d2bi* t, const oc_super* super, double a0, const double* k,
   t->xi0 = 103.9;
   t->xig = 207.5;
   t->useDensityField = 1;
-  for (int i = 0; i < 9; ++i) t->a_cell[i] = a0 * id[i];
+  memcpy(t->a_cell, id, sizeof id); /* set while a0 = 1 (:131) */
   t->sg = NAN;
   t->nuvw = 1;
   identity3(t->R);

@@ -1,0 +1,91 @@
+"""Build libstem.so (and the peak microbenchmark library) in-tree for sm_103a.
+
+nvcc cross-compiles the CUDA sources for sm_103a on any host; the host-side
+C++ is compiled by g++ for the machine it runs on.  Objects go to
+``simulated_tem_gb300/_build/``; the libraries land beside this file.
+Every host translation unit is compiled with -ffp-contract=off so the double
+arithmetic that restates the reference is never fused into multiply-adds.
+"""
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(HERE, "libstem.so")
+PEAKS_LIB = os.path.join(HERE, "libstem_peaks.so")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2",
+                     "--expt-relaxed-constexpr"]
+CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall"]
+
+LIB_SOURCES = ["stem_ctx.cu", "k_bin.cu", "k_column.cu", "k_blur.cu", "host_d2bi.cpp"]
+
+
+def _nvcc():
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found: the CUDA toolkit is required to build libstem")
+
+
+def _cuda_root(nvcc):
+    return os.path.dirname(os.path.dirname(os.path.realpath(nvcc)))
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build step failed:\n%s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
+    return r.stdout + r.stderr
+
+
+def _stale(target, sources):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(s) > t for s in sources)
+
+
+def build(verbose=False, ptxas_info=False):
+    """Compile every source (in parallel) and link the libraries; returns their paths."""
+    nvcc = _nvcc()
+    os.makedirs(BUILD, exist_ok=True)
+    headers = [os.path.join(CSRC, "internal.h"), os.path.join(HERE, "..", "include", "stem.h"),
+               os.path.join(HERE, "..", "include", "stem_host.h")]
+    jobs = []
+    objs = []
+    for src in LIB_SOURCES:
+        path = os.path.join(CSRC, src)
+        obj = os.path.join(BUILD, src + ".o")
+        objs.append(obj)
+        if not _stale(obj, [path] + headers):
+            continue
+        if src.endswith(".cu"):
+            cmd = [nvcc] + NVCC_FLAGS + (["-Xptxas", "-v"] if ptxas_info else []) + ["-c", path, "-o", obj]
+        else:
+            cmd = ["g++"] + CXX_FLAGS + ["-I", os.path.join(_cuda_root(nvcc), "include"), "-c", path, "-o", obj]
+        jobs.append(cmd)
+    outputs = []
+    with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
+        for out in ex.map(_run, jobs):
+            outputs.append(out)
+    if jobs or _stale(LIB, objs):
+        outputs.append(_run([nvcc] + ARCH + ["-shared", "-o", LIB] + objs))
+    peaks_src = os.path.join(CSRC, "peaks.cu")
+    if _stale(PEAKS_LIB, [peaks_src]):
+        outputs.append(_run([nvcc] + NVCC_FLAGS + ["-shared", peaks_src, "-o", PEAKS_LIB]))
+    if verbose:
+        for o in outputs:
+            if o.strip():
+                print(o)
+    return LIB, PEAKS_LIB
+
+
+if __name__ == "__main__":
+    build(verbose=True, ptxas_info="--ptxas" in sys.argv)
+    print("built", LIB, PEAKS_LIB)

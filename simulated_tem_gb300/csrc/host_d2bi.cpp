@@ -1,0 +1,622 @@
+// Host mirror of the reference's Fortran set-up of one image.
+//
+// C++ restatement of the DynamicalTwoBeamImaging type (src/
+// Lib_DynamicalTwoBeamImaging.f90) and the helpers it uses from
+// Lib_SimpleSupercells.f90, Lib_DiffractionConditions.f90 and
+// Lib_RelativisticElectrons.f90.  Compiled with -ffp-contract=off: every
+// expression keeps the reference's left-to-right double arithmetic, so the
+// geometry handed to st_image (cell sizes, offsets, rotations) is the
+// reference's to the last bit.
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <new>
+
+#include "../../include/stem_host.h"
+
+namespace {
+
+constexpr double kPi = 3.141592653589790;  // PI of the reference modules
+constexpr double kMe = 0.056856301036;     // Lib_RelativisticElectrons.f90:9-14
+constexpr double kE = 1.0;
+constexpr double kC = 2997.92458;
+constexpr double kH = 4.135667696;
+const double kHbar = kH / (2 * 3.14159265390);
+const double kHuge1 = (double)FLT_MAX;  // huge(1.0)
+
+struct Mat3 {
+  double m[9];  // column-major
+  double& operator()(int i, int j) { return m[(i - 1) + 3 * (j - 1)]; }
+  double operator()(int i, int j) const { return m[(i - 1) + 3 * (j - 1)]; }
+  static Mat3 identity() {
+    Mat3 r{};
+    r(1, 1) = r(2, 2) = r(3, 3) = 1.0;
+    return r;
+  }
+  static Mat3 from(const double* p) {
+    Mat3 r;
+    std::memcpy(r.m, p, sizeof r.m);
+    return r;
+  }
+};
+
+struct Vec3 {
+  double v[3];
+  double& operator[](int i) { return v[i]; }
+  double operator[](int i) const { return v[i]; }
+};
+
+// gfortran NORM2: scaled sum of squares
+double norm2(const double* v) {
+  double scale = 0.0, res = 1.0;
+  for (int i = 0; i < 3; ++i) {
+    if (v[i] != 0.0) {
+      const double ax = std::fabs(v[i]);
+      if (scale < ax) {
+        const double val = scale / ax;
+        res = 1.0 + res * val * val;
+        scale = ax;
+      } else {
+        const double val = ax / scale;
+        res += val * val;
+      }
+    }
+  }
+  return std::sqrt(res) * scale;
+}
+
+// determinant3Mat (Lib_SimpleSupercells.f90:1240-1256)
+double det3(const Mat3& M) {
+  const double dd[9] = {M(1, 1) * (M(2, 2) * M(3, 3) - M(2, 3) * M(3, 2)),
+                        M(1, 2) * (M(2, 3) * M(3, 1) - M(2, 1) * M(3, 3)),
+                        M(1, 3) * (M(2, 1) * M(3, 2) - M(2, 2) * M(3, 1)),
+                        M(2, 1) * (M(3, 2) * M(1, 3) - M(3, 3) * M(1, 2)),
+                        M(2, 2) * (M(3, 3) * M(1, 1) - M(3, 1) * M(1, 3)),
+                        M(2, 3) * (M(3, 1) * M(1, 2) - M(3, 2) * M(1, 1)),
+                        M(3, 1) * (M(1, 2) * M(2, 3) - M(1, 3) * M(2, 2)),
+                        M(3, 2) * (M(1, 3) * M(2, 1) - M(1, 1) * M(2, 3)),
+                        M(3, 3) * (M(1, 1) * M(2, 2) - M(1, 2) * M(2, 1))};
+  double s = 0.0;
+  for (double d : dd) s += d;
+  return (1.0 / 3.0) * s;
+}
+
+// inverse3Mat (Lib_SimpleSupercells.f90:1205-1236)
+Mat3 inv3(const Mat3& M) {
+  double idd = det3(M);
+  if (std::fabs(idd) < DBL_MIN) return Mat3::identity();
+  idd = 1.0 / idd;
+  Mat3 N;
+  N(1, 1) = (M(2, 2) * M(3, 3) - M(2, 3) * M(3, 2)) * idd;
+  N(2, 1) = (M(2, 3) * M(3, 1) - M(2, 1) * M(3, 3)) * idd;
+  N(3, 1) = (M(2, 1) * M(3, 2) - M(2, 2) * M(3, 1)) * idd;
+  N(1, 2) = (M(1, 3) * M(3, 2) - M(1, 2) * M(3, 3)) * idd;
+  N(2, 2) = (M(1, 1) * M(3, 3) - M(1, 3) * M(3, 1)) * idd;
+  N(3, 2) = (M(1, 2) * M(3, 1) - M(1, 1) * M(3, 2)) * idd;
+  N(1, 3) = (M(1, 2) * M(2, 3) - M(1, 3) * M(2, 2)) * idd;
+  N(2, 3) = (M(1, 3) * M(2, 1) - M(1, 1) * M(2, 3)) * idd;
+  N(3, 3) = (M(1, 1) * M(2, 2) - M(1, 2) * M(2, 1)) * idd;
+  return N;
+}
+
+// matmul, k ascending
+Mat3 mul(const Mat3& a, const Mat3& b) {
+  Mat3 c;
+  for (int j = 1; j <= 3; ++j)
+    for (int i = 1; i <= 3; ++i) {
+      double s = 0.0;
+      for (int k = 1; k <= 3; ++k) s += a(i, k) * b(k, j);
+      c(i, j) = s;
+    }
+  return c;
+}
+
+// y = m(:,1)*v(1) + m(:,2)*v(2) + m(:,3)*v(3)
+Vec3 apply(const Mat3& m, const Vec3& v) {
+  Vec3 y;
+  for (int i = 1; i <= 3; ++i) y[i - 1] = m(i, 1) * v[0] + m(i, 2) * v[1] + m(i, 3) * v[2];
+  return y;
+}
+
+Mat3 transpose(const Mat3& a) {
+  Mat3 t;
+  for (int i = 1; i <= 3; ++i)
+    for (int j = 1; j <= 3; ++j) t(i, j) = a(j, i);
+  return t;
+}
+
+// SimpleSupercell (Lib_SimpleSupercells.f90:51-55, 183-196)
+struct Supercell {
+  int Nx = 1, Ny = 1, Nz = 1;
+  Mat3 a = Mat3::identity(), ia = Mat3::identity();
+  static Supercell make(const Mat3& a, int nx, int ny, int nz) {
+    Supercell s;
+    s.a = a;
+    s.Nx = nx;
+    s.Ny = ny;
+    s.Nz = nz;
+    s.ia = inv3(a);
+    return s;
+  }
+  int n(int i) const { return i == 1 ? Nx : (i == 2 ? Ny : Nz); }
+  Vec3 col(int i) const { return Vec3{{a(1, i), a(2, i), a(3, i)}}; }
+  // getSuperA (:851-860)
+  Mat3 super_a() const {
+    Mat3 s;
+    for (int i = 1; i <= 3; ++i) {
+      s(i, 1) = a(i, 1) * Nx;
+      s(i, 2) = a(i, 2) * Ny;
+      s(i, 3) = a(i, 3) * Nz;
+    }
+    return s;
+  }
+  double cell_side(int i) const {
+    const Vec3 c = col(i);
+    return norm2(c.v);
+  }
+  double super_side(int i) const { return cell_side(i) * n(i); }
+  // cellToRealSpace2 (:338-345)
+  Vec3 cell_to_real(int ix, int iy, int iz) const {
+    Vec3 y;
+    for (int i = 1; i <= 3; ++i) y[i - 1] = a(i, 1) * (double)ix + a(i, 2) * (double)iy + a(i, 3) * (double)iz;
+    return y;
+  }
+};
+
+double wavelength(double V) {  // Lib_RelativisticElectrons.f90:25-38
+  if (V <= 0) return 0.0;
+  const double lambda = 2 * kMe * kE * V * (1 + kE * V / (2 * kMe * kC * kC));
+  return kH / std::sqrt(lambda);
+}
+
+Mat3 reciprocal(const Mat3& a_cell) {  // Lib_DiffractionConditions.f90:1630-1640
+  Mat3 b = inv3(transpose(a_cell));
+  for (double& v : b.m) v = 2 * kPi * v;
+  return b;
+}
+
+Vec3 reflection(const Mat3& B, const double* hkl) {  // :1656-1667
+  Vec3 g;
+  for (int i = 1; i <= 3; ++i) g[i - 1] = B(i, 1) * hkl[0] + B(i, 2) * hkl[1] + B(i, 3) * hkl[2];
+  return g;
+}
+
+double length_sg(double v, double eps) { return -eps / (2 * kPi * kHbar * v); }  // :1194-1204
+
+double energy_deviation(double v, const Vec3& khat, const Vec3& g) {  // :1265-1299
+  const double hbar2on2m = kHbar * kHbar / (2 * kMe);
+  const double cst = 2 * kMe * v / kHbar;
+  double eps = khat[0] * g[0] + khat[1] * g[1] + khat[2] * g[2];
+  eps = cst * eps;
+  eps = eps + g[0] * g[0] + g[1] * g[1] + g[2] * g[2];
+  return eps * hbar2on2m;
+}
+
+// rotateToStandardFrame0 (Lib_DiffractionConditions.f90:65-108)
+Mat3 rotate_to_standard_frame(const double* z0, const Mat3& A_cell, const double* hkl) {
+  const Mat3 BB = reciprocal(A_cell);
+  const Vec3 gg = reflection(BB, hkl);
+  Vec3 zz;
+  for (int i = 1; i <= 3; ++i) {
+    double s = 0.0;
+    for (int k = 1; k <= 3; ++k) s += A_cell(i, k) * z0[k - 1];
+    zz[i - 1] = s;
+  }
+  const double nz = norm2(zz.v);
+  for (int i = 0; i < 3; ++i) zz[i] = zz[i] / nz;
+  double gz = 0.0;
+  for (int i = 0; i < 3; ++i) gz += gg[i] * zz[i];
+  Vec3 xx;
+  for (int i = 0; i < 3; ++i) xx[i] = gg[i] - gz * zz[i];
+  const double nx = norm2(xx.v);
+  for (int i = 0; i < 3; ++i) xx[i] = xx[i] / nx;
+  const Vec3 yy{{zz[1] * xx[2] - zz[2] * xx[1], zz[2] * xx[0] - zz[0] * xx[2], zz[0] * xx[1] - zz[1] * xx[0]}};
+  Mat3 U;
+  for (int j = 1; j <= 3; ++j) {
+    U(1, j) = xx[j - 1];
+    U(2, j) = yy[j - 1];
+    U(3, j) = zz[j - 1];
+  }
+  return U;
+}
+
+Mat3 tilt_about_y(double th) {
+  const double c = std::cos(th), s = std::sin(th);
+  Mat3 R;
+  const double v[9] = {c, 0.0, -s, 0.0, 1.0, 0.0, s, 0.0, c};
+  std::memcpy(R.m, v, sizeof v);
+  return R;
+}
+
+int estimate_max_count_per_cell(double n_cells, int n_total) {  // Lib_LinkCell3D.f90:320-349
+  const double rho = n_total / n_cells;
+  double pp = std::exp(-rho), psum = pp;
+  for (int kk = 1; kk <= n_total; ++kk) {
+    if (psum >= 0.99) return kk;
+    pp = pp * rho / kk;
+    psum = psum + pp;
+  }
+  return n_total;
+}
+
+// FactoriseParallel0 for one to four processes (Lib_FactoriseParallel.f90:33-88)
+bool factorise_parallel(int A, int B, int N, int& C, int& D) {
+  const double a = A, b = B;
+  switch (N) {
+    case 1: C = 1; D = 1; return true;
+    case 2: if (a >= b) { C = 2; D = 1; } else { C = 1; D = 2; } return true;
+    case 3: if (a >= b) { C = 3; D = 1; } else { C = 1; D = 3; } return true;
+    case 4:
+      if (a >= 2 * b) { C = 4; D = 1; }
+      else if (b >= 2 * a) { C = 1; D = 4; }
+      else { C = 2; D = 2; }
+      return true;
+    default: return false;
+  }
+}
+
+}  // namespace
+
+// type(DynamicalTwoBeamImaging) (Lib_DynamicalTwoBeamImaging.f90:59-84)
+struct st_d2bi {
+  double k[3], g[3];
+  double a0;
+  Supercell super;
+  double sg = NAN;
+  int mxy = 0, mzz = 0;
+  double xi0 = 103.9, xig = 207.5;
+  double E = 150.0;
+  bool useDensityField = true;
+  Supercell gksuper;
+  double delta[3] = {0, 0, 0};
+  double vsd[3] = {0, 0, 0};  // voxelSupercellDimensions
+  int nuvw = 1;
+  int uvw[3 * 27] = {0};
+  Mat3 a_cell = Mat3::identity(), U = Mat3::identity(), R = Mat3::identity();
+
+  Vec3 aperture(const Mat3* beam_tilt) const {  // getAperture (:1137-1155)
+    const Mat3 b = reciprocal(a_cell);
+    Vec3 gv = reflection(b, g);
+    Mat3 RU = mul(R, U);
+    if (beam_tilt) RU = mul(*beam_tilt, RU);
+    return apply(RU, gv);
+  }
+  double deviation(const Vec3& gv) const {  // getDeviationParameter (:292-307)
+    const double modk = 2 * kPi / wavelength(E * 1000);
+    const double vv = kHbar * modk / kMe;
+    return length_sg(vv, energy_deviation(vv, Vec3{{0.0, 0.0, 1.0}}, gv));
+  }
+  // findTransformedSupercell (Lib_DiffractionConditions.f90:996-1189) and the
+  // gksuper built from it (:775-784, :1086-1096)
+  void transformed_supercell() {
+    const Mat3 RU = mul(R, U);
+    const Mat3 A = super.super_a();
+    Vec3 xx{{0.5, 0.5, 0.5}};
+    xx = apply(A, xx);
+    xx = apply(RU, xx);
+    for (int i = 0; i < 3; ++i) delta[i] = vsd[i] / 2 - xx[i];
+    int n = 0;
+    for (int iz = -1; iz <= 1; ++iz)
+      for (int iy = -1; iy <= 1; ++iy)
+        for (int ix = -1; ix <= 1; ++ix) {
+          uvw[3 * n] = ix;
+          uvw[3 * n + 1] = iy;
+          uvw[3 * n + 2] = iz;
+          ++n;
+        }
+    nuvw = n;
+    Mat3 D{};
+    D(1, 1) = vsd[0];
+    D(2, 2) = vsd[1];
+    D(3, 3) = vsd[2];
+    const int nx = std::max(mxy, (int)std::lround(mxy * D(1, 1) / a0));
+    const int ny = std::max(mxy, (int)std::lround(mxy * D(2, 2) / a0));
+    const int nz = std::max(mzz, (int)std::lround(mzz * D(3, 3) / a0));
+    D(1, 1) = D(1, 1) / nx;
+    D(2, 2) = D(2, 2) / ny;
+    D(3, 3) = D(3, 3) / nz;
+    gksuper = Supercell::make(D, nx, ny, nz);
+  }
+};
+
+extern "C" {
+
+int st_d2bi_create(st_d2bi** h, const double* a_vox, int32_t Nx, int32_t Ny, int32_t Nz, double a0, const double* k,
+                   const double* g, double E, int32_t mxy, int32_t mzz) {
+  if (!h || !a_vox || !k || !g || Nx < 1 || Ny < 1 || Nz < 1 || !(a0 > 0) || mxy < 1 || mzz < 1) return ST_ERR_ARG;
+  st_d2bi* t = new (std::nothrow) st_d2bi();
+  if (!t) return ST_ERR_ALLOC;
+  t->super = Supercell::make(Mat3::from(a_vox), Nx, Ny, Nz);
+  t->a0 = a0;  // the constructor leaves a_cell = 1.0 * identity (a0 = 1 when it is set, :131)
+  std::memcpy(t->k, k, sizeof t->k);
+  std::memcpy(t->g, g, sizeof t->g);
+  t->E = E;
+  t->mxy = mxy;
+  t->mzz = mzz;
+  *h = t;
+  return ST_OK;
+}
+
+void st_d2bi_destroy(st_d2bi* h) { delete h; }
+
+int st_d2bi_set_conventional_unit_cell(st_d2bi* h, const double* a_cell) {
+  if (!h || !a_cell) return ST_ERR_ARG;
+  h->a_cell = Mat3::from(a_cell);
+  return ST_OK;
+}
+
+int st_d2bi_set_voxel_supercell_size(st_d2bi* h, const double* cs) {
+  if (!h || !cs) return ST_ERR_ARG;
+  const double hkl[3] = {(double)std::lround(h->g[0]), (double)std::lround(h->g[1]), (double)std::lround(h->g[2])};
+  h->U = rotate_to_standard_frame(h->k, h->a_cell, hkl);
+  if (cs[0] == 0 || cs[1] == 0 || cs[2] == 0) return ST_ERR_ARG;  // sizes from the oriented supercell: not mirrored
+  std::memcpy(h->vsd, cs, sizeof h->vsd);
+  return ST_OK;
+}
+
+int st_d2bi_set_deviation_parameter(st_d2bi* h, double sg) {
+  if (!h) return ST_ERR_ARG;
+  h->sg = sg;
+  return ST_OK;
+}
+
+int st_d2bi_set_supercell_tilt0(st_d2bi* t) {
+  if (!t) return ST_ERR_ARG;
+  const double hkl[3] = {(double)std::lround(t->g[0]), (double)std::lround(t->g[1]), (double)std::lround(t->g[2])};
+  t->U = rotate_to_standard_frame(t->k, t->a_cell, hkl);
+  const Mat3 a_cell0 = mul(t->U, t->a_cell);
+  Vec3 gg = reflection(reciprocal(a_cell0), t->g);
+  const double modg = norm2(gg.v);
+  const double modk = 2 * kPi / wavelength(t->E * 1000);
+  const double vv = kHbar * modk / kMe;
+  const Vec3 khat{{0.0, 0.0, 1.0}};
+  double eps = energy_deviation(vv, khat, gg);
+  if (std::isnan(t->sg)) {
+    t->sg = length_sg(vv, eps);
+    t->R = Mat3::identity();
+  } else {
+    const double aa = 2 * kPi * t->sg + kHbar * modg * modg / (2 * kMe * vv);
+    double cc = gg[0] * gg[0] + gg[2] * gg[2];
+    double bb = cc - aa * aa;
+    if (bb < 0) {
+      t->sg = length_sg(vv, eps);
+      t->R = Mat3::identity();
+    } else {
+      bb = std::sqrt(bb);
+      cc = 1 / cc;
+      double th[4], sgs[4];
+      th[0] = std::acos(-(gg[2] * aa + gg[0] * bb) * cc);
+      th[1] = std::acos(-(gg[2] * aa - gg[0] * bb) * cc);
+      th[2] = -th[0];
+      th[3] = -th[1];
+      for (int i = 0; i < 4; ++i) {
+        const Mat3 Ri = tilt_about_y(th[i]);
+        const Vec3 g2 = reflection(reciprocal(mul(Ri, a_cell0)), t->g);
+        sgs[i] = length_sg(vv, energy_deviation(vv, khat, g2));
+      }
+      for (int i = 0; i < 4; ++i)
+        if (std::fabs(th[i]) * 2 > kPi) sgs[i] = kHuge1;
+      int best = 0;
+      double bestv = std::fabs(t->sg - sgs[0]);
+      for (int i = 1; i < 4; ++i) {
+        const double v = std::fabs(t->sg - sgs[i]);
+        if (v < bestv) {
+          bestv = v;
+          best = i;
+        }
+      }
+      t->R = tilt_about_y(th[best]);
+    }
+    gg = reflection(reciprocal(mul(t->R, a_cell0)), t->g);
+    eps = energy_deviation(vv, khat, gg);
+    t->sg = length_sg(vv, eps);
+  }
+  t->transformed_supercell();
+  t->sg = t->deviation(t->aperture(nullptr));
+  return ST_OK;
+}
+
+int st_d2bi_set_supercell_tilt2(st_d2bi* t, const double* U, const double* R) {
+  if (!t || !U || !R) return ST_ERR_ARG;
+  t->U = Mat3::from(U);
+  t->R = Mat3::from(R);
+  t->transformed_supercell();
+  t->sg = t->deviation(t->aperture(nullptr));
+  return ST_OK;
+}
+
+int st_d2bi_set_extinction_distances(st_d2bi* h, double xi0, double xig) {
+  if (!h || !(xi0 != 0) || !(xig != 0)) return ST_ERR_ARG;
+  h->xi0 = xi0;
+  h->xig = xig;
+  return ST_OK;
+}
+
+int st_d2bi_set_use_density_field(st_d2bi* h, int32_t use) {
+  if (!h) return ST_ERR_ARG;
+  h->useDensityField = use != 0;
+  return ST_OK;
+}
+
+int st_d2bi_find_image_parameters(const st_d2bi* t, double* aperpx, double* xmax, double* modg, int32_t* Mx,
+                                  int32_t* My, int32_t* Mz) {
+  if (!t) return ST_ERR_ARG;
+  const Vec3 gg = reflection(reciprocal(t->a_cell), t->g);
+  double xm[3];
+  for (int i = 1; i <= 3; ++i) xm[i - 1] = t->gksuper.super_side(i);
+  const int mx = t->gksuper.Nx, my = t->gksuper.Ny, mz = t->gksuper.Nz;
+  if (aperpx) *aperpx = std::sqrt(xm[0] * xm[1] / (double)(mx * my));
+  if (xmax) std::memcpy(xmax, xm, sizeof xm);
+  if (modg) *modg = norm2(gg.v);
+  if (Mx) *Mx = mx;
+  if (My) *My = my;
+  if (Mz) *Mz = mz;
+  return ST_OK;
+}
+
+int st_d2bi_get_rotation(const st_d2bi* h, double* U, double* R) {
+  if (!h) return ST_ERR_ARG;
+  if (U) std::memcpy(U, h->U.m, sizeof h->U.m);
+  if (R) std::memcpy(R, h->R.m, sizeof h->R.m);
+  return ST_OK;
+}
+
+double st_d2bi_get_deviation_parameter(const st_d2bi* h) { return h ? h->sg : NAN; }
+
+int st_d2bi_image_geometry(const st_d2bi* t, int64_t nAtoms, int32_t nprocs, int32_t jj, double precAngle,
+                           int32_t nPrec, st_geom* G, double* aa) {
+  if (!t || !G || !aa || nPrec < 1 || nAtoms < 0) return ST_ERR_ARG;
+  std::memset(G, 0, sizeof *G);
+  double xmax[3];
+  int Mx, My, Mz;
+  st_d2bi_find_image_parameters(t, nullptr, xmax, nullptr, &Mx, &My, &Mz);
+  double costheta = 1.0, sintheta = 0.0;
+  if (nPrec > 1) {
+    costheta = std::cos(precAngle);
+    sintheta = std::sin(precAngle);
+  }
+  const double sigma = t->a0 / 2;
+  const double cmin = std::min(t->gksuper.cell_side(1), t->gksuper.cell_side(2));
+  const int deltaM = (int)std::ceil(3 * sigma / cmin);
+  const int nMax = estimate_max_count_per_cell((double)Mx * My * Mz, (int)nAtoms) * deltaM * deltaM;
+  int Cx, Cy;
+  if (!factorise_parallel(Mx, My, nprocs, Cx, Cy)) return ST_ERR_ARG;
+  if (jj < 0 || jj >= Cx * Cy) return ST_ERR_ARG;
+  // real(Mx)/Cx and real(Dx)/deltaM + 2 are default-kind (single precision) in the reference
+  const int Dx = (int)std::ceil((float)Mx / (float)Cx);
+  const int Dy = (int)std::ceil((float)My / (float)Cy);
+  const int Ex = std::max(3, (int)std::floor((float)Dx / (float)deltaM + 2.0f));
+  const int Ey = std::max(3, (int)std::floor((float)Dy / (float)deltaM + 2.0f));
+  const int Ez = std::max(3, (int)std::floor((float)Mz / (float)deltaM));
+  const Mat3& a_vox = t->gksuper.a;
+  Mat3 a_col;
+  for (int i = 1; i <= 3; ++i) {
+    a_col(i, 1) = (Dx + 2 * deltaM) * a_vox(i, 1) / Ex;
+    a_col(i, 2) = (Dy + 2 * deltaM) * a_vox(i, 2) / Ey;
+    a_col(i, 3) = Mz * a_vox(i, 3) / Ez;
+  }
+  const Supercell lc = Supercell::make(a_col, Ex, Ey, Ez);
+
+  for (int prec = 1; prec <= nPrec; ++prec) {  // :1805-1831
+    Vec3 gg;
+    if (prec == 1) {
+      gg = t->aperture(nullptr);
+    } else {
+      const double phi = (prec - 1) * 2 * kPi / (nPrec - 1);
+      const double ux = std::sin(phi), uy = std::cos(phi);
+      Mat3 BT;
+      BT(1, 1) = costheta + ux * ux * (1 - costheta);
+      BT(1, 2) = ux * uy * (1 - costheta);
+      BT(1, 3) = uy * sintheta;
+      BT(2, 1) = ux * uy * (1 - costheta);
+      BT(2, 2) = costheta + uy * uy * (1 - costheta);
+      BT(2, 3) = -ux * sintheta;
+      BT(3, 1) = -uy * sintheta;
+      BT(3, 2) = ux * sintheta;
+      BT(3, 3) = costheta;
+      gg = t->aperture(&BT);
+    }
+    Vec3 z{{0.0, 0.0, 0.0}};
+    for (int i = 0; i < 3; ++i) z[i] = gg[i] + z[i];  // + dgAperturePoint (zero for one aperture point)
+    aa[prec - 1] = (2 * kPi * t->deviation(z));
+  }
+
+  const int jy = jj / Cx, jx = jj - jy * Cx;  // :1843-1852
+  const Vec3 p0 = t->gksuper.cell_to_real(jx * Dx, jy * Dy, 0);
+  const Vec3 p1 = lc.cell_to_real(1, 1, 0);
+  for (int i = 0; i < 3; ++i) G->lc_delta[i] = p0[i] - p1[i];
+  G->Mx = Mx;
+  G->My = My;
+  G->Mz = Mz;
+  G->ix0 = jx * Dx;
+  G->ix1 = std::min((jx + 1) * Dx, Mx);
+  G->iy0 = jy * Dy;
+  G->iy1 = std::min((jy + 1) * Dy, My);
+  G->Ex = Ex;
+  G->Ey = Ey;
+  G->Ez = Ez;
+  G->nMax0 = nMax;
+  std::memcpy(G->a_col, lc.a.m, sizeof G->a_col);
+  std::memcpy(G->ia_col, lc.ia.m, sizeof G->ia_col);
+  std::memcpy(G->a_vox, a_vox.m, sizeof G->a_vox);
+  const Mat3 RU = mul(t->R, t->U);
+  std::memcpy(G->RU, RU.m, sizeof G->RU);
+  std::memcpy(G->delta, t->delta, sizeof G->delta);
+  G->nuvw = t->nuvw;
+  const Mat3 sv = t->super.super_a();  // getSuperVector(this%super, i) = a(:,i) N_i
+  for (int n = 0; n < t->nuvw; ++n)
+    for (int i = 1; i <= 3; ++i)
+      G->Ruvw[3 * n + i - 1] = t->uvw[3 * n] * sv(i, 1) + t->uvw[3 * n + 1] * sv(i, 2) + t->uvw[3 * n + 2] * sv(i, 3);
+  const Vec3 g0 = t->aperture(nullptr);
+  std::memcpy(G->g, g0.v, sizeof G->g);
+  G->useDensity = t->useDensityField ? 1 : 0;
+  G->sigma = sigma;
+  G->deltaz = xmax[2] / Mz;
+  G->b0 = (kPi / t->xi0);
+  G->bg = (kPi / t->xig);
+  return ST_OK;
+}
+
+int st_d2bi_compute_img(const st_d2bi* t, st_ctx* ctx, const double* x, int64_t ldx, int64_t nAtoms,
+                        double precAngle, int32_t nPrec, int32_t flags, double* img) {
+  if (!t || !ctx || nPrec < 1) return ST_ERR_ARG;
+  st_geom G;
+  double* aa = new (std::nothrow) double[nPrec];
+  if (!aa) return ST_ERR_ALLOC;
+  int rc = st_d2bi_image_geometry(t, nAtoms, 1, 0, precAngle, nPrec, &G, aa);
+  if (rc == ST_OK) rc = st_image(ctx, &G, x, ldx, nAtoms, aa, nPrec, flags | ST_FLAG_AVERAGE, img);
+  delete[] aa;
+  return rc;
+}
+
+int st_wrap_pbc(const double* a_vox, int32_t Nx, int32_t Ny, int32_t Nz, double* x, int64_t ldx, int64_t n) {
+  if (!a_vox || !x || ldx < 3 || n < 0 || Nx < 1 || Ny < 1 || Nz < 1) return ST_ERR_ARG;
+  const Supercell s = Supercell::make(Mat3::from(a_vox), Nx, Ny, Nz);
+  const int N[3] = {Nx, Ny, Nz};
+  for (int64_t j = 0; j < n; ++j) {  // wrapPBC0 (Lib_SimpleSupercells.f90:992-1023)
+    double* y = x + j * ldx;
+    Vec3 xx = apply(s.ia, Vec3{{y[0], y[1], y[2]}});
+    for (int d = 0; d < 3; ++d) {
+      int ii = (int)std::floor(xx[d]);
+      xx[d] = xx[d] - ii;
+      ii = (ii + (N[d] << 8)) % N[d];
+      xx[d] = (ii + xx[d]);
+    }
+    const Vec3 yp = apply(s.a, xx);
+    y[0] = yp[0];
+    y[1] = yp[1];
+    y[2] = yp[2];
+  }
+  return ST_OK;
+}
+
+int st_atom_extents(const double* k, const double* g, const double* a_cell, const double* x, int64_t ldx, int64_t n,
+                    double* d) {
+  if (!k || !g || !a_cell || !d || (n > 0 && !x) || ldx < 3) return ST_ERR_ARG;
+  const Mat3 rot = rotate_to_standard_frame(k, Mat3::from(a_cell), g);
+  double lo[3] = {kHuge1, kHuge1, kHuge1}, hi[3] = {-kHuge1, -kHuge1, -kHuge1};
+  for (int64_t j = 0; j < n; ++j) {
+    const Vec3 y = apply(rot, Vec3{{x[j * ldx], x[j * ldx + 1], x[j * ldx + 2]}});
+    for (int i = 0; i < 3; ++i) {
+      lo[i] = std::min(lo[i], y[i]);
+      hi[i] = std::max(hi[i], y[i]);
+    }
+  }
+  for (int i = 0; i < 3; ++i) d[i] = hi[i] - lo[i];
+  return ST_OK;
+}
+
+int st_tomography_tilt(double tomoAngle, int32_t nn, int32_t nTomo, const double* R0, double* Rout) {
+  if (!R0 || !Rout || nTomo < 2 || nn < 0 || nn >= nTomo) return ST_ERR_ARG;
+  double theta = tomoAngle - 2 * tomoAngle * nn / (nTomo - 1);
+  theta = theta * 3.141592654 / 180.0;
+  Mat3 R;
+  const double v[9] = {1.0, 0.0, 0.0, 0.0, std::cos(theta), std::sin(theta), 0.0, -std::sin(theta), std::cos(theta)};
+  std::memcpy(R.m, v, sizeof v);
+  const Mat3 out = mul(R, Mat3::from(R0));
+  std::memcpy(Rout, out.m, sizeof out.m);
+  return ST_OK;
+}
+
+}  // extern "C"

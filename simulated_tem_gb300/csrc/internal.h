@@ -1,0 +1,119 @@
+// Internal declarations shared by the libstem translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/stem.h"
+
+namespace stem {
+
+// Fixed-size kernel parameters of the link-cell binning (K1).
+struct BinParams {
+  int64_t n_atoms;
+  int64_t cap;  // capacity of the kept-atom arrays; more kept atoms set the overflow condition
+  int64_t ldx;
+  int nuvw;
+  int Ex, Ey, Ez;
+  int64_t n_cells;
+  double RU[9];
+  double delta[3];
+  double Ruvw[81];
+  double lc_delta[3];
+  double ia[9];  // inverse link-cell vectors
+  double g[3];
+  double a_col[3];  // diagonal of the link-cell vectors (cuboid cells)
+  // FP32 copies for the reject prefilter
+  float RUf[9];
+  float Ruvwf[81];
+  float shiftf[3];  // delta - lc_delta
+  float iaf[3];     // diagonal of ia
+};
+
+// Output of the binning: atoms sorted by link cell, each cell in the
+// reference's insertion order (replica-major, then atom order).
+struct BinnedAtoms {
+  int* cell_start;     // n_cells + 1
+  int* cell_count;     // n_cells
+  // FP64 records
+  double4_32a* f64;        // fx, fy, fz (fractional offset in the cell), unused
+  double2* cs64;       // cos(g.y), sin(g.y)
+  // FP32 records
+  float4* p32;         // a_col11*fx, a_col22*fy, a_col33*fz, bits(packed cell)
+  float2* cs32;        // cos, sin of the FP64-reduced phase
+  int* cell_of;        // packed cell (cx | cy << 10 | cz << 20)
+};
+
+struct Scratch {
+  // binning temporaries, sized for nuvw * n_atoms candidates
+  int* tmp_key = nullptr;   // candidate index nn * N + jj
+  int* tmp_cell = nullptr;  // linear cell index
+  int* tmp_slot = nullptr;  // arrival slot within the cell (atomic order)
+  double4_32a* tmp_f = nullptr; // fx, fy, fz, g.y
+  int* perm = nullptr;      // position-in-cell -> tmp index
+  int* block_sums = nullptr;
+  unsigned long long* counters = nullptr;  // [0] kept, [1] max cell count, [2] tests, [3] accepted
+  size_t cap_candidates = 0;
+  size_t cap_cells = 0;
+  size_t cap_blocks = 0;
+  // per-image tables of the voxel columns
+  int2* xtab = nullptr;  // (home cell, unused) per ix
+  double* xfv = nullptr; // fractional voxel offset per ix
+  int2* ytab = nullptr;
+  double* yfv = nullptr;
+  int2* ztab = nullptr;
+  double* zfv = nullptr;
+  size_t cap_x = 0, cap_y = 0, cap_z = 0;
+  double* aa = nullptr;
+  float* aaf = nullptr;
+  size_t cap_prec = 0;
+};
+
+struct ColumnParams {
+  int Mx, My, Mz;
+  int ix0, ix1, iy0, iy1;
+  int Ex, Ey, Ez;
+  int n_prec;
+  int prec_offset;  // first precession angle of this pass
+  int accumulate;   // add into img instead of overwriting
+  int use_density;
+  int check_cells;  // restrict to the 27 cells around the home cell (needed when a cell is < 3 sigma)
+  int want_stats;
+  double a11, a22, a33;  // link-cell sides (cuboid)
+  double cut2;           // (3 sigma)^2
+  double i2s2;           // 1 / (2 sigma^2)
+  double sigma;
+  double b0, bg, dz;
+  const int* cell_start;
+  const double4_32a* f64;
+  const double2* cs64;
+  const float4* p32;
+  const float2* cs32;
+  const int2* xtab;
+  const double* xfv;
+  const int2* ytab;
+  const double* yfv;
+  const int2* ztab;
+  const double* zfv;
+  const double* aa;
+  const float* aaf;
+  double* img;
+  unsigned long long* counters;  // [0] kept atoms: above `cap` the binning overflowed and the kernel exits
+  int64_t cap;
+};
+
+// launchers (return cudaError_t of the launches)
+cudaError_t launch_bin(const BinParams& p, const double* d_x, Scratch& s, BinnedAtoms& b, cudaStream_t st);
+cudaError_t launch_bin_finalize(const BinParams& p, Scratch& s, BinnedAtoms& b, int want_fp64, cudaStream_t st);
+cudaError_t launch_column_fp32(const ColumnParams& p, cudaStream_t st);
+cudaError_t launch_column_fp64(const ColumnParams& p, cudaStream_t st);
+cudaError_t launch_epilogue(double* img, int Mx, int My, int ix0, int ix1, int iy0, int iy1, double scale,
+                            int bright, cudaStream_t st);
+cudaError_t launch_blur(const double* d_in, double* d_tmp, double* d_out, int nx, int ny, const double* d_kernel,
+                        int nk, cudaStream_t st);
+
+__host__ __device__ inline int pack_cell(int cx, int cy, int cz) { return cx | (cy << 10) | (cz << 20); }
+
+}  // namespace stem

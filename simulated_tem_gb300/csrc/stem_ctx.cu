@@ -1,0 +1,485 @@
+// libstem C ABI: context, device memory and the image / blur entry points.
+//
+// st_image replaces the patch loop of computeD2BI_img
+// (src/Lib_DynamicalTwoBeamImaging.f90:1842-1946): K1 bins the atoms
+// (findGdotR), K2+K3 compute the voxel field and integrate every column, and
+// an epilogue applies the optional average over precession angles and the
+// bright-field flip.  st_blur is gaussianBlurImage (src/d2bi.f90:1543-1624).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "internal.h"
+
+using namespace stem;
+
+struct st_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  Scratch s;
+  BinnedAtoms b{};
+  size_t cap_kept = 0;
+  size_t cap_cells = 0;
+  double* d_x = nullptr;
+  size_t cap_x = 0;
+  double* d_img = nullptr;
+  size_t cap_img = 0;
+  double* d_blur = nullptr;  // in, tmp (+w_stripe), out
+  size_t cap_blur = 0;
+  double* d_kern = nullptr;
+  size_t cap_kern = 0;
+  unsigned long long* h_counters = nullptr;  // pinned
+  void* h_stage = nullptr;                   // pinned staging for tables
+  size_t cap_stage = 0;
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+  st_stats stats{};
+  int64_t last_kept = 0;  // kept atoms of the previous image: sizes the next one
+};
+
+namespace {
+
+int fail(st_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+int cuda_fail(st_ctx* c, cudaError_t e, const char* where) {
+  return fail(c, ST_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+template <typename T>
+cudaError_t ensure(T*& p, size_t& cap, size_t need) {
+  if (need <= cap && p) return cudaSuccess;
+  if (p) cudaFree(p);
+  p = nullptr;
+  cap = 0;
+  size_t n = need + need / 4 + 64;
+  cudaError_t e = cudaMalloc((void**)&p, n * sizeof(T));
+  if (e == cudaSuccess) cap = n;
+  return e;
+}
+
+cudaError_t ensure_host(void*& p, size_t& cap, size_t bytes) {
+  if (bytes <= cap && p) return cudaSuccess;
+  if (p) cudaFreeHost(p);
+  p = nullptr;
+  cap = 0;
+  size_t n = bytes + bytes / 4 + 256;
+  cudaError_t e = cudaMallocHost(&p, n);
+  if (e == cudaSuccess) cap = n;
+  return e;
+}
+
+// Arrays indexed by kept atom (binning temporaries and records).
+bool alloc_kept(st_ctx* c, size_t need) {
+  if (need <= c->cap_kept && c->b.p32) return true;
+  size_t k = 0;
+  cudaError_t e = cudaSuccess;
+  auto grow = [&](auto*& p) {
+    size_t cap = c->cap_kept;
+    if (e == cudaSuccess) e = ensure(p, cap, need);
+    k = cap;
+  };
+  grow(c->s.tmp_key);
+  grow(c->s.tmp_cell);
+  grow(c->s.tmp_slot);
+  grow(c->s.tmp_f);
+  grow(c->s.perm);
+  grow(c->b.f64);
+  grow(c->b.cs64);
+  grow(c->b.p32);
+  grow(c->b.cs32);
+  grow(c->b.cell_of);
+  if (e != cudaSuccess) return false;
+  c->cap_kept = k;
+  c->s.cap_candidates = k;
+  return true;
+}
+
+bool is_cuboid(const double* m) {
+  return m[1] == 0.0 && m[2] == 0.0 && m[3] == 0.0 && m[5] == 0.0 && m[6] == 0.0 && m[7] == 0.0;
+}
+
+// Home link cell and fractional offset of voxel index i along one axis:
+// zi = ia * (a_vox * i - lc_delta); h = mod(floor(zi) + 16 N, N); fv = zi - h
+// (Lib_DynamicalTwoBeamImaging.f90:1878-1879, Lib_LinkCell3D.f90:1547-1560).
+void axis_table(int n, double a_vox, double lcd, double ia, int N, int2* tab, double* fv) {
+  for (int i = 0; i < n; ++i) {
+    const double xx = a_vox * (double)i - lcd;
+    const double zi = ia * xx;
+    int h = (int)std::floor(zi) + 16 * N;
+    h = h % N;
+    if (h < 0) h += N;  // the reference's mod of a non-negative value
+    tab[i] = make_int2(h, 0);
+    fv[i] = zi - (double)h;
+  }
+}
+
+int validate(st_ctx* c, const st_geom* g, int64_t ldx, int64_t nAtoms, int32_t nPrec) {
+  if (!g) return fail(c, ST_ERR_ARG, "geometry is null");
+  if (ldx < 3) return fail(c, ST_ERR_ARG, "ldx must be >= 3");
+  if (nAtoms < 0) return fail(c, ST_ERR_ARG, "nAtoms must be >= 0");
+  if (nPrec < 1) return fail(c, ST_ERR_ARG, "nPrec must be >= 1");
+  if (g->Mx < 1 || g->My < 1 || g->Mz < 1) return fail(c, ST_ERR_ARG, "Mx, My, Mz must be >= 1");
+  if (g->ix0 < 0 || g->ix1 > g->Mx || g->ix0 > g->ix1 || g->iy0 < 0 || g->iy1 > g->My || g->iy0 > g->iy1)
+    return fail(c, ST_ERR_ARG, "patch window outside the image");
+  if (g->Ex < 1 || g->Ey < 1 || g->Ez < 1 || g->Ex > 1023 || g->Ey > 1023 || g->Ez > 1023)
+    return fail(c, ST_ERR_ARG, "link-cell counts must be in 1..1023 per axis");
+  if (g->nuvw < 1 || g->nuvw > 27) return fail(c, ST_ERR_ARG, "nuvw must be in 1..27");
+  if ((double)g->nuvw * (double)nAtoms >= 2147483647.0)
+    return fail(c, ST_ERR_ARG, "nuvw * nAtoms exceeds 2^31 - 1 candidates");
+  if (!is_cuboid(g->a_vox) || !is_cuboid(g->a_col) || !is_cuboid(g->ia_col))
+    return fail(c, ST_ERR_ARG, "voxel and link cells must be cuboids (diagonal a_vox, a_col, ia_col)");
+  if (!(g->sigma > 0.0) || !(g->deltaz > 0.0)) return fail(c, ST_ERR_ARG, "sigma and deltaz must be > 0");
+  return ST_OK;
+}
+
+}  // namespace
+
+extern "C" int st_create(st_ctx** out, int device) {
+  if (!out) return ST_ERR_ARG;
+  *out = nullptr;
+  st_ctx* c = new st_ctx();
+  c->device = device;
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) {
+    delete c;
+    return ST_ERR_CUDA;
+  }
+  e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMallocHost((void**)&c->h_counters, 8 * sizeof(unsigned long long));
+  for (int i = 0; i < 3 && e == cudaSuccess; ++i) e = cudaEventCreate(&c->ev[i]);
+  if (e != cudaSuccess) {
+    delete c;
+    return ST_ERR_CUDA;
+  }
+  *out = c;
+  return ST_OK;
+}
+
+extern "C" void st_destroy(st_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  void* dev_ptrs[] = {c->s.tmp_key, c->s.tmp_cell, c->s.tmp_slot, c->s.tmp_f, c->s.perm, c->s.block_sums,
+                      c->s.counters, c->s.xtab, c->s.xfv, c->s.ytab, c->s.yfv, c->s.ztab, c->s.zfv, c->s.aa,
+                      c->s.aaf, c->b.cell_start, c->b.cell_count, c->b.f64, c->b.cs64, c->b.p32, c->b.cs32,
+                      c->b.cell_of, c->d_x, c->d_img, c->d_blur, c->d_kern};
+  for (void* p : dev_ptrs)
+    if (p) cudaFree(p);
+  if (c->h_counters) cudaFreeHost(c->h_counters);
+  if (c->h_stage) cudaFreeHost(c->h_stage);
+  for (auto& e : c->ev)
+    if (e) cudaEventDestroy(e);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+extern "C" const char* st_last_error(const st_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+extern "C" int st_get_stats(const st_ctx* c, st_stats* out) {
+  if (!c || !out) return ST_ERR_ARG;
+  *out = c->stats;
+  return ST_OK;
+}
+
+extern "C" int st_image_device(st_ctx* c, const st_geom* g, const double* d_x, int64_t ldx, int64_t nAtoms,
+                               const double* aa, int32_t nPrec, int32_t flags, double* d_img, void* stream) {
+  if (!c) return ST_ERR_ARG;
+  int rc = validate(c, g, ldx, nAtoms, nPrec);
+  if (rc != ST_OK) return rc;
+  if (!aa || !d_img || (nAtoms > 0 && !d_x)) return fail(c, ST_ERR_ARG, "null buffer");
+  cudaSetDevice(c->device);
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+  const bool fp32 = (flags & ST_FLAG_FP32) != 0;
+  const int64_t n_cells = (int64_t)g->Ex * g->Ey * g->Ez;
+  const int Mx = g->Mx, My = g->My, Mz = g->Mz;
+
+  // ---- device buffers that do not depend on the kept-atom count
+  cudaError_t e = cudaSuccess;
+  {
+    size_t cc = c->cap_cells;
+    e = ensure(c->b.cell_start, cc, (size_t)n_cells + 1);
+    cc = c->cap_cells;
+    if (e == cudaSuccess) e = ensure(c->b.cell_count, cc, (size_t)n_cells + 1);
+    size_t nb = c->s.cap_blocks;
+    if (e == cudaSuccess) e = ensure(c->s.block_sums, nb, (size_t)(n_cells / 1024 + 2));
+    if (e != cudaSuccess) return cuda_fail(c, e, "allocating cell buffers");
+    c->cap_cells = cc;
+    c->s.cap_blocks = nb;
+    if (!c->s.counters) {
+      e = cudaMalloc((void**)&c->s.counters, 8 * sizeof(unsigned long long));
+      if (e != cudaSuccess) return cuda_fail(c, e, "allocating counters");
+    }
+    size_t cx = c->s.cap_x;
+    e = ensure(c->s.xtab, cx, (size_t)Mx);
+    cx = c->s.cap_x;
+    if (e == cudaSuccess) e = ensure(c->s.xfv, cx, (size_t)Mx);
+    size_t cy = c->s.cap_y;
+    if (e == cudaSuccess) e = ensure(c->s.ytab, cy, (size_t)My);
+    cy = c->s.cap_y;
+    if (e == cudaSuccess) e = ensure(c->s.yfv, cy, (size_t)My);
+    size_t cz = c->s.cap_z;
+    if (e == cudaSuccess) e = ensure(c->s.ztab, cz, (size_t)Mz);
+    cz = c->s.cap_z;
+    if (e == cudaSuccess) e = ensure(c->s.zfv, cz, (size_t)Mz);
+    size_t cp = c->s.cap_prec;
+    if (e == cudaSuccess) e = ensure(c->s.aa, cp, (size_t)nPrec);
+    cp = c->s.cap_prec;
+    if (e == cudaSuccess) e = ensure(c->s.aaf, cp, (size_t)nPrec);
+    if (e != cudaSuccess) return cuda_fail(c, e, "allocating tables");
+    c->s.cap_x = cx;
+    c->s.cap_y = cy;
+    c->s.cap_z = cz;
+    c->s.cap_prec = cp;
+  }
+
+  // ---- per-image tables, staged through pinned memory
+  const size_t stage_bytes = (size_t)(Mx + My + Mz) * (sizeof(int2) + sizeof(double)) + nPrec * 12 + 64;
+  e = ensure_host(c->h_stage, c->cap_stage, stage_bytes);
+  if (e != cudaSuccess) return cuda_fail(c, e, "allocating pinned staging");
+  cudaStreamSynchronize(st);  // the staging buffer may still feed a previous call's copies
+  unsigned char* hp = (unsigned char*)c->h_stage;
+  int2* hxt = (int2*)hp;
+  int2* hyt = hxt + Mx;
+  int2* hzt = hyt + My;
+  double* hxf = (double*)(hzt + Mz);
+  double* hyf = hxf + Mx;
+  double* hzf = hyf + My;
+  double* haa = hzf + Mz;
+  float* haaf = (float*)(haa + nPrec);
+  axis_table(Mx, g->a_vox[0], g->lc_delta[0], g->ia_col[0], g->Ex, hxt, hxf);
+  axis_table(My, g->a_vox[4], g->lc_delta[1], g->ia_col[4], g->Ey, hyt, hyf);
+  axis_table(Mz, g->a_vox[8], g->lc_delta[2], g->ia_col[8], g->Ez, hzt, hzf);
+  for (int k = 0; k < nPrec; ++k) {
+    haa[k] = aa[k];
+    haaf[k] = (float)aa[k];
+  }
+  cudaMemcpyAsync(c->s.xtab, hxt, Mx * sizeof(int2), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(c->s.ytab, hyt, My * sizeof(int2), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(c->s.ztab, hzt, Mz * sizeof(int2), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(c->s.xfv, hxf, Mx * sizeof(double), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(c->s.yfv, hyf, My * sizeof(double), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(c->s.zfv, hzf, Mz * sizeof(double), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(c->s.aa, haa, nPrec * sizeof(double), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(c->s.aaf, haaf, nPrec * sizeof(float), cudaMemcpyHostToDevice, st);
+
+  // ---- K1: binning
+  const size_t n_cand = (size_t)g->nuvw * (size_t)nAtoms;
+  BinParams bp;
+  memset(&bp, 0, sizeof bp);
+  bp.n_atoms = nAtoms;
+  bp.ldx = ldx;
+  bp.nuvw = g->nuvw;
+  bp.Ex = g->Ex;
+  bp.Ey = g->Ey;
+  bp.Ez = g->Ez;
+  bp.n_cells = n_cells;
+  memcpy(bp.RU, g->RU, sizeof bp.RU);
+  memcpy(bp.delta, g->delta, sizeof bp.delta);
+  memcpy(bp.Ruvw, g->Ruvw, sizeof bp.Ruvw);
+  memcpy(bp.lc_delta, g->lc_delta, sizeof bp.lc_delta);
+  memcpy(bp.ia, g->ia_col, sizeof bp.ia);
+  memcpy(bp.g, g->g, sizeof bp.g);
+  bp.a_col[0] = g->a_col[0];
+  bp.a_col[1] = g->a_col[4];
+  bp.a_col[2] = g->a_col[8];
+  for (int i = 0; i < 9; ++i) bp.RUf[i] = (float)g->RU[i];
+  for (int i = 0; i < 81; ++i) bp.Ruvwf[i] = (float)g->Ruvw[i];
+  for (int i = 0; i < 3; ++i) bp.shiftf[i] = (float)(g->delta[i] - g->lc_delta[i]);
+  bp.iaf[0] = (float)g->ia_col[0];
+  bp.iaf[1] = (float)g->ia_col[4];
+  bp.iaf[2] = (float)g->ia_col[8];
+
+  // kept-atom capacity: what the previous image kept, else 4 atoms per input atom
+  int64_t cap = c->last_kept > 0 ? c->last_kept + c->last_kept / 4 + 65536 : 4 * nAtoms + 65536;
+  if (cap > (int64_t)n_cand + 1) cap = (int64_t)n_cand + 1;
+  for (int attempt = 0;; ++attempt) {
+  if (!alloc_kept(c, (size_t)cap)) return cuda_fail(c, cudaErrorMemoryAllocation, "allocating binning buffers");
+  bp.cap = cap;
+  cudaEventRecord(c->ev[0], st);
+  e = launch_bin(bp, d_x, c->s, c->b, st);
+  if (e == cudaSuccess) e = launch_bin_finalize(bp, c->s, c->b, fp32 ? 0 : 1, st);
+  if (e != cudaSuccess) return cuda_fail(c, e, "binning launch");
+
+  // ---- K2+K3: field and columns
+  e = cudaMemsetAsync(d_img, 0, sizeof(double) * (size_t)Mx * My, st);
+  if (e != cudaSuccess) return cuda_fail(c, e, "clearing image");
+  cudaEventRecord(c->ev[1], st);
+  ColumnParams cp;
+  memset(&cp, 0, sizeof cp);
+  cp.Mx = Mx;
+  cp.My = My;
+  cp.Mz = Mz;
+  cp.ix0 = g->ix0;
+  cp.ix1 = g->ix1;
+  cp.iy0 = g->iy0;
+  cp.iy1 = g->iy1;
+  cp.Ex = g->Ex;
+  cp.Ey = g->Ey;
+  cp.Ez = g->Ez;
+  cp.n_prec = nPrec;
+  cp.use_density = g->useDensity;
+  cp.want_stats = (flags & ST_FLAG_STATS) ? 1 : 0;
+  cp.a11 = g->a_col[0];
+  cp.a22 = g->a_col[4];
+  cp.a33 = g->a_col[8];
+  cp.cut2 = (3 * g->sigma) * (3 * g->sigma);
+  cp.i2s2 = 1 / (2 * g->sigma * g->sigma);
+  cp.sigma = g->sigma;
+  cp.b0 = g->b0;
+  cp.bg = g->bg;
+  cp.dz = g->deltaz;
+  // link cells narrower than 3 sigma truncate the search to 27 cells: test the cell offsets too
+  const double r3 = 3 * g->sigma * (1.0 + 1e-6) + 1e-6;
+  cp.check_cells = (cp.a11 < r3 || cp.a22 < r3 || cp.a33 < r3) ? 1 : 0;
+  cp.cell_start = c->b.cell_start;
+  cp.f64 = c->b.f64;
+  cp.cs64 = c->b.cs64;
+  cp.p32 = c->b.p32;
+  cp.cs32 = c->b.cs32;
+  cp.xtab = c->s.xtab;
+  cp.xfv = c->s.xfv;
+  cp.ytab = c->s.ytab;
+  cp.yfv = c->s.yfv;
+  cp.ztab = c->s.ztab;
+  cp.zfv = c->s.zfv;
+  cp.aa = c->s.aa;
+  cp.aaf = c->s.aaf;
+  cp.img = d_img;
+  cp.counters = c->s.counters;
+  cp.cap = cap;
+  if (g->ix1 > g->ix0 && g->iy1 > g->iy0) {
+    const int width = fp32 ? 16 : 4;
+    for (int off = 0; off < nPrec; off += width) {
+      cp.prec_offset = off;
+      cp.accumulate = off > 0 ? 1 : 0;
+      e = fp32 ? launch_column_fp32(cp, st) : launch_column_fp64(cp, st);
+      if (e != cudaSuccess) return cuda_fail(c, e, "column kernel launch");
+    }
+    if (flags & ST_FLAG_AVERAGE) {
+      e = launch_epilogue(d_img, Mx, My, g->ix0, g->ix1, g->iy0, g->iy1, (double)nPrec,
+                          (flags & ST_FLAG_BRIGHT) ? 1 : 0, st);
+      if (e != cudaSuccess) return cuda_fail(c, e, "epilogue launch");
+    }
+  }
+  cudaEventRecord(c->ev[2], st);
+  e = cudaMemcpyAsync(c->h_counters, c->s.counters, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(c, e, "image kernels");
+  if ((int64_t)c->h_counters[0] <= cap) break;
+  if (attempt > 0) return fail(c, ST_ERR_ALLOC, "binning capacity did not converge");
+  cap = (int64_t)c->h_counters[0] + (int64_t)c->h_counters[0] / 8 + 1024;  // grow and redo the image
+  }
+  c->last_kept = (int64_t)c->h_counters[0];
+
+  st_stats& S = c->stats;
+  memset(&S, 0, sizeof S);
+  S.n_atoms = nAtoms;
+  S.n_kept = (int64_t)c->h_counters[0];
+  S.max_cell_count = (int32_t)c->h_counters[1];
+  S.n_tests = (int64_t)c->h_counters[2];
+  S.n_accepted = (int64_t)c->h_counters[3];
+  S.n_voxels = (int64_t)(g->ix1 - g->ix0) * (g->iy1 - g->iy0) * Mz;
+  S.n_prec = nPrec;
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]);
+  S.ms_bin = ms;
+  cudaEventElapsedTime(&ms, c->ev[1], c->ev[2]);
+  S.ms_column = ms;
+  if (g->nMax0 > 0 && S.max_cell_count > 16 * g->nMax0) {
+    char buf[256];
+    snprintf(buf, sizeof buf,
+             "a link cell holds %d atoms, more than 16 x nMax0 = %d (the reference stops in "
+             "Lib_LinkCell3d::add0 here)",
+             S.max_cell_count, 16 * g->nMax0);
+    return fail(c, ST_ERR_CAPACITY, buf);
+  }
+  return ST_OK;
+}
+
+extern "C" int st_image(st_ctx* c, const st_geom* g, const double* x, int64_t ldx, int64_t nAtoms, const double* aa,
+                        int32_t nPrec, int32_t flags, double* img) {
+  if (!c) return ST_ERR_ARG;
+  int rc = validate(c, g, ldx, nAtoms, nPrec);
+  if (rc != ST_OK) return rc;
+  if (!img || !aa || (nAtoms > 0 && !x)) return fail(c, ST_ERR_ARG, "null buffer");
+  cudaSetDevice(c->device);
+  cudaError_t e = ensure(c->d_x, c->cap_x, (size_t)3 * (nAtoms > 0 ? nAtoms : 1));
+  if (e == cudaSuccess) e = ensure(c->d_img, c->cap_img, (size_t)g->Mx * g->My);
+  if (e != cudaSuccess) return cuda_fail(c, e, "allocating image buffers");
+  if (nAtoms > 0) {
+    // x(1:3, :) of a Fortran (ldx, nAtoms) array, packed to (3, nAtoms)
+    if (ldx == 3)
+      e = cudaMemcpyAsync(c->d_x, x, sizeof(double) * 3 * (size_t)nAtoms, cudaMemcpyHostToDevice, c->stream);
+    else
+      e = cudaMemcpy2DAsync(c->d_x, 3 * sizeof(double), x, (size_t)ldx * sizeof(double), 3 * sizeof(double),
+                            (size_t)nAtoms, cudaMemcpyHostToDevice, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "copying atoms");
+  }
+  rc = st_image_device(c, g, c->d_x, 3, nAtoms, aa, nPrec, flags, c->d_img, c->stream);
+  if (rc != ST_OK) return rc;
+  e = cudaMemcpyAsync(img, c->d_img, sizeof(double) * (size_t)g->Mx * g->My, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "copying image");
+  return ST_OK;
+}
+
+namespace {
+
+// kernel(0:Nk) of gaussianBlurImage: Nk = max(5, ceiling(5 t)), exp(-k^2 / (2 t^2)).
+int blur_kernel(double t, std::vector<double>& k) {
+  int nk = (int)std::ceil(t * 5);
+  if (nk < 5) nk = 5;
+  k.assign(nk + 1, 0.0);
+  const double i2s2 = 1 / (2 * t * t);
+  k[0] = 1.0;
+  for (int i = 1; i <= nk; ++i) k[i] = std::exp(-(i * i * i2s2));
+  return nk;
+}
+
+}  // namespace
+
+extern "C" int st_blur_device(st_ctx* c, const double* d_in, int32_t nx, int32_t ny, double t, double* d_out,
+                              void* stream) {
+  if (!c) return ST_ERR_ARG;
+  if (!d_in || !d_out || nx < 1 || ny < 1) return fail(c, ST_ERR_ARG, "invalid blur arguments");
+  if (!(t > 0.0) || !(t < 1e6)) return fail(c, ST_ERR_ARG, "blur width t must be in (0, 1e6) pixels");
+  cudaSetDevice(c->device);
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+  std::vector<double> k;
+  const int nk = blur_kernel(t, k);
+  const size_t n = (size_t)nx * ny;
+  cudaError_t e = ensure(c->d_blur, c->cap_blur, 3 * n + nx);
+  if (e == cudaSuccess) e = ensure(c->d_kern, c->cap_kern, (size_t)nk + 1);
+  if (e != cudaSuccess) return cuda_fail(c, e, "allocating blur buffers");
+  e = cudaMemcpyAsync(c->d_kern, k.data(), (nk + 1) * sizeof(double), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = launch_blur(d_in, c->d_blur + n, d_out, nx, ny, c->d_kern, nk, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(c, e, "blur");
+  return ST_OK;
+}
+
+extern "C" int st_blur(st_ctx* c, const double* in, int32_t nx, int32_t ny, double t, double* out) {
+  if (!c) return ST_ERR_ARG;
+  if (!in || !out || nx < 1 || ny < 1) return fail(c, ST_ERR_ARG, "invalid blur arguments");
+  cudaSetDevice(c->device);
+  const size_t n = (size_t)nx * ny;
+  cudaError_t e = ensure(c->d_blur, c->cap_blur, 3 * n + nx);
+  if (e != cudaSuccess) return cuda_fail(c, e, "allocating blur buffers");
+  e = cudaMemcpyAsync(c->d_blur, in, n * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "copying blur input");
+  // input at d_blur[0, n), scratch at [n, 2n + nx), output at [2n + nx, 3n + nx)
+  double* d_out = c->d_blur + 2 * n + nx;
+  int rc = st_blur_device(c, c->d_blur, nx, ny, t, d_out, c->stream);
+  if (rc != ST_OK) return rc;
+  e = cudaMemcpyAsync(out, d_out, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "copying blur output");
+  return ST_OK;
+}

@@ -1,0 +1,249 @@
+"""Python API over libstem, shaped like the reference's Fortran interfaces.
+
+* ``DynamicalTwoBeamImaging`` mirrors ``type(DynamicalTwoBeamImaging)`` and its
+  public procedures (src/Lib_DynamicalTwoBeamImaging.f90:31-48); its
+  ``compute_d2bi_img`` runs ``computeD2BI_img`` on the GPU.
+* ``Context`` owns the device buffers (``st_ctx``) and exposes the image and
+  blur entry points of include/stem.h.
+* ``d2bi_condition`` follows src/d2bi.f90 for one diffraction condition: the
+  periodic wrap of the input atoms, the image box from the atom extents, the
+  tilt (``-sg``, ``-R``/``-U`` or the default s_g = 0) and the tomography tilt.
+
+Arrays follow the reference's layouts: positions are an (N, 3) C-contiguous
+array (the Fortran (3, N) array in memory), images are (Mx, My) arrays in
+Fortran order (the reference's column-major d2big2).
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import StGeom, StStats, check, lib
+
+_d = ctypes.c_double
+_dp = ctypes.POINTER(ctypes.c_double)
+
+
+def _cm(m):
+    """3x3 matrix -> column-major ctypes double[9]."""
+    a = np.asarray(m, dtype=np.float64).reshape(3, 3).ravel(order="F")
+    return (_d * 9)(*a)
+
+
+def _v3(v):
+    return (_d * 3)(*[float(t) for t in v])
+
+
+def _from_cm(arr):
+    return np.array(list(arr), dtype=np.float64).reshape(3, 3, order="F")
+
+
+def _ptr(a):
+    return a.ctypes.data_as(_dp)
+
+
+class Context:
+    """A libstem context on one CUDA device (st_create / st_destroy)."""
+
+    def __init__(self, device=0):
+        h = ctypes.c_void_p()
+        check(lib().st_create(ctypes.byref(h), device))
+        self.handle = h
+        self.device = device
+
+    def close(self):
+        if self.handle:
+            lib().st_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, code):
+        check(code, self.handle)
+
+    def image(self, geom, x, aa, flags=0):
+        """st_image from host memory: x (N, 3) or (N, ldx) float64; returns the (Mx, My) image (Fortran order)."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        n, ldx = (x.shape[0], x.shape[1]) if x.ndim == 2 else (0, 3)
+        aa = np.ascontiguousarray(np.atleast_1d(aa), dtype=np.float64)
+        img = np.zeros((geom.Mx, geom.My), order="F")
+        self._check(lib().st_image(self.handle, ctypes.byref(geom), _ptr(x), ldx, n, _ptr(aa), len(aa), flags,
+                                   _ptr(img)))
+        return img
+
+    def image_device(self, geom, x_dev_ptr, n_atoms, aa, flags, img_dev_ptr, stream=0, ldx=3):
+        """st_image_device on device pointers (ints, e.g. torch tensor.data_ptr())."""
+        aa = np.ascontiguousarray(np.atleast_1d(aa), dtype=np.float64)
+        self._check(lib().st_image_device(self.handle, ctypes.byref(geom), ctypes.c_void_p(x_dev_ptr), ldx, n_atoms,
+                                          _ptr(aa), len(aa), flags, ctypes.c_void_p(img_dev_ptr),
+                                          ctypes.c_void_p(stream)))
+
+    def blur(self, img, t):
+        """st_blur: gaussianBlurImage of an (Nx, Ny) image with width t pixels."""
+        img = np.asfortranarray(img, dtype=np.float64)
+        out = np.zeros_like(img, order="F")
+        self._check(lib().st_blur(self.handle, _ptr(img), img.shape[0], img.shape[1], float(t), _ptr(out)))
+        return out
+
+    def blur_device(self, in_ptr, nx, ny, t, out_ptr, stream=0):
+        self._check(lib().st_blur_device(self.handle, ctypes.c_void_p(in_ptr), nx, ny, float(t),
+                                         ctypes.c_void_p(out_ptr), ctypes.c_void_p(stream)))
+
+    def stats(self):
+        s = StStats()
+        self._check(lib().st_get_stats(self.handle, ctypes.byref(s)))
+        return s
+
+
+class DynamicalTwoBeamImaging:
+    """type(DynamicalTwoBeamImaging) with the reference's procedures (host mirror in libstem)."""
+
+    def __init__(self, a_vox, n_vox, a0, k, g, E, mxy, mzz):
+        """DynamicalTwoBeamImaging_ctor0(super, latt, a0, k, g, E, mxy, mzz); super = (a_vox, Nx, Ny, Nz)."""
+        h = ctypes.c_void_p()
+        check(lib().st_d2bi_create(ctypes.byref(h), _cm(a_vox), int(n_vox[0]), int(n_vox[1]), int(n_vox[2]),
+                                   float(a0), _v3(k), _v3(g), float(E), int(mxy), int(mzz)))
+        self.handle = h
+        self.a0 = float(a0)
+
+    def __del__(self):
+        try:
+            if self.handle:
+                lib().st_d2bi_destroy(self.handle)
+                self.handle = None
+        except Exception:
+            pass
+
+    def set_conventional_unit_cell(self, a_cell):
+        check(lib().st_d2bi_set_conventional_unit_cell(self.handle, _cm(a_cell)))
+
+    def set_voxel_supercell_size(self, d):
+        check(lib().st_d2bi_set_voxel_supercell_size(self.handle, _v3(d)))
+
+    def set_deviation_parameter(self, sg):
+        check(lib().st_d2bi_set_deviation_parameter(self.handle, float(sg)))
+
+    def set_supercell_tilt(self, U=None, R=None):
+        """setSupercellTilt0 (no arguments) or setSupercellTilt2(U, R)."""
+        if R is None:
+            check(lib().st_d2bi_set_supercell_tilt0(self.handle))
+        else:
+            check(lib().st_d2bi_set_supercell_tilt2(self.handle, _cm(np.eye(3) if U is None else U), _cm(R)))
+
+    def set_extinction_distances(self, xi0, xig):
+        check(lib().st_d2bi_set_extinction_distances(self.handle, float(xi0), float(xig)))
+
+    def set_use_density_field(self, use):
+        check(lib().st_d2bi_set_use_density_field(self.handle, int(bool(use))))
+
+    def find_image_parameters(self):
+        """(aperpx, xmax[3], modg, Mx, My, Mz)."""
+        ap, mg = _d(), _d()
+        xm = (_d * 3)()
+        mx, my, mz = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        check(lib().st_d2bi_find_image_parameters(self.handle, ctypes.byref(ap), xm, ctypes.byref(mg),
+                                                  ctypes.byref(mx), ctypes.byref(my), ctypes.byref(mz)))
+        return ap.value, list(xm), mg.value, mx.value, my.value, mz.value
+
+    def get_rotation(self):
+        U, R = (_d * 9)(), (_d * 9)()
+        check(lib().st_d2bi_get_rotation(self.handle, U, R))
+        return _from_cm(U), _from_cm(R)
+
+    def get_deviation_parameter(self):
+        return lib().st_d2bi_get_deviation_parameter(self.handle)
+
+    def image_geometry(self, n_atoms, prec_angle=0.005, n_prec=1, nprocs=1, jj=0):
+        """The computeD2BI_img prologue: (st_geom, aa[n_prec]) for patch jj of nprocs."""
+        G = StGeom()
+        aa = np.zeros(n_prec)
+        check(lib().st_d2bi_image_geometry(self.handle, int(n_atoms), int(nprocs), int(jj), float(prec_angle),
+                                           int(n_prec), ctypes.byref(G), _ptr(aa)))
+        return G, aa
+
+    def compute_d2bi_img(self, ctx, x, prec_angle=0.005, n_prec=1, flags=0):
+        """computeD2BI_img on one process: the precession-averaged dark-field image (Mx, My)."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        _, _, _, Mx, My, _ = self.find_image_parameters()
+        img = np.zeros((Mx, My), order="F")
+        check(lib().st_d2bi_compute_img(self.handle, ctx.handle, _ptr(x), x.shape[1], x.shape[0], float(prec_angle),
+                                        int(n_prec), int(flags), _ptr(img)), ctx.handle)
+        return img
+
+
+def wrap_pbc(a_super, M, a0, x):
+    """d2bi's periodic wrap of the input atoms on the voxel supercell (src/d2bi.f90:856-866); returns a copy."""
+    a_super = np.asarray(a_super, dtype=np.float64)
+    n = [max(3, int(np.floor(M[0] * _norm2(a_super[:, 0]) / a0))),
+         max(3, int(np.floor(M[0] * _norm2(a_super[:, 1]) / a0))),
+         max(3, int(np.floor(M[1] * _norm2(a_super[:, 2]) / a0)))]
+    a_vox = np.stack([a_super[:, i] / n[i] for i in range(3)], axis=1)
+    x = np.ascontiguousarray(x, dtype=np.float64).copy()
+    check(lib().st_wrap_pbc(_cm(a_vox), n[0], n[1], n[2], _ptr(x), x.shape[1], x.shape[0]))
+    return x, a_vox, n
+
+
+def _norm2(v):
+    """gfortran NORM2 (scaled sum of squares) of a 3-vector."""
+    scale, res = 0.0, 1.0
+    for t in v:
+        t = float(t)
+        if t != 0.0:
+            ax = abs(t)
+            if scale < ax:
+                val = scale / ax
+                res = 1.0 + res * val * val
+                scale = ax
+            else:
+                val = ax / scale
+                res += val * val
+    return float(np.sqrt(res)) * scale
+
+
+def atom_extents(k, g, a_cell, x):
+    d = (_d * 3)()
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    check(lib().st_atom_extents(_v3(k), _v3(g), _cm(a_cell), _ptr(x), x.shape[1], x.shape[0], d))
+    return list(d)
+
+
+def tomography_tilt(tomo_angle, nn, n_tomo, R0):
+    R = (_d * 9)()
+    check(lib().st_tomography_tilt(float(tomo_angle), int(nn), int(n_tomo), _cm(R0), R))
+    return _from_cm(R)
+
+
+def d2bi_condition(a_super, a0, k, g, x, V=200.0, M=(4, 4), sg=None, R=None, U=None, d=None, xi0=103.889565,
+                   xig=207.533203, density=False, n_tomo=1, tomo_angle=20.0, tomo_step=0):
+    """One diffraction condition of the d2bi program (src/d2bi.f90:782-991, 1145-1381).
+
+    Returns (imaging, wrapped positions (N, 3), aperpx).  ``a0`` is the cubic
+    lattice constant (``-a0``); a bcc/fcc/sc conventional cell a0 * I is used.
+    """
+    a0 = (a0 + a0 + a0) / 3  # a0 = (a0in(1) + a0in(2) + a0in(3)) / 3 (:787-788)
+    xw, a_vox, n = wrap_pbc(a_super, M, a0, x)
+    a_cell = a0 * np.eye(3)
+    if d is None:
+        d = atom_extents(k, g, a_cell, xw)
+    t = DynamicalTwoBeamImaging(a_vox, n, a0, k, g, V, M[0], M[1])
+    t.set_conventional_unit_cell(a_cell)
+    t.set_voxel_supercell_size(d)
+    if sg is not None:
+        t.set_deviation_parameter(sg)
+        t.set_supercell_tilt()
+    elif R is not None:
+        t.set_supercell_tilt(np.eye(3) if U is None else U, R)
+    else:
+        t.set_deviation_parameter(0.0)
+        t.set_supercell_tilt()
+    U0, R0 = t.get_rotation()
+    t.set_extinction_distances(xi0, xig)
+    aperpx = t.find_image_parameters()[0]
+    t.set_use_density_field(density)
+    if n_tomo > 1:
+        t.set_supercell_tilt(U0, tomography_tilt(tomo_angle, tomo_step, n_tomo, R0))
+    return t, xw, aperpx

@@ -1,0 +1,191 @@
+"""Parity of the CUDA path (through the C ABI) with the oracle.
+
+Bars: FP64 path max |dI| <= 1e-12 against the oracle (same accept set, same
+summation order; only exp/sin/cos/hypot may differ in the last ulp); FP32
+path max |dI| <= 1e-4 (the precision target of the FP32 + FP64-phase path);
+binning counts and accepted-pair counts identical; the blur identical to the
+last bit.
+"""
+import numpy as np
+import pytest
+
+from oracle import stem_oracle as O
+from simulated_tem_gb300 import _lib, imaging, synth
+from tests import golden_data
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-12
+FP32_TOL = 1e-4
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = imaging.Context(0)
+    yield c
+    c.close()
+
+
+def setup_both(cell, a0=synth.A0_FE, k=(0, 0, 1), g=(1, 1, 0), **kw):
+    m = dict(kw)
+    t, xw, _ = imaging.d2bi_condition(cell.a_super, a0, k, g, cell.pos, **m)
+    ok = {"sg": "sg", "R": "R", "U": "U", "d": "d", "xi0": "xi0", "xig": "xig", "density": "density"}
+    args = O.make_args(cell.a_super, a0, k, g, **{ok[kk]: v for kk, v in kw.items() if kk in ok})
+    so, xo, _ = O.setup(args, cell.pos)
+    assert np.array_equal(xw, xo)
+    return t, so, xw
+
+
+def oracle_patch(so, x, n_prec, prec_angle, nprocs=1, jj=0):
+    G, aa = O.geometry(so, len(x), nPrec=n_prec, precAngle=prec_angle, nProcs=nprocs, jj=jj)
+    img, st = O.patch_image(G, aa, x, nthreads=8)
+    return img, st
+
+
+CELLS = {
+    "screw+void": dict(n=(10, 10, 8), seed=5, n_voids=1, radius=(4.0, 6.0), with_screw=True),
+    "voids": dict(n=(9, 11, 7), seed=6, n_voids=3, radius=(3.0, 5.0), with_screw=False),
+}
+
+
+@pytest.mark.parametrize("cell_name", sorted(CELLS))
+@pytest.mark.parametrize("density", [False, True])
+@pytest.mark.parametrize("sg", [0.0, 0.01])
+def test_fp64_matches_oracle(ctx, cell_name, density, sg):
+    cell = synth.small_cell(**CELLS[cell_name])
+    t, so, x = setup_both(cell, sg=sg, density=density)
+    G, aa = t.image_geometry(len(x))
+    got = ctx.image(G, x, aa, flags=_lib.ST_FLAG_STATS)
+    st = ctx.stats()
+    want, ost = oracle_patch(so, x, 1, 0.005)
+    assert np.abs(got - want).max() <= FP64_TOL
+    assert st.n_kept == ost.n_kept
+    assert st.n_accepted == ost.n_accepted
+    assert st.max_cell_count == ost.max_cell_count
+
+
+@pytest.mark.parametrize("cell_name", sorted(CELLS))
+@pytest.mark.parametrize("density", [False, True])
+def test_fp32_matches_oracle(ctx, cell_name, density):
+    cell = synth.small_cell(**CELLS[cell_name])
+    t, so, x = setup_both(cell, sg=0.01, density=density)
+    G, aa = t.image_geometry(len(x))
+    got = ctx.image(G, x, aa, flags=_lib.ST_FLAG_FP32)
+    want, _ = oracle_patch(so, x, 1, 0.005)
+    d = got - want
+    assert np.abs(d).max() <= FP32_TOL
+    assert np.sqrt((d ** 2).mean()) <= FP32_TOL / 5
+
+
+@pytest.mark.parametrize("n_prec,fp32", [(3, False), (6, False), (5, True), (17, True)])
+def test_precession_passes(ctx, n_prec, fp32):
+    """Precession: one phase field, n_prec integrations (the FP64 kernel runs 4 per
+    pass, the FP32 kernel 16 per pass), averaged (ST_FLAG_AVERAGE)."""
+    cell = synth.small_cell(**CELLS["screw+void"])
+    t, so, x = setup_both(cell, sg=0.01, density=True)
+    G, aa = t.image_geometry(len(x), prec_angle=0.005, n_prec=n_prec)
+    flags = _lib.ST_FLAG_AVERAGE | (_lib.ST_FLAG_FP32 if fp32 else 0)
+    got = ctx.image(G, x, aa, flags=flags)
+    want, _ = oracle_patch(so, x, n_prec, 0.005)
+    want = want / n_prec
+    assert np.abs(got - want).max() <= (FP32_TOL if fp32 else FP64_TOL)
+    # tilts around the cone: s_g(phi) = s_g(2 pi - phi), so the angles come in equal pairs
+    assert len(set(np.round(aa, 12))) >= (n_prec + 1) // 2
+
+
+def test_bright_field_and_average(ctx):
+    cell = synth.small_cell(**CELLS["voids"])
+    t, so, x = setup_both(cell, sg=0.0)
+    G, aa = t.image_geometry(len(x), n_prec=2)
+    raw = ctx.image(G, x, aa)
+    bf = ctx.image(G, x, aa, flags=_lib.ST_FLAG_AVERAGE | _lib.ST_FLAG_BRIGHT)
+    assert np.array_equal(bf, 1.0 - raw / 2)
+
+
+@pytest.mark.parametrize("nprocs", [2, 3, 4])
+def test_patches_match_oracle(ctx, nprocs):
+    """The reference's MPI patch split: each process images its patch; the sum of the
+    zero-padded patch images is the image (MPI_Reduce SUM)."""
+    cell = synth.small_cell(**CELLS["screw+void"])
+    t, so, x = setup_both(cell, sg=0.01, density=True)
+    total = None
+    for jj in range(nprocs):
+        G, aa = t.image_geometry(len(x), nprocs=nprocs, jj=jj)
+        got = ctx.image(G, x, aa)
+        want, _ = oracle_patch(so, x, 1, 0.005, nprocs=nprocs, jj=jj)
+        assert np.abs(got - want).max() <= FP64_TOL
+        outside = np.ones_like(got, dtype=bool)
+        outside[G.ix0:G.ix1, G.iy0:G.iy1] = False
+        assert not got[outside].any()
+        total = got if total is None else total + got
+    G1, aa1 = t.image_geometry(len(x))
+    full = ctx.image(G1, x, aa1)
+    # different patches shift the link-cell origin: equal to rounding, not to the bit
+    assert np.abs(total - full).max() < 1e-9
+
+
+def test_w_loop_golden_on_gpu(ctx):
+    g = golden_data.w_loop()
+    cell = synth.Cell(g["a_super"], g["pos"])
+    t, so, x = setup_both(cell, a0=3.1652, g=(2, 0, 0), R=g["RU"], U=np.eye(3), d=g["d"], xi0=g["xi0"],
+                          xig=g["xig"])
+    img64 = t.compute_d2bi_img(ctx, x)
+    img32 = t.compute_d2bi_img(ctx, x, flags=_lib.ST_FLAG_FP32)
+    want, _ = oracle_patch(so, x, 1, 0.005)
+    assert np.abs(img64 - want).max() <= FP64_TOL
+    assert np.abs(img32 - want).max() <= FP32_TOL
+    assert np.abs(img64 - g["img"]).max() < 2e-4
+
+
+def test_blur_matches_oracle(ctx):
+    g = golden_data.w_loop()
+    for t in (3.1446, 0.7, 12.0):
+        got = ctx.blur(g["img"], t)
+        want = O.gaussian_blur(g["img"], t)
+        assert np.array_equal(got, want)
+    rect = np.random.default_rng(1).random((37, 53))
+    assert np.array_equal(ctx.blur(rect, 2.2), O.gaussian_blur(rect, 2.2))
+
+
+def test_empty_input(ctx):
+    """No atoms: every voxel is void (x = 0), so no diffracted intensity."""
+    cell = synth.small_cell(**CELLS["voids"])
+    t, so, x = setup_both(cell, sg=0.01, density=True)
+    G, aa = t.image_geometry(0)
+    got = ctx.image(G, np.zeros((0, 3)), aa)
+    want, _ = oracle_patch(so, np.zeros((0, 3)), 1, 0.005)
+    assert np.array_equal(got, want)
+    assert not got.any()
+
+
+def test_ldx_fourteen(ctx):
+    """d2bi passes x(1:14, nAtoms) when the input had fewer than 14 columns."""
+    cell = synth.small_cell(**CELLS["voids"])
+    t, so, x = setup_both(cell, sg=0.01)
+    x14 = np.zeros((len(x), 14))
+    x14[:, :3] = x
+    x14[:, 3:] = 7.0
+    G, aa = t.image_geometry(len(x))
+    assert np.array_equal(ctx.image(G, x14, aa), ctx.image(G, x, aa))
+
+
+def test_errors_are_reported(ctx):
+    cell = synth.small_cell(**CELLS["voids"])
+    t, so, x = setup_both(cell, sg=0.01)
+    G, aa = t.image_geometry(len(x))
+    with pytest.raises(_lib.StemError) as e:
+        ctx.image(G, x, np.zeros(0))
+    assert e.value.code == _lib.ST_ERR_ARG
+    G2, _ = t.image_geometry(len(x))
+    G2.a_vox[1] = 1e-3  # not a cuboid voxel
+    with pytest.raises(_lib.StemError) as e:
+        ctx.image(G2, x, aa)
+    assert e.value.code == _lib.ST_ERR_ARG and "cuboid" in str(e.value)
+    G3, _ = t.image_geometry(len(x))
+    G3.nMax0 = 1  # the reference stops once a cell needs more than 16 x nMax0 slots
+    dense = np.concatenate([x] * 20)
+    with pytest.raises(_lib.StemError) as e:
+        ctx.image(G3, dense, aa)
+    assert e.value.code == _lib.ST_ERR_CAPACITY
+    # the context stays usable
+    assert np.isfinite(ctx.image(G, x, aa)).all()
