@@ -118,6 +118,35 @@ int st_blur_device(st_ctx* ctx, const double* d_in, int32_t nx, int32_t ny, doub
 /* Counters and kernel times of the last st_image / st_image_device call. */
 int st_get_stats(const st_ctx* ctx, st_stats* out);
 
+/* Limits of st_blur_noalloc's fixed scratch (16.8 MB of device memory). */
+#define ST_BLUR_NOALLOC_MAX_PIXELS (1 << 21) /* nx * ny <= 2,097,152 */
+#define ST_BLUR_NOALLOC_MAX_NX 4096          /* nx <= 4096 */
+#define ST_BLUR_NOALLOC_MAX_NK 1023          /* ceiling(5 t) <= 1023, i.e. t <= 204.6 pixels */
+
+/* The blur of st_blur_device for callers that cannot let a library allocate
+ * GPU memory: a Fortran host under an MPI or batch runtime that owns the
+ * device memory pool, code imaging inside a fixed memory budget, or a caller
+ * that must not allocate between steps it later replays.  No counterpart in
+ * the reference (its blur runs on the CPU).
+ *
+ * d_in and d_out are caller-owned device buffers of nx * ny doubles
+ * (column-major); the output equals st_blur's bit for bit.  Nothing is
+ * allocated: no cudaMalloc, no cudaFree, no allocating library call.  The one
+ * intermediate (the x-pass image and its column weights) lives in a fixed
+ * file-scope device array that every GPU loading the library holds until the
+ * process exits; larger images than the limits above return ST_ERR_ARG with
+ * the reason in err.  The first call on each device looks that array's device
+ * address up (cudaGetSymbolAddress, which may load the library's GPU module):
+ * make that first call outside any stream capture.  Calls share the array and
+ * it keeps the last call's contents; every entry is rewritten before it is
+ * read, but calls whose work overlaps on the GPU (concurrent streams, or
+ * threads on one device without ordering) race on it.  The kernels are
+ * enqueued on `stream` (a cudaStream_t, 0 for the legacy default stream) and
+ * the call returns without waiting.  err (optional, err_len bytes) receives a
+ * message on failure. */
+int st_blur_noalloc(const double* d_in, int32_t nx, int32_t ny, double t, double* d_out, void* stream, char* err,
+                    int32_t err_len);
+
 #ifdef __cplusplus
 }
 #endif

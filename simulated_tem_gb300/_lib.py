@@ -22,6 +22,9 @@ ST_FLAG_AVERAGE = 0x2
 ST_FLAG_BRIGHT = 0x4
 ST_FLAG_STATS = 0x8
 
+ST_BLUR_NOALLOC_MAX_PIXELS = 1 << 21
+ST_BLUR_NOALLOC_MAX_NX = 4096
+
 _d = ctypes.c_double
 _i32 = ctypes.c_int32
 _i64 = ctypes.c_int64
@@ -61,6 +64,7 @@ _PROTOS = {
     "st_blur": (_i32, [_vp, _dp, _i32, _i32, _d, _dp]),
     "st_blur_device": (_i32, [_vp, _vp, _i32, _i32, _d, _vp, _vp]),
     "st_get_stats": (_i32, [_vp, ctypes.POINTER(StStats)]),
+    "st_blur_noalloc": (_i32, [_vp, _i32, _i32, _d, _vp, _vp, ctypes.c_char_p, _i32]),
     # include/stem_host.h
     "st_d2bi_create": (_i32, [ctypes.POINTER(_vp), _dp, _i32, _i32, _i32, _d, _dp, _dp, _d, _i32, _i32]),
     "st_d2bi_destroy": (None, [_vp]),
