@@ -139,7 +139,7 @@ def run_gpu(args):
     # counters for the roofline (one untimed image with statistics)
     step(flags | _lib.ST_FLAG_STATS)
     st = ctx.stats()
-    n_acc, n_kept = st.n_accepted, st.n_kept
+    n_acc, n_kept, n_tst = st.n_accepted, st.n_kept, st.n_tests
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -209,13 +209,14 @@ def run_gpu(args):
     flops = 8.0 * c_tests + 6.0 * n_acc + 20.0 * V + 165.0 * (G.Mz // 2) * (G.Mx * G.My) * n_prec
     col_avg = float(np.mean(col_ms))
     achieved = flops / (col_avg * 1e-3) / 1e12
-    roof = {"bound": "fp32", "kernel": "k_column_fp32", "achieved": achieved,
+    roof = {"bound": "fp32", "kernel": "k_column_fp32_v2", "achieved": achieved,
             "peak": peaks["fp32_tflops"] if peaks else None, "unit": "TFLOP/s",
             "frac": achieved / peaks["fp32_tflops"] if peaks else None,
             "peak_source": "measured live: FP32 FMA-pipe microbenchmark (libstem_peaks.so) on this GPU",
             "traffic": None,
             "algorithmic": {"flops_per_image": flops, "c_tests": c_tests, "accepted_pairs": n_acc,
                             "voxels": V, "kept_atoms": n_kept, "kernel_ms": col_avg,
+                            "kernel_tests_per_voxel": n_tst / V, "reference_tests_per_voxel": c_tests / V,
                             "formula": "8*C_tests + 6*accepted + 20*V + 165*(Mz/2)*Mx*My*nPrec"}}
     line = {"metric": METRIC, "value": value, "unit": "images/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -341,6 +342,20 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def ncu_case(args):
+    """Two FP32 images of the workload through st_image, nothing else: the
+    single-kernel case for an ncu capture of the column kernel."""
+    from simulated_tem_gb300 import _lib, imaging
+    _, t, x, _ = workload()
+    G, aa = t.image_geometry(len(x))
+    ctx = imaging.Context(0)
+    flags = _lib.ST_FLAG_AVERAGE | (0 if args.ncu_case == "fp64" else _lib.ST_FLAG_FP32)
+    for _ in range(2):
+        img = ctx.image(G, x, aa, flags=flags)
+    print("ncu case %s: mean I %.6f, column kernel %d" % (args.ncu_case, img.mean(), ctx.stats().column_kernel))
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -349,8 +364,12 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-rows", type=int, default=48)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--ncu-case", choices=["fp32", "fp64"], default=None,
+                    help="run two untimed images only (for an ncu capture)")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.ncu_case:
+        ncu_case(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)

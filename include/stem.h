@@ -87,6 +87,8 @@ typedef struct st_stats {
   int32_t n_prec;
   double ms_bin;       /* device time of the binning kernels (ms) */
   double ms_column;    /* device time of the column kernel (ms) */
+  int32_t column_kernel; /* 1 general FP32, 2 slab-ring FP32, 3 FP64 */
+  int32_t pad0;
 } st_stats;
 
 /* Context on CUDA device `device` (made current for the calls). */

@@ -54,7 +54,7 @@ struct Scratch {
   double4_32a* tmp_f = nullptr; // fx, fy, fz, g.y
   int* perm = nullptr;      // position-in-cell -> tmp index
   int* block_sums = nullptr;
-  unsigned long long* counters = nullptr;  // [0] kept, [1] max cell count, [2] tests, [3] accepted
+  unsigned long long* counters = nullptr;  // [0] kept, [1] max cell count, [2] tests, [3] accepted, [4] slab overflow
   size_t cap_candidates = 0;
   size_t cap_cells = 0;
   size_t cap_blocks = 0;
@@ -108,6 +108,7 @@ struct ColumnParams {
 cudaError_t launch_bin(const BinParams& p, const double* d_x, Scratch& s, BinnedAtoms& b, cudaStream_t st);
 cudaError_t launch_bin_finalize(const BinParams& p, Scratch& s, BinnedAtoms& b, int want_fp64, cudaStream_t st);
 cudaError_t launch_column_fp32(const ColumnParams& p, cudaStream_t st);
+cudaError_t launch_column_fp32_v2(const ColumnParams& p, cudaStream_t st);
 cudaError_t launch_column_fp64(const ColumnParams& p, cudaStream_t st);
 cudaError_t launch_epilogue(double* img, int Mx, int My, int ix0, int ix1, int iy0, int iy1, double scale,
                             int bright, cudaStream_t st);

@@ -244,7 +244,7 @@ int grid_for(int64_t n, int threads, int max_blocks) {
 cudaError_t launch_bin(const BinParams& p, const double* d_x, Scratch& s, BinnedAtoms& b, cudaStream_t st) {
   const int64_t n_cells = p.n_cells;
   cudaMemsetAsync(b.cell_count, 0, sizeof(int) * n_cells, st);
-  cudaMemsetAsync(s.counters, 0, sizeof(unsigned long long) * 4, st);
+  cudaMemsetAsync(s.counters, 0, sizeof(unsigned long long) * 8, st);
   const int64_t total = (int64_t)p.nuvw * p.n_atoms;
   int dev = 0, sms = 148;
   cudaGetDevice(&dev);

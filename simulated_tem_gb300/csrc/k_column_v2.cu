@@ -1,0 +1,458 @@
+// K2+K3, FP32, second generation: z-sorted slab ring and two slices per lane.
+//
+// Same computation as k_column_fp32 (the pixel loop of computeD2BI_img,
+// Lib_DynamicalTwoBeamImaging.f90:1870-1900, with the neighbour search of
+// Lib_LinkCell3D.f90:1515-1605 and the integrator of :2316-2480), organised to
+// issue fewer instructions per voxel:
+//
+// * One warp owns an 8 x 4 patch of pixel columns, one lane per column, and
+//   advances two depth slices per step.  Both slices share each candidate's
+//   load and its x-y distance; their z distances and r^2 are one packed
+//   FP32x2 subtraction and one packed FP32x2 fused multiply-add.
+// * Candidates live in a ring of four link-cell slabs (unwrapped z cells)
+//   in warp-private shared memory.  A slab is gathered once, when the march
+//   first needs it: the atoms of its cells in the patch footprint that lie
+//   within 3 sigma of the patch rectangle in x-y, then sorted by z by rank.
+//   A step scans, per slab, only the z-window [z0 - 3 sigma, z1 + 3 sigma]
+//   found by binary search.
+// * The RK4 double step (ii, ii+1, ii+2) runs once per step in registers for
+//   every precession angle; the periodic closure uses the saved first sample.
+//
+// It needs every link cell to be at least 3 sigma wide (then "within 3 sigma"
+// equals the reference's 27-cell search) and at most kCaps staged atoms per
+// slab; otherwise it raises counters[4] and the host recomputes the image with
+// k_column_fp32, which handles both cases.
+#include <cuda_runtime.h>
+
+#include <cfloat>
+
+#include "internal.h"
+
+namespace stem {
+namespace {
+
+constexpr int kWarps = 4;
+constexpr int kTileX = 8, kTileY = 4;
+constexpr int kCaps = 128;  // staged atoms per slab
+constexpr int kRing = 4;    // resident slabs (unwrapped z cells u, slot u & 3)
+constexpr float kHuge1 = FLT_MAX;
+
+constexpr int kBins = 32;  // z bins per slab for the window lookup
+
+struct WarpSmem {
+  float4 p[kRing][kCaps];     // X', Y' (warp frame), z (own cell), cos -- lengths scaled by s
+  float s[kRing][kCaps];      // sin
+  int bin[kRing][kBins + 1];  // bin[b]: first atom with z >= b * (a33 s / kBins); bin[kBins] = count
+  int count[kRing];
+};
+
+__device__ __forceinline__ float ex2_approx(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+__device__ __forceinline__ int pos_mod(int a, int n) {
+  const int r = a % n;
+  return r < 0 ? r + n : r;
+}
+
+__device__ __forceinline__ int floor_div(int a, int n) { return (a >= 0) ? a / n : -((-a + n - 1) / n); }
+
+// Lengths inside the kernel are scaled by s = sqrt(log2(e) / (2 sigma^2)), so that the
+// Gaussian weight exp(-r^2 / (2 sigma^2)) is ex2(-r'^2) of the scaled distance r'.
+struct Geo {
+  int ux_lo, ux_hi, uy_lo, uy_hi, ux_ref, uy_ref;
+  float xmin, xmax, ymin, ymax, pre2;
+  float a11s, a22s, a33s, scale;
+};
+
+// Gather slab u (its cells in the patch footprint, atoms within 3 sigma of the
+// patch rectangle) into its ring slot, sort it by z in place and index its z
+// bins; false when it holds more than kCaps atoms.
+__device__ bool load_slab(const ColumnParams& p, const Geo& G, int u, WarpSmem& W, int lane) {
+  const int cz = pos_mod(u, p.Ez);
+  const int slot = u & (kRing - 1);
+  float4* P = W.p[slot];
+  float* S = W.s[slot];
+  int n = 0;
+  for (int uy = G.uy_lo; uy <= G.uy_hi; ++uy) {
+    const int cy = pos_mod(uy, p.Ey);
+    const int64_t row_base = (int64_t)p.Ex * (cy + (int64_t)p.Ey * cz);
+    const float yoff = G.a22s * (float)(uy - G.uy_ref);
+    for (int ux = G.ux_lo; ux <= G.ux_hi;) {
+      const int k = floor_div(ux, p.Ex);
+      const int run_hi = min(G.ux_hi, (k + 1) * p.Ex - 1);
+      const int shift = k * p.Ex;
+      const int a_lo = p.cell_start[row_base + (ux - shift)];
+      const int a_hi = p.cell_start[row_base + (run_hi - shift) + 1];
+      for (int b = a_lo; b < a_hi; b += 32) {
+        const int j = b + lane;
+        bool keep = false;
+        float4 rec = make_float4(0.f, 0.f, 0.f, 0.f);
+        float sn = 0.f;
+        if (j < a_hi) {
+          const float4 r = p.p32[j];
+          const int packed = __float_as_int(r.w);
+          const int cxu = (packed & 1023) + shift;
+          const float X = fmaf(r.x, G.scale, G.a11s * (float)(cxu - G.ux_ref));
+          const float Y = fmaf(r.y, G.scale, yoff);
+          const float dx = fmaxf(0.f, fmaxf(G.xmin - X, X - G.xmax));
+          const float dy = fmaxf(0.f, fmaxf(G.ymin - Y, Y - G.ymax));
+          keep = dx * dx + dy * dy <= G.pre2;
+          const float2 cs = p.cs32[j];
+          rec = make_float4(X, Y, r.z * G.scale, cs.x);
+          sn = cs.y;
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, keep);
+        const int cnt = __popc(m);
+        if (n + cnt > kCaps) return false;
+        if (keep) {
+          const int d = n + __popc(m & ((1u << lane) - 1));
+          P[d] = rec;
+          S[d] = sn;
+        }
+        n += cnt;
+      }
+      ux = run_hi + 1;
+    }
+  }
+  __syncwarp();
+  // in-place rank sort by z (stable on ties): read all, rank, then write
+  constexpr int kPer = kCaps / 32;
+  float4 e[kPer];
+  float es[kPer];
+  int rk[kPer];
+#pragma unroll
+  for (int k = 0; k < kPer; ++k) {
+    const int i = lane + 32 * k;
+    rk[k] = 0;
+    e[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+    es[k] = 0.f;
+    if (i < n) {
+      e[k] = P[i];
+      es[k] = S[i];
+    }
+  }
+  const int nk = (n + 31) >> 5;
+  for (int jj = 0; jj < n; ++jj) {
+    const float zj = P[jj].z;
+#pragma unroll
+    for (int k = 0; k < kPer; ++k)
+      if (k < nk) rk[k] += (zj < e[k].z) || (zj == e[k].z && jj < lane + 32 * k);
+  }
+  __syncwarp();
+#pragma unroll
+  for (int k = 0; k < kPer; ++k) {
+    if (lane + 32 * k < n) {
+      P[rk[k]] = e[k];
+      S[rk[k]] = es[k];
+    }
+  }
+  __syncwarp();
+  // bin index: first atom with z >= b * dz_bin (binary search, one bin per lane)
+  const float dzb = G.a33s / kBins;
+  for (int b = lane; b <= kBins; b += 32) {
+    int lo = 0, hi = n;
+    if (b == kBins) {
+      lo = n;
+    } else {
+      const float v = (float)b * dzb;
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (P[mid].z < v)
+          lo = mid + 1;
+        else
+          hi = mid;
+      }
+    }
+    W.bin[slot][b] = lo;
+  }
+  if (lane == 0) W.count[slot] = n;
+  __syncwarp();
+  return true;
+}
+
+struct Sample {
+  float c0, cgr, cgi;
+};
+
+__device__ __forceinline__ void deriv(const Sample& s, float a, const float* ph, float* d) {
+  const float ca = s.c0 + a;
+  d[0] = -s.c0 * ph[1] - s.cgi * ph[2] - s.cgr * ph[3];
+  d[1] = s.c0 * ph[0] + s.cgr * ph[2] - s.cgi * ph[3];
+  d[2] = s.cgi * ph[0] - s.cgr * ph[1] - ca * ph[3];
+  d[3] = s.cgr * ph[0] + s.cgi * ph[1] + ca * ph[2];
+}
+
+__device__ __forceinline__ void rk4(const Sample& s0, const Sample& s1, const Sample& s2, float a, float dz,
+                                    float* ph) {
+  float d[4], p1[4], q[4];
+  const float dz3 = dz / 3.f, dz23 = 2.f * dz / 3.f, dz2 = 2.f * dz;
+  deriv(s0, a, ph, d);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    p1[i] = ph[i] + d[i] * dz3;
+    q[i] = ph[i] + d[i] * dz;
+  }
+  deriv(s1, a, q, d);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    q[i] = ph[i] + d[i] * dz;
+    p1[i] = p1[i] + d[i] * dz23;
+  }
+  deriv(s1, a, q, d);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    q[i] = ph[i] + d[i] * dz2;
+    p1[i] = p1[i] + d[i] * dz23;
+  }
+  deriv(s2, a, q, d);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) ph[i] = p1[i] + d[i] * dz3;
+  const float inv = rsqrtf(ph[0] * ph[0] + ph[1] * ph[1] + ph[2] * ph[2] + ph[3] * ph[3]);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) ph[i] *= inv;
+}
+
+__device__ __forceinline__ float rho_of(float r2min, float sig) {
+  if (r2min < sig * sig) return 1.f;
+  if (r2min > 4.f * sig * sig) return 0.f;
+  const float xx = sqrtf(r2min) / sig - 1.f;
+  return 1.f - xx * xx * xx * (10.f - 15.f * xx + 6.f * xx * xx);
+}
+
+template <bool kDensity>
+__device__ __forceinline__ Sample make_sample(float sr, float si, float r2min, float b0, float bg, float sig) {
+  const float inv = rsqrtf(fmaxf(fmaf(sr, sr, si * si), 1e-32f));  // x = S / max(1e-16, |S|)
+  const float rho = kDensity ? rho_of(r2min, sig) : 1.f;
+  return Sample{b0 * rho, bg * rho * (sr * inv), bg * rho * (si * inv)};
+}
+
+template <int NP, bool kDensity, bool kStats>
+__global__ void __launch_bounds__(kWarps * 32, (NP >= 16 ? 4 : 5)) k_column_fp32_v2(const __grid_constant__ ColumnParams p) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  WarpSmem& W = reinterpret_cast<WarpSmem*>(smem_raw)[warp];
+
+  const int Wd = p.ix1 - p.ix0, Hd = p.iy1 - p.iy0;
+  const int tiles_x = (Wd + kTileX - 1) / kTileX, tiles_y = (Hd + kTileY - 1) / kTileY;
+  const int tile = blockIdx.x * kWarps + warp;
+  if (tile >= tiles_x * tiles_y) return;
+  if ((int64_t)p.counters[0] > p.cap) return;  // the binning overflowed: the host retries
+  const int tx = tile % tiles_x, ty = tile / tiles_x;
+  const int ix = p.ix0 + tx * kTileX + (lane & (kTileX - 1));
+  const int iy = p.iy0 + ty * kTileY + lane / kTileX;
+  const bool active = ix < p.ix1 && iy < p.iy1;
+
+  // s = sqrt(log2(e) / (2 sigma^2)): exp(-r^2 / (2 sigma^2)) = ex2(-(s r)^2)
+  const double sd = sqrt(p.i2s2 * 1.4426950408889634);
+  Geo G;
+  G.scale = (float)sd;
+  const int ixc = min(ix, p.ix1 - 1), iyc = min(iy, p.iy1 - 1);
+  const int hx = p.xtab[ixc].x, hy = p.ytab[iyc].x;
+  const double fvx = p.xfv[ixc], fvy = p.yfv[iyc];
+  {
+    const int big = 1 << 29;
+    const int mnx = __reduce_min_sync(0xffffffffu, active ? hx : big);
+    const int mxx = __reduce_max_sync(0xffffffffu, active ? hx : -big);
+    const int mny = __reduce_min_sync(0xffffffffu, active ? hy : big);
+    const int mxy = __reduce_max_sync(0xffffffffu, active ? hy : -big);
+    G.ux_lo = mnx - 1;
+    G.ux_hi = mxx + 1;
+    G.uy_lo = mny - 1;
+    G.uy_hi = mxy + 1;
+    G.ux_ref = mnx;
+    G.uy_ref = mny;
+  }
+  G.a11s = (float)(p.a11 * sd);
+  G.a22s = (float)(p.a22 * sd);
+  G.a33s = (float)(p.a33 * sd);
+  const float Xv = (float)(p.a11 * (fvx + (double)(hx - G.ux_ref)) * sd);
+  const float Yv = (float)(p.a22 * (fvy + (double)(hy - G.uy_ref)) * sd);
+  {
+    const float big = 1e30f;
+    float v = active ? Xv : big, w = active ? -Xv : big, y = active ? Yv : big, z = active ? -Yv : big;
+    for (int o = 16; o > 0; o >>= 1) {
+      v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+      w = fminf(w, __shfl_xor_sync(0xffffffffu, w, o));
+      y = fminf(y, __shfl_xor_sync(0xffffffffu, y, o));
+      z = fminf(z, __shfl_xor_sync(0xffffffffu, z, o));
+    }
+    G.xmin = v;
+    G.xmax = -w;
+    G.ymin = y;
+    G.ymax = -z;
+  }
+  const float cut2 = (float)(p.cut2 * sd * sd);        // (3 sigma)^2 in scaled units
+  const float r3 = sqrtf(cut2) * 1.0001f + 1e-4f;      // z-window half width, rounded up
+  G.pre2 = cut2 * 1.0002f + 1e-3f;
+  const float inv_bin = kBins / G.a33s;
+  const float sig = (float)p.sigma, b0 = (float)p.b0, bg = (float)p.bg, dzs = (float)p.dz;
+  const float r2_to_A2 = (float)(1.0 / (sd * sd));    // scaled r^2 back to A^2 (density)
+
+  const int np = min(NP, p.n_prec - p.prec_offset);
+  float aa[NP], ph[NP][4];
+#pragma unroll
+  for (int k = 0; k < NP; ++k) {
+    aa[k] = (k < np) ? p.aaf[p.prec_offset + k] : 0.f;
+    ph[k][0] = 1.f;
+    ph[k][1] = ph[k][2] = ph[k][3] = 0.f;
+  }
+  Sample s_first{0.f, 0.f, 0.f}, s_prev{0.f, 0.f, 0.f}, s_mid{0.f, 0.f, 0.f};
+  int ring_lo = 1 << 30, ring_hi = (1 << 30) - 1;  // empty
+  unsigned n_acc = 0;
+  unsigned long long n_tst = 0;
+
+  for (int z0 = 0; z0 < p.Mz; z0 += 2) {
+    const bool has1 = z0 + 1 < p.Mz;
+    const int hz0 = p.ztab[z0].x;
+    const int hz1 = has1 ? p.ztab[z0 + 1].x : hz0;
+    // slice depths (scaled) relative to the origin of home cell hz0
+    const float zv0 = (float)(p.a33 * p.zfv[z0] * sd);
+    const float zv1 = has1 ? (float)(p.a33 * (p.zfv[z0 + 1] + (double)(hz1 - hz0)) * sd) : zv0;
+    const int need_lo = hz0 - 1, need_hi = hz1 + 1;
+    if (need_lo > ring_hi || need_hi < ring_lo) {
+      ring_lo = need_lo;
+      ring_hi = need_lo - 1;
+    }
+    if (ring_lo < need_lo) ring_lo = need_lo;
+    bool ok = true;
+    while (ring_hi < need_hi && ok) {
+      ++ring_hi;
+      ok = load_slab(p, G, ring_hi, W, lane);
+    }
+    if (!ok) {
+      if (lane == 0) atomicExch(&p.counters[4], 1ull);
+      return;  // the host recomputes the image with the general kernel
+    }
+    // two accumulator sets (even / odd candidates) for instruction-level parallelism;
+    // .x is slice z0, .y slice z0 + 1
+    float2 srA = make_float2(0.f, 0.f), siA = srA, srB = srA, siB = srA;
+    float2 rmA = make_float2(kHuge1, kHuge1), rmB = rmA;
+    for (int u = need_lo; u <= need_hi; ++u) {
+      const int slot = u & (kRing - 1);
+      const float zoff = G.a33s * (float)(u - hz0);  // cell u's origin relative to hz0's
+      const float t0 = zv0 - zoff, t1 = zv1 - zoff;
+      const int b_lo = max(0, min(kBins, (int)floorf((t0 - r3) * inv_bin)));
+      const int b_hi = max(0, min(kBins, (int)ceilf((t1 + r3) * inv_bin)));
+      const int lo = W.bin[slot][b_lo];
+      const int hi = W.bin[slot][b_hi];
+      // a missing second slice (odd depth) sits far away and accepts nothing
+      const float2 tt = make_float2(-t0, has1 ? -t1 : -1e30f);
+      if (kStats) n_tst += (unsigned long long)(hi - lo);
+      const float4* P = W.p[slot];
+      const float* S = W.s[slot];
+      int j = lo;
+      for (; j + 1 < hi; j += 2) {
+        const float4 qa = P[j], qb = P[j + 1];
+        const float sa = S[j], sb = S[j + 1];
+        const float dxa = qa.x - Xv, dya = qa.y - Yv, dxb = qb.x - Xv, dyb = qb.y - Yv;
+        const float ha = fmaf(dxa, dxa, dya * dya), hb = fmaf(dxb, dxb, dyb * dyb);
+        const float2 dza = __fadd2_rn(make_float2(qa.z, qa.z), tt);
+        const float2 dzb = __fadd2_rn(make_float2(qb.z, qb.z), tt);
+        const float2 ra = __ffma2_rn(dza, dza, make_float2(ha, ha));
+        const float2 rb = __ffma2_rn(dzb, dzb, make_float2(hb, hb));
+        const float2 wa = make_float2(ra.x <= cut2 ? ex2_approx(-ra.x) : 0.f, ra.y <= cut2 ? ex2_approx(-ra.y) : 0.f);
+        const float2 wb = make_float2(rb.x <= cut2 ? ex2_approx(-rb.x) : 0.f, rb.y <= cut2 ? ex2_approx(-rb.y) : 0.f);
+        srA = __ffma2_rn(wa, make_float2(qa.w, qa.w), srA);
+        siA = __ffma2_rn(wa, make_float2(sa, sa), siA);
+        srB = __ffma2_rn(wb, make_float2(qb.w, qb.w), srB);
+        siB = __ffma2_rn(wb, make_float2(sb, sb), siB);
+        if (kDensity) {
+          // r_min over all tested candidates: a candidate beyond 3 sigma only lowers r_min
+          // to a value beyond 2 sigma, where the density is 0 either way
+          rmA.x = fminf(rmA.x, ra.x);
+          rmA.y = fminf(rmA.y, ra.y);
+          rmB.x = fminf(rmB.x, rb.x);
+          rmB.y = fminf(rmB.y, rb.y);
+        }
+        if (kStats) n_acc += (ra.x <= cut2) + (ra.y <= cut2) + (rb.x <= cut2) + (rb.y <= cut2);
+      }
+      if (j < hi) {
+        const float4 qa = P[j];
+        const float sa = S[j];
+        const float dxa = qa.x - Xv, dya = qa.y - Yv;
+        const float ha = fmaf(dxa, dxa, dya * dya);
+        const float2 dza = __fadd2_rn(make_float2(qa.z, qa.z), tt);
+        const float2 ra = __ffma2_rn(dza, dza, make_float2(ha, ha));
+        const float2 wa = make_float2(ra.x <= cut2 ? ex2_approx(-ra.x) : 0.f, ra.y <= cut2 ? ex2_approx(-ra.y) : 0.f);
+        srA = __ffma2_rn(wa, make_float2(qa.w, qa.w), srA);
+        siA = __ffma2_rn(wa, make_float2(sa, sa), siA);
+        if (kDensity) {
+          rmA.x = fminf(rmA.x, ra.x);
+          rmA.y = fminf(rmA.y, ra.y);
+        }
+        if (kStats) n_acc += (ra.x <= cut2) + (ra.y <= cut2);
+      }
+    }
+    const float2 sr = __fadd2_rn(srA, srB), si = __fadd2_rn(siA, siB);
+    const float rm0 = fminf(rmA.x, rmB.x) * r2_to_A2, rm1 = fminf(rmA.y, rmB.y) * r2_to_A2;
+    // field samples z0 (even) and z0 + 1 (odd), then the RK4 double step (z0-2, z0-1, z0)
+    const Sample s0 = make_sample<kDensity>(sr.x, si.x, rm0, b0, bg, sig);
+    if (z0 == 0) {
+      s_first = s0;
+    } else {
+#pragma unroll
+      for (int k = 0; k < NP; ++k)
+        if (k < np) rk4(s_prev, s_mid, s0, aa[k], dzs, ph[k]);
+    }
+    s_prev = s0;
+    if (has1) s_mid = make_sample<kDensity>(sr.y, si.y, rm1, b0, bg, sig);
+  }
+  if ((p.Mz & 1) == 0) {  // closure x(Mz) = x(0)
+#pragma unroll
+    for (int k = 0; k < NP; ++k)
+      if (k < np) rk4(s_prev, s_mid, s_first, aa[k], dzs, ph[k]);
+  }
+  float acc = 0.f;
+#pragma unroll
+  for (int k = 0; k < NP; ++k)
+    if (k < np) acc += ph[k][2] * ph[k][2] + ph[k][3] * ph[k][3];
+  if (active) {
+    double* o = p.img + ix + (int64_t)p.Mx * iy;
+    *o = p.accumulate ? *o + (double)acc : (double)acc;
+  }
+  if (kStats) {
+    unsigned long long acc_w = active ? n_acc : 0u, tst_w = active ? 2 * n_tst : 0u;
+    for (int o = 16; o > 0; o >>= 1) {
+      acc_w += __shfl_xor_sync(0xffffffffu, acc_w, o);
+      tst_w += __shfl_xor_sync(0xffffffffu, tst_w, o);
+    }
+    if (lane == 0) {
+      atomicAdd(&p.counters[2], tst_w);
+      atomicAdd(&p.counters[3], acc_w);
+    }
+  }
+}
+
+template <typename K>
+cudaError_t launch(K kernel, const ColumnParams& p, cudaStream_t st) {
+  const int Wd = p.ix1 - p.ix0, Hd = p.iy1 - p.iy0;
+  const int tiles = ((Wd + kTileX - 1) / kTileX) * ((Hd + kTileY - 1) / kTileY);
+  const int grid = (tiles + kWarps - 1) / kWarps;
+  const size_t smem = sizeof(WarpSmem) * kWarps;
+  cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  kernel<<<grid, kWarps * 32, smem, st>>>(p);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+template <bool kDensity, bool kStats>
+cudaError_t launch_np(const ColumnParams& p, cudaStream_t st) {
+  const int np = p.n_prec - p.prec_offset;
+  if (np <= 1) return launch(k_column_fp32_v2<1, kDensity, kStats>, p, st);
+  if (np <= 2) return launch(k_column_fp32_v2<2, kDensity, kStats>, p, st);
+  if (np <= 4) return launch(k_column_fp32_v2<4, kDensity, kStats>, p, st);
+  if (np <= 8) return launch(k_column_fp32_v2<8, kDensity, kStats>, p, st);
+  return launch(k_column_fp32_v2<16, kDensity, kStats>, p, st);
+}
+
+cudaError_t launch_column_fp32_v2(const ColumnParams& p, cudaStream_t st) {
+  if (p.use_density) return p.want_stats ? launch_np<true, true>(p, st) : launch_np<true, false>(p, st);
+  return p.want_stats ? launch_np<false, true>(p, st) : launch_np<false, false>(p, st);
+}
+
+}  // namespace stem

@@ -9,6 +9,7 @@
 
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -39,6 +40,8 @@ struct st_ctx {
   cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
   st_stats stats{};
   int64_t last_kept = 0;  // kept atoms of the previous image: sizes the next one
+  bool fp32_general = false;  // STEM_FP32_KERNEL=general: always use k_column_fp32
+  int last_column_kernel = 0;  // 1 general FP32, 2 slab-ring FP32, 3 FP64
 };
 
 namespace {
@@ -154,6 +157,8 @@ extern "C" int st_create(st_ctx** out, int device) {
   e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaMallocHost((void**)&c->h_counters, 8 * sizeof(unsigned long long));
   for (int i = 0; i < 3 && e == cudaSuccess; ++i) e = cudaEventCreate(&c->ev[i]);
+  const char* kv = std::getenv("STEM_FP32_KERNEL");
+  c->fp32_general = kv && std::strcmp(kv, "general") == 0;
   if (e != cudaSuccess) {
     delete c;
     return ST_ERR_CUDA;
@@ -354,24 +359,44 @@ extern "C" int st_image_device(st_ctx* c, const st_geom* g, const double* d_x, i
   cp.img = d_img;
   cp.counters = c->s.counters;
   cp.cap = cap;
-  if (g->ix1 > g->ix0 && g->iy1 > g->iy0) {
-    const int width = fp32 ? 16 : 4;
-    for (int off = 0; off < nPrec; off += width) {
-      cp.prec_offset = off;
-      cp.accumulate = off > 0 ? 1 : 0;
-      e = fp32 ? launch_column_fp32(cp, st) : launch_column_fp64(cp, st);
-      if (e != cudaSuccess) return cuda_fail(c, e, "column kernel launch");
+  // the slab-ring FP32 kernel needs cells of at least 3 sigma (no truncated search) and at
+  // least one voxel thick in z; otherwise, or when a slab overflows, the general kernel runs
+  bool ring = fp32 && !cp.check_cells && g->Ez <= Mz && !c->fp32_general;
+  auto columns = [&](bool use_ring) -> cudaError_t {
+    cudaError_t ce = cudaSuccess;
+    if (g->ix1 > g->ix0 && g->iy1 > g->iy0) {
+      const int width = fp32 ? 16 : 4;
+      for (int off = 0; off < nPrec && ce == cudaSuccess; off += width) {
+        cp.prec_offset = off;
+        cp.accumulate = off > 0 ? 1 : 0;
+        ce = !fp32 ? launch_column_fp64(cp, st) : (use_ring ? launch_column_fp32_v2(cp, st)
+                                                           : launch_column_fp32(cp, st));
+      }
+      if (ce == cudaSuccess && (flags & ST_FLAG_AVERAGE))
+        ce = launch_epilogue(d_img, Mx, My, g->ix0, g->ix1, g->iy0, g->iy1, (double)nPrec,
+                             (flags & ST_FLAG_BRIGHT) ? 1 : 0, st);
     }
-    if (flags & ST_FLAG_AVERAGE) {
-      e = launch_epilogue(d_img, Mx, My, g->ix0, g->ix1, g->iy0, g->iy1, (double)nPrec,
-                          (flags & ST_FLAG_BRIGHT) ? 1 : 0, st);
-      if (e != cudaSuccess) return cuda_fail(c, e, "epilogue launch");
-    }
-  }
+    return ce;
+  };
+  e = columns(ring);
+  if (e != cudaSuccess) return cuda_fail(c, e, "column kernel launch");
   cudaEventRecord(c->ev[2], st);
-  e = cudaMemcpyAsync(c->h_counters, c->s.counters, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
+  e = cudaMemcpyAsync(c->h_counters, c->s.counters, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return cuda_fail(c, e, "image kernels");
+  if (ring && c->h_counters[4] != 0 && (int64_t)c->h_counters[0] <= cap) {
+    // a slab held more atoms than the ring kernel stages: recompute with the general kernel
+    ring = false;
+    cudaMemsetAsync(c->s.counters + 2, 0, 3 * sizeof(unsigned long long), st);
+    e = cudaMemsetAsync(d_img, 0, sizeof(double) * (size_t)Mx * My, st);
+    if (e == cudaSuccess) e = columns(false);
+    cudaEventRecord(c->ev[2], st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(c->h_counters, c->s.counters, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(c, e, "image kernels (general FP32 kernel)");
+  }
+  c->last_column_kernel = !fp32 ? 3 : (ring ? 2 : 1);
   if ((int64_t)c->h_counters[0] <= cap) break;
   if (attempt > 0) return fail(c, ST_ERR_ALLOC, "binning capacity did not converge");
   cap = (int64_t)c->h_counters[0] + (int64_t)c->h_counters[0] / 8 + 1024;  // grow and redo the image
@@ -392,6 +417,7 @@ extern "C" int st_image_device(st_ctx* c, const st_geom* g, const double* d_x, i
   S.ms_bin = ms;
   cudaEventElapsedTime(&ms, c->ev[1], c->ev[2]);
   S.ms_column = ms;
+  S.column_kernel = c->last_column_kernel;
   if (g->nMax0 > 0 && S.max_cell_count > 16 * g->nMax0) {
     char buf[256];
     snprintf(buf, sizeof buf,

@@ -189,3 +189,49 @@ def test_errors_are_reported(ctx):
     assert e.value.code == _lib.ST_ERR_CAPACITY
     # the context stays usable
     assert np.isfinite(ctx.image(G, x, aa)).all()
+
+
+def _general_fp32_context():
+    import os
+    old = os.environ.get("STEM_FP32_KERNEL")
+    os.environ["STEM_FP32_KERNEL"] = "general"
+    try:
+        return imaging.Context(0)
+    finally:
+        if old is None:
+            del os.environ["STEM_FP32_KERNEL"]
+        else:
+            os.environ["STEM_FP32_KERNEL"] = old
+
+
+@pytest.mark.parametrize("density", [False, True])
+def test_fp32_ring_and_general_kernels_agree(ctx, density):
+    """The slab-ring FP32 kernel and the general FP32 kernel compute the same image."""
+    cell = synth.small_cell(**CELLS["screw+void"])
+    t, so, x = setup_both(cell, sg=0.01, density=density)
+    G, aa = t.image_geometry(len(x), n_prec=3)
+    ring = ctx.image(G, x, aa, flags=_lib.ST_FLAG_FP32 | _lib.ST_FLAG_STATS)
+    assert ctx.stats().column_kernel == 2
+    gctx = _general_fp32_context()
+    try:
+        gen = gctx.image(G, x, aa, flags=_lib.ST_FLAG_FP32 | _lib.ST_FLAG_STATS)
+        assert gctx.stats().column_kernel == 1
+    finally:
+        gctx.close()
+    want, _ = oracle_patch(so, x, 3, 0.005)
+    assert np.abs(ring - want).max() <= FP32_TOL
+    assert np.abs(gen - want).max() <= FP32_TOL
+    assert np.abs(ring - gen).max() <= 2e-5
+
+
+def test_fp32_ring_overflow_falls_back(ctx):
+    """Four copies of every atom overfill the ring kernel's slab buffers: the image
+    is recomputed by the general kernel and still matches the oracle."""
+    cell = synth.small_cell(**CELLS["voids"])
+    dense = synth.Cell(cell.a_super, np.concatenate([cell.pos] * 4))
+    t, so, x = setup_both(dense, sg=0.01)
+    G, aa = t.image_geometry(len(x))
+    got = ctx.image(G, x, aa, flags=_lib.ST_FLAG_FP32)
+    assert ctx.stats().column_kernel == 1
+    want, _ = oracle_patch(so, x, 1, 0.005)
+    assert np.abs(got - want).max() <= FP32_TOL
