@@ -43,7 +43,6 @@ struct BinnedAtoms {
   // FP32 records
   float4* p32;         // a_col11*fx, a_col22*fy, a_col33*fz, bits(packed cell)
   float2* cs32;        // cos, sin of the FP64-reduced phase
-  int* cell_of;        // packed cell (cx | cy << 10 | cz << 20)
 };
 
 struct Scratch {
@@ -105,7 +104,8 @@ struct ColumnParams {
 };
 
 // launchers (return cudaError_t of the launches)
-cudaError_t launch_bin(const BinParams& p, const double* d_x, Scratch& s, BinnedAtoms& b, cudaStream_t st);
+cudaError_t launch_bin(const BinParams& p, const double* d_x, Scratch& s, BinnedAtoms& b, bool exact,
+                       cudaStream_t st);
 cudaError_t launch_bin_finalize(const BinParams& p, Scratch& s, BinnedAtoms& b, int want_fp64, cudaStream_t st);
 cudaError_t launch_column_fp32(const ColumnParams& p, cudaStream_t st);
 cudaError_t launch_column_fp32_v2(const ColumnParams& p, cudaStream_t st);

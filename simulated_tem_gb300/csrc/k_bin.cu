@@ -29,6 +29,15 @@ __device__ __forceinline__ double dot3_rn(double a0, double a1, double a2, doubl
   return __dadd_rn(__dadd_rn(__dmul_rn(a0, b0), __dmul_rn(a1, b1)), __dmul_rn(a2, b2));
 }
 
+// One thread per candidate (replica nn, atom jj) in the reference's insertion
+// order t = nn * N + jj.  kExact: every kept candidate goes through the
+// reference's rounded FP64 arithmetic (the FP64 imaging path needs its exact
+// fractional offsets).  Otherwise the kept candidates use fused FP64
+// multiply-adds, which agree with the reference to a few ulp, and fall back to
+// the exact arithmetic whenever a cell coordinate lies within 1e-9 cells of a
+// cell face: the cell assignment is bit-identical either way, the offsets and
+// the phase agree to ~1e-14.
+template <bool kExact>
 __global__ void __launch_bounds__(256) k_bin_transform(const __grid_constant__ BinParams p,
                                                        const double* __restrict__ x, int* __restrict__ counts,
                                                        int* __restrict__ tmp_key, int* __restrict__ tmp_cell,
@@ -55,19 +64,33 @@ __global__ void __launch_bounds__(256) k_bin_transform(const __grid_constant__ B
                 cf2 >= -margin && cf2 < p.Ez + margin;
     double c0 = 0, c1 = 0, c2 = 0, y0 = 0, y1 = 0, y2 = 0;
     if (keep) {
-      // exact FP64 transform in the reference's order
       const double yy0 = __dadd_rn(x0, p.Ruvw[3 * nn + 0]);
       const double yy1 = __dadd_rn(x1, p.Ruvw[3 * nn + 1]);
       const double yy2 = __dadd_rn(x2, p.Ruvw[3 * nn + 2]);
-      y0 = __dadd_rn(dot3_rn(p.RU[0], p.RU[3], p.RU[6], yy0, yy1, yy2), p.delta[0]);
-      y1 = __dadd_rn(dot3_rn(p.RU[1], p.RU[4], p.RU[7], yy0, yy1, yy2), p.delta[1]);
-      y2 = __dadd_rn(dot3_rn(p.RU[2], p.RU[5], p.RU[8], yy0, yy1, yy2), p.delta[2]);
-      const double z0 = __dsub_rn(y0, p.lc_delta[0]);
-      const double z1 = __dsub_rn(y1, p.lc_delta[1]);
-      const double z2 = __dsub_rn(y2, p.lc_delta[2]);
-      c0 = dot3_rn(p.ia[0], p.ia[3], p.ia[6], z0, z1, z2);
-      c1 = dot3_rn(p.ia[1], p.ia[4], p.ia[7], z0, z1, z2);
-      c2 = dot3_rn(p.ia[2], p.ia[5], p.ia[8], z0, z1, z2);
+      bool exact = kExact;
+      if (!kExact) {
+        y0 = fma(p.RU[6], yy2, fma(p.RU[3], yy1, p.RU[0] * yy0)) + p.delta[0];
+        y1 = fma(p.RU[7], yy2, fma(p.RU[4], yy1, p.RU[1] * yy0)) + p.delta[1];
+        y2 = fma(p.RU[8], yy2, fma(p.RU[5], yy1, p.RU[2] * yy0)) + p.delta[2];
+        c0 = (y0 - p.lc_delta[0]) * p.ia[0];
+        c1 = (y1 - p.lc_delta[1]) * p.ia[4];
+        c2 = (y2 - p.lc_delta[2]) * p.ia[8];
+        const double e = 1e-9;
+        const double f0 = c0 - floor(c0), f1 = c1 - floor(c1), f2 = c2 - floor(c2);
+        exact = f0 < e || f0 > 1.0 - e || f1 < e || f1 > 1.0 - e || f2 < e || f2 > 1.0 - e;
+      }
+      if (exact) {
+        // the reference's order, every operation rounded separately
+        y0 = __dadd_rn(dot3_rn(p.RU[0], p.RU[3], p.RU[6], yy0, yy1, yy2), p.delta[0]);
+        y1 = __dadd_rn(dot3_rn(p.RU[1], p.RU[4], p.RU[7], yy0, yy1, yy2), p.delta[1]);
+        y2 = __dadd_rn(dot3_rn(p.RU[2], p.RU[5], p.RU[8], yy0, yy1, yy2), p.delta[2]);
+        const double z0 = __dsub_rn(y0, p.lc_delta[0]);
+        const double z1 = __dsub_rn(y1, p.lc_delta[1]);
+        const double z2 = __dsub_rn(y2, p.lc_delta[2]);
+        c0 = dot3_rn(p.ia[0], p.ia[3], p.ia[6], z0, z1, z2);
+        c1 = dot3_rn(p.ia[1], p.ia[4], p.ia[7], z0, z1, z2);
+        c2 = dot3_rn(p.ia[2], p.ia[5], p.ia[8], z0, z1, z2);
+      }
       // pointInSupercell: floor(c) in [0, N) on every axis
       keep = c0 >= 0.0 && c0 < (double)p.Ex && c1 >= 0.0 && c1 < (double)p.Ey && c2 >= 0.0 &&
              c2 < (double)p.Ez;
@@ -87,7 +110,8 @@ __global__ void __launch_bounds__(256) k_bin_transform(const __grid_constant__ B
     const int cell = cx + p.Ex * (cy + p.Ey * cz);
     const int slot = atomicAdd(&counts[cell], 1);
     if (idx >= p.cap) continue;  // overflow: counted, not stored; the host grows the arrays and retries
-    const double gdotr = dot3_rn(p.g[0], p.g[1], p.g[2], y0, y1, y2);
+    const double gdotr = kExact ? dot3_rn(p.g[0], p.g[1], p.g[2], y0, y1, y2)
+                                : fma(p.g[2], y2, fma(p.g[1], y1, p.g[0] * y0));
     tmp_key[idx] = (int)t;
     tmp_cell[idx] = cell;
     tmp_slot[idx] = slot;
@@ -192,7 +216,29 @@ __global__ void __launch_bounds__(256) k_bin_place(const int* __restrict__ tmp_c
     perm[start[tmp_cell[i]] + tmp_slot[i]] = (int)i;
 }
 
-// Per cell: order the entries by candidate index and write the records.
+// Per cell: order the entries by candidate index (the reference's insertion
+// order) and write the records.  Cells of up to kRankRegs entries rank in
+// registers; larger cells rank from memory.
+constexpr int kRankRegs = 24;
+
+__device__ __forceinline__ void write_record(const BinnedAtoms& b, int dst, const double4_32a& f, int packed,
+                                             double a11, double a22, double a33, int want_fp64) {
+  b.p32[dst] = make_float4((float)(a11 * f.x), (float)(a22 * f.y), (float)(a33 * f.z), __int_as_float(packed));
+  if (want_fp64) {
+    double sn, cs;
+    sincos(f.w, &sn, &cs);
+    b.f64[dst] = make_double4_32a(f.x, f.y, f.z, 0.0);
+    b.cs64[dst] = make_double2(cs, sn);
+  } else {
+    // g.y reduced modulo one cycle in FP64, the phasor in FP32
+    double tcyc = f.w * kInv2Pi;
+    tcyc = tcyc - rint(tcyc);
+    float sf, cf;
+    sincospif(2.0f * (float)tcyc, &sf, &cf);
+    b.cs32[dst] = make_float2(cf, sf);
+  }
+}
+
 __global__ void __launch_bounds__(128) k_bin_finalize(const int* __restrict__ start, const int* __restrict__ counts,
                                                       int64_t n_cells, int Ex, int Ey, const int* __restrict__ perm,
                                                       const int* __restrict__ tmp_key,
@@ -206,27 +252,28 @@ __global__ void __launch_bounds__(128) k_bin_finalize(const int* __restrict__ st
     const int rem = (int)(c - (int64_t)cz * Ex * Ey);
     const int cy = rem / Ex, cx = rem - cy * Ex;
     const int packed = pack_cell(cx, cy, cz);
-    for (int i = 0; i < n; ++i) {
-      const int ti = perm[s + i];
-      const int ki = tmp_key[ti];
-      int r = 0;
-      for (int j = 0; j < n; ++j) r += (tmp_key[perm[s + j]] < ki);
-      const int dst = s + r;
-      const double4_32a f = tmp_f[ti];
-      b.cell_of[dst] = packed;
-      b.p32[dst] = make_float4((float)(a11 * f.x), (float)(a22 * f.y), (float)(a33 * f.z), __int_as_float(packed));
-      if (want_fp64) {
-        double sn, cs;
-        sincos(f.w, &sn, &cs);
-        b.f64[dst] = make_double4_32a(f.x, f.y, f.z, 0.0);
-        b.cs64[dst] = make_double2(cs, sn);
-      } else {
-        // g.y reduced modulo one cycle in FP64, the phasor in FP32
-        double tcyc = f.w * kInv2Pi;
-        tcyc = tcyc - rint(tcyc);
-        float sf, cf;
-        sincospif(2.0f * (float)tcyc, &sf, &cf);
-        b.cs32[dst] = make_float2(cf, sf);
+    if (n <= kRankRegs) {
+      int key[kRankRegs], ti[kRankRegs];
+#pragma unroll
+      for (int i = 0; i < kRankRegs; ++i) {
+        ti[i] = (i < n) ? perm[s + i] : 0;
+        key[i] = (i < n) ? tmp_key[ti[i]] : 0x7fffffff;
+      }
+#pragma unroll
+      for (int i = 0; i < kRankRegs; ++i) {
+        if (i >= n) break;
+        int r = 0;
+#pragma unroll
+        for (int j = 0; j < kRankRegs; ++j) r += (key[j] < key[i]);
+        write_record(b, s + r, tmp_f[ti[i]], packed, a11, a22, a33, want_fp64);
+      }
+    } else {
+      for (int i = 0; i < n; ++i) {
+        const int t = perm[s + i];
+        const int ki = tmp_key[t];
+        int r = 0;
+        for (int j = 0; j < n; ++j) r += (tmp_key[perm[s + j]] < ki);
+        write_record(b, s + r, tmp_f[t], packed, a11, a22, a33, want_fp64);
       }
     }
   }
@@ -241,7 +288,8 @@ int grid_for(int64_t n, int threads, int max_blocks) {
 
 }  // namespace
 
-cudaError_t launch_bin(const BinParams& p, const double* d_x, Scratch& s, BinnedAtoms& b, cudaStream_t st) {
+cudaError_t launch_bin(const BinParams& p, const double* d_x, Scratch& s, BinnedAtoms& b, bool exact,
+                       cudaStream_t st) {
   const int64_t n_cells = p.n_cells;
   cudaMemsetAsync(b.cell_count, 0, sizeof(int) * n_cells, st);
   cudaMemsetAsync(s.counters, 0, sizeof(unsigned long long) * 8, st);
@@ -249,8 +297,12 @@ cudaError_t launch_bin(const BinParams& p, const double* d_x, Scratch& s, Binned
   int dev = 0, sms = 148;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  k_bin_transform<<<grid_for(total, 256, sms * 16), 256, 0, st>>>(p, d_x, b.cell_count, s.tmp_key, s.tmp_cell,
-                                                                  s.tmp_slot, s.tmp_f, s.counters);
+  if (exact)
+    k_bin_transform<true><<<grid_for(total, 256, sms * 16), 256, 0, st>>>(p, d_x, b.cell_count, s.tmp_key,
+                                                                        s.tmp_cell, s.tmp_slot, s.tmp_f, s.counters);
+  else
+    k_bin_transform<false><<<grid_for(total, 256, sms * 16), 256, 0, st>>>(p, d_x, b.cell_count, s.tmp_key,
+                                                                         s.tmp_cell, s.tmp_slot, s.tmp_f, s.counters);
   const int nb = (int)((n_cells + kScanBlock - 1) / kScanBlock);
   k_scan_blocks<<<nb, 256, 0, st>>>(b.cell_count, n_cells, s.block_sums, s.counters);
   k_scan_top<<<1, 1024, 0, st>>>(s.block_sums, nb);

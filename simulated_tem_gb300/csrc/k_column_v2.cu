@@ -12,9 +12,13 @@
 // * Candidates live in a ring of four link-cell slabs (unwrapped z cells)
 //   in warp-private shared memory.  A slab is gathered once, when the march
 //   first needs it: the atoms of its cells in the patch footprint that lie
-//   within 3 sigma of the patch rectangle in x-y, then sorted by z by rank.
-//   A step scans, per slab, only the z-window [z0 - 3 sigma, z1 + 3 sigma]
-//   found by binary search.
+//   within 3 sigma of the patch rectangle in x-y, then ordered by z bin (32
+//   bins per cell height, a counting sort).  A step scans, per slab, only the
+//   bins that overlap the z-window [z0 - 3 sigma, z1 + 3 sigma].
+// * Lengths are scaled by s = sqrt(log2 e / (2 sigma^2)), so the weight
+//   exp(-r^2 / 2 sigma^2) is one ex2 of the negated scaled r^2, selected to
+//   zero beyond the cutoff without a branch; both slices accumulate with
+//   packed FP32x2 multiply-adds.
 // * The RK4 double step (ii, ii+1, ii+2) runs once per step in registers for
 //   every precession angle; the periodic closure uses the saved first sample.
 //
@@ -42,7 +46,7 @@ constexpr int kBins = 32;  // z bins per slab for the window lookup
 struct WarpSmem {
   float4 p[kRing][kCaps];     // X', Y' (warp frame), z (own cell), cos -- lengths scaled by s
   float s[kRing][kCaps];      // sin
-  int bin[kRing][kBins + 1];  // bin[b]: first atom with z >= b * (a33 s / kBins); bin[kBins] = count
+  int bin[kRing][kBins + 1];  // bin[b]: first atom of z bin b (width a33 s / kBins); bin[kBins] = count
   int count[kRing];
 };
 
@@ -68,8 +72,8 @@ struct Geo {
 };
 
 // Gather slab u (its cells in the patch footprint, atoms within 3 sigma of the
-// patch rectangle) into its ring slot, sort it by z in place and index its z
-// bins; false when it holds more than kCaps atoms.
+// patch rectangle) into its ring slot and order it by z bin in place; false
+// when it holds more than kCaps atoms.
 __device__ bool load_slab(const ColumnParams& p, const Geo& G, int u, WarpSmem& W, int lane) {
   const int cz = pos_mod(u, p.Ez);
   const int slot = u & (kRing - 1);
@@ -118,56 +122,59 @@ __device__ bool load_slab(const ColumnParams& p, const Geo& G, int u, WarpSmem& 
     }
   }
   __syncwarp();
-  // in-place rank sort by z (stable on ties): read all, rank, then write
+  // counting sort by z bin, in place: every lane first holds its atoms in registers;
+  // within a bin the gather order is kept (deterministic)
   constexpr int kPer = kCaps / 32;
+  const float inv_bin = kBins / G.a33s;
+  int* hist = W.bin[slot];
+  for (int b = lane; b <= kBins; b += 32) hist[b] = 0;
+  __syncwarp();
   float4 e[kPer];
   float es[kPer];
-  int rk[kPer];
+  int eb[kPer], er[kPer];
+  const unsigned lt = (1u << lane) - 1;
 #pragma unroll
   for (int k = 0; k < kPer; ++k) {
     const int i = lane + 32 * k;
-    rk[k] = 0;
+    const bool valid = i < n;
     e[k] = make_float4(0.f, 0.f, 0.f, 0.f);
     es[k] = 0.f;
-    if (i < n) {
+    eb[k] = 0;
+    er[k] = 0;
+    const unsigned act = __ballot_sync(0xffffffffu, valid);
+    if (valid) {
       e[k] = P[i];
       es[k] = S[i];
+      eb[k] = min(kBins - 1, max(0, (int)floorf(e[k].z * inv_bin)));
+      const unsigned m = __match_any_sync(act, eb[k]);
+      er[k] = hist[eb[k]] + __popc(m & lt);
+      __syncwarp(act);
+      if ((m & lt) == 0) hist[eb[k]] += __popc(m);  // the group's first lane counts it
     }
+    __syncwarp();
   }
-  const int nk = (n + 31) >> 5;
-  for (int jj = 0; jj < n; ++jj) {
-    const float zj = P[jj].z;
-#pragma unroll
-    for (int k = 0; k < kPer; ++k)
-      if (k < nk) rk[k] += (zj < e[k].z) || (zj == e[k].z && jj < lane + 32 * k);
+  // exclusive scan of the 32 bin counts: bin starts, bin[kBins] = n
+  {
+    const int v = hist[lane];
+    int incl = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += t;
+    }
+    __syncwarp();
+    hist[lane] = incl - v;
+    if (lane == 0) hist[kBins] = n;
   }
   __syncwarp();
 #pragma unroll
   for (int k = 0; k < kPer; ++k) {
     if (lane + 32 * k < n) {
-      P[rk[k]] = e[k];
-      S[rk[k]] = es[k];
+      const int d = hist[eb[k]] + er[k];
+      P[d] = e[k];
+      S[d] = es[k];
     }
   }
   __syncwarp();
-  // bin index: first atom with z >= b * dz_bin (binary search, one bin per lane)
-  const float dzb = G.a33s / kBins;
-  for (int b = lane; b <= kBins; b += 32) {
-    int lo = 0, hi = n;
-    if (b == kBins) {
-      lo = n;
-    } else {
-      const float v = (float)b * dzb;
-      while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        if (P[mid].z < v)
-          lo = mid + 1;
-        else
-          hi = mid;
-      }
-    }
-    W.bin[slot][b] = lo;
-  }
   if (lane == 0) W.count[slot] = n;
   __syncwarp();
   return true;

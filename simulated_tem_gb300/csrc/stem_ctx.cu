@@ -97,7 +97,6 @@ bool alloc_kept(st_ctx* c, size_t need) {
   grow(c->b.cs64);
   grow(c->b.p32);
   grow(c->b.cs32);
-  grow(c->b.cell_of);
   if (e != cudaSuccess) return false;
   c->cap_kept = k;
   c->s.cap_candidates = k;
@@ -174,7 +173,7 @@ extern "C" void st_destroy(st_ctx* c) {
   void* dev_ptrs[] = {c->s.tmp_key, c->s.tmp_cell, c->s.tmp_slot, c->s.tmp_f, c->s.perm, c->s.block_sums,
                       c->s.counters, c->s.xtab, c->s.xfv, c->s.ytab, c->s.yfv, c->s.ztab, c->s.zfv, c->s.aa,
                       c->s.aaf, c->b.cell_start, c->b.cell_count, c->b.f64, c->b.cs64, c->b.p32, c->b.cs32,
-                      c->b.cell_of, c->d_x, c->d_img, c->d_blur, c->d_kern};
+                      c->d_x, c->d_img, c->d_blur, c->d_kern};
   for (void* p : dev_ptrs)
     if (p) cudaFree(p);
   if (c->h_counters) cudaFreeHost(c->h_counters);
@@ -308,7 +307,7 @@ extern "C" int st_image_device(st_ctx* c, const st_geom* g, const double* d_x, i
   if (!alloc_kept(c, (size_t)cap)) return cuda_fail(c, cudaErrorMemoryAllocation, "allocating binning buffers");
   bp.cap = cap;
   cudaEventRecord(c->ev[0], st);
-  e = launch_bin(bp, d_x, c->s, c->b, st);
+  e = launch_bin(bp, d_x, c->s, c->b, !fp32, st);
   if (e == cudaSuccess) e = launch_bin_finalize(bp, c->s, c->b, fp32 ? 0 : 1, st);
   if (e != cudaSuccess) return cuda_fail(c, e, "binning launch");
 

@@ -70,11 +70,14 @@ def test_fp32_matches_oracle(ctx, cell_name, density):
     cell = synth.small_cell(**CELLS[cell_name])
     t, so, x = setup_both(cell, sg=0.01, density=density)
     G, aa = t.image_geometry(len(x))
-    got = ctx.image(G, x, aa, flags=_lib.ST_FLAG_FP32)
-    want, _ = oracle_patch(so, x, 1, 0.005)
+    got = ctx.image(G, x, aa, flags=_lib.ST_FLAG_FP32 | _lib.ST_FLAG_STATS)
+    st = ctx.stats()
+    want, ost = oracle_patch(so, x, 1, 0.005)
     d = got - want
     assert np.abs(d).max() <= FP32_TOL
     assert np.sqrt((d ** 2).mean()) <= FP32_TOL / 5
+    # the FP32 path's binning assigns cells exactly like the reference
+    assert st.n_kept == ost.n_kept and st.max_cell_count == ost.max_cell_count
 
 
 @pytest.mark.parametrize("n_prec,fp32", [(3, False), (6, False), (5, True), (17, True)])
