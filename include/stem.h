@@ -87,7 +87,7 @@ typedef struct st_stats {
   int32_t n_prec;
   double ms_bin;       /* device time of the binning kernels (ms) */
   double ms_column;    /* device time of the column kernel (ms) */
-  int32_t column_kernel; /* 1 general FP32, 2 slab-ring FP32, 3 FP64 */
+  int32_t column_kernel; /* 1 general FP32, 2 slab-ring FP32 (for at least one image), 3 FP64 */
   int32_t pad0;
 } st_stats;
 
@@ -109,6 +109,28 @@ int st_image(st_ctx* ctx, const st_geom* geom, const double* x, int64_t ldx, int
  * the context's stream).  Returns after the image is complete. */
 int st_image_device(st_ctx* ctx, const st_geom* geom, const double* d_x, int64_t ldx, int64_t nAtoms,
                     const double* aa, int32_t nPrec, int32_t flags, double* d_img, void* stream);
+
+/* One image of a batch: its geometry, its atoms and output in device memory,
+ * and its precession parameters aa(1:nPrec) in host memory. */
+typedef struct st_job {
+  const st_geom* geom;
+  const double* d_x; /* (ldx, nAtoms) */
+  int64_t ldx;
+  int64_t nAtoms;
+  const double* aa;
+  int32_t nPrec;
+  int32_t pad0;
+  double* d_img; /* Mx x My, overwritten as by st_image */
+} st_job;
+
+/* Many images in one call: tomography tilts, precession sets, g-vectors or
+ * independent cells of uneven size.  No counterpart in the reference, which
+ * images one condition per computeD2BI_img call; each image is the one
+ * st_image_device makes for its job.  The binning runs once over the
+ * candidates of all jobs and, on the FP32 path, the columns of all jobs run
+ * as one persistent launch that hands out warp tiles from a global counter.
+ * flags apply to every job.  Returns after every image is complete. */
+int st_batch_device(st_ctx* ctx, int32_t n_jobs, const st_job* jobs, int32_t flags, void* stream);
 
 /* Gaussian blur of width t pixels (src/d2bi.f90:1543-1624) from host buffers;
  * in and out are nx x ny doubles, column-major; out is overwritten. */

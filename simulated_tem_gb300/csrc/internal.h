@@ -11,10 +11,14 @@
 namespace stem {
 
 // Fixed-size kernel parameters of the link-cell binning (K1).
+// One image (job) of a batch; the binning kernels read these from device memory.
 struct BinParams {
   int64_t n_atoms;
   int64_t cap;  // capacity of the kept-atom arrays; more kept atoms set the overflow condition
   int64_t ldx;
+  const double* x;    // positions (ldx, n_atoms) in device memory
+  int64_t cand_base;  // first candidate of this job in the batch (candidates of job j: nuvw * n_atoms)
+  int64_t cell_base;  // first link cell of this job in the batch's concatenated cell arrays
   int nuvw;
   int Ex, Ey, Ez;
   int64_t n_cells;
@@ -104,11 +108,25 @@ struct ColumnParams {
 };
 
 // launchers (return cudaError_t of the launches)
-cudaError_t launch_bin(const BinParams& p, const double* d_x, Scratch& s, BinnedAtoms& b, bool exact,
-                       cudaStream_t st);
-cudaError_t launch_bin_finalize(const BinParams& p, Scratch& s, BinnedAtoms& b, int want_fp64, cudaStream_t st);
+// Binning of a batch: jobs (device memory, n_jobs entries) with candidates
+// [0, total_cand) and cells [0, total_cells) concatenated in job order.
+cudaError_t launch_bin(const BinParams* d_jobs, int n_jobs, int64_t total_cand, int64_t total_cells, int64_t cap,
+                       Scratch& s, BinnedAtoms& b, bool exact, cudaStream_t st);
+cudaError_t launch_bin_finalize(const BinParams* d_jobs, int n_jobs, int64_t total_cells, int64_t cap, Scratch& s,
+                                BinnedAtoms& b, int want_fp64, cudaStream_t st);
 cudaError_t launch_column_fp32(const ColumnParams& p, cudaStream_t st);
-cudaError_t launch_column_fp32_v2(const ColumnParams& p, cudaStream_t st);
+
+// A job of the persistent slab-ring FP32 column kernel: an image and the first
+// warp tile it owns in the batch's tile sequence.
+struct ColumnJob {
+  ColumnParams p;
+  int tile_base;
+  int pad;
+};
+int column_tiles(const ColumnParams& p);
+cudaError_t launch_column_fp32_ring(const ColumnJob* d_jobs, int n_jobs, int total_tiles, int max_np, bool density,
+                                    bool stats, unsigned* work, const unsigned long long* counters, int64_t cap,
+                                    cudaStream_t st);
 cudaError_t launch_column_fp64(const ColumnParams& p, cudaStream_t st);
 cudaError_t launch_epilogue(double* img, int Mx, int My, int ix0, int ix1, int iy0, int iy1, double scale,
                             int bright, cudaStream_t st);

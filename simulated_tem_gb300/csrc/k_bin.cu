@@ -24,6 +24,20 @@ namespace {
 constexpr int kScanBlock = 1024;  // counts per scan block (256 threads x 4)
 constexpr double kInv2Pi = 0.15915494309189533577;
 
+// index of the job whose range [base(j), base(j+1)) holds v (bases ascending)
+template <typename F>
+__device__ __forceinline__ int find_job(int n_jobs, int64_t v, F base) {
+  int lo = 0, hi = n_jobs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (base(mid) <= v)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
 __device__ __forceinline__ double dot3_rn(double a0, double a1, double a2, double b0, double b1, double b2) {
   // (a0*b0 + a1*b1) + a2*b2 with every operation rounded separately
   return __dadd_rn(__dadd_rn(__dmul_rn(a0, b0), __dmul_rn(a1, b1)), __dmul_rn(a2, b2));
@@ -38,18 +52,21 @@ __device__ __forceinline__ double dot3_rn(double a0, double a1, double a2, doubl
 // cell face: the cell assignment is bit-identical either way, the offsets and
 // the phase agree to ~1e-14.
 template <bool kExact>
-__global__ void __launch_bounds__(256) k_bin_transform(const __grid_constant__ BinParams p,
-                                                       const double* __restrict__ x, int* __restrict__ counts,
+__global__ void __launch_bounds__(256) k_bin_transform(const BinParams* __restrict__ jobs, int n_jobs,
+                                                       int64_t total, int64_t cap, int* __restrict__ counts,
                                                        int* __restrict__ tmp_key, int* __restrict__ tmp_cell,
                                                        int* __restrict__ tmp_slot, double4_32a* __restrict__ tmp_f,
                                                        unsigned long long* __restrict__ counters) {
-  const int64_t total = (int64_t)p.nuvw * p.n_atoms;
   const float margin = 2e-3f;  // cells; the FP32 position error is below 1e-4 cells
-  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
-       t += (int64_t)gridDim.x * blockDim.x) {
-    const int nn = (int)(t / p.n_atoms);
+  for (int64_t tg = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; tg < total;
+       tg += (int64_t)gridDim.x * blockDim.x) {
+    const int job = n_jobs == 1 ? 0 : find_job(n_jobs, tg, [&](int k) { return jobs[k].cand_base; });
+    const BinParams& p = jobs[job];
+    const int64_t t = tg - p.cand_base;  // the reference's insertion order within the image
+    const int nn = p.n_atoms <= 0x7fffffff && t <= 0x7fffffff ? (int)((unsigned)t / (unsigned)p.n_atoms)
+                                                               : (int)(t / p.n_atoms);
     const int64_t jj = t - (int64_t)nn * p.n_atoms;
-    const double* xa = x + jj * p.ldx;
+    const double* xa = p.x + jj * p.ldx;
     const double x0 = xa[0], x1 = xa[1], x2 = xa[2];
 
     // FP32 reject test
@@ -107,9 +124,14 @@ __global__ void __launch_bounds__(256) k_bin_transform(const __grid_constant__ B
 
     const double fl0 = floor(c0), fl1 = floor(c1), fl2 = floor(c2);
     const int cx = (int)fl0, cy = (int)fl1, cz = (int)fl2;
-    const int cell = cx + p.Ex * (cy + p.Ey * cz);
-    const int slot = atomicAdd(&counts[cell], 1);
-    if (idx >= p.cap) continue;  // overflow: counted, not stored; the host grows the arrays and retries
+    const int cell = (int)p.cell_base + cx + p.Ex * (cy + p.Ey * cz);
+    // consecutive atoms often share a cell: one atomic per cell and warp
+    const unsigned same = __match_any_sync(mask, cell);
+    const int first = __ffs(same) - 1;
+    int slot0 = 0;
+    if (lane == first) slot0 = atomicAdd(&counts[cell], __popc(same));
+    const int slot = __shfl_sync(same, slot0, first) + __popc(same & ((1u << lane) - 1));
+    if (idx >= cap) continue;  // overflow: counted, not stored; the host grows the arrays and retries
     const double gdotr = kExact ? dot3_rn(p.g[0], p.g[1], p.g[2], y0, y1, y2)
                                 : fma(p.g[2], y2, fma(p.g[1], y1, p.g[0] * y0));
     tmp_key[idx] = (int)t;
@@ -239,17 +261,23 @@ __device__ __forceinline__ void write_record(const BinnedAtoms& b, int dst, cons
   }
 }
 
-__global__ void __launch_bounds__(128) k_bin_finalize(const int* __restrict__ start, const int* __restrict__ counts,
-                                                      int64_t n_cells, int Ex, int Ey, const int* __restrict__ perm,
+__global__ void __launch_bounds__(128) k_bin_finalize(const BinParams* __restrict__ jobs, int n_jobs,
+                                                      const int* __restrict__ start, const int* __restrict__ counts,
+                                                      int64_t n_cells, const int* __restrict__ perm,
                                                       const int* __restrict__ tmp_key,
-                                                      const double4_32a* __restrict__ tmp_f, double a11, double a22,
-                                                      double a33, int want_fp64, BinnedAtoms b,
-                                                      const unsigned long long* __restrict__ counters, int64_t cap) {
+                                                      const double4_32a* __restrict__ tmp_f, int want_fp64,
+                                                      BinnedAtoms b, const unsigned long long* __restrict__ counters,
+                                                      int64_t cap) {
   if ((int64_t)counters[0] > cap) return;
   for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n_cells; c += (int64_t)gridDim.x * blockDim.x) {
+    const int job = n_jobs == 1 ? 0 : find_job(n_jobs, c, [&](int k) { return jobs[k].cell_base; });
+    const BinParams& p = jobs[job];
+    const int Ex = p.Ex, Ey = p.Ey;
+    const double a11 = p.a_col[0], a22 = p.a_col[1], a33 = p.a_col[2];
+    const int64_t cl = c - p.cell_base;
     const int s = start[c], n = counts[c];
-    const int cz = (int)(c / ((int64_t)Ex * Ey));
-    const int rem = (int)(c - (int64_t)cz * Ex * Ey);
+    const int cz = (int)(cl / ((int64_t)Ex * Ey));
+    const int rem = (int)(cl - (int64_t)cz * Ex * Ey);
     const int cy = rem / Ex, cx = rem - cy * Ex;
     const int packed = pack_cell(cx, cy, cz);
     if (n <= kRankRegs) {
@@ -288,37 +316,36 @@ int grid_for(int64_t n, int threads, int max_blocks) {
 
 }  // namespace
 
-cudaError_t launch_bin(const BinParams& p, const double* d_x, Scratch& s, BinnedAtoms& b, bool exact,
-                       cudaStream_t st) {
-  const int64_t n_cells = p.n_cells;
-  cudaMemsetAsync(b.cell_count, 0, sizeof(int) * n_cells, st);
+cudaError_t launch_bin(const BinParams* d_jobs, int n_jobs, int64_t total_cand, int64_t total_cells, int64_t cap,
+                       Scratch& s, BinnedAtoms& b, bool exact, cudaStream_t st) {
+  cudaMemsetAsync(b.cell_count, 0, sizeof(int) * total_cells, st);
   cudaMemsetAsync(s.counters, 0, sizeof(unsigned long long) * 8, st);
-  const int64_t total = (int64_t)p.nuvw * p.n_atoms;
   int dev = 0, sms = 148;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int grid = grid_for(total_cand, 256, sms * 16);
   if (exact)
-    k_bin_transform<true><<<grid_for(total, 256, sms * 16), 256, 0, st>>>(p, d_x, b.cell_count, s.tmp_key,
-                                                                        s.tmp_cell, s.tmp_slot, s.tmp_f, s.counters);
+    k_bin_transform<true><<<grid, 256, 0, st>>>(d_jobs, n_jobs, total_cand, cap, b.cell_count, s.tmp_key, s.tmp_cell,
+                                                s.tmp_slot, s.tmp_f, s.counters);
   else
-    k_bin_transform<false><<<grid_for(total, 256, sms * 16), 256, 0, st>>>(p, d_x, b.cell_count, s.tmp_key,
-                                                                         s.tmp_cell, s.tmp_slot, s.tmp_f, s.counters);
-  const int nb = (int)((n_cells + kScanBlock - 1) / kScanBlock);
-  k_scan_blocks<<<nb, 256, 0, st>>>(b.cell_count, n_cells, s.block_sums, s.counters);
+    k_bin_transform<false><<<grid, 256, 0, st>>>(d_jobs, n_jobs, total_cand, cap, b.cell_count, s.tmp_key,
+                                                 s.tmp_cell, s.tmp_slot, s.tmp_f, s.counters);
+  const int nb = (int)((total_cells + kScanBlock - 1) / kScanBlock);
+  k_scan_blocks<<<nb, 256, 0, st>>>(b.cell_count, total_cells, s.block_sums, s.counters);
   k_scan_top<<<1, 1024, 0, st>>>(s.block_sums, nb);
-  k_scan_final<<<nb, 256, 0, st>>>(b.cell_count, n_cells, s.block_sums, b.cell_start);
-  k_bin_place<<<sms * 8, 256, 0, st>>>(s.tmp_cell, s.tmp_slot, b.cell_start, s.counters, p.cap, s.perm);
+  k_scan_final<<<nb, 256, 0, st>>>(b.cell_count, total_cells, s.block_sums, b.cell_start);
+  k_bin_place<<<sms * 8, 256, 0, st>>>(s.tmp_cell, s.tmp_slot, b.cell_start, s.counters, cap, s.perm);
   return cudaGetLastError();
 }
 
-cudaError_t launch_bin_finalize(const BinParams& p, Scratch& s, BinnedAtoms& b, int want_fp64, cudaStream_t st) {
+cudaError_t launch_bin_finalize(const BinParams* d_jobs, int n_jobs, int64_t total_cells, int64_t cap, Scratch& s,
+                                BinnedAtoms& b, int want_fp64, cudaStream_t st) {
   int dev = 0, sms = 148;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  k_bin_finalize<<<grid_for(p.n_cells, 128, sms * 16), 128, 0, st>>>(b.cell_start, b.cell_count, p.n_cells, p.Ex,
-                                                                     p.Ey, s.perm, s.tmp_key, s.tmp_f, p.a_col[0],
-                                                                     p.a_col[1], p.a_col[2], want_fp64, b,
-                                                                     s.counters, p.cap);
+  k_bin_finalize<<<grid_for(total_cells, 128, sms * 16), 128, 0, st>>>(d_jobs, n_jobs, b.cell_start, b.cell_count,
+                                                                       total_cells, s.perm, s.tmp_key, s.tmp_f,
+                                                                       want_fp64, b, s.counters, cap);
   return cudaGetLastError();
 }
 

@@ -230,23 +230,19 @@ __device__ __forceinline__ float rho_of(float r2min, float sig) {
 }
 
 template <bool kDensity>
-__device__ __forceinline__ Sample make_sample(float sr, float si, float r2min, float b0, float bg, float sig) {
+__device__ __forceinline__ Sample make_sample(float sr, float si, float r2min, float b0, float bg, float sig,
+                                              bool use_density) {
   const float inv = rsqrtf(fmaxf(fmaf(sr, sr, si * si), 1e-32f));  // x = S / max(1e-16, |S|)
-  const float rho = kDensity ? rho_of(r2min, sig) : 1.f;
+  const float rho = (kDensity && use_density) ? rho_of(r2min, sig) : 1.f;
   return Sample{b0 * rho, bg * rho * (sr * inv), bg * rho * (si * inv)};
 }
 
+// One warp tile of one image: the 8 x 4 columns of tile `tile` marched through
+// the depth.  Returns false when a slab overflows its staging (counters[4]).
 template <int NP, bool kDensity, bool kStats>
-__global__ void __launch_bounds__(kWarps * 32, (NP >= 16 ? 4 : 5)) k_column_fp32_v2(const __grid_constant__ ColumnParams p) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  WarpSmem& W = reinterpret_cast<WarpSmem*>(smem_raw)[warp];
-
-  const int Wd = p.ix1 - p.ix0, Hd = p.iy1 - p.iy0;
-  const int tiles_x = (Wd + kTileX - 1) / kTileX, tiles_y = (Hd + kTileY - 1) / kTileY;
-  const int tile = blockIdx.x * kWarps + warp;
-  if (tile >= tiles_x * tiles_y) return;
-  if ((int64_t)p.counters[0] > p.cap) return;  // the binning overflowed: the host retries
+__device__ __noinline__ bool column_tile(const ColumnParams& p, WarpSmem& W, int tile, int lane) {
+  const int Wd = p.ix1 - p.ix0;
+  const int tiles_x = (Wd + kTileX - 1) / kTileX;
   const int tx = tile % tiles_x, ty = tile / tiles_x;
   const int ix = p.ix0 + tx * kTileX + (lane & (kTileX - 1));
   const int iy = p.iy0 + ty * kTileY + lane / kTileX;
@@ -331,7 +327,7 @@ __global__ void __launch_bounds__(kWarps * 32, (NP >= 16 ? 4 : 5)) k_column_fp32
     }
     if (!ok) {
       if (lane == 0) atomicExch(&p.counters[4], 1ull);
-      return;  // the host recomputes the image with the general kernel
+      return false;  // the host recomputes the image with the general kernel
     }
     // two accumulator sets (even / odd candidates) for instruction-level parallelism;
     // .x is slice z0, .y slice z0 + 1
@@ -396,7 +392,7 @@ __global__ void __launch_bounds__(kWarps * 32, (NP >= 16 ? 4 : 5)) k_column_fp32
     const float2 sr = __fadd2_rn(srA, srB), si = __fadd2_rn(siA, siB);
     const float rm0 = fminf(rmA.x, rmB.x) * r2_to_A2, rm1 = fminf(rmA.y, rmB.y) * r2_to_A2;
     // field samples z0 (even) and z0 + 1 (odd), then the RK4 double step (z0-2, z0-1, z0)
-    const Sample s0 = make_sample<kDensity>(sr.x, si.x, rm0, b0, bg, sig);
+    const Sample s0 = make_sample<kDensity>(sr.x, si.x, rm0, b0, bg, sig, p.use_density != 0);
     if (z0 == 0) {
       s_first = s0;
     } else {
@@ -405,7 +401,7 @@ __global__ void __launch_bounds__(kWarps * 32, (NP >= 16 ? 4 : 5)) k_column_fp32
         if (k < np) rk4(s_prev, s_mid, s0, aa[k], dzs, ph[k]);
     }
     s_prev = s0;
-    if (has1) s_mid = make_sample<kDensity>(sr.y, si.y, rm1, b0, bg, sig);
+    if (has1) s_mid = make_sample<kDensity>(sr.y, si.y, rm1, b0, bg, sig, p.use_density != 0);
   }
   if ((p.Mz & 1) == 0) {  // closure x(Mz) = x(0)
 #pragma unroll
@@ -431,35 +427,82 @@ __global__ void __launch_bounds__(kWarps * 32, (NP >= 16 ? 4 : 5)) k_column_fp32
       atomicAdd(&p.counters[3], acc_w);
     }
   }
+  return true;
+}
+
+// Persistent launch over the warp tiles of every job of a batch: each warp
+// takes the next tile from a global counter, so images of uneven size share
+// the GPU without a tail per image.
+template <int NP, bool kDensity, bool kStats>
+__global__ void __launch_bounds__(kWarps * 32, (NP >= 16 ? 4 : 5))
+    k_column_fp32_v2(const ColumnJob* __restrict__ jobs, int n_jobs, int total_tiles, unsigned* __restrict__ work,
+                     const unsigned long long* __restrict__ counters, int64_t cap) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  WarpSmem& W = reinterpret_cast<WarpSmem*>(smem_raw)[warp];
+  if ((int64_t)counters[0] > cap) return;  // the binning overflowed: the host retries
+  for (;;) {
+    int tile = 0;
+    if (lane == 0) tile = (int)atomicAdd(work, 1u);
+    tile = __shfl_sync(0xffffffffu, tile, 0);
+    if (tile >= total_tiles) break;
+    if (counters[4] != 0) break;  // a slab overflowed: the batch is recomputed image by image
+    int lo = 0, hi = n_jobs - 1;  // job of this tile
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (jobs[mid].tile_base <= tile)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    if (!column_tile<NP, kDensity, kStats>(jobs[lo].p, W, tile - jobs[lo].tile_base, lane)) break;
+  }
 }
 
 template <typename K>
-cudaError_t launch(K kernel, const ColumnParams& p, cudaStream_t st) {
-  const int Wd = p.ix1 - p.ix0, Hd = p.iy1 - p.iy0;
-  const int tiles = ((Wd + kTileX - 1) / kTileX) * ((Hd + kTileY - 1) / kTileY);
-  const int grid = (tiles + kWarps - 1) / kWarps;
+cudaError_t launch(K kernel, const ColumnJob* jobs, int n_jobs, int total_tiles, unsigned* work,
+                   const unsigned long long* counters, int64_t cap, int blocks_per_sm, cudaStream_t st) {
   const size_t smem = sizeof(WarpSmem) * kWarps;
   cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  kernel<<<grid, kWarps * 32, smem, st>>>(p);
+  int dev = 0, sms = 148;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int grid = sms * blocks_per_sm;
+  const int need = (total_tiles + kWarps - 1) / kWarps;
+  if (grid > need) grid = need;
+  if (grid < 1) grid = 1;
+  kernel<<<grid, kWarps * 32, smem, st>>>(jobs, n_jobs, total_tiles, work, counters, cap);
   return cudaGetLastError();
+}
+
+template <bool kDensity, bool kStats>
+cudaError_t launch_np(int np, const ColumnJob* jobs, int n_jobs, int total_tiles, unsigned* work,
+                      const unsigned long long* counters, int64_t cap, cudaStream_t st) {
+  if (np <= 1) return launch(k_column_fp32_v2<1, kDensity, kStats>, jobs, n_jobs, total_tiles, work, counters, cap, 5, st);
+  if (np <= 2) return launch(k_column_fp32_v2<2, kDensity, kStats>, jobs, n_jobs, total_tiles, work, counters, cap, 5, st);
+  if (np <= 4) return launch(k_column_fp32_v2<4, kDensity, kStats>, jobs, n_jobs, total_tiles, work, counters, cap, 5, st);
+  if (np <= 8) return launch(k_column_fp32_v2<8, kDensity, kStats>, jobs, n_jobs, total_tiles, work, counters, cap, 5, st);
+  return launch(k_column_fp32_v2<16, kDensity, kStats>, jobs, n_jobs, total_tiles, work, counters, cap, 4, st);
 }
 
 }  // namespace
 
-template <bool kDensity, bool kStats>
-cudaError_t launch_np(const ColumnParams& p, cudaStream_t st) {
-  const int np = p.n_prec - p.prec_offset;
-  if (np <= 1) return launch(k_column_fp32_v2<1, kDensity, kStats>, p, st);
-  if (np <= 2) return launch(k_column_fp32_v2<2, kDensity, kStats>, p, st);
-  if (np <= 4) return launch(k_column_fp32_v2<4, kDensity, kStats>, p, st);
-  if (np <= 8) return launch(k_column_fp32_v2<8, kDensity, kStats>, p, st);
-  return launch(k_column_fp32_v2<16, kDensity, kStats>, p, st);
+int column_tiles(const ColumnParams& p) {
+  const int Wd = p.ix1 - p.ix0, Hd = p.iy1 - p.iy0;
+  if (Wd <= 0 || Hd <= 0) return 0;
+  return ((Wd + kTileX - 1) / kTileX) * ((Hd + kTileY - 1) / kTileY);
 }
 
-cudaError_t launch_column_fp32_v2(const ColumnParams& p, cudaStream_t st) {
-  if (p.use_density) return p.want_stats ? launch_np<true, true>(p, st) : launch_np<true, false>(p, st);
-  return p.want_stats ? launch_np<false, true>(p, st) : launch_np<false, false>(p, st);
+cudaError_t launch_column_fp32_ring(const ColumnJob* d_jobs, int n_jobs, int total_tiles, int max_np, bool density,
+                                    bool stats, unsigned* work, const unsigned long long* counters, int64_t cap,
+                                    cudaStream_t st) {
+  cudaMemsetAsync(work, 0, sizeof(unsigned), st);
+  if (total_tiles <= 0) return cudaSuccess;
+  if (density) return stats ? launch_np<true, true>(max_np, d_jobs, n_jobs, total_tiles, work, counters, cap, st)
+                            : launch_np<true, false>(max_np, d_jobs, n_jobs, total_tiles, work, counters, cap, st);
+  return stats ? launch_np<false, true>(max_np, d_jobs, n_jobs, total_tiles, work, counters, cap, st)
+               : launch_np<false, false>(max_np, d_jobs, n_jobs, total_tiles, work, counters, cap, st);
 }
 
 }  // namespace stem

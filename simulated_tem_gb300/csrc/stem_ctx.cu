@@ -1,12 +1,15 @@
-// libstem C ABI: context, device memory and the image / blur entry points.
+// libstem C ABI: context, device memory and the image / batch / blur entry points.
 //
-// st_image replaces the patch loop of computeD2BI_img
+// An image replaces the patch loop of computeD2BI_img
 // (src/Lib_DynamicalTwoBeamImaging.f90:1842-1946): K1 bins the atoms
 // (findGdotR), K2+K3 compute the voxel field and integrate every column, and
 // an epilogue applies the optional average over precession angles and the
-// bright-field flip.  st_blur is gaussianBlurImage (src/d2bi.f90:1543-1624).
+// bright-field flip.  A batch runs K1 once over the candidates of all its
+// images and K2+K3 as one persistent launch over all their warp tiles.
+// st_blur is gaussianBlurImage (src/d2bi.f90:1543-1624).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -34,13 +37,18 @@ struct st_ctx {
   size_t cap_blur = 0;
   double* d_kern = nullptr;
   size_t cap_kern = 0;
+  BinParams* d_binjobs = nullptr;
+  size_t cap_binjobs = 0;
+  ColumnJob* d_coljobs = nullptr;
+  size_t cap_coljobs = 0;
+  unsigned* d_work = nullptr;
   unsigned long long* h_counters = nullptr;  // pinned
-  void* h_stage = nullptr;                   // pinned staging for tables
+  void* h_stage = nullptr;                   // pinned staging for tables and job descriptors
   size_t cap_stage = 0;
   cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
   st_stats stats{};
-  int64_t last_kept = 0;  // kept atoms of the previous image: sizes the next one
-  bool fp32_general = false;  // STEM_FP32_KERNEL=general: always use k_column_fp32
+  int64_t last_kept = 0;       // kept atoms of the previous call: sizes the next one
+  bool fp32_general = false;   // STEM_FP32_KERNEL=general: always use k_column_fp32
   int last_column_kernel = 0;  // 1 general FP32, 2 slab-ring FP32, 3 FP64
 };
 
@@ -141,6 +149,380 @@ int validate(st_ctx* c, const st_geom* g, int64_t ldx, int64_t nAtoms, int32_t n
   return ST_OK;
 }
 
+// One image of a call, as the host sees it.
+struct Job {
+  const st_geom* g;
+  const double* d_x;
+  int64_t ldx, n_atoms;
+  const double* aa;  // host
+  int n_prec;
+  double* d_img;
+};
+
+BinParams bin_params(const Job& j, int64_t cand_base, int64_t cell_base) {
+  const st_geom* g = j.g;
+  BinParams bp;
+  memset(&bp, 0, sizeof bp);
+  bp.n_atoms = j.n_atoms;
+  bp.ldx = j.ldx;
+  bp.x = j.d_x;
+  bp.cand_base = cand_base;
+  bp.cell_base = cell_base;
+  bp.nuvw = g->nuvw;
+  bp.Ex = g->Ex;
+  bp.Ey = g->Ey;
+  bp.Ez = g->Ez;
+  bp.n_cells = (int64_t)g->Ex * g->Ey * g->Ez;
+  memcpy(bp.RU, g->RU, sizeof bp.RU);
+  memcpy(bp.delta, g->delta, sizeof bp.delta);
+  memcpy(bp.Ruvw, g->Ruvw, sizeof bp.Ruvw);
+  memcpy(bp.lc_delta, g->lc_delta, sizeof bp.lc_delta);
+  memcpy(bp.ia, g->ia_col, sizeof bp.ia);
+  memcpy(bp.g, g->g, sizeof bp.g);
+  bp.a_col[0] = g->a_col[0];
+  bp.a_col[1] = g->a_col[4];
+  bp.a_col[2] = g->a_col[8];
+  for (int i = 0; i < 9; ++i) bp.RUf[i] = (float)g->RU[i];
+  for (int i = 0; i < 81; ++i) bp.Ruvwf[i] = (float)g->Ruvw[i];
+  for (int i = 0; i < 3; ++i) bp.shiftf[i] = (float)(g->delta[i] - g->lc_delta[i]);
+  bp.iaf[0] = (float)g->ia_col[0];
+  bp.iaf[1] = (float)g->ia_col[4];
+  bp.iaf[2] = (float)g->ia_col[8];
+  return bp;
+}
+
+// The records of the kept atoms (reallocated when a call keeps more atoms than they hold).
+void point_at_kept(const st_ctx* c, ColumnParams& cp) {
+  cp.f64 = c->b.f64;
+  cp.cs64 = c->b.cs64;
+  cp.p32 = c->b.p32;
+  cp.cs32 = c->b.cs32;
+}
+
+ColumnParams column_params(st_ctx* c, const Job& j, int64_t cell_base, size_t xoff, size_t yoff, size_t zoff,
+                           size_t aoff, int flags) {
+  const st_geom* g = j.g;
+  ColumnParams cp;
+  memset(&cp, 0, sizeof cp);
+  cp.Mx = g->Mx;
+  cp.My = g->My;
+  cp.Mz = g->Mz;
+  cp.ix0 = g->ix0;
+  cp.ix1 = g->ix1;
+  cp.iy0 = g->iy0;
+  cp.iy1 = g->iy1;
+  cp.Ex = g->Ex;
+  cp.Ey = g->Ey;
+  cp.Ez = g->Ez;
+  cp.n_prec = j.n_prec;
+  cp.use_density = g->useDensity;
+  cp.want_stats = (flags & ST_FLAG_STATS) ? 1 : 0;
+  cp.a11 = g->a_col[0];
+  cp.a22 = g->a_col[4];
+  cp.a33 = g->a_col[8];
+  cp.cut2 = (3 * g->sigma) * (3 * g->sigma);
+  cp.i2s2 = 1 / (2 * g->sigma * g->sigma);
+  cp.sigma = g->sigma;
+  cp.b0 = g->b0;
+  cp.bg = g->bg;
+  cp.dz = g->deltaz;
+  // link cells narrower than 3 sigma truncate the search to 27 cells: test the cell offsets too
+  const double r3 = 3 * g->sigma * (1.0 + 1e-6) + 1e-6;
+  cp.check_cells = (cp.a11 < r3 || cp.a22 < r3 || cp.a33 < r3) ? 1 : 0;
+  cp.cell_start = c->b.cell_start + cell_base;
+  point_at_kept(c, cp);
+  cp.xtab = c->s.xtab + xoff;
+  cp.xfv = c->s.xfv + xoff;
+  cp.ytab = c->s.ytab + yoff;
+  cp.yfv = c->s.yfv + yoff;
+  cp.ztab = c->s.ztab + zoff;
+  cp.zfv = c->s.zfv + zoff;
+  cp.aa = c->s.aa + aoff;
+  cp.aaf = c->s.aaf + aoff;
+  cp.img = j.d_img;
+  cp.counters = c->s.counters;
+  return cp;
+}
+
+// The slab-ring FP32 kernel needs cells of at least 3 sigma (no truncated
+// search) and at least one voxel thick in z.
+bool ring_eligible(const ColumnParams& cp) { return !cp.check_cells && cp.Ez <= cp.Mz; }
+
+// Image the jobs: binning of all, then the column kernels, then the epilogues.
+int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStream_t st) {
+  const int n = (int)jobs.size();
+  const bool fp32 = (flags & ST_FLAG_FP32) != 0;
+  // concatenation offsets
+  std::vector<int64_t> cand_base(n + 1, 0), cell_base(n + 1, 0);
+  std::vector<size_t> xoff(n + 1, 0), yoff(n + 1, 0), zoff(n + 1, 0), aoff(n + 1, 0);
+  for (int i = 0; i < n; ++i) {
+    const st_geom* g = jobs[i].g;
+    cand_base[i + 1] = cand_base[i] + (int64_t)g->nuvw * jobs[i].n_atoms;
+    cell_base[i + 1] = cell_base[i] + (int64_t)g->Ex * g->Ey * g->Ez;
+    xoff[i + 1] = xoff[i] + g->Mx;
+    yoff[i + 1] = yoff[i] + g->My;
+    zoff[i + 1] = zoff[i] + g->Mz;
+    aoff[i + 1] = aoff[i] + jobs[i].n_prec;
+  }
+  const int64_t total_cand = cand_base[n], total_cells = cell_base[n];
+  if (total_cand >= 2147483647LL) return fail(c, ST_ERR_ARG, "a call holds more than 2^31 - 1 candidates");
+  if (total_cells >= 2147483647LL) return fail(c, ST_ERR_ARG, "a call holds more than 2^31 - 1 link cells");
+
+  // ---- device buffers that do not depend on the kept-atom count
+  cudaError_t e = cudaSuccess;
+  {
+    size_t cc = c->cap_cells;
+    e = ensure(c->b.cell_start, cc, (size_t)total_cells + 1);
+    cc = c->cap_cells;
+    if (e == cudaSuccess) e = ensure(c->b.cell_count, cc, (size_t)total_cells + 1);
+    size_t nb = c->s.cap_blocks;
+    if (e == cudaSuccess) e = ensure(c->s.block_sums, nb, (size_t)(total_cells / 1024 + 2));
+    if (e != cudaSuccess) return cuda_fail(c, e, "allocating cell buffers");
+    c->cap_cells = cc;
+    c->s.cap_blocks = nb;
+    if (!c->s.counters) {
+      e = cudaMalloc((void**)&c->s.counters, 8 * sizeof(unsigned long long));
+      if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_work, sizeof(unsigned));
+      if (e != cudaSuccess) return cuda_fail(c, e, "allocating counters");
+    }
+    size_t cx = c->s.cap_x;
+    e = ensure(c->s.xtab, cx, xoff[n]);
+    cx = c->s.cap_x;
+    if (e == cudaSuccess) e = ensure(c->s.xfv, cx, xoff[n]);
+    size_t cy = c->s.cap_y;
+    if (e == cudaSuccess) e = ensure(c->s.ytab, cy, yoff[n]);
+    cy = c->s.cap_y;
+    if (e == cudaSuccess) e = ensure(c->s.yfv, cy, yoff[n]);
+    size_t cz = c->s.cap_z;
+    if (e == cudaSuccess) e = ensure(c->s.ztab, cz, zoff[n]);
+    cz = c->s.cap_z;
+    if (e == cudaSuccess) e = ensure(c->s.zfv, cz, zoff[n]);
+    size_t cp = c->s.cap_prec;
+    if (e == cudaSuccess) e = ensure(c->s.aa, cp, aoff[n]);
+    cp = c->s.cap_prec;
+    if (e == cudaSuccess) e = ensure(c->s.aaf, cp, aoff[n]);
+    if (e != cudaSuccess) return cuda_fail(c, e, "allocating tables");
+    c->s.cap_x = cx;
+    c->s.cap_y = cy;
+    c->s.cap_z = cz;
+    c->s.cap_prec = cp;
+  }
+
+  // ---- kept-atom arrays: sized by what the previous call kept, else 4 atoms per input atom.
+  // They are allocated before the column parameters, which point into them.
+  int64_t n_atoms_all = 0;
+  for (const Job& j : jobs) n_atoms_all += j.n_atoms;
+  int64_t cap = c->last_kept > 0 ? c->last_kept + c->last_kept / 4 + 65536 : 4 * n_atoms_all + 65536;
+  if (cap > total_cand + 1) cap = total_cand + 1;
+  if (!alloc_kept(c, (size_t)cap)) return cuda_fail(c, cudaErrorMemoryAllocation, "allocating binning buffers");
+
+  // ---- column parameters. On the FP32 path every image whose link cells allow it goes
+  // to the persistent slab-ring kernel (passes of 16 precession angles); the others,
+  // and every image of the FP64 path, get per-image launches.
+  std::vector<ColumnParams> cps(n);
+  std::vector<int> ring_jobs;  // images of the persistent launch
+  std::vector<char> on_ring(n, 0);
+  bool dens = false;
+  int max_np = 1, ring_np = 1;
+  for (int i = 0; i < n; ++i) {
+    cps[i] = column_params(c, jobs[i], cell_base[i], xoff[i], yoff[i], zoff[i], aoff[i], flags);
+    max_np = std::max(max_np, jobs[i].n_prec);
+    if (fp32 && !c->fp32_general && ring_eligible(cps[i])) {
+      on_ring[i] = 1;
+      ring_jobs.push_back(i);
+      dens = dens || cps[i].use_density;
+      ring_np = std::max(ring_np, jobs[i].n_prec);
+    }
+  }
+  const bool ring = !ring_jobs.empty();
+  const int n_ring = (int)ring_jobs.size();
+  const int width = fp32 ? 16 : 4;
+  const int passes = (ring_np + width - 1) / width;
+  std::vector<ColumnJob> cj;
+  std::vector<int> pass_tiles(passes, 0);
+  if (ring) {
+    // the density variant of the kernel serves every image of the launch when any image uses it;
+    // an image without the density field then gets rho = 1 from use_density = 0 in the sample
+    cj.resize((size_t)n_ring * passes);
+    for (int pass = 0; pass < passes; ++pass) {
+      int tiles = 0;
+      for (int r = 0; r < n_ring; ++r) {
+        ColumnJob& J = cj[(size_t)pass * n_ring + r];
+        J.p = cps[ring_jobs[r]];
+        J.p.prec_offset = pass * width;
+        J.p.accumulate = pass > 0 ? 1 : 0;
+        J.tile_base = tiles;
+        J.pad = 0;
+        if (J.p.prec_offset < J.p.n_prec) tiles += column_tiles(J.p);  // fewer angles: no tiles this pass
+      }
+      pass_tiles[pass] = tiles;
+    }
+  }
+
+  // ---- per-image tables and job descriptors, staged through pinned memory
+  const size_t tab_bytes = (xoff[n] + yoff[n] + zoff[n]) * (sizeof(int2) + sizeof(double)) + aoff[n] * 12;
+  const size_t job_bytes = (size_t)n * sizeof(BinParams) + cj.size() * sizeof(ColumnJob);
+  e = ensure_host(c->h_stage, c->cap_stage, tab_bytes + job_bytes + 256);
+  if (e == cudaSuccess) e = ensure(c->d_binjobs, c->cap_binjobs, (size_t)n);
+  if (e == cudaSuccess && !cj.empty()) e = ensure(c->d_coljobs, c->cap_coljobs, cj.size());
+  if (e != cudaSuccess) return cuda_fail(c, e, "allocating job descriptors");
+  cudaStreamSynchronize(st);  // the staging buffer may still feed a previous call's copies
+  unsigned char* hp = (unsigned char*)c->h_stage;
+  int2* hxt = (int2*)hp;
+  int2* hyt = hxt + xoff[n];
+  int2* hzt = hyt + yoff[n];
+  double* hxf = (double*)(hzt + zoff[n]);
+  double* hyf = hxf + xoff[n];
+  double* hzf = hyf + yoff[n];
+  double* haa = hzf + zoff[n];
+  float* haaf = (float*)(haa + aoff[n]);
+  unsigned char* hjobs = (unsigned char*)(((uintptr_t)(haaf + aoff[n]) + 63) & ~(uintptr_t)63);
+  BinParams* hbp = (BinParams*)hjobs;
+  ColumnJob* hcj = (ColumnJob*)(hjobs + (size_t)n * sizeof(BinParams));
+  for (int i = 0; i < n; ++i) {
+    const st_geom* g = jobs[i].g;
+    axis_table(g->Mx, g->a_vox[0], g->lc_delta[0], g->ia_col[0], g->Ex, hxt + xoff[i], hxf + xoff[i]);
+    axis_table(g->My, g->a_vox[4], g->lc_delta[1], g->ia_col[4], g->Ey, hyt + yoff[i], hyf + yoff[i]);
+    axis_table(g->Mz, g->a_vox[8], g->lc_delta[2], g->ia_col[8], g->Ez, hzt + zoff[i], hzf + zoff[i]);
+    for (int k = 0; k < jobs[i].n_prec; ++k) {
+      haa[aoff[i] + k] = jobs[i].aa[k];
+      haaf[aoff[i] + k] = (float)jobs[i].aa[k];
+    }
+    hbp[i] = bin_params(jobs[i], cand_base[i], cell_base[i]);
+  }
+  for (size_t k = 0; k < cj.size(); ++k) hcj[k] = cj[k];
+  cudaMemcpyAsync(c->s.xtab, hxt, xoff[n] * sizeof(int2), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(c->s.ytab, hyt, yoff[n] * sizeof(int2), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(c->s.ztab, hzt, zoff[n] * sizeof(int2), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(c->s.xfv, hxf, xoff[n] * sizeof(double), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(c->s.yfv, hyf, yoff[n] * sizeof(double), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(c->s.zfv, hzf, zoff[n] * sizeof(double), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(c->s.aa, haa, aoff[n] * sizeof(double), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(c->s.aaf, haaf, aoff[n] * sizeof(float), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(c->d_binjobs, hbp, (size_t)n * sizeof(BinParams), cudaMemcpyHostToDevice, st);
+  if (!cj.empty()) cudaMemcpyAsync(c->d_coljobs, hcj, cj.size() * sizeof(ColumnJob), cudaMemcpyHostToDevice, st);
+
+  // ---- per-image column launches (general FP32 or FP64 kernel), epilogues, image clearing
+  auto columns_per_image = [&](int64_t kept_cap, bool all) -> cudaError_t {
+    cudaError_t ce = cudaSuccess;
+    for (int i = 0; i < n && ce == cudaSuccess; ++i) {
+      if (on_ring[i] && !all) continue;
+      ColumnParams cp = cps[i];
+      cp.cap = kept_cap;
+      if (cp.ix1 <= cp.ix0 || cp.iy1 <= cp.iy0) continue;
+      for (int off = 0; off < cp.n_prec && ce == cudaSuccess; off += width) {
+        cp.prec_offset = off;
+        cp.accumulate = off > 0 ? 1 : 0;
+        ce = fp32 ? launch_column_fp32(cp, st) : launch_column_fp64(cp, st);
+      }
+    }
+    return ce;
+  };
+  auto epilogues = [&]() -> cudaError_t {
+    cudaError_t ce = cudaSuccess;
+    if (!(flags & ST_FLAG_AVERAGE)) return ce;
+    for (int i = 0; i < n && ce == cudaSuccess; ++i) {
+      const st_geom* g = jobs[i].g;
+      if (g->ix1 <= g->ix0 || g->iy1 <= g->iy0) continue;
+      ce = launch_epilogue(jobs[i].d_img, g->Mx, g->My, g->ix0, g->ix1, g->iy0, g->iy1, (double)jobs[i].n_prec,
+                           (flags & ST_FLAG_BRIGHT) ? 1 : 0, st);
+    }
+    return ce;
+  };
+  auto clear_images = [&]() -> cudaError_t {
+    cudaError_t ce = cudaSuccess;
+    for (int i = 0; i < n && ce == cudaSuccess; ++i)
+      ce = cudaMemsetAsync(jobs[i].d_img, 0, sizeof(double) * (size_t)jobs[i].g->Mx * jobs[i].g->My, st);
+    return ce;
+  };
+
+  bool used_ring = ring;
+  for (int attempt = 0;; ++attempt) {
+    if (attempt > 0) {
+      // grown kept-atom arrays move: point the column parameters and the ring's job table at them
+      // (the previous attempt ended with a stream synchronisation, so the staging buffer is free)
+      if (!alloc_kept(c, (size_t)cap)) return cuda_fail(c, cudaErrorMemoryAllocation, "allocating binning buffers");
+      for (ColumnParams& cp : cps) point_at_kept(c, cp);
+      for (size_t k = 0; k < cj.size(); ++k) point_at_kept(c, hcj[k].p);
+      if (!cj.empty()) {
+        e = cudaMemcpyAsync(c->d_coljobs, hcj, cj.size() * sizeof(ColumnJob), cudaMemcpyHostToDevice, st);
+        if (e != cudaSuccess) return cuda_fail(c, e, "copying column jobs");
+      }
+    }
+    cudaEventRecord(c->ev[0], st);
+    e = launch_bin(c->d_binjobs, n, total_cand, total_cells, cap, c->s, c->b, !fp32, st);
+    if (e == cudaSuccess) e = launch_bin_finalize(c->d_binjobs, n, total_cells, cap, c->s, c->b, fp32 ? 0 : 1, st);
+    if (e != cudaSuccess) return cuda_fail(c, e, "binning launch");
+    e = clear_images();
+    if (e != cudaSuccess) return cuda_fail(c, e, "clearing images");
+    cudaEventRecord(c->ev[1], st);
+    used_ring = ring;
+    for (int pass = 0; ring && pass < passes && e == cudaSuccess; ++pass)
+      e = launch_column_fp32_ring(c->d_coljobs + (size_t)pass * n_ring, n_ring, pass_tiles[pass],
+                                  std::min(width, ring_np - pass * width), dens, (flags & ST_FLAG_STATS) != 0,
+                                  c->d_work, c->s.counters, cap, st);
+    if (e == cudaSuccess && n_ring < n) e = columns_per_image(cap, false);
+    if (e == cudaSuccess) e = epilogues();
+    if (e != cudaSuccess) return cuda_fail(c, e, "column kernel launch");
+    cudaEventRecord(c->ev[2], st);
+    e = cudaMemcpyAsync(c->h_counters, c->s.counters, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(c, e, "image kernels");
+    if ((int64_t)c->h_counters[0] > cap) {
+      if (attempt > 0) return fail(c, ST_ERR_ALLOC, "binning capacity did not converge");
+      cap = (int64_t)c->h_counters[0] + (int64_t)c->h_counters[0] / 8 + 1024;  // grow and redo
+      continue;
+    }
+    if (ring && c->h_counters[4] != 0) {
+      // a slab held more atoms than the ring kernel stages: recompute every image with the general kernel
+      used_ring = false;
+      cudaMemsetAsync(c->s.counters + 2, 0, 3 * sizeof(unsigned long long), st);
+      e = clear_images();
+      if (e == cudaSuccess) e = columns_per_image(cap, true);
+      if (e == cudaSuccess) e = epilogues();
+      cudaEventRecord(c->ev[2], st);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(c->h_counters, c->s.counters, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                            st);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+      if (e != cudaSuccess) return cuda_fail(c, e, "image kernels (general FP32 kernel)");
+    }
+    break;
+  }
+  c->last_kept = (int64_t)c->h_counters[0];
+  c->last_column_kernel = !fp32 ? 3 : (used_ring ? 2 : 1);
+
+  st_stats& S = c->stats;
+  memset(&S, 0, sizeof S);
+  S.n_atoms = n_atoms_all;
+  S.n_kept = (int64_t)c->h_counters[0];
+  S.max_cell_count = (int32_t)c->h_counters[1];
+  S.n_tests = (int64_t)c->h_counters[2];
+  S.n_accepted = (int64_t)c->h_counters[3];
+  for (const Job& j : jobs) S.n_voxels += (int64_t)(j.g->ix1 - j.g->ix0) * (j.g->iy1 - j.g->iy0) * j.g->Mz;
+  S.n_prec = max_np;
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]);
+  S.ms_bin = ms;
+  cudaEventElapsedTime(&ms, c->ev[1], c->ev[2]);
+  S.ms_column = ms;
+  S.column_kernel = c->last_column_kernel;
+  // the reference stops when a link cell needs more than 16 x nMax0 slots; a batch's
+  // largest cell is checked against the smallest nMax0 of its images
+  int min_nmax0 = 0;
+  for (const Job& j : jobs)
+    if (j.g->nMax0 > 0 && (min_nmax0 == 0 || j.g->nMax0 < min_nmax0)) min_nmax0 = j.g->nMax0;
+  if (min_nmax0 > 0 && S.max_cell_count > 16 * min_nmax0) {
+    char buf[256];
+    snprintf(buf, sizeof buf,
+             "a link cell holds %d atoms, more than 16 x nMax0 = %d (the reference stops in "
+             "Lib_LinkCell3d::add0 here)",
+             S.max_cell_count, 16 * min_nmax0);
+    return fail(c, ST_ERR_CAPACITY, buf);
+  }
+  return ST_OK;
+}
+
 }  // namespace
 
 extern "C" int st_create(st_ctx** out, int device) {
@@ -156,12 +538,12 @@ extern "C" int st_create(st_ctx** out, int device) {
   e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaMallocHost((void**)&c->h_counters, 8 * sizeof(unsigned long long));
   for (int i = 0; i < 3 && e == cudaSuccess; ++i) e = cudaEventCreate(&c->ev[i]);
-  const char* kv = std::getenv("STEM_FP32_KERNEL");
-  c->fp32_general = kv && std::strcmp(kv, "general") == 0;
   if (e != cudaSuccess) {
     delete c;
     return ST_ERR_CUDA;
   }
+  const char* kv = std::getenv("STEM_FP32_KERNEL");
+  c->fp32_general = kv && std::strcmp(kv, "general") == 0;
   *out = c;
   return ST_OK;
 }
@@ -173,7 +555,7 @@ extern "C" void st_destroy(st_ctx* c) {
   void* dev_ptrs[] = {c->s.tmp_key, c->s.tmp_cell, c->s.tmp_slot, c->s.tmp_f, c->s.perm, c->s.block_sums,
                       c->s.counters, c->s.xtab, c->s.xfv, c->s.ytab, c->s.yfv, c->s.ztab, c->s.zfv, c->s.aa,
                       c->s.aaf, c->b.cell_start, c->b.cell_count, c->b.f64, c->b.cs64, c->b.p32, c->b.cs32,
-                      c->d_x, c->d_img, c->d_blur, c->d_kern};
+                      c->d_x, c->d_img, c->d_blur, c->d_kern, c->d_binjobs, c->d_coljobs, c->d_work};
   for (void* p : dev_ptrs)
     if (p) cudaFree(p);
   if (c->h_counters) cudaFreeHost(c->h_counters);
@@ -200,232 +582,29 @@ extern "C" int st_image_device(st_ctx* c, const st_geom* g, const double* d_x, i
   if (!aa || !d_img || (nAtoms > 0 && !d_x)) return fail(c, ST_ERR_ARG, "null buffer");
   cudaSetDevice(c->device);
   cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
-  const bool fp32 = (flags & ST_FLAG_FP32) != 0;
-  const int64_t n_cells = (int64_t)g->Ex * g->Ey * g->Ez;
-  const int Mx = g->Mx, My = g->My, Mz = g->Mz;
+  std::vector<Job> jobs{Job{g, d_x, ldx, nAtoms, aa, nPrec, d_img}};
+  return run_images(c, jobs, flags, st);
+}
 
-  // ---- device buffers that do not depend on the kept-atom count
-  cudaError_t e = cudaSuccess;
-  {
-    size_t cc = c->cap_cells;
-    e = ensure(c->b.cell_start, cc, (size_t)n_cells + 1);
-    cc = c->cap_cells;
-    if (e == cudaSuccess) e = ensure(c->b.cell_count, cc, (size_t)n_cells + 1);
-    size_t nb = c->s.cap_blocks;
-    if (e == cudaSuccess) e = ensure(c->s.block_sums, nb, (size_t)(n_cells / 1024 + 2));
-    if (e != cudaSuccess) return cuda_fail(c, e, "allocating cell buffers");
-    c->cap_cells = cc;
-    c->s.cap_blocks = nb;
-    if (!c->s.counters) {
-      e = cudaMalloc((void**)&c->s.counters, 8 * sizeof(unsigned long long));
-      if (e != cudaSuccess) return cuda_fail(c, e, "allocating counters");
+extern "C" int st_batch_device(st_ctx* c, int32_t n_jobs, const st_job* jobs, int32_t flags, void* stream) {
+  if (!c) return ST_ERR_ARG;
+  if (n_jobs < 1 || !jobs) return fail(c, ST_ERR_ARG, "a batch needs at least one job");
+  std::vector<Job> js;
+  js.reserve(n_jobs);
+  for (int i = 0; i < n_jobs; ++i) {
+    const st_job& j = jobs[i];
+    int rc = validate(c, j.geom, j.ldx, j.nAtoms, j.nPrec);
+    if (rc != ST_OK) {
+      c->err = "job " + std::to_string(i) + ": " + c->err;
+      return rc;
     }
-    size_t cx = c->s.cap_x;
-    e = ensure(c->s.xtab, cx, (size_t)Mx);
-    cx = c->s.cap_x;
-    if (e == cudaSuccess) e = ensure(c->s.xfv, cx, (size_t)Mx);
-    size_t cy = c->s.cap_y;
-    if (e == cudaSuccess) e = ensure(c->s.ytab, cy, (size_t)My);
-    cy = c->s.cap_y;
-    if (e == cudaSuccess) e = ensure(c->s.yfv, cy, (size_t)My);
-    size_t cz = c->s.cap_z;
-    if (e == cudaSuccess) e = ensure(c->s.ztab, cz, (size_t)Mz);
-    cz = c->s.cap_z;
-    if (e == cudaSuccess) e = ensure(c->s.zfv, cz, (size_t)Mz);
-    size_t cp = c->s.cap_prec;
-    if (e == cudaSuccess) e = ensure(c->s.aa, cp, (size_t)nPrec);
-    cp = c->s.cap_prec;
-    if (e == cudaSuccess) e = ensure(c->s.aaf, cp, (size_t)nPrec);
-    if (e != cudaSuccess) return cuda_fail(c, e, "allocating tables");
-    c->s.cap_x = cx;
-    c->s.cap_y = cy;
-    c->s.cap_z = cz;
-    c->s.cap_prec = cp;
+    if (!j.aa || !j.d_img || (j.nAtoms > 0 && !j.d_x))
+      return fail(c, ST_ERR_ARG, "job " + std::to_string(i) + ": null buffer");
+    js.push_back(Job{j.geom, j.d_x, j.ldx, j.nAtoms, j.aa, j.nPrec, j.d_img});
   }
-
-  // ---- per-image tables, staged through pinned memory
-  const size_t stage_bytes = (size_t)(Mx + My + Mz) * (sizeof(int2) + sizeof(double)) + nPrec * 12 + 64;
-  e = ensure_host(c->h_stage, c->cap_stage, stage_bytes);
-  if (e != cudaSuccess) return cuda_fail(c, e, "allocating pinned staging");
-  cudaStreamSynchronize(st);  // the staging buffer may still feed a previous call's copies
-  unsigned char* hp = (unsigned char*)c->h_stage;
-  int2* hxt = (int2*)hp;
-  int2* hyt = hxt + Mx;
-  int2* hzt = hyt + My;
-  double* hxf = (double*)(hzt + Mz);
-  double* hyf = hxf + Mx;
-  double* hzf = hyf + My;
-  double* haa = hzf + Mz;
-  float* haaf = (float*)(haa + nPrec);
-  axis_table(Mx, g->a_vox[0], g->lc_delta[0], g->ia_col[0], g->Ex, hxt, hxf);
-  axis_table(My, g->a_vox[4], g->lc_delta[1], g->ia_col[4], g->Ey, hyt, hyf);
-  axis_table(Mz, g->a_vox[8], g->lc_delta[2], g->ia_col[8], g->Ez, hzt, hzf);
-  for (int k = 0; k < nPrec; ++k) {
-    haa[k] = aa[k];
-    haaf[k] = (float)aa[k];
-  }
-  cudaMemcpyAsync(c->s.xtab, hxt, Mx * sizeof(int2), cudaMemcpyHostToDevice, st);
-  cudaMemcpyAsync(c->s.ytab, hyt, My * sizeof(int2), cudaMemcpyHostToDevice, st);
-  cudaMemcpyAsync(c->s.ztab, hzt, Mz * sizeof(int2), cudaMemcpyHostToDevice, st);
-  cudaMemcpyAsync(c->s.xfv, hxf, Mx * sizeof(double), cudaMemcpyHostToDevice, st);
-  cudaMemcpyAsync(c->s.yfv, hyf, My * sizeof(double), cudaMemcpyHostToDevice, st);
-  cudaMemcpyAsync(c->s.zfv, hzf, Mz * sizeof(double), cudaMemcpyHostToDevice, st);
-  cudaMemcpyAsync(c->s.aa, haa, nPrec * sizeof(double), cudaMemcpyHostToDevice, st);
-  cudaMemcpyAsync(c->s.aaf, haaf, nPrec * sizeof(float), cudaMemcpyHostToDevice, st);
-
-  // ---- K1: binning
-  const size_t n_cand = (size_t)g->nuvw * (size_t)nAtoms;
-  BinParams bp;
-  memset(&bp, 0, sizeof bp);
-  bp.n_atoms = nAtoms;
-  bp.ldx = ldx;
-  bp.nuvw = g->nuvw;
-  bp.Ex = g->Ex;
-  bp.Ey = g->Ey;
-  bp.Ez = g->Ez;
-  bp.n_cells = n_cells;
-  memcpy(bp.RU, g->RU, sizeof bp.RU);
-  memcpy(bp.delta, g->delta, sizeof bp.delta);
-  memcpy(bp.Ruvw, g->Ruvw, sizeof bp.Ruvw);
-  memcpy(bp.lc_delta, g->lc_delta, sizeof bp.lc_delta);
-  memcpy(bp.ia, g->ia_col, sizeof bp.ia);
-  memcpy(bp.g, g->g, sizeof bp.g);
-  bp.a_col[0] = g->a_col[0];
-  bp.a_col[1] = g->a_col[4];
-  bp.a_col[2] = g->a_col[8];
-  for (int i = 0; i < 9; ++i) bp.RUf[i] = (float)g->RU[i];
-  for (int i = 0; i < 81; ++i) bp.Ruvwf[i] = (float)g->Ruvw[i];
-  for (int i = 0; i < 3; ++i) bp.shiftf[i] = (float)(g->delta[i] - g->lc_delta[i]);
-  bp.iaf[0] = (float)g->ia_col[0];
-  bp.iaf[1] = (float)g->ia_col[4];
-  bp.iaf[2] = (float)g->ia_col[8];
-
-  // kept-atom capacity: what the previous image kept, else 4 atoms per input atom
-  int64_t cap = c->last_kept > 0 ? c->last_kept + c->last_kept / 4 + 65536 : 4 * nAtoms + 65536;
-  if (cap > (int64_t)n_cand + 1) cap = (int64_t)n_cand + 1;
-  for (int attempt = 0;; ++attempt) {
-  if (!alloc_kept(c, (size_t)cap)) return cuda_fail(c, cudaErrorMemoryAllocation, "allocating binning buffers");
-  bp.cap = cap;
-  cudaEventRecord(c->ev[0], st);
-  e = launch_bin(bp, d_x, c->s, c->b, !fp32, st);
-  if (e == cudaSuccess) e = launch_bin_finalize(bp, c->s, c->b, fp32 ? 0 : 1, st);
-  if (e != cudaSuccess) return cuda_fail(c, e, "binning launch");
-
-  // ---- K2+K3: field and columns
-  e = cudaMemsetAsync(d_img, 0, sizeof(double) * (size_t)Mx * My, st);
-  if (e != cudaSuccess) return cuda_fail(c, e, "clearing image");
-  cudaEventRecord(c->ev[1], st);
-  ColumnParams cp;
-  memset(&cp, 0, sizeof cp);
-  cp.Mx = Mx;
-  cp.My = My;
-  cp.Mz = Mz;
-  cp.ix0 = g->ix0;
-  cp.ix1 = g->ix1;
-  cp.iy0 = g->iy0;
-  cp.iy1 = g->iy1;
-  cp.Ex = g->Ex;
-  cp.Ey = g->Ey;
-  cp.Ez = g->Ez;
-  cp.n_prec = nPrec;
-  cp.use_density = g->useDensity;
-  cp.want_stats = (flags & ST_FLAG_STATS) ? 1 : 0;
-  cp.a11 = g->a_col[0];
-  cp.a22 = g->a_col[4];
-  cp.a33 = g->a_col[8];
-  cp.cut2 = (3 * g->sigma) * (3 * g->sigma);
-  cp.i2s2 = 1 / (2 * g->sigma * g->sigma);
-  cp.sigma = g->sigma;
-  cp.b0 = g->b0;
-  cp.bg = g->bg;
-  cp.dz = g->deltaz;
-  // link cells narrower than 3 sigma truncate the search to 27 cells: test the cell offsets too
-  const double r3 = 3 * g->sigma * (1.0 + 1e-6) + 1e-6;
-  cp.check_cells = (cp.a11 < r3 || cp.a22 < r3 || cp.a33 < r3) ? 1 : 0;
-  cp.cell_start = c->b.cell_start;
-  cp.f64 = c->b.f64;
-  cp.cs64 = c->b.cs64;
-  cp.p32 = c->b.p32;
-  cp.cs32 = c->b.cs32;
-  cp.xtab = c->s.xtab;
-  cp.xfv = c->s.xfv;
-  cp.ytab = c->s.ytab;
-  cp.yfv = c->s.yfv;
-  cp.ztab = c->s.ztab;
-  cp.zfv = c->s.zfv;
-  cp.aa = c->s.aa;
-  cp.aaf = c->s.aaf;
-  cp.img = d_img;
-  cp.counters = c->s.counters;
-  cp.cap = cap;
-  // the slab-ring FP32 kernel needs cells of at least 3 sigma (no truncated search) and at
-  // least one voxel thick in z; otherwise, or when a slab overflows, the general kernel runs
-  bool ring = fp32 && !cp.check_cells && g->Ez <= Mz && !c->fp32_general;
-  auto columns = [&](bool use_ring) -> cudaError_t {
-    cudaError_t ce = cudaSuccess;
-    if (g->ix1 > g->ix0 && g->iy1 > g->iy0) {
-      const int width = fp32 ? 16 : 4;
-      for (int off = 0; off < nPrec && ce == cudaSuccess; off += width) {
-        cp.prec_offset = off;
-        cp.accumulate = off > 0 ? 1 : 0;
-        ce = !fp32 ? launch_column_fp64(cp, st) : (use_ring ? launch_column_fp32_v2(cp, st)
-                                                           : launch_column_fp32(cp, st));
-      }
-      if (ce == cudaSuccess && (flags & ST_FLAG_AVERAGE))
-        ce = launch_epilogue(d_img, Mx, My, g->ix0, g->ix1, g->iy0, g->iy1, (double)nPrec,
-                             (flags & ST_FLAG_BRIGHT) ? 1 : 0, st);
-    }
-    return ce;
-  };
-  e = columns(ring);
-  if (e != cudaSuccess) return cuda_fail(c, e, "column kernel launch");
-  cudaEventRecord(c->ev[2], st);
-  e = cudaMemcpyAsync(c->h_counters, c->s.counters, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-  if (e != cudaSuccess) return cuda_fail(c, e, "image kernels");
-  if (ring && c->h_counters[4] != 0 && (int64_t)c->h_counters[0] <= cap) {
-    // a slab held more atoms than the ring kernel stages: recompute with the general kernel
-    ring = false;
-    cudaMemsetAsync(c->s.counters + 2, 0, 3 * sizeof(unsigned long long), st);
-    e = cudaMemsetAsync(d_img, 0, sizeof(double) * (size_t)Mx * My, st);
-    if (e == cudaSuccess) e = columns(false);
-    cudaEventRecord(c->ev[2], st);
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(c->h_counters, c->s.counters, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) return cuda_fail(c, e, "image kernels (general FP32 kernel)");
-  }
-  c->last_column_kernel = !fp32 ? 3 : (ring ? 2 : 1);
-  if ((int64_t)c->h_counters[0] <= cap) break;
-  if (attempt > 0) return fail(c, ST_ERR_ALLOC, "binning capacity did not converge");
-  cap = (int64_t)c->h_counters[0] + (int64_t)c->h_counters[0] / 8 + 1024;  // grow and redo the image
-  }
-  c->last_kept = (int64_t)c->h_counters[0];
-
-  st_stats& S = c->stats;
-  memset(&S, 0, sizeof S);
-  S.n_atoms = nAtoms;
-  S.n_kept = (int64_t)c->h_counters[0];
-  S.max_cell_count = (int32_t)c->h_counters[1];
-  S.n_tests = (int64_t)c->h_counters[2];
-  S.n_accepted = (int64_t)c->h_counters[3];
-  S.n_voxels = (int64_t)(g->ix1 - g->ix0) * (g->iy1 - g->iy0) * Mz;
-  S.n_prec = nPrec;
-  float ms = 0.f;
-  cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]);
-  S.ms_bin = ms;
-  cudaEventElapsedTime(&ms, c->ev[1], c->ev[2]);
-  S.ms_column = ms;
-  S.column_kernel = c->last_column_kernel;
-  if (g->nMax0 > 0 && S.max_cell_count > 16 * g->nMax0) {
-    char buf[256];
-    snprintf(buf, sizeof buf,
-             "a link cell holds %d atoms, more than 16 x nMax0 = %d (the reference stops in "
-             "Lib_LinkCell3d::add0 here)",
-             S.max_cell_count, 16 * g->nMax0);
-    return fail(c, ST_ERR_CAPACITY, buf);
-  }
-  return ST_OK;
+  cudaSetDevice(c->device);
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+  return run_images(c, js, flags, st);
 }
 
 extern "C" int st_image(st_ctx* c, const st_geom* g, const double* x, int64_t ldx, int64_t nAtoms, const double* aa,

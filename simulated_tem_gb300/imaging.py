@@ -82,6 +82,24 @@ class Context:
                                           _ptr(aa), len(aa), flags, ctypes.c_void_p(img_dev_ptr),
                                           ctypes.c_void_p(stream)))
 
+    def batch_device(self, jobs, flags, stream=0):
+        """st_batch_device: jobs is a list of (geom, x_dev_ptr, n_atoms, aa, img_dev_ptr[, ldx])."""
+        arr = (_lib.StJob * len(jobs))()
+        keep = []
+        for k, job in enumerate(jobs):
+            geom, xp, n, aa, ip = job[:5]
+            ldx = job[5] if len(job) > 5 else 3
+            aa = np.ascontiguousarray(np.atleast_1d(aa), dtype=np.float64)
+            keep.append((geom, aa))
+            arr[k].geom = ctypes.pointer(geom)
+            arr[k].d_x = xp
+            arr[k].ldx = ldx
+            arr[k].nAtoms = n
+            arr[k].aa = _ptr(aa)
+            arr[k].nPrec = len(aa)
+            arr[k].d_img = ip
+        self._check(lib().st_batch_device(self.handle, len(jobs), arr, flags, ctypes.c_void_p(stream)))
+
     def blur(self, img, t):
         """st_blur: gaussianBlurImage of an (Nx, Ny) image with width t pixels."""
         img = np.asfortranarray(img, dtype=np.float64)

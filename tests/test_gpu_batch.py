@@ -1,0 +1,195 @@
+"""Batches through st_batch_device.
+
+A batch runs one binning pass over the candidates of all its images and, on
+the FP32 path, one persistent column launch over the warp tiles of all its
+images.  Every image of a batch must equal, to the last bit, the image the
+single-image entry point makes for the same job (same kernels, same
+summation order per voxel), and must match the oracle to the path's bar.
+"""
+import numpy as np
+import pytest
+
+from oracle import stem_oracle as O
+from simulated_tem_gb300 import _lib, imaging, synth
+
+torch = pytest.importorskip("torch")
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-12
+FP32_TOL = 1e-4
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = imaging.Context(0)
+    yield c
+    c.close()
+
+
+def _condition(cell, g=(1, 1, 0), n_tomo=1, step=0, **kw):
+    t, xw, _ = imaging.d2bi_condition(cell.a_super, synth.A0_FE, (0, 0, 1), g, cell.pos, n_tomo=n_tomo,
+                                      tomo_step=step, **kw)
+    args = O.make_args(cell.a_super, synth.A0_FE, (0, 0, 1), g, nTomo=n_tomo,
+                       **{k: v for k, v in kw.items() if k in ("sg", "density")})
+    so, xo, _ = O.setup(args, cell.pos, nn=step)
+    assert np.array_equal(xw, xo)
+    return t, so, xw
+
+
+def _batch(ctx, specs, flags):
+    """specs: (geom, aa, x) per job; x arrays with the same id share one device buffer."""
+    dev, imgs, jobs = {}, [], []
+    for G, aa, x in specs:
+        if id(x) not in dev:
+            dev[id(x)] = torch.from_numpy(np.ascontiguousarray(x)).to("cuda") if len(x) else \
+                torch.zeros(3, dtype=torch.float64, device="cuda")
+        im = torch.full((G.My, G.Mx), 7.0, dtype=torch.float64, device="cuda")  # overwritten by the batch
+        imgs.append(im)
+        jobs.append((G, dev[id(x)].data_ptr(), len(x), aa, im.data_ptr()))
+    torch.cuda.synchronize()
+    ctx.batch_device(jobs, flags, torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    return [im.cpu().numpy().T for im in imgs]
+
+
+def _mixed_specs(fp32):
+    """Images of different cells, sizes, g-vectors, density settings, precession counts and patches."""
+    sv = synth.small_cell(n=(10, 10, 8), seed=5, n_voids=1, radius=(4.0, 6.0), with_screw=True)
+    vo = synth.small_cell(n=(9, 11, 7), seed=6, n_voids=3, radius=(3.0, 5.0), with_screw=False)
+    specs, oracles = [], []
+    t, so, x = _condition(sv, sg=0.01, density=True)
+    G, aa = t.image_geometry(len(x), n_prec=3)
+    specs.append((G, aa, x)), oracles.append((so, x, 3, 1, 0))
+    t, so, x2 = _condition(vo, sg=0.0)
+    G, aa = t.image_geometry(len(x2))
+    specs.append((G, aa, x2)), oracles.append((so, x2, 1, 1, 0))
+    t, so, x3 = _condition(sv, g=(2, 0, 0), sg=-0.005)
+    n_prec = 17 if fp32 else 6  # more angles than one pass of the column kernel holds
+    G, aa = t.image_geometry(len(x3), n_prec=n_prec)
+    specs.append((G, aa, x3)), oracles.append((so, x3, n_prec, 1, 0))
+    t, so, x4 = _condition(vo, sg=0.01, density=True)
+    G, aa = t.image_geometry(len(x4), nprocs=3, jj=1)
+    specs.append((G, aa, x4)), oracles.append((so, x4, 1, 3, 1))
+    G, aa = t.image_geometry(0)
+    empty = np.zeros((0, 3))
+    specs.append((G, aa, empty)), oracles.append((so, empty, 1, 1, 0))
+    return specs, oracles
+
+
+@pytest.mark.parametrize("fp32", [False, True])
+@pytest.mark.parametrize("average", [False, True])
+def test_mixed_batch_equals_single_images(ctx, fp32, average):
+    flags = (_lib.ST_FLAG_FP32 if fp32 else 0) | (_lib.ST_FLAG_AVERAGE if average else 0)
+    specs, oracles = _mixed_specs(fp32)
+    got = _batch(ctx, specs, flags | _lib.ST_FLAG_STATS)
+    st = ctx.stats()
+    if fp32:
+        assert st.column_kernel == 2  # one persistent slab-ring launch per pass
+    n_kept = 0
+    for (G, aa, x), img, (so, xo, n_prec, nprocs, jj) in zip(specs, got, oracles):
+        single = ctx.image(G, x, aa, flags=flags | _lib.ST_FLAG_STATS)
+        n_kept += ctx.stats().n_kept
+        assert np.array_equal(img, single)
+        Go, aao = O.geometry(so, len(xo), nPrec=n_prec, precAngle=0.005, nProcs=nprocs, jj=jj)
+        want, _ = O.patch_image(Go, aao, xo, nthreads=8)
+        if average:
+            want = want.copy()
+            want[Go.ix0:Go.ix1, Go.iy0:Go.iy1] /= n_prec
+        assert np.abs(img - want).max() <= (FP32_TOL if fp32 else FP64_TOL)
+    assert st.n_kept == n_kept
+
+
+@pytest.mark.parametrize("fp32", [False, True])
+def test_tomography_series_shares_atoms(ctx, fp32):
+    """A tilt series: five tomography tilts of one cell image the same device atoms."""
+    cell = synth.small_cell(n=(10, 10, 8), seed=5, n_voids=1, radius=(4.0, 6.0), with_screw=True)
+    specs, oracles = [], []
+    x0 = None
+    for step in range(5):
+        t, so, x = _condition(cell, n_tomo=5, step=step, sg=0.01, density=True)
+        x0 = x if x0 is None else x0
+        assert np.array_equal(x, x0)
+        G, aa = t.image_geometry(len(x0), n_prec=2)
+        specs.append((G, aa, x0))
+        oracles.append(so)
+    flags = _lib.ST_FLAG_FP32 if fp32 else 0
+    got = _batch(ctx, specs, flags)
+    for (G, aa, x), img, so in zip(specs, got, oracles):
+        assert np.array_equal(img, ctx.image(G, x, aa, flags=flags))
+        Go, aao = O.geometry(so, len(x), nPrec=2, precAngle=0.005)
+        want, _ = O.patch_image(Go, aao, x, nthreads=8)
+        assert np.abs(img - want).max() <= (FP32_TOL if fp32 else FP64_TOL)
+    assert not np.array_equal(got[0], got[2])  # the tilts give different images
+
+
+def test_uneven_cells_batch(ctx):
+    """Independent cells of 0.6k to 60k atoms and different shapes in one FP32 batch."""
+    cells = synth.uneven_cells(count=12, lo=8_000, hi=60_000)  # voids leave 637 to 57k atoms
+    specs = []
+    for cell, sg in cells:
+        t, xw, _ = imaging.d2bi_condition(cell.a_super, synth.A0_FE, (0, 0, 1), (1, 1, 0), cell.pos, sg=sg)
+        G, aa = t.image_geometry(len(xw))
+        specs.append((G, aa, xw))
+    assert len({(G.Mx, G.My, G.Mz) for G, _, _ in specs}) > 6
+    got = _batch(ctx, specs, _lib.ST_FLAG_FP32)
+    for (G, aa, x), img in zip(specs, got):
+        assert np.array_equal(img, ctx.image(G, x, aa, flags=_lib.ST_FLAG_FP32))
+    # the smallest cell against the oracle
+    k = int(np.argmin([cell.n_atoms for cell, _ in cells]))
+    cell, sg = cells[k]
+    args = O.make_args(cell.a_super, synth.A0_FE, (0, 0, 1), (1, 1, 0), sg=sg)
+    so, xo, _ = O.setup(args, cell.pos)
+    assert np.array_equal(xo, specs[k][2])
+    Go, aao = O.geometry(so, len(xo))
+    want, _ = O.patch_image(Go, aao, xo, nthreads=8)
+    assert np.abs(got[k] - want).max() <= FP32_TOL
+
+
+def test_batch_errors(ctx):
+    cell = synth.small_cell()
+    t, so, x = _condition(cell, sg=0.01)
+    G, aa = t.image_geometry(len(x))
+    xd = torch.from_numpy(x).to("cuda")
+    im = torch.zeros((G.My, G.Mx), dtype=torch.float64, device="cuda")
+    with pytest.raises(_lib.StemError) as e:
+        ctx.batch_device([], 0)
+    assert e.value.code == _lib.ST_ERR_ARG
+    with pytest.raises(_lib.StemError) as e:
+        ctx.batch_device([(G, xd.data_ptr(), len(x), aa, im.data_ptr()), (G, 0, len(x), aa, im.data_ptr())], 0)
+    assert e.value.code == _lib.ST_ERR_ARG and "job 1" in str(e.value)
+    ctx.batch_device([(G, xd.data_ptr(), len(x), aa, im.data_ptr())], 0, torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert np.array_equal(im.cpu().numpy().T, ctx.image(G, x, aa))
+
+
+@pytest.mark.parametrize("fp32", [False, True])
+def test_capacity_retry_after_small_image(fp32):
+    """The kept-atom arrays are sized by the previous call: a small image followed by a
+    larger batch overflows them, and the batch is binned again into grown arrays."""
+    flags = _lib.ST_FLAG_FP32 if fp32 else 0
+    small = synth.small_cell(n=(6, 6, 4), seed=8, n_voids=0, with_screw=False)
+    t, so, xs = _condition(small, sg=0.01)
+    Gs, aas = t.image_geometry(len(xs))
+    big = synth.small_cell(n=(30, 30, 12), seed=9, n_voids=2, radius=(4.0, 8.0), with_screw=True)
+    tb, sob, xb = _condition(big, sg=0.01, density=True)
+    Gb, aab = tb.image_geometry(len(xb), n_prec=2)
+    fresh = imaging.Context(0)
+    try:
+        want_big = fresh.image(Gb, xb, aab, flags=flags | _lib.ST_FLAG_STATS)
+        kept_big = fresh.stats().n_kept
+    finally:
+        fresh.close()
+    c = imaging.Context(0)
+    try:
+        c.image(Gs, xs, aas, flags=flags | _lib.ST_FLAG_STATS)
+        kept_small = c.stats().n_kept
+        assert 2 * kept_big > kept_small + kept_small // 4 + 65536  # the batch cannot fit the first guess
+        got = _batch(c, [(Gb, aab, xb), (Gs, aas, xs), (Gb, aab, xb)], flags | _lib.ST_FLAG_STATS)
+        assert c.stats().n_kept == 2 * kept_big + kept_small
+    finally:
+        c.close()
+    assert np.array_equal(got[0], want_big) and np.array_equal(got[2], want_big)
+    Go, aao = O.geometry(sob, len(xb), nPrec=2, precAngle=0.005)
+    want, _ = O.patch_image(Go, aao, xb, nthreads=8)
+    assert np.abs(got[0] - want).max() <= (FP32_TOL if fp32 else FP64_TOL)
