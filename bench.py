@@ -14,6 +14,11 @@ FP64 cell assignment and FP64 g.r reduction.
          from pinned host buffers: the H2D copy of the atoms and the D2H copy
          of the image are inside the timed region.
   also   the plain FP64 GPU path (images/s) and max |dI| FP32 vs FP64.
+  batched  st_batch_device on (a) the tilt x precession x g sweep of the same
+         cell (41 x 16 x 3: 123 images, 1,968 integration passes) and (b) 256
+         independent cells of uneven size; images/s, voxel-slices/s and the
+         FP32-vs-FP64 accuracy of one image of each.  The clock record spans
+         the single-image steps and both batched legs.
 
 ``--impl reference`` times the reference's algorithm on the host cores: the
 reference (Fortran) cannot be built here, so the oracle's C restatement runs,
@@ -48,6 +53,122 @@ def workload():
     t, x, aperpx = imaging.d2bi_condition(cell.a_super, synth.A0_FE, (0, 0, 1), (1, 1, 0), cell.pos, sg=0.01,
                                           xi0=103.9, xig=207.5, V=200.0, M=(4, 4))
     return cell, t, x, aperpx
+
+
+SWEEP_G = ((1, 1, 0), (2, 0, 0), (2, 1, 1))
+
+
+def sweep_specs(cell, n_tomo=41, n_prec=16, gs=SWEEP_G):
+    """Tilt series x precession x g on the 1.2M-atom cell: nTomoAngle = 41 tilts over
+    +-20 deg, 16 precession angles at 5 mrad, g in {110, 200, 211}.  Returns the
+    wrapped positions (shared by every image) and one (geometry, aa) per output image."""
+    from simulated_tem_gb300 import imaging, synth
+    x0, specs = None, []
+    for g in gs:
+        for step in range(n_tomo):
+            t, x, _ = imaging.d2bi_condition(cell.a_super, synth.A0_FE, (0, 0, 1), g, cell.pos, sg=0.01,
+                                             xi0=103.9, xig=207.5, V=200.0, M=(4, 4), n_tomo=n_tomo,
+                                             tomo_angle=20.0, tomo_step=step)
+            if x0 is None:
+                x0 = x
+            elif step == 0 and not np.array_equal(x, x0):
+                raise RuntimeError("the sweep's conditions wrap the atoms differently")
+            G, aa = t.image_geometry(len(x0), prec_angle=0.005, n_prec=n_prec)
+            specs.append((G, aa))
+    return x0, specs
+
+
+def uneven_specs():
+    """256 independent bcc Fe cells, atom counts log-uniform in [10k, 500k] before voids,
+    aspect ratios U(0.5, 2), Poisson(10) voids of radius U(4, 20) A, s_g ~ U(-0.02, 0.02)."""
+    from simulated_tem_gb300 import imaging, synth
+    out = []
+    for cell, sg in synth.uneven_cells():
+        t, x, _ = imaging.d2bi_condition(cell.a_super, synth.A0_FE, (0, 0, 1), (1, 1, 0), cell.pos, sg=sg,
+                                         xi0=103.9, xig=207.5, V=200.0, M=(4, 4))
+        G, aa = t.image_geometry(len(x))
+        out.append((G, aa, x))
+    return out
+
+
+def time_batch(ctx, jobs, flags, stream, steps, warmup, flush):
+    """CUDA-event time of st_batch_device over `jobs`, L2 flushed before each call."""
+    import torch
+    sptr = stream.cuda_stream
+    for _ in range(warmup):
+        ctx.batch_device(jobs, flags, sptr)
+    ms = []
+    for i in range(steps):
+        flush.fill_(float(i))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ctx.batch_device(jobs, flags, sptr)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    return ms
+
+
+def batched_legs(ctx, cell, stream, flush, steps, warmup):
+    """The two batched workloads through st_batch_device: the tilt x precession x g
+    sweep on the 1.2M-atom cell and the 256-cell uneven batch, FP32 path; for each,
+    one image is recomputed on the plain FP64 path for the accuracy figure."""
+    import torch
+
+    from simulated_tem_gb300 import _lib
+    out = {}
+    f32 = _lib.ST_FLAG_FP32 | _lib.ST_FLAG_AVERAGE
+
+    def accuracy(G, x_ptr, n, aa, img):
+        ref = torch.empty((G.My, G.Mx), dtype=torch.float64, device="cuda")
+        ctx.image_device(G, x_ptr, n, aa, _lib.ST_FLAG_AVERAGE, ref.data_ptr(), stream=stream.cuda_stream)
+        torch.cuda.synchronize()
+        d = (img - ref).abs()
+        return {"max_abs_dI_fp32_vs_fp64": float(d.max()), "rms_dI_fp32_vs_fp64": float(d.pow(2).mean().sqrt())}
+
+    # tilt x precession x g sweep
+    x, specs = sweep_specs(cell)
+    d_x = torch.from_numpy(np.ascontiguousarray(x)).cuda()
+    imgs = [torch.empty((G.My, G.Mx), dtype=torch.float64, device="cuda") for G, _ in specs]
+    jobs = [(G, d_x.data_ptr(), len(x), aa, im.data_ptr()) for (G, aa), im in zip(specs, imgs)]
+    ms = time_batch(ctx, jobs, f32 | _lib.ST_FLAG_STATS, stream, 1, 0, flush)  # statistics
+    st = ctx.stats()
+    ms = time_batch(ctx, jobs, f32, stream, steps, warmup, flush)
+    t = float(np.mean(ms)) * 1e-3
+    n_img, n_pass = len(specs), sum(len(aa) for _, aa in specs)
+    vs = sum((G.ix1 - G.ix0) * (G.iy1 - G.iy0) * G.Mz * len(aa) for G, aa in specs)
+    k = len(specs) // (2 * len(SWEEP_G))  # a mid-series tilt of g = 110
+    G, aa = specs[k]
+    out["sweep"] = {"workload": "1.2M-atom cell: 41 tilts over +-20 deg x 16 precession angles (5 mrad) x "
+                                "g in {110, 200, 211}, FP32, images averaged over precession",
+                    "images": n_img, "integration_passes": n_pass, "images_per_s": n_img / t,
+                    "passes_per_s": n_pass / t, "voxel_slices_per_s": vs / t, "ms_per_batch": t * 1e3,
+                    "steps": steps, "image_sizes": sorted({(G_.Mx, G_.My, G_.Mz) for G_, _ in specs}),
+                    "kept_atoms": st.n_kept, "column_kernel": st.column_kernel,
+                    "ms_bin": st.ms_bin, "ms_column": st.ms_column,
+                    "accuracy_one_image": accuracy(G, d_x.data_ptr(), len(x), aa, imgs[k])}
+    del imgs, jobs
+
+    # 256 independent cells of uneven size
+    specs = uneven_specs()
+    d_xs = [torch.from_numpy(np.ascontiguousarray(x_)).cuda() for _, _, x_ in specs]
+    imgs = [torch.empty((G.My, G.Mx), dtype=torch.float64, device="cuda") for G, _, _ in specs]
+    jobs = [(G, dx.data_ptr(), len(x_), aa, im.data_ptr()) for (G, aa, x_), dx, im in zip(specs, d_xs, imgs)]
+    time_batch(ctx, jobs, f32 | _lib.ST_FLAG_STATS, stream, 1, 0, flush)
+    st = ctx.stats()
+    ms = time_batch(ctx, jobs, f32, stream, steps, warmup, flush)
+    t = float(np.mean(ms)) * 1e-3
+    vs = sum((G.ix1 - G.ix0) * (G.iy1 - G.iy0) * G.Mz for G, _, _ in specs)
+    k = int(np.argmax([len(x_) for _, _, x_ in specs]))
+    G, aa, x_ = specs[k]
+    out["uneven"] = {"workload": "256 bcc Fe cells, atoms log-uniform in [10k, 500k] before voids, aspect U(0.5, 2), "
+                                 "Poisson(10) voids of radius U(4, 20) A, s_g U(-0.02, 0.02), FP32",
+                     "images": len(specs), "atoms": int(sum(len(x_) for _, _, x_ in specs)),
+                     "images_per_s": len(specs) / t, "voxel_slices_per_s": vs / t, "ms_per_batch": t * 1e3,
+                     "steps": steps, "kept_atoms": st.n_kept, "column_kernel": st.column_kernel,
+                     "ms_bin": st.ms_bin, "ms_column": st.ms_column,
+                     "accuracy_largest_cell": accuracy(G, d_xs[k].data_ptr(), len(x_), aa, imgs[k])}
+    return out
 
 
 def dist_env():
@@ -158,6 +279,8 @@ def run_gpu(args):
             col_ms.append(ctx.stats().ms_column)
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
+        batched = None if args.no_batched else batched_legs(ctx, cell, stream, flush, args.batch_steps,
+                                                             args.warmup)
     step_ms = [a.elapsed_time(b) for a, b in ev]
     ms = float(np.mean(step_ms))
     if ws > 1:
@@ -230,7 +353,7 @@ def run_gpu(args):
             "accuracy": {"max_abs_dI_fp32_vs_fp64": float(np.abs(d).max()),
                          "rms_dI_fp32_vs_fp64": float(np.sqrt((d ** 2).mean()))},
             "gpu_launches": args.steps * launches_per_image(n_prec, fp32=True, average=True),
-            "roofline": roof, "peaks": peaks, "wall_s": wall, "clocks": clk.summary()}
+            "roofline": roof, "peaks": peaks, "wall_s": wall, "clocks": clk.summary(), "batched": batched}
     if rank == 0:
         if ws == 1 and not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline(x_state=(cell, t, x), rows=args.cpu_rows)
@@ -364,6 +487,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-rows", type=int, default=48)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched sweep and uneven-cell legs")
+    ap.add_argument("--batch-steps", type=int, default=3)
     ap.add_argument("--ncu-case", choices=["fp32", "fp64"], default=None,
                     help="run two untimed images only (for an ncu capture)")
     args = ap.parse_args()

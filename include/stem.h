@@ -129,7 +129,9 @@ typedef struct st_job {
  * st_image_device makes for its job.  The binning runs once over the
  * candidates of all jobs and, on the FP32 path, the columns of all jobs run
  * as one persistent launch that hands out warp tiles from a global counter.
- * flags apply to every job.  Returns after every image is complete. */
+ * A batch of 2^31 or more candidates (nuvw x nAtoms summed over its jobs) runs
+ * as consecutive groups below that size.  flags apply to every job.  Returns
+ * after every image is complete; st_get_stats then sums over the batch. */
 int st_batch_device(st_ctx* ctx, int32_t n_jobs, const st_job* jobs, int32_t flags, void* stream);
 
 /* Gaussian blur of width t pixels (src/d2bi.f90:1543-1624) from host buffers;

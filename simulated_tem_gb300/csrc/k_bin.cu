@@ -120,7 +120,7 @@ __global__ void __launch_bounds__(256) k_bin_transform(const BinParams* __restri
     unsigned long long base = 0;
     if (lane == leader) base = atomicAdd(&counters[0], (unsigned long long)__popc(mask));
     base = __shfl_sync(mask, base, leader);
-    const int idx = (int)(base + __popc(mask & ((1u << lane) - 1)));
+    const int64_t idx = (int64_t)base + __popc(mask & ((1u << lane) - 1));
 
     const double fl0 = floor(c0), fl1 = floor(c1), fl2 = floor(c2);
     const int cx = (int)fl0, cy = (int)fl1, cz = (int)fl2;

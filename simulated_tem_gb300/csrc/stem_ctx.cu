@@ -265,7 +265,8 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
     aoff[i + 1] = aoff[i] + jobs[i].n_prec;
   }
   const int64_t total_cand = cand_base[n], total_cells = cell_base[n];
-  if (total_cand >= 2147483647LL) return fail(c, ST_ERR_ARG, "a call holds more than 2^31 - 1 candidates");
+  // kept atoms are indexed by int (cell starts, permutation): at most total_cand of them
+  if (total_cand >= 2147483647LL) return fail(c, ST_ERR_ARG, "a binning pass holds more than 2^31 - 1 candidates");
   if (total_cells >= 2147483647LL) return fail(c, ST_ERR_ARG, "a call holds more than 2^31 - 1 link cells");
 
   // ---- device buffers that do not depend on the kept-atom count
@@ -604,7 +605,37 @@ extern "C" int st_batch_device(st_ctx* c, int32_t n_jobs, const st_job* jobs, in
   }
   cudaSetDevice(c->device);
   cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
-  return run_images(c, js, flags, st);
+  // one binning pass and one persistent launch per group of jobs with fewer than 2^31
+  // candidates (replicas x atoms) in total; most batches are a single group
+  st_stats total{};
+  int first = 0;
+  while (first < n_jobs) {
+    int last = first;
+    int64_t cand = 0;
+    while (last < n_jobs) {
+      const int64_t jc = (int64_t)js[last].g->nuvw * js[last].n_atoms;
+      if (last > first && cand + jc >= 2147483647LL) break;
+      cand += jc;
+      ++last;
+    }
+    std::vector<Job> group(js.begin() + first, js.begin() + last);
+    const int rc = run_images(c, group, flags, st);
+    if (rc != ST_OK) return rc;
+    const st_stats& S = c->stats;
+    total.n_atoms += S.n_atoms;
+    total.n_kept += S.n_kept;
+    total.n_tests += S.n_tests;
+    total.n_accepted += S.n_accepted;
+    total.n_voxels += S.n_voxels;
+    total.max_cell_count = std::max(total.max_cell_count, S.max_cell_count);
+    total.n_prec = std::max(total.n_prec, S.n_prec);
+    total.ms_bin += S.ms_bin;
+    total.ms_column += S.ms_column;
+    total.column_kernel = std::max(total.column_kernel, S.column_kernel);
+    first = last;
+  }
+  c->stats = total;
+  return ST_OK;
 }
 
 extern "C" int st_image(st_ctx* c, const st_geom* g, const double* x, int64_t ldx, int64_t nAtoms, const double* aa,
