@@ -171,6 +171,68 @@ def batched_legs(ctx, cell, stream, flush, steps, warmup):
     return out
 
 
+def cfg1_leg(ctx, stream, flush, steps, warmup, cpu=True):
+    """The 128k-atom void cell (40^3 bcc cells, 8 voids of 10 A), g = 110, s_g = 0, -density,
+    M = 4,4: one dark-field image, the bright field 1 - DF, and both blurred at 2.5 A, on the
+    plain FP64 path and on the FP32 path; the oracle times the same on the host cores."""
+    import torch
+
+    from simulated_tem_gb300 import _lib, imaging, synth
+    cell = synth.void_cell_128k()
+    t, x, aperpx = imaging.d2bi_condition(cell.a_super, synth.A0_FE, (0, 0, 1), (1, 1, 0), cell.pos, sg=0.0,
+                                          xi0=103.9, xig=207.5, V=200.0, M=(4, 4), density=True)
+    G, aa = t.image_geometry(len(x))
+    tpx = 2.5 / aperpx
+    sp = stream.cuda_stream
+    d_x = torch.from_numpy(np.ascontiguousarray(x)).cuda()
+    df, bf, dfb, bfb = (torch.empty((G.My, G.Mx), dtype=torch.float64, device="cuda") for _ in range(4))
+
+    def step(flags):
+        ctx.image_device(G, d_x.data_ptr(), len(x), aa, flags | _lib.ST_FLAG_AVERAGE, df.data_ptr(), stream=sp)
+        torch.neg(df, out=bf)
+        bf.add_(1.0)
+        ctx.blur_device(df.data_ptr(), G.Mx, G.My, tpx, dfb.data_ptr(), stream=sp)
+        ctx.blur_device(bf.data_ptr(), G.Mx, G.My, tpx, bfb.data_ptr(), stream=sp)
+
+    out = {"workload": "bcc Fe 40^3 cells (%d atoms), 8 voids of 10 A, g=[110] k=[001] s_g=0, -density, M=4,4, "
+                       "DF + BF, blur 2.5 A (%.3f px)" % (len(x), tpx), "image": [G.Mx, G.My, G.Mz]}
+    imgs = {}
+    for name, flags in (("gpu_fp64", 0), ("gpu_fp32", _lib.ST_FLAG_FP32)):
+        for _ in range(warmup):
+            step(flags)
+        ms = []
+        for i in range(steps):
+            flush.fill_(float(i))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step(flags)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        out[name] = {"images_per_s": 1000.0 / float(np.mean(ms)), "ms": float(np.mean(ms)),
+                     "note": "one DF + BF pair with both blurs per image"}
+        imgs[name] = df.cpu().numpy().T.copy()
+    d = imgs["gpu_fp32"] - imgs["gpu_fp64"]
+    out["accuracy_fp32_vs_fp64"] = {"max_abs_dI": float(np.abs(d).max()), "rms_dI": float(np.sqrt((d ** 2).mean()))}
+    if cpu:
+        from oracle import stem_oracle as O
+        threads = os.cpu_count() or 1
+        args = O.make_args(cell.a_super, synth.A0_FE, (0, 0, 1), (1, 1, 0), sg=0.0, xi0=103.9, xig=207.5,
+                           density=True)
+        so, xo, _ = O.setup(args, cell.pos)
+        Go, aao = O.geometry(so, len(xo))
+        t0 = time.perf_counter()
+        img, _ = O.patch_image(Go, aao, xo, nthreads=threads)
+        O.gaussian_blur(img, tpx)
+        O.gaussian_blur(1.0 - img, tpx)
+        tc = time.perf_counter() - t0
+        dd = imgs["gpu_fp64"] - img
+        out["cpu_oracle"] = {"images_per_s": 1.0 / tc, "s": tc, "cores": threads, "kind": "port",
+                             "note": "oracle C restatement, whole image + both blurs"}
+        out["accuracy_gpu_fp64_vs_oracle"] = {"max_abs_dI": float(np.abs(dd).max())}
+    return out
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -247,7 +309,9 @@ def run_gpu(args):
     G, aa = t.image_geometry(len(x))
     n_prec = len(aa)
     ctx = imaging.Context(local)
-    stream = torch.cuda.current_stream()
+    # one stream for torch's buffers, the L2 flush, the events and the library's kernels
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     sptr = stream.cuda_stream
     d_x = torch.from_numpy(np.ascontiguousarray(x)).cuda()
     d_img = torch.zeros((G.My, G.Mx), dtype=torch.float64, device="cuda")
@@ -281,6 +345,8 @@ def run_gpu(args):
         wall = time.perf_counter() - t0
         batched = None if args.no_batched else batched_legs(ctx, cell, stream, flush, args.batch_steps,
                                                              args.warmup)
+        cfg1 = None if args.no_batched else cfg1_leg(ctx, stream, flush, 5, args.warmup,
+                                                      cpu=(rank == 0 and not args.no_cpu))
     step_ms = [a.elapsed_time(b) for a, b in ev]
     ms = float(np.mean(step_ms))
     if ws > 1:
@@ -353,7 +419,7 @@ def run_gpu(args):
             "accuracy": {"max_abs_dI_fp32_vs_fp64": float(np.abs(d).max()),
                          "rms_dI_fp32_vs_fp64": float(np.sqrt((d ** 2).mean()))},
             "gpu_launches": args.steps * launches_per_image(n_prec, fp32=True, average=True),
-            "roofline": roof, "peaks": peaks, "wall_s": wall, "clocks": clk.summary(), "batched": batched}
+            "roofline": roof, "peaks": peaks, "wall_s": wall, "clocks": clk.summary(), "batched": batched, "cfg1_128k": cfg1}
     if rank == 0:
         if ws == 1 and not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline(x_state=(cell, t, x), rows=args.cpu_rows)

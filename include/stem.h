@@ -110,17 +110,18 @@ int st_image(st_ctx* ctx, const st_geom* geom, const double* x, int64_t ldx, int
 int st_image_device(st_ctx* ctx, const st_geom* geom, const double* d_x, int64_t ldx, int64_t nAtoms,
                     const double* aa, int32_t nPrec, int32_t flags, double* d_img, void* stream);
 
-/* One image of a batch: its geometry, its atoms and output in device memory,
- * and its precession parameters aa(1:nPrec) in host memory. */
+/* One image of a batch: its geometry, its atoms, its precession parameters
+ * aa(1:nPrec) in host memory, and its output.  x and img are device pointers
+ * for st_batch_device and host pointers for st_batch. */
 typedef struct st_job {
   const st_geom* geom;
-  const double* d_x; /* (ldx, nAtoms) */
+  const double* x; /* (ldx, nAtoms) */
   int64_t ldx;
   int64_t nAtoms;
   const double* aa;
   int32_t nPrec;
   int32_t pad0;
-  double* d_img; /* Mx x My, overwritten as by st_image */
+  double* img; /* Mx x My column-major, overwritten as by st_image */
 } st_job;
 
 /* Many images in one call: tomography tilts, precession sets, g-vectors or
@@ -133,6 +134,12 @@ typedef struct st_job {
  * as consecutive groups below that size.  flags apply to every job.  Returns
  * after every image is complete; st_get_stats then sums over the batch. */
 int st_batch_device(st_ctx* ctx, int32_t n_jobs, const st_job* jobs, int32_t flags, void* stream);
+
+/* st_batch_device from host buffers, the call a Fortran driver of a tilt
+ * series or a set of cells makes.  Jobs that name the same atoms (same x,
+ * ldx and nAtoms) share one device copy, so a tilt series uploads its atoms
+ * once.  The images are copied back before it returns. */
+int st_batch(st_ctx* ctx, int32_t n_jobs, const st_job* jobs, int32_t flags);
 
 /* Gaussian blur of width t pixels (src/d2bi.f90:1543-1624) from host buffers;
  * in and out are nx x ny doubles, column-major; out is overwritten. */

@@ -50,8 +50,8 @@ class StStats(ctypes.Structure):
 
 class StJob(ctypes.Structure):
     """st_job of include/stem.h."""
-    _fields_ = [("geom", ctypes.POINTER(StGeom)), ("d_x", _vp), ("ldx", _i64), ("nAtoms", _i64), ("aa", _dp),
-                ("nPrec", _i32), ("pad0", _i32), ("d_img", _vp)]
+    _fields_ = [("geom", ctypes.POINTER(StGeom)), ("x", _vp), ("ldx", _i64), ("nAtoms", _i64), ("aa", _dp),
+                ("nPrec", _i32), ("pad0", _i32), ("img", _vp)]
 
 
 class StemError(RuntimeError):
@@ -72,6 +72,7 @@ _PROTOS = {
     "st_get_stats": (_i32, [_vp, ctypes.POINTER(StStats)]),
     "st_blur_noalloc": (_i32, [_vp, _i32, _i32, _d, _vp, _vp, ctypes.c_char_p, _i32]),
     "st_batch_device": (_i32, [_vp, _i32, ctypes.POINTER(StJob), _i32, _vp]),
+    "st_batch": (_i32, [_vp, _i32, ctypes.POINTER(StJob), _i32]),
     # include/stem_host.h
     "st_d2bi_create": (_i32, [ctypes.POINTER(_vp), _dp, _i32, _i32, _i32, _d, _dp, _dp, _d, _i32, _i32]),
     "st_d2bi_destroy": (None, [_vp]),

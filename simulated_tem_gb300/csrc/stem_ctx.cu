@@ -42,6 +42,10 @@ struct st_ctx {
   ColumnJob* d_coljobs = nullptr;
   size_t cap_coljobs = 0;
   unsigned* d_work = nullptr;
+  double* d_bx = nullptr;  // st_batch: packed atoms of the distinct atom arrays
+  size_t cap_bx = 0;
+  double* d_bimg = nullptr;  // st_batch: images
+  size_t cap_bimg = 0;
   unsigned long long* h_counters = nullptr;  // pinned
   void* h_stage = nullptr;                   // pinned staging for tables and job descriptors
   size_t cap_stage = 0;
@@ -556,7 +560,7 @@ extern "C" void st_destroy(st_ctx* c) {
   void* dev_ptrs[] = {c->s.tmp_key, c->s.tmp_cell, c->s.tmp_slot, c->s.tmp_f, c->s.perm, c->s.block_sums,
                       c->s.counters, c->s.xtab, c->s.xfv, c->s.ytab, c->s.yfv, c->s.ztab, c->s.zfv, c->s.aa,
                       c->s.aaf, c->b.cell_start, c->b.cell_count, c->b.f64, c->b.cs64, c->b.p32, c->b.cs32,
-                      c->d_x, c->d_img, c->d_blur, c->d_kern, c->d_binjobs, c->d_coljobs, c->d_work};
+                      c->d_x, c->d_img, c->d_blur, c->d_kern, c->d_binjobs, c->d_coljobs, c->d_work, c->d_bx, c->d_bimg};
   for (void* p : dev_ptrs)
     if (p) cudaFree(p);
   if (c->h_counters) cudaFreeHost(c->h_counters);
@@ -587,10 +591,12 @@ extern "C" int st_image_device(st_ctx* c, const st_geom* g, const double* d_x, i
   return run_images(c, jobs, flags, st);
 }
 
-extern "C" int st_batch_device(st_ctx* c, int32_t n_jobs, const st_job* jobs, int32_t flags, void* stream) {
-  if (!c) return ST_ERR_ARG;
+namespace {
+
+// Checks the jobs of a batch call and converts them to the internal form.
+int collect_jobs(st_ctx* c, int32_t n_jobs, const st_job* jobs, std::vector<Job>& js) {
   if (n_jobs < 1 || !jobs) return fail(c, ST_ERR_ARG, "a batch needs at least one job");
-  std::vector<Job> js;
+  js.clear();
   js.reserve(n_jobs);
   for (int i = 0; i < n_jobs; ++i) {
     const st_job& j = jobs[i];
@@ -599,14 +605,17 @@ extern "C" int st_batch_device(st_ctx* c, int32_t n_jobs, const st_job* jobs, in
       c->err = "job " + std::to_string(i) + ": " + c->err;
       return rc;
     }
-    if (!j.aa || !j.d_img || (j.nAtoms > 0 && !j.d_x))
+    if (!j.aa || !j.img || (j.nAtoms > 0 && !j.x))
       return fail(c, ST_ERR_ARG, "job " + std::to_string(i) + ": null buffer");
-    js.push_back(Job{j.geom, j.d_x, j.ldx, j.nAtoms, j.aa, j.nPrec, j.d_img});
+    js.push_back(Job{j.geom, j.x, j.ldx, j.nAtoms, j.aa, j.nPrec, j.img});
   }
-  cudaSetDevice(c->device);
-  cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
-  // one binning pass and one persistent launch per group of jobs with fewer than 2^31
-  // candidates (replicas x atoms) in total; most batches are a single group
+  return ST_OK;
+}
+
+// One binning pass and one persistent launch per group of jobs with fewer than 2^31
+// candidates (replicas x atoms) in total; most batches are a single group.
+int run_batch(st_ctx* c, const std::vector<Job>& js, int32_t flags, cudaStream_t st) {
+  const int n_jobs = (int)js.size();
   st_stats total{};
   int first = 0;
   while (first < n_jobs) {
@@ -635,6 +644,77 @@ extern "C" int st_batch_device(st_ctx* c, int32_t n_jobs, const st_job* jobs, in
     first = last;
   }
   c->stats = total;
+  return ST_OK;
+}
+
+}  // namespace
+
+extern "C" int st_batch_device(st_ctx* c, int32_t n_jobs, const st_job* jobs, int32_t flags, void* stream) {
+  if (!c) return ST_ERR_ARG;
+  std::vector<Job> js;
+  int rc = collect_jobs(c, n_jobs, jobs, js);
+  if (rc != ST_OK) return rc;
+  cudaSetDevice(c->device);
+  return run_batch(c, js, flags, stream ? (cudaStream_t)stream : c->stream);
+}
+
+extern "C" int st_batch(st_ctx* c, int32_t n_jobs, const st_job* jobs, int32_t flags) {
+  if (!c) return ST_ERR_ARG;
+  std::vector<Job> js;
+  int rc = collect_jobs(c, n_jobs, jobs, js);
+  if (rc != ST_OK) return rc;
+  cudaSetDevice(c->device);
+  cudaStream_t st = c->stream;
+  // device layout: the distinct atom arrays packed to (3, n), then the images
+  std::vector<size_t> x_off(n_jobs), img_off(n_jobs);
+  std::vector<int> src_of(n_jobs);
+  std::vector<int> srcs;  // first job of each distinct atom array
+  size_t n_x = 0, n_img = 0;
+  for (int i = 0; i < n_jobs; ++i) {
+    int s = -1;
+    for (int k = (int)srcs.size() - 1; k >= 0 && s < 0; --k) {
+      const Job& o = js[srcs[k]];
+      if (o.d_x == js[i].d_x && o.ldx == js[i].ldx && o.n_atoms == js[i].n_atoms) s = k;
+    }
+    if (s < 0) {
+      s = (int)srcs.size();
+      srcs.push_back(i);
+      x_off[i] = n_x;
+      n_x += (size_t)3 * js[i].n_atoms;
+    } else {
+      x_off[i] = x_off[srcs[s]];
+    }
+    src_of[i] = s;
+    img_off[i] = n_img;
+    n_img += (size_t)js[i].g->Mx * js[i].g->My;
+  }
+  cudaError_t e = ensure(c->d_bx, c->cap_bx, n_x > 0 ? n_x : 1);
+  if (e == cudaSuccess) e = ensure(c->d_bimg, c->cap_bimg, n_img);
+  if (e != cudaSuccess) return cuda_fail(c, e, "allocating batch buffers");
+  for (int i : srcs) {
+    const Job& j = js[i];
+    if (j.n_atoms == 0) continue;
+    if (j.ldx == 3)
+      e = cudaMemcpyAsync(c->d_bx + x_off[i], j.d_x, sizeof(double) * 3 * (size_t)j.n_atoms, cudaMemcpyHostToDevice,
+                          st);
+    else
+      e = cudaMemcpy2DAsync(c->d_bx + x_off[i], 3 * sizeof(double), j.d_x, (size_t)j.ldx * sizeof(double),
+                            3 * sizeof(double), (size_t)j.n_atoms, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_fail(c, e, "copying atoms");
+  }
+  std::vector<Job> dj(js);
+  for (int i = 0; i < n_jobs; ++i) {
+    dj[i].d_x = c->d_bx + x_off[i];
+    dj[i].ldx = 3;
+    dj[i].d_img = c->d_bimg + img_off[i];
+  }
+  rc = run_batch(c, dj, flags, st);
+  if (rc != ST_OK) return rc;
+  for (int i = 0; i < n_jobs && e == cudaSuccess; ++i)
+    e = cudaMemcpyAsync(js[i].d_img, c->d_bimg + img_off[i], sizeof(double) * (size_t)js[i].g->Mx * js[i].g->My,
+                        cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(c, e, "copying images");
   return ST_OK;
 }
 

@@ -82,8 +82,9 @@ class Context:
                                           _ptr(aa), len(aa), flags, ctypes.c_void_p(img_dev_ptr),
                                           ctypes.c_void_p(stream)))
 
-    def batch_device(self, jobs, flags, stream=0):
-        """st_batch_device: jobs is a list of (geom, x_dev_ptr, n_atoms, aa, img_dev_ptr[, ldx])."""
+    @staticmethod
+    def _job_array(jobs):
+        """(geom, x, n_atoms, aa, img[, ldx]) tuples -> st_job array (+ the arrays it points into)."""
         arr = (_lib.StJob * len(jobs))()
         keep = []
         for k, job in enumerate(jobs):
@@ -92,13 +93,34 @@ class Context:
             aa = np.ascontiguousarray(np.atleast_1d(aa), dtype=np.float64)
             keep.append((geom, aa))
             arr[k].geom = ctypes.pointer(geom)
-            arr[k].d_x = xp
+            arr[k].x = xp
             arr[k].ldx = ldx
             arr[k].nAtoms = n
             arr[k].aa = _ptr(aa)
             arr[k].nPrec = len(aa)
-            arr[k].d_img = ip
+            arr[k].img = ip
+        return arr, keep
+
+    def batch_device(self, jobs, flags, stream=0):
+        """st_batch_device: jobs is a list of (geom, x_dev_ptr, n_atoms, aa, img_dev_ptr[, ldx])."""
+        arr, keep = self._job_array(jobs)
         self._check(lib().st_batch_device(self.handle, len(jobs), arr, flags, ctypes.c_void_p(stream)))
+
+    def batch(self, specs, flags=0):
+        """st_batch from host arrays: specs is a list of (geom, x (N, 3) or (N, ldx), aa); returns the images.
+        Specs that pass the same x array share one device copy of it."""
+        xs, imgs, jobs = {}, [], []
+        for geom, x, aa in specs:
+            if id(x) not in xs:
+                xs[id(x)] = np.ascontiguousarray(x, dtype=np.float64)
+            xc = xs[id(x)]
+            n, ldx = (xc.shape[0], xc.shape[1]) if xc.ndim == 2 else (0, 3)
+            img = np.zeros((geom.Mx, geom.My), order="F")
+            imgs.append(img)
+            jobs.append((geom, xc.ctypes.data, n, aa, img.ctypes.data, ldx))
+        arr, keep = self._job_array(jobs)
+        self._check(lib().st_batch(self.handle, len(jobs), arr, flags))
+        return imgs
 
     def blur(self, img, t):
         """st_blur: gaussianBlurImage of an (Nx, Ny) image with width t pixels."""

@@ -193,3 +193,21 @@ def test_capacity_retry_after_small_image(fp32):
     Go, aao = O.geometry(sob, len(xb), nPrec=2, precAngle=0.005)
     want, _ = O.patch_image(Go, aao, xb, nthreads=8)
     assert np.abs(got[0] - want).max() <= (FP32_TOL if fp32 else FP64_TOL)
+
+
+@pytest.mark.parametrize("fp32", [False, True])
+def test_host_batch_equals_device_batch(ctx, fp32):
+    """st_batch (host buffers, atoms shared by several jobs uploaded once, ldx = 14
+    packed on the way) gives the images of st_batch_device."""
+    flags = (_lib.ST_FLAG_FP32 if fp32 else 0) | _lib.ST_FLAG_AVERAGE
+    specs, _ = _mixed_specs(fp32)
+    G0, aa0, x0 = specs[0]
+    x14 = np.zeros((len(x0), 14))
+    x14[:, :3] = x0
+    x14[:, 3:] = -3.0
+    host_specs = [(G, x, aa) for G, aa, x in specs] + [(G0, x0, aa0), (G0, x14, aa0)]  # x0 twice: one upload
+    got = ctx.batch(host_specs, flags)
+    want = _batch(ctx, specs, flags)
+    for a, b in zip(got, want):
+        assert np.array_equal(a, b)
+    assert np.array_equal(got[-2], want[0]) and np.array_equal(got[-1], want[0])
