@@ -88,7 +88,7 @@ typedef struct st_stats {
   double ms_bin;       /* device time of the binning kernels (ms) */
   double ms_column;    /* device time of the column kernel (ms) */
   int32_t column_kernel; /* 1 general FP32, 2 slab-ring FP32 (for at least one image), 3 FP64 */
-  int32_t pad0;
+  int32_t ring_variant;  /* occupancy variant of the last slab-ring launch, -1 if none ran */
 } st_stats;
 
 /* Context on CUDA device `device` (made current for the calls). */
@@ -109,6 +109,18 @@ int st_image(st_ctx* ctx, const st_geom* geom, const double* x, int64_t ldx, int
  * the context's stream).  Returns after the image is complete. */
 int st_image_device(st_ctx* ctx, const st_geom* geom, const double* d_x, int64_t ldx, int64_t nAtoms,
                     const double* aa, int32_t nPrec, int32_t flags, double* d_img, void* stream);
+
+/* Launch tuning of the slab-ring FP32 kernel.  Its variants differ only in the
+ * register budget per thread (CTAs per SM) and compute identical images.
+ * ST_TUNE_AUTO (the default): the first pass of each (angles per pass,
+ * density) kind in a context times every variant on the real work and keeps
+ * the fastest for the context's later calls.  ST_TUNE_OFF: variant 0 always.
+ * mode >= 0: that variant always.  No counterpart in the reference. */
+#define ST_TUNE_AUTO (-1)
+#define ST_TUNE_OFF (-2)
+int st_tune(st_ctx* ctx, int32_t mode);
+/* Number of slab-ring variants (valid forced modes are 0 .. count - 1). */
+int st_tune_variants(void);
 
 /* One image of a batch: its geometry, its atoms, its precession parameters
  * aa(1:nPrec) in host memory, and its output.  x and img are device pointers

@@ -21,6 +21,8 @@ ST_FLAG_FP32 = 0x1
 ST_FLAG_AVERAGE = 0x2
 ST_FLAG_BRIGHT = 0x4
 ST_FLAG_STATS = 0x8
+ST_TUNE_AUTO = -1
+ST_TUNE_OFF = -2
 
 ST_BLUR_NOALLOC_MAX_PIXELS = 1 << 21
 ST_BLUR_NOALLOC_MAX_NX = 4096
@@ -45,7 +47,7 @@ class StStats(ctypes.Structure):
     """st_stats of include/stem.h."""
     _fields_ = [("n_atoms", _i64), ("n_kept", _i64), ("n_tests", _i64), ("n_accepted", _i64),
                 ("n_voxels", _i64), ("max_cell_count", _i32), ("n_prec", _i32), ("ms_bin", _d),
-                ("ms_column", _d), ("column_kernel", _i32), ("pad0", _i32)]
+                ("ms_column", _d), ("column_kernel", _i32), ("ring_variant", _i32)]
 
 
 class StJob(ctypes.Structure):
@@ -73,6 +75,8 @@ _PROTOS = {
     "st_blur_noalloc": (_i32, [_vp, _i32, _i32, _d, _vp, _vp, ctypes.c_char_p, _i32]),
     "st_batch_device": (_i32, [_vp, _i32, ctypes.POINTER(StJob), _i32, _vp]),
     "st_batch": (_i32, [_vp, _i32, ctypes.POINTER(StJob), _i32]),
+    "st_tune": (_i32, [_vp, _i32]),
+    "st_tune_variants": (_i32, []),
     # include/stem_host.h
     "st_d2bi_create": (_i32, [ctypes.POINTER(_vp), _dp, _i32, _i32, _i32, _d, _dp, _dp, _d, _i32, _i32]),
     "st_d2bi_destroy": (None, [_vp]),

@@ -66,7 +66,7 @@ struct Scratch {
   double* xfv = nullptr; // fractional voxel offset per ix
   int2* ytab = nullptr;
   double* yfv = nullptr;
-  int2* ztab = nullptr;
+  int2* ztab = nullptr;  // (home cell, FP32 bits of the slab-ring kernel's scaled slice depth) per iz
   double* zfv = nullptr;
   size_t cap_x = 0, cap_y = 0, cap_z = 0;
   double* aa = nullptr;
@@ -124,9 +124,13 @@ struct ColumnJob {
   int pad;
 };
 int column_tiles(const ColumnParams& p);
+// `variant` selects the register budget (occupancy) of the launch, 0 .. ring_variant_count() - 1;
+// every variant computes the same image to the last bit.
 cudaError_t launch_column_fp32_ring(const ColumnJob* d_jobs, int n_jobs, int total_tiles, int max_np, bool density,
-                                    bool stats, unsigned* work, const unsigned long long* counters, int64_t cap,
-                                    cudaStream_t st);
+                                    bool stats, int variant, unsigned* work, const unsigned long long* counters,
+                                    int64_t cap, cudaStream_t st);
+int ring_variant_count();
+int ring_np_bucket(int max_np);  // the kernel template (angles per pass) serving max_np angles
 cudaError_t launch_column_fp64(const ColumnParams& p, cudaStream_t st);
 cudaError_t launch_epilogue(double* img, int Mx, int My, int ix0, int ix1, int iy0, int iy1, double scale,
                             int bright, cudaStream_t st);

@@ -21,6 +21,8 @@
 //   packed FP32x2 multiply-adds.
 // * The RK4 double step (ii, ii+1, ii+2) runs once per step in registers for
 //   every precession angle; the periodic closure uses the saved first sample.
+// * The march does no FP64 arithmetic: the slice depths come from a per-image
+//   table of FP32 values that the host computes in FP64.
 //
 // It needs every link cell to be at least 3 sigma wide (then "within 3 sigma"
 // equals the reference's 27-cell search) and at most kCaps staged atoms per
@@ -295,10 +297,14 @@ __device__ __noinline__ bool column_tile(const ColumnParams& p, WarpSmem& W, int
   const float r2_to_A2 = (float)(1.0 / (sd * sd));    // scaled r^2 back to A^2 (density)
 
   const int np = min(NP, p.n_prec - p.prec_offset);
-  float aa[NP], ph[NP][4];
+  // the precession coefficients a_k stay in registers for few angles; for many they are
+  // read from L1 at each step, which leaves the registers to the phases
+  constexpr bool kAaReg = NP <= 4;
+  const float* __restrict__ aag = p.aaf + p.prec_offset;
+  float aa[kAaReg ? NP : 1], ph[NP][4];
 #pragma unroll
   for (int k = 0; k < NP; ++k) {
-    aa[k] = (k < np) ? p.aaf[p.prec_offset + k] : 0.f;
+    if (kAaReg) aa[k] = (k < np) ? aag[k] : 0.f;
     ph[k][0] = 1.f;
     ph[k][1] = ph[k][2] = ph[k][3] = 0.f;
   }
@@ -309,11 +315,11 @@ __device__ __noinline__ bool column_tile(const ColumnParams& p, WarpSmem& W, int
 
   for (int z0 = 0; z0 < p.Mz; z0 += 2) {
     const bool has1 = z0 + 1 < p.Mz;
-    const int hz0 = p.ztab[z0].x;
-    const int hz1 = has1 ? p.ztab[z0 + 1].x : hz0;
-    // slice depths (scaled) relative to the origin of home cell hz0
-    const float zv0 = (float)(p.a33 * p.zfv[z0] * sd);
-    const float zv1 = has1 ? (float)(p.a33 * (p.zfv[z0 + 1] + (double)(hz1 - hz0)) * sd) : zv0;
+    // home cells and slice depths (scaled, relative to the origin of home cell hz0)
+    const int2 e0 = p.ztab[z0];
+    const int2 e1 = has1 ? p.ztab[z0 + 1] : e0;
+    const int hz0 = e0.x, hz1 = e1.x;
+    const float zv0 = __int_as_float(e0.y), zv1 = __int_as_float(e1.y);
     const int need_lo = hz0 - 1, need_hi = hz1 + 1;
     if (need_lo > ring_hi || need_hi < ring_lo) {
       ring_lo = need_lo;
@@ -398,7 +404,7 @@ __device__ __noinline__ bool column_tile(const ColumnParams& p, WarpSmem& W, int
     } else {
 #pragma unroll
       for (int k = 0; k < NP; ++k)
-        if (k < np) rk4(s_prev, s_mid, s0, aa[k], dzs, ph[k]);
+        if (k < np) rk4(s_prev, s_mid, s0, kAaReg ? aa[k] : __ldg(aag + k), dzs, ph[k]);
     }
     s_prev = s0;
     if (has1) s_mid = make_sample<kDensity>(sr.y, si.y, rm1, b0, bg, sig, p.use_density != 0);
@@ -406,7 +412,7 @@ __device__ __noinline__ bool column_tile(const ColumnParams& p, WarpSmem& W, int
   if ((p.Mz & 1) == 0) {  // closure x(Mz) = x(0)
 #pragma unroll
     for (int k = 0; k < NP; ++k)
-      if (k < np) rk4(s_prev, s_mid, s_first, aa[k], dzs, ph[k]);
+      if (k < np) rk4(s_prev, s_mid, s_first, kAaReg ? aa[k] : __ldg(aag + k), dzs, ph[k]);
   }
   float acc = 0.f;
 #pragma unroll
@@ -433,8 +439,8 @@ __device__ __noinline__ bool column_tile(const ColumnParams& p, WarpSmem& W, int
 // Persistent launch over the warp tiles of every job of a batch: each warp
 // takes the next tile from a global counter, so images of uneven size share
 // the GPU without a tail per image.
-template <int NP, bool kDensity, bool kStats>
-__global__ void __launch_bounds__(kWarps * 32, (NP >= 16 ? 4 : 5))
+template <int NP, bool kDensity, bool kStats, int kMinBlocks>
+__global__ void __launch_bounds__(kWarps * 32, kMinBlocks)
     k_column_fp32_v2(const ColumnJob* __restrict__ jobs, int n_jobs, int total_tiles, unsigned* __restrict__ work,
                      const unsigned long long* __restrict__ counters, int64_t cap) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -476,14 +482,32 @@ cudaError_t launch(K kernel, const ColumnJob* jobs, int n_jobs, int total_tiles,
   return cudaGetLastError();
 }
 
+// Occupancy variants: variant v sets the register budget for (base - v) CTAs per SM,
+// base = 5 for up to 8 precession angles per pass (96 registers), 4 for 16 (128).  The
+// arithmetic is the same in every variant; the host's autotuner picks by timing.
+constexpr int kVariants = 2;
+inline int base_blocks(int np) { return np <= 8 ? 5 : 4; }
+
+template <int NP, bool kDensity, bool kStats>
+cudaError_t launch_v(int v, const ColumnJob* jobs, int n_jobs, int total_tiles, unsigned* work,
+                     const unsigned long long* counters, int64_t cap, cudaStream_t st) {
+  constexpr int B = NP <= 8 ? 5 : 4;
+  if constexpr (!kStats) {
+    if (v == 1)
+      return launch(k_column_fp32_v2<NP, kDensity, kStats, B - 1>, jobs, n_jobs, total_tiles, work, counters, cap,
+                    B - 1, st);
+  }
+  return launch(k_column_fp32_v2<NP, kDensity, kStats, B>, jobs, n_jobs, total_tiles, work, counters, cap, B, st);
+}
+
 template <bool kDensity, bool kStats>
-cudaError_t launch_np(int np, const ColumnJob* jobs, int n_jobs, int total_tiles, unsigned* work,
+cudaError_t launch_np(int np, int v, const ColumnJob* jobs, int n_jobs, int total_tiles, unsigned* work,
                       const unsigned long long* counters, int64_t cap, cudaStream_t st) {
-  if (np <= 1) return launch(k_column_fp32_v2<1, kDensity, kStats>, jobs, n_jobs, total_tiles, work, counters, cap, 5, st);
-  if (np <= 2) return launch(k_column_fp32_v2<2, kDensity, kStats>, jobs, n_jobs, total_tiles, work, counters, cap, 5, st);
-  if (np <= 4) return launch(k_column_fp32_v2<4, kDensity, kStats>, jobs, n_jobs, total_tiles, work, counters, cap, 5, st);
-  if (np <= 8) return launch(k_column_fp32_v2<8, kDensity, kStats>, jobs, n_jobs, total_tiles, work, counters, cap, 5, st);
-  return launch(k_column_fp32_v2<16, kDensity, kStats>, jobs, n_jobs, total_tiles, work, counters, cap, 4, st);
+  if (np <= 1) return launch_v<1, kDensity, kStats>(v, jobs, n_jobs, total_tiles, work, counters, cap, st);
+  if (np <= 2) return launch_v<2, kDensity, kStats>(v, jobs, n_jobs, total_tiles, work, counters, cap, st);
+  if (np <= 4) return launch_v<4, kDensity, kStats>(v, jobs, n_jobs, total_tiles, work, counters, cap, st);
+  if (np <= 8) return launch_v<8, kDensity, kStats>(v, jobs, n_jobs, total_tiles, work, counters, cap, st);
+  return launch_v<16, kDensity, kStats>(v, jobs, n_jobs, total_tiles, work, counters, cap, st);
 }
 
 }  // namespace
@@ -494,15 +518,21 @@ int column_tiles(const ColumnParams& p) {
   return ((Wd + kTileX - 1) / kTileX) * ((Hd + kTileY - 1) / kTileY);
 }
 
+int ring_variant_count() { return kVariants; }
+
+int ring_np_bucket(int max_np) { return max_np <= 1 ? 1 : max_np <= 2 ? 2 : max_np <= 4 ? 4 : max_np <= 8 ? 8 : 16; }
+
 cudaError_t launch_column_fp32_ring(const ColumnJob* d_jobs, int n_jobs, int total_tiles, int max_np, bool density,
-                                    bool stats, unsigned* work, const unsigned long long* counters, int64_t cap,
-                                    cudaStream_t st) {
+                                    bool stats, int variant, unsigned* work, const unsigned long long* counters,
+                                    int64_t cap, cudaStream_t st) {
   cudaMemsetAsync(work, 0, sizeof(unsigned), st);
   if (total_tiles <= 0) return cudaSuccess;
-  if (density) return stats ? launch_np<true, true>(max_np, d_jobs, n_jobs, total_tiles, work, counters, cap, st)
-                            : launch_np<true, false>(max_np, d_jobs, n_jobs, total_tiles, work, counters, cap, st);
-  return stats ? launch_np<false, true>(max_np, d_jobs, n_jobs, total_tiles, work, counters, cap, st)
-               : launch_np<false, false>(max_np, d_jobs, n_jobs, total_tiles, work, counters, cap, st);
+  const int v = (variant > 0 && variant < kVariants && !stats) ? variant : 0;  // statistics: variant 0
+  if (density)
+    return stats ? launch_np<true, true>(max_np, v, d_jobs, n_jobs, total_tiles, work, counters, cap, st)
+                 : launch_np<true, false>(max_np, v, d_jobs, n_jobs, total_tiles, work, counters, cap, st);
+  return stats ? launch_np<false, true>(max_np, v, d_jobs, n_jobs, total_tiles, work, counters, cap, st)
+               : launch_np<false, false>(max_np, v, d_jobs, n_jobs, total_tiles, work, counters, cap, st);
 }
 
 }  // namespace stem

@@ -14,6 +14,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -54,6 +55,10 @@ struct st_ctx {
   int64_t last_kept = 0;       // kept atoms of the previous call: sizes the next one
   bool fp32_general = false;   // STEM_FP32_KERNEL=general: always use k_column_fp32
   int last_column_kernel = 0;  // 1 general FP32, 2 slab-ring FP32, 3 FP64
+  int tune_mode = ST_TUNE_AUTO;
+  std::map<int, int> ring_tuned;  // (angles per pass, density) -> fastest slab-ring variant
+  cudaEvent_t tev[3] = {nullptr, nullptr, nullptr};
+  int last_ring_variant = -1;
 };
 
 namespace {
@@ -115,6 +120,12 @@ bool alloc_kept(st_ctx* c, size_t need) {
   return true;
 }
 
+int __float_as_int_host(float v) {
+  int b;
+  std::memcpy(&b, &v, sizeof b);
+  return b;
+}
+
 bool is_cuboid(const double* m) {
   return m[1] == 0.0 && m[2] == 0.0 && m[3] == 0.0 && m[5] == 0.0 && m[6] == 0.0 && m[7] == 0.0;
 }
@@ -131,6 +142,21 @@ void axis_table(int n, double a_vox, double lcd, double ia, int N, int2* tab, do
     if (h < 0) h += N;  // the reference's mod of a non-negative value
     tab[i] = make_int2(h, 0);
     fv[i] = zi - (double)h;
+  }
+}
+
+// Slice depths for the slab-ring kernel, in the .y half of the z table: the depth of
+// slice z (FP32 bits) in units scaled by s = sqrt(log2 e / (2 sigma^2)), measured from the
+// origin of the home cell of the even slice of its pair (z & ~1), which is the frame the
+// kernel marches in.  Computed in FP64 exactly as a33 (fv + dh) s, rounded once to FP32.
+void depth_table(const st_geom* g, int2* tab, const double* fv) {
+  const double i2s2 = 1 / (2 * g->sigma * g->sigma);
+  const double sd = std::sqrt(i2s2 * 1.4426950408889634);
+  const double a33 = g->a_col[8];
+  for (int z = 0; z < g->Mz; ++z) {
+    const int h_even = tab[z & ~1].x;
+    const float v = (z & 1) ? (float)(a33 * (fv[z] + (double)(tab[z].x - h_even)) * sd) : (float)(a33 * fv[z] * sd);
+    tab[z].y = __float_as_int_host(v);
   }
 }
 
@@ -246,6 +272,36 @@ ColumnParams column_params(st_ctx* c, const Job& j, int64_t cell_base, size_t xo
   cp.img = j.d_img;
   cp.counters = c->s.counters;
   return cp;
+}
+
+// Times every slab-ring variant once on the same pass (each overwrites the pass's
+// images with the same values) and returns the fastest in `best`, or -1 when a
+// trial found the binning or a slab overflowed (the timings mean nothing then).
+template <typename F>
+cudaError_t tune_ring(st_ctx* c, F&& launch_variant, int64_t cap, cudaStream_t st, int& best) {
+  best = -1;
+  cudaError_t e = cudaSuccess;
+  for (int i = 0; i < 3 && e == cudaSuccess; ++i)
+    if (!c->tev[i]) e = cudaEventCreate(&c->tev[i]);
+  const int nv = ring_variant_count();
+  std::vector<float> ms(nv, 0.f);
+  for (int v = 0; v < nv && e == cudaSuccess; ++v) {
+    cudaEventRecord(c->tev[0], st);
+    e = launch_variant(v);
+    cudaEventRecord(c->tev[1], st);
+    if (e == cudaSuccess) e = cudaEventSynchronize(c->tev[1]);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms[v], c->tev[0], c->tev[1]);
+  }
+  if (e != cudaSuccess) return e;
+  unsigned long long h[5];
+  e = cudaMemcpy(h, c->s.counters, sizeof h, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return e;
+  if (h[4] != 0 || (int64_t)h[0] > cap) return cudaSuccess;
+  best = 0;
+  for (int v = 1; v < nv; ++v)
+    if (ms[v] < ms[best]) best = v;
+  c->last_ring_variant = best;
+  return cudaSuccess;
 }
 
 // The slab-ring FP32 kernel needs cells of at least 3 sigma (no truncated
@@ -389,6 +445,7 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
     axis_table(g->Mx, g->a_vox[0], g->lc_delta[0], g->ia_col[0], g->Ex, hxt + xoff[i], hxf + xoff[i]);
     axis_table(g->My, g->a_vox[4], g->lc_delta[1], g->ia_col[4], g->Ey, hyt + yoff[i], hyf + yoff[i]);
     axis_table(g->Mz, g->a_vox[8], g->lc_delta[2], g->ia_col[8], g->Ez, hzt + zoff[i], hzf + zoff[i]);
+    depth_table(g, hzt + zoff[i], hzf + zoff[i]);
     for (int k = 0; k < jobs[i].n_prec; ++k) {
       haa[aoff[i] + k] = jobs[i].aa[k];
       haaf[aoff[i] + k] = (float)jobs[i].aa[k];
@@ -462,10 +519,35 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
     if (e != cudaSuccess) return cuda_fail(c, e, "clearing images");
     cudaEventRecord(c->ev[1], st);
     used_ring = ring;
-    for (int pass = 0; ring && pass < passes && e == cudaSuccess; ++pass)
-      e = launch_column_fp32_ring(c->d_coljobs + (size_t)pass * n_ring, n_ring, pass_tiles[pass],
-                                  std::min(width, ring_np - pass * width), dens, (flags & ST_FLAG_STATS) != 0,
-                                  c->d_work, c->s.counters, cap, st);
+    for (int pass = 0; ring && pass < passes && e == cudaSuccess; ++pass) {
+      const int np_pass = std::min(width, ring_np - pass * width);
+      const bool stats = (flags & ST_FLAG_STATS) != 0;
+      auto ring_launch = [&](int v) {
+        return launch_column_fp32_ring(c->d_coljobs + (size_t)pass * n_ring, n_ring, pass_tiles[pass], np_pass,
+                                       dens, stats, v, c->d_work, c->s.counters, cap, st);
+      };
+      const int key = ring_np_bucket(np_pass) * 2 + (dens ? 1 : 0);
+      int v = 0;
+      if (c->tune_mode >= 0) {
+        v = c->tune_mode;
+      } else if (c->tune_mode == ST_TUNE_AUTO && !stats) {
+        auto it = c->ring_tuned.find(key);
+        if (it != c->ring_tuned.end()) {
+          v = it->second;
+        } else if (pass == 0 && pass_tiles[0] >= 4096) {
+          // autotune on the real work: the first pass overwrites its images, so every trial
+          // leaves the same result; keep the fastest for the later calls of this context
+          e = tune_ring(c, ring_launch, cap, st, v);
+          if (e == cudaSuccess && v >= 0) {
+            c->ring_tuned[key] = v;
+            continue;  // the last trial's output is the pass's result
+          }
+          v = 0;
+        }
+      }
+      if (e == cudaSuccess) e = ring_launch(v);
+      c->last_ring_variant = stats ? 0 : v;
+    }
     if (e == cudaSuccess && n_ring < n) e = columns_per_image(cap, false);
     if (e == cudaSuccess) e = epilogues();
     if (e != cudaSuccess) return cuda_fail(c, e, "column kernel launch");
@@ -512,6 +594,7 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
   cudaEventElapsedTime(&ms, c->ev[1], c->ev[2]);
   S.ms_column = ms;
   S.column_kernel = c->last_column_kernel;
+  S.ring_variant = used_ring ? c->last_ring_variant : -1;
   // the reference stops when a link cell needs more than 16 x nMax0 slots; a batch's
   // largest cell is checked against the smallest nMax0 of its images
   int min_nmax0 = 0;
@@ -567,9 +650,21 @@ extern "C" void st_destroy(st_ctx* c) {
   if (c->h_stage) cudaFreeHost(c->h_stage);
   for (auto& e : c->ev)
     if (e) cudaEventDestroy(e);
+  for (auto& e : c->tev)
+    if (e) cudaEventDestroy(e);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
+
+extern "C" int st_tune(st_ctx* c, int32_t mode) {
+  if (!c) return ST_ERR_ARG;
+  if (mode != ST_TUNE_AUTO && mode != ST_TUNE_OFF && (mode < 0 || mode >= ring_variant_count()))
+    return fail(c, ST_ERR_ARG, "tuning mode must be ST_TUNE_AUTO, ST_TUNE_OFF or a variant index");
+  c->tune_mode = mode;
+  return ST_OK;
+}
+
+extern "C" int st_tune_variants(void) { return ring_variant_count(); }
 
 extern "C" const char* st_last_error(const st_ctx* c) { return c ? c->err.c_str() : "null context"; }
 

@@ -133,6 +133,10 @@ class Context:
         self._check(lib().st_blur_device(self.handle, ctypes.c_void_p(in_ptr), nx, ny, float(t),
                                          ctypes.c_void_p(out_ptr), ctypes.c_void_p(stream)))
 
+    def tune(self, mode):
+        """st_tune: ST_TUNE_AUTO, ST_TUNE_OFF or a forced slab-ring variant (0 .. st_tune_variants() - 1)."""
+        self._check(lib().st_tune(self.handle, int(mode)))
+
     def stats(self):
         s = StStats()
         self._check(lib().st_get_stats(self.handle, ctypes.byref(s)))

@@ -211,3 +211,36 @@ def test_host_batch_equals_device_batch(ctx, fp32):
     for a, b in zip(got, want):
         assert np.array_equal(a, b)
     assert np.array_equal(got[-2], want[0]) and np.array_equal(got[-1], want[0])
+
+
+def test_ring_variants_identical_and_autotuned():
+    """Every occupancy variant of the slab-ring kernel computes the same image to the last
+    bit; with ST_TUNE_AUTO a context times them on its first large pass and keeps one."""
+    cell = synth.make_cell(70, 70, 8, 11, n_voids=2, void_radius=(5.0, 8.0), with_screw=True)
+    t, so, x = _condition(cell, sg=0.01, density=True)
+    G, aa = t.image_geometry(len(x), n_prec=3)
+    flags = _lib.ST_FLAG_FP32 | _lib.ST_FLAG_AVERAGE
+    n_var = _lib.lib().st_tune_variants()
+    assert n_var >= 2
+    imgs = []
+    c = imaging.Context(0)
+    try:
+        for v in range(n_var):
+            c.tune(v)
+            imgs.append(c.image(G, x, aa, flags=flags))
+            assert c.stats().ring_variant == v
+        c.tune(_lib.ST_TUNE_AUTO)
+        auto = c.image(G, x, aa, flags=flags)
+        chosen = c.stats().ring_variant
+        assert 0 <= chosen < n_var
+        again = c.image(G, x, aa, flags=flags)
+        assert c.stats().ring_variant == chosen
+        with pytest.raises(_lib.StemError):
+            c.tune(n_var)
+    finally:
+        c.close()
+    for im in imgs[1:] + [auto, again]:
+        assert np.array_equal(im, imgs[0])
+    Go, aao = O.geometry(so, len(x), nPrec=3, precAngle=0.005)
+    want, _ = O.patch_image(Go, aao, x, nthreads=8)
+    assert np.abs(imgs[0] - want / 3).max() <= FP32_TOL
