@@ -109,6 +109,28 @@ def time_batch(ctx, jobs, flags, stream, steps, warmup, flush):
     return ms
 
 
+def time_plan(ctx, jobs, flags, stream, steps, warmup, flush):
+    """CUDA-event time of st_plan_launch + st_plan_wait (a recorded batch replayed), L2
+    flushed before each replay."""
+    import torch
+    sptr = stream.cuda_stream
+    plan = ctx.plan(jobs, flags, sptr)
+    ms = []
+    try:
+        for i in range(warmup + steps):
+            flush.fill_(float(i))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            plan.launch(sptr)
+            e1.record(stream)
+            plan.wait(sptr)
+            if i >= warmup:
+                ms.append(e0.elapsed_time(e1))
+    finally:
+        plan.close()
+    return ms
+
+
 def batched_legs(ctx, cell, stream, flush, steps, warmup):
     """The two batched workloads through st_batch_device: the tilt x precession x g
     sweep on the 1.2M-atom cell and the 256-cell uneven batch, FP32 path; for each,
@@ -147,6 +169,10 @@ def batched_legs(ctx, cell, stream, flush, steps, warmup):
                     "kept_atoms": st.n_kept, "column_kernel": st.column_kernel,
                     "ms_bin": st.ms_bin, "ms_column": st.ms_column,
                     "accuracy_one_image": accuracy(G, d_x.data_ptr(), len(x), aa, imgs[k])}
+    pms = time_plan(ctx, jobs, f32, stream, steps, 1, flush)
+    tp = float(np.mean(pms)) * 1e-3
+    out["sweep"]["plan"] = {"note": "the same batch recorded once as a CUDA graph (st_plan) and replayed",
+                            "ms_per_batch": tp * 1e3, "images_per_s": n_img / tp, "passes_per_s": n_pass / tp}
     del imgs, jobs
 
     # 256 independent cells of uneven size
@@ -380,6 +406,11 @@ def run_gpu(args):
         e2e_ms.append((time.perf_counter() - t1) * 1e3)
     e2e_value = ws * 1000.0 / float(np.mean(e2e_ms))
 
+    # the same image recorded as a CUDA graph (st_plan) and replayed
+    pms = time_plan(ctx, [(G, d_x.data_ptr(), len(x), aa, d_img.data_ptr())], flags, stream, args.steps,
+                    args.warmup, flush)
+    plan_value = ws * 1000.0 / float(np.mean(pms))
+
     # plain FP64 GPU path on the same image
     step(_lib.ST_FLAG_AVERAGE)
     torch.cuda.synchronize()
@@ -416,6 +447,8 @@ def run_gpu(args):
             "e2e": {"value": e2e_value, "unit": "images/s", "h2d_bytes_per_step": int(x.nbytes),
                     "d2h_bytes_per_step": int(G.Mx * G.My * 8)},
             "fp64": {"value": 1000.0 / fp64_ms, "unit": "images/s", "ms": fp64_ms},
+            "plan": {"value": plan_value, "unit": "images/s",
+                     "note": "the same step recorded once as a CUDA graph (st_plan) and replayed"},
             "accuracy": {"max_abs_dI_fp32_vs_fp64": float(np.abs(d).max()),
                          "rms_dI_fp32_vs_fp64": float(np.sqrt((d ** 2).mean()))},
             "gpu_launches": args.steps * launches_per_image(n_prec, fp32=True, average=True),

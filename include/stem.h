@@ -153,6 +153,30 @@ int st_batch_device(st_ctx* ctx, int32_t n_jobs, const st_job* jobs, int32_t fla
  * once.  The images are copied back before it returns. */
 int st_batch(st_ctx* ctx, int32_t n_jobs, const st_job* jobs, int32_t flags);
 
+/* A batch recorded as a CUDA graph, for the same images computed again and
+ * again (a trajectory whose atoms move, a sweep repeated on new data): the
+ * binning, the persistent column launch(es), the epilogues and the read-back
+ * of the overflow counters are replayed without host work.  The plan keeps
+ * copies of the geometries and aa; the device buffers x and img of the jobs
+ * must stay allocated while the plan exists (their contents may change, nAtoms
+ * may not).  The plan owns its own device memory (the context's stays free
+ * for other calls) and inherits the context's tuning.
+ *
+ * st_plan_create runs the batch once (the images are then complete) and
+ * records it.  st_plan_launch enqueues one replay on `stream` and returns.
+ * st_plan_wait waits for it; when the replay's binning outgrew the recorded
+ * capacity or a slab overflowed, it recomputes the batch on the eager path
+ * (then the images are right) and records the plan again.  No counterpart in
+ * the reference. */
+typedef struct st_plan st_plan;
+int st_plan_create(st_ctx* ctx, int32_t n_jobs, const st_job* jobs, int32_t flags, void* stream, st_plan** plan);
+int st_plan_launch(st_plan* plan, void* stream);
+int st_plan_wait(st_plan* plan, void* stream);
+/* Statistics of the plan's last eager run (counts) or replay (n_kept). */
+int st_plan_stats(const st_plan* plan, st_stats* out);
+const char* st_plan_last_error(const st_plan* plan);
+void st_plan_destroy(st_plan* plan);
+
 /* Gaussian blur of width t pixels (src/d2bi.f90:1543-1624) from host buffers;
  * in and out are nx x ny doubles, column-major; out is overwritten. */
 int st_blur(st_ctx* ctx, const double* in, int32_t nx, int32_t ny, double t, double* out);

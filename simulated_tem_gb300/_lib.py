@@ -76,6 +76,12 @@ _PROTOS = {
     "st_batch_device": (_i32, [_vp, _i32, ctypes.POINTER(StJob), _i32, _vp]),
     "st_batch": (_i32, [_vp, _i32, ctypes.POINTER(StJob), _i32]),
     "st_tune": (_i32, [_vp, _i32]),
+    "st_plan_create": (_i32, [_vp, _i32, ctypes.POINTER(StJob), _i32, _vp, ctypes.POINTER(_vp)]),
+    "st_plan_launch": (_i32, [_vp, _vp]),
+    "st_plan_wait": (_i32, [_vp, _vp]),
+    "st_plan_stats": (_i32, [_vp, ctypes.POINTER(StStats)]),
+    "st_plan_last_error": (ctypes.c_char_p, [_vp]),
+    "st_plan_destroy": (None, [_vp]),
     "st_tune_variants": (_i32, []),
     # include/stem_host.h
     "st_d2bi_create": (_i32, [ctypes.POINTER(_vp), _dp, _i32, _i32, _i32, _d, _dp, _dp, _d, _i32, _i32]),

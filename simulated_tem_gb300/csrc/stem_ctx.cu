@@ -308,8 +308,15 @@ cudaError_t tune_ring(st_ctx* c, F&& launch_variant, int64_t cap, cudaStream_t s
 // search) and at least one voxel thick in z.
 bool ring_eligible(const ColumnParams& cp) { return !cp.check_cells && cp.Ez <= cp.Mz; }
 
+// A recorded call (st_plan): the instantiated graph and what its kernels were recorded with.
+struct GraphOut {
+  cudaGraphExec_t exec = nullptr;
+  int64_t cap = 0;    // kept-atom capacity the binning was recorded with
+  bool ring = false;  // the slab-ring kernel ran (its slab overflow needs the eager path)
+};
+
 // Image the jobs: binning of all, then the column kernels, then the epilogues.
-int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStream_t st) {
+int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStream_t st, GraphOut* gout = nullptr) {
   const int n = (int)jobs.size();
   const bool fp32 = (flags & ST_FLAG_FP32) != 0;
   // concatenation offsets
@@ -498,7 +505,61 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
     return ce;
   };
 
-  bool used_ring = ring;
+  // Everything a call enqueues after the tables: binning, clearing, column kernels,
+  // epilogues and the read-back of the counters.  `capturing`: no events, no tuning
+  // (the variants and the kernel choice of the eager run are replayed).
+  bool ring_ok = ring;  // false once a slab overflowed: every image takes the general kernel
+  const bool stats = (flags & ST_FLAG_STATS) != 0;
+  std::vector<int> pass_variant(passes, 0);
+  auto enqueue = [&](bool capturing) -> cudaError_t {
+    cudaError_t ce = cudaSuccess;
+    if (!capturing) cudaEventRecord(c->ev[0], st);
+    ce = launch_bin(c->d_binjobs, n, total_cand, total_cells, cap, c->s, c->b, !fp32, st);
+    if (ce == cudaSuccess) ce = launch_bin_finalize(c->d_binjobs, n, total_cells, cap, c->s, c->b, fp32 ? 0 : 1, st);
+    if (ce == cudaSuccess) ce = clear_images();
+    if (!capturing) cudaEventRecord(c->ev[1], st);
+    for (int pass = 0; ring_ok && pass < passes && ce == cudaSuccess; ++pass) {
+      const int np_pass = std::min(width, ring_np - pass * width);
+      auto ring_launch = [&](int v) {
+        return launch_column_fp32_ring(c->d_coljobs + (size_t)pass * n_ring, n_ring, pass_tiles[pass], np_pass,
+                                       dens, stats, v, c->d_work, c->s.counters, cap, st);
+      };
+      if (capturing) {
+        ce = ring_launch(pass_variant[pass]);
+        continue;
+      }
+      const int key = ring_np_bucket(np_pass) * 2 + (dens ? 1 : 0);
+      int v = 0;
+      if (c->tune_mode >= 0) {
+        v = c->tune_mode;
+      } else if (c->tune_mode == ST_TUNE_AUTO && !stats) {
+        auto it = c->ring_tuned.find(key);
+        if (it != c->ring_tuned.end()) {
+          v = it->second;
+        } else if (pass == 0 && pass_tiles[0] >= 4096) {
+          // autotune on the real work: the first pass overwrites its images, so every trial
+          // leaves the same result; keep the fastest for the later calls of this context
+          ce = tune_ring(c, ring_launch, cap, st, v);
+          if (ce == cudaSuccess && v >= 0) {
+            c->ring_tuned[key] = v;
+            pass_variant[pass] = v;
+            continue;  // the last trial's output is the pass's result
+          }
+          v = 0;
+        }
+      }
+      if (ce == cudaSuccess) ce = ring_launch(v);
+      pass_variant[pass] = v;
+      c->last_ring_variant = stats ? 0 : v;
+    }
+    if (ce == cudaSuccess && (!ring_ok || n_ring < n)) ce = columns_per_image(cap, !ring_ok);
+    if (ce == cudaSuccess) ce = epilogues();
+    if (!capturing) cudaEventRecord(c->ev[2], st);
+    if (ce == cudaSuccess)
+      ce = cudaMemcpyAsync(c->h_counters, c->s.counters, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
+    return ce;
+  };
+
   for (int attempt = 0;; ++attempt) {
     if (attempt > 0) {
       // grown kept-atom arrays move: point the column parameters and the ring's job table at them
@@ -511,48 +572,7 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
         if (e != cudaSuccess) return cuda_fail(c, e, "copying column jobs");
       }
     }
-    cudaEventRecord(c->ev[0], st);
-    e = launch_bin(c->d_binjobs, n, total_cand, total_cells, cap, c->s, c->b, !fp32, st);
-    if (e == cudaSuccess) e = launch_bin_finalize(c->d_binjobs, n, total_cells, cap, c->s, c->b, fp32 ? 0 : 1, st);
-    if (e != cudaSuccess) return cuda_fail(c, e, "binning launch");
-    e = clear_images();
-    if (e != cudaSuccess) return cuda_fail(c, e, "clearing images");
-    cudaEventRecord(c->ev[1], st);
-    used_ring = ring;
-    for (int pass = 0; ring && pass < passes && e == cudaSuccess; ++pass) {
-      const int np_pass = std::min(width, ring_np - pass * width);
-      const bool stats = (flags & ST_FLAG_STATS) != 0;
-      auto ring_launch = [&](int v) {
-        return launch_column_fp32_ring(c->d_coljobs + (size_t)pass * n_ring, n_ring, pass_tiles[pass], np_pass,
-                                       dens, stats, v, c->d_work, c->s.counters, cap, st);
-      };
-      const int key = ring_np_bucket(np_pass) * 2 + (dens ? 1 : 0);
-      int v = 0;
-      if (c->tune_mode >= 0) {
-        v = c->tune_mode;
-      } else if (c->tune_mode == ST_TUNE_AUTO && !stats) {
-        auto it = c->ring_tuned.find(key);
-        if (it != c->ring_tuned.end()) {
-          v = it->second;
-        } else if (pass == 0 && pass_tiles[0] >= 4096) {
-          // autotune on the real work: the first pass overwrites its images, so every trial
-          // leaves the same result; keep the fastest for the later calls of this context
-          e = tune_ring(c, ring_launch, cap, st, v);
-          if (e == cudaSuccess && v >= 0) {
-            c->ring_tuned[key] = v;
-            continue;  // the last trial's output is the pass's result
-          }
-          v = 0;
-        }
-      }
-      if (e == cudaSuccess) e = ring_launch(v);
-      c->last_ring_variant = stats ? 0 : v;
-    }
-    if (e == cudaSuccess && n_ring < n) e = columns_per_image(cap, false);
-    if (e == cudaSuccess) e = epilogues();
-    if (e != cudaSuccess) return cuda_fail(c, e, "column kernel launch");
-    cudaEventRecord(c->ev[2], st);
-    e = cudaMemcpyAsync(c->h_counters, c->s.counters, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
+    e = enqueue(false);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_fail(c, e, "image kernels");
     if ((int64_t)c->h_counters[0] > cap) {
@@ -560,9 +580,9 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
       cap = (int64_t)c->h_counters[0] + (int64_t)c->h_counters[0] / 8 + 1024;  // grow and redo
       continue;
     }
-    if (ring && c->h_counters[4] != 0) {
+    if (ring_ok && c->h_counters[4] != 0) {
       // a slab held more atoms than the ring kernel stages: recompute every image with the general kernel
-      used_ring = false;
+      ring_ok = false;
       cudaMemsetAsync(c->s.counters + 2, 0, 3 * sizeof(unsigned long long), st);
       e = clear_images();
       if (e == cudaSuccess) e = columns_per_image(cap, true);
@@ -575,6 +595,24 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
       if (e != cudaSuccess) return cuda_fail(c, e, "image kernels (general FP32 kernel)");
     }
     break;
+  }
+  const bool used_ring = ring_ok;
+  if (gout) {
+    // record the same work as a CUDA graph for replay (st_plan)
+    if (gout->exec) cudaGraphExecDestroy(gout->exec);
+    gout->exec = nullptr;
+    cudaGraph_t graph = nullptr;
+    e = cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed);
+    if (e == cudaSuccess) {
+      const cudaError_t ce = enqueue(true);
+      e = cudaStreamEndCapture(st, &graph);
+      if (ce != cudaSuccess) e = ce;
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&gout->exec, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return cuda_fail(c, e, "recording the CUDA graph");
+    gout->cap = cap;
+    gout->ring = used_ring;
   }
   c->last_kept = (int64_t)c->h_counters[0];
   c->last_column_kernel = !fp32 ? 3 : (used_ring ? 2 : 1);
@@ -811,6 +849,176 @@ extern "C" int st_batch(st_ctx* c, int32_t n_jobs, const st_job* jobs, int32_t f
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return cuda_fail(c, e, "copying images");
   return ST_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Plans: batches recorded as CUDA graphs
+// ---------------------------------------------------------------------------
+
+struct st_plan {
+  struct Group {
+    st_ctx* c = nullptr;  // private context: the recorded pointers are its buffers
+    std::vector<Job> jobs;
+    GraphOut g;
+  };
+  int device = 0;
+  int32_t flags = 0;
+  std::vector<st_geom> geoms;
+  std::vector<std::vector<double>> aas;
+  std::vector<Group> groups;
+  std::string err;
+  st_stats stats{};
+};
+
+namespace {
+
+int plan_fail(st_plan* p, int code, const std::string& msg) {
+  p->err = msg;
+  return code;
+}
+
+// Eager run of one group, recorded into its graph.
+int plan_record(st_plan* p, st_plan::Group& G, cudaStream_t st) {
+  const int rc = run_images(G.c, G.jobs, p->flags, st, &G.g);
+  if (rc != ST_OK) return plan_fail(p, rc, G.c->err);
+  return ST_OK;
+}
+
+void plan_sum_stats(st_plan* p) {
+  st_stats t{};
+  for (auto& G : p->groups) {
+    const st_stats& S = G.c->stats;
+    t.n_atoms += S.n_atoms;
+    t.n_kept += S.n_kept;
+    t.n_tests += S.n_tests;
+    t.n_accepted += S.n_accepted;
+    t.n_voxels += S.n_voxels;
+    t.max_cell_count = std::max(t.max_cell_count, S.max_cell_count);
+    t.n_prec = std::max(t.n_prec, S.n_prec);
+    t.ms_bin += S.ms_bin;
+    t.ms_column += S.ms_column;
+    t.column_kernel = std::max(t.column_kernel, S.column_kernel);
+    t.ring_variant = std::max(t.ring_variant, S.ring_variant);
+  }
+  p->stats = t;
+}
+
+}  // namespace
+
+extern "C" int st_plan_create(st_ctx* c, int32_t n_jobs, const st_job* jobs, int32_t flags, void* stream,
+                              st_plan** out) {
+  if (!c || !out) return ST_ERR_ARG;
+  *out = nullptr;
+  std::vector<Job> js;
+  int rc = collect_jobs(c, n_jobs, jobs, js);
+  if (rc != ST_OK) return rc;
+  cudaSetDevice(c->device);
+  st_plan* p = new st_plan();
+  p->device = c->device;
+  p->flags = flags;
+  p->geoms.resize(n_jobs);
+  p->aas.resize(n_jobs);
+  for (int i = 0; i < n_jobs; ++i) {
+    p->geoms[i] = *js[i].g;
+    p->aas[i].assign(js[i].aa, js[i].aa + js[i].n_prec);
+    js[i].g = &p->geoms[i];
+    js[i].aa = p->aas[i].data();
+  }
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+  // groups below 2^31 candidates, each with its own context
+  int first = 0;
+  while (first < n_jobs) {
+    int last = first;
+    int64_t cand = 0;
+    while (last < n_jobs) {
+      const int64_t jc = (int64_t)js[last].g->nuvw * js[last].n_atoms;
+      if (last > first && cand + jc >= 2147483647LL) break;
+      cand += jc;
+      ++last;
+    }
+    st_plan::Group G;
+    rc = st_create(&G.c, c->device);
+    if (rc != ST_OK) {
+      st_plan_destroy(p);
+      return fail(c, rc, "creating the plan's context");
+    }
+    G.c->tune_mode = c->tune_mode;
+    G.c->ring_tuned = c->ring_tuned;
+    G.c->fp32_general = c->fp32_general;
+    G.jobs.assign(js.begin() + first, js.begin() + last);
+    p->groups.push_back(G);
+    first = last;
+  }
+  for (auto& G : p->groups) {
+    // the private stream of the group's context records; the eager run is ordered after
+    // the caller's stream (its atoms may just have been written there)
+    cudaEvent_t ready;
+    cudaEventCreateWithFlags(&ready, cudaEventDisableTiming);
+    cudaEventRecord(ready, st);
+    cudaStreamWaitEvent(G.c->stream, ready, 0);
+    cudaEventDestroy(ready);
+    rc = plan_record(p, G, G.c->stream);
+    if (rc != ST_OK) {
+      const std::string msg = p->err;
+      st_plan_destroy(p);
+      return fail(c, rc, "recording the plan: " + msg);
+    }
+  }
+  plan_sum_stats(p);
+  *out = p;
+  return ST_OK;
+}
+
+extern "C" int st_plan_launch(st_plan* p, void* stream) {
+  if (!p) return ST_ERR_ARG;
+  cudaSetDevice(p->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  for (auto& G : p->groups) {
+    const cudaError_t e = cudaGraphLaunch(G.g.exec, st);
+    if (e != cudaSuccess) return plan_fail(p, ST_ERR_CUDA, std::string("graph launch: ") + cudaGetErrorString(e));
+  }
+  return ST_OK;
+}
+
+extern "C" int st_plan_wait(st_plan* p, void* stream) {
+  if (!p) return ST_ERR_ARG;
+  cudaSetDevice(p->device);
+  cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+  if (e != cudaSuccess) return plan_fail(p, ST_ERR_CUDA, std::string("plan replay: ") + cudaGetErrorString(e));
+  // the groups ran one after another on the stream and share nothing, so each group's
+  // counters (read back by its last graph node) tell whether its images are complete
+  int64_t kept = 0;
+  for (auto& G : p->groups) {
+    const unsigned long long* h = G.c->h_counters;
+    kept += (int64_t)h[0];
+    if ((int64_t)h[0] > G.g.cap || (G.g.ring && h[4] != 0)) {
+      const int rc = plan_record(p, G, G.c->stream);  // eager recompute, then record again
+      if (rc != ST_OK) return rc;
+      e = cudaStreamSynchronize(G.c->stream);
+      if (e != cudaSuccess) return plan_fail(p, ST_ERR_CUDA, std::string("plan rerun: ") + cudaGetErrorString(e));
+    }
+  }
+  plan_sum_stats(p);
+  p->stats.n_kept = std::max(p->stats.n_kept, kept);
+  return ST_OK;
+}
+
+extern "C" int st_plan_stats(const st_plan* p, st_stats* out) {
+  if (!p || !out) return ST_ERR_ARG;
+  *out = p->stats;
+  return ST_OK;
+}
+
+extern "C" const char* st_plan_last_error(const st_plan* p) { return p ? p->err.c_str() : "null plan"; }
+
+extern "C" void st_plan_destroy(st_plan* p) {
+  if (!p) return;
+  cudaSetDevice(p->device);
+  for (auto& G : p->groups) {
+    if (G.g.exec) cudaGraphExecDestroy(G.g.exec);
+    st_destroy(G.c);
+  }
+  delete p;
 }
 
 extern "C" int st_image(st_ctx* c, const st_geom* g, const double* x, int64_t ldx, int64_t nAtoms, const double* aa,

@@ -106,6 +106,10 @@ class Context:
         arr, keep = self._job_array(jobs)
         self._check(lib().st_batch_device(self.handle, len(jobs), arr, flags, ctypes.c_void_p(stream)))
 
+    def plan(self, jobs, flags, stream=0):
+        """st_plan_create over (geom, x_dev_ptr, n_atoms, aa, img_dev_ptr[, ldx]) jobs; see Plan."""
+        return Plan(self, jobs, flags, stream)
+
     def batch(self, specs, flags=0):
         """st_batch from host arrays: specs is a list of (geom, x (N, 3) or (N, ldx), aa); returns the images.
         Specs that pass the same x array share one device copy of it."""
@@ -141,6 +145,43 @@ class Context:
         s = StStats()
         self._check(lib().st_get_stats(self.handle, ctypes.byref(s)))
         return s
+
+
+class Plan:
+    """A batch recorded as a CUDA graph (st_plan_*): launch() replays it on a stream,
+    wait() completes it (recomputing on the eager path after an overflow)."""
+
+    def __init__(self, ctx, jobs, flags, stream=0):
+        arr, keep = ctx._job_array(jobs)
+        h = ctypes.c_void_p()
+        ctx._check(lib().st_plan_create(ctx.handle, len(jobs), arr, flags, ctypes.c_void_p(stream), ctypes.byref(h)))
+        self.handle = h
+
+    def _check(self, code):
+        if code != _lib.ST_OK:
+            raise _lib.StemError(code, lib().st_plan_last_error(self.handle).decode())
+
+    def launch(self, stream=0):
+        self._check(lib().st_plan_launch(self.handle, ctypes.c_void_p(stream)))
+
+    def wait(self, stream=0):
+        self._check(lib().st_plan_wait(self.handle, ctypes.c_void_p(stream)))
+
+    def stats(self):
+        s = StStats()
+        self._check(lib().st_plan_stats(self.handle, ctypes.byref(s)))
+        return s
+
+    def close(self):
+        if self.handle:
+            lib().st_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class DynamicalTwoBeamImaging:

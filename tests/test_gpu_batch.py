@@ -244,3 +244,101 @@ def test_ring_variants_identical_and_autotuned():
     Go, aao = O.geometry(so, len(x), nPrec=3, precAngle=0.005)
     want, _ = O.patch_image(Go, aao, x, nthreads=8)
     assert np.abs(imgs[0] - want / 3).max() <= FP32_TOL
+
+
+def _device_jobs(specs):
+    """(G, aa, x) specs -> device buffers and (geom, x_ptr, n, aa, img_ptr) jobs."""
+    dev, imgs, jobs = {}, [], []
+    for G, aa, x in specs:
+        if id(x) not in dev:
+            dev[id(x)] = torch.from_numpy(np.ascontiguousarray(x)).to("cuda") if len(x) else \
+                torch.zeros(3, dtype=torch.float64, device="cuda")
+        im = torch.full((G.My, G.Mx), 7.0, dtype=torch.float64, device="cuda")
+        imgs.append(im)
+        jobs.append((G, dev[id(x)].data_ptr(), len(x), aa, im.data_ptr()))
+    return dev, imgs, jobs
+
+
+@pytest.mark.parametrize("fp32", [False, True])
+def test_plan_replay_equals_batch(ctx, fp32):
+    """A recorded plan replays the batch: its images equal st_batch_device's bit for bit,
+    after the recording run and after every replay."""
+    flags = (_lib.ST_FLAG_FP32 if fp32 else 0) | _lib.ST_FLAG_AVERAGE
+    specs, _ = _mixed_specs(fp32)
+    want = _batch(ctx, specs, flags)
+    dev, imgs, jobs = _device_jobs(specs)
+    torch.cuda.synchronize()
+    plan = ctx.plan(jobs, flags)
+    try:
+        torch.cuda.synchronize()
+        for a, b in zip(imgs, want):
+            assert np.array_equal(a.cpu().numpy().T, b)
+        for _ in range(3):
+            for im in imgs:
+                im.fill_(-1.0)
+            torch.cuda.synchronize()
+            plan.launch()
+            plan.wait()
+            for a, b in zip(imgs, want):
+                assert np.array_equal(a.cpu().numpy().T, b)
+    finally:
+        plan.close()
+
+
+def test_plan_follows_moving_atoms(ctx):
+    """Positions rewritten in place between replays (a trajectory): each replay images
+    the current positions, equal to a fresh call on them."""
+    cell = synth.small_cell(n=(10, 10, 8), seed=5, n_voids=1, radius=(4.0, 6.0), with_screw=True)
+    t, so, x = _condition(cell, sg=0.01, density=True)
+    G, aa = t.image_geometry(len(x), n_prec=2)
+    flags = _lib.ST_FLAG_FP32 | _lib.ST_FLAG_AVERAGE
+    dev, imgs, jobs = _device_jobs([(G, aa, x)])
+    d_x = dev[id(x)]
+    torch.cuda.synchronize()
+    plan = ctx.plan(jobs, flags)
+    rng = np.random.default_rng(3)
+    try:
+        for frame in range(3):
+            xf = x + rng.normal(0.0, 0.05, size=x.shape)
+            d_x.copy_(torch.from_numpy(xf))
+            torch.cuda.synchronize()
+            plan.launch()
+            plan.wait()
+            assert np.array_equal(imgs[0].cpu().numpy().T, ctx.image(G, xf, aa, flags=flags))
+    finally:
+        plan.close()
+
+
+def test_plan_recovers_from_slab_overflow(ctx):
+    """A replay whose atoms overfill the ring kernel's slabs is recomputed on the eager
+    path (general kernel) by st_plan_wait, then recorded again."""
+    cell = synth.small_cell(n=(9, 11, 7), seed=6, n_voids=3, radius=(3.0, 5.0), with_screw=False)
+    t, so, x = _condition(cell, sg=0.01)
+    G, aa = t.image_geometry(len(x))
+    flags = _lib.ST_FLAG_FP32
+    dev, imgs, jobs = _device_jobs([(G, aa, x)])
+    d_x = dev[id(x)]
+    torch.cuda.synchronize()
+    plan = ctx.plan(jobs, flags)
+    try:
+        assert plan.stats().column_kernel == 2
+        q = len(x) // 4
+        dense = np.concatenate([x[:q]] * 4 + [x[:len(x) - 4 * q]])  # same atom count, 4x local density
+        d_x.copy_(torch.from_numpy(dense))
+        torch.cuda.synchronize()
+        plan.launch()
+        plan.wait()
+        assert plan.stats().column_kernel == 1
+        want = ctx.image(G, dense, aa, flags=flags)
+        assert ctx.stats().column_kernel == 1
+        assert np.array_equal(imgs[0].cpu().numpy().T, want)
+        # back to the original atoms: the re-recorded plan (general kernel) still images them
+        d_x.copy_(torch.from_numpy(x))
+        torch.cuda.synchronize()
+        plan.launch()
+        plan.wait()
+        Go, aao = O.geometry(so, len(x))
+        ref, _ = O.patch_image(Go, aao, x, nthreads=8)
+        assert np.abs(imgs[0].cpu().numpy().T - ref).max() <= FP32_TOL
+    finally:
+        plan.close()
