@@ -56,6 +56,9 @@ def workload():
 
 
 SWEEP_G = ((1, 1, 0), (2, 0, 0), (2, 1, 1))
+# DRAM bytes (read + write) of one k_column_fp32_v2 launch on the 1.2M-atom image, from an
+# ncu capture of `python bench.py --ncu-case fp32` (61.37 MB read + 2.94 MB written)
+COLUMN_TRAFFIC_BYTES = 6.431e7
 
 
 def sweep_specs(cell, n_tomo=41, n_prec=16, gs=SWEEP_G):
@@ -433,7 +436,9 @@ def run_gpu(args):
             "peak": peaks["fp32_tflops"] if peaks else None, "unit": "TFLOP/s",
             "frac": achieved / peaks["fp32_tflops"] if peaks else None,
             "peak_source": "measured live: FP32 FMA-pipe microbenchmark (libstem_peaks.so) on this GPU",
-            "traffic": None,
+            "traffic": COLUMN_TRAFFIC_BYTES, "traffic_unit": "bytes per launch",
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_column_fp32_v2 on this "
+                              "image (profiles/k_column_fp32_v2_1p2m_screw.md)",
             "algorithmic": {"flops_per_image": flops, "c_tests": c_tests, "accepted_pairs": n_acc,
                             "voxels": V, "kept_atoms": n_kept, "kernel_ms": col_avg,
                             "kernel_tests_per_voxel": n_tst / V, "reference_tests_per_voxel": c_tests / V,
