@@ -1,4 +1,5 @@
-"""Build libstem.so (and the peak microbenchmark library) in-tree for sm_103a.
+"""Build libstem.so, libstem_nn.so (the corrector) and the peak microbenchmark library in-tree
+for sm_103a.
 
 nvcc cross-compiles the CUDA sources for sm_103a on any host; the host-side
 C++ is compiled by g++ for the machine it runs on.  Objects go to
@@ -25,6 +26,8 @@ CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math"
 
 LIB_SOURCES = ["stem_ctx.cu", "k_bin.cu", "k_column.cu", "k_column_v2.cu", "k_blur.cu", "blur_noalloc.cu",
                "host_d2bi.cpp"]
+NN_LIB = os.path.join(HERE, "libstem_nn.so")
+NN_SOURCES = ["nn_conv.cu", "nn_api.cu"]
 
 
 def _nvcc():
@@ -56,27 +59,35 @@ def build(verbose=False, ptxas_info=False):
     """Compile every source (in parallel) and link the libraries; returns their paths."""
     nvcc = _nvcc()
     os.makedirs(BUILD, exist_ok=True)
-    headers = [os.path.join(CSRC, "internal.h"), os.path.join(HERE, "..", "include", "stem.h"),
-               os.path.join(HERE, "..", "include", "stem_host.h")]
-    jobs = []
-    objs = []
-    for src in LIB_SOURCES:
-        path = os.path.join(CSRC, src)
-        obj = os.path.join(BUILD, src + ".o")
-        objs.append(obj)
-        if not _stale(obj, [path] + headers):
-            continue
-        if src.endswith(".cu"):
-            cmd = [nvcc] + NVCC_FLAGS + (["-Xptxas", "-v"] if ptxas_info else []) + ["-c", path, "-o", obj]
-        else:
-            cmd = ["g++"] + CXX_FLAGS + ["-I", os.path.join(_cuda_root(nvcc), "include"), "-c", path, "-o", obj]
-        jobs.append(cmd)
+    inc = os.path.join(HERE, "..", "include")
+    libs = [
+        (LIB, LIB_SOURCES, [os.path.join(CSRC, "internal.h"), os.path.join(inc, "stem.h"),
+                            os.path.join(inc, "stem_host.h")]),
+        (NN_LIB, NN_SOURCES, [os.path.join(CSRC, "nn.h"), os.path.join(CSRC, "tc_sm100.cuh"),
+                              os.path.join(inc, "stem_nn.h")]),
+    ]
+    jobs, link = [], []
+    for lib, sources, headers in libs:
+        objs = []
+        for src in sources:
+            path = os.path.join(CSRC, src)
+            obj = os.path.join(BUILD, src + ".o")
+            objs.append(obj)
+            if not _stale(obj, [path] + headers):
+                continue
+            if src.endswith(".cu"):
+                cmd = [nvcc] + NVCC_FLAGS + (["-Xptxas", "-v"] if ptxas_info else []) + ["-c", path, "-o", obj]
+            else:
+                cmd = ["g++"] + CXX_FLAGS + ["-I", os.path.join(_cuda_root(nvcc), "include"), "-c", path, "-o", obj]
+            jobs.append(cmd)
+        link.append((lib, objs))
     outputs = []
     with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         for out in ex.map(_run, jobs):
             outputs.append(out)
-    if jobs or _stale(LIB, objs):
-        outputs.append(_run([nvcc] + ARCH + ["-shared", "-o", LIB] + objs))
+    for lib, objs in link:
+        if _stale(lib, objs):
+            outputs.append(_run([nvcc] + ARCH + ["-shared", "-o", lib] + objs))
     peaks_src = os.path.join(CSRC, "peaks.cu")
     if _stale(PEAKS_LIB, [peaks_src]):
         outputs.append(_run([nvcc] + NVCC_FLAGS + ["-shared", peaks_src, "-o", PEAKS_LIB]))
@@ -89,4 +100,4 @@ def build(verbose=False, ptxas_info=False):
 
 if __name__ == "__main__":
     build(verbose=True, ptxas_info="--ptxas" in sys.argv)
-    print("built", LIB, PEAKS_LIB)
+    print("built", LIB, NN_LIB, PEAKS_LIB)
