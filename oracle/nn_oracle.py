@@ -82,3 +82,22 @@ def conv2d_grad_weight(x, gy, taps):
 
 def conv2d_grad_bias(gy):
     return np.asarray(gy, dtype=np.float64).reshape(-1, gy.shape[-1]).sum(axis=0)
+
+
+def avgpool2(x):
+    B, H, W, C = x.shape
+    x = np.asarray(x, dtype=np.float64)
+    return 0.25 * ((x[:, 0::2, 0::2] + x[:, 0::2, 1::2]) + (x[:, 1::2, 0::2] + x[:, 1::2, 1::2]))
+
+
+def avgpool2_bwd(gy):
+    return 0.25 * np.repeat(np.repeat(np.asarray(gy, dtype=np.float64), 2, axis=1), 2, axis=2)
+
+
+def upsample2(x):
+    return np.repeat(np.repeat(np.asarray(x, dtype=np.float64), 2, axis=1), 2, axis=2)
+
+
+def upsample2_bwd(gy):
+    g = np.asarray(gy, dtype=np.float64)
+    return (g[:, 0::2, 0::2] + g[:, 0::2, 1::2]) + (g[:, 1::2, 0::2] + g[:, 1::2, 1::2])

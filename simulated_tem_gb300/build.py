@@ -27,7 +27,7 @@ CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math"
 LIB_SOURCES = ["stem_ctx.cu", "k_bin.cu", "k_column.cu", "k_column_v2.cu", "k_blur.cu", "blur_noalloc.cu",
                "host_d2bi.cpp"]
 NN_LIB = os.path.join(HERE, "libstem_nn.so")
-NN_SOURCES = ["nn_conv.cu", "nn_api.cu"]
+NN_SOURCES = ["nn_conv.cu", "nn_ops.cu", "nn_api.cu"]
 
 
 def _nvcc():

@@ -10,8 +10,35 @@ namespace nn {
 // y = act(conv(x, w) + bias) over NHWC BF16 activations; taps 9 (3 x 3, "same" padding)
 // or 1.  Cin a multiple of 16, Cout a multiple of 8.  y is BF16, or FP32 when y_fp32.
 // Returns 0, 1 for invalid arguments, 2 for a launch error.
+// mask (same shape as y, or null): outputs where mask <= 0 are zeroed, the gradient through
+// the ReLU that produced a layer's input.
 int conv_fwd(const __nv_bfloat16* x, int B, int H, int W, int Cin, const __nv_bfloat16* w, int Cout, int taps,
-             const float* bias, int relu, void* y, int y_fp32, cudaStream_t st);
+             const float* bias, int relu, const __nv_bfloat16* mask, void* y, int y_fp32, cudaStream_t st);
+
+// gw[co][t][ci] += sum over pixels of gy[p][co] x[p + d_t][ci] (FP32, accumulated).
+int conv_wgrad(const __nv_bfloat16* x, const __nv_bfloat16* gy, int B, int H, int W, int Cin, int Cout, int taps,
+               float* gw, cudaStream_t st);
+
+// wt[ci][taps - 1 - t][co] = w[co][t][ci]: input-gradient weights.
+int flip_transpose(const __nv_bfloat16* w, __nv_bfloat16* wt, int Cout, int taps, int Cin, cudaStream_t st);
+
+// Element-wise layers (nn_ops.cu); NHWC BF16 unless stated.
+int avgpool2(const __nv_bfloat16* x, __nv_bfloat16* y, int B, int H, int W, int C, cudaStream_t st);
+int avgpool2_bwd(const __nv_bfloat16* gy, __nv_bfloat16* gx, int B, int H, int W, int C, cudaStream_t st);
+int upsample2(const __nv_bfloat16* x, __nv_bfloat16* y, int B, int H, int W, int C, cudaStream_t st);
+int upsample2_bwd(const __nv_bfloat16* gy, __nv_bfloat16* gx, int B, int H, int W, int C, cudaStream_t st);
+int concat(const __nv_bfloat16* a, const __nv_bfloat16* b, __nv_bfloat16* y, long long npix, int Ca, int Cb,
+           cudaStream_t st);
+int split(const __nv_bfloat16* gy, __nv_bfloat16* ga, __nv_bfloat16* gb, long long npix, int Ca, int Cb,
+          cudaStream_t st);
+int relu_mask(__nv_bfloat16* g, const __nv_bfloat16* y, long long n, cudaStream_t st);
+int bias_grad(const __nv_bfloat16* g, float* gb, long long npix, int C, cudaStream_t st);
+int mse(const float* pred, const float* target, __nv_bfloat16* g, float* loss, long long npix, int Cp,
+        cudaStream_t st);
+int adam(float* w, float* m, float* v, const float* g, __nv_bfloat16* w16, long long n, float lr, float b1, float b2,
+         float eps, int step, float wd, cudaStream_t st);
+int pack(const float* planes, int nplanes, __nv_bfloat16* y, long long npix, int C, cudaStream_t st);
+int to_bf16(const float* x, __nv_bfloat16* y, long long n, cudaStream_t st);
 
 // First failure recorded by a corrector kernel (0 = none), then cleared; synchronises.
 int take_error();

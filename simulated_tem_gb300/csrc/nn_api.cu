@@ -7,11 +7,61 @@
 
 using namespace stem::nn;
 
-extern "C" int stn_conv2d_fwd(const void* x, int32_t B, int32_t H, int32_t W, int32_t Cin, const void* w,
-                              int32_t Cout, int32_t taps, const float* bias, int32_t relu, void* y, int32_t y_fp32,
-                              void* stream) {
-  return conv_fwd(static_cast<const __nv_bfloat16*>(x), B, H, W, Cin, static_cast<const __nv_bfloat16*>(w), Cout,
-                  taps, bias, relu, y, y_fp32, (cudaStream_t)stream);
-}
+namespace {
+typedef __nv_bfloat16 bf16;
+inline const bf16* cb(const void* p) { return static_cast<const bf16*>(p); }
+inline bf16* mb(void* p) { return static_cast<bf16*>(p); }
+inline cudaStream_t cs(void* s) { return (cudaStream_t)s; }
+}  // namespace
 
+extern "C" int stn_conv2d_fwd(const void* x, int32_t B, int32_t H, int32_t W, int32_t Cin, const void* w,
+                              int32_t Cout, int32_t taps, const float* bias, int32_t relu, const void* mask, void* y,
+                              int32_t y_fp32, void* stream) {
+  return conv_fwd(cb(x), B, H, W, Cin, cb(w), Cout, taps, bias, relu, cb(mask), y, y_fp32, cs(stream));
+}
+extern "C" int stn_conv2d_wgrad(const void* x, const void* gy, int32_t B, int32_t H, int32_t W, int32_t Cin,
+                                int32_t Cout, int32_t taps, float* gw, void* stream) {
+  return conv_wgrad(cb(x), cb(gy), B, H, W, Cin, Cout, taps, gw, cs(stream));
+}
+extern "C" int stn_weight_flip(const void* w, void* wt, int32_t Cout, int32_t taps, int32_t Cin, void* stream) {
+  return flip_transpose(cb(w), mb(wt), Cout, taps, Cin, cs(stream));
+}
+extern "C" int stn_avgpool2(const void* x, void* y, int32_t B, int32_t H, int32_t W, int32_t C, void* stream) {
+  return avgpool2(cb(x), mb(y), B, H, W, C, cs(stream));
+}
+extern "C" int stn_avgpool2_bwd(const void* gy, void* gx, int32_t B, int32_t H, int32_t W, int32_t C, void* stream) {
+  return avgpool2_bwd(cb(gy), mb(gx), B, H, W, C, cs(stream));
+}
+extern "C" int stn_upsample2(const void* x, void* y, int32_t B, int32_t H, int32_t W, int32_t C, void* stream) {
+  return upsample2(cb(x), mb(y), B, H, W, C, cs(stream));
+}
+extern "C" int stn_upsample2_bwd(const void* gy, void* gx, int32_t B, int32_t H, int32_t W, int32_t C, void* stream) {
+  return upsample2_bwd(cb(gy), mb(gx), B, H, W, C, cs(stream));
+}
+extern "C" int stn_concat(const void* a, const void* b, void* y, int64_t npix, int32_t Ca, int32_t Cb, void* stream) {
+  return concat(cb(a), cb(b), mb(y), npix, Ca, Cb, cs(stream));
+}
+extern "C" int stn_split(const void* gy, void* ga, void* gb, int64_t npix, int32_t Ca, int32_t Cb, void* stream) {
+  return split(cb(gy), mb(ga), mb(gb), npix, Ca, Cb, cs(stream));
+}
+extern "C" int stn_relu_mask(void* g, const void* y, int64_t n, void* stream) {
+  return relu_mask(mb(g), cb(y), n, cs(stream));
+}
+extern "C" int stn_bias_grad(const void* g, float* gb, int64_t npix, int32_t C, void* stream) {
+  return bias_grad(cb(g), gb, npix, C, cs(stream));
+}
+extern "C" int stn_mse(const float* pred, const float* target, void* g, float* loss, int64_t npix, int32_t Cp,
+                       void* stream) {
+  return mse(pred, target, mb(g), loss, npix, Cp, cs(stream));
+}
+extern "C" int stn_adam(float* w, float* m, float* v, const float* g, void* w16, int64_t n, float lr, float beta1,
+                        float beta2, float eps, int32_t step, float wd, void* stream) {
+  return adam(w, m, v, g, mb(w16), n, lr, beta1, beta2, eps, step, wd, cs(stream));
+}
+extern "C" int stn_pack(const float* planes, int32_t nplanes, void* y, int64_t npix, int32_t C, void* stream) {
+  return pack(planes, nplanes, mb(y), npix, C, cs(stream));
+}
+extern "C" int stn_to_bf16(const float* x, void* y, int64_t n, void* stream) {
+  return to_bf16(x, mb(y), n, cs(stream));
+}
 extern "C" int stn_last_kernel_error(void) { return take_error(); }

@@ -30,10 +30,11 @@ constexpr int kThreads = 128;
 constexpr uint32_t kWaitLimit = 1u << 20;  // polls of an mbarrier before giving up (about a second)
 
 struct ConvArgs {
-  const __nv_bfloat16* x;  // [B][H][W][Cin]
-  const __nv_bfloat16* w;  // [Cout][taps][Cin]
-  const float* bias;       // [Cout] or null
-  void* y;                 // [B][H][W][Cout], BF16 or FP32
+  const __nv_bfloat16* x;     // [B][H][W][Cin]
+  const __nv_bfloat16* w;     // [Cout][taps][Cin]
+  const float* bias;          // [Cout] or null
+  const __nv_bfloat16* mask;  // [B][H][W][Cout] or null: outputs where mask <= 0 are zeroed
+  void* y;                    // [B][H][W][Cout], BF16 or FP32
   int B, H, W, Cin, Cout, taps, relu, y_fp32;
 };
 
@@ -155,6 +156,13 @@ __global__ void __launch_bounds__(kThreads) k_conv_fwd(const ConvArgs a) {
           if (a.bias) v[i] += a.bias[n + i];
           if (a.relu) v[i] = fmaxf(v[i], 0.f);
         }
+        if (a.mask) {  // gradient through the ReLU that produced this layer's input
+          const uint4 mv = *reinterpret_cast<const uint4*>(a.mask + (size_t)p * a.Cout + n);
+          const __nv_bfloat16* m = reinterpret_cast<const __nv_bfloat16*>(&mv);
+#pragma unroll
+          for (int i = 0; i < 8; ++i)
+            if (!(__bfloat162float(m[i]) > 0.f)) v[i] = 0.f;
+        }
         if (a.y_fp32) {
           float* dst = reinterpret_cast<float*>(a.y) + (size_t)p * a.Cout + n;
           *reinterpret_cast<float4*>(dst) = make_float4(v[0], v[1], v[2], v[3]);
@@ -195,11 +203,11 @@ cudaError_t launch_fwd_kc(const ConvArgs& a, cudaStream_t st) {
 }  // namespace
 
 int conv_fwd(const __nv_bfloat16* x, int B, int H, int W, int Cin, const __nv_bfloat16* w, int Cout, int taps,
-             const float* bias, int relu, void* y, int y_fp32, cudaStream_t st) {
+             const float* bias, int relu, const __nv_bfloat16* mask, void* y, int y_fp32, cudaStream_t st) {
   if (!x || !w || !y || B < 1 || H < 1 || W < 1) return 1;
   if (Cin < 16 || Cin % 16 != 0 || Cout < 8 || Cout % 8 != 0 || (taps != 1 && taps != 9)) return 1;
   if ((long long)B * H * W >= (1LL << 31)) return 1;
-  ConvArgs a{x, w, bias, y, B, H, W, Cin, Cout, taps, relu, y_fp32};
+  ConvArgs a{x, w, bias, mask, y, B, H, W, Cin, Cout, taps, relu, y_fp32};
   cudaError_t e;
   if (Cin % 64 == 0)
     e = launch_fwd_kc<64>(a, st);
@@ -208,6 +216,208 @@ int conv_fwd(const __nv_bfloat16* x, int B, int H, int W, int Cin, const __nv_bf
   else
     e = launch_fwd_kc<16>(a, st);
   return e == cudaSuccess ? 0 : 2;
+}
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// Weight gradient: gw[co, t, ci] += sum_p gy[p, co] x[p + d_t, ci]
+// ---------------------------------------------------------------------------
+// GEMM per tap with K = pixels: A[co, p] = gy[p, co], B_t[ci, p] = x[p + d_t, ci], both
+// transposed while staged (K-major tiles, p along K).  A CTA owns 128 output channels x
+// BN input channels x TG taps (TG x BN TMEM columns) for one range of pixels, in chunks
+// of 64 pixels; the A tile of a chunk serves all TG taps.  Partial sums over the CTA's
+// pixels are added to the FP32 gradient with reductions (red.global.add).
+struct WgradArgs {
+  const __nv_bfloat16* x;   // [B][H][W][Cin]
+  const __nv_bfloat16* gy;  // [B][H][W][Cout]
+  float* gw;                // [Cout][taps][Cin], accumulated into
+  int B, H, W, Cin, Cout, taps;
+  int chunks_per_cta;       // 64-pixel chunks per CTA (pixel split)
+};
+
+template <int BN, int TG>
+struct WSmem {
+  alignas(1024) unsigned char a[2][128 * 64 * 2];
+  alignas(1024) unsigned char b[2][TG][BN * 64 * 2];
+  alignas(8) unsigned long long mbar[2];
+  uint32_t tmem;
+};
+
+__host__ __device__ constexpr int tmem_cols(int n) { return n <= 32 ? 32 : n <= 64 ? 64 : n <= 128 ? 128 : n <= 256 ? 256 : 512; }
+
+// Stage 8 consecutive channels of pixel p (or zeros) as column kp of rows r0 .. r0 + 7.
+__device__ __forceinline__ void put_column8(unsigned char* tile, int r0, int kp, const __nv_bfloat16* src) {
+  uint4 v = make_uint4(0u, 0u, 0u, 0u);
+  if (src) v = *reinterpret_cast<const uint4*>(src);
+  const unsigned short* h = reinterpret_cast<const unsigned short*>(&v);
+#pragma unroll
+  for (int i = 0; i < 8; ++i) *reinterpret_cast<unsigned short*>(tile + tc::tile_offset(r0 + i, kp, 64)) = h[i];
+}
+
+template <int BN, int TG>
+__global__ void __launch_bounds__(kThreads) k_conv_wgrad(const WgradArgs a) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  WSmem<BN, TG>& S = *reinterpret_cast<WSmem<BN, TG>*>(smem_raw + ((1024 - ((uintptr_t)smem_raw & 1023)) & 1023));
+  const int t = threadIdx.x, warp = t >> 5;
+  const int m0 = blockIdx.y * 128;                    // output channels
+  const int n_ctiles = (a.Cin + BN - 1) / BN;
+  const int c0 = (blockIdx.z % n_ctiles) * BN;        // input channels
+  const int t0 = (blockIdx.z / n_ctiles) * TG;        // first tap of the group
+  const int ntap = min(TG, a.taps - t0);
+  const int npix = a.B * a.H * a.W;
+  const int chunk0 = blockIdx.x * a.chunks_per_cta;
+  const int nchunks = max(0, min(a.chunks_per_cta, (npix + 63) / 64 - chunk0));
+  constexpr int kCols = tmem_cols(TG * BN);
+
+  if (warp == 0) tc::tmem_alloc(tc::smem_addr(&S.tmem), kCols);
+  if (t == 0) {
+    tc::mbar_init(tc::smem_addr(&S.mbar[0]), 1);
+    tc::mbar_init(tc::smem_addr(&S.mbar[1]), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = S.tmem;
+  constexpr uint32_t idesc = tc::make_idesc_bf16(128, BN);
+
+  const int kp = t & 63, half = t >> 6;
+  bool ok = true;
+  int issued = 0;
+  for (int c = 0; c < nchunks; ++c) {
+    const int st = c & 1;
+    if (c >= 2) ok = tc::mbar_wait(tc::smem_addr(&S.mbar[st]), ((c - 2) >> 1) & 1, kWaitLimit);
+    ok = __syncthreads_and(ok);
+    if (!ok) break;
+    const int p = (chunk0 + c) * 64 + kp;
+    int b = 0, yh = 0, xw = 0;
+    if (p < npix) {
+      xw = p % a.W;
+      const int rest = p / a.W;
+      yh = rest % a.H;
+      b = rest / a.H;
+    }
+    // A: 128 output channels x 64 pixels
+    for (int g = half; g < 16; g += 2) {
+      const int co = m0 + 8 * g;
+      const __nv_bfloat16* src = (p < npix && co < a.Cout) ? a.gy + (size_t)p * a.Cout + co : nullptr;
+      put_column8(S.a[st], 8 * g, kp, src);
+    }
+    // B_t: BN input channels x 64 pixels, one tile per tap of the group
+    for (int j = 0; j < TG; ++j) {
+      const int tap = t0 + j;
+      const int dy = a.taps == 9 ? tap / 3 - 1 : 0, dx = a.taps == 9 ? tap % 3 - 1 : 0;
+      const int yy = yh + dy, xx = xw + dx;
+      const bool in = j < ntap && p < npix && yy >= 0 && yy < a.H && xx >= 0 && xx < a.W;
+      for (int g = half; g < BN / 8; g += 2) {
+        const int ci = c0 + 8 * g;
+        const __nv_bfloat16* src =
+            (in && ci < a.Cin) ? a.x + (((size_t)b * a.H + yy) * a.W + xx) * a.Cin + ci : nullptr;
+        put_column8(S.b[st][j], 8 * g, kp, src);
+      }
+    }
+    tc::fence_proxy_async_smem();
+    __syncthreads();
+    if (t == 0) {
+      tc::fence_after_sync();
+      const uint32_t sa = tc::smem_addr(S.a[st]);
+      for (int j = 0; j < ntap; ++j) {
+        const uint32_t sb = tc::smem_addr(S.b[st][j]);
+#pragma unroll
+        for (int s = 0; s < 4; ++s)
+          tc::mma_bf16(tmem + (uint32_t)(j * BN), tc::make_desc(sa + 256 * s, 128, 64 * 16),
+                       tc::make_desc(sb + 256 * s, 128, 64 * 16), idesc, (c > 0 || s > 0) ? 1u : 0u);
+      }
+      tc::mma_commit(tc::smem_addr(&S.mbar[st]));
+    }
+    issued = c + 1;
+  }
+  if (issued > 0) {
+    const int last = issued - 1;
+    bool done = tc::mbar_wait(tc::smem_addr(&S.mbar[last & 1]), (last >> 1) & 1, kWaitLimit);
+    done = __syncthreads_and(done);
+    if (!done) tc::mbar_wait(tc::smem_addr(&S.mbar[last & 1]), (last >> 1) & 1, kWaitLimit);
+    ok = ok && done;
+  }
+  if (!ok && t == 0) atomicCAS(&g_nn_error, 0, 1);
+  tc::fence_after_sync();
+
+  if (ok && issued > 0) {
+    const int co = m0 + 32 * warp + (t & 31);
+    for (int j = 0; j < ntap; ++j) {
+      for (int col = 0; col < BN; col += 8) {
+        float v[8];
+        tc::tmem_ld8(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(j * BN + col), v);
+        const int ci = c0 + col;
+        if (co < a.Cout && ci < a.Cin) {
+          float* dst = a.gw + ((size_t)co * a.taps + t0 + j) * a.Cin + ci;
+#pragma unroll
+          for (int i = 0; i < 8; ++i) atomicAdd(dst + i, v[i]);
+        }
+      }
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, kCols);
+}
+
+template <int BN, int TG>
+cudaError_t launch_wgrad(WgradArgs a, cudaStream_t st) {
+  const size_t smem = sizeof(WSmem<BN, TG>) + 1024;
+  cudaError_t e = cudaFuncSetAttribute(k_conv_wgrad<BN, TG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  int dev = 0, sms = 148;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int npix = a.B * a.H * a.W;
+  const int chunks = (npix + 63) / 64;
+  const int tiles = ((a.Cout + 127) / 128) * ((a.Cin + BN - 1) / BN) * ((a.taps + TG - 1) / TG);
+  // about two waves of CTAs; at least 8 chunks per CTA so the partial sums amortise
+  int splits = (2 * sms + tiles - 1) / tiles;
+  splits = max(1, min(splits, (chunks + 7) / 8));
+  a.chunks_per_cta = (chunks + splits - 1) / splits;
+  splits = (chunks + a.chunks_per_cta - 1) / a.chunks_per_cta;
+  dim3 grid(splits, (a.Cout + 127) / 128, ((a.Cin + BN - 1) / BN) * ((a.taps + TG - 1) / TG));
+  k_conv_wgrad<BN, TG><<<grid, kThreads, smem, st>>>(a);
+  return cudaGetLastError();
+}
+
+// wt[ci][8 - t][co] = w[co][t][ci] (taps 9) or wt[ci][0][co] = w[co][0][ci]: the weights
+// of the input gradient as a forward convolution of the output gradient.
+__global__ void k_flip_transpose(const __nv_bfloat16* __restrict__ w, __nv_bfloat16* __restrict__ wt, int Cout,
+                                 int taps, int Cin) {
+  const int n = Cout * taps * Cin;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int ci = i % Cin;
+    const int rest = i / Cin;
+    const int tp = rest % taps, co = rest / taps;
+    wt[((size_t)ci * taps + (taps - 1 - tp)) * Cout + co] = w[i];
+  }
+}
+
+}  // namespace
+
+int conv_wgrad(const __nv_bfloat16* x, const __nv_bfloat16* gy, int B, int H, int W, int Cin, int Cout, int taps,
+               float* gw, cudaStream_t st) {
+  if (!x || !gy || !gw || B < 1 || H < 1 || W < 1) return 1;
+  if (Cin < 8 || Cin % 8 != 0 || Cout < 8 || Cout % 8 != 0 || (taps != 1 && taps != 9)) return 1;
+  if ((long long)B * H * W >= (1LL << 31)) return 1;
+  WgradArgs a{x, gy, gw, B, H, W, Cin, Cout, taps, 1};
+  cudaError_t e;
+  if (taps == 1)
+    e = Cin <= 32 ? launch_wgrad<32, 1>(a, st) : Cin <= 64 ? launch_wgrad<64, 1>(a, st) : launch_wgrad<128, 1>(a, st);
+  else
+    e = Cin <= 32 ? launch_wgrad<32, 9>(a, st) : Cin <= 64 ? launch_wgrad<64, 3>(a, st) : launch_wgrad<128, 3>(a, st);
+  return e == cudaSuccess ? 0 : 2;
+}
+
+int flip_transpose(const __nv_bfloat16* w, __nv_bfloat16* wt, int Cout, int taps, int Cin, cudaStream_t st) {
+  if (!w || !wt || Cout < 1 || Cin < 1 || (taps != 1 && taps != 9)) return 1;
+  const int n = Cout * taps * Cin;
+  k_flip_transpose<<<(n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096, 256, 0, st>>>(w, wt, Cout, taps, Cin);
+  return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 
 int take_error() {

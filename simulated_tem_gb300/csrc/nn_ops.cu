@@ -1,0 +1,281 @@
+// Element-wise and reduction layers of the learned corrector (NHWC, BF16 activations,
+// FP32 where a sum or a parameter update needs it).  Memory-bound: grid-stride loops
+// over 16-byte vectors where the channel count allows.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "nn.h"
+
+namespace stem {
+namespace nn {
+namespace {
+
+constexpr int kBlock = 256;
+
+int grid_for(long long n) {
+  long long g = (n + kBlock - 1) / kBlock;
+  if (g < 1) g = 1;
+  if (g > 16384) g = 16384;
+  return (int)g;
+}
+
+__device__ __forceinline__ float bf(__nv_bfloat16 v) { return __bfloat162float(v); }
+__device__ __forceinline__ __nv_bfloat16 tobf(float v) { return __float2bfloat16_rn(v); }
+
+// y[b, i, j, c] = (x[b, 2i, 2j] + x[b, 2i, 2j + 1] + x[b, 2i + 1, 2j] + x[b, 2i + 1, 2j + 1]) / 4
+__global__ void k_avgpool2(const __nv_bfloat16* __restrict__ x, __nv_bfloat16* __restrict__ y, int B, int H, int W,
+                           int C) {
+  const int Ho = H / 2, Wo = W / 2;
+  const long long n = (long long)B * Ho * Wo * C;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int c = (int)(i % C);
+    long long r = i / C;
+    const int j = (int)(r % Wo);
+    r /= Wo;
+    const int ii = (int)(r % Ho);
+    const int b = (int)(r / Ho);
+    const __nv_bfloat16* s = x + (((long long)b * H + 2 * ii) * W + 2 * j) * C + c;
+    const float v = (bf(s[0]) + bf(s[C])) + (bf(s[(long long)W * C]) + bf(s[(long long)W * C + C]));
+    y[i] = tobf(0.25f * v);
+  }
+}
+
+// gx[b, y, x, c] = gy[b, y / 2, x / 2, c] / 4
+__global__ void k_avgpool2_bwd(const __nv_bfloat16* __restrict__ gy, __nv_bfloat16* __restrict__ gx, int B, int H,
+                               int W, int C) {
+  const long long n = (long long)B * H * W * C;
+  const int Ho = H / 2, Wo = W / 2;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int c = (int)(i % C);
+    long long r = i / C;
+    const int xw = (int)(r % W);
+    r /= W;
+    const int yh = (int)(r % H);
+    const int b = (int)(r / H);
+    gx[i] = tobf(0.25f * bf(gy[(((long long)b * Ho + yh / 2) * Wo + xw / 2) * C + c]));
+  }
+}
+
+// nearest 2x upsampling: y[b, y, x, c] = x[b, y / 2, x / 2, c]
+__global__ void k_upsample2(const __nv_bfloat16* __restrict__ x, __nv_bfloat16* __restrict__ y, int B, int H, int W,
+                            int C) {
+  const int Ho = 2 * H, Wo = 2 * W;
+  const long long n = (long long)B * Ho * Wo * C;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int c = (int)(i % C);
+    long long r = i / C;
+    const int xw = (int)(r % Wo);
+    r /= Wo;
+    const int yh = (int)(r % Ho);
+    const int b = (int)(r / Ho);
+    y[i] = x[(((long long)b * H + yh / 2) * W + xw / 2) * C + c];
+  }
+}
+
+// gx[b, i, j, c] = sum of gy over the 2 x 2 block it was copied to (FP32 sum, one rounding)
+__global__ void k_upsample2_bwd(const __nv_bfloat16* __restrict__ gy, __nv_bfloat16* __restrict__ gx, int B, int H,
+                                int W, int C) {
+  const long long n = (long long)B * H * W * C;
+  const int Wo = 2 * W;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int c = (int)(i % C);
+    long long r = i / C;
+    const int j = (int)(r % W);
+    r /= W;
+    const int ii = (int)(r % H);
+    const int b = (int)(r / H);
+    const __nv_bfloat16* s = gy + (((long long)b * 2 * H + 2 * ii) * Wo + 2 * j) * C + c;
+    const float v = (bf(s[0]) + bf(s[C])) + (bf(s[(long long)Wo * C]) + bf(s[(long long)Wo * C + C]));
+    gx[i] = tobf(v);
+  }
+}
+
+// y[p, 0:Ca] = a[p], y[p, Ca:Ca+Cb] = b[p]  (both channel counts multiples of 8)
+__global__ void k_concat(const __nv_bfloat16* __restrict__ a, const __nv_bfloat16* __restrict__ b,
+                         __nv_bfloat16* __restrict__ y, long long npix, int Ca, int Cb) {
+  const int C = Ca + Cb, V = C / 8;
+  const long long n = npix * V;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const long long p = i / V;
+    const int c = (int)(i % V) * 8;
+    const uint4 v = c < Ca ? *reinterpret_cast<const uint4*>(a + p * Ca + c)
+                           : *reinterpret_cast<const uint4*>(b + p * Cb + (c - Ca));
+    *reinterpret_cast<uint4*>(y + p * C + c) = v;
+  }
+}
+
+// the inverse: ga[p] = gy[p, 0:Ca], gb[p] = gy[p, Ca:Ca+Cb] (either output may be null)
+__global__ void k_split(const __nv_bfloat16* __restrict__ gy, __nv_bfloat16* __restrict__ ga,
+                        __nv_bfloat16* __restrict__ gb, long long npix, int Ca, int Cb) {
+  const int C = Ca + Cb, V = C / 8;
+  const long long n = npix * V;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const long long p = i / V;
+    const int c = (int)(i % V) * 8;
+    const uint4 v = *reinterpret_cast<const uint4*>(gy + p * C + c);
+    if (c < Ca) {
+      if (ga) *reinterpret_cast<uint4*>(ga + p * Ca + c) = v;
+    } else if (gb) {
+      *reinterpret_cast<uint4*>(gb + p * Cb + (c - Ca)) = v;
+    }
+  }
+}
+
+// g *= (y > 0): the gradient through a ReLU whose output was y
+__global__ void k_relu_mask(__nv_bfloat16* __restrict__ g, const __nv_bfloat16* __restrict__ y, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    if (!(bf(y[i]) > 0.f)) g[i] = tobf(0.f);
+}
+
+// gb[c] += sum_p g[p, c]: per-block partial sums in shared FP32, one global reduction per
+// channel and block
+__global__ void k_bias_grad(const __nv_bfloat16* __restrict__ g, float* __restrict__ gb, long long npix, int C) {
+  extern __shared__ float part[];
+  for (int c = threadIdx.x; c < C; c += blockDim.x) part[c] = 0.f;
+  __syncthreads();
+  const long long n = npix * C;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    atomicAdd(&part[i % C], bf(g[i]));
+  __syncthreads();
+  for (int c = threadIdx.x; c < C; c += blockDim.x) atomicAdd(&gb[c], part[c]);
+}
+
+// loss = mean_p (pred[p, 0] - target[p])^2 over npix pixels (pred FP32 [npix][Cp]);
+// g[p, 0] = 2 (pred - target) / npix as BF16 [npix][Cp] (other channels 0); the loss sum
+// is added to *loss.
+__global__ void k_mse(const float* __restrict__ pred, const float* __restrict__ target, __nv_bfloat16* __restrict__ g,
+                      float* __restrict__ loss, long long npix, int Cp) {
+  __shared__ float red[kBlock / 32];
+  float s = 0.f;
+  const float scale = 2.f / (float)npix;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npix;
+       p += (long long)gridDim.x * blockDim.x) {
+    const float d = pred[p * Cp] - target[p];
+    s += d * d;
+    if (g) {
+      g[p * Cp] = tobf(scale * d);
+      for (int c = 1; c < Cp; ++c) g[p * Cp + c] = tobf(0.f);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float t = 0.f;
+    for (int w = 0; w < (int)(blockDim.x / 32); ++w) t += red[w];
+    atomicAdd(loss, t / (float)npix);
+  }
+}
+
+// Adam on FP32 master parameters; the BF16 copy (if any) is refreshed.
+__global__ void k_adam(float* __restrict__ w, float* __restrict__ m, float* __restrict__ v,
+                       const float* __restrict__ g, __nv_bfloat16* __restrict__ w16, long long n, float lr, float b1,
+                       float b2, float eps, float bc1, float bc2, float wd) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const float gi = g[i] + wd * w[i];
+    const float mi = b1 * m[i] + (1.f - b1) * gi;
+    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    const float wi = w[i] - lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+    w[i] = wi;
+    if (w16) w16[i] = tobf(wi);
+  }
+}
+
+// pack FP32 planes [nplanes][npix] into BF16 NHWC [npix][C] (channels >= nplanes zero)
+__global__ void k_pack(const float* __restrict__ planes, int nplanes, __nv_bfloat16* __restrict__ y, long long npix,
+                       int C) {
+  const long long n = npix * C;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int c = (int)(i % C);
+    const long long p = i / C;
+    y[i] = tobf(c < nplanes ? planes[(long long)c * npix + p] : 0.f);
+  }
+}
+
+// FP32 -> BF16 copy
+__global__ void k_to_bf16(const float* __restrict__ x, __nv_bfloat16* __restrict__ y, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    y[i] = tobf(x[i]);
+}
+
+int status() { return cudaGetLastError() == cudaSuccess ? 0 : 2; }
+
+}  // namespace
+
+int avgpool2(const __nv_bfloat16* x, __nv_bfloat16* y, int B, int H, int W, int C, cudaStream_t st) {
+  if (!x || !y || H % 2 || W % 2 || C < 1) return 1;
+  k_avgpool2<<<grid_for((long long)B * H * W * C / 4), kBlock, 0, st>>>(x, y, B, H, W, C);
+  return status();
+}
+int avgpool2_bwd(const __nv_bfloat16* gy, __nv_bfloat16* gx, int B, int H, int W, int C, cudaStream_t st) {
+  if (!gy || !gx || H % 2 || W % 2 || C < 1) return 1;
+  k_avgpool2_bwd<<<grid_for((long long)B * H * W * C), kBlock, 0, st>>>(gy, gx, B, H, W, C);
+  return status();
+}
+int upsample2(const __nv_bfloat16* x, __nv_bfloat16* y, int B, int H, int W, int C, cudaStream_t st) {
+  if (!x || !y || C < 1) return 1;
+  k_upsample2<<<grid_for((long long)B * H * W * C * 4), kBlock, 0, st>>>(x, y, B, H, W, C);
+  return status();
+}
+int upsample2_bwd(const __nv_bfloat16* gy, __nv_bfloat16* gx, int B, int H, int W, int C, cudaStream_t st) {
+  if (!gy || !gx || C < 1) return 1;
+  k_upsample2_bwd<<<grid_for((long long)B * H * W * C), kBlock, 0, st>>>(gy, gx, B, H, W, C);
+  return status();
+}
+int concat(const __nv_bfloat16* a, const __nv_bfloat16* b, __nv_bfloat16* y, long long npix, int Ca, int Cb,
+           cudaStream_t st) {
+  if (!a || !b || !y || Ca % 8 || Cb % 8) return 1;
+  k_concat<<<grid_for(npix * (Ca + Cb) / 8), kBlock, 0, st>>>(a, b, y, npix, Ca, Cb);
+  return status();
+}
+int split(const __nv_bfloat16* gy, __nv_bfloat16* ga, __nv_bfloat16* gb, long long npix, int Ca, int Cb,
+          cudaStream_t st) {
+  if (!gy || Ca % 8 || Cb % 8) return 1;
+  k_split<<<grid_for(npix * (Ca + Cb) / 8), kBlock, 0, st>>>(gy, ga, gb, npix, Ca, Cb);
+  return status();
+}
+int relu_mask(__nv_bfloat16* g, const __nv_bfloat16* y, long long n, cudaStream_t st) {
+  if (!g || !y) return 1;
+  k_relu_mask<<<grid_for(n), kBlock, 0, st>>>(g, y, n);
+  return status();
+}
+int bias_grad(const __nv_bfloat16* g, float* gb, long long npix, int C, cudaStream_t st) {
+  if (!g || !gb || C < 1 || C > 4096) return 1;
+  long long n = npix * C;
+  int grid = grid_for(n / 16);
+  k_bias_grad<<<grid, kBlock, C * sizeof(float), st>>>(g, gb, npix, C);
+  return status();
+}
+int mse(const float* pred, const float* target, __nv_bfloat16* g, float* loss, long long npix, int Cp,
+        cudaStream_t st) {
+  if (!pred || !target || !loss || Cp < 1) return 1;
+  k_mse<<<grid_for(npix / 4), kBlock, 0, st>>>(pred, target, g, loss, npix, Cp);
+  return status();
+}
+int adam(float* w, float* m, float* v, const float* g, __nv_bfloat16* w16, long long n, float lr, float b1, float b2,
+         float eps, int step, float wd, cudaStream_t st) {
+  if (!w || !m || !v || !g || step < 1) return 1;
+  float bc1 = 1.f, bc2 = 1.f;
+  for (int i = 0; i < step && i < 100000; ++i) {
+    bc1 *= b1;
+    bc2 *= b2;
+  }
+  k_adam<<<grid_for(n), kBlock, 0, st>>>(w, m, v, g, w16, n, lr, b1, b2, eps, 1.f - bc1, 1.f - bc2, wd);
+  return status();
+}
+int pack(const float* planes, int nplanes, __nv_bfloat16* y, long long npix, int C, cudaStream_t st) {
+  if (!planes || !y || nplanes < 1 || nplanes > C) return 1;
+  k_pack<<<grid_for(npix * C), kBlock, 0, st>>>(planes, nplanes, y, npix, C);
+  return status();
+}
+int to_bf16(const float* x, __nv_bfloat16* y, long long n, cudaStream_t st) {
+  if (!x || !y) return 1;
+  k_to_bf16<<<grid_for(n), kBlock, 0, st>>>(x, y, n);
+  return status();
+}
+
+}  // namespace nn
+}  // namespace stem

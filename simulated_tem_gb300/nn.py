@@ -9,8 +9,23 @@ NN_PATH = os.path.join(HERE, "libstem_nn.so")
 
 _vp, _i32 = ctypes.c_void_p, ctypes.c_int32
 _fp = ctypes.POINTER(ctypes.c_float)
+_i64, _f32 = ctypes.c_int64, ctypes.c_float
 _PROTOS = {
-    "stn_conv2d_fwd": (_i32, [_vp, _i32, _i32, _i32, _i32, _vp, _i32, _i32, _vp, _i32, _vp, _i32, _vp]),
+    "stn_conv2d_fwd": (_i32, [_vp, _i32, _i32, _i32, _i32, _vp, _i32, _i32, _vp, _i32, _vp, _vp, _i32, _vp]),
+    "stn_conv2d_wgrad": (_i32, [_vp, _vp, _i32, _i32, _i32, _i32, _i32, _i32, _vp, _vp]),
+    "stn_weight_flip": (_i32, [_vp, _vp, _i32, _i32, _i32, _vp]),
+    "stn_avgpool2": (_i32, [_vp, _vp, _i32, _i32, _i32, _i32, _vp]),
+    "stn_avgpool2_bwd": (_i32, [_vp, _vp, _i32, _i32, _i32, _i32, _vp]),
+    "stn_upsample2": (_i32, [_vp, _vp, _i32, _i32, _i32, _i32, _vp]),
+    "stn_upsample2_bwd": (_i32, [_vp, _vp, _i32, _i32, _i32, _i32, _vp]),
+    "stn_concat": (_i32, [_vp, _vp, _vp, _i64, _i32, _i32, _vp]),
+    "stn_split": (_i32, [_vp, _vp, _vp, _i64, _i32, _i32, _vp]),
+    "stn_relu_mask": (_i32, [_vp, _vp, _i64, _vp]),
+    "stn_bias_grad": (_i32, [_vp, _vp, _i64, _i32, _vp]),
+    "stn_mse": (_i32, [_vp, _vp, _vp, _vp, _i64, _i32, _vp]),
+    "stn_adam": (_i32, [_vp, _vp, _vp, _vp, _vp, _i64, _f32, _f32, _f32, _f32, _i32, _f32, _vp]),
+    "stn_pack": (_i32, [_vp, _i32, _vp, _i64, _i32, _vp]),
+    "stn_to_bf16": (_i32, [_vp, _vp, _i64, _vp]),
     "stn_last_kernel_error": (_i32, []),
 }
 _lib = None
@@ -47,7 +62,12 @@ def _ptr(t):
     return None if t is None else t.data_ptr()
 
 
-def conv2d(x, w, bias=None, relu=False, out_fp32=False, out=None):
+def _bf16_empty(shape, like):
+    import torch
+    return torch.empty(shape, dtype=torch.bfloat16, device=like.device)
+
+
+def conv2d(x, w, bias=None, relu=False, out_fp32=False, out=None, mask=None):
     """NHWC BF16 x (B, H, W, Cin), weights (Cout, taps, Cin) BF16 -> (B, H, W, Cout)."""
     import torch
     B, H, W, Cin = x.shape
@@ -56,10 +76,117 @@ def conv2d(x, w, bias=None, relu=False, out_fp32=False, out=None):
     assert x.is_contiguous() and w.is_contiguous()
     if bias is not None:
         assert bias.dtype == torch.float32 and bias.is_contiguous() and bias.numel() == Cout
+    if mask is not None:
+        assert mask.shape == (B, H, W, Cout) and mask.dtype == torch.bfloat16 and mask.is_contiguous()
     if out is None:
         out = torch.empty((B, H, W, Cout), dtype=torch.float32 if out_fp32 else torch.bfloat16, device=x.device)
-    _check(lib().stn_conv2d_fwd(_ptr(x), B, H, W, Cin, _ptr(w), Cout, taps, _ptr(bias), int(relu), _ptr(out),
-                                int(out_fp32), _stream()), "stn_conv2d_fwd")
+    _check(lib().stn_conv2d_fwd(_ptr(x), B, H, W, Cin, _ptr(w), Cout, taps, _ptr(bias), int(relu), _ptr(mask),
+                                _ptr(out), int(out_fp32), _stream()), "stn_conv2d_fwd")
+    return out
+
+
+def conv2d_wgrad(x, gy, taps, gw):
+    """gw (Cout, taps, Cin) FP32 += weight gradient of a convolution with input x, output gradient gy."""
+    B, H, W, Cin = x.shape
+    Cout = gy.shape[3]
+    assert gy.shape[:3] == x.shape[:3] and gw.shape == (Cout, taps, Cin)
+    _check(lib().stn_conv2d_wgrad(_ptr(x), _ptr(gy), B, H, W, Cin, Cout, taps, _ptr(gw), _stream()),
+           "stn_conv2d_wgrad")
+    return gw
+
+
+def weight_flip(w, out=None):
+    """(Cout, taps, Cin) -> (Cin, taps, Cout) with the taps reversed."""
+    Cout, taps, Cin = w.shape
+    if out is None:
+        out = _bf16_empty((Cin, taps, Cout), w)
+    _check(lib().stn_weight_flip(_ptr(w), _ptr(out), Cout, taps, Cin, _stream()), "stn_weight_flip")
+    return out
+
+
+def conv2d_dgrad(gy, wt, mask=None, out=None):
+    """Input gradient of a convolution: conv of gy with flipped weights wt, masked by mask > 0."""
+    return conv2d(gy, wt, out=out, mask=mask)
+
+
+def avgpool2(x, out=None):
+    B, H, W, C = x.shape
+    out = _bf16_empty((B, H // 2, W // 2, C), x) if out is None else out
+    _check(lib().stn_avgpool2(_ptr(x), _ptr(out), B, H, W, C, _stream()), "stn_avgpool2")
+    return out
+
+
+def avgpool2_bwd(gy, out=None):
+    B, H2, W2, C = gy.shape
+    out = _bf16_empty((B, 2 * H2, 2 * W2, C), gy) if out is None else out
+    _check(lib().stn_avgpool2_bwd(_ptr(gy), _ptr(out), B, 2 * H2, 2 * W2, C, _stream()), "stn_avgpool2_bwd")
+    return out
+
+
+def upsample2(x, out=None):
+    B, H, W, C = x.shape
+    out = _bf16_empty((B, 2 * H, 2 * W, C), x) if out is None else out
+    _check(lib().stn_upsample2(_ptr(x), _ptr(out), B, H, W, C, _stream()), "stn_upsample2")
+    return out
+
+
+def upsample2_bwd(gy, out=None):
+    B, H2, W2, C = gy.shape
+    out = _bf16_empty((B, H2 // 2, W2 // 2, C), gy) if out is None else out
+    _check(lib().stn_upsample2_bwd(_ptr(gy), _ptr(out), B, H2 // 2, W2 // 2, C, _stream()), "stn_upsample2_bwd")
+    return out
+
+
+def concat(a, b, out=None):
+    B, H, W, Ca = a.shape
+    Cb = b.shape[3]
+    out = _bf16_empty((B, H, W, Ca + Cb), a) if out is None else out
+    _check(lib().stn_concat(_ptr(a), _ptr(b), _ptr(out), B * H * W, Ca, Cb, _stream()), "stn_concat")
+    return out
+
+
+def split(gy, Ca, ga=None, gb=None):
+    B, H, W, C = gy.shape
+    _check(lib().stn_split(_ptr(gy), _ptr(ga), _ptr(gb), B * H * W, Ca, C - Ca, _stream()), "stn_split")
+    return ga, gb
+
+
+def relu_mask(g, y):
+    _check(lib().stn_relu_mask(_ptr(g), _ptr(y), g.numel(), _stream()), "stn_relu_mask")
+    return g
+
+
+def bias_grad(g, gb):
+    C = g.shape[-1]
+    _check(lib().stn_bias_grad(_ptr(g), _ptr(gb), g.numel() // C, C, _stream()), "stn_bias_grad")
+    return gb
+
+
+def mse(pred, target, g, loss):
+    """loss (FP32 scalar tensor) += mean (pred[..., 0] - target)^2; g = its gradient (BF16)."""
+    Cp = pred.shape[-1]
+    _check(lib().stn_mse(_ptr(pred), _ptr(target), _ptr(g), _ptr(loss), pred.numel() // Cp, Cp, _stream()), "stn_mse")
+    return loss
+
+
+def adam(w, m, v, g, step, lr, w16=None, beta1=0.9, beta2=0.999, eps=1e-8, wd=0.0):
+    _check(lib().stn_adam(_ptr(w), _ptr(m), _ptr(v), _ptr(g), _ptr(w16), w.numel(), lr, beta1, beta2, eps, step, wd,
+                          _stream()), "stn_adam")
+
+
+def pack(planes, C, out=None):
+    """FP32 planes (n, B, H, W) -> NHWC BF16 (B, H, W, C)."""
+    n = planes.shape[0]
+    B, H, W = planes.shape[1:]
+    out = _bf16_empty((B, H, W, C), planes) if out is None else out
+    _check(lib().stn_pack(_ptr(planes), n, _ptr(out), B * H * W, C, _stream()), "stn_pack")
+    return out
+
+
+def to_bf16(x, out=None):
+    import torch
+    out = torch.empty(x.shape, dtype=torch.bfloat16, device=x.device) if out is None else out
+    _check(lib().stn_to_bf16(_ptr(x), _ptr(out), x.numel(), _stream()), "stn_to_bf16")
     return out
 
 

@@ -53,3 +53,65 @@ def test_conv_fwd_matches_oracle(nn, B, H, W, Cin, Cout, taps):
     got16 = nn.conv2d(_bf16(x), _bf16(w), torch.from_numpy(bias).cuda(), relu=True).float().cpu().numpy()
     ref = np.maximum(want, 0.0)
     assert np.all(np.abs(got16 - ref) <= np.abs(ref) * 2.0 ** -8 + 1e-5 * scale)
+
+
+@pytest.mark.parametrize("B,H,W,Cin,Cout,taps", [
+    (1, 16, 16, 32, 64, 9),
+    (2, 13, 17, 16, 32, 9),
+    (1, 20, 24, 64, 128, 9),
+    (1, 12, 12, 128, 256, 9),
+    (2, 1, 300, 64, 32, 1),
+])
+def test_conv_backward_matches_oracle(nn, B, H, W, Cin, Cout, taps):
+    """Input gradient (flipped weights + masked forward convolution) and weight gradient."""
+    rng = np.random.default_rng(7 * B + H + Cin + Cout)
+    x = NO.bf16_round(np.maximum(rng.standard_normal((B, H, W, Cin)).astype(np.float32), 0.0))  # post-ReLU
+    w = _rand(rng, Cout, taps, Cin, scale=1.0 / np.sqrt(taps * Cin))
+    gy = _rand(rng, B, H, W, Cout)
+    # input gradient, masked by the ReLU that produced x
+    wt = nn.weight_flip(_bf16(w))
+    got = nn.conv2d(_bf16(gy), wt, mask=_bf16(x), out_fp32=True).cpu().numpy()
+    want = NO.conv2d_grad_input(gy, w) * (x > 0)
+    assert np.abs(got - want).max() <= 1e-5 * np.abs(want).max()
+    # weight gradient (FP32, accumulated into zeros)
+    gw = torch.zeros((Cout, taps, Cin), dtype=torch.float32, device="cuda")
+    nn.conv2d_wgrad(_bf16(x), _bf16(gy), taps, gw)
+    torch.cuda.synchronize()
+    assert nn.last_kernel_error() == 0
+    want_w = NO.conv2d_grad_weight(x, gy, taps)
+    assert np.abs(gw.cpu().numpy() - want_w).max() <= 1e-5 * np.abs(want_w).max() + 1e-6
+
+
+def test_elementwise_layers_match_oracle(nn):
+    rng = np.random.default_rng(11)
+    x = _rand(rng, 2, 8, 12, 32)
+    g = _rand(rng, 2, 4, 6, 32)
+    assert np.allclose(nn.avgpool2(_bf16(x)).float().cpu().numpy(), NO.bf16_round(NO.avgpool2(x).astype(np.float32)))
+    assert np.allclose(nn.avgpool2_bwd(_bf16(g)).float().cpu().numpy(),
+                       NO.bf16_round(NO.avgpool2_bwd(g).astype(np.float32)))
+    assert np.array_equal(nn.upsample2(_bf16(g)).float().cpu().numpy(), NO.upsample2(g))
+    assert np.allclose(nn.upsample2_bwd(_bf16(x)).float().cpu().numpy(),
+                       NO.bf16_round(NO.upsample2_bwd(x).astype(np.float32)))
+    a, b = _rand(rng, 2, 5, 7, 16), _rand(rng, 2, 5, 7, 24)
+    cat = nn.concat(_bf16(a), _bf16(b))
+    assert np.array_equal(cat.float().cpu().numpy(), np.concatenate([a, b], axis=3))
+    ga = torch.empty((2, 5, 7, 16), dtype=torch.bfloat16, device="cuda")
+    gb = torch.empty((2, 5, 7, 24), dtype=torch.bfloat16, device="cuda")
+    nn.split(cat, 16, ga, gb)
+    assert np.array_equal(ga.float().cpu().numpy(), a) and np.array_equal(gb.float().cpu().numpy(), b)
+    gm = _bf16(x)
+    nn.relu_mask(gm, _bf16(np.abs(x) - 0.5))
+    assert np.array_equal(gm.float().cpu().numpy(), x * (np.abs(x) - 0.5 > 0))
+    gbias = torch.zeros(32, dtype=torch.float32, device="cuda")
+    nn.bias_grad(_bf16(x), gbias)
+    assert np.allclose(gbias.cpu().numpy(), NO.conv2d_grad_bias(x), rtol=1e-5, atol=1e-4)
+    pred = rng.standard_normal((3, 9, 10, 16)).astype(np.float32)
+    tgt = rng.standard_normal((3, 9, 10)).astype(np.float32)
+    loss = torch.zeros(1, dtype=torch.float32, device="cuda")
+    gl = torch.empty((3, 9, 10, 16), dtype=torch.bfloat16, device="cuda")
+    nn.mse(torch.from_numpy(pred).cuda(), torch.from_numpy(tgt).cuda(), gl, loss)
+    d = pred[..., 0].astype(np.float64) - tgt
+    assert abs(loss.item() - (d ** 2).mean()) <= 1e-5 * (d ** 2).mean()
+    glh = gl.float().cpu().numpy()
+    assert np.allclose(glh[..., 0], NO.bf16_round((2 * d / d.size).astype(np.float32)), rtol=0, atol=1e-7)
+    assert not glh[..., 1:].any()
