@@ -122,6 +122,16 @@ int st_tune(st_ctx* ctx, int32_t mode);
 /* Number of slab-ring variants (valid forced modes are 0 .. count - 1). */
 int st_tune_variants(void);
 
+/* st_image_device restricted to chosen tiles: d_tile_mask (device, one byte per mask_T x
+ * mask_T pixel tile, ceil(Mx / mask_T) tiles per row, row-major) selects the tiles whose
+ * columns are computed; the other pixels are left 0.  mask_T a multiple of 8, the
+ * geometry's window origin a multiple of 8 (x) and 4 (y).  The binning is that of the
+ * whole window.  Used to recompute only the tiles a faster estimate cannot be trusted on
+ * (the learned corrector's fallback).  No counterpart in the reference. */
+int st_image_device_masked(st_ctx* ctx, const st_geom* geom, const double* d_x, int64_t ldx, int64_t nAtoms,
+                           const double* aa, int32_t nPrec, int32_t flags, double* d_img,
+                           const unsigned char* d_tile_mask, int32_t mask_T, void* stream);
+
 /* One image of a batch: its geometry, its atoms, its precession parameters
  * aa(1:nPrec) in host memory, and its output.  x and img are device pointers
  * for st_batch_device and host pointers for st_batch. */

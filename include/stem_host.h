@@ -53,6 +53,13 @@ double st_d2bi_get_deviation_parameter(const st_d2bi* h);
  * `nprocs` and patch jj: the st_image geometry and aa(1:nPrec). */
 int st_d2bi_image_geometry(const st_d2bi* h, int64_t nAtoms, int32_t nprocs, int32_t jj, double precAngle,
                            int32_t nPrec, st_geom* geom, double* aa);
+
+/* The same for an arbitrary pixel window [ix0, ix0 + Dx) x [iy0, iy0 + Dy) (clipped to the
+ * image): the link-cell box of a patch of that size at that origin.  No counterpart in the
+ * reference, whose patches come from the process split; used to recompute chosen tiles of
+ * an image (the corrector's fallback). */
+int st_d2bi_window_geometry(const st_d2bi* t, int64_t nAtoms, int32_t ix0, int32_t iy0, int32_t Dx, int32_t Dy,
+                            double precAngle, int32_t nPrec, st_geom* G, double* aa);
 /* computeD2BI_img (:1563-1998) on one process through st_image: the
  * precession-averaged dark-field image (Mx x My, column-major). */
 int st_d2bi_compute_img(const st_d2bi* h, st_ctx* ctx, const double* x, int64_t ldx, int64_t nAtoms,

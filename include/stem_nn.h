@@ -50,9 +50,12 @@ int stn_relu_mask(void* g, const void* y, int64_t n, void* stream);
 /* gb[c] += sum over pixels of g[p][c] (gb FP32). */
 int stn_bias_grad(const void* g, float* gb, int64_t npix, int32_t C, void* stream);
 
-/* *loss += mean over pixels of (pred[p][0] - target[p])^2 (pred FP32 [npix][Cp], target
- * FP32 [npix]); g (BF16 [npix][Cp], may be null) = the loss gradient, zero in channels >= 1. */
-int stn_mse(const float* pred, const float* target, void* g, float* loss, int64_t npix, int32_t Cp, void* stream);
+/* *loss += mean over pixels of (pred[p][0] - target[p])^2 + w1 (pred[p][1] - |target[p]|)^2
+ * (pred FP32 [npix][Cp], target FP32 [npix]; the second term when w1 > 0): channel 0
+ * regresses the target, channel 1 its magnitude.  g (BF16 [npix][Cp], may be null) = the
+ * loss gradient, zero in the other channels. */
+int stn_mse(const float* pred, const float* target, void* g, float* loss, int64_t npix, int32_t Cp, float w1,
+            void* stream);
 
 /* One Adam step (step >= 1) on FP32 parameters w with moments m, v and gradient g; w16
  * (BF16, may be null) receives the updated parameters.  wd: decoupled weight decay. */
@@ -63,6 +66,33 @@ int stn_adam(float* w, float* m, float* v, const float* g, void* w16, int64_t n,
  * BF16 copy. */
 int stn_pack(const float* planes, int32_t nplanes, void* y, int64_t npix, int32_t C, void* stream);
 int stn_to_bf16(const float* x, void* y, int64_t n, void* stream);
+
+/* a += b (BF16, n values); memset of `bytes` bytes to zero. */
+int stn_add(void* a, const void* b, int64_t n, void* stream);
+int stn_fill_zero(void* p, int64_t bytes, void* stream);
+
+/* *mean = the mean of an FP64 image of n pixels (device scalar). */
+int stn_image_mean(const double* img, int64_t n, double* mean, void* stream);
+
+/* The corrector's planes on the fine grid (Hp x Wp >= My8 x Mx8, extended periodically):
+ * with DF the coarse image img2 (FP64 Mx2 x My2, column-major) interpolated bilinearly at
+ * the fine pixels' positions (pixel i of an N-pixel axis at i d / N) and mu = *mean,
+ * planes (FP32 [5][Hp][Wp]) = (DF - mu) contrast, (mu - DF) contrast, sg_value, mu, DF. */
+int stn_resample_planes(const double* img2, int32_t Mx2, int32_t My2, int32_t Mx8, int32_t My8, int32_t Wp,
+                        int32_t Hp, float sg_value, const double* mean, float contrast, float* planes, void* stream);
+
+/* out (FP64 Mx8 x My8 column-major) = base + pred[..][0] * scale (base FP32 [Hp][Wp], pred
+ * FP32 [Hp][Wp][Cp]). */
+int stn_apply_correction(const float* base, const float* pred, int32_t Cp, int32_t Mx8, int32_t My8, int32_t Wp,
+                         float scale, double* out, void* stream);
+
+/* Per T x T tile of the Mx8 x My8 image: max |pred[..][ch]| -> tile_max [ceil(My8/T)][ceil(Mx8/T)]. */
+int stn_tile_maxabs(const float* pred, int32_t Cp, int32_t ch, int32_t Mx8, int32_t My8, int32_t Wp, int32_t T,
+                    float* tile_max, void* stream);
+
+/* out = fine on every T x T tile whose flag (int32 [ceil(My/T)][ntx]) is nonzero. */
+int stn_merge_tiles(const double* fine, const int32_t* flags, int32_t ntx, int32_t T, int32_t Mx, int32_t My,
+                    double* out, void* stream);
 
 /* First failure recorded by a corrector kernel since the last call (0 = none; 1 = a
  * tensor-core wait ran out), then cleared.  Synchronises the device. */

@@ -75,6 +75,8 @@ _PROTOS = {
     "st_blur_noalloc": (_i32, [_vp, _i32, _i32, _d, _vp, _vp, ctypes.c_char_p, _i32]),
     "st_batch_device": (_i32, [_vp, _i32, ctypes.POINTER(StJob), _i32, _vp]),
     "st_batch": (_i32, [_vp, _i32, ctypes.POINTER(StJob), _i32]),
+    "st_image_device_masked": (_i32, [_vp, ctypes.POINTER(StGeom), _vp, _i64, _i64, _dp, _i32, _i32, _vp, _vp, _i32,
+                                      _vp]),
     "st_tune": (_i32, [_vp, _i32]),
     "st_plan_create": (_i32, [_vp, _i32, ctypes.POINTER(StJob), _i32, _vp, ctypes.POINTER(_vp)]),
     "st_plan_launch": (_i32, [_vp, _vp]),
@@ -98,6 +100,7 @@ _PROTOS = {
     "st_d2bi_get_rotation": (_i32, [_vp, _dp, _dp]),
     "st_d2bi_get_deviation_parameter": (_d, [_vp]),
     "st_d2bi_image_geometry": (_i32, [_vp, _i64, _i32, _i32, _d, _i32, ctypes.POINTER(StGeom), _dp]),
+    "st_d2bi_window_geometry": (_i32, [_vp, _i64, _i32, _i32, _i32, _i32, _d, _i32, ctypes.POINTER(StGeom), _dp]),
     "st_d2bi_compute_img": (_i32, [_vp, _vp, _dp, _i64, _i64, _d, _i32, _i32, _dp]),
     "st_wrap_pbc": (_i32, [_dp, _i32, _i32, _i32, _dp, _i64, _i64]),
     "st_atom_extents": (_i32, [_dp, _dp, _dp, _dp, _i64, _i64, _dp]),

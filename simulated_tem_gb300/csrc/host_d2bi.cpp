@@ -464,13 +464,18 @@ int st_d2bi_get_rotation(const st_d2bi* h, double* U, double* R) {
 
 double st_d2bi_get_deviation_parameter(const st_d2bi* h) { return h ? h->sg : NAN; }
 
-int st_d2bi_image_geometry(const st_d2bi* t, int64_t nAtoms, int32_t nprocs, int32_t jj, double precAngle,
-                           int32_t nPrec, st_geom* G, double* aa) {
-  if (!t || !G || !aa || nPrec < 1 || nAtoms < 0) return ST_ERR_ARG;
+namespace {
+
+// The geometry of the pixel window [ix0, ix0 + Dx) x [iy0, iy0 + Dy) (clipped to the
+// image): the patch set-up of computeD2BI_img (:1714-1760, 1843-1852) with the patch
+// origin jx Dx, jy Dy replaced by (ix0, iy0).
+int window_geometry(const st_d2bi* t, int64_t nAtoms, int ix0, int iy0, int Dx, int Dy, double precAngle,
+                    int32_t nPrec, st_geom* G, double* aa) {
   std::memset(G, 0, sizeof *G);
   double xmax[3];
   int Mx, My, Mz;
   st_d2bi_find_image_parameters(t, nullptr, xmax, nullptr, &Mx, &My, &Mz);
+  if (ix0 < 0 || iy0 < 0 || ix0 >= Mx || iy0 >= My || Dx < 1 || Dy < 1) return ST_ERR_ARG;
   double costheta = 1.0, sintheta = 0.0;
   if (nPrec > 1) {
     costheta = std::cos(precAngle);
@@ -480,12 +485,7 @@ int st_d2bi_image_geometry(const st_d2bi* t, int64_t nAtoms, int32_t nprocs, int
   const double cmin = std::min(t->gksuper.cell_side(1), t->gksuper.cell_side(2));
   const int deltaM = (int)std::ceil(3 * sigma / cmin);
   const int nMax = estimate_max_count_per_cell((double)Mx * My * Mz, (int)nAtoms) * deltaM * deltaM;
-  int Cx, Cy;
-  if (!factorise_parallel(Mx, My, nprocs, Cx, Cy)) return ST_ERR_ARG;
-  if (jj < 0 || jj >= Cx * Cy) return ST_ERR_ARG;
-  // real(Mx)/Cx and real(Dx)/deltaM + 2 are default-kind (single precision) in the reference
-  const int Dx = (int)std::ceil((float)Mx / (float)Cx);
-  const int Dy = (int)std::ceil((float)My / (float)Cy);
+  // real(Dx)/deltaM + 2 is default-kind (single precision) in the reference
   const int Ex = std::max(3, (int)std::floor((float)Dx / (float)deltaM + 2.0f));
   const int Ey = std::max(3, (int)std::floor((float)Dy / (float)deltaM + 2.0f));
   const int Ez = std::max(3, (int)std::floor((float)Mz / (float)deltaM));
@@ -522,17 +522,16 @@ int st_d2bi_image_geometry(const st_d2bi* t, int64_t nAtoms, int32_t nprocs, int
     aa[prec - 1] = (2 * kPi * t->deviation(z));
   }
 
-  const int jy = jj / Cx, jx = jj - jy * Cx;  // :1843-1852
-  const Vec3 p0 = t->gksuper.cell_to_real(jx * Dx, jy * Dy, 0);
+  const Vec3 p0 = t->gksuper.cell_to_real(ix0, iy0, 0);  // :1843-1852
   const Vec3 p1 = lc.cell_to_real(1, 1, 0);
   for (int i = 0; i < 3; ++i) G->lc_delta[i] = p0[i] - p1[i];
   G->Mx = Mx;
   G->My = My;
   G->Mz = Mz;
-  G->ix0 = jx * Dx;
-  G->ix1 = std::min((jx + 1) * Dx, Mx);
-  G->iy0 = jy * Dy;
-  G->iy1 = std::min((jy + 1) * Dy, My);
+  G->ix0 = ix0;
+  G->ix1 = std::min(ix0 + Dx, Mx);
+  G->iy0 = iy0;
+  G->iy1 = std::min(iy0 + Dy, My);
   G->Ex = Ex;
   G->Ey = Ey;
   G->Ez = Ez;
@@ -556,6 +555,30 @@ int st_d2bi_image_geometry(const st_d2bi* t, int64_t nAtoms, int32_t nprocs, int
   G->b0 = (kPi / t->xi0);
   G->bg = (kPi / t->xig);
   return ST_OK;
+}
+
+}  // namespace
+
+int st_d2bi_image_geometry(const st_d2bi* t, int64_t nAtoms, int32_t nprocs, int32_t jj, double precAngle,
+                           int32_t nPrec, st_geom* G, double* aa) {
+  if (!t || !G || !aa || nPrec < 1 || nAtoms < 0) return ST_ERR_ARG;
+  double xmax[3];
+  int Mx, My, Mz;
+  st_d2bi_find_image_parameters(t, nullptr, xmax, nullptr, &Mx, &My, &Mz);
+  int Cx, Cy;
+  if (!factorise_parallel(Mx, My, nprocs, Cx, Cy)) return ST_ERR_ARG;
+  if (jj < 0 || jj >= Cx * Cy) return ST_ERR_ARG;
+  // real(Mx)/Cx is default-kind (single precision) in the reference
+  const int Dx = (int)std::ceil((float)Mx / (float)Cx);
+  const int Dy = (int)std::ceil((float)My / (float)Cy);
+  const int jy = jj / Cx, jx = jj - jy * Cx;
+  return window_geometry(t, nAtoms, jx * Dx, jy * Dy, Dx, Dy, precAngle, nPrec, G, aa);
+}
+
+int st_d2bi_window_geometry(const st_d2bi* t, int64_t nAtoms, int32_t ix0, int32_t iy0, int32_t Dx, int32_t Dy,
+                            double precAngle, int32_t nPrec, st_geom* G, double* aa) {
+  if (!t || !G || !aa || nPrec < 1 || nAtoms < 0) return ST_ERR_ARG;
+  return window_geometry(t, nAtoms, ix0, iy0, Dx, Dy, precAngle, nPrec, G, aa);
 }
 
 int st_d2bi_compute_img(const st_d2bi* t, st_ctx* ctx, const double* x, int64_t ldx, int64_t nAtoms,

@@ -105,7 +105,17 @@ struct ColumnParams {
   double* img;
   unsigned long long* counters;  // [0] kept atoms: above `cap` the binning overflowed and the kernel exits
   int64_t cap;
+  // null, or one byte per mask_T x mask_T pixel tile (mask_ntx tiles per row): the columns of
+  // tiles whose byte is 0 are not computed (mask_T a multiple of 8, window origin aligned)
+  const unsigned char* tile_mask;
+  int mask_T, mask_ntx;
 };
+
+// Whether warp tile (tx, ty) of a column launch is to be computed.
+__device__ __forceinline__ bool tile_wanted(const ColumnParams& p, int tx, int ty, int tile_x, int tile_y) {
+  if (!p.tile_mask) return true;
+  return p.tile_mask[((p.iy0 + ty * tile_y) / p.mask_T) * p.mask_ntx + (p.ix0 + tx * tile_x) / p.mask_T] != 0;
+}
 
 // launchers (return cudaError_t of the launches)
 // Binning of a batch: jobs (device memory, n_jobs entries) with candidates

@@ -242,6 +242,7 @@ __global__ void __launch_bounds__(kWarps * 32) k_column_fp32(const __grid_consta
   if (tile >= tiles_x * tiles_y) return;
   if ((int64_t)p.counters[0] > p.cap) return;  // the binning overflowed: the host retries
   const int tx = tile % tiles_x, ty = tile / tiles_x;
+  if (!tile_wanted(p, tx, ty, kTileX, kTileY)) return;
   const int ix = p.ix0 + tx * kTileX + (lane & (kTileX - 1));
   const int iy = p.iy0 + ty * kTileY + lane / kTileX;
   const bool active = ix < p.ix1 && iy < p.iy1;
@@ -471,6 +472,7 @@ __global__ void __launch_bounds__(kWarps * 32) k_column_fp64(const __grid_consta
   if (tile >= tiles_x * tiles_y) return;
   if ((int64_t)p.counters[0] > p.cap) return;  // the binning overflowed: the host retries
   const int tx = tile % tiles_x, ty = tile / tiles_x;
+  if (!tile_wanted(p, tx, ty, kTileX, kTileY)) return;
   const int ix = p.ix0 + tx * kTileX + (lane & (kTileX - 1));
   const int iy = p.iy0 + ty * kTileY + lane / kTileX;
   const bool active = ix < p.ix1 && iy < p.iy1;

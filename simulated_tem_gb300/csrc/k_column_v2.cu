@@ -246,6 +246,7 @@ __device__ __noinline__ bool column_tile(const ColumnParams& p, WarpSmem& W, int
   const int Wd = p.ix1 - p.ix0;
   const int tiles_x = (Wd + kTileX - 1) / kTileX;
   const int tx = tile % tiles_x, ty = tile / tiles_x;
+  if (!tile_wanted(p, tx, ty, kTileX, kTileY)) return true;
   const int ix = p.ix0 + tx * kTileX + (lane & (kTileX - 1));
   const int iy = p.iy0 + ty * kTileY + lane / kTileX;
   const bool active = ix < p.ix1 && iy < p.iy1;

@@ -33,12 +33,20 @@ int split(const __nv_bfloat16* gy, __nv_bfloat16* ga, __nv_bfloat16* gb, long lo
           cudaStream_t st);
 int relu_mask(__nv_bfloat16* g, const __nv_bfloat16* y, long long n, cudaStream_t st);
 int bias_grad(const __nv_bfloat16* g, float* gb, long long npix, int C, cudaStream_t st);
-int mse(const float* pred, const float* target, __nv_bfloat16* g, float* loss, long long npix, int Cp,
+int mse(const float* pred, const float* target, __nv_bfloat16* g, float* loss, long long npix, int Cp, float w1,
         cudaStream_t st);
 int adam(float* w, float* m, float* v, const float* g, __nv_bfloat16* w16, long long n, float lr, float b1, float b2,
          float eps, int step, float wd, cudaStream_t st);
 int pack(const float* planes, int nplanes, __nv_bfloat16* y, long long npix, int C, cudaStream_t st);
 int to_bf16(const float* x, __nv_bfloat16* y, long long n, cudaStream_t st);
+int add(__nv_bfloat16* a, const __nv_bfloat16* b, long long n, cudaStream_t st);
+int image_mean(const double* img, long long n, double* mean, cudaStream_t st);
+int resample_planes(const double* img2, int Mx2, int My2, int Mx8, int My8, int Wp, int Hp, float sg_value,
+                    const double* mean, float contrast, float* planes, cudaStream_t st);
+int apply_correction(const float* base, const float* pred, int Cp, int Mx8, int My8, int Wp, float scale, double* out,
+                     cudaStream_t st);
+int tile_maxabs(const float* pred, int Cp, int ch, int Mx8, int My8, int Wp, int T, float* tile_max, cudaStream_t st);
+int merge_tiles(const double* fine, const int* flags, int ntx, int T, int Mx, int My, double* out, cudaStream_t st);
 
 // First failure recorded by a corrector kernel (0 = none), then cleared; synchronises.
 int take_error();

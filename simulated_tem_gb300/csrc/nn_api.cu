@@ -51,8 +51,8 @@ extern "C" int stn_bias_grad(const void* g, float* gb, int64_t npix, int32_t C, 
   return bias_grad(cb(g), gb, npix, C, cs(stream));
 }
 extern "C" int stn_mse(const float* pred, const float* target, void* g, float* loss, int64_t npix, int32_t Cp,
-                       void* stream) {
-  return mse(pred, target, mb(g), loss, npix, Cp, cs(stream));
+                       float w1, void* stream) {
+  return mse(pred, target, mb(g), loss, npix, Cp, w1, cs(stream));
 }
 extern "C" int stn_adam(float* w, float* m, float* v, const float* g, void* w16, int64_t n, float lr, float beta1,
                         float beta2, float eps, int32_t step, float wd, void* stream) {
@@ -63,5 +63,30 @@ extern "C" int stn_pack(const float* planes, int32_t nplanes, void* y, int64_t n
 }
 extern "C" int stn_to_bf16(const float* x, void* y, int64_t n, void* stream) {
   return to_bf16(x, mb(y), n, cs(stream));
+}
+extern "C" int stn_add(void* a, const void* b, int64_t n, void* stream) { return add(mb(a), cb(b), n, cs(stream)); }
+extern "C" int stn_fill_zero(void* p, int64_t bytes, void* stream) {
+  if (!p || bytes < 0) return 1;
+  return cudaMemsetAsync(p, 0, (size_t)bytes, cs(stream)) == cudaSuccess ? 0 : 2;
+}
+extern "C" int stn_image_mean(const double* img, int64_t n, double* mean, void* stream) {
+  return image_mean(img, n, mean, cs(stream));
+}
+extern "C" int stn_resample_planes(const double* img2, int32_t Mx2, int32_t My2, int32_t Mx8, int32_t My8,
+                                   int32_t Wp, int32_t Hp, float sg_value, const double* mean, float contrast,
+                                   float* planes, void* stream) {
+  return resample_planes(img2, Mx2, My2, Mx8, My8, Wp, Hp, sg_value, mean, contrast, planes, cs(stream));
+}
+extern "C" int stn_apply_correction(const float* base, const float* pred, int32_t Cp, int32_t Mx8, int32_t My8,
+                                    int32_t Wp, float scale, double* out, void* stream) {
+  return apply_correction(base, pred, Cp, Mx8, My8, Wp, scale, out, cs(stream));
+}
+extern "C" int stn_tile_maxabs(const float* pred, int32_t Cp, int32_t ch, int32_t Mx8, int32_t My8, int32_t Wp,
+                               int32_t T, float* tile_max, void* stream) {
+  return tile_maxabs(pred, Cp, ch, Mx8, My8, Wp, T, tile_max, cs(stream));
+}
+extern "C" int stn_merge_tiles(const double* fine, const int32_t* flags, int32_t ntx, int32_t T, int32_t Mx,
+                               int32_t My, double* out, void* stream) {
+  return merge_tiles(fine, flags, ntx, T, Mx, My, out, cs(stream));
 }
 extern "C" int stn_last_kernel_error(void) { return take_error(); }

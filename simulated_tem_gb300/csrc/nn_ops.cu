@@ -141,21 +141,24 @@ __global__ void k_bias_grad(const __nv_bfloat16* __restrict__ g, float* __restri
   for (int c = threadIdx.x; c < C; c += blockDim.x) atomicAdd(&gb[c], part[c]);
 }
 
-// loss = mean_p (pred[p, 0] - target[p])^2 over npix pixels (pred FP32 [npix][Cp]);
-// g[p, 0] = 2 (pred - target) / npix as BF16 [npix][Cp] (other channels 0); the loss sum
-// is added to *loss.
+// loss = mean_p (pred[p, 0] - target[p])^2 + w1 mean_p (pred[p, 1] - |target[p]|)^2 over
+// npix pixels (pred FP32 [npix][Cp]): channel 0 regresses the target, channel 1 (when
+// w1 > 0) its magnitude; g (BF16 [npix][Cp]) = the loss gradient, 0 in the other channels.
+// The loss is added to *loss.
 __global__ void k_mse(const float* __restrict__ pred, const float* __restrict__ target, __nv_bfloat16* __restrict__ g,
-                      float* __restrict__ loss, long long npix, int Cp) {
+                      float* __restrict__ loss, long long npix, int Cp, float w1) {
   __shared__ float red[kBlock / 32];
   float s = 0.f;
   const float scale = 2.f / (float)npix;
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npix;
        p += (long long)gridDim.x * blockDim.x) {
-    const float d = pred[p * Cp] - target[p];
-    s += d * d;
+    const float t = target[p];
+    const float d = pred[p * Cp] - t;
+    const float d1 = w1 > 0.f ? pred[p * Cp + 1] - fabsf(t) : 0.f;
+    s += d * d + w1 * d1 * d1;
     if (g) {
       g[p * Cp] = tobf(scale * d);
-      for (int c = 1; c < Cp; ++c) g[p * Cp + c] = tobf(0.f);
+      for (int c = 1; c < Cp; ++c) g[p * Cp + c] = tobf(c == 1 ? scale * w1 * d1 : 0.f);
     }
   }
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
@@ -199,6 +202,103 @@ __global__ void k_pack(const float* __restrict__ planes, int nplanes, __nv_bfloa
 __global__ void k_to_bf16(const float* __restrict__ x, __nv_bfloat16* __restrict__ y, long long n) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
     y[i] = tobf(x[i]);
+}
+
+// a += b (BF16, FP32 arithmetic)
+__global__ void k_add(__nv_bfloat16* __restrict__ a, const __nv_bfloat16* __restrict__ b, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    a[i] = tobf(bf(a[i]) + bf(b[i]));
+}
+
+// mean[0] += sum of img / n (FP64); mean must be zeroed before
+__global__ void k_image_mean(const double* __restrict__ img, long long n, double* __restrict__ mean) {
+  __shared__ double red[kBlock / 32];
+  double s = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    s += img[i];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x / 32); ++w) t += red[w];
+    atomicAdd(mean, t / (double)n);
+  }
+}
+
+// The corrector's planes on the fine (M = 8) pixel grid, Hp x Wp (the image My8 x Mx8
+// extended periodically).  DF is the coarse (M = 2) image interpolated bilinearly at the
+// fine pixels' positions (pixel i of an N-pixel axis sits at i d / N on both grids; the
+// supercell is periodic); mu is the coarse image's mean.  Planes (FP32 [5][Hp][Wp]):
+// 0: (DF - mu) * contrast, 1: (BF - (1 - mu)) * contrast with BF = 1 - DF, 2: sg_value,
+// 3: mu, 4: DF (the base the correction is added to).  Planes 0-3 are the network's input:
+// the contrast, a few 1e-3 on a level near 0.1-0.7, would not survive BF16 unshifted.
+// img2: FP64 (Mx2, My2) column-major.
+__global__ void k_resample_planes(const double* __restrict__ img2, int Mx2, int My2, int Mx8, int My8, int Wp, int Hp,
+                                  float sg_value, const double* __restrict__ mean, float contrast,
+                                  float* __restrict__ planes) {
+  const long long n = (long long)Wp * Hp;
+  const double sx = (double)Mx2 / Mx8, sy = (double)My2 / My8;
+  const double mu = *mean;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int px = (int)(i % Wp) % Mx8, py = (int)(i / Wp) % My8;
+    const double u = px * sx, v = py * sy;
+    int i0 = (int)floor(u), j0 = (int)floor(v);
+    const double fu = u - i0, fv = v - j0;
+    i0 %= Mx2;
+    j0 %= My2;
+    const int i1 = (i0 + 1) % Mx2, j1 = (j0 + 1) % My2;
+    const double a = img2[i0 + (long long)Mx2 * j0], b = img2[i1 + (long long)Mx2 * j0];
+    const double c = img2[i0 + (long long)Mx2 * j1], d = img2[i1 + (long long)Mx2 * j1];
+    const double df = (1.0 - fv) * ((1.0 - fu) * a + fu * b) + fv * ((1.0 - fu) * c + fu * d);
+    planes[i] = (float)((df - mu) * contrast);
+    planes[n + i] = (float)(-(df - mu) * contrast);
+    planes[2 * n + i] = sg_value;
+    planes[3 * n + i] = (float)mu;
+    planes[4 * n + i] = (float)df;
+  }
+}
+
+// out (FP64, Mx8 x My8 column-major) = base + pred[p][0] * scale, p over the Hp x Wp
+// grid's top-left My8 x Mx8 block.
+__global__ void k_apply_correction(const float* __restrict__ base, const float* __restrict__ pred, int Cp, int Mx8,
+                                   int My8, int Wp, float scale, double* __restrict__ out) {
+  const long long n = (long long)Mx8 * My8;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(i % Mx8), y = (int)(i / Mx8);
+    const long long p = (long long)y * Wp + x;
+    out[i] = (double)base[p] + (double)pred[p * Cp] * (double)scale;
+  }
+}
+
+// tile_max[ty][tx] = max |pred[p][ch]| over the T x T tile (inside Mx8 x My8); one block per tile
+__global__ void k_tile_maxabs(const float* __restrict__ pred, int Cp, int ch, int Mx8, int My8, int Wp, int T,
+                              float* __restrict__ tile_max) {
+  const int tx = blockIdx.x, ty = blockIdx.y;
+  float m = 0.f;
+  for (int k = threadIdx.x; k < T * T; k += blockDim.x) {
+    const int x = tx * T + k % T, y = ty * T + k / T;
+    if (x < Mx8 && y < My8) m = fmaxf(m, fabsf(pred[((long long)y * Wp + x) * Cp + ch]));
+  }
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  __shared__ float red[kBlock / 32];
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float t = 0.f;
+    for (int w = 0; w < (int)(blockDim.x / 32); ++w) t = fmaxf(t, red[w]);
+    tile_max[ty * gridDim.x + tx] = t;
+  }
+}
+
+// out[tile] = fine[tile] for every tile with flag != 0 (FP64 images, Mx x My column-major)
+__global__ void k_merge_tiles(const double* __restrict__ fine, const int* __restrict__ flags, int ntx, int T, int Mx,
+                              int My, double* __restrict__ out) {
+  const long long n = (long long)Mx * My;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(i % Mx), y = (int)(i / Mx);
+    if (flags[(y / T) * ntx + x / T]) out[i] = fine[i];
+  }
 }
 
 int status() { return cudaGetLastError() == cudaSuccess ? 0 : 2; }
@@ -249,10 +349,10 @@ int bias_grad(const __nv_bfloat16* g, float* gb, long long npix, int C, cudaStre
   k_bias_grad<<<grid, kBlock, C * sizeof(float), st>>>(g, gb, npix, C);
   return status();
 }
-int mse(const float* pred, const float* target, __nv_bfloat16* g, float* loss, long long npix, int Cp,
+int mse(const float* pred, const float* target, __nv_bfloat16* g, float* loss, long long npix, int Cp, float w1,
         cudaStream_t st) {
-  if (!pred || !target || !loss || Cp < 1) return 1;
-  k_mse<<<grid_for(npix / 4), kBlock, 0, st>>>(pred, target, g, loss, npix, Cp);
+  if (!pred || !target || !loss || Cp < 1 || (w1 > 0.f && Cp < 2)) return 1;
+  k_mse<<<grid_for(npix / 4), kBlock, 0, st>>>(pred, target, g, loss, npix, Cp, w1);
   return status();
 }
 int adam(float* w, float* m, float* v, const float* g, __nv_bfloat16* w16, long long n, float lr, float b1, float b2,
@@ -269,6 +369,41 @@ int adam(float* w, float* m, float* v, const float* g, __nv_bfloat16* w16, long 
 int pack(const float* planes, int nplanes, __nv_bfloat16* y, long long npix, int C, cudaStream_t st) {
   if (!planes || !y || nplanes < 1 || nplanes > C) return 1;
   k_pack<<<grid_for(npix * C), kBlock, 0, st>>>(planes, nplanes, y, npix, C);
+  return status();
+}
+int add(__nv_bfloat16* a, const __nv_bfloat16* b, long long n, cudaStream_t st) {
+  if (!a || !b) return 1;
+  k_add<<<grid_for(n), kBlock, 0, st>>>(a, b, n);
+  return status();
+}
+int image_mean(const double* img, long long n, double* mean, cudaStream_t st) {
+  if (!img || !mean || n < 1) return 1;
+  if (cudaMemsetAsync(mean, 0, sizeof(double), st) != cudaSuccess) return 2;
+  k_image_mean<<<grid_for(n) < 1024 ? grid_for(n) : 1024, kBlock, 0, st>>>(img, n, mean);
+  return status();
+}
+int resample_planes(const double* img2, int Mx2, int My2, int Mx8, int My8, int Wp, int Hp, float sg_value,
+                    const double* mean, float contrast, float* planes, cudaStream_t st) {
+  if (!img2 || !planes || !mean || Mx2 < 1 || My2 < 1 || Mx8 < 1 || My8 < 1 || Wp < Mx8 || Hp < My8) return 1;
+  k_resample_planes<<<grid_for((long long)Wp * Hp), kBlock, 0, st>>>(img2, Mx2, My2, Mx8, My8, Wp, Hp, sg_value,
+                                                                    mean, contrast, planes);
+  return status();
+}
+int apply_correction(const float* base, const float* pred, int Cp, int Mx8, int My8, int Wp, float scale, double* out,
+                     cudaStream_t st) {
+  if (!base || !pred || !out || Wp < Mx8) return 1;
+  k_apply_correction<<<grid_for((long long)Mx8 * My8), kBlock, 0, st>>>(base, pred, Cp, Mx8, My8, Wp, scale, out);
+  return status();
+}
+int tile_maxabs(const float* pred, int Cp, int ch, int Mx8, int My8, int Wp, int T, float* tile_max, cudaStream_t st) {
+  if (!pred || !tile_max || T < 1 || Wp < Mx8 || ch < 0 || ch >= Cp) return 1;
+  dim3 grid((Mx8 + T - 1) / T, (My8 + T - 1) / T);
+  k_tile_maxabs<<<grid, kBlock, 0, st>>>(pred, Cp, ch, Mx8, My8, Wp, T, tile_max);
+  return status();
+}
+int merge_tiles(const double* fine, const int* flags, int ntx, int T, int Mx, int My, double* out, cudaStream_t st) {
+  if (!fine || !flags || !out || T < 1) return 1;
+  k_merge_tiles<<<grid_for((long long)Mx * My), kBlock, 0, st>>>(fine, flags, ntx, T, Mx, My, out);
   return status();
 }
 int to_bf16(const float* x, __nv_bfloat16* y, long long n, cudaStream_t st) {

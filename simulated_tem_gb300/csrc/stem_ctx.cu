@@ -187,6 +187,8 @@ struct Job {
   const double* aa;  // host
   int n_prec;
   double* d_img;
+  const unsigned char* tile_mask = nullptr;  // device; see ColumnParams
+  int mask_T = 0;
 };
 
 BinParams bin_params(const Job& j, int64_t cand_base, int64_t cell_base) {
@@ -271,6 +273,9 @@ ColumnParams column_params(st_ctx* c, const Job& j, int64_t cell_base, size_t xo
   cp.aaf = c->s.aaf + aoff;
   cp.img = j.d_img;
   cp.counters = c->s.counters;
+  cp.tile_mask = j.tile_mask;
+  cp.mask_T = j.mask_T;
+  cp.mask_ntx = j.mask_T > 0 ? (g->Mx + j.mask_T - 1) / j.mask_T : 0;
   return cp;
 }
 
@@ -499,9 +504,14 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
     return ce;
   };
   auto clear_images = [&]() -> cudaError_t {
+    // every image is cleared before any column kernel runs, so jobs may share one image
+    // buffer with disjoint windows; a shared buffer is cleared once
     cudaError_t ce = cudaSuccess;
-    for (int i = 0; i < n && ce == cudaSuccess; ++i)
-      ce = cudaMemsetAsync(jobs[i].d_img, 0, sizeof(double) * (size_t)jobs[i].g->Mx * jobs[i].g->My, st);
+    for (int i = 0; i < n && ce == cudaSuccess; ++i) {
+      bool seen = false;
+      for (int k = 0; k < i && !seen; ++k) seen = jobs[k].d_img == jobs[i].d_img;
+      if (!seen) ce = cudaMemsetAsync(jobs[i].d_img, 0, sizeof(double) * (size_t)jobs[i].g->Mx * jobs[i].g->My, st);
+    }
     return ce;
   };
 
@@ -781,6 +791,24 @@ int run_batch(st_ctx* c, const std::vector<Job>& js, int32_t flags, cudaStream_t
 }
 
 }  // namespace
+
+extern "C" int st_image_device_masked(st_ctx* c, const st_geom* g, const double* d_x, int64_t ldx, int64_t nAtoms,
+                                      const double* aa, int32_t nPrec, int32_t flags, double* d_img,
+                                      const unsigned char* d_tile_mask, int32_t mask_T, void* stream) {
+  if (!c) return ST_ERR_ARG;
+  int rc = validate(c, g, ldx, nAtoms, nPrec);
+  if (rc != ST_OK) return rc;
+  if (!aa || !d_img || !d_tile_mask || (nAtoms > 0 && !d_x)) return fail(c, ST_ERR_ARG, "null buffer");
+  if (mask_T < 8 || mask_T % 8 != 0 || g->ix0 % 8 != 0 || g->iy0 % 4 != 0)
+    return fail(c, ST_ERR_ARG, "mask tiles must be a multiple of 8 pixels and the window origin aligned to them");
+  cudaSetDevice(c->device);
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+  Job j{g, d_x, ldx, nAtoms, aa, nPrec, d_img};
+  j.tile_mask = d_tile_mask;
+  j.mask_T = mask_T;
+  std::vector<Job> jobs{j};
+  return run_images(c, jobs, flags, st);
+}
 
 extern "C" int st_batch_device(st_ctx* c, int32_t n_jobs, const st_job* jobs, int32_t flags, void* stream) {
   if (!c) return ST_ERR_ARG;

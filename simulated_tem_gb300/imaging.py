@@ -82,6 +82,14 @@ class Context:
                                           _ptr(aa), len(aa), flags, ctypes.c_void_p(img_dev_ptr),
                                           ctypes.c_void_p(stream)))
 
+    def image_device_masked(self, geom, x_dev_ptr, n_atoms, aa, flags, img_dev_ptr, mask_dev_ptr, mask_T, stream=0,
+                            ldx=3):
+        """st_image_device_masked: only the mask_T x mask_T tiles whose mask byte is nonzero."""
+        aa = np.ascontiguousarray(np.atleast_1d(aa), dtype=np.float64)
+        self._check(lib().st_image_device_masked(self.handle, ctypes.byref(geom), ctypes.c_void_p(x_dev_ptr), ldx,
+                                                 n_atoms, _ptr(aa), len(aa), flags, ctypes.c_void_p(img_dev_ptr),
+                                                 ctypes.c_void_p(mask_dev_ptr), int(mask_T), ctypes.c_void_p(stream)))
+
     @staticmethod
     def _job_array(jobs):
         """(geom, x, n_atoms, aa, img[, ldx]) tuples -> st_job array (+ the arrays it points into)."""
@@ -248,6 +256,14 @@ class DynamicalTwoBeamImaging:
         aa = np.zeros(n_prec)
         check(lib().st_d2bi_image_geometry(self.handle, int(n_atoms), int(nprocs), int(jj), float(prec_angle),
                                            int(n_prec), ctypes.byref(G), _ptr(aa)))
+        return G, aa
+
+    def window_geometry(self, n_atoms, ix0, iy0, dx, dy, prec_angle=0.005, n_prec=1):
+        """(st_geom, aa) of the pixel window [ix0, ix0 + dx) x [iy0, iy0 + dy)."""
+        G = StGeom()
+        aa = np.zeros(n_prec)
+        check(lib().st_d2bi_window_geometry(self.handle, int(n_atoms), int(ix0), int(iy0), int(dx), int(dy),
+                                            float(prec_angle), int(n_prec), ctypes.byref(G), _ptr(aa)))
         return G, aa
 
     def compute_d2bi_img(self, ctx, x, prec_angle=0.005, n_prec=1, flags=0):

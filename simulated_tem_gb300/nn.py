@@ -22,10 +22,17 @@ _PROTOS = {
     "stn_split": (_i32, [_vp, _vp, _vp, _i64, _i32, _i32, _vp]),
     "stn_relu_mask": (_i32, [_vp, _vp, _i64, _vp]),
     "stn_bias_grad": (_i32, [_vp, _vp, _i64, _i32, _vp]),
-    "stn_mse": (_i32, [_vp, _vp, _vp, _vp, _i64, _i32, _vp]),
+    "stn_mse": (_i32, [_vp, _vp, _vp, _vp, _i64, _i32, _f32, _vp]),
     "stn_adam": (_i32, [_vp, _vp, _vp, _vp, _vp, _i64, _f32, _f32, _f32, _f32, _i32, _f32, _vp]),
     "stn_pack": (_i32, [_vp, _i32, _vp, _i64, _i32, _vp]),
     "stn_to_bf16": (_i32, [_vp, _vp, _i64, _vp]),
+    "stn_add": (_i32, [_vp, _vp, _i64, _vp]),
+    "stn_fill_zero": (_i32, [_vp, _i64, _vp]),
+    "stn_image_mean": (_i32, [_vp, _i64, _vp, _vp]),
+    "stn_resample_planes": (_i32, [_vp, _i32, _i32, _i32, _i32, _i32, _i32, _f32, _vp, _f32, _vp, _vp]),
+    "stn_apply_correction": (_i32, [_vp, _vp, _i32, _i32, _i32, _i32, _f32, _vp, _vp]),
+    "stn_tile_maxabs": (_i32, [_vp, _i32, _i32, _i32, _i32, _i32, _i32, _vp, _vp]),
+    "stn_merge_tiles": (_i32, [_vp, _vp, _i32, _i32, _i32, _i32, _vp, _vp]),
     "stn_last_kernel_error": (_i32, []),
 }
 _lib = None
@@ -162,10 +169,12 @@ def bias_grad(g, gb):
     return gb
 
 
-def mse(pred, target, g, loss):
-    """loss (FP32 scalar tensor) += mean (pred[..., 0] - target)^2; g = its gradient (BF16)."""
+def mse(pred, target, g, loss, w1=0.0):
+    """loss (FP32 scalar tensor) += mean (pred[..., 0] - target)^2 + w1 mean (pred[..., 1] -
+    |target|)^2; g = its gradient (BF16)."""
     Cp = pred.shape[-1]
-    _check(lib().stn_mse(_ptr(pred), _ptr(target), _ptr(g), _ptr(loss), pred.numel() // Cp, Cp, _stream()), "stn_mse")
+    _check(lib().stn_mse(_ptr(pred), _ptr(target), _ptr(g), _ptr(loss), pred.numel() // Cp, Cp, float(w1),
+                         _stream()), "stn_mse")
     return loss
 
 
@@ -192,3 +201,47 @@ def to_bf16(x, out=None):
 
 def last_kernel_error():
     return lib().stn_last_kernel_error()
+
+
+def add_(a, b):
+    """a += b (BF16)."""
+    _check(lib().stn_add(_ptr(a), _ptr(b), a.numel(), _stream()), "stn_add")
+    return a
+
+
+def zero_(t):
+    _check(lib().stn_fill_zero(_ptr(t), t.numel() * t.element_size(), _stream()), "stn_fill_zero")
+    return t
+
+
+def image_mean(img, out):
+    _check(lib().stn_image_mean(_ptr(img), img.numel(), _ptr(out), _stream()), "stn_image_mean")
+    return out
+
+
+def resample_planes(img2, Mx2, My2, Mx8, My8, Wp, Hp, sg_value, mean, contrast, planes):
+    """img2: FP64 device image (Mx2 x My2 column-major); mean: FP64 device scalar; planes:
+    FP32 (5, Hp, Wp)."""
+    _check(lib().stn_resample_planes(_ptr(img2), Mx2, My2, Mx8, My8, Wp, Hp, float(sg_value), _ptr(mean),
+                                     float(contrast), _ptr(planes), _stream()), "stn_resample_planes")
+    return planes
+
+
+def apply_correction(base, pred, Mx8, My8, scale, out):
+    Hp, Wp = base.shape[-2:]
+    _check(lib().stn_apply_correction(_ptr(base), _ptr(pred), pred.shape[-1], Mx8, My8, Wp, float(scale), _ptr(out),
+                                      _stream()), "stn_apply_correction")
+    return out
+
+
+def tile_maxabs(pred, Mx8, My8, T, out, ch=0):
+    Wp = pred.shape[-2]
+    _check(lib().stn_tile_maxabs(_ptr(pred), pred.shape[-1], ch, Mx8, My8, Wp, T, _ptr(out), _stream()),
+           "stn_tile_maxabs")
+    return out
+
+
+def merge_tiles(fine, flags, T, Mx, My, out):
+    _check(lib().stn_merge_tiles(_ptr(fine), _ptr(flags), flags.shape[-1], T, Mx, My, _ptr(out), _stream()),
+           "stn_merge_tiles")
+    return out

@@ -109,9 +109,12 @@ def test_elementwise_layers_match_oracle(nn):
     tgt = rng.standard_normal((3, 9, 10)).astype(np.float32)
     loss = torch.zeros(1, dtype=torch.float32, device="cuda")
     gl = torch.empty((3, 9, 10, 16), dtype=torch.bfloat16, device="cuda")
-    nn.mse(torch.from_numpy(pred).cuda(), torch.from_numpy(tgt).cuda(), gl, loss)
+    nn.mse(torch.from_numpy(pred).cuda(), torch.from_numpy(tgt).cuda(), gl, loss, w1=0.5)
     d = pred[..., 0].astype(np.float64) - tgt
-    assert abs(loss.item() - (d ** 2).mean()) <= 1e-5 * (d ** 2).mean()
+    d1 = pred[..., 1].astype(np.float64) - np.abs(tgt)
+    want = (d ** 2).mean() + 0.5 * (d1 ** 2).mean()
+    assert abs(loss.item() - want) <= 1e-5 * want
     glh = gl.float().cpu().numpy()
     assert np.allclose(glh[..., 0], NO.bf16_round((2 * d / d.size).astype(np.float32)), rtol=0, atol=1e-7)
-    assert not glh[..., 1:].any()
+    assert np.allclose(glh[..., 1], NO.bf16_round((0.5 * 2 * d1 / d1.size).astype(np.float32)), rtol=0, atol=1e-7)
+    assert not glh[..., 2:].any()
