@@ -262,6 +262,82 @@ def cfg1_leg(ctx, stream, flush, steps, warmup, cpu=True):
     return out
 
 
+CORRECTOR_WEIGHTS = os.path.join(ROOT, "simulated_tem_gb300", "weights", "corrector_m2_m8.npz")
+
+
+def cfg5_leg(ctx, stream, flush, steps, warmup, weights=CORRECTOR_WEIGHTS):
+    """The learned corrector on the 4.8M-atom cell (200 x 200 x 60 bcc cells, screw
+    dislocation, 20 voids of radius U(5, 15) A), s_g = 0.01: the plain M = 8 FP32 solve against
+    the M = 2 FP32 solve + corrector + fallback (the fine solve on the flagged tiles), both
+    timed with CUDA events; the M = 8 solve judges the corrected image."""
+    import torch
+
+    from simulated_tem_gb300 import _lib, corrector as C, synth
+    if not os.path.exists(weights):
+        return {"unavailable": "no trained corrector weights at %s" % os.path.relpath(weights, ROOT)}
+    model = C.UNet().load(weights)
+    tau = float(model.meta["tau"])
+    cell = synth.make_cell(200, 200, 60, synth.BASE_SEED + 5, n_voids=20, void_radius=(5.0, 15.0), with_screw=True,
+                           name="bcc Fe 200x200x60, screw + 20 voids")
+    sg = 0.01
+    t2, x = C.condition(cell, 2, sg)
+    t8, _ = C.condition(cell, 8, sg)
+    G8, aa8 = t8.image_geometry(len(x))
+    d_x = torch.from_numpy(np.ascontiguousarray(x)).cuda()
+    sp = stream.cuda_stream
+    fine = torch.empty((G8.My, G8.Mx), dtype=torch.float64, device="cuda")
+    imager = C.CorrectedImager(model, ctx, tile=16, tau=tau)
+
+    def fine_step():
+        ctx.image_device(G8, d_x.data_ptr(), len(x), aa8, _lib.ST_FLAG_FP32, fine.data_ptr(), stream=sp)
+
+    res = {}
+
+    def corrected_step():
+        res["img"], res["nflag"], res["ntiles"] = imager.image(t2, t8, d_x, len(x), sg, stream=sp)
+
+    def timed(fn):
+        for _ in range(warmup):
+            fn()
+        ms = []
+        for i in range(steps):
+            flush.fill_(float(i))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return float(np.mean(ms))
+
+    ms_fine = timed(fine_step)
+    ms_corr = timed(corrected_step)
+    ref = fine.cpu().numpy()
+    got = res["img"].cpu().numpy()
+    # the M = 2 image alone, interpolated (the method without the corrector)
+    diag = {}
+    plain, _, _ = C.CorrectedImager(model, ctx, tile=16, tau=np.inf).image(t2, t8, d_x, len(x), sg, fallback=False,
+                                                                          diag=diag)
+    G2, aa2 = t2.image_geometry(len(x))
+    img2 = torch.empty((G2.My, G2.Mx), dtype=torch.float64, device="cuda")
+    ctx.image_device(G2, d_x.data_ptr(), len(x), aa2, _lib.ST_FLAG_FP32, img2.data_ptr(), stream=sp)
+    base = C.coarse_planes(img2, G2, G8, sg)[4, :G8.My, :G8.Mx].cpu().numpy()
+    d_c, d_n, d_u = got - ref, plain.cpu().numpy() - ref, base - ref
+    return {"workload": "bcc Fe 200x200x60 cells (%d atoms), screw + 20 voids, g=[110] s_g=0.01; M=8 image %dx%dx%d"
+                        % (len(x), G8.Mx, G8.My, G8.Mz),
+            "m8_fp32": {"images_per_s": 1000.0 / ms_fine, "ms": ms_fine},
+            "m2_corrector_fallback": {"images_per_s": 1000.0 / ms_corr, "ms": ms_corr,
+                                      "fallback_tiles": res["nflag"], "tiles": res["ntiles"],
+                                      "fallback_fraction": res["nflag"] / res["ntiles"], "tau": tau,
+                                      "max_abs_dI_vs_m8": float(np.abs(d_c).max()),
+                                      "rms_dI_vs_m8": float(np.sqrt((d_c ** 2).mean()))},
+            "m2_corrector_no_fallback": {"max_abs_dI_vs_m8": float(np.abs(d_n).max()),
+                                         "rms_dI_vs_m8": float(np.sqrt((d_n ** 2).mean()))},
+            "m2_interpolated": {"max_abs_dI_vs_m8": float(np.abs(d_u).max()),
+                                "rms_dI_vs_m8": float(np.sqrt((d_u ** 2).mean()))},
+            "speedup": ms_fine / ms_corr}
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -376,6 +452,7 @@ def run_gpu(args):
                                                              args.warmup)
         cfg1 = None if args.no_batched else cfg1_leg(ctx, stream, flush, 5, args.warmup,
                                                       cpu=(rank == 0 and not args.no_cpu))
+        cfg5 = None if args.no_batched else cfg5_leg(ctx, stream, flush, 3, args.warmup)
     step_ms = [a.elapsed_time(b) for a, b in ev]
     ms = float(np.mean(step_ms))
     if ws > 1:
@@ -457,7 +534,7 @@ def run_gpu(args):
             "accuracy": {"max_abs_dI_fp32_vs_fp64": float(np.abs(d).max()),
                          "rms_dI_fp32_vs_fp64": float(np.sqrt((d ** 2).mean()))},
             "gpu_launches": args.steps * launches_per_image(n_prec, fp32=True, average=True),
-            "roofline": roof, "peaks": peaks, "wall_s": wall, "clocks": clk.summary(), "batched": batched, "cfg1_128k": cfg1}
+            "roofline": roof, "peaks": peaks, "wall_s": wall, "clocks": clk.summary(), "batched": batched, "cfg1_128k": cfg1, "cfg5_corrector": cfg5}
     if rank == 0:
         if ws == 1 and not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline(x_state=(cell, t, x), rows=args.cpu_rows)

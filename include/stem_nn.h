@@ -50,12 +50,12 @@ int stn_relu_mask(void* g, const void* y, int64_t n, void* stream);
 /* gb[c] += sum over pixels of g[p][c] (gb FP32). */
 int stn_bias_grad(const void* g, float* gb, int64_t npix, int32_t C, void* stream);
 
-/* *loss += mean over pixels of (pred[p][0] - target[p])^2 + w1 (pred[p][1] - |target[p]|)^2
- * (pred FP32 [npix][Cp], target FP32 [npix]; the second term when w1 > 0): channel 0
- * regresses the target, channel 1 its magnitude.  g (BF16 [npix][Cp], may be null) = the
- * loss gradient, zero in the other channels. */
-int stn_mse(const float* pred, const float* target, void* g, float* loss, int64_t npix, int32_t Cp, float w1,
-            void* stream);
+/* *loss += mean over pixels of (pred[p][0] - target[p])^2 + w1 (pred[p][1] - t1[p])^2 with
+ * t1 = target1[p], or |target[p]| when target1 is null (pred FP32 [npix][Cp], targets FP32
+ * [npix]; the second term when w1 > 0).  g (BF16 [npix][Cp], may be null) = the loss
+ * gradient, zero in the other channels. */
+int stn_mse(const float* pred, const float* target, const float* target1, void* g, float* loss, int64_t npix,
+            int32_t Cp, float w1, void* stream);
 
 /* One Adam step (step >= 1) on FP32 parameters w with moments m, v and gradient g; w16
  * (BF16, may be null) receives the updated parameters.  wd: decoupled weight decay. */
@@ -74,9 +74,10 @@ int stn_fill_zero(void* p, int64_t bytes, void* stream);
 /* *mean = the mean of an FP64 image of n pixels (device scalar). */
 int stn_image_mean(const double* img, int64_t n, double* mean, void* stream);
 
-/* The corrector's planes on the fine grid (Hp x Wp >= My8 x Mx8, extended periodically):
- * with DF the coarse image img2 (FP64 Mx2 x My2, column-major) interpolated bilinearly at
- * the fine pixels' positions (pixel i of an N-pixel axis at i d / N) and mu = *mean,
+/* The corrector's planes on the fine grid (Hp x Wp >= My8 x Mx8, extended by the last row
+ * and column): with DF the coarse image img2 (FP64 Mx2 x My2, column-major) interpolated
+ * bilinearly at the fine pixels' positions (pixel i of an N-pixel axis at i d / N, clamped
+ * at the edges) and mu = *mean,
  * planes (FP32 [5][Hp][Wp]) = (DF - mu) contrast, (mu - DF) contrast, sg_value, mu, DF. */
 int stn_resample_planes(const double* img2, int32_t Mx2, int32_t My2, int32_t Mx8, int32_t My8, int32_t Wp,
                         int32_t Hp, float sg_value, const double* mean, float contrast, float* planes, void* stream);

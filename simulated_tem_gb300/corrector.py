@@ -12,9 +12,9 @@ libstem_nn's kernels (tensor-core convolutions on sm_103a).  torch holds device 
 
 Training pairs are made by the imaging path itself (the same cell and condition solved at
 M = 2 and M = 8).  At inference the plain fine-grid solve is the fallback: a second head channel, trained to
-predict the magnitude of the needed correction, flags tiles that are recomputed at M = 8
-(the columns of those tiles only), and the fine solve is the judge of the corrector's
-error in the tests and the bench.
+predict the largest needed correction within ERR_WINDOW pixels, flags tiles that are
+recomputed at M = 8 (the columns of those tiles only), and the fine solve is the judge of
+the corrector's error in the tests and the bench.
 """
 import numpy as np
 
@@ -23,8 +23,9 @@ from . import nn as N
 CH = (32, 64, 128, 256)
 IN_C = 16    # packed input channels (N_IN used)
 N_IN = 4     # input planes: DF contrast, BF contrast, s_g, mean level
-OUT_C = 16   # head channels: 0 the correction, 1 its expected magnitude (the fallback's guide)
-ERR_WEIGHT = 1.0  # weight of channel 1's loss
+OUT_C = 16   # head channels: 0 the correction, 1 the expected local error (the fallback's guide)
+ERR_WEIGHT = 0.1  # weight of channel 1's loss
+ERR_WINDOW = 33   # channel 1 learns the largest |correction| within this window (pixels)
 SG_SCALE = 50.0    # s_g (1/A) -> input plane value
 CONTRAST = 20.0    # (DF - mean) -> input plane value
 RES_SCALE = 100.0  # the network predicts (fine - interpolated coarse) * RES_SCALE
@@ -277,7 +278,16 @@ def make_pairs(ctx, cell, sgs, crop, per_image, rng, fp32=True):
             pin = planes[:, y0:y0 + crop, x0:x0 + crop]
             ins.append(pin[:N_IN])
             tgs.append((fine[y0:y0 + crop, x0:x0 + crop] - pin[4]) * RES_SCALE)
+    if not ins:
+        return np.zeros((0, N_IN, crop, crop), np.float32), np.zeros((0, crop, crop), np.float32)
     return np.stack(ins).astype(np.float32), np.stack(tgs).astype(np.float32)
+
+
+def local_error(targets, window=ERR_WINDOW):
+    """Channel 1's target: the largest |target| within window x window pixels around each
+    pixel (a bound for the error anywhere in a tile of that size containing it)."""
+    from scipy.ndimage import maximum_filter
+    return np.stack([maximum_filter(np.abs(t), size=window, mode="nearest") for t in targets]).astype(np.float32)
 
 
 class Trainer:
@@ -295,6 +305,7 @@ class Trainer:
         self.x = N.pack(planes, IN_C)  # (n, S, S, 16)
         del planes
         self.y = torch.from_numpy(np.ascontiguousarray(targets)).cuda()
+        self.y1 = torch.from_numpy(local_error(targets)).cuda()
         self.loss = torch.zeros(1, dtype=torch.float32, device="cuda")
         self.g = torch.empty((batch, S, S, OUT_C), dtype=torch.bfloat16, device="cuda")
         self.pos = 0
@@ -305,9 +316,10 @@ class Trainer:
             self.pos = 0
         x = self.x[self.pos:self.pos + b]
         y = self.y[self.pos:self.pos + b]
+        y1 = self.y1[self.pos:self.pos + b]
         self.pos += b
         out = self.model.forward(x, keep=True)
-        N.mse(out, y, self.g, self.loss, ERR_WEIGHT)
+        N.mse(out, y, self.g, self.loss, ERR_WEIGHT, target1=y1)
         self.model.backward(self.g)
         self.model.adam_step(lr)
 
@@ -357,7 +369,7 @@ class CorrectedImager:
     """M = 8 images from the M = 2 solve and the corrector, with the plain fine-grid solve
     as the fallback on T x T tiles whose predicted correction exceeds `tau`."""
 
-    def __init__(self, model, ctx, tile=32, tau=0.05):
+    def __init__(self, model, ctx, tile=16, tau=0.05):
         self.model, self.ctx, self.T, self.tau = model, ctx, tile, tau
 
     def image(self, t2, t8, x_dev, n_atoms, sg, fallback=True, stream=0, diag=None):
@@ -389,6 +401,8 @@ class CorrectedImager:
         if not fallback:
             return img, 0, ntx * nty
         flags = (tm > self.tau * RES_SCALE).astype(np.int32)
+        flags[0, :] = flags[-1, :] = 1  # the image's border: the coarse image is clamped there
+        flags[:, 0] = flags[:, -1] = 1
         nflag = int(flags.sum())
         if nflag:
             mask = torch.from_numpy(flags.astype(np.uint8)).to(dev)
@@ -433,15 +447,16 @@ def build_dataset(ctx, n_pairs, crop, seed, conds_per_cell=10, crops_per_image=5
     return np.concatenate(xs)[:n_pairs], np.concatenate(ys)[:n_pairs]
 
 
-def calibrate(model, ctx, conditions, tile=32, target=1e-2):
+def calibrate(model, ctx, conditions, tile=16, target=1e-2):
     """The fallback threshold: over whole validation images (cell, s_g), the largest tau for
-    which every tile whose corrected error exceeds `target` has a predicted error magnitude
-    above tau (so it falls back).  Returns (tau, report)."""
+    which every interior tile whose corrected error exceeds `target` has a predicted local
+    error above tau (so it falls back; the border ring of tiles always does).  Returns
+    (tau, report)."""
     import torch
 
     from . import _lib
     imager = CorrectedImager(model, ctx, tile=tile, tau=np.inf)
-    bad_pred, all_pred, worst = [], [], 0.0
+    bad_pred, all_pred, worst, n_border = [], [], 0.0, 0
     for cell, sg in conditions:
         t2, x = condition(cell, 2, sg)
         t8, _ = condition(cell, 8, sg)
@@ -452,16 +467,20 @@ def calibrate(model, ctx, conditions, tile=32, target=1e-2):
         err = np.abs(img.cpu().numpy() - fine)
         worst = max(worst, float(err.max()))
         tm = diag["tile_max"]
-        for ty in range(tm.shape[0]):
-            for tx in range(tm.shape[1]):
+        ny, nx = tm.shape
+        n_border += 2 * (nx + ny) - 4
+        for ty in range(1, ny - 1):  # the border ring always falls back
+            for tx in range(1, nx - 1):
                 e = err[ty * tile:(ty + 1) * tile, tx * tile:(tx + 1) * tile].max()
                 all_pred.append(tm[ty, tx])
                 if e > target:
                     bad_pred.append(tm[ty, tx])
     all_pred = np.array(all_pred)
     tau = 0.9 * float(min(bad_pred)) if bad_pred else float(all_pred.max()) * 1.1 + 1e-6
-    frac = float((all_pred > tau).mean())
-    return tau, {"tiles": int(all_pred.size), "tiles_above_target": len(bad_pred), "fallback_fraction": frac,
+    n_tiles = all_pred.size + n_border
+    frac = float(((all_pred > tau).sum() + n_border) / n_tiles)
+    return tau, {"tiles": int(n_tiles), "interior_tiles_above_target": len(bad_pred), "fallback_fraction": frac,
+                 "interior_fallback_fraction": float((all_pred > tau).mean()),
                  "max_error_without_fallback": worst}
 
 

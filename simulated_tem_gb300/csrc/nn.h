@@ -33,8 +33,8 @@ int split(const __nv_bfloat16* gy, __nv_bfloat16* ga, __nv_bfloat16* gb, long lo
           cudaStream_t st);
 int relu_mask(__nv_bfloat16* g, const __nv_bfloat16* y, long long n, cudaStream_t st);
 int bias_grad(const __nv_bfloat16* g, float* gb, long long npix, int C, cudaStream_t st);
-int mse(const float* pred, const float* target, __nv_bfloat16* g, float* loss, long long npix, int Cp, float w1,
-        cudaStream_t st);
+int mse(const float* pred, const float* target, const float* target1, __nv_bfloat16* g, float* loss, long long npix,
+        int Cp, float w1, cudaStream_t st);
 int adam(float* w, float* m, float* v, const float* g, __nv_bfloat16* w16, long long n, float lr, float b1, float b2,
          float eps, int step, float wd, cudaStream_t st);
 int pack(const float* planes, int nplanes, __nv_bfloat16* y, long long npix, int C, cudaStream_t st);

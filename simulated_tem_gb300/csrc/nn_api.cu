@@ -50,9 +50,9 @@ extern "C" int stn_relu_mask(void* g, const void* y, int64_t n, void* stream) {
 extern "C" int stn_bias_grad(const void* g, float* gb, int64_t npix, int32_t C, void* stream) {
   return bias_grad(cb(g), gb, npix, C, cs(stream));
 }
-extern "C" int stn_mse(const float* pred, const float* target, void* g, float* loss, int64_t npix, int32_t Cp,
-                       float w1, void* stream) {
-  return mse(pred, target, mb(g), loss, npix, Cp, w1, cs(stream));
+extern "C" int stn_mse(const float* pred, const float* target, const float* target1, void* g, float* loss,
+                       int64_t npix, int32_t Cp, float w1, void* stream) {
+  return mse(pred, target, target1, mb(g), loss, npix, Cp, w1, cs(stream));
 }
 extern "C" int stn_adam(float* w, float* m, float* v, const float* g, void* w16, int64_t n, float lr, float beta1,
                         float beta2, float eps, int32_t step, float wd, void* stream) {

@@ -141,12 +141,13 @@ __global__ void k_bias_grad(const __nv_bfloat16* __restrict__ g, float* __restri
   for (int c = threadIdx.x; c < C; c += blockDim.x) atomicAdd(&gb[c], part[c]);
 }
 
-// loss = mean_p (pred[p, 0] - target[p])^2 + w1 mean_p (pred[p, 1] - |target[p]|)^2 over
-// npix pixels (pred FP32 [npix][Cp]): channel 0 regresses the target, channel 1 (when
-// w1 > 0) its magnitude; g (BF16 [npix][Cp]) = the loss gradient, 0 in the other channels.
-// The loss is added to *loss.
-__global__ void k_mse(const float* __restrict__ pred, const float* __restrict__ target, __nv_bfloat16* __restrict__ g,
-                      float* __restrict__ loss, long long npix, int Cp, float w1) {
+// loss = mean_p (pred[p, 0] - target[p])^2 + w1 mean_p (pred[p, 1] - t1[p])^2 over npix
+// pixels (pred FP32 [npix][Cp]), t1 = target1[p] or, without target1, |target[p]|: channel
+// 0 regresses the target, channel 1 (when w1 > 0) a magnitude; g (BF16 [npix][Cp]) = the
+// loss gradient, 0 in the other channels.  The loss is added to *loss.
+__global__ void k_mse(const float* __restrict__ pred, const float* __restrict__ target,
+                      const float* __restrict__ target1, __nv_bfloat16* __restrict__ g, float* __restrict__ loss,
+                      long long npix, int Cp, float w1) {
   __shared__ float red[kBlock / 32];
   float s = 0.f;
   const float scale = 2.f / (float)npix;
@@ -154,7 +155,7 @@ __global__ void k_mse(const float* __restrict__ pred, const float* __restrict__ 
        p += (long long)gridDim.x * blockDim.x) {
     const float t = target[p];
     const float d = pred[p * Cp] - t;
-    const float d1 = w1 > 0.f ? pred[p * Cp + 1] - fabsf(t) : 0.f;
+    const float d1 = w1 > 0.f ? pred[p * Cp + 1] - (target1 ? target1[p] : fabsf(t)) : 0.f;
     s += d * d + w1 * d1 * d1;
     if (g) {
       g[p * Cp] = tobf(scale * d);
@@ -226,10 +227,11 @@ __global__ void k_image_mean(const double* __restrict__ img, long long n, double
   }
 }
 
-// The corrector's planes on the fine (M = 8) pixel grid, Hp x Wp (the image My8 x Mx8
-// extended periodically).  DF is the coarse (M = 2) image interpolated bilinearly at the
-// fine pixels' positions (pixel i of an N-pixel axis sits at i d / N on both grids; the
-// supercell is periodic); mu is the coarse image's mean.  Planes (FP32 [5][Hp][Wp]):
+// The corrector's planes on the fine (M = 8) pixel grid, Hp x Wp (the image My8 x Mx8,
+// extended by its last row and column).  DF is the coarse (M = 2) image interpolated
+// bilinearly at the fine pixels' positions (pixel i of an N-pixel axis sits at i d / N on
+// both grids), clamped at the image's edges: the tilted crystal makes the image
+// non-periodic.  mu is the coarse image's mean.  Planes (FP32 [5][Hp][Wp]):
 // 0: (DF - mu) * contrast, 1: (BF - (1 - mu)) * contrast with BF = 1 - DF, 2: sg_value,
 // 3: mu, 4: DF (the base the correction is added to).  Planes 0-3 are the network's input:
 // the contrast, a few 1e-3 on a level near 0.1-0.7, would not survive BF16 unshifted.
@@ -241,13 +243,11 @@ __global__ void k_resample_planes(const double* __restrict__ img2, int Mx2, int 
   const double sx = (double)Mx2 / Mx8, sy = (double)My2 / My8;
   const double mu = *mean;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const int px = (int)(i % Wp) % Mx8, py = (int)(i / Wp) % My8;
+    const int px = min((int)(i % Wp), Mx8 - 1), py = min((int)(i / Wp), My8 - 1);
     const double u = px * sx, v = py * sy;
-    int i0 = (int)floor(u), j0 = (int)floor(v);
+    int i0 = min((int)floor(u), Mx2 - 1), j0 = min((int)floor(v), My2 - 1);
     const double fu = u - i0, fv = v - j0;
-    i0 %= Mx2;
-    j0 %= My2;
-    const int i1 = (i0 + 1) % Mx2, j1 = (j0 + 1) % My2;
+    const int i1 = min(i0 + 1, Mx2 - 1), j1 = min(j0 + 1, My2 - 1);
     const double a = img2[i0 + (long long)Mx2 * j0], b = img2[i1 + (long long)Mx2 * j0];
     const double c = img2[i0 + (long long)Mx2 * j1], d = img2[i1 + (long long)Mx2 * j1];
     const double df = (1.0 - fv) * ((1.0 - fu) * a + fu * b) + fv * ((1.0 - fu) * c + fu * d);
@@ -349,10 +349,10 @@ int bias_grad(const __nv_bfloat16* g, float* gb, long long npix, int C, cudaStre
   k_bias_grad<<<grid, kBlock, C * sizeof(float), st>>>(g, gb, npix, C);
   return status();
 }
-int mse(const float* pred, const float* target, __nv_bfloat16* g, float* loss, long long npix, int Cp, float w1,
-        cudaStream_t st) {
+int mse(const float* pred, const float* target, const float* target1, __nv_bfloat16* g, float* loss, long long npix,
+        int Cp, float w1, cudaStream_t st) {
   if (!pred || !target || !loss || Cp < 1 || (w1 > 0.f && Cp < 2)) return 1;
-  k_mse<<<grid_for(npix / 4), kBlock, 0, st>>>(pred, target, g, loss, npix, Cp, w1);
+  k_mse<<<grid_for(npix / 4), kBlock, 0, st>>>(pred, target, target1, g, loss, npix, Cp, w1);
   return status();
 }
 int adam(float* w, float* m, float* v, const float* g, __nv_bfloat16* w16, long long n, float lr, float b1, float b2,

@@ -22,7 +22,7 @@ _PROTOS = {
     "stn_split": (_i32, [_vp, _vp, _vp, _i64, _i32, _i32, _vp]),
     "stn_relu_mask": (_i32, [_vp, _vp, _i64, _vp]),
     "stn_bias_grad": (_i32, [_vp, _vp, _i64, _i32, _vp]),
-    "stn_mse": (_i32, [_vp, _vp, _vp, _vp, _i64, _i32, _f32, _vp]),
+    "stn_mse": (_i32, [_vp, _vp, _vp, _vp, _vp, _i64, _i32, _f32, _vp]),
     "stn_adam": (_i32, [_vp, _vp, _vp, _vp, _vp, _i64, _f32, _f32, _f32, _f32, _i32, _f32, _vp]),
     "stn_pack": (_i32, [_vp, _i32, _vp, _i64, _i32, _vp]),
     "stn_to_bf16": (_i32, [_vp, _vp, _i64, _vp]),
@@ -169,12 +169,12 @@ def bias_grad(g, gb):
     return gb
 
 
-def mse(pred, target, g, loss, w1=0.0):
+def mse(pred, target, g, loss, w1=0.0, target1=None):
     """loss (FP32 scalar tensor) += mean (pred[..., 0] - target)^2 + w1 mean (pred[..., 1] -
-    |target|)^2; g = its gradient (BF16)."""
+    t1)^2 with t1 = target1 or |target|; g = its gradient (BF16)."""
     Cp = pred.shape[-1]
-    _check(lib().stn_mse(_ptr(pred), _ptr(target), _ptr(g), _ptr(loss), pred.numel() // Cp, Cp, float(w1),
-                         _stream()), "stn_mse")
+    _check(lib().stn_mse(_ptr(pred), _ptr(target), _ptr(target1), _ptr(g), _ptr(loss), pred.numel() // Cp, Cp,
+                         float(w1), _stream()), "stn_mse")
     return loss
 
 
