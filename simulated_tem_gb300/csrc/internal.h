@@ -135,10 +135,11 @@ struct ColumnJob {
 };
 int column_tiles(const ColumnParams& p);
 // `variant` selects the register budget (occupancy) of the launch, 0 .. ring_variant_count() - 1;
-// every variant computes the same image to the last bit.
+// `big_slabs` stages up to 256 atoms per slab instead of 128 (dense footprints).  Every
+// variant computes the same image to the last bit.
 cudaError_t launch_column_fp32_ring(const ColumnJob* d_jobs, int n_jobs, int total_tiles, int max_np, bool density,
-                                    bool stats, int variant, unsigned* work, const unsigned long long* counters,
-                                    int64_t cap, cudaStream_t st);
+                                    bool stats, int variant, bool big_slabs, unsigned* work,
+                                    const unsigned long long* counters, int64_t cap, cudaStream_t st);
 int ring_variant_count();
 int ring_np_bucket(int max_np);  // the kernel template (angles per pass) serving max_np angles
 cudaError_t launch_column_fp64(const ColumnParams& p, cudaStream_t st);

@@ -25,9 +25,11 @@
 //   table of FP32 values that the host computes in FP64.
 //
 // It needs every link cell to be at least 3 sigma wide (then "within 3 sigma"
-// equals the reference's 27-cell search) and at most kCaps staged atoms per
-// slab; otherwise it raises counters[4] and the host recomputes the image with
-// k_column_fp32, which handles both cases.
+// equals the reference's 27-cell search) and at most CAPS staged atoms per
+// slab (128, or 256 for dense footprints such as coarse voxel grids); otherwise
+// it raises counters[4] and the host retries with the larger capacity, then with
+// k_column_fp32, which handles both cases.  The capacity does not change which
+// candidates are tested or their order: every instance computes the same image.
 #include <cuda_runtime.h>
 
 #include <cfloat>
@@ -39,15 +41,15 @@ namespace {
 
 constexpr int kWarps = 4;
 constexpr int kTileX = 8, kTileY = 4;
-constexpr int kCaps = 128;  // staged atoms per slab
 constexpr int kRing = 4;    // resident slabs (unwrapped z cells u, slot u & 3)
 constexpr float kHuge1 = FLT_MAX;
 
 constexpr int kBins = 32;  // z bins per slab for the window lookup
 
+template <int CAPS>  // staged atoms per slab
 struct WarpSmem {
-  float4 p[kRing][kCaps];     // X', Y' (warp frame), z (own cell), cos -- lengths scaled by s
-  float s[kRing][kCaps];      // sin
+  float4 p[kRing][CAPS];      // X', Y' (warp frame), z (own cell), cos -- lengths scaled by s
+  float s[kRing][CAPS];       // sin
   int bin[kRing][kBins + 1];  // bin[b]: first atom of z bin b (width a33 s / kBins); bin[kBins] = count
   int count[kRing];
 };
@@ -75,8 +77,9 @@ struct Geo {
 
 // Gather slab u (its cells in the patch footprint, atoms within 3 sigma of the
 // patch rectangle) into its ring slot and order it by z bin in place; false
-// when it holds more than kCaps atoms.
-__device__ bool load_slab(const ColumnParams& p, const Geo& G, int u, WarpSmem& W, int lane) {
+// when it holds more than CAPS atoms.
+template <int CAPS>
+__device__ bool load_slab(const ColumnParams& p, const Geo& G, int u, WarpSmem<CAPS>& W, int lane) {
   const int cz = pos_mod(u, p.Ez);
   const int slot = u & (kRing - 1);
   float4* P = W.p[slot];
@@ -112,7 +115,7 @@ __device__ bool load_slab(const ColumnParams& p, const Geo& G, int u, WarpSmem& 
         }
         const unsigned m = __ballot_sync(0xffffffffu, keep);
         const int cnt = __popc(m);
-        if (n + cnt > kCaps) return false;
+        if (n + cnt > CAPS) return false;
         if (keep) {
           const int d = n + __popc(m & ((1u << lane) - 1));
           P[d] = rec;
@@ -126,7 +129,7 @@ __device__ bool load_slab(const ColumnParams& p, const Geo& G, int u, WarpSmem& 
   __syncwarp();
   // counting sort by z bin, in place: every lane first holds its atoms in registers;
   // within a bin the gather order is kept (deterministic)
-  constexpr int kPer = kCaps / 32;
+  constexpr int kPer = CAPS / 32;
   const float inv_bin = kBins / G.a33s;
   int* hist = W.bin[slot];
   for (int b = lane; b <= kBins; b += 32) hist[b] = 0;
@@ -241,8 +244,8 @@ __device__ __forceinline__ Sample make_sample(float sr, float si, float r2min, f
 
 // One warp tile of one image: the 8 x 4 columns of tile `tile` marched through
 // the depth.  Returns false when a slab overflows its staging (counters[4]).
-template <int NP, bool kDensity, bool kStats>
-__device__ __noinline__ bool column_tile(const ColumnParams& p, WarpSmem& W, int tile, int lane) {
+template <int NP, bool kDensity, bool kStats, int CAPS>
+__device__ __noinline__ bool column_tile(const ColumnParams& p, WarpSmem<CAPS>& W, int tile, int lane) {
   const int Wd = p.ix1 - p.ix0;
   const int tiles_x = (Wd + kTileX - 1) / kTileX;
   const int tx = tile % tiles_x, ty = tile / tiles_x;
@@ -330,7 +333,7 @@ __device__ __noinline__ bool column_tile(const ColumnParams& p, WarpSmem& W, int
     bool ok = true;
     while (ring_hi < need_hi && ok) {
       ++ring_hi;
-      ok = load_slab(p, G, ring_hi, W, lane);
+      ok = load_slab<CAPS>(p, G, ring_hi, W, lane);
     }
     if (!ok) {
       if (lane == 0) atomicExch(&p.counters[4], 1ull);
@@ -440,13 +443,13 @@ __device__ __noinline__ bool column_tile(const ColumnParams& p, WarpSmem& W, int
 // Persistent launch over the warp tiles of every job of a batch: each warp
 // takes the next tile from a global counter, so images of uneven size share
 // the GPU without a tail per image.
-template <int NP, bool kDensity, bool kStats, int kMinBlocks>
+template <int NP, bool kDensity, bool kStats, int kMinBlocks, int CAPS>
 __global__ void __launch_bounds__(kWarps * 32, kMinBlocks)
     k_column_fp32_v2(const ColumnJob* __restrict__ jobs, int n_jobs, int total_tiles, unsigned* __restrict__ work,
                      const unsigned long long* __restrict__ counters, int64_t cap) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  WarpSmem& W = reinterpret_cast<WarpSmem*>(smem_raw)[warp];
+  WarpSmem<CAPS>& W = reinterpret_cast<WarpSmem<CAPS>*>(smem_raw)[warp];
   if ((int64_t)counters[0] > cap) return;  // the binning overflowed: the host retries
   for (;;) {
     int tile = 0;
@@ -462,14 +465,14 @@ __global__ void __launch_bounds__(kWarps * 32, kMinBlocks)
       else
         hi = mid - 1;
     }
-    if (!column_tile<NP, kDensity, kStats>(jobs[lo].p, W, tile - jobs[lo].tile_base, lane)) break;
+    if (!column_tile<NP, kDensity, kStats, CAPS>(jobs[lo].p, W, tile - jobs[lo].tile_base, lane)) break;
   }
 }
 
-template <typename K>
+template <int CAPS, typename K>
 cudaError_t launch(K kernel, const ColumnJob* jobs, int n_jobs, int total_tiles, unsigned* work,
                    const unsigned long long* counters, int64_t cap, int blocks_per_sm, cudaStream_t st) {
-  const size_t smem = sizeof(WarpSmem) * kWarps;
+  const size_t smem = sizeof(WarpSmem<CAPS>) * kWarps;
   cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   int dev = 0, sms = 148;
@@ -490,25 +493,29 @@ constexpr int kVariants = 2;
 inline int base_blocks(int np) { return np <= 8 ? 5 : 4; }
 
 template <int NP, bool kDensity, bool kStats>
-cudaError_t launch_v(int v, const ColumnJob* jobs, int n_jobs, int total_tiles, unsigned* work,
+cudaError_t launch_v(int v, bool big, const ColumnJob* jobs, int n_jobs, int total_tiles, unsigned* work,
                      const unsigned long long* counters, int64_t cap, cudaStream_t st) {
   constexpr int B = NP <= 8 ? 5 : 4;
+  if (big)  // 256-atom slabs: 84 KB of shared memory per CTA, two CTAs per SM
+    return launch<256>(k_column_fp32_v2<NP, kDensity, kStats, 2, 256>, jobs, n_jobs, total_tiles, work, counters,
+                       cap, 2, st);
   if constexpr (!kStats) {
     if (v == 1)
-      return launch(k_column_fp32_v2<NP, kDensity, kStats, B - 1>, jobs, n_jobs, total_tiles, work, counters, cap,
-                    B - 1, st);
+      return launch<128>(k_column_fp32_v2<NP, kDensity, kStats, B - 1, 128>, jobs, n_jobs, total_tiles, work, counters,
+                         cap, B - 1, st);
   }
-  return launch(k_column_fp32_v2<NP, kDensity, kStats, B>, jobs, n_jobs, total_tiles, work, counters, cap, B, st);
+  return launch<128>(k_column_fp32_v2<NP, kDensity, kStats, B, 128>, jobs, n_jobs, total_tiles, work, counters, cap, B,
+                     st);
 }
 
 template <bool kDensity, bool kStats>
-cudaError_t launch_np(int np, int v, const ColumnJob* jobs, int n_jobs, int total_tiles, unsigned* work,
+cudaError_t launch_np(int np, int v, bool big, const ColumnJob* jobs, int n_jobs, int total_tiles, unsigned* work,
                       const unsigned long long* counters, int64_t cap, cudaStream_t st) {
-  if (np <= 1) return launch_v<1, kDensity, kStats>(v, jobs, n_jobs, total_tiles, work, counters, cap, st);
-  if (np <= 2) return launch_v<2, kDensity, kStats>(v, jobs, n_jobs, total_tiles, work, counters, cap, st);
-  if (np <= 4) return launch_v<4, kDensity, kStats>(v, jobs, n_jobs, total_tiles, work, counters, cap, st);
-  if (np <= 8) return launch_v<8, kDensity, kStats>(v, jobs, n_jobs, total_tiles, work, counters, cap, st);
-  return launch_v<16, kDensity, kStats>(v, jobs, n_jobs, total_tiles, work, counters, cap, st);
+  if (np <= 1) return launch_v<1, kDensity, kStats>(v, big, jobs, n_jobs, total_tiles, work, counters, cap, st);
+  if (np <= 2) return launch_v<2, kDensity, kStats>(v, big, jobs, n_jobs, total_tiles, work, counters, cap, st);
+  if (np <= 4) return launch_v<4, kDensity, kStats>(v, big, jobs, n_jobs, total_tiles, work, counters, cap, st);
+  if (np <= 8) return launch_v<8, kDensity, kStats>(v, big, jobs, n_jobs, total_tiles, work, counters, cap, st);
+  return launch_v<16, kDensity, kStats>(v, big, jobs, n_jobs, total_tiles, work, counters, cap, st);
 }
 
 }  // namespace
@@ -524,16 +531,17 @@ int ring_variant_count() { return kVariants; }
 int ring_np_bucket(int max_np) { return max_np <= 1 ? 1 : max_np <= 2 ? 2 : max_np <= 4 ? 4 : max_np <= 8 ? 8 : 16; }
 
 cudaError_t launch_column_fp32_ring(const ColumnJob* d_jobs, int n_jobs, int total_tiles, int max_np, bool density,
-                                    bool stats, int variant, unsigned* work, const unsigned long long* counters,
-                                    int64_t cap, cudaStream_t st) {
+                                    bool stats, int variant, bool big_slabs, unsigned* work,
+                                    const unsigned long long* counters, int64_t cap, cudaStream_t st) {
   cudaMemsetAsync(work, 0, sizeof(unsigned), st);
   if (total_tiles <= 0) return cudaSuccess;
   const int v = (variant > 0 && variant < kVariants && !stats) ? variant : 0;  // statistics: variant 0
+  const bool b = big_slabs;
   if (density)
-    return stats ? launch_np<true, true>(max_np, v, d_jobs, n_jobs, total_tiles, work, counters, cap, st)
-                 : launch_np<true, false>(max_np, v, d_jobs, n_jobs, total_tiles, work, counters, cap, st);
-  return stats ? launch_np<false, true>(max_np, v, d_jobs, n_jobs, total_tiles, work, counters, cap, st)
-               : launch_np<false, false>(max_np, v, d_jobs, n_jobs, total_tiles, work, counters, cap, st);
+    return stats ? launch_np<true, true>(max_np, v, b, d_jobs, n_jobs, total_tiles, work, counters, cap, st)
+                 : launch_np<true, false>(max_np, v, b, d_jobs, n_jobs, total_tiles, work, counters, cap, st);
+  return stats ? launch_np<false, true>(max_np, v, b, d_jobs, n_jobs, total_tiles, work, counters, cap, st)
+               : launch_np<false, false>(max_np, v, b, d_jobs, n_jobs, total_tiles, work, counters, cap, st);
 }
 
 }  // namespace stem

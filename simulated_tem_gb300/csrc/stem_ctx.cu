@@ -57,6 +57,7 @@ struct st_ctx {
   int last_column_kernel = 0;  // 1 general FP32, 2 slab-ring FP32, 3 FP64
   int tune_mode = ST_TUNE_AUTO;
   std::map<int, int> ring_tuned;  // (angles per pass, density) -> fastest slab-ring variant
+  std::map<int, int> ring_big;    // kinds whose slabs needed 256-atom staging in this context
   cudaEvent_t tev[3] = {nullptr, nullptr, nullptr};
   int last_ring_variant = -1;
 };
@@ -518,21 +519,30 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
   // Everything a call enqueues after the tables: binning, clearing, column kernels,
   // epilogues and the read-back of the counters.  `capturing`: no events, no tuning
   // (the variants and the kernel choice of the eager run are replayed).
-  bool ring_ok = ring;  // false once a slab overflowed: every image takes the general kernel
+  bool ring_ok = ring;  // false once a slab overflowed even 256-atom staging: the general kernel
   const bool stats = (flags & ST_FLAG_STATS) != 0;
   std::vector<int> pass_variant(passes, 0);
-  auto enqueue = [&](bool capturing) -> cudaError_t {
+  // big slabs when an earlier call of this context needed them for one of this call's kinds
+  bool big = false;
+  for (int pass = 0; pass < passes; ++pass) {
+    const int key = ring_np_bucket(std::min(width, ring_np - pass * width)) * 2 + (dens ? 1 : 0);
+    big = big || c->ring_big.count(key) > 0;
+  }
+  // with_bin false: the column phase only, on the binning already in place
+  auto enqueue = [&](bool capturing, bool with_bin) -> cudaError_t {
     cudaError_t ce = cudaSuccess;
     if (!capturing) cudaEventRecord(c->ev[0], st);
-    ce = launch_bin(c->d_binjobs, n, total_cand, total_cells, cap, c->s, c->b, !fp32, st);
-    if (ce == cudaSuccess) ce = launch_bin_finalize(c->d_binjobs, n, total_cells, cap, c->s, c->b, fp32 ? 0 : 1, st);
+    if (with_bin) {
+      ce = launch_bin(c->d_binjobs, n, total_cand, total_cells, cap, c->s, c->b, !fp32, st);
+      if (ce == cudaSuccess) ce = launch_bin_finalize(c->d_binjobs, n, total_cells, cap, c->s, c->b, fp32 ? 0 : 1, st);
+    }
     if (ce == cudaSuccess) ce = clear_images();
     if (!capturing) cudaEventRecord(c->ev[1], st);
     for (int pass = 0; ring_ok && pass < passes && ce == cudaSuccess; ++pass) {
       const int np_pass = std::min(width, ring_np - pass * width);
       auto ring_launch = [&](int v) {
         return launch_column_fp32_ring(c->d_coljobs + (size_t)pass * n_ring, n_ring, pass_tiles[pass], np_pass,
-                                       dens, stats, v, c->d_work, c->s.counters, cap, st);
+                                       dens, stats, v, big, c->d_work, c->s.counters, cap, st);
       };
       if (capturing) {
         ce = ring_launch(pass_variant[pass]);
@@ -546,7 +556,7 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
         auto it = c->ring_tuned.find(key);
         if (it != c->ring_tuned.end()) {
           v = it->second;
-        } else if (pass == 0 && pass_tiles[0] >= 4096) {
+        } else if (pass == 0 && pass_tiles[0] >= 4096 && !big) {
           // autotune on the real work: the first pass overwrites its images, so every trial
           // leaves the same result; keep the fastest for the later calls of this context
           ce = tune_ring(c, ring_launch, cap, st, v);
@@ -582,13 +592,24 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
         if (e != cudaSuccess) return cuda_fail(c, e, "copying column jobs");
       }
     }
-    e = enqueue(false);
+    e = enqueue(false, true);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_fail(c, e, "image kernels");
     if ((int64_t)c->h_counters[0] > cap) {
       if (attempt > 0) return fail(c, ST_ERR_ALLOC, "binning capacity did not converge");
       cap = (int64_t)c->h_counters[0] + (int64_t)c->h_counters[0] / 8 + 1024;  // grow and redo
       continue;
+    }
+    if (ring_ok && c->h_counters[4] != 0 && !big) {
+      // a slab held more than 128 atoms: the column phase again with 256-atom slabs, and this
+      // context keeps them for these kinds of pass
+      big = true;
+      for (int pass = 0; pass < passes; ++pass)
+        c->ring_big[ring_np_bucket(std::min(width, ring_np - pass * width)) * 2 + (dens ? 1 : 0)] = 1;
+      cudaMemsetAsync(c->s.counters + 2, 0, 3 * sizeof(unsigned long long), st);
+      e = enqueue(false, false);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+      if (e != cudaSuccess) return cuda_fail(c, e, "image kernels (256-atom slabs)");
     }
     if (ring_ok && c->h_counters[4] != 0) {
       // a slab held more atoms than the ring kernel stages: recompute every image with the general kernel
@@ -614,7 +635,7 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
     cudaGraph_t graph = nullptr;
     e = cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed);
     if (e == cudaSuccess) {
-      const cudaError_t ce = enqueue(true);
+      const cudaError_t ce = enqueue(true, true);
       e = cudaStreamEndCapture(st, &graph);
       if (ce != cudaSuccess) e = ce;
     }

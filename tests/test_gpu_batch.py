@@ -310,8 +310,9 @@ def test_plan_follows_moving_atoms(ctx):
 
 
 def test_plan_recovers_from_slab_overflow(ctx):
-    """A replay whose atoms overfill the ring kernel's slabs is recomputed on the eager
-    path (general kernel) by st_plan_wait, then recorded again."""
+    """A replay whose atoms overfill the ring kernel's slabs (even 256-atom ones: a ball at
+    eight times the density) is recomputed on the eager path (general kernel) by
+    st_plan_wait, then recorded again."""
     cell = synth.small_cell(n=(9, 11, 7), seed=6, n_voids=3, radius=(3.0, 5.0), with_screw=False)
     t, so, x = _condition(cell, sg=0.01)
     G, aa = t.image_geometry(len(x))
@@ -322,8 +323,10 @@ def test_plan_recovers_from_slab_overflow(ctx):
     plan = ctx.plan(jobs, flags)
     try:
         assert plan.stats().column_kernel == 2
-        q = len(x) // 4
-        dense = np.concatenate([x[:q]] * 4 + [x[:len(x) - 4 * q]])  # same atom count, 4x local density
+        # same atom count: the eighth of the atoms nearest the cell centre, eight times over
+        q = len(x) // 8
+        near = np.argsort(((x - x.mean(axis=0)) ** 2).sum(axis=1))[:q]
+        dense = np.concatenate([x[near]] * 8 + [x[:len(x) - 8 * q]])
         d_x.copy_(torch.from_numpy(dense))
         torch.cuda.synchronize()
         plan.launch()

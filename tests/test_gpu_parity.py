@@ -228,13 +228,37 @@ def test_fp32_ring_and_general_kernels_agree(ctx, density):
 
 
 def test_fp32_ring_overflow_falls_back(ctx):
-    """Four copies of every atom overfill the ring kernel's slab buffers: the image
-    is recomputed by the general kernel and still matches the oracle."""
+    """Sixteen copies of every atom overfill even 256-atom slabs: the image is recomputed by
+    the general kernel and still matches the oracle."""
     cell = synth.small_cell(**CELLS["voids"])
-    dense = synth.Cell(cell.a_super, np.concatenate([cell.pos] * 4))
+    dense = synth.Cell(cell.a_super, np.concatenate([cell.pos] * 16))
     t, so, x = setup_both(dense, sg=0.01)
     G, aa = t.image_geometry(len(x))
-    got = ctx.image(G, x, aa, flags=_lib.ST_FLAG_FP32)
-    assert ctx.stats().column_kernel == 1
+    c = imaging.Context(0)
+    try:
+        got = c.image(G, x, aa, flags=_lib.ST_FLAG_FP32)
+        assert c.stats().column_kernel == 1
+    finally:
+        c.close()
+    want, _ = oracle_patch(so, x, 1, 0.005)
+    assert np.abs(got - want).max() <= FP32_TOL
+
+
+def test_fp32_ring_big_slabs(ctx):
+    """Three copies of every atom overfill 128-atom slabs: the ring kernel reruns with
+    256-atom slabs, and the context keeps them for the next image of that kind."""
+    cell = synth.small_cell(**CELLS["voids"])
+    dense = synth.Cell(cell.a_super, np.concatenate([cell.pos] * 3))
+    t, so, x = setup_both(dense, sg=0.01)
+    G, aa = t.image_geometry(len(x))
+    c = imaging.Context(0)
+    try:
+        got = c.image(G, x, aa, flags=_lib.ST_FLAG_FP32)
+        assert c.stats().column_kernel == 2
+        again = c.image(G, x, aa, flags=_lib.ST_FLAG_FP32)
+        assert c.stats().column_kernel == 2
+        assert np.array_equal(again, got)
+    finally:
+        c.close()
     want, _ = oracle_patch(so, x, 1, 0.005)
     assert np.abs(got - want).max() <= FP32_TOL
