@@ -136,9 +136,10 @@ struct ColumnJob {
 int column_tiles(const ColumnParams& p);
 // `variant` selects the register budget (occupancy) of the launch, 0 .. ring_variant_count() - 1;
 // `big_slabs` stages up to 256 atoms per slab instead of 128 (dense footprints).  Every
-// variant computes the same image to the last bit.
+// variant computes the same image to the last bit.  `masked`: some jobs carry a tile mask
+// (then max_np must be 1 and stats false).
 cudaError_t launch_column_fp32_ring(const ColumnJob* d_jobs, int n_jobs, int total_tiles, int max_np, bool density,
-                                    bool stats, int variant, bool big_slabs, unsigned* work,
+                                    bool stats, int variant, bool big_slabs, bool masked, unsigned* work,
                                     const unsigned long long* counters, int64_t cap, cudaStream_t st);
 int ring_variant_count();
 int ring_np_bucket(int max_np);  // the kernel template (angles per pass) serving max_np angles

@@ -249,7 +249,6 @@ __device__ __noinline__ bool column_tile(const ColumnParams& p, WarpSmem<CAPS>& 
   const int Wd = p.ix1 - p.ix0;
   const int tiles_x = (Wd + kTileX - 1) / kTileX;
   const int tx = tile % tiles_x, ty = tile / tiles_x;
-  if (!tile_wanted(p, tx, ty, kTileX, kTileY)) return true;
   const int ix = p.ix0 + tx * kTileX + (lane & (kTileX - 1));
   const int iy = p.iy0 + ty * kTileY + lane / kTileX;
   const bool active = ix < p.ix1 && iy < p.iy1;
@@ -443,7 +442,9 @@ __device__ __noinline__ bool column_tile(const ColumnParams& p, WarpSmem<CAPS>& 
 // Persistent launch over the warp tiles of every job of a batch: each warp
 // takes the next tile from a global counter, so images of uneven size share
 // the GPU without a tail per image.
-template <int NP, bool kDensity, bool kStats, int kMinBlocks, int CAPS>
+// kMasked: jobs may carry a tile mask (warp tiles outside it are skipped here, before the
+// march, so that the unmasked instances carry no code for it).
+template <int NP, bool kDensity, bool kStats, int kMinBlocks, int CAPS, bool kMasked = false>
 __global__ void __launch_bounds__(kWarps * 32, kMinBlocks)
     k_column_fp32_v2(const ColumnJob* __restrict__ jobs, int n_jobs, int total_tiles, unsigned* __restrict__ work,
                      const unsigned long long* __restrict__ counters, int64_t cap) {
@@ -464,6 +465,12 @@ __global__ void __launch_bounds__(kWarps * 32, kMinBlocks)
         lo = mid;
       else
         hi = mid - 1;
+    }
+    if constexpr (kMasked) {
+      const ColumnParams& P = jobs[lo].p;
+      const int local = tile - jobs[lo].tile_base;
+      const int tiles_x = (P.ix1 - P.ix0 + kTileX - 1) / kTileX;
+      if (!tile_wanted(P, local % tiles_x, local / tiles_x, kTileX, kTileY)) continue;
     }
     if (!column_tile<NP, kDensity, kStats, CAPS>(jobs[lo].p, W, tile - jobs[lo].tile_base, lane)) break;
   }
@@ -531,10 +538,22 @@ int ring_variant_count() { return kVariants; }
 int ring_np_bucket(int max_np) { return max_np <= 1 ? 1 : max_np <= 2 ? 2 : max_np <= 4 ? 4 : max_np <= 8 ? 8 : 16; }
 
 cudaError_t launch_column_fp32_ring(const ColumnJob* d_jobs, int n_jobs, int total_tiles, int max_np, bool density,
-                                    bool stats, int variant, bool big_slabs, unsigned* work,
+                                    bool stats, int variant, bool big_slabs, bool masked, unsigned* work,
                                     const unsigned long long* counters, int64_t cap, cudaStream_t st) {
   cudaMemsetAsync(work, 0, sizeof(unsigned), st);
   if (total_tiles <= 0) return cudaSuccess;
+  if (masked) {  // tile-masked jobs: one precession angle, no statistics (the host sends others elsewhere)
+    if (max_np != 1 || stats) return cudaErrorInvalidValue;
+    if (big_slabs)
+      return density ? launch<256>(k_column_fp32_v2<1, true, false, 2, 256, true>, d_jobs, n_jobs, total_tiles, work,
+                                   counters, cap, 2, st)
+                     : launch<256>(k_column_fp32_v2<1, false, false, 2, 256, true>, d_jobs, n_jobs, total_tiles, work,
+                                   counters, cap, 2, st);
+    return density ? launch<128>(k_column_fp32_v2<1, true, false, 5, 128, true>, d_jobs, n_jobs, total_tiles, work,
+                                 counters, cap, 5, st)
+                   : launch<128>(k_column_fp32_v2<1, false, false, 5, 128, true>, d_jobs, n_jobs, total_tiles, work,
+                                 counters, cap, 5, st);
+  }
   const int v = (variant > 0 && variant < kVariants && !stats) ? variant : 0;  // statistics: variant 0
   const bool b = big_slabs;
   if (density)

@@ -57,7 +57,7 @@ struct st_ctx {
   int last_column_kernel = 0;  // 1 general FP32, 2 slab-ring FP32, 3 FP64
   int tune_mode = ST_TUNE_AUTO;
   std::map<int, int> ring_tuned;  // (angles per pass, density) -> fastest slab-ring variant
-  std::map<int, int> ring_big;    // kinds whose slabs needed 256-atom staging in this context
+  std::map<uint64_t, int> ring_big;  // (pass kind, image and link-cell shape) needing 256-atom slabs
   cudaEvent_t tev[3] = {nullptr, nullptr, nullptr};
   int last_ring_variant = -1;
 };
@@ -312,7 +312,10 @@ cudaError_t tune_ring(st_ctx* c, F&& launch_variant, int64_t cap, cudaStream_t s
 
 // The slab-ring FP32 kernel needs cells of at least 3 sigma (no truncated
 // search) and at least one voxel thick in z.
-bool ring_eligible(const ColumnParams& cp) { return !cp.check_cells && cp.Ez <= cp.Mz; }
+bool ring_eligible(const ColumnParams& cp, bool stats) {
+  if (cp.tile_mask && (cp.n_prec != 1 || stats)) return false;  // masked ring: one angle, no statistics
+  return !cp.check_cells && cp.Ez <= cp.Mz;
+}
 
 // A recorded call (st_plan): the instantiated graph and what its kernels were recorded with.
 struct GraphOut {
@@ -401,11 +404,23 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
   for (int i = 0; i < n; ++i) {
     cps[i] = column_params(c, jobs[i], cell_base[i], xoff[i], yoff[i], zoff[i], aoff[i], flags);
     max_np = std::max(max_np, jobs[i].n_prec);
-    if (fp32 && !c->fp32_general && ring_eligible(cps[i])) {
+    if (fp32 && !c->fp32_general && ring_eligible(cps[i], (flags & ST_FLAG_STATS) != 0)) {
       on_ring[i] = 1;
       ring_jobs.push_back(i);
       dens = dens || cps[i].use_density;
       ring_np = std::max(ring_np, jobs[i].n_prec);
+    }
+  }
+  if (ring_np > 1) {  // masked ring instances march one angle: masked images then go per image
+    std::vector<int> kept;
+    for (int r : ring_jobs) {
+      if (cps[r].tile_mask) on_ring[r] = 0;
+      else kept.push_back(r);
+    }
+    if (kept.size() != ring_jobs.size()) {
+      ring_jobs.swap(kept);
+      dens = false;
+      for (int r : ring_jobs) dens = dens || cps[r].use_density;
     }
   }
   const bool ring = !ring_jobs.empty();
@@ -522,12 +537,21 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
   bool ring_ok = ring;  // false once a slab overflowed even 256-atom staging: the general kernel
   const bool stats = (flags & ST_FLAG_STATS) != 0;
   std::vector<int> pass_variant(passes, 0);
-  // big slabs when an earlier call of this context needed them for one of this call's kinds
+  // big slabs when an earlier call of this context needed them for the same kind of pass on
+  // images of the same shape (the first ring image's image and link-cell dimensions)
+  auto big_key = [&](int pass) -> uint64_t {
+    uint64_t h = (uint64_t)(ring_np_bucket(std::min(width, ring_np - pass * width)) * 2 + (dens ? 1 : 0));
+    if (!ring_jobs.empty()) {
+      const st_geom* g = jobs[ring_jobs[0]].g;
+      const int dims[6] = {g->Mx, g->My, g->Mz, g->Ex, g->Ey, g->Ez};
+      for (int d : dims) h = h * 1000003ull + (uint64_t)d;
+    }
+    return h;
+  };
   bool big = false;
-  for (int pass = 0; pass < passes; ++pass) {
-    const int key = ring_np_bucket(std::min(width, ring_np - pass * width)) * 2 + (dens ? 1 : 0);
-    big = big || c->ring_big.count(key) > 0;
-  }
+  for (int pass = 0; pass < passes; ++pass) big = big || c->ring_big.count(big_key(pass)) > 0;
+  bool masked = false;  // tile-masked ring jobs take the masked kernel instances
+  for (int r : ring_jobs) masked = masked || cps[r].tile_mask != nullptr;
   // with_bin false: the column phase only, on the binning already in place
   auto enqueue = [&](bool capturing, bool with_bin) -> cudaError_t {
     cudaError_t ce = cudaSuccess;
@@ -542,7 +566,7 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
       const int np_pass = std::min(width, ring_np - pass * width);
       auto ring_launch = [&](int v) {
         return launch_column_fp32_ring(c->d_coljobs + (size_t)pass * n_ring, n_ring, pass_tiles[pass], np_pass,
-                                       dens, stats, v, big, c->d_work, c->s.counters, cap, st);
+                                       dens, stats, v, big, masked, c->d_work, c->s.counters, cap, st);
       };
       if (capturing) {
         ce = ring_launch(pass_variant[pass]);
@@ -556,7 +580,7 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
         auto it = c->ring_tuned.find(key);
         if (it != c->ring_tuned.end()) {
           v = it->second;
-        } else if (pass == 0 && pass_tiles[0] >= 4096 && !big) {
+        } else if (pass == 0 && pass_tiles[0] >= 4096 && !big && !masked) {
           // autotune on the real work: the first pass overwrites its images, so every trial
           // leaves the same result; keep the fastest for the later calls of this context
           ce = tune_ring(c, ring_launch, cap, st, v);
@@ -602,10 +626,9 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
     }
     if (ring_ok && c->h_counters[4] != 0 && !big) {
       // a slab held more than 128 atoms: the column phase again with 256-atom slabs, and this
-      // context keeps them for these kinds of pass
+      // context keeps them for these kinds of pass on images of this shape
       big = true;
-      for (int pass = 0; pass < passes; ++pass)
-        c->ring_big[ring_np_bucket(std::min(width, ring_np - pass * width)) * 2 + (dens ? 1 : 0)] = 1;
+      for (int pass = 0; pass < passes; ++pass) c->ring_big[big_key(pass)] = 1;
       cudaMemsetAsync(c->s.counters + 2, 0, 3 * sizeof(unsigned long long), st);
       e = enqueue(false, false);
       if (e == cudaSuccess) e = cudaStreamSynchronize(st);
