@@ -647,9 +647,26 @@ def run_reference(args):
 
 
 def ncu_case(args):
-    """Two FP32 images of the workload through st_image, nothing else: the
-    single-kernel case for an ncu capture of the column kernel."""
+    """Untimed cases for ncu captures.  fp32 / fp64: two images of the workload through
+    st_image, nothing else (binning and column kernels).  cfg1: one warm-up and one step of
+    the 128k-atom DF + BF + blur leg on both paths (FP64 column kernel, blur).  corrector:
+    one warm-up and one step of the 4.8M-atom corrector leg (convolutions)."""
     from simulated_tem_gb300 import _lib, imaging
+    if args.ncu_case in ("cfg1", "corrector"):
+        import torch
+        stream = torch.cuda.Stream()
+        flush = torch.empty(64 << 20, dtype=torch.float64, device="cuda")
+        ctx = imaging.Context(0)
+        with torch.cuda.stream(stream):
+            if args.ncu_case == "cfg1":
+                r = cfg1_leg(ctx, stream, flush, 1, 1, cpu=False)
+                print("ncu case cfg1: FP64 %.1f images/s" % r["gpu_fp64"]["images_per_s"])
+            else:
+                r = cfg5_leg(ctx, stream, flush, 1, 1)
+                print("ncu case corrector: %s" % json.dumps(r.get("m2_corrector_fallback", r)))
+        torch.cuda.synchronize()
+        ctx.close()
+        return
     _, t, x, _ = workload()
     G, aa = t.image_geometry(len(x))
     ctx = imaging.Context(0)
@@ -670,8 +687,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched sweep and uneven-cell legs")
     ap.add_argument("--batch-steps", type=int, default=3)
-    ap.add_argument("--ncu-case", choices=["fp32", "fp64"], default=None,
-                    help="run two untimed images only (for an ncu capture)")
+    ap.add_argument("--ncu-case", choices=["fp32", "fp64", "cfg1", "corrector"], default=None,
+                    help="run one small untimed case only (for an ncu capture)")
     args = ap.parse_args()
     if args.ncu_case:
         ncu_case(args)

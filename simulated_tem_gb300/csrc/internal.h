@@ -29,11 +29,22 @@ struct BinParams {
   double ia[9];  // inverse link-cell vectors
   double g[3];
   double a_col[3];  // diagonal of the link-cell vectors (cuboid cells)
-  // FP32 copies for the reject prefilter
+  // FP32 copies for the FP64 path's reject prefilter
   float RUf[9];
   float Ruvwf[81];
   float shiftf[3];  // delta - lc_delta
   float iaf[3];     // diagonal of ia
+  // FP32 imaging path (k_bin_atoms_fp32): link-cell coordinates c = A x + B(nn) and g.y in
+  // cycles = gA x + gB(nn), the x part per atom in FP64, the replica part B(nn) per job, both
+  // summed in 64-bit fixed point of 2^-36 (cells or cycles)
+  int64_t atom_base;  // first atom of this job in the batch
+  double Afx[9];      // (ia RU)(a, k) * 2^36, row-major
+  double gAfx[3];     // (g^T RU)(k) / (2 pi) * 2^36
+  long long Bfx[81];  // round(2^36 * ia (RU Ruvw(nn) + delta - lc_delta)), 3 per replica
+  long long gBfx[27]; // round(2^36 * frac(g . (RU Ruvw(nn) + delta) / (2 pi)))
+  float Bf[81];       // B(nn) in cells, for the FP32 reject prefilter
+  float a_colf[3];
+  int fix_ok;         // 0: |B| too large for the fixed point; every candidate takes the exact arithmetic
 };
 
 // Output of the binning: atoms sorted by link cell, each cell in the
@@ -49,12 +60,19 @@ struct BinnedAtoms {
   float2* cs32;        // cos, sin of the FP64-reduced phase
 };
 
+// A kept atom's record of the FP32 path as the binning makes it (same size as double4_32a).
+struct alignas(16) Rec32 {
+  float4 p;   // a_col11*fx, a_col22*fy, a_col33*fz, bits(packed cell)
+  float2 cs;  // cos, sin of the phase
+  float2 pad;
+};
+
 struct Scratch {
   // binning temporaries, sized for nuvw * n_atoms candidates
   int* tmp_key = nullptr;   // candidate index nn * N + jj
   int* tmp_cell = nullptr;  // linear cell index
   int* tmp_slot = nullptr;  // arrival slot within the cell (atomic order)
-  double4_32a* tmp_f = nullptr; // fx, fy, fz, g.y
+  double4_32a* tmp_f = nullptr; // fx, fy, fz, g.y (FP64 path); Rec32 (FP32 path)
   int* perm = nullptr;      // position-in-cell -> tmp index
   int* block_sums = nullptr;
   unsigned long long* counters = nullptr;  // [0] kept, [1] max cell count, [2] tests, [3] accepted, [4] slab overflow
@@ -118,12 +136,14 @@ __device__ __forceinline__ bool tile_wanted(const ColumnParams& p, int tx, int t
 }
 
 // launchers (return cudaError_t of the launches)
-// Binning of a batch: jobs (device memory, n_jobs entries) with candidates
-// [0, total_cand) and cells [0, total_cells) concatenated in job order.
-cudaError_t launch_bin(const BinParams* d_jobs, int n_jobs, int64_t total_cand, int64_t total_cells, int64_t cap,
-                       Scratch& s, BinnedAtoms& b, bool exact, cudaStream_t st);
+// Binning of a batch: jobs (device memory, n_jobs entries) with atoms [0, total_atoms),
+// candidates [0, total_cand) and cells [0, total_cells) concatenated in job order.
+// fp32: the FP32 path's records (Rec32); else the FP64 path's, in the reference's rounded
+// arithmetic.
+cudaError_t launch_bin(const BinParams* d_jobs, int n_jobs, int64_t total_atoms, int64_t total_cand,
+                       int64_t total_cells, int64_t cap, Scratch& s, BinnedAtoms& b, bool fp32, cudaStream_t st);
 cudaError_t launch_bin_finalize(const BinParams* d_jobs, int n_jobs, int64_t total_cells, int64_t cap, Scratch& s,
-                                BinnedAtoms& b, int want_fp64, cudaStream_t st);
+                                BinnedAtoms& b, bool fp32, cudaStream_t st);
 cudaError_t launch_column_fp32(const ColumnParams& p, cudaStream_t st);
 
 // A job of the persistent slab-ring FP32 column kernel: an image and the first

@@ -5,10 +5,26 @@
 //   y = RU (x + Ruvw(nn)) + delta,  z = y - lc_delta,
 // the atom is kept when floor(ia z) lies inside the link-cell box; it goes to
 // cell floor(ia z) with fractional offset ia z - floor(ia z), and its phase is
-// g . y.  The cell assignment is computed in FP64 with explicitly rounded
-// operations in the reference's evaluation order, so it is bit-identical to
-// the reference's.  An FP32 pass rejects candidates that are far outside the
-// box first (the FP64 path only runs near and inside it).
+// g . y.
+//
+// FP64 path (k_bin_transform_exact): one thread per candidate (nn, jj); every kept
+// candidate goes through the reference's rounded FP64 arithmetic in its order, so the
+// offsets and the phase are bit-identical to the reference's.  An FP32 pass rejects
+// candidates far outside the box first.
+//
+// FP32 path (k_bin_atoms_fp32): one thread per atom, looping over the replicas.  FP64
+// runs at 1/64 of the FP32 rate on this GPU, so the FP64 work is done once per atom:
+// c = A x + B(nn) with A = ia RU and B(nn) = ia (RU Ruvw(nn) + delta - lc_delta), and
+// g.y / 2 pi = gA x + gB(nn); the x parts in FP64, rounded to 64-bit fixed point of
+// 2^-36, then every replica is an integer add (B(nn) in the same fixed point, computed
+// on the host).  The cell is the fixed-point value's integer part, which equals the
+// reference's floor(c) unless c lies within 1e-9 cells of a cell face (the fixed-point
+// value is within 3e-11 cells of the exact c, the reference's rounded c within 1e-12);
+// those rare candidates, and atoms too far out for the fixed point, take the reference's
+// arithmetic, so the cell assignment is bit-identical to the reference's either way.
+// The phase, g.y reduced modulo one cycle, is exact in the fixed point to 1e-11 cycles.
+// The kernel writes the FP32 records directly (offsets times the cell sides and the
+// phasor), leaving the finalize pass only the ordering.
 //
 // Instead of per-cell arrays grown by doubling, the kept atoms are counted per
 // cell, the counts scanned, and the atoms scattered; a per-cell rank by
@@ -23,6 +39,11 @@ namespace {
 
 constexpr int kScanBlock = 1024;  // counts per scan block (256 threads x 4)
 constexpr double kInv2Pi = 0.15915494309189533577;
+constexpr int kFixBits = 36;
+constexpr long long kFracMask = (1LL << kFixBits) - 1;
+constexpr long long kFixFace = 69;  // 1e-9 cells (or cycles) in units of 2^-36
+constexpr double kFixScale = 68719476736.0;  // 2^36
+constexpr double kFixLimit = 1125899906842624.0;  // 2^50: |A x| below 2^14 cells for the fixed point
 
 // index of the job whose range [base(j), base(j+1)) holds v (bases ascending)
 template <typename F>
@@ -43,20 +64,50 @@ __device__ __forceinline__ double dot3_rn(double a0, double a1, double a2, doubl
   return __dadd_rn(__dadd_rn(__dmul_rn(a0, b0), __dmul_rn(a1, b1)), __dmul_rn(a2, b2));
 }
 
-// One thread per candidate (replica nn, atom jj) in the reference's insertion
-// order t = nn * N + jj.  kExact: every kept candidate goes through the
-// reference's rounded FP64 arithmetic (the FP64 imaging path needs its exact
-// fractional offsets).  Otherwise the kept candidates use fused FP64
-// multiply-adds, which agree with the reference to a few ulp, and fall back to
-// the exact arithmetic whenever a cell coordinate lies within 1e-9 cells of a
-// cell face: the cell assignment is bit-identical either way, the offsets and
-// the phase agree to ~1e-14.
-template <bool kExact>
-__global__ void __launch_bounds__(256) k_bin_transform(const BinParams* __restrict__ jobs, int n_jobs,
-                                                       int64_t total, int64_t cap, int* __restrict__ counts,
-                                                       int* __restrict__ tmp_key, int* __restrict__ tmp_cell,
-                                                       int* __restrict__ tmp_slot, double4_32a* __restrict__ tmp_f,
-                                                       unsigned long long* __restrict__ counters) {
+// The reference's transform of candidate (nn, x), every operation rounded separately in
+// its order: y = RU (x + Ruvw(nn)) + delta and the link-cell coordinates c = ia (y - lc_delta).
+__device__ __forceinline__ void reference_transform(const BinParams& p, int nn, double x0, double x1, double x2,
+                                                    double* y, double* c) {
+  const double yy0 = __dadd_rn(x0, p.Ruvw[3 * nn + 0]);
+  const double yy1 = __dadd_rn(x1, p.Ruvw[3 * nn + 1]);
+  const double yy2 = __dadd_rn(x2, p.Ruvw[3 * nn + 2]);
+  y[0] = __dadd_rn(dot3_rn(p.RU[0], p.RU[3], p.RU[6], yy0, yy1, yy2), p.delta[0]);
+  y[1] = __dadd_rn(dot3_rn(p.RU[1], p.RU[4], p.RU[7], yy0, yy1, yy2), p.delta[1]);
+  y[2] = __dadd_rn(dot3_rn(p.RU[2], p.RU[5], p.RU[8], yy0, yy1, yy2), p.delta[2]);
+  const double z0 = __dsub_rn(y[0], p.lc_delta[0]);
+  const double z1 = __dsub_rn(y[1], p.lc_delta[1]);
+  const double z2 = __dsub_rn(y[2], p.lc_delta[2]);
+  c[0] = dot3_rn(p.ia[0], p.ia[3], p.ia[6], z0, z1, z2);
+  c[1] = dot3_rn(p.ia[1], p.ia[4], p.ia[7], z0, z1, z2);
+  c[2] = dot3_rn(p.ia[2], p.ia[5], p.ia[8], z0, z1, z2);
+}
+
+// Warp-aggregated slots: the compaction index of a kept candidate and its arrival slot in
+// its cell.  Called by exactly the lanes in `mask` (the kept ones).
+__device__ __forceinline__ void claim_slots(unsigned mask, int cell, int* counts, unsigned long long* counters,
+                                            int64_t& idx, int& slot) {
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(mask) - 1;
+  unsigned long long base = 0;
+  if (lane == leader) base = atomicAdd(&counters[0], (unsigned long long)__popc(mask));
+  base = __shfl_sync(mask, base, leader);
+  idx = (int64_t)base + __popc(mask & ((1u << lane) - 1));
+  // consecutive atoms often share a cell: one atomic per cell and warp
+  const unsigned same = __match_any_sync(mask, cell);
+  const int first = __ffs(same) - 1;
+  int slot0 = 0;
+  if (lane == first) slot0 = atomicAdd(&counts[cell], __popc(same));
+  slot = __shfl_sync(same, slot0, first) + __popc(same & ((1u << lane) - 1));
+}
+
+// FP64 path: one thread per candidate (replica nn, atom jj) in the reference's insertion
+// order t = nn * N + jj; every kept candidate in the reference's rounded arithmetic.
+__global__ void __launch_bounds__(256) k_bin_transform_exact(const BinParams* __restrict__ jobs, int n_jobs,
+                                                             int64_t total, int64_t cap, int* __restrict__ counts,
+                                                             int* __restrict__ tmp_key, int* __restrict__ tmp_cell,
+                                                             int* __restrict__ tmp_slot,
+                                                             double4_32a* __restrict__ tmp_f,
+                                                             unsigned long long* __restrict__ counters) {
   const float margin = 2e-3f;  // cells; the FP32 position error is below 1e-4 cells
   for (int64_t tg = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; tg < total;
        tg += (int64_t)gridDim.x * blockDim.x) {
@@ -79,65 +130,153 @@ __global__ void __launch_bounds__(256) k_bin_transform(const BinParams* __restri
     const float cf0 = zf0 * p.iaf[0], cf1 = zf1 * p.iaf[1], cf2 = zf2 * p.iaf[2];
     bool keep = cf0 >= -margin && cf0 < p.Ex + margin && cf1 >= -margin && cf1 < p.Ey + margin &&
                 cf2 >= -margin && cf2 < p.Ez + margin;
-    double c0 = 0, c1 = 0, c2 = 0, y0 = 0, y1 = 0, y2 = 0;
+    double c[3] = {0, 0, 0}, y[3] = {0, 0, 0};
     if (keep) {
-      const double yy0 = __dadd_rn(x0, p.Ruvw[3 * nn + 0]);
-      const double yy1 = __dadd_rn(x1, p.Ruvw[3 * nn + 1]);
-      const double yy2 = __dadd_rn(x2, p.Ruvw[3 * nn + 2]);
-      bool exact = kExact;
-      if (!kExact) {
-        y0 = fma(p.RU[6], yy2, fma(p.RU[3], yy1, p.RU[0] * yy0)) + p.delta[0];
-        y1 = fma(p.RU[7], yy2, fma(p.RU[4], yy1, p.RU[1] * yy0)) + p.delta[1];
-        y2 = fma(p.RU[8], yy2, fma(p.RU[5], yy1, p.RU[2] * yy0)) + p.delta[2];
-        c0 = (y0 - p.lc_delta[0]) * p.ia[0];
-        c1 = (y1 - p.lc_delta[1]) * p.ia[4];
-        c2 = (y2 - p.lc_delta[2]) * p.ia[8];
-        const double e = 1e-9;
-        const double f0 = c0 - floor(c0), f1 = c1 - floor(c1), f2 = c2 - floor(c2);
-        exact = f0 < e || f0 > 1.0 - e || f1 < e || f1 > 1.0 - e || f2 < e || f2 > 1.0 - e;
-      }
-      if (exact) {
-        // the reference's order, every operation rounded separately
-        y0 = __dadd_rn(dot3_rn(p.RU[0], p.RU[3], p.RU[6], yy0, yy1, yy2), p.delta[0]);
-        y1 = __dadd_rn(dot3_rn(p.RU[1], p.RU[4], p.RU[7], yy0, yy1, yy2), p.delta[1]);
-        y2 = __dadd_rn(dot3_rn(p.RU[2], p.RU[5], p.RU[8], yy0, yy1, yy2), p.delta[2]);
-        const double z0 = __dsub_rn(y0, p.lc_delta[0]);
-        const double z1 = __dsub_rn(y1, p.lc_delta[1]);
-        const double z2 = __dsub_rn(y2, p.lc_delta[2]);
-        c0 = dot3_rn(p.ia[0], p.ia[3], p.ia[6], z0, z1, z2);
-        c1 = dot3_rn(p.ia[1], p.ia[4], p.ia[7], z0, z1, z2);
-        c2 = dot3_rn(p.ia[2], p.ia[5], p.ia[8], z0, z1, z2);
-      }
+      reference_transform(p, nn, x0, x1, x2, y, c);
       // pointInSupercell: floor(c) in [0, N) on every axis
-      keep = c0 >= 0.0 && c0 < (double)p.Ex && c1 >= 0.0 && c1 < (double)p.Ey && c2 >= 0.0 &&
-             c2 < (double)p.Ez;
+      keep = c[0] >= 0.0 && c[0] < (double)p.Ex && c[1] >= 0.0 && c[1] < (double)p.Ey && c[2] >= 0.0 &&
+             c[2] < (double)p.Ez;
     }
-    // warp-aggregated compaction slot
     const unsigned mask = __ballot_sync(__activemask(), keep);
     if (!keep) continue;
-    const int lane = threadIdx.x & 31;
-    const int leader = __ffs(mask) - 1;
-    unsigned long long base = 0;
-    if (lane == leader) base = atomicAdd(&counters[0], (unsigned long long)__popc(mask));
-    base = __shfl_sync(mask, base, leader);
-    const int64_t idx = (int64_t)base + __popc(mask & ((1u << lane) - 1));
-
-    const double fl0 = floor(c0), fl1 = floor(c1), fl2 = floor(c2);
-    const int cx = (int)fl0, cy = (int)fl1, cz = (int)fl2;
-    const int cell = (int)p.cell_base + cx + p.Ex * (cy + p.Ey * cz);
-    // consecutive atoms often share a cell: one atomic per cell and warp
-    const unsigned same = __match_any_sync(mask, cell);
-    const int first = __ffs(same) - 1;
-    int slot0 = 0;
-    if (lane == first) slot0 = atomicAdd(&counts[cell], __popc(same));
-    const int slot = __shfl_sync(same, slot0, first) + __popc(same & ((1u << lane) - 1));
+    const double fl0 = floor(c[0]), fl1 = floor(c[1]), fl2 = floor(c[2]);
+    const int cell = (int)p.cell_base + (int)fl0 + p.Ex * ((int)fl1 + p.Ey * (int)fl2);
+    int64_t idx;
+    int slot;
+    claim_slots(mask, cell, counts, counters, idx, slot);
     if (idx >= cap) continue;  // overflow: counted, not stored; the host grows the arrays and retries
-    const double gdotr = kExact ? dot3_rn(p.g[0], p.g[1], p.g[2], y0, y1, y2)
-                                : fma(p.g[2], y2, fma(p.g[1], y1, p.g[0] * y0));
     tmp_key[idx] = (int)t;
     tmp_cell[idx] = cell;
     tmp_slot[idx] = slot;
-    tmp_f[idx] = make_double4_32a(__dsub_rn(c0, fl0), __dsub_rn(c1, fl1), __dsub_rn(c2, fl2), gdotr);
+    tmp_f[idx] = make_double4_32a(__dsub_rn(c[0], fl0), __dsub_rn(c[1], fl1), __dsub_rn(c[2], fl2),
+                                  dot3_rn(p.g[0], p.g[1], p.g[2], y[0], y[1], y[2]));
+  }
+}
+
+// 2^-32 * (32 bits of a 2^-36 fixed-point fraction in [0, 1)), rounded to FP32
+__device__ __forceinline__ float fix_frac_to_float(long long f) {
+  return (float)(unsigned)(f >> 4) * 2.3283064365386963e-10f;
+}
+
+// FP32 path: one thread per atom, all replicas; warps stay converged (every lane runs the
+// same replica loop, lanes past the end or past their job's replicas keep nothing).
+__global__ void __launch_bounds__(256) k_bin_atoms_fp32(const BinParams* __restrict__ jobs, int n_jobs,
+                                                        int64_t total_atoms, int64_t cap, int* __restrict__ counts,
+                                                        int* __restrict__ tmp_key, int* __restrict__ tmp_cell,
+                                                        int* __restrict__ tmp_slot, Rec32* __restrict__ tmp_r,
+                                                        unsigned long long* __restrict__ counters) {
+  const float margin = 2e-3f;  // cells; the prefilter's error is below 1e-4 cells
+  const int lane = threadIdx.x & 31;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < total_atoms; base += stride) {
+    const int64_t ag = base + lane;
+    const bool valid = ag < total_atoms;
+    const int job = (!valid || n_jobs == 1) ? 0 : find_job(n_jobs, ag, [&](int k) { return jobs[k].atom_base; });
+    const BinParams& p = jobs[job];
+    const int64_t jj = valid ? ag - p.atom_base : 0;
+    const int nrep = valid ? p.nuvw : 0;
+    double x0 = 0, x1 = 0, x2 = 0;
+    if (valid) {
+      const double* xa = p.x + jj * p.ldx;
+      x0 = xa[0];
+      x1 = xa[1];
+      x2 = xa[2];
+    }
+    // the atom's part, in FP64, then in fixed point
+    const double u0 = fma(p.Afx[2], x2, fma(p.Afx[1], x1, p.Afx[0] * x0));
+    const double u1 = fma(p.Afx[5], x2, fma(p.Afx[4], x1, p.Afx[3] * x0));
+    const double u2 = fma(p.Afx[8], x2, fma(p.Afx[7], x1, p.Afx[6] * x0));
+    const double gu = fma(p.gAfx[2], x2, fma(p.gAfx[1], x1, p.gAfx[0] * x0));
+    const bool fixed = p.fix_ok && fabs(u0) < kFixLimit && fabs(u1) < kFixLimit && fabs(u2) < kFixLimit &&
+                       fabs(gu) < kFixLimit;
+    long long q0 = 0, q1 = 0, q2 = 0, gq = 0;
+    if (fixed) {
+      q0 = __double2ll_rn(u0);
+      q1 = __double2ll_rn(u1);
+      q2 = __double2ll_rn(u2);
+      gq = __double2ll_rn(gu);
+    }
+    // FP32 copy for the prefilter (2^-16 cells)
+    const float v0 = (float)(int)(q0 >> 20) * 1.52587890625e-05f;
+    const float v1 = (float)(int)(q1 >> 20) * 1.52587890625e-05f;
+    const float v2 = (float)(int)(q2 >> 20) * 1.52587890625e-05f;
+    const int nmax = __reduce_max_sync(0xffffffffu, nrep);
+    for (int nn = 0; nn < nmax; ++nn) {
+      bool cand = nn < nrep;
+      if (cand && fixed) {
+        const float cf0 = v0 + p.Bf[3 * nn + 0], cf1 = v1 + p.Bf[3 * nn + 1], cf2 = v2 + p.Bf[3 * nn + 2];
+        cand = cf0 >= -margin && cf0 < p.Ex + margin && cf1 >= -margin && cf1 < p.Ey + margin &&
+               cf2 >= -margin && cf2 < p.Ez + margin;
+      }
+      if (__any_sync(0xffffffffu, cand)) {
+        bool keep = false;
+        long long c0 = 0, c1 = 0, c2 = 0, gt = 0;
+        if (cand) {
+          bool exact = !fixed;
+          if (fixed) {
+            c0 = q0 + p.Bfx[3 * nn + 0];
+            c1 = q1 + p.Bfx[3 * nn + 1];
+            c2 = q2 + p.Bfx[3 * nn + 2];
+            gt = gq + p.gBfx[nn];
+            const int k0 = (int)(c0 >> kFixBits), k1 = (int)(c1 >> kFixBits), k2 = (int)(c2 >> kFixBits);
+            const long long f0 = c0 & kFracMask, f1 = c1 & kFracMask, f2 = c2 & kFracMask;
+            const bool near = f0 < kFixFace || f0 > kFracMask - kFixFace || f1 < kFixFace ||
+                              f1 > kFracMask - kFixFace || f2 < kFixFace || f2 > kFracMask - kFixFace;
+            const bool reach = k0 >= -1 && k0 <= p.Ex && k1 >= -1 && k1 <= p.Ey && k2 >= -1 && k2 <= p.Ez;
+            exact = near && reach;
+            keep = !exact && (unsigned)k0 < (unsigned)p.Ex && (unsigned)k1 < (unsigned)p.Ey &&
+                   (unsigned)k2 < (unsigned)p.Ez;
+          }
+          if (exact) {
+            // the reference's arithmetic decides (a cell face within 1e-9 cells, or coordinates
+            // beyond the fixed point's range)
+            double y[3], c[3];
+            reference_transform(p, nn, x0, x1, x2, y, c);
+            keep = c[0] >= 0.0 && c[0] < (double)p.Ex && c[1] >= 0.0 && c[1] < (double)p.Ey && c[2] >= 0.0 &&
+                   c[2] < (double)p.Ez;
+            if (keep) {
+              long long cf[3];
+              for (int a = 0; a < 3; ++a) {
+                const double fl = floor(c[a]);
+                const long long fr = __double2ll_rn(__dsub_rn(c[a], fl) * kFixScale);
+                cf[a] = ((long long)fl << kFixBits) | (fr > kFracMask ? kFracMask : fr);
+              }
+              c0 = cf[0];
+              c1 = cf[1];
+              c2 = cf[2];
+              if (!fixed) {
+                const double cyc = dot3_rn(p.g[0], p.g[1], p.g[2], y[0], y[1], y[2]) * kInv2Pi;
+                gt = __double2ll_rn((cyc - rint(cyc)) * kFixScale);
+              }
+            }
+          }
+        }
+        const unsigned mask = __ballot_sync(0xffffffffu, keep);
+        if (keep) {
+          const int k0 = (int)(c0 >> kFixBits), k1 = (int)(c1 >> kFixBits), k2 = (int)(c2 >> kFixBits);
+          const int cell = (int)p.cell_base + k0 + p.Ex * (k1 + p.Ey * k2);
+          int64_t idx;
+          int slot;
+          claim_slots(mask, cell, counts, counters, idx, slot);
+          if (idx < cap) {  // else overflow: counted, not stored; the host grows the arrays and retries
+            // phase: g.y / 2 pi reduced to [-1/2, 1/2) cycles (sign-extended 36-bit fraction)
+            const long long r = (long long)((unsigned long long)gt << (64 - kFixBits)) >> (64 - kFixBits);
+            const float tc = (float)(int)(r >> 4) * 2.3283064365386963e-10f;
+            float sf, cf;
+            sincospif(2.0f * tc, &sf, &cf);
+            tmp_key[idx] = (int)((int64_t)nn * p.n_atoms + jj);
+            tmp_cell[idx] = cell;
+            tmp_slot[idx] = slot;
+            tmp_r[idx].p = make_float4(p.a_colf[0] * fix_frac_to_float(c0 & kFracMask),
+                                       p.a_colf[1] * fix_frac_to_float(c1 & kFracMask),
+                                       p.a_colf[2] * fix_frac_to_float(c2 & kFracMask),
+                                       __int_as_float(pack_cell(k0, k1, k2)));
+            tmp_r[idx].cs = make_float2(cf, sf);
+          }
+        }
+      }
+      __syncwarp();
+    }
   }
 }
 
@@ -243,32 +382,31 @@ __global__ void __launch_bounds__(256) k_bin_place(const int* __restrict__ tmp_c
 // registers; larger cells rank from memory.
 constexpr int kRankRegs = 24;
 
+// FP64 path: the records from the exact offsets and g.y
 __device__ __forceinline__ void write_record(const BinnedAtoms& b, int dst, const double4_32a& f, int packed,
-                                             double a11, double a22, double a33, int want_fp64) {
+                                             double a11, double a22, double a33) {
   b.p32[dst] = make_float4((float)(a11 * f.x), (float)(a22 * f.y), (float)(a33 * f.z), __int_as_float(packed));
-  if (want_fp64) {
-    double sn, cs;
-    sincos(f.w, &sn, &cs);
-    b.f64[dst] = make_double4_32a(f.x, f.y, f.z, 0.0);
-    b.cs64[dst] = make_double2(cs, sn);
-  } else {
-    // g.y reduced modulo one cycle in FP64, the phasor in FP32
-    double tcyc = f.w * kInv2Pi;
-    tcyc = tcyc - rint(tcyc);
-    float sf, cf;
-    sincospif(2.0f * (float)tcyc, &sf, &cf);
-    b.cs32[dst] = make_float2(cf, sf);
-  }
+  double sn, cs;
+  sincos(f.w, &sn, &cs);
+  b.f64[dst] = make_double4_32a(f.x, f.y, f.z, 0.0);
+  b.cs64[dst] = make_double2(cs, sn);
 }
 
+// FP32 path: the binning wrote the records; they move to their place
+__device__ __forceinline__ void move_record(const BinnedAtoms& b, int dst, const Rec32* __restrict__ r) {
+  b.p32[dst] = r->p;
+  b.cs32[dst] = r->cs;
+}
+
+template <bool kFp32>
 __global__ void __launch_bounds__(128) k_bin_finalize(const BinParams* __restrict__ jobs, int n_jobs,
                                                       const int* __restrict__ start, const int* __restrict__ counts,
                                                       int64_t n_cells, const int* __restrict__ perm,
                                                       const int* __restrict__ tmp_key,
-                                                      const double4_32a* __restrict__ tmp_f, int want_fp64,
-                                                      BinnedAtoms b, const unsigned long long* __restrict__ counters,
-                                                      int64_t cap) {
+                                                      const double4_32a* __restrict__ tmp_f, BinnedAtoms b,
+                                                      const unsigned long long* __restrict__ counters, int64_t cap) {
   if ((int64_t)counters[0] > cap) return;
+  const Rec32* tmp_r = reinterpret_cast<const Rec32*>(tmp_f);
   for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n_cells; c += (int64_t)gridDim.x * blockDim.x) {
     const int job = n_jobs == 1 ? 0 : find_job(n_jobs, c, [&](int k) { return jobs[k].cell_base; });
     const BinParams& p = jobs[job];
@@ -293,7 +431,10 @@ __global__ void __launch_bounds__(128) k_bin_finalize(const BinParams* __restric
         int r = 0;
 #pragma unroll
         for (int j = 0; j < kRankRegs; ++j) r += (key[j] < key[i]);
-        write_record(b, s + r, tmp_f[ti[i]], packed, a11, a22, a33, want_fp64);
+        if constexpr (kFp32)
+          move_record(b, s + r, tmp_r + ti[i]);
+        else
+          write_record(b, s + r, tmp_f[ti[i]], packed, a11, a22, a33);
       }
     } else {
       for (int i = 0; i < n; ++i) {
@@ -301,7 +442,10 @@ __global__ void __launch_bounds__(128) k_bin_finalize(const BinParams* __restric
         const int ki = tmp_key[t];
         int r = 0;
         for (int j = 0; j < n; ++j) r += (tmp_key[perm[s + j]] < ki);
-        write_record(b, s + r, tmp_f[t], packed, a11, a22, a33, want_fp64);
+        if constexpr (kFp32)
+          move_record(b, s + r, tmp_r + t);
+        else
+          write_record(b, s + r, tmp_f[t], packed, a11, a22, a33);
       }
     }
   }
@@ -316,20 +460,20 @@ int grid_for(int64_t n, int threads, int max_blocks) {
 
 }  // namespace
 
-cudaError_t launch_bin(const BinParams* d_jobs, int n_jobs, int64_t total_cand, int64_t total_cells, int64_t cap,
-                       Scratch& s, BinnedAtoms& b, bool exact, cudaStream_t st) {
+cudaError_t launch_bin(const BinParams* d_jobs, int n_jobs, int64_t total_atoms, int64_t total_cand,
+                       int64_t total_cells, int64_t cap, Scratch& s, BinnedAtoms& b, bool fp32, cudaStream_t st) {
   cudaMemsetAsync(b.cell_count, 0, sizeof(int) * total_cells, st);
   cudaMemsetAsync(s.counters, 0, sizeof(unsigned long long) * 8, st);
   int dev = 0, sms = 148;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const int grid = grid_for(total_cand, 256, sms * 16);
-  if (exact)
-    k_bin_transform<true><<<grid, 256, 0, st>>>(d_jobs, n_jobs, total_cand, cap, b.cell_count, s.tmp_key, s.tmp_cell,
-                                                s.tmp_slot, s.tmp_f, s.counters);
+  if (fp32)
+    k_bin_atoms_fp32<<<grid_for(total_atoms, 256, sms * 16), 256, 0, st>>>(
+        d_jobs, n_jobs, total_atoms, cap, b.cell_count, s.tmp_key, s.tmp_cell, s.tmp_slot,
+        reinterpret_cast<Rec32*>(s.tmp_f), s.counters);
   else
-    k_bin_transform<false><<<grid, 256, 0, st>>>(d_jobs, n_jobs, total_cand, cap, b.cell_count, s.tmp_key,
-                                                 s.tmp_cell, s.tmp_slot, s.tmp_f, s.counters);
+    k_bin_transform_exact<<<grid_for(total_cand, 256, sms * 16), 256, 0, st>>>(
+        d_jobs, n_jobs, total_cand, cap, b.cell_count, s.tmp_key, s.tmp_cell, s.tmp_slot, s.tmp_f, s.counters);
   const int nb = (int)((total_cells + kScanBlock - 1) / kScanBlock);
   k_scan_blocks<<<nb, 256, 0, st>>>(b.cell_count, total_cells, s.block_sums, s.counters);
   k_scan_top<<<1, 1024, 0, st>>>(s.block_sums, nb);
@@ -339,13 +483,17 @@ cudaError_t launch_bin(const BinParams* d_jobs, int n_jobs, int64_t total_cand, 
 }
 
 cudaError_t launch_bin_finalize(const BinParams* d_jobs, int n_jobs, int64_t total_cells, int64_t cap, Scratch& s,
-                                BinnedAtoms& b, int want_fp64, cudaStream_t st) {
+                                BinnedAtoms& b, bool fp32, cudaStream_t st) {
   int dev = 0, sms = 148;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  k_bin_finalize<<<grid_for(total_cells, 128, sms * 16), 128, 0, st>>>(d_jobs, n_jobs, b.cell_start, b.cell_count,
-                                                                       total_cells, s.perm, s.tmp_key, s.tmp_f,
-                                                                       want_fp64, b, s.counters, cap);
+  const int grid = grid_for(total_cells, 128, sms * 16);
+  if (fp32)
+    k_bin_finalize<true><<<grid, 128, 0, st>>>(d_jobs, n_jobs, b.cell_start, b.cell_count, total_cells, s.perm,
+                                               s.tmp_key, s.tmp_f, b, s.counters, cap);
+  else
+    k_bin_finalize<false><<<grid, 128, 0, st>>>(d_jobs, n_jobs, b.cell_start, b.cell_count, total_cells, s.perm,
+                                                s.tmp_key, s.tmp_f, b, s.counters, cap);
   return cudaGetLastError();
 }
 

@@ -192,7 +192,7 @@ struct Job {
   int mask_T = 0;
 };
 
-BinParams bin_params(const Job& j, int64_t cand_base, int64_t cell_base) {
+BinParams bin_params(const Job& j, int64_t cand_base, int64_t cell_base, int64_t atom_base) {
   const st_geom* g = j.g;
   BinParams bp;
   memset(&bp, 0, sizeof bp);
@@ -221,6 +221,44 @@ BinParams bin_params(const Job& j, int64_t cand_base, int64_t cell_base) {
   bp.iaf[0] = (float)g->ia_col[0];
   bp.iaf[1] = (float)g->ia_col[4];
   bp.iaf[2] = (float)g->ia_col[8];
+  // the FP32 path's fixed-point form (2^-36): c = A x + B(nn), g.y / 2 pi = gA x + gB(nn),
+  // matrices column-major as in st_geom (M(a, b) = M[a + 3 b])
+  const double S = 68719476736.0, inv2pi = 0.15915494309189533577;
+  bp.atom_base = atom_base;
+  bp.fix_ok = 1;
+  for (int a = 0; a < 3; ++a)
+    for (int k = 0; k < 3; ++k) {
+      double s_ak = 0.0;
+      for (int b = 0; b < 3; ++b) s_ak += g->ia_col[a + 3 * b] * g->RU[b + 3 * k];
+      bp.Afx[3 * a + k] = s_ak * S;
+    }
+  for (int k = 0; k < 3; ++k) {
+    double s_k = 0.0;
+    for (int a = 0; a < 3; ++a) s_k += g->g[a] * g->RU[a + 3 * k];
+    bp.gAfx[k] = s_k * inv2pi * S;
+  }
+  for (int nn = 0; nn < g->nuvw; ++nn) {
+    double w[3];  // RU Ruvw(nn) + delta
+    for (int b = 0; b < 3; ++b) {
+      w[b] = g->delta[b];
+      for (int k = 0; k < 3; ++k) w[b] += g->RU[b + 3 * k] * g->Ruvw[3 * nn + k];
+    }
+    double gw = 0.0;
+    for (int a = 0; a < 3; ++a) {
+      double ba = 0.0;
+      for (int b = 0; b < 3; ++b) ba += g->ia_col[a + 3 * b] * (w[b] - g->lc_delta[b]);
+      if (!(std::fabs(ba) < 16384.0)) bp.fix_ok = 0;  // beyond 2^14 cells: the exact arithmetic throughout
+      bp.Bfx[3 * nn + a] = bp.fix_ok ? std::llrint(ba * S) : 0;
+      bp.Bf[3 * nn + a] = (float)ba;
+      gw += g->g[a] * w[a];
+    }
+    const double cyc = gw * inv2pi;
+    bp.gBfx[nn] = std::isfinite(cyc) ? std::llrint((cyc - std::rint(cyc)) * S) : 0;
+    if (!std::isfinite(cyc)) bp.fix_ok = 0;
+  }
+  for (int a = 0; a < 3; ++a) bp.a_colf[a] = (float)bp.a_col[a];
+  for (int i = 0; i < 9; ++i)
+    if (!std::isfinite(bp.Afx[i])) bp.fix_ok = 0;
   return bp;
 }
 
@@ -329,11 +367,12 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
   const int n = (int)jobs.size();
   const bool fp32 = (flags & ST_FLAG_FP32) != 0;
   // concatenation offsets
-  std::vector<int64_t> cand_base(n + 1, 0), cell_base(n + 1, 0);
+  std::vector<int64_t> cand_base(n + 1, 0), cell_base(n + 1, 0), atom_base(n + 1, 0);
   std::vector<size_t> xoff(n + 1, 0), yoff(n + 1, 0), zoff(n + 1, 0), aoff(n + 1, 0);
   for (int i = 0; i < n; ++i) {
     const st_geom* g = jobs[i].g;
     cand_base[i + 1] = cand_base[i] + (int64_t)g->nuvw * jobs[i].n_atoms;
+    atom_base[i + 1] = atom_base[i] + jobs[i].n_atoms;
     cell_base[i + 1] = cell_base[i] + (int64_t)g->Ex * g->Ey * g->Ez;
     xoff[i + 1] = xoff[i] + g->Mx;
     yoff[i + 1] = yoff[i] + g->My;
@@ -478,7 +517,7 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
       haa[aoff[i] + k] = jobs[i].aa[k];
       haaf[aoff[i] + k] = (float)jobs[i].aa[k];
     }
-    hbp[i] = bin_params(jobs[i], cand_base[i], cell_base[i]);
+    hbp[i] = bin_params(jobs[i], cand_base[i], cell_base[i], atom_base[i]);
   }
   for (size_t k = 0; k < cj.size(); ++k) hcj[k] = cj[k];
   cudaMemcpyAsync(c->s.xtab, hxt, xoff[n] * sizeof(int2), cudaMemcpyHostToDevice, st);
@@ -557,8 +596,8 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
     cudaError_t ce = cudaSuccess;
     if (!capturing) cudaEventRecord(c->ev[0], st);
     if (with_bin) {
-      ce = launch_bin(c->d_binjobs, n, total_cand, total_cells, cap, c->s, c->b, !fp32, st);
-      if (ce == cudaSuccess) ce = launch_bin_finalize(c->d_binjobs, n, total_cells, cap, c->s, c->b, fp32 ? 0 : 1, st);
+      ce = launch_bin(c->d_binjobs, n, atom_base[n], total_cand, total_cells, cap, c->s, c->b, fp32, st);
+      if (ce == cudaSuccess) ce = launch_bin_finalize(c->d_binjobs, n, total_cells, cap, c->s, c->b, fp32, st);
     }
     if (ce == cudaSuccess) ce = clear_images();
     if (!capturing) cudaEventRecord(c->ev[1], st);
