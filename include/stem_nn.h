@@ -23,9 +23,13 @@ int stn_conv2d_fwd(const void* x, int32_t B, int32_t H, int32_t W, int32_t Cin, 
                    void* stream);
 
 /* Weight gradient, accumulated: gw[co][t][ci] += sum over pixels of gy[p][co] x[p + d_t][ci]
- * (gw FP32; x [B][H][W][Cin], gy [B][H][W][Cout] BF16; Cin, Cout multiples of 8). */
+ * (gw FP32; x [B][H][W][Cin], gy [B][H][W][Cout] BF16; Cin, Cout multiples of 8).  ws: FP32
+ * device workspace of at least stn_conv2d_wgrad_workspace(...) floats (0 = invalid
+ * arguments) for the partial sums of the pixel split, which are added in a fixed order, so
+ * the gradient does not depend on scheduling. */
+int64_t stn_conv2d_wgrad_workspace(int32_t B, int32_t H, int32_t W, int32_t Cin, int32_t Cout, int32_t taps);
 int stn_conv2d_wgrad(const void* x, const void* gy, int32_t B, int32_t H, int32_t W, int32_t Cin, int32_t Cout,
-                     int32_t taps, float* gw, void* stream);
+                     int32_t taps, float* gw, float* ws, int64_t ws_floats, void* stream);
 
 /* wt[ci][taps - 1 - t][co] = w[co][t][ci]: the input gradient of a convolution is the
  * convolution of the output gradient with wt. */
@@ -47,8 +51,10 @@ int stn_split(const void* gy, void* ga, void* gb, int64_t npix, int32_t Ca, int3
 /* g *= (y > 0), element-wise over n values. */
 int stn_relu_mask(void* g, const void* y, int64_t n, void* stream);
 
-/* gb[c] += sum over pixels of g[p][c] (gb FP32). */
-int stn_bias_grad(const void* g, float* gb, int64_t npix, int32_t C, void* stream);
+/* gb[c] += sum over pixels of g[p][c] (gb FP32), in a fixed order through a workspace of
+ * stn_bias_grad_workspace(C) floats. */
+int64_t stn_bias_grad_workspace(int32_t C);
+int stn_bias_grad(const void* g, float* gb, int64_t npix, int32_t C, float* ws, int64_t ws_floats, void* stream);
 
 /* *loss += mean over pixels of (pred[p][0] - target[p])^2 + w1 (pred[p][1] - t1[p])^2 with
  * t1 = target1[p], or |target[p]| when target1 is null (pred FP32 [npix][Cp], targets FP32

@@ -158,102 +158,114 @@ __device__ __forceinline__ float fix_frac_to_float(long long f) {
   return (float)(unsigned)(f >> 4) * 2.3283064365386963e-10f;
 }
 
-// FP32 path: one thread per atom, all replicas; warps stay converged (every lane runs the
-// same replica loop, lanes past the end or past their job's replicas keep nothing).
+// The FP32 path's decision for candidate (nn, atom): kept or not, and, when kept, the
+// fixed-point link-cell coordinates c[3] (cell << 36 | fraction) and phase gt (cycles,
+// 2^-36).  `fixed` atoms use the fixed point (the reference's arithmetic decides within
+// 1e-9 cells of a face), the others the reference's arithmetic throughout.
+struct AtomFix {
+  double x0, x1, x2;
+  long long q0, q1, q2, gq;  // A x and gA x in 2^-36 fixed point
+  float v0, v1, v2;          // A x in cells, FP32, for the prefilter
+  bool fixed;
+};
+
+__device__ __forceinline__ bool prefilter(const BinParams& p, const AtomFix& a, int nn) {
+  if (!a.fixed) return true;
+  const float margin = 2e-3f;  // cells; the prefilter's error is below 1e-4 cells
+  const float cf0 = a.v0 + p.Bf[3 * nn + 0], cf1 = a.v1 + p.Bf[3 * nn + 1], cf2 = a.v2 + p.Bf[3 * nn + 2];
+  return cf0 >= -margin && cf0 < p.Ex + margin && cf1 >= -margin && cf1 < p.Ey + margin && cf2 >= -margin &&
+         cf2 < p.Ez + margin;
+}
+
+__device__ __forceinline__ bool decide(const BinParams& p, const AtomFix& a, int nn, long long* c, long long& gt) {
+  bool exact = !a.fixed, keep = false;
+  if (a.fixed) {
+    c[0] = a.q0 + p.Bfx[3 * nn + 0];
+    c[1] = a.q1 + p.Bfx[3 * nn + 1];
+    c[2] = a.q2 + p.Bfx[3 * nn + 2];
+    gt = a.gq + p.gBfx[nn];
+    const int k0 = (int)(c[0] >> kFixBits), k1 = (int)(c[1] >> kFixBits), k2 = (int)(c[2] >> kFixBits);
+    const long long f0 = c[0] & kFracMask, f1 = c[1] & kFracMask, f2 = c[2] & kFracMask;
+    const bool near = f0 < kFixFace || f0 > kFracMask - kFixFace || f1 < kFixFace || f1 > kFracMask - kFixFace ||
+                      f2 < kFixFace || f2 > kFracMask - kFixFace;
+    const bool reach = k0 >= -1 && k0 <= p.Ex && k1 >= -1 && k1 <= p.Ey && k2 >= -1 && k2 <= p.Ez;
+    exact = near && reach;
+    keep = !exact && (unsigned)k0 < (unsigned)p.Ex && (unsigned)k1 < (unsigned)p.Ey && (unsigned)k2 < (unsigned)p.Ez;
+  }
+  if (exact) {
+    // the reference's arithmetic decides (a cell face within 1e-9 cells, or coordinates
+    // beyond the fixed point's range)
+    double y[3], cd[3];
+    reference_transform(p, nn, a.x0, a.x1, a.x2, y, cd);
+    keep = cd[0] >= 0.0 && cd[0] < (double)p.Ex && cd[1] >= 0.0 && cd[1] < (double)p.Ey && cd[2] >= 0.0 &&
+           cd[2] < (double)p.Ez;
+    if (keep) {
+      for (int k = 0; k < 3; ++k) {
+        const double fl = floor(cd[k]);
+        const long long fr = __double2ll_rn(__dsub_rn(cd[k], fl) * kFixScale);
+        c[k] = ((long long)fl << kFixBits) | (fr > kFracMask ? kFracMask : fr);
+      }
+      if (!a.fixed) {
+        const double cyc = dot3_rn(p.g[0], p.g[1], p.g[2], y[0], y[1], y[2]) * kInv2Pi;
+        gt = __double2ll_rn((cyc - rint(cyc)) * kFixScale);
+      }
+    }
+  }
+  return keep;
+}
+
+// FP32 path: one thread per atom, all replicas.  Warps stay converged: every lane runs
+// the same replica loop, lanes past the end or past their job's replicas keep nothing.
+// (Counting first and claiming one compaction range per block halves the atomics on the
+// kept-atom counter but decides every candidate twice: slower.)
 __global__ void __launch_bounds__(256) k_bin_atoms_fp32(const BinParams* __restrict__ jobs, int n_jobs,
                                                         int64_t total_atoms, int64_t cap, int* __restrict__ counts,
                                                         int* __restrict__ tmp_key, int* __restrict__ tmp_cell,
                                                         int* __restrict__ tmp_slot, Rec32* __restrict__ tmp_r,
                                                         unsigned long long* __restrict__ counters) {
-  const float margin = 2e-3f;  // cells; the prefilter's error is below 1e-4 cells
   const int lane = threadIdx.x & 31;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < total_atoms; base += stride) {
-    const int64_t ag = base + lane;
+    const int64_t ag = base + lane;  // warp-uniform loop
     const bool valid = ag < total_atoms;
     const int job = (!valid || n_jobs == 1) ? 0 : find_job(n_jobs, ag, [&](int k) { return jobs[k].atom_base; });
     const BinParams& p = jobs[job];
     const int64_t jj = valid ? ag - p.atom_base : 0;
     const int nrep = valid ? p.nuvw : 0;
-    double x0 = 0, x1 = 0, x2 = 0;
+    AtomFix a;
+    a.x0 = a.x1 = a.x2 = 0.0;
     if (valid) {
       const double* xa = p.x + jj * p.ldx;
-      x0 = xa[0];
-      x1 = xa[1];
-      x2 = xa[2];
+      a.x0 = xa[0];
+      a.x1 = xa[1];
+      a.x2 = xa[2];
     }
     // the atom's part, in FP64, then in fixed point
-    const double u0 = fma(p.Afx[2], x2, fma(p.Afx[1], x1, p.Afx[0] * x0));
-    const double u1 = fma(p.Afx[5], x2, fma(p.Afx[4], x1, p.Afx[3] * x0));
-    const double u2 = fma(p.Afx[8], x2, fma(p.Afx[7], x1, p.Afx[6] * x0));
-    const double gu = fma(p.gAfx[2], x2, fma(p.gAfx[1], x1, p.gAfx[0] * x0));
-    const bool fixed = p.fix_ok && fabs(u0) < kFixLimit && fabs(u1) < kFixLimit && fabs(u2) < kFixLimit &&
-                       fabs(gu) < kFixLimit;
-    long long q0 = 0, q1 = 0, q2 = 0, gq = 0;
-    if (fixed) {
-      q0 = __double2ll_rn(u0);
-      q1 = __double2ll_rn(u1);
-      q2 = __double2ll_rn(u2);
-      gq = __double2ll_rn(gu);
+    const double u0 = fma(p.Afx[2], a.x2, fma(p.Afx[1], a.x1, p.Afx[0] * a.x0));
+    const double u1 = fma(p.Afx[5], a.x2, fma(p.Afx[4], a.x1, p.Afx[3] * a.x0));
+    const double u2 = fma(p.Afx[8], a.x2, fma(p.Afx[7], a.x1, p.Afx[6] * a.x0));
+    const double gu = fma(p.gAfx[2], a.x2, fma(p.gAfx[1], a.x1, p.gAfx[0] * a.x0));
+    a.fixed = p.fix_ok && fabs(u0) < kFixLimit && fabs(u1) < kFixLimit && fabs(u2) < kFixLimit &&
+              fabs(gu) < kFixLimit;
+    a.q0 = a.q1 = a.q2 = a.gq = 0;
+    if (a.fixed) {
+      a.q0 = __double2ll_rn(u0);
+      a.q1 = __double2ll_rn(u1);
+      a.q2 = __double2ll_rn(u2);
+      a.gq = __double2ll_rn(gu);
     }
-    // FP32 copy for the prefilter (2^-16 cells)
-    const float v0 = (float)(int)(q0 >> 20) * 1.52587890625e-05f;
-    const float v1 = (float)(int)(q1 >> 20) * 1.52587890625e-05f;
-    const float v2 = (float)(int)(q2 >> 20) * 1.52587890625e-05f;
+    a.v0 = (float)(int)(a.q0 >> 20) * 1.52587890625e-05f;  // 2^-16 cells
+    a.v1 = (float)(int)(a.q1 >> 20) * 1.52587890625e-05f;
+    a.v2 = (float)(int)(a.q2 >> 20) * 1.52587890625e-05f;
     const int nmax = __reduce_max_sync(0xffffffffu, nrep);
     for (int nn = 0; nn < nmax; ++nn) {
-      bool cand = nn < nrep;
-      if (cand && fixed) {
-        const float cf0 = v0 + p.Bf[3 * nn + 0], cf1 = v1 + p.Bf[3 * nn + 1], cf2 = v2 + p.Bf[3 * nn + 2];
-        cand = cf0 >= -margin && cf0 < p.Ex + margin && cf1 >= -margin && cf1 < p.Ey + margin &&
-               cf2 >= -margin && cf2 < p.Ez + margin;
-      }
+      const bool cand = nn < nrep && prefilter(p, a, nn);
       if (__any_sync(0xffffffffu, cand)) {
-        bool keep = false;
-        long long c0 = 0, c1 = 0, c2 = 0, gt = 0;
-        if (cand) {
-          bool exact = !fixed;
-          if (fixed) {
-            c0 = q0 + p.Bfx[3 * nn + 0];
-            c1 = q1 + p.Bfx[3 * nn + 1];
-            c2 = q2 + p.Bfx[3 * nn + 2];
-            gt = gq + p.gBfx[nn];
-            const int k0 = (int)(c0 >> kFixBits), k1 = (int)(c1 >> kFixBits), k2 = (int)(c2 >> kFixBits);
-            const long long f0 = c0 & kFracMask, f1 = c1 & kFracMask, f2 = c2 & kFracMask;
-            const bool near = f0 < kFixFace || f0 > kFracMask - kFixFace || f1 < kFixFace ||
-                              f1 > kFracMask - kFixFace || f2 < kFixFace || f2 > kFracMask - kFixFace;
-            const bool reach = k0 >= -1 && k0 <= p.Ex && k1 >= -1 && k1 <= p.Ey && k2 >= -1 && k2 <= p.Ez;
-            exact = near && reach;
-            keep = !exact && (unsigned)k0 < (unsigned)p.Ex && (unsigned)k1 < (unsigned)p.Ey &&
-                   (unsigned)k2 < (unsigned)p.Ez;
-          }
-          if (exact) {
-            // the reference's arithmetic decides (a cell face within 1e-9 cells, or coordinates
-            // beyond the fixed point's range)
-            double y[3], c[3];
-            reference_transform(p, nn, x0, x1, x2, y, c);
-            keep = c[0] >= 0.0 && c[0] < (double)p.Ex && c[1] >= 0.0 && c[1] < (double)p.Ey && c[2] >= 0.0 &&
-                   c[2] < (double)p.Ez;
-            if (keep) {
-              long long cf[3];
-              for (int a = 0; a < 3; ++a) {
-                const double fl = floor(c[a]);
-                const long long fr = __double2ll_rn(__dsub_rn(c[a], fl) * kFixScale);
-                cf[a] = ((long long)fl << kFixBits) | (fr > kFracMask ? kFracMask : fr);
-              }
-              c0 = cf[0];
-              c1 = cf[1];
-              c2 = cf[2];
-              if (!fixed) {
-                const double cyc = dot3_rn(p.g[0], p.g[1], p.g[2], y[0], y[1], y[2]) * kInv2Pi;
-                gt = __double2ll_rn((cyc - rint(cyc)) * kFixScale);
-              }
-            }
-          }
-        }
+        long long c[3] = {0, 0, 0}, gt = 0;
+        const bool keep = cand && decide(p, a, nn, c, gt);
         const unsigned mask = __ballot_sync(0xffffffffu, keep);
         if (keep) {
-          const int k0 = (int)(c0 >> kFixBits), k1 = (int)(c1 >> kFixBits), k2 = (int)(c2 >> kFixBits);
+          const int k0 = (int)(c[0] >> kFixBits), k1 = (int)(c[1] >> kFixBits), k2 = (int)(c[2] >> kFixBits);
           const int cell = (int)p.cell_base + k0 + p.Ex * (k1 + p.Ey * k2);
           int64_t idx;
           int slot;
@@ -267,11 +279,13 @@ __global__ void __launch_bounds__(256) k_bin_atoms_fp32(const BinParams* __restr
             tmp_key[idx] = (int)((int64_t)nn * p.n_atoms + jj);
             tmp_cell[idx] = cell;
             tmp_slot[idx] = slot;
-            tmp_r[idx].p = make_float4(p.a_colf[0] * fix_frac_to_float(c0 & kFracMask),
-                                       p.a_colf[1] * fix_frac_to_float(c1 & kFracMask),
-                                       p.a_colf[2] * fix_frac_to_float(c2 & kFracMask),
-                                       __int_as_float(pack_cell(k0, k1, k2)));
-            tmp_r[idx].cs = make_float2(cf, sf);
+            // both 16-byte halves of the 32-byte record, so no sector is partly written
+            float4* rec = reinterpret_cast<float4*>(tmp_r + idx);
+            rec[0] = make_float4(p.a_colf[0] * fix_frac_to_float(c[0] & kFracMask),
+                                 p.a_colf[1] * fix_frac_to_float(c[1] & kFracMask),
+                                 p.a_colf[2] * fix_frac_to_float(c[2] & kFracMask),
+                                 __int_as_float(pack_cell(k0, k1, k2)));
+            rec[1] = make_float4(cf, sf, 0.0f, 0.0f);
           }
         }
       }
@@ -377,12 +391,10 @@ __global__ void __launch_bounds__(256) k_bin_place(const int* __restrict__ tmp_c
     perm[start[tmp_cell[i]] + tmp_slot[i]] = (int)i;
 }
 
-// Per cell: order the entries by candidate index (the reference's insertion
-// order) and write the records.  Cells of up to kRankRegs entries rank in
-// registers; larger cells rank from memory.
-constexpr int kRankRegs = 24;
-
-// FP64 path: the records from the exact offsets and g.y
+// Ordering: the entry at sorted position q (cell c, arrival slot order) moves to
+// start[c] + its rank by candidate index among the cell's entries (the reference's
+// insertion order).  One thread per kept atom; the threads of a cell read the same few
+// keys (L1 hits).
 __device__ __forceinline__ void write_record(const BinnedAtoms& b, int dst, const double4_32a& f, int packed,
                                              double a11, double a22, double a33) {
   b.p32[dst] = make_float4((float)(a11 * f.x), (float)(a22 * f.y), (float)(a33 * f.z), __int_as_float(packed));
@@ -392,61 +404,36 @@ __device__ __forceinline__ void write_record(const BinnedAtoms& b, int dst, cons
   b.cs64[dst] = make_double2(cs, sn);
 }
 
-// FP32 path: the binning wrote the records; they move to their place
-__device__ __forceinline__ void move_record(const BinnedAtoms& b, int dst, const Rec32* __restrict__ r) {
-  b.p32[dst] = r->p;
-  b.cs32[dst] = r->cs;
-}
-
 template <bool kFp32>
-__global__ void __launch_bounds__(128) k_bin_finalize(const BinParams* __restrict__ jobs, int n_jobs,
+__global__ void __launch_bounds__(256) k_bin_finalize(const BinParams* __restrict__ jobs, int n_jobs,
                                                       const int* __restrict__ start, const int* __restrict__ counts,
-                                                      int64_t n_cells, const int* __restrict__ perm,
-                                                      const int* __restrict__ tmp_key,
+                                                      const int* __restrict__ perm, const int* __restrict__ tmp_key,
+                                                      const int* __restrict__ tmp_cell,
                                                       const double4_32a* __restrict__ tmp_f, BinnedAtoms b,
                                                       const unsigned long long* __restrict__ counters, int64_t cap) {
-  if ((int64_t)counters[0] > cap) return;
-  const Rec32* tmp_r = reinterpret_cast<const Rec32*>(tmp_f);
-  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n_cells; c += (int64_t)gridDim.x * blockDim.x) {
-    const int job = n_jobs == 1 ? 0 : find_job(n_jobs, c, [&](int k) { return jobs[k].cell_base; });
-    const BinParams& p = jobs[job];
-    const int Ex = p.Ex, Ey = p.Ey;
-    const double a11 = p.a_col[0], a22 = p.a_col[1], a33 = p.a_col[2];
-    const int64_t cl = c - p.cell_base;
-    const int s = start[c], n = counts[c];
-    const int cz = (int)(cl / ((int64_t)Ex * Ey));
-    const int rem = (int)(cl - (int64_t)cz * Ex * Ey);
-    const int cy = rem / Ex, cx = rem - cy * Ex;
-    const int packed = pack_cell(cx, cy, cz);
-    if (n <= kRankRegs) {
-      int key[kRankRegs], ti[kRankRegs];
-#pragma unroll
-      for (int i = 0; i < kRankRegs; ++i) {
-        ti[i] = (i < n) ? perm[s + i] : 0;
-        key[i] = (i < n) ? tmp_key[ti[i]] : 0x7fffffff;
-      }
-#pragma unroll
-      for (int i = 0; i < kRankRegs; ++i) {
-        if (i >= n) break;
-        int r = 0;
-#pragma unroll
-        for (int j = 0; j < kRankRegs; ++j) r += (key[j] < key[i]);
-        if constexpr (kFp32)
-          move_record(b, s + r, tmp_r + ti[i]);
-        else
-          write_record(b, s + r, tmp_f[ti[i]], packed, a11, a22, a33);
-      }
+  const int64_t nkept = (int64_t)counters[0];
+  if (nkept > cap) return;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nkept; q += (int64_t)gridDim.x * blockDim.x) {
+    const int t = perm[q];
+    const int cell = tmp_cell[t];
+    const int key = tmp_key[t];
+    const int s = start[cell], n = counts[cell];
+    int r = 0;
+    for (int j = 0; j < n; ++j) r += (tmp_key[perm[s + j]] < key);
+    if constexpr (kFp32) {
+      // the binning wrote the records; they move to their place
+      const float4* rec = reinterpret_cast<const float4*>(tmp_f + t);
+      const float4 hi = rec[1];
+      b.p32[s + r] = rec[0];
+      b.cs32[s + r] = make_float2(hi.x, hi.y);
     } else {
-      for (int i = 0; i < n; ++i) {
-        const int t = perm[s + i];
-        const int ki = tmp_key[t];
-        int r = 0;
-        for (int j = 0; j < n; ++j) r += (tmp_key[perm[s + j]] < ki);
-        if constexpr (kFp32)
-          move_record(b, s + r, tmp_r + t);
-        else
-          write_record(b, s + r, tmp_f[t], packed, a11, a22, a33);
-      }
+      const int job = n_jobs == 1 ? 0 : find_job(n_jobs, cell, [&](int k) { return jobs[k].cell_base; });
+      const BinParams& p = jobs[job];
+      const int64_t cl = cell - p.cell_base;
+      const int cz = (int)(cl / ((int64_t)p.Ex * p.Ey));
+      const int rem = (int)(cl - (int64_t)cz * p.Ex * p.Ey);
+      const int cy = rem / p.Ex, cx = rem - cy * p.Ex;
+      write_record(b, s + r, tmp_f[t], pack_cell(cx, cy, cz), p.a_col[0], p.a_col[1], p.a_col[2]);
     }
   }
 }
@@ -484,16 +471,17 @@ cudaError_t launch_bin(const BinParams* d_jobs, int n_jobs, int64_t total_atoms,
 
 cudaError_t launch_bin_finalize(const BinParams* d_jobs, int n_jobs, int64_t total_cells, int64_t cap, Scratch& s,
                                 BinnedAtoms& b, bool fp32, cudaStream_t st) {
+  (void)total_cells;
   int dev = 0, sms = 148;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const int grid = grid_for(total_cells, 128, sms * 16);
+  const int grid = grid_for(cap, 256, sms * 8);  // the kernel reads the kept count on the device
   if (fp32)
-    k_bin_finalize<true><<<grid, 128, 0, st>>>(d_jobs, n_jobs, b.cell_start, b.cell_count, total_cells, s.perm,
-                                               s.tmp_key, s.tmp_f, b, s.counters, cap);
+    k_bin_finalize<true><<<grid, 256, 0, st>>>(d_jobs, n_jobs, b.cell_start, b.cell_count, s.perm, s.tmp_key,
+                                               s.tmp_cell, s.tmp_f, b, s.counters, cap);
   else
-    k_bin_finalize<false><<<grid, 128, 0, st>>>(d_jobs, n_jobs, b.cell_start, b.cell_count, total_cells, s.perm,
-                                                s.tmp_key, s.tmp_f, b, s.counters, cap);
+    k_bin_finalize<false><<<grid, 256, 0, st>>>(d_jobs, n_jobs, b.cell_start, b.cell_count, s.perm, s.tmp_key,
+                                                s.tmp_cell, s.tmp_f, b, s.counters, cap);
   return cudaGetLastError();
 }
 

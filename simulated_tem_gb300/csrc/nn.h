@@ -15,9 +15,11 @@ namespace nn {
 int conv_fwd(const __nv_bfloat16* x, int B, int H, int W, int Cin, const __nv_bfloat16* w, int Cout, int taps,
              const float* bias, int relu, const __nv_bfloat16* mask, void* y, int y_fp32, cudaStream_t st);
 
-// gw[co][t][ci] += sum over pixels of gy[p][co] x[p + d_t][ci] (FP32, accumulated).
+// gw[co][t][ci] += sum over pixels of gy[p][co] x[p + d_t][ci] (FP32, accumulated), the
+// partial sums of the pixel split in ws (conv_wgrad_workspace floats), added in a fixed order.
+size_t conv_wgrad_workspace(int B, int H, int W, int Cin, int Cout, int taps);
 int conv_wgrad(const __nv_bfloat16* x, const __nv_bfloat16* gy, int B, int H, int W, int Cin, int Cout, int taps,
-               float* gw, cudaStream_t st);
+               float* gw, float* ws, size_t ws_floats, cudaStream_t st);
 
 // wt[ci][taps - 1 - t][co] = w[co][t][ci]: input-gradient weights.
 int flip_transpose(const __nv_bfloat16* w, __nv_bfloat16* wt, int Cout, int taps, int Cin, cudaStream_t st);
@@ -32,7 +34,10 @@ int concat(const __nv_bfloat16* a, const __nv_bfloat16* b, __nv_bfloat16* y, lon
 int split(const __nv_bfloat16* gy, __nv_bfloat16* ga, __nv_bfloat16* gb, long long npix, int Ca, int Cb,
           cudaStream_t st);
 int relu_mask(__nv_bfloat16* g, const __nv_bfloat16* y, long long n, cudaStream_t st);
-int bias_grad(const __nv_bfloat16* g, float* gb, long long npix, int C, cudaStream_t st);
+// gb[c] += sum over pixels of g[p][c], per-block partial sums in ws (bias_grad_workspace
+// floats) added in block order.
+size_t bias_grad_workspace(int C);
+int bias_grad(const __nv_bfloat16* g, float* gb, long long npix, int C, float* ws, size_t ws_floats, cudaStream_t st);
 int mse(const float* pred, const float* target, const float* target1, __nv_bfloat16* g, float* loss, long long npix,
         int Cp, float w1, cudaStream_t st);
 int adam(float* w, float* m, float* v, const float* g, __nv_bfloat16* w16, long long n, float lr, float b1, float b2,

@@ -19,9 +19,14 @@ extern "C" int stn_conv2d_fwd(const void* x, int32_t B, int32_t H, int32_t W, in
                               int32_t y_fp32, void* stream) {
   return conv_fwd(cb(x), B, H, W, Cin, cb(w), Cout, taps, bias, relu, cb(mask), y, y_fp32, cs(stream));
 }
+extern "C" int64_t stn_conv2d_wgrad_workspace(int32_t B, int32_t H, int32_t W, int32_t Cin, int32_t Cout,
+                                              int32_t taps) {
+  return (int64_t)conv_wgrad_workspace(B, H, W, Cin, Cout, taps);
+}
 extern "C" int stn_conv2d_wgrad(const void* x, const void* gy, int32_t B, int32_t H, int32_t W, int32_t Cin,
-                                int32_t Cout, int32_t taps, float* gw, void* stream) {
-  return conv_wgrad(cb(x), cb(gy), B, H, W, Cin, Cout, taps, gw, cs(stream));
+                                int32_t Cout, int32_t taps, float* gw, float* ws, int64_t ws_floats, void* stream) {
+  if (ws_floats < 0) return 1;
+  return conv_wgrad(cb(x), cb(gy), B, H, W, Cin, Cout, taps, gw, ws, (size_t)ws_floats, cs(stream));
 }
 extern "C" int stn_weight_flip(const void* w, void* wt, int32_t Cout, int32_t taps, int32_t Cin, void* stream) {
   return flip_transpose(cb(w), mb(wt), Cout, taps, Cin, cs(stream));
@@ -47,8 +52,11 @@ extern "C" int stn_split(const void* gy, void* ga, void* gb, int64_t npix, int32
 extern "C" int stn_relu_mask(void* g, const void* y, int64_t n, void* stream) {
   return relu_mask(mb(g), cb(y), n, cs(stream));
 }
-extern "C" int stn_bias_grad(const void* g, float* gb, int64_t npix, int32_t C, void* stream) {
-  return bias_grad(cb(g), gb, npix, C, cs(stream));
+extern "C" int64_t stn_bias_grad_workspace(int32_t C) { return (int64_t)bias_grad_workspace(C); }
+extern "C" int stn_bias_grad(const void* g, float* gb, int64_t npix, int32_t C, float* ws, int64_t ws_floats,
+                             void* stream) {
+  if (ws_floats < 0) return 1;
+  return bias_grad(cb(g), gb, npix, C, ws, (size_t)ws_floats, cs(stream));
 }
 extern "C" int stn_mse(const float* pred, const float* target, const float* target1, void* g, float* loss,
                        int64_t npix, int32_t Cp, float w1, void* stream) {

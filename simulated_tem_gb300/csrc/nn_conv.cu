@@ -227,11 +227,13 @@ namespace {
 // transposed while staged (K-major tiles, p along K).  A CTA owns 128 output channels x
 // BN input channels x TG taps (TG x BN TMEM columns) for one range of pixels, in chunks
 // of 64 pixels; the A tile of a chunk serves all TG taps.  Partial sums over the CTA's
-// pixels are added to the FP32 gradient with reductions (red.global.add).
+// pixels go to the CTA's slice of a workspace (one slice per pixel split), which a second
+// kernel adds to the FP32 gradient in split order: the result does not depend on the
+// order in which CTAs finish (training is reproducible).
 struct WgradArgs {
   const __nv_bfloat16* x;   // [B][H][W][Cin]
   const __nv_bfloat16* gy;  // [B][H][W][Cout]
-  float* gw;                // [Cout][taps][Cin], accumulated into
+  float* ws;                // [splits][Cout][taps][Cin] partial sums
   int B, H, W, Cin, Cout, taps;
   int chunks_per_cta;       // 64-pixel chunks per CTA (pixel split)
 };
@@ -351,9 +353,9 @@ __global__ void __launch_bounds__(kThreads) k_conv_wgrad(const WgradArgs a) {
         tc::tmem_ld8(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(j * BN + col), v);
         const int ci = c0 + col;
         if (co < a.Cout && ci < a.Cin) {
-          float* dst = a.gw + ((size_t)co * a.taps + t0 + j) * a.Cin + ci;
-#pragma unroll
-          for (int i = 0; i < 8; ++i) atomicAdd(dst + i, v[i]);
+          float* dst = a.ws + (size_t)blockIdx.x * a.Cout * a.taps * a.Cin + ((size_t)co * a.taps + t0 + j) * a.Cin + ci;
+          reinterpret_cast<float4*>(dst)[0] = make_float4(v[0], v[1], v[2], v[3]);
+          reinterpret_cast<float4*>(dst)[1] = make_float4(v[4], v[5], v[6], v[7]);
         }
       }
     }
@@ -363,25 +365,52 @@ __global__ void __launch_bounds__(kThreads) k_conv_wgrad(const WgradArgs a) {
   if (warp == 0) tc::tmem_dealloc(tmem, kCols);
 }
 
+// gw[i] += sum over splits s (in order) of ws[s][i]
+__global__ void k_wgrad_reduce(const float* __restrict__ ws, int splits, long long n, float* __restrict__ gw) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    float s = 0.f;
+    for (int k = 0; k < splits; ++k) s += ws[(size_t)k * n + i];
+    gw[i] += s;
+  }
+}
+
+// Pixel split of a weight-gradient launch: about two waves of CTAs, at least 8 chunks per
+// CTA so the partial sums amortise.
 template <int BN, int TG>
-cudaError_t launch_wgrad(WgradArgs a, cudaStream_t st) {
-  const size_t smem = sizeof(WSmem<BN, TG>) + 1024;
-  cudaError_t e = cudaFuncSetAttribute(k_conv_wgrad<BN, TG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
+void wgrad_split(int B, int H, int W, int Cin, int Cout, int taps, int& splits, int& chunks_per_cta) {
   int dev = 0, sms = 148;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const int npix = a.B * a.H * a.W;
+  const int npix = B * H * W;
   const int chunks = (npix + 63) / 64;
-  const int tiles = ((a.Cout + 127) / 128) * ((a.Cin + BN - 1) / BN) * ((a.taps + TG - 1) / TG);
-  // about two waves of CTAs; at least 8 chunks per CTA so the partial sums amortise
-  int splits = (2 * sms + tiles - 1) / tiles;
+  const int tiles = ((Cout + 127) / 128) * ((Cin + BN - 1) / BN) * ((taps + TG - 1) / TG);
+  splits = (2 * sms + tiles - 1) / tiles;
   splits = max(1, min(splits, (chunks + 7) / 8));
-  a.chunks_per_cta = (chunks + splits - 1) / splits;
-  splits = (chunks + a.chunks_per_cta - 1) / a.chunks_per_cta;
+  chunks_per_cta = (chunks + splits - 1) / splits;
+  splits = (chunks + chunks_per_cta - 1) / chunks_per_cta;
+}
+
+template <int BN, int TG>
+cudaError_t launch_wgrad(WgradArgs a, float* gw, size_t ws_floats, cudaStream_t st) {
+  const size_t smem = sizeof(WSmem<BN, TG>) + 1024;
+  cudaError_t e = cudaFuncSetAttribute(k_conv_wgrad<BN, TG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  int splits = 1;
+  wgrad_split<BN, TG>(a.B, a.H, a.W, a.Cin, a.Cout, a.taps, splits, a.chunks_per_cta);
+  const long long n = (long long)a.Cout * a.taps * a.Cin;
+  if ((size_t)splits * (size_t)n > ws_floats) return cudaErrorInvalidValue;
   dim3 grid(splits, (a.Cout + 127) / 128, ((a.Cin + BN - 1) / BN) * ((a.taps + TG - 1) / TG));
   k_conv_wgrad<BN, TG><<<grid, kThreads, smem, st>>>(a);
+  const long long blocks = (n + 255) / 256;
+  k_wgrad_reduce<<<(int)(blocks < 1024 ? blocks : 1024), 256, 0, st>>>(a.ws, splits, n, gw);
   return cudaGetLastError();
+}
+
+template <int BN, int TG>
+size_t wgrad_ws(int B, int H, int W, int Cin, int Cout, int taps) {
+  int splits = 1, cpc = 1;
+  wgrad_split<BN, TG>(B, H, W, Cin, Cout, taps, splits, cpc);
+  return (size_t)splits * Cout * taps * Cin;
 }
 
 // wt[ci][8 - t][co] = w[co][t][ci] (taps 9) or wt[ci][0][co] = w[co][0][ci]: the weights
@@ -399,17 +428,33 @@ __global__ void k_flip_transpose(const __nv_bfloat16* __restrict__ w, __nv_bfloa
 
 }  // namespace
 
+bool wgrad_args_ok(int B, int H, int W, int Cin, int Cout, int taps) {
+  if (B < 1 || H < 1 || W < 1) return false;
+  if (Cin < 8 || Cin % 8 != 0 || Cout < 8 || Cout % 8 != 0 || (taps != 1 && taps != 9)) return false;
+  return (long long)B * H * W < (1LL << 31);
+}
+
+size_t conv_wgrad_workspace(int B, int H, int W, int Cin, int Cout, int taps) {
+  if (!wgrad_args_ok(B, H, W, Cin, Cout, taps)) return 0;
+  if (taps == 1)
+    return Cin <= 32 ? wgrad_ws<32, 1>(B, H, W, Cin, Cout, taps)
+                     : Cin <= 64 ? wgrad_ws<64, 1>(B, H, W, Cin, Cout, taps) : wgrad_ws<128, 1>(B, H, W, Cin, Cout, taps);
+  return Cin <= 32 ? wgrad_ws<32, 9>(B, H, W, Cin, Cout, taps)
+                   : Cin <= 64 ? wgrad_ws<64, 3>(B, H, W, Cin, Cout, taps) : wgrad_ws<128, 3>(B, H, W, Cin, Cout, taps);
+}
+
 int conv_wgrad(const __nv_bfloat16* x, const __nv_bfloat16* gy, int B, int H, int W, int Cin, int Cout, int taps,
-               float* gw, cudaStream_t st) {
-  if (!x || !gy || !gw || B < 1 || H < 1 || W < 1) return 1;
-  if (Cin < 8 || Cin % 8 != 0 || Cout < 8 || Cout % 8 != 0 || (taps != 1 && taps != 9)) return 1;
-  if ((long long)B * H * W >= (1LL << 31)) return 1;
-  WgradArgs a{x, gy, gw, B, H, W, Cin, Cout, taps, 1};
+               float* gw, float* ws, size_t ws_floats, cudaStream_t st) {
+  if (!x || !gy || !gw || !ws || !wgrad_args_ok(B, H, W, Cin, Cout, taps)) return 1;
+  if (ws_floats < conv_wgrad_workspace(B, H, W, Cin, Cout, taps)) return 1;
+  WgradArgs a{x, gy, ws, B, H, W, Cin, Cout, taps, 1};
   cudaError_t e;
   if (taps == 1)
-    e = Cin <= 32 ? launch_wgrad<32, 1>(a, st) : Cin <= 64 ? launch_wgrad<64, 1>(a, st) : launch_wgrad<128, 1>(a, st);
+    e = Cin <= 32 ? launch_wgrad<32, 1>(a, gw, ws_floats, st)
+                  : Cin <= 64 ? launch_wgrad<64, 1>(a, gw, ws_floats, st) : launch_wgrad<128, 1>(a, gw, ws_floats, st);
   else
-    e = Cin <= 32 ? launch_wgrad<32, 9>(a, st) : Cin <= 64 ? launch_wgrad<64, 3>(a, st) : launch_wgrad<128, 3>(a, st);
+    e = Cin <= 32 ? launch_wgrad<32, 9>(a, gw, ws_floats, st)
+                  : Cin <= 64 ? launch_wgrad<64, 3>(a, gw, ws_floats, st) : launch_wgrad<128, 3>(a, gw, ws_floats, st);
   return e == cudaSuccess ? 0 : 2;
 }
 

@@ -128,17 +128,40 @@ __global__ void k_relu_mask(__nv_bfloat16* __restrict__ g, const __nv_bfloat16* 
     if (!(bf(y[i]) > 0.f)) g[i] = tobf(0.f);
 }
 
-// gb[c] += sum_p g[p, c]: per-block partial sums in shared FP32, one global reduction per
-// channel and block
-__global__ void k_bias_grad(const __nv_bfloat16* __restrict__ g, float* __restrict__ gb, long long npix, int C) {
-  extern __shared__ float part[];
-  for (int c = threadIdx.x; c < C; c += blockDim.x) part[c] = 0.f;
-  __syncthreads();
-  const long long n = npix * C;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-    atomicAdd(&part[i % C], bf(g[i]));
-  __syncthreads();
-  for (int c = threadIdx.x; c < C; c += blockDim.x) atomicAdd(&gb[c], part[c]);
+// gb[c] += sum_p g[p, c] in a fixed order: block b sums the pixels of its range (thread
+// (r, c) the pixels r, r + R, ... of it, R = 256 / C rows of threads, then the rows in
+// order) into part[b][c]; a second kernel adds the blocks' sums in block order.
+constexpr int kBiasBlocks = 256;
+
+__global__ void k_bias_grad_part(const __nv_bfloat16* __restrict__ g, float* __restrict__ part, long long npix,
+                                 int C) {
+  extern __shared__ float rows_sum[];  // [R][Cg]
+  const long long per = (npix + gridDim.x - 1) / gridDim.x;
+  const long long p0 = blockIdx.x * per, p1 = min(npix, p0 + per);
+  for (int c0 = 0; c0 < C; c0 += blockDim.x) {
+    const int Cg = min((int)blockDim.x, C - c0);
+    const int R = blockDim.x / Cg;
+    const int r = threadIdx.x / Cg, c = threadIdx.x - r * Cg;
+    float s = 0.f;
+    if (r < R)
+      for (long long p = p0 + r; p < p1; p += R) s += bf(g[p * C + c0 + c]);
+    if (r < R) rows_sum[r * Cg + c] = s;
+    __syncthreads();
+    if (threadIdx.x < Cg) {
+      float t = 0.f;
+      for (int k = 0; k < R; ++k) t += rows_sum[k * Cg + threadIdx.x];
+      part[(size_t)blockIdx.x * C + c0 + threadIdx.x] = t;
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void k_bias_grad_sum(const float* __restrict__ part, int nb, int C, float* __restrict__ gb) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < C; c += gridDim.x * blockDim.x) {
+    float t = 0.f;
+    for (int b = 0; b < nb; ++b) t += part[(size_t)b * C + c];
+    gb[c] += t;
+  }
 }
 
 // loss = mean_p (pred[p, 0] - target[p])^2 + w1 mean_p (pred[p, 1] - t1[p])^2 over npix
@@ -211,19 +234,20 @@ __global__ void k_add(__nv_bfloat16* __restrict__ a, const __nv_bfloat16* __rest
     a[i] = tobf(bf(a[i]) + bf(b[i]));
 }
 
-// mean[0] += sum of img / n (FP64); mean must be zeroed before
-__global__ void k_image_mean(const double* __restrict__ img, long long n, double* __restrict__ mean) {
-  __shared__ double red[kBlock / 32];
+// mean[0] = sum of img / n (FP64), one block in a fixed order (the images are coarse:
+// a few 1e5 pixels)
+__global__ void __launch_bounds__(1024) k_image_mean(const double* __restrict__ img, long long n,
+                                                     double* __restrict__ mean) {
+  __shared__ double red[32];
   double s = 0.0;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-    s += img[i];
+  for (long long i = threadIdx.x; i < n; i += blockDim.x) s += img[i];
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
   __syncthreads();
   if (threadIdx.x == 0) {
     double t = 0.0;
     for (int w = 0; w < (int)(blockDim.x / 32); ++w) t += red[w];
-    atomicAdd(mean, t / (double)n);
+    mean[0] = t / (double)n;
   }
 }
 
@@ -342,11 +366,11 @@ int relu_mask(__nv_bfloat16* g, const __nv_bfloat16* y, long long n, cudaStream_
   k_relu_mask<<<grid_for(n), kBlock, 0, st>>>(g, y, n);
   return status();
 }
-int bias_grad(const __nv_bfloat16* g, float* gb, long long npix, int C, cudaStream_t st) {
-  if (!g || !gb || C < 1 || C > 4096) return 1;
-  long long n = npix * C;
-  int grid = grid_for(n / 16);
-  k_bias_grad<<<grid, kBlock, C * sizeof(float), st>>>(g, gb, npix, C);
+size_t bias_grad_workspace(int C) { return C < 1 ? 0 : (size_t)kBiasBlocks * C; }
+int bias_grad(const __nv_bfloat16* g, float* gb, long long npix, int C, float* ws, size_t ws_floats, cudaStream_t st) {
+  if (!g || !gb || !ws || C < 1 || C > 4096 || npix < 0 || ws_floats < bias_grad_workspace(C)) return 1;
+  k_bias_grad_part<<<kBiasBlocks, 256, 256 * sizeof(float), st>>>(g, ws, npix, C);
+  k_bias_grad_sum<<<(C + 255) / 256, 256, 0, st>>>(ws, kBiasBlocks, C, gb);
   return status();
 }
 int mse(const float* pred, const float* target, const float* target1, __nv_bfloat16* g, float* loss, long long npix,
@@ -378,8 +402,7 @@ int add(__nv_bfloat16* a, const __nv_bfloat16* b, long long n, cudaStream_t st) 
 }
 int image_mean(const double* img, long long n, double* mean, cudaStream_t st) {
   if (!img || !mean || n < 1) return 1;
-  if (cudaMemsetAsync(mean, 0, sizeof(double), st) != cudaSuccess) return 2;
-  k_image_mean<<<grid_for(n) < 1024 ? grid_for(n) : 1024, kBlock, 0, st>>>(img, n, mean);
+  k_image_mean<<<1, 1024, 0, st>>>(img, n, mean);
   return status();
 }
 int resample_planes(const double* img2, int Mx2, int My2, int Mx8, int My8, int Wp, int Hp, float sg_value,

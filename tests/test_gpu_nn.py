@@ -80,6 +80,10 @@ def test_conv_backward_matches_oracle(nn, B, H, W, Cin, Cout, taps):
     assert nn.last_kernel_error() == 0
     want_w = NO.conv2d_grad_weight(x, gy, taps)
     assert np.abs(gw.cpu().numpy() - want_w).max() <= 1e-5 * np.abs(want_w).max() + 1e-6
+    # the partial sums of the pixel split are added in a fixed order: the same bits every time
+    gw2 = torch.zeros_like(gw)
+    nn.conv2d_wgrad(_bf16(x), _bf16(gy), taps, gw2)
+    assert torch.equal(gw, gw2)
 
 
 def test_elementwise_layers_match_oracle(nn):
@@ -105,6 +109,14 @@ def test_elementwise_layers_match_oracle(nn):
     gbias = torch.zeros(32, dtype=torch.float32, device="cuda")
     nn.bias_grad(_bf16(x), gbias)
     assert np.allclose(gbias.cpu().numpy(), NO.conv2d_grad_bias(x), rtol=1e-5, atol=1e-4)
+    gbias2 = torch.zeros_like(gbias)
+    nn.bias_grad(_bf16(x), gbias2)
+    assert torch.equal(gbias, gbias2)
+    # wide layers: more channels than threads of a block
+    big = _rand(rng, 3, 7, 9, 512)
+    gbig = torch.zeros(512, dtype=torch.float32, device="cuda")
+    nn.bias_grad(_bf16(big), gbig)
+    assert np.allclose(gbig.cpu().numpy(), NO.conv2d_grad_bias(big), rtol=1e-5, atol=1e-4)
     pred = rng.standard_normal((3, 9, 10, 16)).astype(np.float32)
     tgt = rng.standard_normal((3, 9, 10)).astype(np.float32)
     loss = torch.zeros(1, dtype=torch.float32, device="cuda")
