@@ -1,19 +1,29 @@
 // Convolution kernels of the learned corrector on the fifth-generation tensor cores.
 //
-// A 3 x 3 ("same" padding) or 1 x 1 convolution over NHWC BF16 activations is an
-// implicit GEMM: D[p, co] = sum_k A[p, k] B[co, k] with p the output pixel, k = (tap,
-// ci) and A gathered from the input on the fly (zero outside the image).  A CTA of four
-// warps owns 128 pixels x BN output channels; the FP32 accumulator lives in TMEM
-// (BN columns).  K advances in chunks of KC = min(64, Cin) channels of one tap: all
-// threads gather the A and B chunk into shared memory (two stages, so gathering chunk
-// c + 1 overlaps the MMAs of chunk c), one thread issues the tcgen05 MMAs (K = 16 each)
-// and commits them to the stage's mbarrier.  The epilogue reads TMEM with tcgen05.ld,
-// adds the bias, applies ReLU and stores BF16 (or FP32) NHWC.
+// Forward (and input-gradient) convolution, 3 x 3 ("same" padding) or 1 x 1, over NHWC
+// BF16 activations: an implicit GEMM D[p, co] = sum_k A[p, k] B[co, k], p the output
+// pixel, k = (tap, ci).  A CTA owns 128 consecutive pixels of one image row x BN output
+// channels; the FP32 accumulator lives in TMEM (BN columns).  No thread touches the
+// operands: one thread moves them with TMA, one issues the MMAs, and the epilogue reads
+// TMEM.
+//
+// Per chunk of KC input channels the producer loads a halo tile: the input rows y - 1,
+// y, y + 1 (one row for 1 x 1), pixels x0 - 1 .. x0 + 128, as (KC / 8) slabs of 130 rows
+// x 16 bytes (8 channels) per input row.  In such a slab the rows are 16 bytes apart, so
+// the K-major core matrices (8 rows x 16 bytes) of the pixels shifted by dx start 16 dx
+// bytes further: all nine taps read the same tile through shifted descriptors (LBO =
+// slab pitch between 8-channel groups, SBO = 128 between 8-pixel groups).  Outside the
+// image the TMA box is zero-filled: the padding.  The weights of each (tap, chunk) come
+// by TMA into a ring of B slots ([BN rows][16 bytes] per 8-channel group).  mbarriers
+// pace the two rings (full: TMA transaction bytes; empty: the MMAs' commit).
 //
 // Every wait on an mbarrier is bounded; a wait that runs out records an error in
-// g_nn_error, waits once more (bounded) for the MMAs in flight and still frees TMEM.
+// g_nn_error, the producer waits (bounded) for every load it issued, the MMAs issued so
+// far are waited for, and TMEM is always freed.
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
 #include <stdint.h>
 
 #include "nn.h"
@@ -28,150 +38,170 @@ namespace {
 
 constexpr int kThreads = 128;
 constexpr uint32_t kWaitLimit = 1u << 20;  // polls of an mbarrier before giving up (about a second)
+constexpr int kTileX = 128;                // output pixels per CTA (one image row)
+constexpr int kHalo = kTileX + 2;          // input pixels per halo row
+constexpr int kSlab = 2176;                // bytes per (input row, 8 channels) slab: 130 x 16 rounded to 128
+constexpr int kBSlots = 4;                 // weight ring depth
 
 struct ConvArgs {
-  const __nv_bfloat16* x;     // [B][H][W][Cin]
-  const __nv_bfloat16* w;     // [Cout][taps][Cin]
   const float* bias;          // [Cout] or null
   const __nv_bfloat16* mask;  // [B][H][W][Cout] or null: outputs where mask <= 0 are zeroed
   void* y;                    // [B][H][W][Cout], BF16 or FP32
   int B, H, W, Cin, Cout, taps, relu, y_fp32;
+  int n_ntiles;               // output-channel tiles (grid z = B * n_ntiles)
 };
 
-template <int BN, int KC>
-struct Smem {
-  alignas(1024) unsigned char a[2][128 * KC * 2];
-  alignas(1024) unsigned char b[2][BN * KC * 2];
-  alignas(8) unsigned long long mbar[2];
+template <int BN, int KC, int NR>
+struct TSmem {
+  alignas(1024) unsigned char a[2][NR * (KC / 8) * kSlab];
+  alignas(1024) unsigned char b[kBSlots][(KC / 8) * BN * 16];
+  alignas(8) unsigned long long a_full[2], a_empty[2], b_full[kBSlots], b_empty[kBSlots], done;
   uint32_t tmem;
 };
 
-// Gather chunk (tap, ci0) of A (128 pixels from p0) and B (BN output channels from n0).
-template <int BN, int KC>
-__device__ __forceinline__ void gather(const ConvArgs& a, int p0, int n0, int tap, int ci0, unsigned char* sa,
-                                       unsigned char* sb) {
-  const int t = threadIdx.x;
-  const int npix = a.B * a.H * a.W;
-  const int dy = a.taps == 9 ? tap / 3 - 1 : 0, dx = a.taps == 9 ? tap % 3 - 1 : 0;
-  // A: thread t owns pixel row t; KC / 8 units of 16 bytes
-  {
-    const int p = p0 + t;
-    const __nv_bfloat16* src = nullptr;
-    if (p < npix) {
-      const int xw = p % a.W;
-      const int rest = p / a.W;
-      const int yh = rest % a.H, b = rest / a.H;
-      const int yy = yh + dy, xx = xw + dx;
-      if (yy >= 0 && yy < a.H && xx >= 0 && xx < a.W)
-        src = a.x + (((size_t)b * a.H + yy) * a.W + xx) * a.Cin + ci0;
-    }
-#pragma unroll
-    for (int u = 0; u < KC / 8; ++u) {
-      uint4 v = make_uint4(0u, 0u, 0u, 0u);
-      if (src) v = *reinterpret_cast<const uint4*>(src + 8 * u);
-      *reinterpret_cast<uint4*>(sa + tc::tile_offset(t, 8 * u, KC)) = v;
-    }
-  }
-  // B: BN rows of KC
-#pragma unroll
-  for (int r = t; r < BN; r += kThreads) {
-    const int n = n0 + r;
-    const __nv_bfloat16* src = n < a.Cout ? a.w + ((size_t)n * a.taps + tap) * a.Cin + ci0 : nullptr;
-#pragma unroll
-    for (int u = 0; u < KC / 8; ++u) {
-      uint4 v = make_uint4(0u, 0u, 0u, 0u);
-      if (src) v = *reinterpret_cast<const uint4*>(src + 8 * u);
-      *reinterpret_cast<uint4*>(sb + tc::tile_offset(r, 8 * u, KC)) = v;
-    }
-  }
-}
-
-template <int BN, int KC>
-__global__ void __launch_bounds__(kThreads) k_conv_fwd(const ConvArgs a) {
+// NR = 3 input rows for a 3 x 3 convolution, 1 for 1 x 1 (then taps = 1).
+template <int BN, int KC, int NR>
+__global__ void __launch_bounds__(kThreads) k_conv_fwd(const ConvArgs a, const __grid_constant__ CUtensorMap tmx,
+                                                       const __grid_constant__ CUtensorMap tmw) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
-  Smem<BN, KC>& S = *reinterpret_cast<Smem<BN, KC>*>(
+  TSmem<BN, KC, NR>& S = *reinterpret_cast<TSmem<BN, KC, NR>*>(
       smem_raw + ((1024 - ((uintptr_t)smem_raw & 1023)) & 1023));
-  const int t = threadIdx.x, warp = t >> 5;
-  const int p0 = blockIdx.x * 128, n0 = blockIdx.y * BN;
+  constexpr int kTaps = NR == 3 ? 9 : 1;
+  constexpr int kG = KC / 8;                        // 8-channel groups per chunk
+  constexpr uint32_t kBytesA = NR * kG * kHalo * 16;
+  constexpr uint32_t kBytesB = kG * BN * 16;
+  constexpr uint32_t kCols = BN < 32 ? 32 : BN;
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  const int x0 = blockIdx.x * kTileX, yrow = blockIdx.y;
+  const int img = blockIdx.z / a.n_ntiles, n0 = (blockIdx.z % a.n_ntiles) * BN;
+  const int nchunks = a.Cin / KC;
 
-  if (warp == 0) tc::tmem_alloc(tc::smem_addr(&S.tmem), BN < 32 ? 32 : BN);
+  if (warp == 0) tc::tmem_alloc(tc::smem_addr(&S.tmem), kCols);
   if (t == 0) {
-    tc::mbar_init(tc::smem_addr(&S.mbar[0]), 1);
-    tc::mbar_init(tc::smem_addr(&S.mbar[1]), 1);
+    for (int i = 0; i < 2; ++i) {
+      tc::mbar_init(tc::smem_addr(&S.a_full[i]), 1);
+      tc::mbar_init(tc::smem_addr(&S.a_empty[i]), 1);
+    }
+    for (int i = 0; i < kBSlots; ++i) {
+      tc::mbar_init(tc::smem_addr(&S.b_full[i]), 1);
+      tc::mbar_init(tc::smem_addr(&S.b_empty[i]), 1);
+    }
+    tc::mbar_init(tc::smem_addr(&S.done), 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = S.tmem;
-
-  const int chunks_per_tap = a.Cin / KC;
-  const int nchunks = a.taps * chunks_per_tap;
-  constexpr uint32_t idesc = tc::make_idesc_bf16(128, BN);
-  // every decision to go on is CTA-uniform (__syncthreads_and), so no thread leaves a
-  // barrier or a warp-collective TMEM load behind
   bool ok = true;
-  int issued = 0;  // chunks whose MMAs were issued
-  for (int c = 0; c < nchunks; ++c) {
-    const int st = c & 1;
-    if (c >= 2) ok = tc::mbar_wait(tc::smem_addr(&S.mbar[st]), ((c - 2) >> 1) & 1, kWaitLimit);
-    ok = __syncthreads_and(ok);
-    if (!ok) break;
-    gather<BN, KC>(a, p0, n0, c / chunks_per_tap, (c % chunks_per_tap) * KC, S.a[st], S.b[st]);
-    tc::fence_proxy_async_smem();
-    __syncthreads();
-    if (t == 0) {
-      tc::fence_after_sync();
-      const uint32_t sa = tc::smem_addr(S.a[st]), sb = tc::smem_addr(S.b[st]);
-#pragma unroll
-      for (int s = 0; s < KC / 16; ++s)
-        tc::mma_bf16(tmem, tc::make_desc(sa + 256 * s, 128, KC * 16), tc::make_desc(sb + 256 * s, 128, KC * 16),
-                     idesc, (c > 0 || s > 0) ? 1u : 0u);
-      tc::mma_commit(tc::smem_addr(&S.mbar[st]));
+
+  if (warp == 0 && lane == 0) {
+    // producer: halo tiles and weight slots, in the order the MMAs consume them
+    int na[2] = {0, 0}, nb[kBSlots] = {0, 0, 0, 0};  // loads armed per stage / slot
+    int jb = 0;
+    for (int c = 0; c < nchunks && ok; ++c) {
+      const int sa = c & 1;
+      if (c >= 2 && !tc::mbar_wait(tc::smem_addr(&S.a_empty[sa]), ((c - 2) >> 1) & 1, kWaitLimit)) {
+        ok = false;
+        break;
+      }
+      const uint32_t fa = tc::smem_addr(&S.a_full[sa]);
+      tc::mbar_arrive_expect_tx(fa, kBytesA);
+      ++na[sa];
+      for (int r = 0; r < NR; ++r)
+        for (int g = 0; g < kG; ++g)
+          tc::tma_load_4d(tc::smem_addr(S.a[sa] + (r * kG + g) * kSlab), &tmx, c * KC + 8 * g, x0 - 1,
+                          yrow + r - (NR == 3 ? 1 : 0), img, fa);
+      for (int tap = 0; tap < kTaps; ++tap, ++jb) {
+        const int sb = jb % kBSlots;
+        if (jb >= kBSlots && !tc::mbar_wait(tc::smem_addr(&S.b_empty[sb]), (jb / kBSlots - 1) & 1, kWaitLimit)) {
+          ok = false;
+          break;
+        }
+        const uint32_t fb = tc::smem_addr(&S.b_full[sb]);
+        tc::mbar_arrive_expect_tx(fb, kBytesB);
+        ++nb[sb];
+        for (int g = 0; g < kG; ++g)
+          tc::tma_load_3d(tc::smem_addr(S.b[sb] + g * BN * 16), &tmw, c * KC + 8 * g, tap, n0, fb);
+      }
     }
-    issued = c + 1;
+    // every load issued has landed before the CTA may leave (bounded)
+    for (int i = 0; i < 2; ++i)
+      if (na[i] > 0 && !tc::mbar_wait(tc::smem_addr(&S.a_full[i]), (na[i] - 1) & 1, kWaitLimit)) ok = false;
+    for (int i = 0; i < kBSlots; ++i)
+      if (nb[i] > 0 && !tc::mbar_wait(tc::smem_addr(&S.b_full[i]), (nb[i] - 1) & 1, kWaitLimit)) ok = false;
+  } else if (warp == 1 && lane == 0) {
+    // MMA issuer
+    constexpr uint32_t idesc = tc::make_idesc_bf16(128, BN);
+    int jb = 0;
+    bool first = true;
+    for (int c = 0; c < nchunks && ok; ++c) {
+      const int sa = c & 1;
+      if (!tc::mbar_wait(tc::smem_addr(&S.a_full[sa]), (c >> 1) & 1, kWaitLimit)) {
+        ok = false;
+        break;
+      }
+      const uint32_t abase = tc::smem_addr(S.a[sa]);
+      for (int tap = 0; tap < kTaps; ++tap, ++jb) {
+        const int sb = jb % kBSlots;
+        if (!tc::mbar_wait(tc::smem_addr(&S.b_full[sb]), (jb / kBSlots) & 1, kWaitLimit)) {
+          ok = false;
+          break;
+        }
+        tc::fence_after_sync();
+        const int dy = NR == 3 ? tap / 3 : 0, dx = NR == 3 ? tap % 3 : 1;  // halo row / column offset
+        const uint32_t bbase = tc::smem_addr(S.b[sb]);
+#pragma unroll
+        for (int s = 0; s < KC / 16; ++s) {
+          const uint64_t ad = tc::make_desc(abase + (dy * kG + 2 * s) * kSlab + dx * 16, kSlab, 128);
+          const uint64_t bd = tc::make_desc(bbase + 2 * s * BN * 16, BN * 16, 128);
+          tc::mma_bf16(tmem, ad, bd, idesc, first ? 0u : 1u);
+          first = false;
+        }
+        tc::mma_commit(tc::smem_addr(&S.b_empty[sb]));
+      }
+      if (!ok) break;
+      tc::mma_commit(tc::smem_addr(&S.a_empty[sa]));
+    }
+    tc::mma_commit(tc::smem_addr(&S.done));  // arrives when every MMA issued above has completed
   }
-  // the last commit covers every MMA issued before it
-  if (issued > 0) {
-    const int last = issued - 1;
-    bool done = tc::mbar_wait(tc::smem_addr(&S.mbar[last & 1]), (last >> 1) & 1, kWaitLimit);
-    done = __syncthreads_and(done);
-    if (!done) tc::mbar_wait(tc::smem_addr(&S.mbar[last & 1]), (last >> 1) & 1, kWaitLimit);
-    ok = ok && done;
-  }
+  __syncwarp();
+  // everyone: the accumulator is complete (bounded wait; the MMA thread always commits)
+  bool done = tc::mbar_wait(tc::smem_addr(&S.done), 0, kWaitLimit);
+  ok = __syncthreads_and(ok && done);
   if (!ok && t == 0) atomicCAS(&g_nn_error, 0, 1);
   tc::fence_after_sync();
 
   if (ok) {
-    // epilogue: warp w holds TMEM lanes (pixels) 32w .. 32w + 31
-    const int p = p0 + 32 * warp + (t & 31);
-    const int npix = a.B * a.H * a.W;
+    // epilogue: warp w holds TMEM lanes (pixels x0 + 32w .. x0 + 32w + 31)
+    const int xw = x0 + 32 * warp + lane;
+    const size_t p = ((size_t)img * a.H + yrow) * a.W + xw;
     for (int col = 0; col < BN; col += 8) {
       float v[8];
       tc::tmem_ld8(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)col, v);
       const int n = n0 + col;
-      if (p < npix && n < a.Cout) {
+      if (xw < a.W && n < a.Cout) {
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
           if (a.bias) v[i] += a.bias[n + i];
           if (a.relu) v[i] = fmaxf(v[i], 0.f);
         }
         if (a.mask) {  // gradient through the ReLU that produced this layer's input
-          const uint4 mv = *reinterpret_cast<const uint4*>(a.mask + (size_t)p * a.Cout + n);
+          const uint4 mv = *reinterpret_cast<const uint4*>(a.mask + p * a.Cout + n);
           const __nv_bfloat16* m = reinterpret_cast<const __nv_bfloat16*>(&mv);
 #pragma unroll
           for (int i = 0; i < 8; ++i)
             if (!(__bfloat162float(m[i]) > 0.f)) v[i] = 0.f;
         }
         if (a.y_fp32) {
-          float* dst = reinterpret_cast<float*>(a.y) + (size_t)p * a.Cout + n;
+          float* dst = reinterpret_cast<float*>(a.y) + p * a.Cout + n;
           *reinterpret_cast<float4*>(dst) = make_float4(v[0], v[1], v[2], v[3]);
           *reinterpret_cast<float4*>(dst + 4) = make_float4(v[4], v[5], v[6], v[7]);
         } else {
           __align__(16) __nv_bfloat162 h[4];
 #pragma unroll
           for (int i = 0; i < 4; ++i) h[i] = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
-          *reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(a.y) + (size_t)p * a.Cout + n) =
+          *reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(a.y) + p * a.Cout + n) =
               *reinterpret_cast<const uint4*>(h);
         }
       }
@@ -179,42 +209,80 @@ __global__ void __launch_bounds__(kThreads) k_conv_fwd(const ConvArgs a) {
   }
   tc::fence_before_sync();
   __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(tmem, BN < 32 ? 32 : BN);
+  if (warp == 0) tc::tmem_dealloc(tmem, kCols);
 }
 
-template <int BN, int KC>
-cudaError_t launch_fwd(const ConvArgs& a, cudaStream_t st) {
-  const size_t smem = sizeof(Smem<BN, KC>) + 1024;
-  cudaError_t e = cudaFuncSetAttribute(k_conv_fwd<BN, KC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link to libcuda)
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+// BF16 tensor map of `rank` dims (innermost first) with a box; zero fill outside.
+bool make_map(CUtensorMap* m, const void* base, int rank, const cuuint64_t* dims, const cuuint64_t* strides_bytes,
+              const cuuint32_t* box) {
+  PFN_cuTensorMapEncodeTiled_v12000 fn = encode_fn();
+  if (!fn) return false;
+  const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, (cuuint32_t)rank, const_cast<void*>(base), dims, strides_bytes, box,
+            estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int BN, int KC, int NR>
+cudaError_t launch_fwd(const __nv_bfloat16* x, const __nv_bfloat16* w, ConvArgs a, cudaStream_t st) {
+  CUtensorMap tmx, tmw;
+  const cuuint64_t xd[4] = {(cuuint64_t)a.Cin, (cuuint64_t)a.W, (cuuint64_t)a.H, (cuuint64_t)a.B};
+  const cuuint64_t xs[3] = {(cuuint64_t)a.Cin * 2, (cuuint64_t)a.W * a.Cin * 2, (cuuint64_t)a.H * a.W * a.Cin * 2};
+  const cuuint32_t xb[4] = {8, kHalo, 1, 1};
+  const cuuint64_t wd[3] = {(cuuint64_t)a.Cin, (cuuint64_t)a.taps, (cuuint64_t)a.Cout};
+  const cuuint64_t ws[2] = {(cuuint64_t)a.Cin * 2, (cuuint64_t)a.taps * a.Cin * 2};
+  const cuuint32_t wb[3] = {8, 1, (cuuint32_t)BN};
+  if (!make_map(&tmx, x, 4, xd, xs, xb) || !make_map(&tmw, w, 3, wd, ws, wb)) return cudaErrorInvalidValue;
+  // shared memory also caps the CTAs per SM so that their TMEM columns fit in 512 (an
+  // allocation beyond that would wait for another CTA to finish)
+  constexpr size_t kCols = BN < 32 ? 32 : BN;
+  const size_t need = sizeof(TSmem<BN, KC, NR>) + 1024, floor_tmem = 232448 / (512 / kCols) - 1023;
+  const size_t smem = need > floor_tmem ? need : floor_tmem;
+  cudaError_t e =
+      cudaFuncSetAttribute(k_conv_fwd<BN, KC, NR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  const int npix = a.B * a.H * a.W;
-  dim3 grid((npix + 127) / 128, (a.Cout + BN - 1) / BN);
-  k_conv_fwd<BN, KC><<<grid, kThreads, smem, st>>>(a);
+  a.n_ntiles = (a.Cout + BN - 1) / BN;
+  dim3 grid((a.W + kTileX - 1) / kTileX, a.H, a.B * a.n_ntiles);
+  k_conv_fwd<BN, KC, NR><<<grid, kThreads, smem, st>>>(a, tmx, tmw);
   return cudaGetLastError();
 }
 
-template <int KC>
-cudaError_t launch_fwd_kc(const ConvArgs& a, cudaStream_t st) {
-  if (a.Cout <= 32) return launch_fwd<32, KC>(a, st);
-  if (a.Cout <= 64) return launch_fwd<64, KC>(a, st);
-  return launch_fwd<128, KC>(a, st);
+template <int KC, int NR>
+cudaError_t launch_fwd_n(const __nv_bfloat16* x, const __nv_bfloat16* w, const ConvArgs& a, cudaStream_t st) {
+  if (a.Cout <= 32) return launch_fwd<32, KC, NR>(x, w, a, st);
+  if (a.Cout <= 64) return launch_fwd<64, KC, NR>(x, w, a, st);
+  return launch_fwd<128, KC, NR>(x, w, a, st);
 }
 
 }  // namespace
 
 int conv_fwd(const __nv_bfloat16* x, int B, int H, int W, int Cin, const __nv_bfloat16* w, int Cout, int taps,
              const float* bias, int relu, const __nv_bfloat16* mask, void* y, int y_fp32, cudaStream_t st) {
-  if (!x || !w || !y || B < 1 || H < 1 || W < 1) return 1;
+  if (!x || !w || !y || B < 1 || H < 1 || W < 1 || H > 65535) return 1;
   if (Cin < 16 || Cin % 16 != 0 || Cout < 8 || Cout % 8 != 0 || (taps != 1 && taps != 9)) return 1;
-  if ((long long)B * H * W >= (1LL << 31)) return 1;
-  ConvArgs a{x, w, bias, mask, y, B, H, W, Cin, Cout, taps, relu, y_fp32};
+  if ((long long)B * H * W >= (1LL << 31) || (long long)B * ((Cout + 31) / 32) > 65535) return 1;
+  // TMA: 16-byte aligned tensors (every stride is a multiple of 16 bytes: Cin % 8 == 0)
+  if (((uintptr_t)x & 15) || ((uintptr_t)w & 15)) return 1;
+  ConvArgs a{bias, mask, y, B, H, W, Cin, Cout, taps, relu, y_fp32, 1};
   cudaError_t e;
-  if (Cin % 64 == 0)
-    e = launch_fwd_kc<64>(a, st);
-  else if (Cin % 32 == 0)
-    e = launch_fwd_kc<32>(a, st);
+  if (taps == 9)
+    e = Cin % 32 == 0 ? launch_fwd_n<32, 3>(x, w, a, st) : launch_fwd_n<16, 3>(x, w, a, st);
   else
-    e = launch_fwd_kc<16>(a, st);
+    e = Cin % 32 == 0 ? launch_fwd_n<32, 1>(x, w, a, st) : launch_fwd_n<16, 1>(x, w, a, st);
   return e == cudaSuccess ? 0 : 2;
 }
 
