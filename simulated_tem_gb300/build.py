@@ -63,7 +63,7 @@ def build(verbose=False, ptxas_info=False):
     libs = [
         (LIB, LIB_SOURCES, [os.path.join(CSRC, "internal.h"), os.path.join(inc, "stem.h"),
                             os.path.join(inc, "stem_host.h")]),
-        (NN_LIB, NN_SOURCES, [os.path.join(CSRC, "nn.h"), os.path.join(CSRC, "tc_sm100.cuh"),
+        (NN_LIB, NN_SOURCES, [os.path.join(CSRC, "nn.h"), os.path.join(CSRC, "tc_sm100.cuh"), os.path.join(CSRC, "nn_conv_strip.cuh"),
                               os.path.join(inc, "stem_nn.h")]),
     ]
     jobs, link = [], []

@@ -14,6 +14,10 @@ namespace nn {
 // the ReLU that produced a layer's input.
 int conv_fwd(const __nv_bfloat16* x, int B, int H, int W, int Cin, const __nv_bfloat16* w, int Cout, int taps,
              const float* bias, int relu, const __nv_bfloat16* mask, void* y, int y_fp32, cudaStream_t st);
+// The strip-persistent kernel for Cout <= 64 and Cin <= 128 (same contract as conv_fwd, whose
+// checks have passed); -1 when the layer does not fit it.
+int conv_fwd_strip(const __nv_bfloat16* x, int B, int H, int W, int Cin, const __nv_bfloat16* w, int Cout, int taps,
+                   const float* bias, int relu, const __nv_bfloat16* mask, void* y, int y_fp32, cudaStream_t st);
 
 // gw[co][t][ci] += sum over pixels of gy[p][co] x[p + d_t][ci] (FP32, accumulated), the
 // partial sums of the pixel split in ws (conv_wgrad_workspace floats), added in a fixed order.

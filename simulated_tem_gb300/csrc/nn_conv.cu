@@ -2,10 +2,9 @@
 //
 // Forward (and input-gradient) convolution, 3 x 3 ("same" padding) or 1 x 1, over NHWC
 // BF16 activations: an implicit GEMM D[p, co] = sum_k A[p, k] B[co, k], p the output
-// pixel, k = (tap, ci).  A CTA owns 128 consecutive pixels of one image row x BN output
-// channels; the FP32 accumulator lives in TMEM (BN columns).  No thread touches the
-// operands: one thread moves them with TMA, one issues the MMAs, and the epilogue reads
-// TMEM.
+// pixel, k = (tap, ci).  A tile is 128 consecutive pixels of one image row x BN output
+// channels; its FP32 accumulator lives in TMEM (BN columns).  No thread touches the
+// operands: one thread moves them with TMA, one issues the MMAs, four warps drain TMEM.
 //
 // Per chunk of KC input channels the producer loads a halo tile: the input rows y - 1,
 // y, y + 1 (one row for 1 x 1), pixels x0 - 1 .. x0 + 128, as (KC / 8) slabs of 130 rows
@@ -14,12 +13,19 @@
 // bytes further: all nine taps read the same tile through shifted descriptors (LBO =
 // slab pitch between 8-channel groups, SBO = 128 between 8-pixel groups).  Outside the
 // image the TMA box is zero-filled: the padding.  The weights of each (tap, chunk) come
-// by TMA into a ring of B slots ([BN rows][16 bytes] per 8-channel group).  mbarriers
-// pace the two rings (full: TMA transaction bytes; empty: the MMAs' commit).
+// by TMA into a ring of B slots ([BN rows][16 bytes] per 8-channel group).
 //
-// Every wait on an mbarrier is bounded; a wait that runs out records an error in
-// g_nn_error, the producer waits (bounded) for every load it issued, the MMAs issued so
-// far are waited for, and TMEM is always freed.
+// The kernel is persistent: a CTA takes tiles t = blockIdx.x, blockIdx.x + gridDim.x, ...
+// and its rings run on from one tile to the next, so the loads of the next tile overlap
+// the MMAs of this one; two TMEM accumulators let the epilogue of one tile overlap the
+// MMAs of the next.  Warp roles (192 threads): warps 0-3 epilogue (warp w reads TMEM lanes
+// 32w .. 32w + 31), warp 4 lane 0 loads, warp 5 lane 0 issues the MMAs.  mbarriers: A
+// stages and B slots full (TMA bytes) / empty (MMA commit); accumulators full (MMA
+// commit) / empty (one arrival per epilogue warp).
+//
+// Every wait on an mbarrier is bounded and watches a shared abort flag; a wait that runs
+// out records an error in g_nn_error, the producer waits (bounded) for every load it
+// issued, the MMAs issued so far are waited for, and TMEM is always freed.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -36,9 +42,10 @@ __device__ int g_nn_error = 0;  // first failure code of a corrector kernel (0 =
 
 namespace {
 
-constexpr int kThreads = 128;
+constexpr int kThreads = 128;              // weight-gradient kernel
+constexpr int kTileThreads = 192;          // persistent forward kernel: 4 epilogue warps, producer, issuer
 constexpr uint32_t kWaitLimit = 1u << 20;  // polls of an mbarrier before giving up (about a second)
-constexpr int kTileX = 128;                // output pixels per CTA (one image row)
+constexpr int kTileX = 128;                // output pixels per tile (one image row)
 constexpr int kHalo = kTileX + 2;          // input pixels per halo row
 constexpr int kSlab = 2176;                // bytes per (input row, 8 channels) slab: 130 x 16 rounded to 128
 constexpr int kBSlots = 4;                 // weight ring depth
@@ -48,21 +55,48 @@ struct ConvArgs {
   const __nv_bfloat16* mask;  // [B][H][W][Cout] or null: outputs where mask <= 0 are zeroed
   void* y;                    // [B][H][W][Cout], BF16 or FP32
   int B, H, W, Cin, Cout, taps, relu, y_fp32;
-  int n_ntiles;               // output-channel tiles (grid z = B * n_ntiles)
+  int n_ntiles;               // output-channel tiles
+  int xtiles, n_tiles;        // tiles: (x tile, row, image, channel tile)
 };
 
 template <int BN, int KC, int NR>
 struct TSmem {
   alignas(1024) unsigned char a[2][NR * (KC / 8) * kSlab];
   alignas(1024) unsigned char b[kBSlots][(KC / 8) * BN * 16];
-  alignas(8) unsigned long long a_full[2], a_empty[2], b_full[kBSlots], b_empty[kBSlots], done;
+  alignas(8) unsigned long long a_full[2], a_empty[2], b_full[kBSlots], b_empty[kBSlots], acc_full[2],
+      acc_empty[2], done;
   uint32_t tmem;
+  int abort;
 };
+
+// bounded wait that gives up early when another role has aborted
+__device__ __forceinline__ bool wait_or_abort(uint32_t mbar, uint32_t parity, volatile int* abort) {
+  for (uint32_t i = 0; i < kWaitLimit; ++i) {
+    if (tc::mbar_try_wait(mbar, parity)) return true;
+    if ((i & 255) == 255 && *abort) return false;
+  }
+  *abort = 1;
+  return false;
+}
+
+struct Tile {
+  int xt, y, img, n0;
+};
+__device__ __forceinline__ Tile tile_of(const ConvArgs& a, int t, int BN) {
+  Tile r;
+  r.xt = t % a.xtiles;
+  int rest = t / a.xtiles;
+  r.y = rest % a.H;
+  rest /= a.H;
+  r.img = rest % a.B;
+  r.n0 = (rest / a.B) * BN;
+  return r;
+}
 
 // NR = 3 input rows for a 3 x 3 convolution, 1 for 1 x 1 (then taps = 1).
 template <int BN, int KC, int NR>
-__global__ void __launch_bounds__(kThreads) k_conv_fwd(const ConvArgs a, const __grid_constant__ CUtensorMap tmx,
-                                                       const __grid_constant__ CUtensorMap tmw) {
+__global__ void __launch_bounds__(kTileThreads) k_conv_fwd(const ConvArgs a, const __grid_constant__ CUtensorMap tmx,
+                                                           const __grid_constant__ CUtensorMap tmw) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   TSmem<BN, KC, NR>& S = *reinterpret_cast<TSmem<BN, KC, NR>*>(
       smem_raw + ((1024 - ((uintptr_t)smem_raw & 1023)) & 1023));
@@ -70,146 +104,186 @@ __global__ void __launch_bounds__(kThreads) k_conv_fwd(const ConvArgs a, const _
   constexpr int kG = KC / 8;                        // 8-channel groups per chunk
   constexpr uint32_t kBytesA = NR * kG * kHalo * 16;
   constexpr uint32_t kBytesB = kG * BN * 16;
-  constexpr uint32_t kCols = BN < 32 ? 32 : BN;
+  constexpr uint32_t kCols = 2 * BN;                // two accumulators
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-  const int x0 = blockIdx.x * kTileX, yrow = blockIdx.y;
-  const int img = blockIdx.z / a.n_ntiles, n0 = (blockIdx.z % a.n_ntiles) * BN;
   const int nchunks = a.Cin / KC;
+  volatile int* abort = &S.abort;
 
-  if (warp == 0) tc::tmem_alloc(tc::smem_addr(&S.tmem), kCols);
+  if (warp == 5) tc::tmem_alloc(tc::smem_addr(&S.tmem), kCols);
   if (t == 0) {
     for (int i = 0; i < 2; ++i) {
       tc::mbar_init(tc::smem_addr(&S.a_full[i]), 1);
       tc::mbar_init(tc::smem_addr(&S.a_empty[i]), 1);
+      tc::mbar_init(tc::smem_addr(&S.acc_full[i]), 1);
+      tc::mbar_init(tc::smem_addr(&S.acc_empty[i]), 4);
     }
     for (int i = 0; i < kBSlots; ++i) {
       tc::mbar_init(tc::smem_addr(&S.b_full[i]), 1);
       tc::mbar_init(tc::smem_addr(&S.b_empty[i]), 1);
     }
     tc::mbar_init(tc::smem_addr(&S.done), 1);
+    S.abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = S.tmem;
-  bool ok = true;
 
-  if (warp == 0 && lane == 0) {
-    // producer: halo tiles and weight slots, in the order the MMAs consume them
-    int na[2] = {0, 0}, nb[kBSlots] = {0, 0, 0, 0};  // loads armed per stage / slot
-    int jb = 0;
-    for (int c = 0; c < nchunks && ok; ++c) {
-      const int sa = c & 1;
-      if (c >= 2 && !tc::mbar_wait(tc::smem_addr(&S.a_empty[sa]), ((c - 2) >> 1) & 1, kWaitLimit)) {
-        ok = false;
-        break;
-      }
-      const uint32_t fa = tc::smem_addr(&S.a_full[sa]);
-      tc::mbar_arrive_expect_tx(fa, kBytesA);
-      ++na[sa];
-      for (int r = 0; r < NR; ++r)
-        for (int g = 0; g < kG; ++g)
-          tc::tma_load_4d(tc::smem_addr(S.a[sa] + (r * kG + g) * kSlab), &tmx, c * KC + 8 * g, x0 - 1,
-                          yrow + r - (NR == 3 ? 1 : 0), img, fa);
-      for (int tap = 0; tap < kTaps; ++tap, ++jb) {
-        const int sb = jb % kBSlots;
-        if (jb >= kBSlots && !tc::mbar_wait(tc::smem_addr(&S.b_empty[sb]), (jb / kBSlots - 1) & 1, kWaitLimit)) {
-          ok = false;
-          break;
+  if (warp == 4) {
+    if (lane == 0) {
+      // ---- producer: halo tiles and weight slots, in the order the MMAs consume them
+      int na[2] = {0, 0}, nb[kBSlots] = {0, 0, 0, 0};  // loads armed per stage / slot
+      int ca = 0, jb = 0;                              // chunks and weight loads issued
+      bool ok = true;
+      for (int tt = blockIdx.x; tt < a.n_tiles && ok; tt += gridDim.x) {
+        const Tile tl = tile_of(a, tt, BN);
+        for (int c = 0; c < nchunks && ok; ++c, ++ca) {
+          const int sa = ca & 1;
+          if (ca >= 2 && !wait_or_abort(tc::smem_addr(&S.a_empty[sa]), ((ca - 2) >> 1) & 1, abort)) {
+            ok = false;
+            break;
+          }
+          const uint32_t fa = tc::smem_addr(&S.a_full[sa]);
+          tc::mbar_arrive_expect_tx(fa, kBytesA);
+          ++na[sa];
+          for (int r = 0; r < NR; ++r)
+            for (int g = 0; g < kG; ++g)
+              tc::tma_load_4d(tc::smem_addr(S.a[sa] + (r * kG + g) * kSlab), &tmx, c * KC + 8 * g,
+                              tl.xt * kTileX - 1, tl.y + r - (NR == 3 ? 1 : 0), tl.img, fa);
+          for (int tap = 0; tap < kTaps; ++tap, ++jb) {
+            const int sb = jb % kBSlots;
+            if (jb >= kBSlots &&
+                !wait_or_abort(tc::smem_addr(&S.b_empty[sb]), (jb / kBSlots - 1) & 1, abort)) {
+              ok = false;
+              break;
+            }
+            const uint32_t fb = tc::smem_addr(&S.b_full[sb]);
+            tc::mbar_arrive_expect_tx(fb, kBytesB);
+            ++nb[sb];
+            for (int g = 0; g < kG; ++g)
+              tc::tma_load_3d(tc::smem_addr(S.b[sb] + g * BN * 16), &tmw, c * KC + 8 * g, tap, tl.n0, fb);
+          }
         }
-        const uint32_t fb = tc::smem_addr(&S.b_full[sb]);
-        tc::mbar_arrive_expect_tx(fb, kBytesB);
-        ++nb[sb];
-        for (int g = 0; g < kG; ++g)
-          tc::tma_load_3d(tc::smem_addr(S.b[sb] + g * BN * 16), &tmw, c * KC + 8 * g, tap, n0, fb);
       }
+      // every load issued has landed before the CTA may leave (bounded)
+      for (int i = 0; i < 2; ++i)
+        if (na[i] > 0 && !tc::mbar_wait(tc::smem_addr(&S.a_full[i]), (na[i] - 1) & 1, kWaitLimit)) *abort = 1;
+      for (int i = 0; i < kBSlots; ++i)
+        if (nb[i] > 0 && !tc::mbar_wait(tc::smem_addr(&S.b_full[i]), (nb[i] - 1) & 1, kWaitLimit)) *abort = 1;
     }
-    // every load issued has landed before the CTA may leave (bounded)
-    for (int i = 0; i < 2; ++i)
-      if (na[i] > 0 && !tc::mbar_wait(tc::smem_addr(&S.a_full[i]), (na[i] - 1) & 1, kWaitLimit)) ok = false;
-    for (int i = 0; i < kBSlots; ++i)
-      if (nb[i] > 0 && !tc::mbar_wait(tc::smem_addr(&S.b_full[i]), (nb[i] - 1) & 1, kWaitLimit)) ok = false;
-  } else if (warp == 1 && lane == 0) {
-    // MMA issuer
-    constexpr uint32_t idesc = tc::make_idesc_bf16(128, BN);
-    int jb = 0;
-    bool first = true;
-    for (int c = 0; c < nchunks && ok; ++c) {
-      const int sa = c & 1;
-      if (!tc::mbar_wait(tc::smem_addr(&S.a_full[sa]), (c >> 1) & 1, kWaitLimit)) {
-        ok = false;
-        break;
-      }
-      const uint32_t abase = tc::smem_addr(S.a[sa]);
-      for (int tap = 0; tap < kTaps; ++tap, ++jb) {
-        const int sb = jb % kBSlots;
-        if (!tc::mbar_wait(tc::smem_addr(&S.b_full[sb]), (jb / kBSlots) & 1, kWaitLimit)) {
+  } else if (warp == 5) {
+    if (lane == 0) {
+      // ---- MMA issuer
+      constexpr uint32_t idesc = tc::make_idesc_bf16(128, BN);
+      int ca = 0, jb = 0, k = 0;  // chunks, weight slots and tiles consumed
+      bool ok = true;
+      for (int tt = blockIdx.x; tt < a.n_tiles && ok; tt += gridDim.x, ++k) {
+        const int buf = k & 1;
+        if (k >= 2 && !wait_or_abort(tc::smem_addr(&S.acc_empty[buf]), ((k >> 1) - 1) & 1, abort)) {
           ok = false;
           break;
         }
         tc::fence_after_sync();
-        const int dy = NR == 3 ? tap / 3 : 0, dx = NR == 3 ? tap % 3 : 1;  // halo row / column offset
-        const uint32_t bbase = tc::smem_addr(S.b[sb]);
+        const uint32_t acc = tmem + (uint32_t)(buf * BN);
+        for (int c = 0; c < nchunks && ok; ++c, ++ca) {
+          const int sa = ca & 1;
+          if (!wait_or_abort(tc::smem_addr(&S.a_full[sa]), (ca >> 1) & 1, abort)) {
+            ok = false;
+            break;
+          }
+          const uint64_t adesc0 = tc::make_desc(tc::smem_addr(S.a[sa]), kSlab, 128);
+          for (int tap = 0; tap < kTaps; ++tap, ++jb) {
+            const int sb = jb % kBSlots;
+            if (!wait_or_abort(tc::smem_addr(&S.b_full[sb]), (jb / kBSlots) & 1, abort)) {
+              ok = false;
+              break;
+            }
+            tc::fence_after_sync();
+            const int dy = NR == 3 ? tap / 3 : 0, dx = NR == 3 ? tap % 3 : 1;  // halo row / column offset
+            // start addresses in 16-byte units (descriptor bits 0-13)
+            uint64_t ad = adesc0 + (uint64_t)(dy * kG * (kSlab / 16) + dx);
+            uint64_t bd = tc::make_desc(tc::smem_addr(S.b[sb]), BN * 16, 128);
 #pragma unroll
-        for (int s = 0; s < KC / 16; ++s) {
-          const uint64_t ad = tc::make_desc(abase + (dy * kG + 2 * s) * kSlab + dx * 16, kSlab, 128);
-          const uint64_t bd = tc::make_desc(bbase + 2 * s * BN * 16, BN * 16, 128);
-          tc::mma_bf16(tmem, ad, bd, idesc, first ? 0u : 1u);
-          first = false;
+            for (int s = 0; s < KC / 16; ++s) {
+              tc::mma_bf16(acc, ad, bd, idesc, (c == 0 && tap == 0 && s == 0) ? 0u : 1u);
+              ad += 2 * kSlab / 16;
+              bd += 2 * BN;
+            }
+            tc::mma_commit(tc::smem_addr(&S.b_empty[sb]));
+          }
+          if (!ok) break;
+          tc::mma_commit(tc::smem_addr(&S.a_empty[sa]));
         }
-        tc::mma_commit(tc::smem_addr(&S.b_empty[sb]));
+        if (!ok) break;
+        tc::mma_commit(tc::smem_addr(&S.acc_full[buf]));
       }
-      if (!ok) break;
-      tc::mma_commit(tc::smem_addr(&S.a_empty[sa]));
+      tc::mma_commit(tc::smem_addr(&S.done));  // arrives when every MMA issued above has completed
+      if (!tc::mbar_wait(tc::smem_addr(&S.done), 0, kWaitLimit)) *abort = 1;
     }
-    tc::mma_commit(tc::smem_addr(&S.done));  // arrives when every MMA issued above has completed
-  }
-  __syncwarp();
-  // everyone: the accumulator is complete (bounded wait; the MMA thread always commits)
-  bool done = tc::mbar_wait(tc::smem_addr(&S.done), 0, kWaitLimit);
-  ok = __syncthreads_and(ok && done);
-  if (!ok && t == 0) atomicCAS(&g_nn_error, 0, 1);
-  tc::fence_after_sync();
-
-  if (ok) {
-    // epilogue: warp w holds TMEM lanes (pixels x0 + 32w .. x0 + 32w + 31)
-    const int xw = x0 + 32 * warp + lane;
-    const size_t p = ((size_t)img * a.H + yrow) * a.W + xw;
-    for (int col = 0; col < BN; col += 8) {
-      float v[8];
-      tc::tmem_ld8(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)col, v);
-      const int n = n0 + col;
-      if (xw < a.W && n < a.Cout) {
+  } else {
+    // ---- epilogue warps 0-3: TMEM lanes 32 warp .. 32 warp + 31 = pixels of the tile
+    int k = 0;
+    for (int tt = blockIdx.x; tt < a.n_tiles; tt += gridDim.x, ++k) {
+      const Tile tl = tile_of(a, tt, BN);
+      const int buf = k & 1;
+      if (!wait_or_abort(tc::smem_addr(&S.acc_full[buf]), (k >> 1) & 1, abort)) break;
+      tc::fence_after_sync();
+      float v[BN];
+      {
+        uint32_t reg[BN];
+        if constexpr (BN >= 32) {
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          if (a.bias) v[i] += a.bias[n + i];
-          if (a.relu) v[i] = fmaxf(v[i], 0.f);
+          for (int col = 0; col < BN; col += 32)
+            tc::tmem_ld32_nowait(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(buf * BN + col), reg + col);
+          tc::tmem_wait_ld();
         }
-        if (a.mask) {  // gradient through the ReLU that produced this layer's input
-          const uint4 mv = *reinterpret_cast<const uint4*>(a.mask + p * a.Cout + n);
-          const __nv_bfloat16* m = reinterpret_cast<const __nv_bfloat16*>(&mv);
 #pragma unroll
-          for (int i = 0; i < 8; ++i)
-            if (!(__bfloat162float(m[i]) > 0.f)) v[i] = 0.f;
-        }
-        if (a.y_fp32) {
-          float* dst = reinterpret_cast<float*>(a.y) + p * a.Cout + n;
-          *reinterpret_cast<float4*>(dst) = make_float4(v[0], v[1], v[2], v[3]);
-          *reinterpret_cast<float4*>(dst + 4) = make_float4(v[4], v[5], v[6], v[7]);
-        } else {
-          __align__(16) __nv_bfloat162 h[4];
+        for (int c2 = 0; c2 < BN; ++c2) v[c2] = __uint_as_float(reg[c2]);
+      }
+      tc::fence_before_sync();
+      __syncwarp();
+      if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc::smem_addr(&S.acc_empty[buf]))
+                                  : "memory");
+      const int xw = tl.xt * kTileX + 32 * warp + lane;
+      if (xw < a.W) {
+        const size_t p = ((size_t)tl.img * a.H + tl.y) * a.W + xw;
 #pragma unroll
-          for (int i = 0; i < 4; ++i) h[i] = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
-          *reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(a.y) + p * a.Cout + n) =
-              *reinterpret_cast<const uint4*>(h);
+        for (int col = 0; col < BN; col += 8) {
+          const int n = tl.n0 + col;
+          if (n >= a.Cout) break;
+          float* vv = v + col;
+#pragma unroll
+          for (int i = 0; i < 8; ++i) {
+            if (a.bias) vv[i] += a.bias[n + i];
+            if (a.relu) vv[i] = fmaxf(vv[i], 0.f);
+          }
+          if (a.mask) {  // gradient through the ReLU that produced this layer's input
+            const uint4 mv = *reinterpret_cast<const uint4*>(a.mask + p * a.Cout + n);
+            const __nv_bfloat16* m = reinterpret_cast<const __nv_bfloat16*>(&mv);
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+              if (!(__bfloat162float(m[i]) > 0.f)) vv[i] = 0.f;
+          }
+          if (a.y_fp32) {
+            float* dst = reinterpret_cast<float*>(a.y) + p * a.Cout + n;
+            *reinterpret_cast<float4*>(dst) = make_float4(vv[0], vv[1], vv[2], vv[3]);
+            *reinterpret_cast<float4*>(dst + 4) = make_float4(vv[4], vv[5], vv[6], vv[7]);
+          } else {
+            __align__(16) __nv_bfloat162 h[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) h[i] = __floats2bfloat162_rn(vv[2 * i], vv[2 * i + 1]);
+            *reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(a.y) + p * a.Cout + n) =
+                *reinterpret_cast<const uint4*>(h);
+          }
         }
       }
     }
   }
-  tc::fence_before_sync();
   __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(tmem, kCols);
+  if (t == 0 && S.abort) atomicCAS(&g_nn_error, 0, 1);
+  tc::fence_after_sync();
+  if (warp == 5) tc::tmem_dealloc(tmem, kCols);
 }
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no link to libcuda)
@@ -247,17 +321,25 @@ cudaError_t launch_fwd(const __nv_bfloat16* x, const __nv_bfloat16* w, ConvArgs 
   const cuuint64_t ws[2] = {(cuuint64_t)a.Cin * 2, (cuuint64_t)a.taps * a.Cin * 2};
   const cuuint32_t wb[3] = {8, 1, (cuuint32_t)BN};
   if (!make_map(&tmx, x, 4, xd, xs, xb) || !make_map(&tmw, w, 3, wd, ws, wb)) return cudaErrorInvalidValue;
-  // shared memory also caps the CTAs per SM so that their TMEM columns fit in 512 (an
-  // allocation beyond that would wait for another CTA to finish)
-  constexpr size_t kCols = BN < 32 ? 32 : BN;
-  const size_t need = sizeof(TSmem<BN, KC, NR>) + 1024, floor_tmem = 232448 / (512 / kCols) - 1023;
-  const size_t smem = need > floor_tmem ? need : floor_tmem;
+  // CTAs per SM: shared memory, and TMEM (2 BN columns each, 512 per SM)
+  const size_t per_sm = 232448, need = sizeof(TSmem<BN, KC, NR>) + 1024;
+  int ctas = (int)(per_sm / (need + 1024));
+  ctas = ctas < 1 ? 1 : ctas;
+  if (ctas * 2 * BN > 512) ctas = 512 / (2 * BN);
+  const size_t smem = per_sm / ctas - 1024 > need ? per_sm / ctas - 1024 : need;
   cudaError_t e =
       cudaFuncSetAttribute(k_conv_fwd<BN, KC, NR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
+  int dev = 0, sms = 148;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   a.n_ntiles = (a.Cout + BN - 1) / BN;
-  dim3 grid((a.W + kTileX - 1) / kTileX, a.H, a.B * a.n_ntiles);
-  k_conv_fwd<BN, KC, NR><<<grid, kThreads, smem, st>>>(a, tmx, tmw);
+  a.xtiles = (a.W + kTileX - 1) / kTileX;
+  const long long tiles = (long long)a.xtiles * a.H * a.B * a.n_ntiles;
+  if (tiles >= (1LL << 31)) return cudaErrorInvalidValue;
+  a.n_tiles = (int)tiles;
+  const int grid = a.n_tiles < ctas * sms ? a.n_tiles : ctas * sms;
+  k_conv_fwd<BN, KC, NR><<<grid, kTileThreads, smem, st>>>(a, tmx, tmw);
   return cudaGetLastError();
 }
 
@@ -272,12 +354,15 @@ cudaError_t launch_fwd_n(const __nv_bfloat16* x, const __nv_bfloat16* w, const C
 
 int conv_fwd(const __nv_bfloat16* x, int B, int H, int W, int Cin, const __nv_bfloat16* w, int Cout, int taps,
              const float* bias, int relu, const __nv_bfloat16* mask, void* y, int y_fp32, cudaStream_t st) {
-  if (!x || !w || !y || B < 1 || H < 1 || W < 1 || H > 65535) return 1;
+  if (!x || !w || !y || B < 1 || H < 1 || W < 1) return 1;
   if (Cin < 16 || Cin % 16 != 0 || Cout < 8 || Cout % 8 != 0 || (taps != 1 && taps != 9)) return 1;
-  if ((long long)B * H * W >= (1LL << 31) || (long long)B * ((Cout + 31) / 32) > 65535) return 1;
+  if ((long long)B * H * W >= (1LL << 31)) return 1;
   // TMA: 16-byte aligned tensors (every stride is a multiple of 16 bytes: Cin % 8 == 0)
   if (((uintptr_t)x & 15) || ((uintptr_t)w & 15)) return 1;
-  ConvArgs a{bias, mask, y, B, H, W, Cin, Cout, taps, relu, y_fp32, 1};
+  // wide, shallow layers: the strip-persistent kernel (resident weights, rolling input rows)
+  const int rs = conv_fwd_strip(x, B, H, W, Cin, w, Cout, taps, bias, relu, mask, y, y_fp32, st);
+  if (rs >= 0) return rs;
+  ConvArgs a{bias, mask, y, B, H, W, Cin, Cout, taps, relu, y_fp32, 1, 1, 1};
   cudaError_t e;
   if (taps == 9)
     e = Cin % 32 == 0 ? launch_fwd_n<32, 3>(x, w, a, st) : launch_fwd_n<16, 3>(x, w, a, st);
@@ -543,3 +628,6 @@ int take_error() {
 
 }  // namespace nn
 }  // namespace stem
+
+// the strip-persistent forward convolution (uses g_nn_error and make_map above)
+#include "nn_conv_strip.cuh"
