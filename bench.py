@@ -338,6 +338,72 @@ def cfg5_leg(ctx, stream, flush, steps, warmup, weights=CORRECTOR_WEIGHTS):
             "speedup": ms_fine / ms_corr}
 
 
+def io_leg(ctx, stream, flush, steps, warmup, cpu=True):
+    """d2bi's output files at the M = 8 image size of the 4.8M-atom cell (2263 x 2263,
+    synthetic intensities in [0, 0.3)): the '(1000f12.7)' records of the .dat file and the
+    16-bit PNG levels on the GPU (device-resident image, CUDA events), the whole
+    st_write_dat / st_write_png calls (host image to file), and the oracle's C formatter
+    and levels on one host core for the same image."""
+    import tempfile
+
+    import torch
+
+    from simulated_tem_gb300 import imaging
+    nx = ny = 2263
+    n = nx * ny
+    rng = np.random.default_rng(20261203 + 7)
+    img = np.asfortranarray(rng.random((nx, ny)) * 0.3)
+    d_img = torch.from_numpy(img.T.copy()).cuda()
+    cap = imaging.lib().st_dat_text_bytes(n)
+    d_text = torch.empty(cap, dtype=torch.uint8, device="cuda")
+    d_lv = torch.empty(n, dtype=torch.int16, device="cuda")
+    sp = stream.cuda_stream
+
+    def timed(fn):
+        for _ in range(warmup):
+            fn()
+        ms = []
+        for i in range(steps):
+            flush.fill_(float(i))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return float(np.median(ms))
+
+    ms_dat = timed(lambda: ctx.format_dat_device(d_img.data_ptr(), n, d_text.data_ptr(), cap, stream=sp))
+    ms_png = timed(lambda: ctx.png_levels_device(d_img.data_ptr(), nx, ny, d_lv.data_ptr(), stream=sp))
+    hdr = dict(modg=3.97017, sg=0.01, xmax=(811.9, 811.9, 172.2), aperpx=0.3588)
+    with tempfile.TemporaryDirectory() as tmp:
+        walls = {}
+        for name, fn in (("write_dat", lambda: ctx.write_dat(os.path.join(tmp, "i.dat"), hdr, img)),
+                         ("write_png", lambda: ctx.write_png(os.path.join(tmp, "i.png"), img, blur_t=6.97))):
+            fn()
+            t0 = time.perf_counter()
+            for _ in range(3):
+                fn()
+            walls[name] = (time.perf_counter() - t0) / 3 * 1e3
+    out = {"workload": "%d x %d image, synthetic intensities in [0, 0.3)" % (nx, ny),
+           "dat_records_gpu": {"ms": ms_dat, "MB_per_s": cap / ms_dat / 1e3, "bytes": int(cap)},
+           "png_levels_gpu": {"ms": ms_png, "Mpixel_per_s": n / ms_png / 1e3},
+           "write_dat_file_ms": walls["write_dat"], "write_png_file_ms": walls["write_png"],
+           "note": "write_*_file: host image to file through st_write_dat / st_write_png (the PNG blurred "
+                   "at 6.97 px = 2.5 A first); GPU legs device-resident, CUDA events, L2 flushed"}
+    if cpu:
+        from oracle import stem_oracle as O
+        t0 = time.perf_counter()
+        O.format_f12_7(img.T.ravel())
+        t_dat = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        O.png_levels(img)
+        t_png = time.perf_counter() - t0
+        out["cpu_oracle"] = {"dat_records_ms": t_dat * 1e3, "png_levels_ms": t_png * 1e3, "cores": 1,
+                             "kind": "port", "note": "oracle C restatement (snprintf per value), one core"}
+    return out
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -453,6 +519,8 @@ def run_gpu(args):
         cfg1 = None if args.no_batched else cfg1_leg(ctx, stream, flush, 5, args.warmup,
                                                       cpu=(rank == 0 and not args.no_cpu))
         cfg5 = None if args.no_batched else cfg5_leg(ctx, stream, flush, 3, args.warmup)
+        io = None if args.no_batched else io_leg(ctx, stream, flush, 5, args.warmup,
+                                                  cpu=(rank == 0 and not args.no_cpu))
     step_ms = [a.elapsed_time(b) for a, b in ev]
     ms = float(np.mean(step_ms))
     if ws > 1:
@@ -534,7 +602,8 @@ def run_gpu(args):
             "accuracy": {"max_abs_dI_fp32_vs_fp64": float(np.abs(d).max()),
                          "rms_dI_fp32_vs_fp64": float(np.sqrt((d ** 2).mean()))},
             "gpu_launches": args.steps * launches_per_image(n_prec, fp32=True, average=True),
-            "roofline": roof, "peaks": peaks, "wall_s": wall, "clocks": clk.summary(), "batched": batched, "cfg1_128k": cfg1, "cfg5_corrector": cfg5}
+            "roofline": roof, "peaks": peaks, "wall_s": wall, "clocks": clk.summary(), "batched": batched, "cfg1_128k": cfg1, "cfg5_corrector": cfg5,
+            "output_files": io}
     if rank == 0:
         if ws == 1 and not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline(x_state=(cell, t, x), rows=args.cpu_rows)

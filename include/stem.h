@@ -226,6 +226,66 @@ int st_get_stats(const st_ctx* ctx, st_stats* out);
 int st_blur_noalloc(const double* d_in, int32_t nx, int32_t ny, double t, double* d_out, void* stream, char* err,
                     int32_t err_len);
 
+/* ---- Output files of d2bi: the .dat image and the 16-bit PNG ----------------------
+ * The .dat file (src/d2bi.f90:1429-1457): header lines, then '(2i8)' nx ny, then the
+ * image column-major in records of '(1000f12.7)'.  The header fields, as d2bi writes
+ * them: */
+typedef struct st_dat_header {
+  char version[32];   /* "# d2bi v.<version>" */
+  int32_t miller4;    /* 1: k and g are 4-index (hexagonal) vectors */
+  double k[4], g[4];  /* '(a,3f10.3)' or '(a,4f10.3)' */
+  double modg;        /* |g| (1/A), '(f12.5)' after g */
+  int32_t nM, M[3];   /* '(a,3i8)': the first nM values */
+  double V;           /* keV, '(a,3f10.0)' */
+  double xi0, xig;    /* A, '(a,3f12.5)' */
+  int32_t has_ng;     /* 1: the '# n_g' line ('(a,f8.3)') is written */
+  double ng;
+  double sg;          /* 1/A, '(a,3f12.5)' */
+  double xmax[3];     /* img space (A), '(a,3f12.3)' */
+  double aperpx;      /* scale (A/px), '(a,3f12.5)' */
+  double rotation[9]; /* matmul(R, U) column-major, '(a,9f12.6)' */
+} st_dat_header;
+
+/* The header text (up to and including the '(2i8)' size line) into buf (cap bytes,
+ * NUL-terminated); *len = its length.  Host only.  Fortran F editing: rounded to
+ * nearest, at least one integer digit when the field has room, a trailing '.' for
+ * zero decimals, asterisks when the number does not fit. */
+int st_format_dat_header(const st_dat_header* h, int32_t nx, int32_t ny, char* buf, int64_t cap, int64_t* len);
+
+/* Bytes of the '(1000f12.7)' records of n values: 12 n plus a newline per record. */
+int64_t st_dat_text_bytes(int64_t n);
+
+/* The '(1000f12.7)' records of n device values d_v into device memory d_text (cap bytes,
+ * at least st_dat_text_bytes(n)); enqueued on stream (0: the context's stream),
+ * returns without waiting. */
+int st_format_dat_device(st_ctx* ctx, const double* d_v, int64_t n, char* d_text, int64_t cap, void* stream);
+
+/* Write a .dat file: header, size line, records (formatted on the GPU).  img is the host
+ * image (nx x ny, column-major).  Written to <path>.tmp, then renamed to path. */
+int st_write_dat(st_ctx* ctx, const char* path, const st_dat_header* h, const double* img, int32_t nx, int32_t ny);
+
+/* The 16-bit levels of d2bi's PNG output (outputImgAsPng, src/d2bi.f90:1509-1538, and
+ * write_greyscale_png, src/Lib_Png.f90:117-181 with src/Lib_Greyscale.c:230-245): with
+ * iso_min == iso_max the image is normalised to [0, 1 - 1/65536] by its minimum and
+ * maximum, otherwise scaled to (v - iso_min) / (iso_max - iso_min) and clamped to [0, 1];
+ * the level is (int)(65536 f) of the FP32 value f clamped to [0, 0.999984741].
+ * d_levels: nx * ny native-endian uint16, image order (x fastest).  No blur here (see
+ * st_write_png); enqueued on stream, returns without waiting. */
+int st_png_levels_device(st_ctx* ctx, const double* d_img, int32_t nx, int32_t ny, double iso_min, double iso_max,
+                         uint16_t* d_levels, void* stream);
+
+/* A 16-bit greyscale PNG (no interlace, filter none, zlib stored blocks) of the levels
+ * (nx x ny, row y = levels[nx y .. nx y + nx - 1]) into out (cap bytes); *len = the file
+ * size.  Host only.  Decoders see the same pixels as in d2bi's PNG files. */
+int64_t st_png16_bytes(int32_t nx, int32_t ny);
+int st_encode_png16(const uint16_t* levels, int32_t nx, int32_t ny, uint8_t* out, int64_t cap, int64_t* len);
+
+/* d2bi's PNG file of a host image: the blur of width blur_t pixels first when blur_t > 0
+ * (gaussianBlurImage), then the levels above, then the PNG; written to <path>.tmp, then
+ * renamed to path. */
+int st_write_png(st_ctx* ctx, const char* path, const double* img, int32_t nx, int32_t ny, double iso_min,
+                 double iso_max, double blur_t);
+
 #ifdef __cplusplus
 }
 #endif

@@ -8,6 +8,7 @@
 #include "stem_oracle.h"
 
 #include <float.h>
+#include <stdio.h>
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
@@ -1216,3 +1217,54 @@ void oc_png_levels(const double* img, int Nx, int Ny, uint16_t* levels) {
       levels[(size_t)y * Nx + x] = (uint16_t)i;
     }
 }
+
+/* outputImgAsPng, contrast mode (src/d2bi.f90:1531-1535): img = (img - lo)/(hi - lo),
+ * clamped to [0, 1], then Lib_Png.f90:164-165 with aa = 1, bb = 0 and
+ * Lib_Greyscale.c:230-245. */
+void oc_png_levels_window(const double* img, int Nx, int Ny, double lo, double hi, uint16_t* levels) {
+  for (int y = 0; y < Ny; ++y)
+    for (int x = 0; x < Nx; ++x) {
+      double v = (img[(size_t)x + (size_t)Nx * y] - lo) / (hi - lo);
+      v = v < 1.0 ? v : 1.0;
+      v = v > 0.0 ? v : 0.0;
+      float f = (float)(1.0 * v + 0.0);
+      if (f > 0.999984741) {
+        f = 0.999984741f;
+      } else if (f < 0.0) {
+        f = 0.0f;
+      }
+      levels[(size_t)y * Nx + x] = (uint16_t)(int)(f * 65536);
+    }
+}
+
+/* Fortran F12.7 of one value: C's correctly rounded %.7f of |v| (no exact ties arise at
+ * 7 decimals of a binary value), '-' for negative values, right-justified, asterisks
+ * when longer than 12 characters; NaN and Infinity spelled as gfortran does. */
+static void f12_7(double v, char* o) {
+  char s[400];
+  if (isnan(v)) {
+    snprintf(s, sizeof s, "NaN");
+  } else if (isinf(v)) {
+    snprintf(s, sizeof s, "%s", v > 0 ? "Infinity" : "-Infinity");
+  } else {
+    snprintf(s, sizeof s, "%s%.7f", signbit(v) ? "-" : "", fabs(v));
+  }
+  const size_t len = strlen(s);
+  if (len > 12) {
+    memset(o, '*', 12);
+  } else {
+    memset(o, ' ', 12 - len);
+    memcpy(o + 12 - len, s, len);
+  }
+}
+
+long long oc_format_f12_7(const double* v, long long n, char* out) {
+  long long p = 0;
+  for (long long i = 0; i < n; ++i) {
+    f12_7(v[i], out + p);
+    p += 12;
+    if (i % 1000 == 999 || i == n - 1) out[p++] = '\n';
+  }
+  return p;
+}
+

@@ -182,6 +182,13 @@ void oc_gaussian_blur(const double* f_in, int Nx, int Ny, double t, double* f_ou
 /* write_greyscale_png normalise=.true. quantisation (Lib_Png.f90:117-181,
  * Lib_Greyscale.c:234-241): png[y*Nx + x] = 16-bit level of img(x, y). */
 void oc_png_levels(const double* img, int Nx, int Ny, uint16_t* levels);
+/* outputImgAsPng's contrast mode (src/d2bi.f90:1531-1535), then write_greyscale_png
+ * with normalise=.false.: the levels of clamp((v - lo) / (hi - lo), 0, 1). */
+void oc_png_levels_window(const double* img, int Nx, int Ny, double lo, double hi, uint16_t* levels);
+/* The '(1000f12.7)' records of d2bi's .dat file (src/d2bi.f90:1455): every value in
+ * Fortran F12.7 editing, a newline after each 1000 values and after the last; returns
+ * the number of bytes written to out. */
+long long oc_format_f12_7(const double* v, long long n, char* out);
 
 #ifdef __cplusplus
 }

@@ -189,6 +189,67 @@ def gaussian_blur(img, t):
     return out
 
 
+def png_levels_window(img, lo, hi):
+    """outputImgAsPng's contrast mode: levels of clamp((v - lo) / (hi - lo), 0, 1)."""
+    img = np.asfortranarray(img, dtype=np.float64)
+    Nx, Ny = img.shape
+    lv = np.zeros((Ny, Nx), dtype=np.uint16)
+    lib().oc_png_levels_window(_dptr(img), _i(Nx), _i(Ny), _d(lo), _d(hi),
+                               lv.ctypes.data_as(ctypes.POINTER(ctypes.c_uint16)))
+    return lv
+
+
+def format_f12_7(values):
+    """The '(1000f12.7)' records of a .dat file for a flat array of values (bytes)."""
+    v = np.ascontiguousarray(values, dtype=np.float64).ravel()
+    out = ctypes.create_string_buffer(12 * v.size + v.size // 1000 + 2)
+    L = lib()
+    L.oc_format_f12_7.restype = ctypes.c_longlong
+    n = L.oc_format_f12_7(_dptr(v), ctypes.c_longlong(v.size), out)
+    return out.raw[:n]
+
+
+def fortran_f(x, w, d):
+    """Fortran Fw.d editing of one number (the .dat header's fields)."""
+    if x != x:
+        s = "NaN"
+    elif x in (float("inf"), float("-inf")):
+        s = "Infinity" if x > 0 else "-Infinity"
+    else:
+        s = "%.*f" % (d, abs(x)) + ("." if d == 0 else "")
+        if np.signbit(x):
+            s = "-" + s
+        if len(s) > w and s.lstrip("-").startswith("0."):
+            s = s.replace("0.", ".", 1)
+    return "*" * w if len(s) > w else s.rjust(w)
+
+
+def fortran_i(v, w):
+    """Fortran Iw editing."""
+    s = "%d" % v
+    return "*" * w if len(s) > w else s.rjust(w)
+
+
+def dat_header(h, nx, ny):
+    """The header and size lines of d2bi's .dat file (src/d2bi.f90:1430-1454) for a dict
+    of the written fields."""
+    nv = 4 if h.get("miller4") else 3
+    out = ["# d2bi v." + h["version"],
+           "# k       " + "".join(fortran_f(v, 10, 3) for v in h["k"][:nv]),
+           "# g       " + "".join(fortran_f(v, 10, 3) for v in h["g"][:nv]) + fortran_f(h["modg"], 12, 5),
+           "# M       " + "".join(fortran_i(m, 8) for m in h["M"]),
+           "# V (keV) " + fortran_f(h["V"], 10, 0),
+           "# xi (A)  " + fortran_f(h["xi0"], 12, 5) + fortran_f(h["xig"], 12, 5)]
+    if h.get("ng") is not None:
+        out.append("# n_g     " + fortran_f(h["ng"], 8, 3))
+    out += ["# s_g (1/A)    " + fortran_f(h["sg"], 12, 5),
+            "# img space (A)" + "".join(fortran_f(v, 12, 3) for v in h["xmax"]),
+            "# scale (A/px) " + fortran_f(h["aperpx"], 12, 5),
+            "# rotation " + "".join(fortran_f(v, 12, 6) for v in h["rotation"]),
+            fortran_i(nx, 8) + fortran_i(ny, 8)]
+    return "\n".join(out) + "\n"
+
+
 def png_levels(img):
     img = np.asfortranarray(img, dtype=np.float64)
     Nx, Ny = img.shape

@@ -56,6 +56,13 @@ class StJob(ctypes.Structure):
                 ("nPrec", _i32), ("pad0", _i32), ("img", _vp)]
 
 
+class StDatHeader(ctypes.Structure):
+    """st_dat_header of include/stem.h (the .dat file's header fields)."""
+    _fields_ = [("version", ctypes.c_char * 32), ("miller4", _i32), ("k", _d * 4), ("g", _d * 4), ("modg", _d),
+                ("nM", _i32), ("M", _i32 * 3), ("V", _d), ("xi0", _d), ("xig", _d), ("has_ng", _i32), ("ng", _d),
+                ("sg", _d), ("xmax", _d * 3), ("aperpx", _d), ("rotation", _d * 9)]
+
+
 class StemError(RuntimeError):
     def __init__(self, code, msg):
         super().__init__("libstem error %d: %s" % (code, msg))
@@ -85,6 +92,15 @@ _PROTOS = {
     "st_plan_last_error": (ctypes.c_char_p, [_vp]),
     "st_plan_destroy": (None, [_vp]),
     "st_tune_variants": (_i32, []),
+    "st_format_dat_header": (_i32, [ctypes.POINTER(StDatHeader), _i32, _i32, ctypes.c_char_p, _i64,
+                                    ctypes.POINTER(_i64)]),
+    "st_dat_text_bytes": (_i64, [_i64]),
+    "st_format_dat_device": (_i32, [_vp, _vp, _i64, _vp, _i64, _vp]),
+    "st_write_dat": (_i32, [_vp, ctypes.c_char_p, ctypes.POINTER(StDatHeader), _dp, _i32, _i32]),
+    "st_png_levels_device": (_i32, [_vp, _vp, _i32, _i32, _d, _d, _vp, _vp]),
+    "st_png16_bytes": (_i64, [_i32, _i32]),
+    "st_encode_png16": (_i32, [_vp, _i32, _i32, _vp, _i64, ctypes.POINTER(_i64)]),
+    "st_write_png": (_i32, [_vp, ctypes.c_char_p, _dp, _i32, _i32, _d, _d, _d]),
     # include/stem_host.h
     "st_d2bi_create": (_i32, [ctypes.POINTER(_vp), _dp, _i32, _i32, _i32, _d, _dp, _dp, _d, _i32, _i32]),
     "st_d2bi_destroy": (None, [_vp]),

@@ -171,4 +171,12 @@ cudaError_t launch_blur(const double* d_in, double* d_tmp, double* d_out, int nx
 
 __host__ __device__ inline int pack_cell(int cx, int cy, int cz) { return cx | (cy << 10) | (cz << 20); }
 
+// Output files (k_output.cu).  PNG levels: d_part holds 2 kLevelParts doubles (partial
+// minima and maxima), d_ab 2 (the level map); d_levels nx * ny values.
+constexpr int kLevelParts = 256;
+cudaError_t launch_png_levels(const double* d_img, int nx, int ny, double iso_min, double iso_max, double* d_part,
+                              double* d_ab, uint16_t* d_levels, cudaStream_t st);
+// '(1000f12.7)' records of n values (st_dat_text_bytes(n) bytes)
+cudaError_t launch_format_dat(const double* d_v, int64_t n, char* d_text, cudaStream_t st);
+
 }  // namespace stem

@@ -60,6 +60,12 @@ struct st_ctx {
   std::map<uint64_t, int> ring_big;  // (pass kind, image and link-cell shape) needing 256-atom slabs
   cudaEvent_t tev[3] = {nullptr, nullptr, nullptr};
   int last_ring_variant = -1;
+  double* d_lvaux = nullptr;  // PNG levels: partial minima/maxima and the level map
+  size_t cap_lvaux = 0;
+  uint16_t* d_levels = nullptr;
+  size_t cap_levels = 0;
+  char* d_text = nullptr;  // .dat records
+  size_t cap_text = 0;
 };
 
 namespace {
@@ -774,7 +780,8 @@ extern "C" void st_destroy(st_ctx* c) {
   void* dev_ptrs[] = {c->s.tmp_key, c->s.tmp_cell, c->s.tmp_slot, c->s.tmp_f, c->s.perm, c->s.block_sums,
                       c->s.counters, c->s.xtab, c->s.xfv, c->s.ytab, c->s.yfv, c->s.ztab, c->s.zfv, c->s.aa,
                       c->s.aaf, c->b.cell_start, c->b.cell_count, c->b.f64, c->b.cs64, c->b.p32, c->b.cs32,
-                      c->d_x, c->d_img, c->d_blur, c->d_kern, c->d_binjobs, c->d_coljobs, c->d_work, c->d_bx, c->d_bimg};
+                      c->d_x, c->d_img, c->d_blur, c->d_kern, c->d_binjobs, c->d_coljobs, c->d_work, c->d_bx, c->d_bimg,
+                      c->d_lvaux, c->d_levels, c->d_text};
   for (void* p : dev_ptrs)
     if (p) cudaFree(p);
   if (c->h_counters) cudaFreeHost(c->h_counters);
@@ -1212,3 +1219,107 @@ extern "C" int st_blur(st_ctx* c, const double* in, int32_t nx, int32_t ny, doub
   if (e != cudaSuccess) return cuda_fail(c, e, "copying blur output");
   return ST_OK;
 }
+
+// ---------------------------------------------------------------------------------------
+// Output files (src/d2bi.f90:1429-1457 and 1509-1538): the levels and the f12.7 records on
+// the GPU (k_output.cu), the header and the PNG container on the host (host_output.cpp).
+namespace {
+
+// write bytes to <path>.tmp, then rename it to path (as d2bi does with mv)
+int write_file(st_ctx* c, const char* path, const std::vector<std::pair<const char*, size_t>>& parts) {
+  const std::string tmp = std::string(path) + ".tmp";
+  FILE* f = std::fopen(tmp.c_str(), "wb");
+  if (!f) return fail(c, ST_ERR_ARG, "cannot open " + tmp + " for writing");
+  bool ok = true;
+  for (const auto& p : parts) ok = ok && std::fwrite(p.first, 1, p.second, f) == p.second;
+  ok = (std::fclose(f) == 0) && ok;
+  if (!ok || std::rename(tmp.c_str(), path) != 0) {
+    std::remove(tmp.c_str());
+    return fail(c, ST_ERR_ARG, std::string("writing ") + path + " failed");
+  }
+  return ST_OK;
+}
+
+}  // namespace
+
+extern "C" int st_png_levels_device(st_ctx* c, const double* d_img, int32_t nx, int32_t ny, double iso_min,
+                                    double iso_max, uint16_t* d_levels, void* stream) {
+  if (!c) return ST_ERR_ARG;
+  if (!d_img || !d_levels || nx < 1 || ny < 1) return fail(c, ST_ERR_ARG, "invalid PNG level arguments");
+  cudaSetDevice(c->device);
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+  cudaError_t e = ensure(c->d_lvaux, c->cap_lvaux, (size_t)2 * kLevelParts + 2);
+  if (e == cudaSuccess)
+    e = launch_png_levels(d_img, nx, ny, iso_min, iso_max, c->d_lvaux, c->d_lvaux + 2 * kLevelParts, d_levels, st);
+  if (e != cudaSuccess) return cuda_fail(c, e, "PNG levels");
+  return ST_OK;
+}
+
+extern "C" int st_write_png(st_ctx* c, const char* path, const double* img, int32_t nx, int32_t ny, double iso_min,
+                            double iso_max, double blur_t) {
+  if (!c) return ST_ERR_ARG;
+  if (!path || !img || nx < 1 || ny < 1) return fail(c, ST_ERR_ARG, "invalid PNG arguments");
+  cudaSetDevice(c->device);
+  const size_t n = (size_t)nx * ny;
+  cudaError_t e = ensure(c->d_blur, c->cap_blur, 3 * n + nx);
+  if (e == cudaSuccess) e = ensure(c->d_levels, c->cap_levels, n);
+  if (e != cudaSuccess) return cuda_fail(c, e, "allocating PNG buffers");
+  e = cudaMemcpyAsync(c->d_blur, img, n * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "copying the PNG image");
+  const double* src = c->d_blur;
+  if (blur_t > 0) {  // outputImgAsPng blurs first when png_blur > 0
+    double* d_out = c->d_blur + 2 * n + nx;
+    const int rc = st_blur_device(c, c->d_blur, nx, ny, blur_t, d_out, c->stream);
+    if (rc != ST_OK) return rc;
+    src = d_out;
+  }
+  int rc = st_png_levels_device(c, src, nx, ny, iso_min, iso_max, c->d_levels, c->stream);
+  if (rc != ST_OK) return rc;
+  std::vector<uint16_t> lv(n);
+  e = cudaMemcpyAsync(lv.data(), c->d_levels, n * sizeof(uint16_t), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "PNG levels");
+  const int64_t cap = st_png16_bytes(nx, ny);
+  std::vector<uint8_t> png((size_t)cap);
+  int64_t len = 0;
+  rc = st_encode_png16(lv.data(), nx, ny, png.data(), cap, &len);
+  if (rc != ST_OK) return fail(c, rc, "PNG encoding (image too large for one IDAT chunk)");
+  return write_file(c, path, {{(const char*)png.data(), (size_t)len}});
+}
+
+extern "C" int st_format_dat_device(st_ctx* c, const double* d_v, int64_t n, char* d_text, int64_t cap,
+                                    void* stream) {
+  if (!c) return ST_ERR_ARG;
+  if (!d_v || !d_text || n < 0 || cap < st_dat_text_bytes(n)) return fail(c, ST_ERR_ARG, "invalid .dat arguments");
+  cudaSetDevice(c->device);
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+  const cudaError_t e = launch_format_dat(d_v, n, d_text, st);
+  if (e != cudaSuccess) return cuda_fail(c, e, ".dat records");
+  return ST_OK;
+}
+
+extern "C" int st_write_dat(st_ctx* c, const char* path, const st_dat_header* h, const double* img, int32_t nx,
+                            int32_t ny) {
+  if (!c) return ST_ERR_ARG;
+  if (!path || !h || !img || nx < 1 || ny < 1) return fail(c, ST_ERR_ARG, "invalid .dat arguments");
+  std::vector<char> head(4096);
+  int64_t hlen = 0;
+  int rc = st_format_dat_header(h, nx, ny, head.data(), (int64_t)head.size(), &hlen);
+  if (rc != ST_OK) return fail(c, rc, "invalid .dat header");
+  cudaSetDevice(c->device);
+  const size_t n = (size_t)nx * ny;
+  const int64_t tb = st_dat_text_bytes((int64_t)n);
+  cudaError_t e = ensure(c->d_img, c->cap_img, n);
+  if (e == cudaSuccess) e = ensure(c->d_text, c->cap_text, (size_t)tb);
+  if (e != cudaSuccess) return cuda_fail(c, e, "allocating .dat buffers");
+  e = cudaMemcpyAsync(c->d_img, img, n * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "copying the .dat image");
+  rc = st_format_dat_device(c, c->d_img, (int64_t)n, c->d_text, tb, c->stream);
+  if (rc != ST_OK) return rc;
+  std::vector<char> text((size_t)tb);
+  e = cudaMemcpyAsync(text.data(), c->d_text, (size_t)tb, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, ".dat records");
+  return write_file(c, path, {{head.data(), (size_t)hlen}, {text.data(), (size_t)tb}});
+}
+

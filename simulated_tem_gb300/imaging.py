@@ -14,6 +14,7 @@ array (the Fortran (3, N) array in memory), images are (Mx, My) arrays in
 Fortran order (the reference's column-major d2big2).
 """
 import ctypes
+import os
 
 import numpy as np
 
@@ -145,6 +146,32 @@ class Context:
         self._check(lib().st_blur_device(self.handle, ctypes.c_void_p(in_ptr), nx, ny, float(t),
                                          ctypes.c_void_p(out_ptr), ctypes.c_void_p(stream)))
 
+    def write_dat(self, path, header, img):
+        """st_write_dat: d2bi's .dat file of an (Nx, Ny) image; `header` a dict of
+        dat_header() fields or an StDatHeader."""
+        img = np.asfortranarray(img, dtype=np.float64)
+        h = header if isinstance(header, _lib.StDatHeader) else dat_header(**header)
+        self._check(lib().st_write_dat(self.handle, os.fsencode(path), ctypes.byref(h), _ptr(img), img.shape[0],
+                                       img.shape[1]))
+
+    def write_png(self, path, img, iso_min=0.0, iso_max=0.0, blur_t=0.0):
+        """st_write_png: d2bi's 16-bit PNG of an (Nx, Ny) image (normalised when iso_min ==
+        iso_max, else scaled to that window), blurred first when blur_t > 0 pixels."""
+        img = np.asfortranarray(img, dtype=np.float64)
+        self._check(lib().st_write_png(self.handle, os.fsencode(path), _ptr(img), img.shape[0], img.shape[1],
+                                       float(iso_min), float(iso_max), float(blur_t)))
+
+    def png_levels_device(self, img_ptr, nx, ny, levels_ptr, iso_min=0.0, iso_max=0.0, stream=0):
+        """st_png_levels_device: nx * ny uint16 levels (x fastest) of a device image."""
+        self._check(lib().st_png_levels_device(self.handle, ctypes.c_void_p(img_ptr), nx, ny, float(iso_min),
+                                               float(iso_max), ctypes.c_void_p(levels_ptr),
+                                               ctypes.c_void_p(stream)))
+
+    def format_dat_device(self, v_ptr, n, text_ptr, cap, stream=0):
+        """st_format_dat_device: the '(1000f12.7)' records of n device values."""
+        self._check(lib().st_format_dat_device(self.handle, ctypes.c_void_p(v_ptr), int(n),
+                                               ctypes.c_void_p(text_ptr), int(cap), ctypes.c_void_p(stream)))
+
     def tune(self, mode):
         """st_tune: ST_TUNE_AUTO, ST_TUNE_OFF or a forced slab-ring variant (0 .. st_tune_variants() - 1)."""
         self._check(lib().st_tune(self.handle, int(mode)))
@@ -274,6 +301,53 @@ class DynamicalTwoBeamImaging:
         check(lib().st_d2bi_compute_img(self.handle, ctx.handle, _ptr(x), x.shape[1], x.shape[0], float(prec_angle),
                                         int(n_prec), int(flags), _ptr(img)), ctx.handle)
         return img
+
+
+def dat_header(version="1.1.6", k=(0, 0, 1), g=(1, 1, 0), modg=0.0, M=(4, 4), V=200.0, xi0=103.889565,
+               xig=207.531624, ng=None, sg=0.0, xmax=(0, 0, 0), aperpx=1.0, rotation=np.eye(3), miller4=False):
+    """An StDatHeader from the fields d2bi writes (rotation: the 3 x 3 matrix matmul(R, U))."""
+    h = _lib.StDatHeader()
+    h.version = version.encode()[:31]
+    h.miller4 = 1 if miller4 else 0
+    for i, v in enumerate(k):
+        h.k[i] = v
+    for i, v in enumerate(g):
+        h.g[i] = v
+    h.modg = modg
+    h.nM = len(M)
+    for i, v in enumerate(M):
+        h.M[i] = int(v)
+    h.V, h.xi0, h.xig = V, xi0, xig
+    h.has_ng = 0 if ng is None else 1
+    h.ng = 0.0 if ng is None else ng
+    h.sg = sg
+    for i, v in enumerate(xmax):
+        h.xmax[i] = v
+    h.aperpx = aperpx
+    rot = np.asarray(rotation, dtype=np.float64)
+    for i, v in enumerate(rot.reshape(-1) if rot.ndim == 1 else rot.T.reshape(-1)):  # column-major
+        h.rotation[i] = v
+    return h
+
+
+def format_dat_header(header, nx, ny):
+    """st_format_dat_header: the .dat header and size lines (str)."""
+    h = header if isinstance(header, _lib.StDatHeader) else dat_header(**header)
+    buf = ctypes.create_string_buffer(4096)
+    n = ctypes.c_int64(0)
+    _lib.check(lib().st_format_dat_header(ctypes.byref(h), nx, ny, buf, 4096, ctypes.byref(n)))
+    return buf.raw[:n.value].decode()
+
+
+def encode_png16(levels):
+    """st_encode_png16: a 16-bit greyscale PNG (bytes) of levels [row y, column x]."""
+    lv = np.ascontiguousarray(levels, dtype=np.uint16)
+    ny, nx = lv.shape
+    cap = lib().st_png16_bytes(nx, ny)
+    out = ctypes.create_string_buffer(int(cap))
+    n = ctypes.c_int64(0)
+    _lib.check(lib().st_encode_png16(ctypes.c_void_p(lv.ctypes.data), nx, ny, out, cap, ctypes.byref(n)))
+    return out.raw[:n.value]
 
 
 def wrap_pbc(a_super, M, a0, x):

@@ -9,6 +9,8 @@ data and writes compact fixtures beside this script:
   (``Data/test/test.i111_loop_W.lammps.g2_0_0.k0.00_0.00_1.00_ng1.00.dat``).
 * ``w_loop_png.npz``     -- the 16-bit greyscale levels of the shipped PNG of
   that image (decoded here with zlib; no imaging library is needed).
+* ``w_loop_dat_text.json`` -- the same .dat file as text: its header lines, the size
+  line, and its first and last '(1000f12.7)' records (the output-format fixture).
 * ``linkcell_kat.json``  -- the 200 points and the stored neighbour list of
   ``test/testLib_LinkCell3D.f90``.
 * ``electrons_kat.json`` -- the stored wavelength/velocity strings of
@@ -123,6 +125,15 @@ def decode_png16(path):
     return levels.astype(np.uint16)  # [row y, column x]
 
 
+def dat_text(path):
+    with open(path) as f:
+        lines = f.read().split("\n")
+    k = next(i for i, line in enumerate(lines) if not line.startswith("#"))
+    records = [line for line in lines[k + 1:] if line]
+    return {"header_lines": lines[:k + 1], "n_records": len(records), "first_record": records[0],
+            "last_record": records[-1]}
+
+
 def linkcell_kat(path):
     with open(path) as f:
         text = f.read()
@@ -158,6 +169,8 @@ def main(ref):
     header, img = read_dat(os.path.join(ref, dat + ".dat"))
     np.savez_compressed(os.path.join(HERE, "w_loop_dat.npz"), img=img,
                         header=json.dumps(header))
+    with open(os.path.join(HERE, "w_loop_dat_text.json"), "w") as f:
+        json.dump(dat_text(os.path.join(ref, dat + ".dat")), f)
     levels = decode_png16(os.path.join(ref, dat + ".png"))
     np.savez_compressed(os.path.join(HERE, "w_loop_png.npz"), levels=levels)
     with open(os.path.join(HERE, "linkcell_kat.json"), "w") as f:
