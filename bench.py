@@ -404,6 +404,57 @@ def io_leg(ctx, stream, flush, steps, warmup, cpu=True):
     return out
 
 
+def input_leg(ctx, cell, stream, steps, warmup, cpu=True):
+    """Reading the 1.2M-atom cell from a LAMMPS data file (written here with shortest
+    round-trip coordinates, the layout of LAMMPS' write_data): st_read_lammps end to end
+    (file to host positions: read, copy, GPU parse, copy back), the GPU parse alone on the
+    resident text (CUDA events), and the oracle's reader (fgets + sscanf, one core)."""
+    import tempfile
+
+    import torch
+
+    from simulated_tem_gb300 import imaging, synth
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, "cell.lammps")
+        synth.write_lammps(path, cell.pos, np.diag(cell.a_super))
+        info = imaging.lammps_header(path)
+        nb = info.file_bytes - info.data_offset
+        walls = []
+        for i in range(warmup + steps):
+            t0 = time.perf_counter()
+            x, _, _ = ctx.read_lammps(path, info)
+            if i >= warmup:
+                walls.append(time.perf_counter() - t0)
+        exact = bool(np.array_equal(x, cell.pos))
+        with open(path, "rb") as f:
+            f.seek(info.data_offset)
+            text = np.frombuffer(f.read(), dtype=np.uint8)
+        d_t = torch.from_numpy(text.copy()).cuda()
+        d_x = torch.empty((info.n_atoms, 3), dtype=torch.float64, device="cuda")
+        sp = stream.cuda_stream
+        ms = []
+        for i in range(warmup + steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            ctx.parse_atoms_device(d_t.data_ptr(), nb, info.n_atoms, d_x.data_ptr(), stream=sp)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if i >= warmup:
+                ms.append(e0.elapsed_time(e1))
+        out = {"workload": "LAMMPS data file of the 1.2M-atom cell (%d atoms, %.1f MB of atom lines)"
+                           % (info.n_atoms, nb / 1e6),
+               "read_file_ms": float(np.median(walls)) * 1e3, "positions_exact": exact,
+               "gpu_parse_ms": float(np.median(ms)), "gpu_parse_GB_per_s": nb / float(np.median(ms)) / 1e6,
+               "note": "read_file: st_read_lammps, file in the page cache; gpu_parse: text resident in HBM"}
+        if cpu:
+            from oracle import stem_oracle as O
+            t0 = time.perf_counter()
+            O.read_lammps_atoms(path, info.data_offset, info.n_atoms)
+            out["cpu_oracle"] = {"ms": (time.perf_counter() - t0) * 1e3, "cores": 1, "kind": "port",
+                                 "note": "oracle reader: fgets + sscanf per atom line, one core"}
+    return out
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -521,6 +572,8 @@ def run_gpu(args):
         cfg5 = None if args.no_batched else cfg5_leg(ctx, stream, flush, 3, args.warmup)
         io = None if args.no_batched else io_leg(ctx, stream, flush, 5, args.warmup,
                                                   cpu=(rank == 0 and not args.no_cpu))
+        inp = None if args.no_batched else input_leg(ctx, cell, stream, 3, args.warmup,
+                                                     cpu=(rank == 0 and not args.no_cpu))
     step_ms = [a.elapsed_time(b) for a, b in ev]
     ms = float(np.mean(step_ms))
     if ws > 1:
@@ -603,7 +656,7 @@ def run_gpu(args):
                          "rms_dI_fp32_vs_fp64": float(np.sqrt((d ** 2).mean()))},
             "gpu_launches": args.steps * launches_per_image(n_prec, fp32=True, average=True),
             "roofline": roof, "peaks": peaks, "wall_s": wall, "clocks": clk.summary(), "batched": batched, "cfg1_128k": cfg1, "cfg5_corrector": cfg5,
-            "output_files": io}
+            "output_files": io, "input_file": inp}
     if rank == 0:
         if ws == 1 and not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline(x_state=(cell, t, x), rows=args.cpu_rows)

@@ -286,6 +286,42 @@ int st_encode_png16(const uint16_t* levels, int32_t nx, int32_t ny, uint8_t* out
 int st_write_png(st_ctx* ctx, const char* path, const double* img, int32_t nx, int32_t ny, double iso_min,
                  double iso_max, double blur_t);
 
+/* ---- Input: the LAMMPS data files d2bi reads (src/Lib_XYZFiles.f90) ----------------- */
+typedef struct st_lammps_info {
+  int64_t n_atoms;      /* the "atoms" line */
+  int32_t n_types;      /* the "atom types" line */
+  int32_t pad0;
+  double lo[3], hi[3];  /* the xlo xhi, ylo yhi, zlo zhi lines */
+  int64_t data_offset;  /* byte offset of the first atom line */
+  int64_t file_bytes;
+} st_lammps_info;
+
+/* The header of a LAMMPS data file, read as readHeader_lammps and input_lammps read it
+ * (src/Lib_XYZFiles.f90:628-716, 1092-1101).  Host only. */
+int st_lammps_header(const char* path, st_lammps_info* info);
+
+/* The atom lines of a LAMMPS Atoms block in device memory (d_text, n_bytes, starting at
+ * the first atom line): for atom i, the line's id, type, x, y, z as a list-directed read
+ * gives them (src/Lib_XYZFiles.f90:1108-1117): d_x[i ldx + 0..2] = x, y, z (correctly
+ * rounded), d_types[i] = type (d_types may be null).  Blanks and commas separate values;
+ * the rest of a line is ignored.  A missing or malformed value returns ST_ERR_ARG with the
+ * first such line (0-based within the block) in *bad_line (-1 when none).  Waits for the
+ * parse to finish. */
+int st_parse_atoms_device(st_ctx* ctx, const char* d_text, int64_t n_bytes, int64_t n_atoms, double* d_x,
+                          int64_t ldx, int32_t* d_types, int64_t* bad_line, void* stream);
+
+/* The number parser of st_parse_atoms_device, on the host: the correctly rounded FP64 value
+ * of the decimal number starting at text (len bytes; Fortran D exponents accepted), *used =
+ * the characters it spans.  ST_ERR_ARG for malformed text or a value outside the parser's
+ * exact range (normal numbers from about 1e-20 to 1e38). */
+int st_parse_real(const char* text, int64_t len, double* out, int32_t* used);
+
+/* A LAMMPS data file into host arrays: x(ldx, n_atoms) rows 0..2 = positions (ldx >= 3;
+ * other rows untouched), types (n_atoms values, may be null).  info: the header
+ * (st_lammps_header); the atom lines are parsed on the GPU. */
+int st_read_lammps(st_ctx* ctx, const char* path, const st_lammps_info* info, double* x, int64_t ldx,
+                   int32_t* types);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1268,3 +1268,34 @@ long long oc_format_f12_7(const double* v, long long n, char* out) {
   return p;
 }
 
+long long oc_read_lammps_atoms(const char* path, long long offset, long long n_atoms, double* x, int* types) {
+  FILE* f = fopen(path, "rb");
+  if (!f) return 1;
+  fseek(f, offset, SEEK_SET);
+  size_t cap = 1 << 16;
+  char* line = (char*)malloc(cap);
+  long long bad = 0;
+  for (long long i = 0; i < n_atoms; ++i) {
+    if (!fgets(line, (int)cap, f)) {
+      bad = i + 1;
+      break;
+    }
+    for (char* q = line; *q; ++q)
+      if (*q == ',') *q = ' ';  /* list-directed reads also separate by commas */
+    long long id;
+    int ty;
+    double a, b, c;
+    if (sscanf(line, "%lld %d %lf %lf %lf", &id, &ty, &a, &b, &c) != 5) {
+      bad = i + 1;
+      break;
+    }
+    x[3 * i] = a;
+    x[3 * i + 1] = b;
+    x[3 * i + 2] = c;
+    types[i] = ty;
+  }
+  free(line);
+  fclose(f);
+  return bad;
+}
+

@@ -189,6 +189,10 @@ void oc_png_levels_window(const double* img, int Nx, int Ny, double lo, double h
  * Fortran F12.7 editing, a newline after each 1000 values and after the last; returns
  * the number of bytes written to out. */
 long long oc_format_f12_7(const double* v, long long n, char* out);
+/* input_lammps (src/Lib_XYZFiles.f90:1108-1117): from byte offset `offset` of the file,
+ * n_atoms lines read as id, type, x, y, z (strtod-rounded); x(3, n), types(n).  Returns
+ * 0, or 1 + the 0-based index of the first line that does not hold five values. */
+long long oc_read_lammps_atoms(const char* path, long long offset, long long n_atoms, double* x, int* types);
 
 #ifdef __cplusplus
 }

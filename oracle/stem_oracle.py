@@ -250,6 +250,19 @@ def dat_header(h, nx, ny):
     return "\n".join(out) + "\n"
 
 
+def read_lammps_atoms(path, offset, n_atoms):
+    """input_lammps's atom lines: (positions (n, 3), types (n,)); raises on a bad line."""
+    x = np.zeros((n_atoms, 3), dtype=np.float64)
+    ty = np.zeros(n_atoms, dtype=np.int32)
+    L = lib()
+    L.oc_read_lammps_atoms.restype = ctypes.c_longlong
+    bad = L.oc_read_lammps_atoms(os.fsencode(path), ctypes.c_longlong(offset), ctypes.c_longlong(n_atoms),
+                                 _dptr(x), ty.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
+    if bad:
+        raise ValueError("atom line %d does not hold id type x y z" % bad)
+    return x, ty
+
+
 def png_levels(img):
     img = np.asfortranarray(img, dtype=np.float64)
     Nx, Ny = img.shape

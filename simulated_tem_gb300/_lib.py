@@ -63,6 +63,12 @@ class StDatHeader(ctypes.Structure):
                 ("sg", _d), ("xmax", _d * 3), ("aperpx", _d), ("rotation", _d * 9)]
 
 
+class StLammpsInfo(ctypes.Structure):
+    """st_lammps_info of include/stem.h (a LAMMPS data file's header)."""
+    _fields_ = [("n_atoms", _i64), ("n_types", _i32), ("pad0", _i32), ("lo", _d * 3), ("hi", _d * 3),
+                ("data_offset", _i64), ("file_bytes", _i64)]
+
+
 class StemError(RuntimeError):
     def __init__(self, code, msg):
         super().__init__("libstem error %d: %s" % (code, msg))
@@ -101,6 +107,10 @@ _PROTOS = {
     "st_png16_bytes": (_i64, [_i32, _i32]),
     "st_encode_png16": (_i32, [_vp, _i32, _i32, _vp, _i64, ctypes.POINTER(_i64)]),
     "st_write_png": (_i32, [_vp, ctypes.c_char_p, _dp, _i32, _i32, _d, _d, _d]),
+    "st_lammps_header": (_i32, [ctypes.c_char_p, ctypes.POINTER(StLammpsInfo)]),
+    "st_parse_real": (_i32, [ctypes.c_char_p, _i64, _dp, ctypes.POINTER(_i32)]),
+    "st_parse_atoms_device": (_i32, [_vp, _vp, _i64, _i64, _vp, _i64, _vp, ctypes.POINTER(_i64), _vp]),
+    "st_read_lammps": (_i32, [_vp, ctypes.c_char_p, ctypes.POINTER(StLammpsInfo), _dp, _i64, _vp]),
     # include/stem_host.h
     "st_d2bi_create": (_i32, [ctypes.POINTER(_vp), _dp, _i32, _i32, _i32, _d, _dp, _dp, _d, _i32, _i32]),
     "st_d2bi_destroy": (None, [_vp]),

@@ -178,5 +178,11 @@ cudaError_t launch_png_levels(const double* d_img, int nx, int ny, double iso_mi
                               double* d_ab, uint16_t* d_levels, cudaStream_t st);
 // '(1000f12.7)' records of n values (st_dat_text_bytes(n) bytes)
 cudaError_t launch_format_dat(const double* d_v, int64_t n, char* d_text, cudaStream_t st);
+// LAMMPS Atoms block (k_parse.cu): d_seg holds parse_segments(n_bytes) values, d_starts
+// n_atoms; *d_bad = the first malformed atom line, or all ones
+int64_t parse_segments(int64_t n_bytes);
+cudaError_t launch_parse_atoms(const char* d_text, int64_t n_bytes, int64_t n_atoms, long long* d_seg,
+                               long long* d_starts, double* d_x, int64_t ldx, int* d_types,
+                               unsigned long long* d_bad, cudaStream_t st);
 
 }  // namespace stem

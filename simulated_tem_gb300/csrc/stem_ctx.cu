@@ -64,8 +64,16 @@ struct st_ctx {
   size_t cap_lvaux = 0;
   uint16_t* d_levels = nullptr;
   size_t cap_levels = 0;
-  char* d_text = nullptr;  // .dat records
+  char* d_text = nullptr;  // .dat records; LAMMPS text
   size_t cap_text = 0;
+  long long* d_pseg = nullptr;  // LAMMPS parse: segment counts, line starts
+  size_t cap_pseg = 0;
+  long long* d_pstart = nullptr;
+  size_t cap_pstart = 0;
+  unsigned long long* d_pbad = nullptr;
+  size_t cap_pbad = 0;
+  void* h_text = nullptr;  // pinned staging of a data file
+  size_t cap_htext = 0;
 };
 
 namespace {
@@ -781,11 +789,12 @@ extern "C" void st_destroy(st_ctx* c) {
                       c->s.counters, c->s.xtab, c->s.xfv, c->s.ytab, c->s.yfv, c->s.ztab, c->s.zfv, c->s.aa,
                       c->s.aaf, c->b.cell_start, c->b.cell_count, c->b.f64, c->b.cs64, c->b.p32, c->b.cs32,
                       c->d_x, c->d_img, c->d_blur, c->d_kern, c->d_binjobs, c->d_coljobs, c->d_work, c->d_bx, c->d_bimg,
-                      c->d_lvaux, c->d_levels, c->d_text};
+                      c->d_lvaux, c->d_levels, c->d_text, c->d_pseg, c->d_pstart, c->d_pbad};
   for (void* p : dev_ptrs)
     if (p) cudaFree(p);
   if (c->h_counters) cudaFreeHost(c->h_counters);
   if (c->h_stage) cudaFreeHost(c->h_stage);
+  if (c->h_text) cudaFreeHost(c->h_text);
   for (auto& e : c->ev)
     if (e) cudaEventDestroy(e);
   for (auto& e : c->tev)
@@ -1321,5 +1330,95 @@ extern "C" int st_write_dat(st_ctx* c, const char* path, const st_dat_header* h,
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return cuda_fail(c, e, ".dat records");
   return write_file(c, path, {{head.data(), (size_t)hlen}, {text.data(), (size_t)tb}});
+}
+
+// ---------------------------------------------------------------------------------------
+// Input: the atom lines of LAMMPS data files parsed on the GPU (k_parse.cu)
+
+extern "C" int st_parse_atoms_device(st_ctx* c, const char* d_text, int64_t n_bytes, int64_t n_atoms, double* d_x,
+                                     int64_t ldx, int32_t* d_types, int64_t* bad_line, void* stream) {
+  if (!c) return ST_ERR_ARG;
+  if (bad_line) *bad_line = -1;
+  if (!d_text || n_bytes < 0 || n_atoms < 0 || !d_x || ldx < 3)
+    return fail(c, ST_ERR_ARG, "invalid atom-line arguments");
+  if (n_atoms == 0) return ST_OK;
+  if (n_bytes == 0) {
+    if (bad_line) *bad_line = 0;
+    return fail(c, ST_ERR_ARG, "no atom lines");
+  }
+  cudaSetDevice(c->device);
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+  cudaError_t e = ensure(c->d_pseg, c->cap_pseg, (size_t)parse_segments(n_bytes) + 1);
+  if (e == cudaSuccess) e = ensure(c->d_pstart, c->cap_pstart, (size_t)n_atoms);
+  if (e == cudaSuccess) e = ensure(c->d_pbad, c->cap_pbad, 1);
+  if (e != cudaSuccess) return cuda_fail(c, e, "allocating parse buffers");
+  e = launch_parse_atoms(d_text, n_bytes, n_atoms, c->d_pseg, c->d_pstart, d_x, ldx, d_types, c->d_pbad, st);
+  unsigned long long bad = ~0ull;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(c->h_counters, c->d_pbad, sizeof bad, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(c, e, "parsing atom lines");
+  bad = c->h_counters[0];
+  if (bad != ~0ull) {
+    if (bad_line) *bad_line = (int64_t)bad;
+    return fail(c, ST_ERR_ARG, "atom line " + std::to_string(bad + 1) +
+                                   " of the Atoms block is missing or malformed (id type x y z expected)");
+  }
+  return ST_OK;
+}
+
+extern "C" int st_read_lammps(st_ctx* c, const char* path, const st_lammps_info* info, double* x, int64_t ldx,
+                              int32_t* types) {
+  if (!c) return ST_ERR_ARG;
+  if (!path || !info || !x || ldx < 3 || info->n_atoms < 0 || info->data_offset < 0)
+    return fail(c, ST_ERR_ARG, "invalid LAMMPS read arguments");
+  const int64_t n = info->n_atoms;
+  if (n == 0) return ST_OK;
+  cudaSetDevice(c->device);
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return fail(c, ST_ERR_ARG, std::string("cannot open ") + path);
+  std::fseek(f, 0, SEEK_END);
+  const long long size = std::ftell(f);
+  const long long nb = size - info->data_offset;
+  if (nb <= 0) {
+    std::fclose(f);
+    return fail(c, ST_ERR_ARG, "no atom lines after the header");
+  }
+  cudaError_t e = ensure_host(c->h_text, c->cap_htext, (size_t)nb);
+  if (e == cudaSuccess) e = ensure(c->d_text, c->cap_text, (size_t)nb);
+  if (e == cudaSuccess) e = ensure(c->d_x, c->cap_x, (size_t)3 * n);
+  if (e != cudaSuccess) {
+    std::fclose(f);
+    return cuda_fail(c, e, "allocating read buffers");
+  }
+  std::fseek(f, info->data_offset, SEEK_SET);
+  const size_t got = std::fread(c->h_text, 1, (size_t)nb, f);
+  std::fclose(f);
+  if (got != (size_t)nb) return fail(c, ST_ERR_ARG, std::string("reading ") + path + " failed");
+  e = cudaMemcpyAsync(c->d_text, c->h_text, (size_t)nb, cudaMemcpyHostToDevice, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "copying the atom lines");
+  int32_t* d_types = nullptr;
+  if (types) {
+    e = ensure(c->d_bimg, c->cap_bimg, (size_t)(n + 1) / 2);  // n int32 in the batch-image scratch
+    if (e != cudaSuccess) return cuda_fail(c, e, "allocating read buffers");
+    d_types = reinterpret_cast<int32_t*>(c->d_bimg);
+  }
+  int64_t bad = -1;
+  const int rc = st_parse_atoms_device(c, c->d_text, nb, n, c->d_x, 3, d_types, &bad, c->stream);
+  if (rc != ST_OK) return rc;
+  std::vector<double> xs;
+  double* dst = x;
+  if (ldx != 3) {
+    xs.resize((size_t)3 * n);
+    dst = xs.data();
+  }
+  e = cudaMemcpyAsync(dst, c->d_x, (size_t)3 * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess && types)
+    e = cudaMemcpyAsync(types, d_types, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "copying the positions");
+  if (ldx != 3)
+    for (int64_t i = 0; i < n; ++i)
+      for (int k = 0; k < 3; ++k) x[i * ldx + k] = xs[(size_t)3 * i + k];
+  return ST_OK;
 }
 

@@ -172,6 +172,27 @@ class Context:
         self._check(lib().st_format_dat_device(self.handle, ctypes.c_void_p(v_ptr), int(n),
                                                ctypes.c_void_p(text_ptr), int(cap), ctypes.c_void_p(stream)))
 
+    def read_lammps(self, path, info=None):
+        """st_read_lammps: (positions (N, 3), types (N,), header) of a LAMMPS data file, the
+        atom lines parsed on the GPU."""
+        info = lammps_header(path) if info is None else info
+        n = info.n_atoms
+        x = np.zeros((n, 3), dtype=np.float64)
+        types = np.zeros(n, dtype=np.int32)
+        self._check(lib().st_read_lammps(self.handle, os.fsencode(path), ctypes.byref(info), _ptr(x), 3,
+                                         ctypes.c_void_p(types.ctypes.data)))
+        return x, types, info
+
+    def parse_atoms_device(self, text_ptr, n_bytes, n_atoms, x_ptr, types_ptr=0, stream=0):
+        """st_parse_atoms_device on device buffers; returns the first bad line or -1."""
+        bad = ctypes.c_int64(-1)
+        code = lib().st_parse_atoms_device(self.handle, ctypes.c_void_p(text_ptr), int(n_bytes), int(n_atoms),
+                                           ctypes.c_void_p(x_ptr), 3, ctypes.c_void_p(types_ptr) if types_ptr else None,
+                                           ctypes.byref(bad), ctypes.c_void_p(stream))
+        if code != _lib.ST_OK and bad.value < 0:
+            self._check(code)
+        return bad.value
+
     def tune(self, mode):
         """st_tune: ST_TUNE_AUTO, ST_TUNE_OFF or a forced slab-ring variant (0 .. st_tune_variants() - 1)."""
         self._check(lib().st_tune(self.handle, int(mode)))
@@ -348,6 +369,16 @@ def encode_png16(levels):
     n = ctypes.c_int64(0)
     _lib.check(lib().st_encode_png16(ctypes.c_void_p(lv.ctypes.data), nx, ny, out, cap, ctypes.byref(n)))
     return out.raw[:n.value]
+
+
+def lammps_header(path):
+    """st_lammps_header: the StLammpsInfo of a LAMMPS data file (n_atoms, n_types, lo, hi,
+    data_offset)."""
+    info = _lib.StLammpsInfo()
+    code = lib().st_lammps_header(os.fsencode(path), ctypes.byref(info))
+    if code != _lib.ST_OK:
+        raise _lib.StemError(code, "cannot read the LAMMPS header of %s" % path)
+    return info
 
 
 def wrap_pbc(a_super, M, a0, x):

@@ -106,3 +106,22 @@ def uneven_cells(count=256, seed=BASE_SEED + 4, lo=10_000, hi=500_000):
                          name="cell %d" % i)
         out.append((cell, sg))
     return out
+
+
+def write_lammps(path, pos, box_hi, mass=55.845, box_lo=(0.0, 0.0, 0.0)):
+    """A LAMMPS data file in the layout of LAMMPS' write_data (atom_style atomic, one type):
+    the reference's input format (src/Lib_XYZFiles.f90:628-716, 1061-1117).  Coordinates are
+    written as the shortest decimal strings that read back to the same doubles."""
+    pos = np.asarray(pos, dtype=np.float64)
+    n = len(pos)
+    head = ["LAMMPS data file written by simulated_tem_gb300.synth", "", "%d atoms" % n, "1 atom types", ""]
+    for k, ax in enumerate("xyz"):
+        head.append("%r %r %slo %shi" % (float(box_lo[k]), float(box_hi[k]), ax, ax))
+    head += ["", "Masses", "", "1 %r" % mass, "", "Atoms # atomic", ""]
+    with open(path, "w") as f:
+        f.write("\n".join(head) + "\n")
+        chunk = 100_000
+        for s in range(0, n, chunk):
+            p = pos[s:s + chunk]
+            f.write("".join("%d 1 %r %r %r 0 0 0\n" % (s + i + 1, a, b, c)
+                            for i, (a, b, c) in enumerate(p.tolist())))

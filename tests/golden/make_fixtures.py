@@ -11,6 +11,8 @@ data and writes compact fixtures beside this script:
   that image (decoded here with zlib; no imaging library is needed).
 * ``w_loop_dat_text.json`` -- the same .dat file as text: its header lines, the size
   line, and its first and last '(1000f12.7)' records (the output-format fixture).
+* ``w_loop_head.lammps`` -- the first 3,000 atom lines of that input with its header
+  (the atom count line set to 3000): the reader's fixture.
 * ``linkcell_kat.json``  -- the 200 points and the stored neighbour list of
   ``test/testLib_LinkCell3D.f90``.
 * ``electrons_kat.json`` -- the stored wavelength/velocity strings of
@@ -125,6 +127,14 @@ def decode_png16(path):
     return levels.astype(np.uint16)  # [row y, column x]
 
 
+def lammps_head(path, n=3000):
+    with open(path) as f:
+        lines = f.read().split("\n")
+    k = next(i for i, line in enumerate(lines) if line.startswith("Atoms")) + 2
+    head = [("%d atoms" % n) if line.strip().endswith(" atoms") else line for line in lines[:k]]
+    return "\n".join(head + lines[k:k + n]) + "\n"
+
+
 def dat_text(path):
     with open(path) as f:
         lines = f.read().split("\n")
@@ -169,6 +179,8 @@ def main(ref):
     header, img = read_dat(os.path.join(ref, dat + ".dat"))
     np.savez_compressed(os.path.join(HERE, "w_loop_dat.npz"), img=img,
                         header=json.dumps(header))
+    with open(os.path.join(HERE, "w_loop_head.lammps"), "w") as f:
+        f.write(lammps_head(os.path.join(ref, "Data/test/test.i111_loop_W.lammps")))
     with open(os.path.join(HERE, "w_loop_dat_text.json"), "w") as f:
         json.dump(dat_text(os.path.join(ref, dat + ".dat")), f)
     levels = decode_png16(os.path.join(ref, dat + ".png"))
