@@ -520,7 +520,7 @@ def measure_fp32_peak():
 def run_gpu(args):
     import torch
 
-    from simulated_tem_gb300 import _lib, imaging
+    from simulated_tem_gb300 import _lib, imaging, replicas
 
     ws, rank, local = dist_env()
     torch.cuda.set_device(local)
@@ -576,11 +576,8 @@ def run_gpu(args):
                                                      cpu=(rank == 0 and not args.no_cpu))
     step_ms = [a.elapsed_time(b) for a, b in ev]
     ms = float(np.mean(step_ms))
-    if ws > 1:
-        tmax = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(tmax, op=torch.distributed.ReduceOp.MAX)
-        ms = float(tmax.item())
-    value = ws * 1000.0 / ms
+    # replicas: one image per rank per step; the slowest rank's time, all ranks' images
+    value, ms, _ = replicas.job_rate(ms, 1)
     img32 = d_img.cpu().numpy().T.copy()
 
     # end to end through st_image from pinned host memory
@@ -605,12 +602,12 @@ def run_gpu(args):
         t1 = time.perf_counter()
         e2e_step()
         e2e_ms.append((time.perf_counter() - t1) * 1e3)
-    e2e_value = ws * 1000.0 / float(np.mean(e2e_ms))
+    e2e_value, _, _ = replicas.job_rate(float(np.mean(e2e_ms)), 1)
 
     # the same image recorded as a CUDA graph (st_plan) and replayed
     pms = time_plan(ctx, [(G, d_x.data_ptr(), len(x), aa, d_img.data_ptr())], flags, stream, args.steps,
                     args.warmup, flush)
-    plan_value = ws * 1000.0 / float(np.mean(pms))
+    plan_value, _, _ = replicas.job_rate(float(np.mean(pms)), 1)
 
     # plain FP64 GPU path on the same image
     step(_lib.ST_FLAG_AVERAGE)
