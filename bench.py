@@ -769,8 +769,24 @@ def ncu_case(args):
     """Untimed cases for ncu captures.  fp32 / fp64: two images of the workload through
     st_image, nothing else (binning and column kernels).  cfg1: one warm-up and one step of
     the 128k-atom DF + BF + blur leg on both paths (FP64 column kernel, blur).  corrector:
-    one warm-up and one step of the 4.8M-atom corrector leg (convolutions)."""
+    one warm-up and one step of the 4.8M-atom corrector leg (convolutions).  io / input: one
+    warm-up and one step of the output-file and input-file legs."""
     from simulated_tem_gb300 import _lib, imaging
+    if args.ncu_case in ("io", "input"):
+        import torch
+        stream = torch.cuda.Stream()
+        flush = torch.empty(64 << 20, dtype=torch.float64, device="cuda")
+        ctx = imaging.Context(0)
+        with torch.cuda.stream(stream):
+            if args.ncu_case == "io":
+                r = io_leg(ctx, stream, flush, 1, 1, cpu=False)
+            else:
+                cell, _, _, _ = workload()
+                r = input_leg(ctx, cell, stream, 1, 1, cpu=False)
+        torch.cuda.synchronize()
+        print("ncu case %s: %s" % (args.ncu_case, json.dumps(r)))
+        ctx.close()
+        return
     if args.ncu_case in ("cfg1", "corrector"):
         import torch
         stream = torch.cuda.Stream()
@@ -806,7 +822,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched sweep and uneven-cell legs")
     ap.add_argument("--batch-steps", type=int, default=3)
-    ap.add_argument("--ncu-case", choices=["fp32", "fp64", "cfg1", "corrector"], default=None,
+    ap.add_argument("--ncu-case", choices=["fp32", "fp64", "cfg1", "corrector", "io", "input"], default=None,
                     help="run one small untimed case only (for an ncu capture)")
     args = ap.parse_args()
     if args.ncu_case:

@@ -43,6 +43,12 @@ int stn_avgpool2_bwd(const void* gy, void* gx, int32_t B, int32_t H, int32_t W, 
 int stn_upsample2(const void* x, void* y, int32_t B, int32_t H, int32_t W, int32_t C, void* stream);
 int stn_upsample2_bwd(const void* gy, void* gx, int32_t B, int32_t H, int32_t W, int32_t C, void* stream);
 
+/* The decoder's input in one pass: y = [upsample2(d), e] along channels, y and e of
+ * B x H x W pixels, d of B x H/2 x W/2 (Cd, Ce multiples of 8); the upsampled tensor is not
+ * stored. */
+int stn_upsample2_concat(const void* d, const void* e, void* y, int32_t B, int32_t H, int32_t W, int32_t Cd,
+                         int32_t Ce, void* stream);
+
 /* Channel concatenation y = [a, b] and its inverse (Ca, Cb multiples of 8; ga or gb may be
  * null). */
 int stn_concat(const void* a, const void* b, void* y, int64_t npix, int32_t Ca, int32_t Cb, void* stream);

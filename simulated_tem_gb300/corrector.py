@@ -127,13 +127,13 @@ class UNet:
         a["p3"] = N.avgpool2(a["e2"])
         a["e3a"] = self._conv("bota", a["p3"])
         a["e3"] = self._conv("botb", a["e3a"])
-        a["c2"] = N.concat(N.upsample2(a["e3"]), a["e2"])
+        a["c2"] = N.upsample2_concat(a["e3"], a["e2"])
         a["d2a"] = self._conv("dec2a", a["c2"])
         a["d2"] = self._conv("dec2b", a["d2a"])
-        a["c1"] = N.concat(N.upsample2(a["d2"]), a["e1"])
+        a["c1"] = N.upsample2_concat(a["d2"], a["e1"])
         a["d1a"] = self._conv("dec1a", a["c1"])
         a["d1"] = self._conv("dec1b", a["d1a"])
-        a["c0"] = N.concat(N.upsample2(a["d1"]), a["e0"])
+        a["c0"] = N.upsample2_concat(a["d1"], a["e0"])
         a["d0a"] = self._conv("dec0a", a["c0"])
         a["d0"] = self._conv("dec0b", a["d0a"])
         out = self._conv("head", a["d0"], out_fp32=True)

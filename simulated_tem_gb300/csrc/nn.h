@@ -33,6 +33,9 @@ int avgpool2(const __nv_bfloat16* x, __nv_bfloat16* y, int B, int H, int W, int 
 int avgpool2_bwd(const __nv_bfloat16* gy, __nv_bfloat16* gx, int B, int H, int W, int C, cudaStream_t st);
 int upsample2(const __nv_bfloat16* x, __nv_bfloat16* y, int B, int H, int W, int C, cudaStream_t st);
 int upsample2_bwd(const __nv_bfloat16* gy, __nv_bfloat16* gx, int B, int H, int W, int C, cudaStream_t st);
+// y = concat(upsample2(d), e), H x W the full-resolution size
+int upsample2_concat(const __nv_bfloat16* d, const __nv_bfloat16* e, __nv_bfloat16* y, int B, int H, int W, int Cd,
+                     int Ce, cudaStream_t st);
 int concat(const __nv_bfloat16* a, const __nv_bfloat16* b, __nv_bfloat16* y, long long npix, int Ca, int Cb,
            cudaStream_t st);
 int split(const __nv_bfloat16* gy, __nv_bfloat16* ga, __nv_bfloat16* gb, long long npix, int Ca, int Cb,

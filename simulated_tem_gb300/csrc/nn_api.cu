@@ -43,6 +43,10 @@ extern "C" int stn_upsample2(const void* x, void* y, int32_t B, int32_t H, int32
 extern "C" int stn_upsample2_bwd(const void* gy, void* gx, int32_t B, int32_t H, int32_t W, int32_t C, void* stream) {
   return upsample2_bwd(cb(gy), mb(gx), B, H, W, C, cs(stream));
 }
+extern "C" int stn_upsample2_concat(const void* d, const void* e, void* y, int32_t B, int32_t H, int32_t W,
+                                    int32_t Cd, int32_t Ce, void* stream) {
+  return upsample2_concat(cb(d), cb(e), mb(y), B, H, W, Cd, Ce, cs(stream));
+}
 extern "C" int stn_concat(const void* a, const void* b, void* y, int64_t npix, int32_t Ca, int32_t Cb, void* stream) {
   return concat(cb(a), cb(b), mb(y), npix, Ca, Cb, cs(stream));
 }

@@ -23,71 +23,120 @@ int grid_for(long long n) {
 __device__ __forceinline__ float bf(__nv_bfloat16 v) { return __bfloat162float(v); }
 __device__ __forceinline__ __nv_bfloat16 tobf(float v) { return __float2bfloat16_rn(v); }
 
+// Eight BF16 channels as one 16-byte vector, and their FP32 values.
+struct V8 {
+  float f[8];
+};
+__device__ __forceinline__ V8 load8(const __nv_bfloat16* p) {
+  const uint4 u = *reinterpret_cast<const uint4*>(p);
+  const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&u);
+  V8 r;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const float2 f = __bfloat1622float2(h[i]);
+    r.f[2 * i] = f.x;
+    r.f[2 * i + 1] = f.y;
+  }
+  return r;
+}
+__device__ __forceinline__ void store8(__nv_bfloat16* p, const V8& v) {
+  __align__(16) __nv_bfloat162 h[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) h[i] = __floats2bfloat162_rn(v.f[2 * i], v.f[2 * i + 1]);
+  *reinterpret_cast<uint4*>(p) = *reinterpret_cast<const uint4*>(h);
+}
+
+// The layers below run one thread per (pixel, 8 channels) with 32-bit pixel indices (the
+// convolutions limit a tensor to fewer than 2^31 pixels); C is a multiple of 8.
+
 // y[b, i, j, c] = (x[b, 2i, 2j] + x[b, 2i, 2j + 1] + x[b, 2i + 1, 2j] + x[b, 2i + 1, 2j + 1]) / 4
 __global__ void k_avgpool2(const __nv_bfloat16* __restrict__ x, __nv_bfloat16* __restrict__ y, int B, int H, int W,
                            int C) {
-  const int Ho = H / 2, Wo = W / 2;
-  const long long n = (long long)B * Ho * Wo * C;
+  const int Ho = H / 2, Wo = W / 2, V = C / 8;
+  const long long n = (long long)B * Ho * Wo * V;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const int c = (int)(i % C);
-    long long r = i / C;
-    const int j = (int)(r % Wo);
-    r /= Wo;
-    const int ii = (int)(r % Ho);
-    const int b = (int)(r / Ho);
-    const __nv_bfloat16* s = x + (((long long)b * H + 2 * ii) * W + 2 * j) * C + c;
-    const float v = (bf(s[0]) + bf(s[C])) + (bf(s[(long long)W * C]) + bf(s[(long long)W * C + C]));
-    y[i] = tobf(0.25f * v);
+    const int c = (int)(i % V) * 8;
+    const unsigned po = (unsigned)(i / V);  // output pixel
+    const unsigned j = po % Wo, r = po / Wo;
+    const unsigned ii = r % Ho, b = r / Ho;
+    const __nv_bfloat16* s = x + ((size_t)(b * H + 2 * ii) * W + 2 * j) * C + c;
+    const V8 a = load8(s), bb = load8(s + C), cc = load8(s + (size_t)W * C), d = load8(s + (size_t)W * C + C);
+    V8 o;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) o.f[k] = 0.25f * ((a.f[k] + bb.f[k]) + (cc.f[k] + d.f[k]));
+    store8(y + (size_t)po * C + c, o);
   }
 }
 
 // gx[b, y, x, c] = gy[b, y / 2, x / 2, c] / 4
 __global__ void k_avgpool2_bwd(const __nv_bfloat16* __restrict__ gy, __nv_bfloat16* __restrict__ gx, int B, int H,
                                int W, int C) {
-  const long long n = (long long)B * H * W * C;
-  const int Ho = H / 2, Wo = W / 2;
+  const int Ho = H / 2, Wo = W / 2, V = C / 8;
+  const long long n = (long long)B * H * W * V;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const int c = (int)(i % C);
-    long long r = i / C;
-    const int xw = (int)(r % W);
-    r /= W;
-    const int yh = (int)(r % H);
-    const int b = (int)(r / H);
-    gx[i] = tobf(0.25f * bf(gy[(((long long)b * Ho + yh / 2) * Wo + xw / 2) * C + c]));
+    const int c = (int)(i % V) * 8;
+    const unsigned p = (unsigned)(i / V);
+    const unsigned xw = p % W, r = p / W;
+    const unsigned yh = r % H, b = r / H;
+    V8 v = load8(gy + ((size_t)(b * Ho + yh / 2) * Wo + xw / 2) * C + c);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v.f[k] *= 0.25f;
+    store8(gx + (size_t)p * C + c, v);
   }
 }
 
 // nearest 2x upsampling: y[b, y, x, c] = x[b, y / 2, x / 2, c]
 __global__ void k_upsample2(const __nv_bfloat16* __restrict__ x, __nv_bfloat16* __restrict__ y, int B, int H, int W,
                             int C) {
-  const int Ho = 2 * H, Wo = 2 * W;
-  const long long n = (long long)B * Ho * Wo * C;
+  const int Ho = 2 * H, Wo = 2 * W, V = C / 8;
+  const long long n = (long long)B * Ho * Wo * V;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const int c = (int)(i % C);
-    long long r = i / C;
-    const int xw = (int)(r % Wo);
-    r /= Wo;
-    const int yh = (int)(r % Ho);
-    const int b = (int)(r / Ho);
-    y[i] = x[(((long long)b * H + yh / 2) * W + xw / 2) * C + c];
+    const int c = (int)(i % V) * 8;
+    const unsigned p = (unsigned)(i / V);
+    const unsigned xw = p % Wo, r = p / Wo;
+    const unsigned yh = r % Ho, b = r / Ho;
+    *reinterpret_cast<uint4*>(y + (size_t)p * C + c) =
+        *reinterpret_cast<const uint4*>(x + ((size_t)(b * H + yh / 2) * W + xw / 2) * C + c);
+  }
+}
+
+// y = concat(upsample2(d), e): y[b, y, x, 0:Cd] = d[b, y / 2, x / 2], y[b, y, x, Cd:] =
+// e[b, y, x] (H, W: the full-resolution sizes); the upsampled tensor is never stored
+__global__ void k_upsample2_concat(const __nv_bfloat16* __restrict__ d, const __nv_bfloat16* __restrict__ e,
+                                   __nv_bfloat16* __restrict__ y, int B, int H, int W, int Cd, int Ce) {
+  const int C = Cd + Ce, V = C / 8, Hd = H / 2, Wd = W / 2;
+  const long long n = (long long)B * H * W * V;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int c = (int)(i % V) * 8;
+    const unsigned p = (unsigned)(i / V);
+    uint4 v;
+    if (c < Cd) {
+      const unsigned xw = p % W, r = p / W;
+      const unsigned yh = r % H, b = r / H;
+      v = *reinterpret_cast<const uint4*>(d + ((size_t)(b * Hd + yh / 2) * Wd + xw / 2) * Cd + c);
+    } else {
+      v = *reinterpret_cast<const uint4*>(e + (size_t)p * Ce + (c - Cd));
+    }
+    *reinterpret_cast<uint4*>(y + (size_t)p * C + c) = v;
   }
 }
 
 // gx[b, i, j, c] = sum of gy over the 2 x 2 block it was copied to (FP32 sum, one rounding)
 __global__ void k_upsample2_bwd(const __nv_bfloat16* __restrict__ gy, __nv_bfloat16* __restrict__ gx, int B, int H,
                                 int W, int C) {
-  const long long n = (long long)B * H * W * C;
-  const int Wo = 2 * W;
+  const int Wo = 2 * W, V = C / 8;
+  const long long n = (long long)B * H * W * V;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const int c = (int)(i % C);
-    long long r = i / C;
-    const int j = (int)(r % W);
-    r /= W;
-    const int ii = (int)(r % H);
-    const int b = (int)(r / H);
-    const __nv_bfloat16* s = gy + (((long long)b * 2 * H + 2 * ii) * Wo + 2 * j) * C + c;
-    const float v = (bf(s[0]) + bf(s[C])) + (bf(s[(long long)Wo * C]) + bf(s[(long long)Wo * C + C]));
-    gx[i] = tobf(v);
+    const int c = (int)(i % V) * 8;
+    const unsigned p = (unsigned)(i / V);
+    const unsigned j = p % W, r = p / W;
+    const unsigned ii = r % H, b = r / H;
+    const __nv_bfloat16* s = gy + ((size_t)(b * 2 * H + 2 * ii) * Wo + 2 * j) * C + c;
+    const V8 a = load8(s), bb = load8(s + C), cc = load8(s + (size_t)Wo * C), dd = load8(s + (size_t)Wo * C + C);
+    V8 o;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) o.f[k] = (a.f[k] + bb.f[k]) + (cc.f[k] + dd.f[k]);
+    store8(gx + (size_t)p * C + c, o);
   }
 }
 
@@ -329,24 +378,33 @@ int status() { return cudaGetLastError() == cudaSuccess ? 0 : 2; }
 
 }  // namespace
 
+bool pix_ok(int B, int H, int W, int C) {
+  return B >= 1 && H >= 1 && W >= 1 && C >= 8 && C % 8 == 0 && (long long)B * H * W < (1LL << 31);
+}
 int avgpool2(const __nv_bfloat16* x, __nv_bfloat16* y, int B, int H, int W, int C, cudaStream_t st) {
-  if (!x || !y || H % 2 || W % 2 || C < 1) return 1;
-  k_avgpool2<<<grid_for((long long)B * H * W * C / 4), kBlock, 0, st>>>(x, y, B, H, W, C);
+  if (!x || !y || H % 2 || W % 2 || !pix_ok(B, H, W, C)) return 1;
+  k_avgpool2<<<grid_for((long long)B * H * W * C / 32), kBlock, 0, st>>>(x, y, B, H, W, C);
   return status();
 }
 int avgpool2_bwd(const __nv_bfloat16* gy, __nv_bfloat16* gx, int B, int H, int W, int C, cudaStream_t st) {
-  if (!gy || !gx || H % 2 || W % 2 || C < 1) return 1;
-  k_avgpool2_bwd<<<grid_for((long long)B * H * W * C), kBlock, 0, st>>>(gy, gx, B, H, W, C);
+  if (!gy || !gx || H % 2 || W % 2 || !pix_ok(B, H, W, C)) return 1;
+  k_avgpool2_bwd<<<grid_for((long long)B * H * W * C / 8), kBlock, 0, st>>>(gy, gx, B, H, W, C);
   return status();
 }
 int upsample2(const __nv_bfloat16* x, __nv_bfloat16* y, int B, int H, int W, int C, cudaStream_t st) {
-  if (!x || !y || C < 1) return 1;
-  k_upsample2<<<grid_for((long long)B * H * W * C * 4), kBlock, 0, st>>>(x, y, B, H, W, C);
+  if (!x || !y || !pix_ok(B, 2 * H, 2 * W, C)) return 1;
+  k_upsample2<<<grid_for((long long)B * H * W * C / 2), kBlock, 0, st>>>(x, y, B, H, W, C);
+  return status();
+}
+int upsample2_concat(const __nv_bfloat16* d, const __nv_bfloat16* e, __nv_bfloat16* y, int B, int H, int W, int Cd,
+                     int Ce, cudaStream_t st) {
+  if (!d || !e || !y || H % 2 || W % 2 || Cd % 8 || !pix_ok(B, H, W, Cd + Ce) || Ce < 8 || Ce % 8) return 1;
+  k_upsample2_concat<<<grid_for((long long)B * H * W * (Cd + Ce) / 8), kBlock, 0, st>>>(d, e, y, B, H, W, Cd, Ce);
   return status();
 }
 int upsample2_bwd(const __nv_bfloat16* gy, __nv_bfloat16* gx, int B, int H, int W, int C, cudaStream_t st) {
-  if (!gy || !gx || C < 1) return 1;
-  k_upsample2_bwd<<<grid_for((long long)B * H * W * C), kBlock, 0, st>>>(gy, gx, B, H, W, C);
+  if (!gy || !gx || !pix_ok(B, 2 * H, 2 * W, C)) return 1;
+  k_upsample2_bwd<<<grid_for((long long)B * H * W * C / 8), kBlock, 0, st>>>(gy, gx, B, H, W, C);
   return status();
 }
 int concat(const __nv_bfloat16* a, const __nv_bfloat16* b, __nv_bfloat16* y, long long npix, int Ca, int Cb,

@@ -21,6 +21,7 @@ _PROTOS = {
     "stn_upsample2": (_i32, [_vp, _vp, _i32, _i32, _i32, _i32, _vp]),
     "stn_upsample2_bwd": (_i32, [_vp, _vp, _i32, _i32, _i32, _i32, _vp]),
     "stn_concat": (_i32, [_vp, _vp, _vp, _i64, _i32, _i32, _vp]),
+    "stn_upsample2_concat": (_i32, [_vp, _vp, _vp, _i32, _i32, _i32, _i32, _i32, _vp]),
     "stn_split": (_i32, [_vp, _vp, _vp, _i64, _i32, _i32, _vp]),
     "stn_relu_mask": (_i32, [_vp, _vp, _i64, _vp]),
     "stn_bias_grad": (_i32, [_vp, _vp, _i64, _i32, _vp, _i64, _vp]),
@@ -170,6 +171,17 @@ def concat(a, b, out=None):
     Cb = b.shape[3]
     out = _bf16_empty((B, H, W, Ca + Cb), a) if out is None else out
     _check(lib().stn_concat(_ptr(a), _ptr(b), _ptr(out), B * H * W, Ca, Cb, _stream()), "stn_concat")
+    return out
+
+
+def upsample2_concat(d, e, out=None):
+    """concat(upsample2(d), e) in one pass (d at half the resolution of e)."""
+    B, H, W, Ce = e.shape
+    Cd = d.shape[3]
+    assert d.shape[:3] == (B, H // 2, W // 2)
+    out = _bf16_empty((B, H, W, Cd + Ce), e) if out is None else out
+    _check(lib().stn_upsample2_concat(_ptr(d), _ptr(e), _ptr(out), B, H, W, Cd, Ce, _stream()),
+           "stn_upsample2_concat")
     return out
 
 

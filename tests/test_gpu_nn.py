@@ -96,6 +96,10 @@ def test_elementwise_layers_match_oracle(nn):
     assert np.array_equal(nn.upsample2(_bf16(g)).float().cpu().numpy(), NO.upsample2(g))
     assert np.allclose(nn.upsample2_bwd(_bf16(x)).float().cpu().numpy(),
                        NO.bf16_round(NO.upsample2_bwd(x).astype(np.float32)))
+    # the decoder's fused input: concat(upsample2(d), e)
+    d, e = _rand(rng, 2, 4, 6, 32), _rand(rng, 2, 8, 12, 16)
+    assert np.array_equal(nn.upsample2_concat(_bf16(d), _bf16(e)).float().cpu().numpy(),
+                          np.concatenate([NO.upsample2(d), e], axis=3))
     a, b = _rand(rng, 2, 5, 7, 16), _rand(rng, 2, 5, 7, 24)
     cat = nn.concat(_bf16(a), _bf16(b))
     assert np.array_equal(cat.float().cpu().numpy(), np.concatenate([a, b], axis=3))
