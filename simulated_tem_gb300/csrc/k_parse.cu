@@ -3,10 +3,10 @@
 // line is ignored).
 //
 // The block's bytes are in device memory.  Line starts: each block of threads owns a
-// 64 KB segment and counts its newlines; an exclusive scan over the segments gives each
-// segment's first line number; each segment then writes the starts of its lines (the
-// byte after each newline) in order, its threads owning consecutive 256-byte pieces with a
-// block-wide scan of their counts.  Then one thread per atom line reads five tokens:
+// 64 KB segment and counts its newlines (16-byte loads, coalesced); an exclusive scan over
+// the segments gives each segment's first line number; each segment then writes the starts
+// of its lines (the byte after each newline) in order, 4 KB per step with a block-wide scan
+// of the threads' newline counts.  Then one thread per atom line reads five tokens:
 // two integers and three reals, each correctly rounded (parse_number.cuh), separated by
 // blanks or commas.  A line with fewer than five tokens, a malformed token or a number
 // outside the exact parser's range records its line number (the smallest such line wins)
@@ -20,16 +20,35 @@
 namespace stem {
 namespace {
 
-constexpr int kSeg = 65536;    // bytes per segment (one block)
-constexpr int kPiece = 256;    // bytes per thread within a segment
+constexpr int kSeg = 65536;   // bytes per segment (one block)
+constexpr int kChunk = 4096;  // bytes per block-wide step: 256 threads x 16 bytes
+
+// newlines among the 16 bytes at t[i0, i0 + 16) (bytes at or past n are not newlines),
+// as a bit mask (bit k: byte i0 + k)
+__device__ __forceinline__ unsigned newline_mask(const char* __restrict__ t, int64_t n, int64_t i0) {
+  unsigned m = 0;
+  if (i0 + 16 <= n && ((uintptr_t)(t + i0) & 15) == 0) {  // a caller's buffer may start unaligned
+    const uint4 v = *reinterpret_cast<const uint4*>(t + i0);
+    const unsigned w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int k = 0; k < 16; ++k)
+      if (((w[k >> 2] >> (8 * (k & 3))) & 0xFFu) == (unsigned)'\n') m |= 1u << k;
+  } else {  // the end of the text, or an unaligned buffer
+    for (int k = 0; k < 16 && i0 + k < n; ++k)
+      if (t[i0 + k] == '\n') m |= 1u << k;
+  }
+  return m;
+}
 
 __global__ void __launch_bounds__(256) k_count_lines(const char* __restrict__ t, int64_t n, int64_t nseg,
                                                      long long* __restrict__ seg_count) {
-  __shared__ long long part[8];
+  __shared__ int part[8];
   for (int64_t sg = blockIdx.x; sg < nseg; sg += gridDim.x) {
-    const int64_t b0 = sg * kSeg, b1 = min(n, b0 + kSeg);
-    long long c = 0;
-    for (int64_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) c += t[i] == '\n';
+    int c = 0;
+    for (int ch = 0; ch < kSeg / kChunk; ++ch) {
+      const int64_t i0 = sg * kSeg + (int64_t)ch * kChunk + 16 * threadIdx.x;
+      if (i0 < n) c += __popc(newline_mask(t, n, i0));
+    }
     for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
     if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = c;
     __syncthreads();
@@ -66,31 +85,41 @@ __global__ void __launch_bounds__(1024) k_scan_segments(long long* __restrict__ 
   }
 }
 
-// starts[k] = byte offset of line k (k < n_lines; the rest stay -1); line 0 starts at 0
+// starts[k] = byte offset of line k (k < n_lines; the rest stay -1); line 0 starts at 0.
+// Per 4 KB step every thread holds the newline mask of its 16 bytes; a block-wide scan of
+// the counts gives each newline its line number.
 __global__ void __launch_bounds__(256) k_line_starts(const char* __restrict__ t, int64_t n, int64_t nseg,
                                                      const long long* __restrict__ seg_base, int64_t n_lines,
                                                      long long* __restrict__ starts) {
-  __shared__ int scan[256];
+  __shared__ int wsum[8];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int64_t sg = blockIdx.x; sg < nseg; sg += gridDim.x) {
-    const int64_t p0 = sg * kSeg + (int64_t)threadIdx.x * kPiece, p1 = min(n, p0 + kPiece);
-    int c = 0;
-    for (int64_t i = p0; i < p1; ++i) c += t[i] == '\n';
-    scan[threadIdx.x] = c;
-    __syncthreads();
-    for (int d = 1; d < 256; d <<= 1) {
-      const int a = threadIdx.x >= d ? scan[threadIdx.x - d] : 0;
-      __syncthreads();
-      scan[threadIdx.x] += a;
-      __syncthreads();
-    }
-    long long k = seg_base[sg] + scan[threadIdx.x] - c + 1;  // the line a newline here starts
-    for (int64_t i = p0; i < p1; ++i)
-      if (t[i] == '\n') {
-        if (k < n_lines) starts[k] = i + 1;
-        ++k;
+    long long base = seg_base[sg];  // newlines before this step
+    for (int ch = 0; ch < kSeg / kChunk; ++ch) {
+      const int64_t c0 = sg * kSeg + (int64_t)ch * kChunk;
+      if (c0 >= n) break;  // block-uniform
+      const int64_t i0 = c0 + 16 * threadIdx.x;
+      const unsigned m = i0 < n ? newline_mask(t, n, i0) : 0u;
+      const int c = __popc(m);
+      int incl = c;  // inclusive warp scan
+      for (int o = 1; o < 32; o <<= 1) {
+        const int a = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += a;
       }
+      if (lane == 31) wsum[warp] = incl;
+      __syncthreads();
+      int woff = 0, total = 0;
+      for (int w = 0; w < 8; ++w) {
+        if (w < warp) woff += wsum[w];
+        total += wsum[w];
+      }
+      long long k = base + woff + incl - c + 1;  // the line the first newline here starts
+      for (unsigned mm = m; mm; mm &= mm - 1, ++k)
+        if (k < n_lines) starts[k] = i0 + __ffs(mm);  // the byte after the newline
+      base += total;
+      __syncthreads();  // wsum is rewritten by the next step
+    }
     if (sg == 0 && threadIdx.x == 0 && n_lines > 0) starts[0] = 0;
-    __syncthreads();
   }
 }
 

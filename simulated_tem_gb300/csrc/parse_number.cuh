@@ -4,7 +4,9 @@
 //
 // A number is [+|-]digits[.digits][(e|E|d|D)[+|-]digits].  Its first 38 significant digits
 // form an integer W (< 2^127) with a decimal exponent q: the value is W 10^q (digits beyond
-// the 38th set a sticky flag).  The result is exact by construction:
+// the 38th set a sticky flag).  When W <= 2^53 and |q| <= 22 both W and 10^|q| are exact
+// FP64 numbers and one IEEE multiplication or division is the correctly rounded result
+// (Clinger's fast path).  Otherwise the result is exact by construction:
 //   * an FP64 estimate of W 10^q (within a few ulp) gives a candidate m 2^e (m of 53 bits);
 //   * the candidate is moved until w 10^q lies between its lower and upper midpoints,
 //     decided by exact comparisons of 256-bit integers (W 10^q against a midpoint num 2^sh,
@@ -104,6 +106,12 @@ PN_HD bool mul_pow10(U256& a, int k) {
     k -= s;
   }
   return true;
+}
+
+PN_HD double pow10_exact(int k) {  // 10^k for 0 <= k <= 22: exact in FP64
+  double r = 1.0;
+  for (int i = 0; i < k; ++i) r *= 10.0;  // every partial product is exact
+  return r;
 }
 
 PN_HD double pow10_est(int k) {  // 10^k in FP64 (exact up to 10^22), for the estimate only
@@ -263,6 +271,14 @@ PN_HD bool parse_real(const char* p, const char* end, double& out, int& used) {
   used = (int)(s - p);
   if (w1 == 0) {
     out = neg ? -0.0 : 0.0;
+    return true;
+  }
+  // Clinger's fast path: an integer significand below 2^53 and a power of ten below 10^23
+  // are both exact in FP64, so one IEEE multiplication or division rounds correctly
+  if (n2 == 0 && !sticky && w1 <= (1ULL << 53) && q >= -22 && q <= 22) {
+    const double wd = (double)w1, p10 = pow10_exact(q < 0 ? -q : q);
+    const double r = q < 0 ? wd / p10 : wd * p10;
+    out = neg ? -r : r;
     return true;
   }
   // W = w1 10^n2 + w2, and its FP64 estimate

@@ -64,6 +64,19 @@ def test_number_forms_and_separators(ctx):
     assert np.array_equal(ty, 1 + np.arange(n) % 3)
 
 
+def test_unaligned_text_buffer(ctx):
+    """A text block starting at an odd device address (inside a larger buffer)."""
+    text = "".join("%d 2 %r %r %r\n" % (i + 1, 0.25 * i, -1.5, 1e-3 * i) for i in range(5000))
+    b = np.frombuffer(("x" + text).encode(), dtype=np.uint8)
+    d_t = torch.from_numpy(b.copy()).cuda()
+    d_x = torch.zeros((5000, 3), dtype=torch.float64, device="cuda")
+    bad = ctx.parse_atoms_device(d_t.data_ptr() + 1, b.size - 1, 5000, d_x.data_ptr(),
+                                 stream=torch.cuda.current_stream().cuda_stream)
+    assert bad == -1
+    want = np.array([[0.25 * i, -1.5, 1e-3 * i] for i in range(5000)])
+    assert np.array_equal(d_x.cpu().numpy(), want)
+
+
 def test_bad_lines_are_reported(ctx):
     good = "".join("%d 1 %r %r %r\n" % (i + 1, 0.5 * i, 1.0, 2.0) for i in range(100))
     lines = good.split("\n")
