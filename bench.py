@@ -151,9 +151,21 @@ def batched_legs(ctx, cell, stream, flush, steps, warmup):
         d = (img - ref).abs()
         return {"max_abs_dI_fp32_vs_fp64": float(d.max()), "rms_dI_fp32_vs_fp64": float(d.pow(2).mean().sqrt())}
 
-    # tilt x precession x g sweep
-    x, specs = sweep_specs(cell)
-    d_x = torch.from_numpy(np.ascontiguousarray(x)).cuda()
+    # tilt x precession x g sweep: set up on the host condition by condition (the atoms
+    # wrapped and their extents taken for every image), and on the GPU (wrapped once, the
+    # extents of the three g in one pass); the two give the same geometry bit for bit
+    from simulated_tem_gb300 import imaging, synth
+    t0 = time.perf_counter()
+    x, specs_host = sweep_specs(cell)
+    setup_host = time.perf_counter() - t0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    d_x, specs, _ = imaging.d2bi_sweep(ctx, cell.a_super, synth.A0_FE, (0, 0, 1), SWEEP_G, cell.pos, n_tomo=41,
+                                       tomo_angle=20.0, prec_angle=0.005, n_prec=16, sg=0.01, xi0=103.9, xig=207.5)
+    torch.cuda.synchronize()
+    setup_dev = time.perf_counter() - t0
+    same = all(bytes(a[0]) == bytes(b[0]) and np.array_equal(a[1], b[1]) for a, b in zip(specs, specs_host))
+    same = same and bool(np.array_equal(d_x.cpu().numpy(), x))
     imgs = [torch.empty((G.My, G.Mx), dtype=torch.float64, device="cuda") for G, _ in specs]
     jobs = [(G, d_x.data_ptr(), len(x), aa, im.data_ptr()) for (G, aa), im in zip(specs, imgs)]
     ms = time_batch(ctx, jobs, f32 | _lib.ST_FLAG_STATS, stream, 1, 0, flush)  # statistics
@@ -171,7 +183,11 @@ def batched_legs(ctx, cell, stream, flush, steps, warmup):
                     "steps": steps, "image_sizes": sorted({(G_.Mx, G_.My, G_.Mz) for G_, _ in specs}),
                     "kept_atoms": st.n_kept, "column_kernel": st.column_kernel,
                     "ms_bin": st.ms_bin, "ms_column": st.ms_column,
-                    "accuracy_one_image": accuracy(G, d_x.data_ptr(), len(x), aa, imgs[k])}
+                    "accuracy_one_image": accuracy(G, d_x.data_ptr(), len(x), aa, imgs[k]),
+                    "setup": {"host_s": setup_host, "device_s": setup_dev, "same_geometry": same,
+                              "images_per_s_with_device_setup": n_img / (t + setup_dev),
+                              "note": "set-up of the 123 geometries: host (wrap and extents per image) vs "
+                                      "d2bi_sweep (one wrap and one extents pass on the GPU)"}}
     pms = time_plan(ctx, jobs, f32, stream, steps, 1, flush)
     tp = float(np.mean(pms)) * 1e-3
     out["sweep"]["plan"] = {"note": "the same batch recorded once as a CUDA graph (st_plan) and replayed",

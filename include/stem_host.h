@@ -74,6 +74,17 @@ int st_atom_extents(const double* k, const double* g, const double* a_cell, cons
 /* tomography tilt R = Rx(theta) R0 for step nn of nTomo (:1365-1372) */
 int st_tomography_tilt(double tomoAngle, int32_t nn, int32_t nTomo, const double* R0, double* R);
 
+/* The two passes over the atoms on the GPU, with the host versions' bits.  st_wrap_pbc
+ * on device positions d_x (ldx, n), in place, enqueued on stream (0: the context's).
+ * st_atom_extents for n_cond conditions (k, g: 3 n_cond values each; 1 <= n_cond <= 32)
+ * in one pass over the device positions; d: 3 n_cond host values; waits for the result.
+ * For a tomography sweep the atoms are wrapped once and the extents depend only on
+ * (k, g), not on the tilt. */
+int st_wrap_pbc_device(st_ctx* ctx, const double* a_vox, int32_t Nx, int32_t Ny, int32_t Nz, double* d_x,
+                       int64_t ldx, int64_t n, void* stream);
+int st_atom_extents_device(st_ctx* ctx, int32_t n_cond, const double* k, const double* g, const double* a_cell,
+                           const double* d_x, int64_t ldx, int64_t n, double* d);
+
 #ifdef __cplusplus
 }
 #endif

@@ -131,6 +131,8 @@ _PROTOS = {
     "st_wrap_pbc": (_i32, [_dp, _i32, _i32, _i32, _dp, _i64, _i64]),
     "st_atom_extents": (_i32, [_dp, _dp, _dp, _dp, _i64, _i64, _dp]),
     "st_tomography_tilt": (_i32, [_d, _i32, _i32, _dp, _dp]),
+    "st_wrap_pbc_device": (_i32, [_vp, _dp, _i32, _i32, _i32, _vp, _i64, _i64, _vp]),
+    "st_atom_extents_device": (_i32, [_vp, _i32, _dp, _dp, _dp, _vp, _i64, _i64, _dp]),
 }
 
 _lib = None

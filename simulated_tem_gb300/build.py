@@ -25,7 +25,8 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall"]
 
 LIB_SOURCES = ["stem_ctx.cu", "k_bin.cu", "k_column.cu", "k_column_v2.cu", "k_blur.cu", "blur_noalloc.cu", "k_output.cu",
-               "k_parse.cu", "host_d2bi.cpp", "host_output.cpp", "host_input.cpp"]
+               "k_parse.cu", "k_geom.cu", "host_d2bi.cpp", "host_output.cpp",
+               "host_input.cpp"]
 NN_LIB = os.path.join(HERE, "libstem_nn.so")
 NN_SOURCES = ["nn_conv.cu", "nn_ops.cu", "nn_api.cu"]
 

@@ -14,6 +14,7 @@
 #include <new>
 
 #include "../../include/stem_host.h"
+#include "internal.h"
 
 namespace {
 
@@ -627,6 +628,50 @@ int st_atom_extents(const double* k, const double* g, const double* a_cell, cons
     }
   }
   for (int i = 0; i < 3; ++i) d[i] = hi[i] - lo[i];
+  return ST_OK;
+}
+
+// ---- the same two passes over the atoms on the GPU (k_geom.cu), bit for bit
+
+int st_wrap_pbc_device(st_ctx* ctx, const double* a_vox, int32_t Nx, int32_t Ny, int32_t Nz, double* d_x,
+                       int64_t ldx, int64_t n, void* stream) {
+  if (!ctx) return ST_ERR_ARG;
+  if (!a_vox || !d_x || ldx < 3 || n < 0 || Nx < 1 || Ny < 1 || Nz < 1)
+    return stem::ctx_fail(ctx, ST_ERR_ARG, "invalid wrap arguments");
+  const Supercell s = Supercell::make(Mat3::from(a_vox), Nx, Ny, Nz);
+  stem::GeomWrap w;
+  std::memcpy(w.a, s.a.m, sizeof w.a);
+  std::memcpy(w.ia, s.ia.m, sizeof w.ia);
+  w.N[0] = Nx;
+  w.N[1] = Ny;
+  w.N[2] = Nz;
+  const cudaStream_t st = stem::ctx_stream(ctx, stream);
+  const cudaError_t e = stem::launch_wrap_pbc(w, d_x, ldx, n, st);
+  if (e != cudaSuccess) return stem::ctx_cuda_fail(ctx, e, "wrap");
+  return ST_OK;
+}
+
+int st_atom_extents_device(st_ctx* ctx, int32_t n_cond, const double* k, const double* g, const double* a_cell,
+                           const double* d_x, int64_t ldx, int64_t n, double* d) {
+  if (!ctx) return ST_ERR_ARG;
+  if (n_cond < 1 || n_cond > stem::kMaxRot || !k || !g || !a_cell || !d || (n > 0 && !d_x) || ldx < 3 || n < 1)
+    return stem::ctx_fail(ctx, ST_ERR_ARG, "invalid extents arguments (1 to 32 conditions, n >= 1)");
+  stem::GeomRot rot;
+  rot.n = n_cond;
+  for (int r = 0; r < n_cond; ++r) {
+    const Mat3 U = rotate_to_standard_frame(k + 3 * r, Mat3::from(a_cell), g + 3 * r);
+    std::memcpy(rot.U + 9 * r, U.m, sizeof U.m);
+  }
+  const cudaStream_t st = stem::ctx_stream(ctx, nullptr);
+  double *part = nullptr, *out = nullptr;
+  cudaError_t e = stem::ctx_geom_scratch(ctx, &part, &out);
+  if (e == cudaSuccess) e = stem::launch_extents(rot, d_x, ldx, n, part, out, st);
+  double mm[6 * stem::kMaxRot];
+  if (e == cudaSuccess) e = cudaMemcpyAsync(mm, out, 6 * n_cond * sizeof(double), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return stem::ctx_cuda_fail(ctx, e, "atom extents");
+  for (int r = 0; r < n_cond; ++r)
+    for (int i = 0; i < 3; ++i) d[3 * r + i] = mm[6 * r + 3 + i] - mm[6 * r + i];
   return ST_OK;
 }
 

@@ -178,6 +178,27 @@ cudaError_t launch_png_levels(const double* d_img, int nx, int ny, double iso_mi
                               double* d_ab, uint16_t* d_levels, cudaStream_t st);
 // '(1000f12.7)' records of n values (st_dat_text_bytes(n) bytes)
 cudaError_t launch_format_dat(const double* d_v, int64_t n, char* d_text, cudaStream_t st);
+// Geometry over the atoms (k_geom.cu)
+struct GeomWrap {
+  double a[9], ia[9];  // voxel supercell and its inverse, column-major
+  int N[3];
+};
+constexpr int kMaxRot = 32;       // conditions per extents pass
+constexpr int kExtentBlocks = 1024;
+struct GeomRot {
+  double U[9 * kMaxRot];  // rotations to the standard frame, column-major
+  int n;
+};
+cudaError_t launch_wrap_pbc(const GeomWrap& w, double* d_x, int64_t ldx, int64_t n, cudaStream_t st);
+// context accessors for the host translation units (stem_ctx.cu)
+cudaStream_t ctx_stream(st_ctx* c, void* stream);  // stream, or the context's when null; makes its device current
+int ctx_fail(st_ctx* c, int code, const char* msg);
+int ctx_cuda_fail(st_ctx* c, cudaError_t e, const char* where);
+// scratch of the extents pass: *part (kExtentBlocks * kMaxRot * 6 doubles), *out (6 * kMaxRot)
+cudaError_t ctx_geom_scratch(st_ctx* c, double** part, double** out);
+// d_part: kExtentBlocks * kMaxRot * 6 doubles; d_out: 6 per rotation (min x, y, z, max x, y, z)
+cudaError_t launch_extents(const GeomRot& rot, const double* d_x, int64_t ldx, int64_t n, double* d_part,
+                           double* d_out, cudaStream_t st);
 // LAMMPS Atoms block (k_parse.cu): d_seg holds parse_segments(n_bytes) values, d_starts
 // n_atoms; *d_bad = the first malformed atom line, or all ones
 int64_t parse_segments(int64_t n_bytes);

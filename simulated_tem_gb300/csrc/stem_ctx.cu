@@ -74,6 +74,8 @@ struct st_ctx {
   size_t cap_pbad = 0;
   void* h_text = nullptr;  // pinned staging of a data file
   size_t cap_htext = 0;
+  double* d_geom = nullptr;  // extents pass: partial and final minima / maxima
+  size_t cap_geom = 0;
 };
 
 namespace {
@@ -789,7 +791,7 @@ extern "C" void st_destroy(st_ctx* c) {
                       c->s.counters, c->s.xtab, c->s.xfv, c->s.ytab, c->s.yfv, c->s.ztab, c->s.zfv, c->s.aa,
                       c->s.aaf, c->b.cell_start, c->b.cell_count, c->b.f64, c->b.cs64, c->b.p32, c->b.cs32,
                       c->d_x, c->d_img, c->d_blur, c->d_kern, c->d_binjobs, c->d_coljobs, c->d_work, c->d_bx, c->d_bimg,
-                      c->d_lvaux, c->d_levels, c->d_text, c->d_pseg, c->d_pstart, c->d_pbad};
+                      c->d_lvaux, c->d_levels, c->d_text, c->d_pseg, c->d_pstart, c->d_pbad, c->d_geom};
   for (void* p : dev_ptrs)
     if (p) cudaFree(p);
   if (c->h_counters) cudaFreeHost(c->h_counters);
@@ -1421,4 +1423,24 @@ extern "C" int st_read_lammps(st_ctx* c, const char* path, const st_lammps_info*
       for (int k = 0; k < 3; ++k) x[i * ldx + k] = xs[(size_t)3 * i + k];
   return ST_OK;
 }
+
+// ---------------------------------------------------------------------------------------
+// Accessors for the host translation units (host_d2bi.cpp: geometry over the atoms)
+namespace stem {
+cudaStream_t ctx_stream(st_ctx* c, void* stream) {
+  cudaSetDevice(c->device);
+  return stream ? (cudaStream_t)stream : c->stream;
+}
+int ctx_fail(st_ctx* c, int code, const char* msg) { return fail(c, code, msg); }
+int ctx_cuda_fail(st_ctx* c, cudaError_t e, const char* where) { return cuda_fail(c, e, where); }
+cudaError_t ctx_geom_scratch(st_ctx* c, double** part, double** out) {
+  const size_t np = (size_t)kExtentBlocks * kMaxRot * 6;
+  const cudaError_t e = ensure(c->d_geom, c->cap_geom, np + 6 * kMaxRot);
+  if (e == cudaSuccess) {
+    *part = c->d_geom;
+    *out = c->d_geom + np;
+  }
+  return e;
+}
+}  // namespace stem
 

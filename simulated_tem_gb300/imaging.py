@@ -381,13 +381,19 @@ def lammps_header(path):
     return info
 
 
-def wrap_pbc(a_super, M, a0, x):
-    """d2bi's periodic wrap of the input atoms on the voxel supercell (src/d2bi.f90:856-866); returns a copy."""
+def voxel_supercell(a_super, M, a0):
+    """d2bi's voxel supercell of the input cell (src/d2bi.f90:856-866): (a_vox, n)."""
     a_super = np.asarray(a_super, dtype=np.float64)
     n = [max(3, int(np.floor(M[0] * _norm2(a_super[:, 0]) / a0))),
          max(3, int(np.floor(M[0] * _norm2(a_super[:, 1]) / a0))),
          max(3, int(np.floor(M[1] * _norm2(a_super[:, 2]) / a0)))]
     a_vox = np.stack([a_super[:, i] / n[i] for i in range(3)], axis=1)
+    return a_vox, n
+
+
+def wrap_pbc(a_super, M, a0, x):
+    """d2bi's periodic wrap of the input atoms on the voxel supercell (src/d2bi.f90:856-866); returns a copy."""
+    a_vox, n = voxel_supercell(a_super, M, a0)
     x = np.ascontiguousarray(x, dtype=np.float64).copy()
     check(lib().st_wrap_pbc(_cm(a_vox), n[0], n[1], n[2], _ptr(x), x.shape[1], x.shape[0]))
     return x, a_vox, n
@@ -435,6 +441,13 @@ def d2bi_condition(a_super, a0, k, g, x, V=200.0, M=(4, 4), sg=None, R=None, U=N
     a_cell = a0 * np.eye(3)
     if d is None:
         d = atom_extents(k, g, a_cell, xw)
+    t = _condition(a_vox, n, a0, k, g, d, V, M, sg, R, U, xi0, xig, density, n_tomo, tomo_angle, tomo_step)
+    return t, xw, t.aperpx
+
+
+def _condition(a_vox, n, a0, k, g, d, V, M, sg, R, U, xi0, xig, density, n_tomo, tomo_angle, tomo_step):
+    """The imaging set-up of one condition on already wrapped atoms with extents d."""
+    a_cell = a0 * np.eye(3)
     t = DynamicalTwoBeamImaging(a_vox, n, a0, k, g, V, M[0], M[1])
     t.set_conventional_unit_cell(a_cell)
     t.set_voxel_supercell_size(d)
@@ -448,8 +461,45 @@ def d2bi_condition(a_super, a0, k, g, x, V=200.0, M=(4, 4), sg=None, R=None, U=N
         t.set_supercell_tilt()
     U0, R0 = t.get_rotation()
     t.set_extinction_distances(xi0, xig)
-    aperpx = t.find_image_parameters()[0]
+    t.aperpx = t.find_image_parameters()[0]
     t.set_use_density_field(density)
     if n_tomo > 1:
         t.set_supercell_tilt(U0, tomography_tilt(tomo_angle, tomo_step, n_tomo, R0))
-    return t, xw, aperpx
+    return t
+
+
+def d2bi_sweep(ctx, a_super, a0, k, gs, x, n_tomo=1, tomo_angle=20.0, prec_angle=0.0, n_prec=1, V=200.0, M=(4, 4),
+               sg=None, xi0=103.889565, xig=207.533203, density=False, stream=0):
+    """The conditions of a d2bi sweep (g-vectors gs x tomography steps) with the passes over
+    the atoms on the GPU: the atoms are wrapped once in device memory (st_wrap_pbc_device)
+    and the extents of every g come from one pass (st_atom_extents_device); the per-image
+    set-up is scalar host work.  Returns (wrapped positions: a torch device tensor (N, 3),
+    [(geometry, aa)] in g-major order, the imaging objects).  The geometries equal those of
+    d2bi_condition for each (g, step), bit for bit."""
+    import torch
+    a0 = (a0 + a0 + a0) / 3
+    a_vox, n = voxel_supercell(a_super, M, a0)
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    d_x = torch.from_numpy(x).to("cuda").contiguous()
+    ctx._check(lib().st_wrap_pbc_device(ctx.handle, _cm(a_vox), n[0], n[1], n[2], ctypes.c_void_p(d_x.data_ptr()),
+                                        3, len(x), ctypes.c_void_p(stream)))
+    a_cell = a0 * np.eye(3)
+    gs = [tuple(g) for g in gs]
+    nc = len(gs)
+    ks = (_d * (3 * nc))(*[float(v) for _ in gs for v in k])
+    gv = (_d * (3 * nc))(*[float(v) for g in gs for v in g])
+    dd = (_d * (3 * nc))()
+    if stream:
+        torch.cuda.current_stream().synchronize()
+    ctx._check(lib().st_atom_extents_device(ctx.handle, nc, ks, gv, _cm(a_cell), ctypes.c_void_p(d_x.data_ptr()),
+                                            3, len(x), dd))
+    specs, conds = [], []
+    for c, g in enumerate(gs):
+        d = [dd[3 * c], dd[3 * c + 1], dd[3 * c + 2]]
+        for step in range(n_tomo):
+            t = _condition(a_vox, n, a0, k, g, d, V, M, sg, None, None, xi0, xig, density, n_tomo, tomo_angle,
+                           step)
+            G, aa = t.image_geometry(len(x), prec_angle=prec_angle, n_prec=n_prec)
+            specs.append((G, aa))
+            conds.append(t)
+    return d_x, specs, conds
