@@ -471,6 +471,81 @@ def input_leg(ctx, cell, stream, steps, warmup, cpu=True):
     return out
 
 
+def tilt_leg(ctx, cell, steps, warmup, cpu=True):
+    """The -ng tilt search (setSupercellTilt1a): the testD2BI search itself (27,847 W atoms,
+    -k 0,0,1 -g 2,0,0 -ng 1 with its extinction table: 4,000 candidate beam directions x
+    2,123 bcc reflections) end to end on the host API with the scores on the GPU, the
+    scoring launch alone (CUDA events), and the oracle's scalar search on one core; then
+    the same search with the foil thickness from the atoms (-surf) on the 1.2M-atom cell
+    (the W table reused: a timing workload for the pass over 27 replicas of every atom)."""
+    import torch
+
+    from simulated_tem_gb300 import imaging
+    here = os.path.dirname(os.path.abspath(__file__))
+    xifile = os.path.join(here, "tests", "golden", "w_xi_V200_T300.dat")
+    w = np.load(os.path.join(here, "tests", "golden", "w_loop_input.npz"))
+    box = w["box"]
+    a_super = np.diag(box[:, 1] - box[:, 0])
+
+    def one(a_sup, a0, g, pos):
+        a0 = (a0 + a0 + a0) / 3  # as d2bi forms a0 from -a0 (src/d2bi.f90:787-788)
+        xw, a_vox, n = imaging.wrap_pbc(a_sup, (4, 4), a0, pos)
+        d = imaging.atom_extents((0, 0, 1), g, a0 * np.eye(3), xw)
+        t = imaging.DynamicalTwoBeamImaging(a_vox, n, a0, (0, 0, 1), g, 200.0, 4, 4)
+        t.set_conventional_unit_cell(a0 * np.eye(3))
+        t.set_voxel_supercell_size(d)
+        return t, xw
+
+    t, xw = one(a_super, 3.1652, (2, 0, 0), w["pos"])
+    walls, scans = [], []
+    for i in range(warmup + steps):
+        t, _ = one(a_super, 3.1652, (2, 0, 0), w["pos"])
+        t0 = time.perf_counter()
+        info = t.set_supercell_tilt_ng(ctx, 1.0, xifile)
+        if i >= warmup:
+            walls.append(time.perf_counter() - t0)
+            scans.append(info["scan_ms"])
+    U, R = t.get_rotation()
+    pairs = info["nk"] * (info["nn"] - 2)
+    scan = float(np.median(scans))
+    out = {"workload": "testD2BI -ng 1 search: 27,847 W atoms, k [001], g [200], %d directions x %d reflections"
+                       % (info["nk"], info["nn"]),
+           "setup_ms": float(np.median(walls)) * 1e3, "scan_ms": scan, "pairs_per_s": pairs / (scan * 1e-3),
+           "n_recheck": info["n_recheck"], "ii_best": info["ii_best"], "RU": (R @ U).tolist(),
+           "note": "setup: st_d2bi_set_supercell_tilt1a end to end (reflections, table, directions, GPU scores, "
+                   "exact near-tie re-scoring, dark-field golden section, quaternion round trip); scan: the "
+                   "scoring launch alone"}
+    if cpu:
+        from oracle import stem_oracle as O
+        args = O.make_args(a_super, 3.1652, (0, 0, 1), (2, 0, 0), V=200.0, M=(4, 4), ng=1.0, xifile=xifile)
+        t0 = time.perf_counter()
+        so, _, _ = O.setup(args, w["pos"])
+        out["cpu_oracle"] = {"ms": (time.perf_counter() - t0) * 1e3, "cores": 1, "kind": "port",
+                             "same_rotation": bool(np.array_equal(np.array(list(so.R)).reshape(3, 3).T, R)),
+                             "note": "oracle set-up with the -ng search (wrap, extents, search), one core"}
+    # -surf on the 1.2M-atom cell: the foil-thickness pass over 27 x 1.2M replicas
+    a0 = (2.87 + 2.87 + 2.87) / 3
+    xw, a_vox, n = imaging.wrap_pbc(cell.a_super, (4, 4), a0, cell.pos)
+    d_x = torch.from_numpy(np.ascontiguousarray(xw)).cuda()
+    d = imaging.atom_extents((0, 0, 1), (1, 1, 0), a0 * np.eye(3), xw)
+    fms, swall = [], []
+    for i in range(warmup + steps):
+        ts = imaging.DynamicalTwoBeamImaging(a_vox, n, a0, (0, 0, 1), (1, 1, 0), 200.0, 4, 4)
+        ts.set_conventional_unit_cell(a0 * np.eye(3))
+        ts.set_voxel_supercell_size(d)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        si = ts.set_supercell_tilt_ng(ctx, 1.0, xifile, d_x=d_x.data_ptr(), n_atoms=len(xw))
+        if i >= warmup:
+            swall.append(time.perf_counter() - t0)
+            fms.append(si["foil_ms"])
+    foil = float(np.median(fms))
+    out["surf_1p2m"] = {"atoms": len(xw), "setup_ms": float(np.median(swall)) * 1e3, "foil_pass_ms": foil,
+                        "replica_atoms_per_s": 27 * len(xw) / (foil * 1e-3), "foil": si["foil"],
+                        "foil_sigma": si["foil_sigma"]}
+    return out
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -590,6 +665,7 @@ def run_gpu(args):
                                                   cpu=(rank == 0 and not args.no_cpu))
         inp = None if args.no_batched else input_leg(ctx, cell, stream, 3, args.warmup,
                                                      cpu=(rank == 0 and not args.no_cpu))
+        tilt = None if args.no_batched else tilt_leg(ctx, cell, 3, args.warmup, cpu=(rank == 0 and not args.no_cpu))
     step_ms = [a.elapsed_time(b) for a, b in ev]
     ms = float(np.mean(step_ms))
     # replicas: one image per rank per step; the slowest rank's time, all ranks' images
@@ -669,7 +745,7 @@ def run_gpu(args):
                          "rms_dI_fp32_vs_fp64": float(np.sqrt((d ** 2).mean()))},
             "gpu_launches": args.steps * launches_per_image(n_prec, fp32=True, average=True),
             "roofline": roof, "peaks": peaks, "wall_s": wall, "clocks": clk.summary(), "batched": batched, "cfg1_128k": cfg1, "cfg5_corrector": cfg5,
-            "output_files": io, "input_file": inp}
+            "output_files": io, "input_file": inp, "tilt_search": tilt}
     if rank == 0:
         if ws == 1 and not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline(x_state=(cell, t, x), rows=args.cpu_rows)
@@ -788,6 +864,13 @@ def ncu_case(args):
     one warm-up and one step of the 4.8M-atom corrector leg (convolutions).  io / input: one
     warm-up and one step of the output-file and input-file legs."""
     from simulated_tem_gb300 import _lib, imaging
+    if args.ncu_case == "tilt":
+        ctx = imaging.Context(0)
+        cell, _, _, _ = workload()
+        r = tilt_leg(ctx, cell, 1, 1, cpu=False)
+        print("ncu case tilt: %s" % json.dumps(r))
+        ctx.close()
+        return
     if args.ncu_case in ("io", "input"):
         import torch
         stream = torch.cuda.Stream()
@@ -838,7 +921,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched sweep and uneven-cell legs")
     ap.add_argument("--batch-steps", type=int, default=3)
-    ap.add_argument("--ncu-case", choices=["fp32", "fp64", "cfg1", "corrector", "io", "input"], default=None,
+    ap.add_argument("--ncu-case", choices=["fp32", "fp64", "cfg1", "corrector", "io", "input", "tilt"], default=None,
                     help="run one small untimed case only (for an ncu capture)")
     args = ap.parse_args()
     if args.ncu_case:

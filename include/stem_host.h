@@ -85,6 +85,76 @@ int st_wrap_pbc_device(st_ctx* ctx, const double* a_vox, int32_t Nx, int32_t Ny,
 int st_atom_extents_device(st_ctx* ctx, int32_t n_cond, const double* k, const double* g, const double* a_cell,
                            const double* d_x, int64_t ldx, int64_t n, double* d);
 
+/* ---- the -ng tilt search: setSupercellTilt1a / setSupercellTilt1
+ * (Lib_DynamicalTwoBeamImaging.f90:795-1045), findBestRotationMatrix and tiltToDarkField
+ * (Lib_DiffractionConditions.f90:129-357, 751-927).  The scores of every candidate beam
+ * direction against every permitted reflection are computed on the GPU; the host takes
+ * the best, re-scoring in the reference's own arithmetic every candidate whose score
+ * lies within the GPU scores' error bound of the best, so that the chosen direction is
+ * the one the reference's arithmetic chooses. */
+
+/* Lattice types (Lib_Lattices.f90:65-69) and table symmetries (Lib_ReadExtinctionDistances.f90:20-22) */
+#define ST_LATTICE_SC 1
+#define ST_LATTICE_BCC 2
+#define ST_LATTICE_FCC 3
+#define ST_LATTICE_HCP 4
+#define ST_SYMMETRY_CUBIC 1
+#define ST_SYMMETRY_HEXAGONAL 2
+
+/* What a tilt search did. */
+typedef struct {
+  int32_t nk;          /* candidate incident vectors (findAllEulerAngles) */
+  int32_t nn;          /* permitted reflections within RHO_MAX */
+  int32_t ii_best;     /* 1-based index of the chosen incident vector */
+  int32_t attempt;     /* 1: THETA_MAX, 2: doubled, 3: no phi limit */
+  int32_t xi_status;   /* readExtinctionDistance: 1 all found, 0 some missing, -1 no file */
+  int32_t n_recheck;   /* candidates re-scored on the host */
+  double ss_best;      /* the chosen score */
+  double theta, phi;   /* the tilt angles of the chosen direction (rad) */
+  double foil;         /* foil thickness used (A) */
+  double foil_sigma;   /* spread of the column thickness with atoms given (A) */
+  double dark_theta;   /* tiltToDarkField's tilt about y (rad) */
+  double scan_ms;      /* GPU time of the scoring launch (CUDA events on the context's stream) */
+  double foil_ms;      /* GPU time of the foil-thickness pass (with atoms given) */
+} st_tilt_info;
+
+/* type(Lattice) of the imaging object (the d2bi -lattice option; default bcc) */
+int st_d2bi_set_lattice(st_d2bi* h, int32_t lattice);
+/* setSupercellTilt1a(this, ng, extinction_distances_filename [, x]) with the module
+ * globals THETA_MAX (deg) and RHO_MAX.  d_x: NULL, or the atoms (ldx, n) in device memory
+ * for the foil thickness from the atoms (d2bi -surf).  info may be NULL. */
+int st_d2bi_set_supercell_tilt1a(st_d2bi* h, st_ctx* ctx, double ng, const char* xifile, double theta_max,
+                                 double rho_max, const double* d_x, int64_t ldx, int64_t n, st_tilt_info* info);
+/* findBestRotationMatrix(v, z0, A_cell, latt, hkl, U, R, xifile, foil_thickness):
+ * U and R column-major. */
+int st_find_best_rotation(st_ctx* ctx, double v, const double* z0, const double* a_cell, int32_t lattice,
+                          const int32_t* hkl, const char* xifile, double foil, double theta_max, double rho_max,
+                          double* U, double* R, st_tilt_info* info);
+/* The scores alone: khat (3, nk) incident vectors against reflections ghkl (3, nn) with
+ * extinction distances xi_g (nn), for velocity v and foil thickness foil; scores[nk]
+ * (host arrays).  The first two reflections are not scored (the reference's [000] and
+ * [hkl] slots) and xi_g[0] is the xi_0 of every term. */
+int st_tilt_scores(st_ctx* ctx, double v, const double* khat, int32_t nk, const double* ghkl, const double* xi_g,
+                   int32_t nn, double foil, double* scores);
+/* tiltToDarkField(v, A_cell, hkl, xi0, xig, foil_thickness, U, R): R updated in place;
+ * theta (may be NULL) receives the tilt about y. */
+int st_tilt_to_dark_field(double v, const double* a_cell, const int32_t* hkl, double xi0, double xig, double foil,
+                          double theta_max, const double* U, double* R, double* theta);
+/* readExtinctionDistance (Lib_ReadExtinctionDistances.f90:29-109): xi_g of n reflections
+ * hkl (3, n) under the table symmetry; *status 1 all found, 0 some missing (those
+ * keep huge(1.0)), -1 no file or no header. */
+int st_read_extinction_distances(const char* path, int32_t n, const int32_t* hkl, int32_t symmetry, double* xi_g,
+                                 int32_t* status);
+/* permittedReflections (Lib_Lattices.f90:678-735): *n reflections with |hkl| <= rho;
+ * the first cap are written to hkl (3, cap) when hkl is not NULL. */
+int st_permitted_reflections(int32_t lattice, double rho, int32_t* hkl, int32_t cap, int32_t* n);
+/* Lib_Quaternions.f90 RotMatToQuaternion (:246-288; LAPACK DSYEV's dominant eigenvector
+ * restated as a Jacobi eigen-solve), quaternionToRotMat (:290-321), slerp (:526-564);
+ * q = (w, x, y, z). */
+int st_rotmat_to_quaternion(const double* R, double* q);
+int st_quaternion_to_rotmat(const double* q, double* R);
+int st_slerp(const double* q1, const double* q2, double x, double* q);
+
 #ifdef __cplusplus
 }
 #endif

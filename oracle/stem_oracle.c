@@ -1110,11 +1110,24 @@ int oc_d2bi_setup(const oc_args* args, double* x, int64_t ldx, int64_t nAtoms, i
     }
     for (int k = 0; k < 3; ++k) d[k] = xmax[k] - xmin[k];
   }
+  double xi0 = args->xi0, xig = args->xig;
+  if (args->xifile[0]) { /* d2bi.f90:1183-1192 */
+    int idat[6] = {0, 0, 0, (int)lround(args->g[0]), (int)lround(args->g[1]), (int)lround(args->g[2])};
+    double dat[2];
+    int symm = args->lattice == OC_LATTICE_HCP ? OC_SYM_HEX : OC_SYM_CUBIC;
+    if (oc_read_extinction_distances(args->xifile, idat, 2, symm, dat) != 1) return OC_ERR_ARG;
+    xi0 = dat[0];
+    xig = dat[1];
+  }
   oc_d2bi_ctor(t, &super, a0, args->k, args->g, args->V, args->M[0], args->M[1]);
   oc_set_conventional_unit_cell(t, a_cell);
   int rc = oc_set_voxel_supercell_size(t, d);
   if (rc != OC_OK) return rc;
-  if (args->tilt_mode == 1) {
+  if (args->tilt_mode == 3) {
+    rc = oc_set_supercell_tilt1a(t, args->ng, args->xifile, args->lattice, args->thetaMax, args->rhoMax,
+                                 args->surf ? x : NULL, ldx, nAtoms, NULL);
+    if (rc != OC_OK) return rc;
+  } else if (args->tilt_mode == 1) {
     oc_set_deviation_parameter(t, args->sg);
     oc_set_supercell_tilt0(t);
   } else if (args->tilt_mode == 2) {
@@ -1131,7 +1144,7 @@ int oc_d2bi_setup(const oc_args* args, double* x, int64_t ldx, int64_t nAtoms, i
   double U0[9], R0[9];
   memcpy(U0, t->U, sizeof U0);
   memcpy(R0, t->R, sizeof R0);
-  oc_set_extinction_distances(t, args->xi0, args->xig);
+  oc_set_extinction_distances(t, xi0, xig);
   double aperpx, xm[3], modg;
   int mx, my, mz;
   oc_find_image_parameters(t, &aperpx, xm, &modg, &mx, &my, &mz);
@@ -1299,3 +1312,802 @@ long long oc_read_lammps_atoms(const char* path, long long offset, long long n_a
   return bad;
 }
 
+
+/* ------------------------------------------------------------------------ */
+/* The -ng tilt search (setSupercellTilt1a / setSupercellTilt1)             */
+/* ------------------------------------------------------------------------ */
+
+/* NTHETA (Lib_DiffractionConditions.f90:22) and DEGTORAD (:26). */
+#define OC_NTHETA 2000
+static const double DEGTORAD = 3.141592654 / 180;
+
+/* symmetry (Lib_ReadExtinctionDistances.f90:112-170): the standard form of a
+ * reflection under cubic or hexagonal symmetry. */
+static void xi_symmetry(const int* in, int symm, int* out) {
+  int hh = abs(in[0]), kk = abs(in[1]), ll = abs(in[2]);
+  if (symm == OC_SYM_CUBIC) {
+    if (hh >= (kk > ll ? kk : ll)) {
+      if (kk >= ll) { out[0] = hh; out[1] = kk; out[2] = ll; }
+      else { out[0] = hh; out[1] = ll; out[2] = kk; }
+    } else if (kk >= (hh > ll ? hh : ll)) {
+      if (hh >= ll) { out[0] = kk; out[1] = hh; out[2] = ll; }
+      else { out[0] = kk; out[1] = ll; out[2] = hh; }
+    } else {
+      if (hh >= kk) { out[0] = ll; out[1] = hh; out[2] = kk; }
+      else { out[0] = ll; out[1] = kk; out[2] = hh; }
+    }
+  } else {
+    if (in[0] * in[1] >= 0) {
+      if (hh >= kk) { out[0] = hh; out[1] = kk; out[2] = ll; }
+      else { out[0] = kk; out[1] = hh; out[2] = ll; }
+    } else {
+      if (hh >= kk) { out[0] = hh; out[1] = -kk; out[2] = ll; }
+      else { out[0] = kk; out[1] = -hh; out[2] = ll; }
+    }
+  }
+}
+
+/* One list-directed READ of `dummy, idat(3), rdat(5)`: a new record per READ,
+ * items separated by blanks or commas and continued over records as needed.
+ * Returns 0, or -1 at the end of the file or on an item of the wrong form. */
+static int read_xi_record(FILE* f, int* idat, double* rdat) {
+  char line[4096];
+  int got = 0;
+  while (got < 9) {
+    if (!fgets(line, sizeof line, f)) return -1;
+    char* p = line;
+    while (got < 9) {
+      while (*p == ' ' || *p == '\t' || *p == ',' || *p == '\r' || *p == '\n') ++p;
+      if (!*p) break;
+      char* s = p;
+      while (*p && *p != ' ' && *p != '\t' && *p != ',' && *p != '\r' && *p != '\n') ++p;
+      char tok[256];
+      size_t len = (size_t)(p - s) < sizeof tok - 1 ? (size_t)(p - s) : sizeof tok - 1;
+      memcpy(tok, s, len);
+      tok[len] = 0;
+      if (got == 0) {
+        /* the element name: any token */
+      } else if (got <= 3) {
+        char* e;
+        long v = strtol(tok, &e, 10);
+        if (e == tok || *e) return -1;
+        idat[got - 1] = (int)v;
+      } else {
+        for (char* q = tok; *q; ++q)
+          if (*q == 'd' || *q == 'D') *q = 'E';
+        char* e;
+        double v = strtod(tok, &e);
+        if (e == tok || *e) return -1;
+        rdat[got - 4] = v;
+      }
+      ++got;
+    }
+  }
+  return 0;
+}
+
+/* readExtinctionDistance (Lib_ReadExtinctionDistances.f90:29-109). */
+int oc_read_extinction_distances(const char* path, const int* hkl, int n, int symm, double* xi_g) {
+  for (int j = 0; j < n; ++j) xi_g[j] = HUGE1;
+  FILE* f = fopen(path, "r");
+  if (!f) return -1;
+  int* hs = (int*)malloc(sizeof(int) * 3 * (n > 0 ? n : 1));
+  char* found = (char*)calloc(n > 0 ? n : 1, 1);
+  for (int j = 0; j < n; ++j) xi_symmetry(&hkl[3 * j], symm, &hs[3 * j]);
+  char line[4096];
+  int bad = !fgets(line, sizeof line, f);
+  bad = !fgets(line, sizeof line, f); /* only the second read's status is checked */
+  if (bad) {
+    free(hs);
+    free(found);
+    fclose(f);
+    return -1;
+  }
+  for (int ii = 1; ii <= 1000; ++ii) {
+    int idat[3], is[3];
+    double rdat[5];
+    if (read_xi_record(f, idat, rdat) != 0) break;
+    xi_symmetry(idat, symm, is);
+    int all = 1;
+    for (int j = 0; j < n; ++j) {
+      if (is[0] == hs[3 * j] && is[1] == hs[3 * j + 1] && is[2] == hs[3 * j + 2]) {
+        found[j] = 1;
+        xi_g[j] = rdat[4];
+      }
+      all = all && found[j];
+    }
+    if (all) break;
+  }
+  int ok = 1;
+  for (int j = 0; j < n; ++j) ok = ok && found[j];
+  free(hs);
+  free(found);
+  fclose(f);
+  return ok;
+}
+
+/* permittedReflections (Lib_Lattices.f90:678-735): the reflections with
+ * |hkl|^2 <= rho^2 allowed by the lattice, l outermost, h innermost. */
+int oc_permitted_reflections(int latt, double rho, int* hkl, int cap) {
+  int mm = (int)ceil(rho + 1.0e-12);
+  int n = 0;
+  for (int lp = -mm; lp <= mm; ++lp)
+    for (int kp = -mm; kp <= mm; ++kp)
+      for (int hp = -mm; hp <= mm; ++hp) {
+        int rr = lp * lp + kp * kp + hp * hp, ok;
+        if (latt == OC_LATTICE_HCP) {
+          rr = (int)floor((double)((hp + kp) * (hp + kp) + (hp - kp) * (hp - kp) / 3) + lp * lp * 0.375);
+          if (rr > rho * rho + 1.0e-6) continue;
+          ok = !((imod(hp + 2 * kp, 3) == 0) && (imod(abs(lp), 2) == 1));
+        } else {
+          if (rr > rho * rho + 1.0e-6) continue;
+          if (latt == OC_LATTICE_FCC) {
+            int hx = imod(hp, 2), kx = imod(kp, 2), lx = imod(lp, 2);
+            ok = (hx * hx + kx * kx + lx * lx) - (hx * kx + kx * lx + lx * hx) == 0;
+          } else if (latt == OC_LATTICE_BCC) {
+            ok = imod(hp + kp + lp, 2) == 0;
+          } else {
+            ok = 1;
+          }
+        }
+        if (ok) {
+          if (hkl && n < cap) {
+            hkl[3 * n] = hp;
+            hkl[3 * n + 1] = kp;
+            hkl[3 * n + 2] = lp;
+          }
+          ++n;
+        }
+      }
+  return n;
+}
+
+/* find_gvectors_permittedReflections (Lib_DiffractionConditions.f90:1727-1790),
+ * including its second swap, which exchanges hklp(:,1) (not hklp(:,2)) with
+ * hklp(:,ihkl) while ghkl(:,2) is exchanged with ghkl(:,ihkl). */
+static int gvectors_permitted(int latt, const double* B, const int* hkl, double rho, double** ghkl_out,
+                              int** hklp_out) {
+  int n = oc_permitted_reflections(latt, rho, NULL, 0);
+  int* hklp = (int*)malloc(sizeof(int) * 3 * (n > 0 ? n : 1));
+  double* ghkl = (double*)malloc(sizeof(double) * 3 * (n > 0 ? n : 1));
+  oc_permitted_reflections(latt, rho, hklp, n);
+  int i000 = 0, ihkl = 0;
+  for (int ii = 1; ii <= n; ++ii) {
+    int* h = &hklp[3 * (ii - 1)];
+    if (h[0] * h[0] + h[1] * h[1] + h[2] * h[2] == 0) i000 = ii;
+    int d0 = h[0] - hkl[0], d1 = h[1] - hkl[1], d2 = h[2] - hkl[2];
+    if (d0 * d0 + d1 * d1 + d2 * d2 == 0) ihkl = ii;
+    double hd[3] = {(double)h[0], (double)h[1], (double)h[2]};
+    reflection(B, hd, &ghkl[3 * (ii - 1)]);
+  }
+  if (i000 != 0) {
+    for (int c = 0; c < 3; ++c) {
+      double t = ghkl[c];
+      ghkl[c] = ghkl[3 * (i000 - 1) + c];
+      ghkl[3 * (i000 - 1) + c] = t;
+      int u = hklp[c];
+      hklp[c] = hklp[3 * (i000 - 1) + c];
+      hklp[3 * (i000 - 1) + c] = u;
+    }
+  }
+  if (ihkl != 0) {
+    for (int c = 0; c < 3; ++c) {
+      double t = ghkl[3 + c];
+      ghkl[3 + c] = ghkl[3 * (ihkl - 1) + c];
+      ghkl[3 * (ihkl - 1) + c] = t;
+      int u = hklp[c];
+      hklp[c] = hklp[3 * (ihkl - 1) + c];
+      hklp[3 * (ihkl - 1) + c] = u;
+    }
+  }
+  *ghkl_out = ghkl;
+  *hklp_out = hklp;
+  return n;
+}
+
+/* findRotationsForBraggCondition2 (Lib_DiffractionConditions.f90:1382-1515).
+ * mode 0: nolimitPhi absent (|phi - phi0| <= THETA_MAX degrees); 1: present and
+ * true (no limit); 2: present and false (2 THETA_MAX degrees). */
+static int bragg_rotations(double v, const double* g, double cosq, double sinq, double phi0, double theta_max_deg,
+                           int mode, double* phi) {
+  int nphi = 0;
+  double xx = g[1] * sinq + g[2] * cosq;
+  double aa = g[0] * g[0] + g[1] * g[1] + g[2] * g[2];
+  aa = -aa * HBAR / (2 * ME * v);
+  double uu = g[0] * g[0] + xx * xx;
+  double vv = uu - aa * aa;
+  if (vv < 0) return 0;
+  uu = 1 / uu;
+  vv = sqrt(vv) * g[0] * uu;
+  uu = aa * xx * uu;
+  double lim = mode == 2 ? 2 * theta_max_deg * DEGTORAD : theta_max_deg * DEGTORAD;
+  for (int branch = 0; branch < 2; ++branch) {
+    double c = branch == 0 ? uu + vv : uu - vv;
+    if (fabs(c) <= 1) {
+      double pp = acos(c);
+      long jj = lround((pp - phi0) / (2 * PI));
+      pp = pp - 2 * jj * PI;
+      if (mode == 1 || fabs(pp - phi0) <= lim) {
+        phi[nphi] = pp;
+        phi[nphi + 1] = -pp;
+        nphi += 2;
+      }
+    }
+  }
+  return nphi;
+}
+
+/* findAllEulerAngles (Lib_DiffractionConditions.f90:1565-1625): khat(3, 4 NTHETA). */
+static int find_all_euler_angles(double v, const double* g, double theta0, double phi0, double theta_max,
+                                 double theta_max_deg, int mode, double* khat) {
+  double theta_min = theta0 - theta_max / 2;
+  if (!(theta_min > 0.0)) theta_min = 0.0;
+  int nk = 0;
+  for (int ii = 1; ii <= OC_NTHETA; ++ii) {
+    double theta = theta_min + theta_max * ii / OC_NTHETA;
+    double cost = cos(theta), sint = sin(theta), phi[4];
+    int nphi = bragg_rotations(v, g, cost, sint, phi0, theta_max_deg, mode, phi);
+    for (int jj = 0; jj < nphi; ++jj) {
+      double pp = phi[jj], cosp = cos(pp), sinp = sin(pp);
+      khat[3 * (nk + jj)] = -sinp;
+      khat[3 * (nk + jj) + 1] = sint * cosp;
+      khat[3 * (nk + jj) + 2] = cost * cosp;
+    }
+    nk += nphi;
+  }
+  return nk;
+}
+
+/* intensityAtDepthZ (Lib_DiffractionConditions.f90:1209-1259) in the
+ * reference's order of operations: (phig * bg) / (2 dd), then |phig|^2. */
+static double intensity_exact(double xi0, double xig, double sg, double z) {
+  double b0 = PI / xi0, bg = PI / xig, aa = 2 * PI * sg;
+  double dd = sqrt(aa * aa / 4 + bg * bg);
+  double l1 = (b0 + aa / 2) + dd, l2 = (b0 + aa / 2) - dd;
+  double re = cos(l1 * z) - cos(l2 * z), im = sin(l1 * z) - sin(l2 * z);
+  re = re * bg / (2 * dd);
+  im = im * bg / (2 * dd);
+  return re * re + im * im;
+}
+
+/* scoreForIncidentVector1 (Lib_DiffractionConditions.f90:1835-1867). */
+double oc_score_incident_vector(double v, const double* khat, const double* ghkl, const double* xi_g, int nn,
+                                double foil) {
+  double s = 0;
+  for (int ii = 3; ii <= nn; ++ii) {
+    const double* g = &ghkl[3 * (ii - 1)];
+    double eps = energy_deviation_parameter(v, khat, g);
+    double sg = energy_to_length_sg(v, eps);
+    s = s + intensity_exact(xi_g[0], xi_g[ii - 1], sg, foil);
+  }
+  return s;
+}
+
+static int lattice_symmetry(int latt) {
+  if (latt == OC_LATTICE_HCP) return OC_SYM_HEX;
+  if (latt >= OC_LATTICE_SC && latt <= OC_LATTICE_FCC) return OC_SYM_CUBIC;
+  return -1;
+}
+
+/* findBestRotationMatrix (Lib_DiffractionConditions.f90:129-357) without the
+ * optional near-Bragg list.  scores (optional) receives every incident
+ * vector's score, khat (optional) the incident vectors: both 4 NTHETA long. */
+int oc_find_best_rotation(double v, const double* z0, const double* A_cell, int latt, const int* hkl,
+                          const char* xifile, double foil, double theta_max_deg, double rho_max, double* U,
+                          double* R, oc_tilt_info* info, double* scores, double* khat_out) {
+  int symm = lattice_symmetry(latt);
+  if (symm < 0) return OC_ERR_ARG;
+  double BB[9], gg[3], ghkl0[3], hd[3] = {(double)hkl[0], (double)hkl[1], (double)hkl[2]};
+  reciprocal(A_cell, BB);
+  reflection(BB, hd, gg);
+  oc_rotate_to_standard_frame(z0, A_cell, hd, U);
+  mat_vec(U, gg, ghkl0);
+  double* ghkl;
+  int* hklp;
+  int nn = gvectors_permitted(latt, BB, hkl, rho_max, &ghkl, &hklp);
+  double* xi_g = (double*)malloc(sizeof(double) * (nn > 0 ? nn : 1));
+  int xi_ok = oc_read_extinction_distances(xifile, hklp, nn, symm, xi_g);
+  double* khat = (double*)malloc(sizeof(double) * 3 * 4 * OC_NTHETA);
+  int nk = find_all_euler_angles(v, ghkl0, 0.0, 0.0, theta_max_deg * DEGTORAD, theta_max_deg, 0, khat);
+  int attempt = 1;
+  if (nk == 0) {
+    attempt = 2;
+    nk = find_all_euler_angles(v, ghkl0, 0.0, 0.0, 2 * theta_max_deg * DEGTORAD, theta_max_deg, 0, khat);
+    if (nk == 0) {
+      attempt = 3;
+      nk = find_all_euler_angles(v, ghkl0, 0.0, 0.0, theta_max_deg * DEGTORAD, theta_max_deg, 1, khat);
+    }
+  }
+  if (nk == 0) {
+    free(ghkl);
+    free(hklp);
+    free(xi_g);
+    free(khat);
+    return OC_ERR_ARG;
+  }
+  double ss_best = HUGE1;
+  int ii_best = 0;
+  for (int ii = 1; ii <= nk; ++ii) {
+    double ss = oc_score_incident_vector(v, &khat[3 * (ii - 1)], ghkl, xi_g, nn, foil);
+    if (scores) scores[ii - 1] = ss;
+    if (ss < ss_best) {
+      ss_best = ss;
+      ii_best = ii;
+    }
+  }
+  const double* kb = &khat[3 * (ii_best - 1)];
+  double phi = -asin(kb[0]);
+  double theta = acos(kb[2] / cos(phi));
+  A(R, 1, 1) = cos(phi);
+  A(R, 1, 2) = sin(theta) * sin(phi);
+  A(R, 1, 3) = cos(theta) * sin(phi);
+  A(R, 2, 1) = 0.0;
+  A(R, 2, 2) = cos(theta);
+  A(R, 2, 3) = -sin(theta);
+  A(R, 3, 1) = -sin(phi);
+  A(R, 3, 2) = sin(theta) * cos(phi);
+  A(R, 3, 3) = cos(theta) * cos(phi);
+  if (A(R, 3, 3) < 0) {
+    for (int i = 1; i <= 3; ++i) {
+      A(R, i, 3) = -A(R, i, 3);
+      A(R, i, 2) = -A(R, i, 2);
+    }
+  }
+  if (khat_out) memcpy(khat_out, khat, sizeof(double) * 3 * nk);
+  if (info) {
+    info->nk = nk;
+    info->nn = nn;
+    info->ii_best = ii_best;
+    info->attempt = attempt;
+    info->xi_ok = xi_ok;
+    info->ss_best = ss_best;
+    info->theta = theta;
+    info->phi = phi;
+  }
+  free(ghkl);
+  free(hklp);
+  free(xi_g);
+  free(khat);
+  return OC_OK;
+}
+
+/* The scoring inputs of findBestRotationMatrix: the permitted g-vectors after both swaps
+ * and their extinction distances (Lib_DiffractionConditions.f90:204-214).  Returns nn;
+ * the first cap go to ghkl(3, cap) and xi_g(cap). */
+int oc_tilt_reflections(int latt, const double* A_cell, const int* hkl, double rho, const char* xifile,
+                        double* ghkl_out, double* xi_out, int cap) {
+  int symm = lattice_symmetry(latt);
+  if (symm < 0) return -1;
+  double BB[9];
+  reciprocal(A_cell, BB);
+  double* ghkl;
+  int* hklp;
+  int nn = gvectors_permitted(latt, BB, hkl, rho, &ghkl, &hklp);
+  double* xi_g = (double*)malloc(sizeof(double) * (nn > 0 ? nn : 1));
+  oc_read_extinction_distances(xifile, hklp, nn, symm, xi_g);
+  for (int i = 0; i < nn && i < cap; ++i) {
+    memcpy(&ghkl_out[3 * i], &ghkl[3 * i], 3 * sizeof(double));
+    xi_out[i] = xi_g[i];
+  }
+  free(ghkl);
+  free(hklp);
+  free(xi_g);
+  return nn;
+}
+
+/* GoldenSection (Lib_GoldenSection.f90:41-52, 126-150, 152-264, 266-306, 308-381). */
+typedef struct {
+  double x1, x2, x3, y1, y2, y3;
+  int bounded, step;
+  double xtol, ytol;
+} oc_gold;
+
+static const double GOLD_TOL = 1.0e-6, GOLD_MINSTEP = 50, GOLD_BOUNDSTEP = 10;
+
+static double gold_ratio(void) { return (1 + sqrt(5.0)) / 2; }
+
+static void gold_ctor(oc_gold* g, double x1, double x3, double y1, double y3) {
+  if (x1 < x3) {
+    g->x1 = x1; g->x3 = x3; g->y1 = y1; g->y3 = y3;
+  } else {
+    g->x3 = x3; g->x1 = x1; g->y3 = y3; g->y1 = y1;
+  }
+  g->x2 = 0.0;
+  g->y2 = HUGE1;
+  g->step = 0;
+  g->bounded = 0;
+  g->xtol = (g->x3 - g->x1) * GOLD_TOL;
+  double dy = fabs(g->y3 - g->y1);
+  g->ytol = (GOLD_TOL > dy ? GOLD_TOL : dy) * GOLD_TOL;
+}
+
+static void gold_check_bounds(oc_gold* g, double xt, double yt) {
+  if (g->step == 1) {
+    double m = g->y1 < g->y3 ? g->y1 : g->y3;
+    if (yt < m) {
+      g->bounded = 1; g->x2 = xt; g->y2 = yt;
+    } else if (yt > g->y1 && g->y1 > g->y3) {
+      g->bounded = 0; g->x1 = xt; g->y1 = yt;
+    } else if (yt > g->y3 && g->y3 > g->y1) {
+      g->bounded = 0; g->x3 = xt; g->y3 = yt;
+    } else if (g->y1 > yt && yt > g->y3) {
+      g->bounded = 0; g->x1 = xt; g->y1 = yt;
+    } else if (g->y3 > yt && yt > g->y1) {
+      g->bounded = 0; g->x3 = xt; g->y3 = yt;
+    }
+    return;
+  }
+  if (g->y1 < g->y3) {
+    g->bounded = !(yt < g->y1);
+    g->x2 = g->x1; g->x1 = xt; g->y2 = g->y1; g->y1 = yt;
+  } else {
+    g->bounded = !(yt < g->y3);
+    g->x2 = g->x3; g->x3 = xt; g->y2 = g->y3; g->y3 = yt;
+  }
+}
+
+static double gold_next_point(const oc_gold* g) {
+  const double GOLD = gold_ratio();
+  if (!g->bounded) {
+    if (g->step == 0) return g->x1 + (g->x3 - g->x1) * (GOLD - 1);
+    if (g->y1 < g->y3) return g->x1 - (g->x3 - g->x1) / GOLD;
+    return g->x3 + (g->x3 - g->x1) / GOLD;
+  }
+  return g->x1 + (g->x3 - g->x2);
+}
+
+static void gold_minimise(oc_gold* g, double* xt, double* yt, int* is, int* ok) {
+  g->step = g->step + 1;
+  if (!g->bounded) {
+    gold_check_bounds(g, *xt, *yt);
+    *is = 0;
+    *ok = g->bounded || (g->step <= GOLD_BOUNDSTEP);
+    return;
+  }
+  *is = 0;
+  *ok = g->step <= GOLD_MINSTEP;
+  if (!*ok) return;
+  if (*yt < g->y2) {
+    if (*xt < g->x2) {
+      g->x3 = g->x2; g->y3 = g->y2; g->x2 = *xt; g->y2 = *yt;
+    } else {
+      g->x1 = g->x2; g->y1 = g->y2; g->x2 = *xt; g->y2 = *yt;
+    }
+  } else {
+    if (*xt > g->x2) {
+      g->x3 = *xt; g->y3 = *yt;
+    } else {
+      g->x1 = *xt; g->y1 = *yt;
+    }
+  }
+  double ym = g->y1 > g->y3 ? g->y1 : g->y3;
+  *is = (fabs(g->x3 - g->x1) < g->xtol) || (fabs(g->y2 - ym) < g->ytol);
+  if (*is) {
+    *xt = g->x2;
+    *yt = g->y2;
+  }
+}
+
+/* |phi_g(L')|^2 after a tilt x about y (Lib_DiffractionConditions.f90:831-859). */
+static double dark_field_intensity(double x, const double* gg, double bg, double foil) {
+  double cost = cos(x), sint = sin(x);
+  double Lp = foil / cost;
+  double sgp = (sint * gg[0] - cost * gg[2]) / (2 * PI);
+  double s = bg * sin(PI * sqrt(sgp * sgp + bg * bg) * Lp);
+  return s * s / (sgp * sgp + bg * bg);
+}
+
+/* tiltToDarkField (Lib_DiffractionConditions.f90:751-927): R <- Ry(theta) R. */
+int oc_tilt_to_dark_field(double v, const double* A_cell, const int* hkl, double xi0, double xig, double foil,
+                          double theta_max_deg, const double* U, double* R, double* theta_out) {
+  (void)xi0;
+  double BB[9], kk[3], RU[9], gg[3], hd[3] = {(double)hkl[0], (double)hkl[1], (double)hkl[2]};
+  reciprocal(A_cell, BB);
+  reflection(BB, hd, kk);
+  mat_mul(R, U, RU);
+  mat_vec(RU, kk, gg);
+  double bg = 1 / xig;
+  const double kz[3] = {0.0, 0.0, 1.0};
+  double uu = energy_deviation_parameter(v, kz, gg);
+  double sg = energy_to_length_sg(v, uu);
+  double s0 = bg * sin(PI * sqrt(sg * sg + bg * bg) * foil);
+  double phiL2 = s0 * s0 / (sg * sg + bg * bg);
+  double x1 = -(theta_max_deg * 0.01 * DEGTORAD), x3 = +(theta_max_deg * 0.01 * DEGTORAD);
+  double y1 = dark_field_intensity(x1, gg, bg, foil), y3 = dark_field_intensity(x3, gg, bg, foil);
+  oc_gold gold;
+  gold_ctor(&gold, x1, x3, y1, y3);
+  double x2, y2;
+  for (;;) {
+    x2 = gold_next_point(&gold);
+    y2 = dark_field_intensity(x2, gg, bg, foil);
+    int conv, ok;
+    gold_minimise(&gold, &x2, &y2, &conv, &ok);
+    if (conv) break;
+    if (!ok) break;
+  }
+  double theta, cost, sint;
+  if (y2 < phiL2) {
+    theta = x2; cost = cos(x2); sint = sin(x2);
+  } else {
+    theta = 0.0; cost = 1.0; sint = 0.0;
+  }
+  double RR[9];
+  A(RR, 1, 1) = cost; A(RR, 1, 2) = 0.0; A(RR, 1, 3) = sint;
+  A(RR, 2, 1) = 0.0;  A(RR, 2, 2) = 1.0; A(RR, 2, 3) = 0.0;
+  A(RR, 3, 1) = -sint; A(RR, 3, 2) = 0.0; A(RR, 3, 3) = cost;
+  mat_mul(RR, R, R);
+  if (theta_out) *theta_out = theta;
+  return OC_OK;
+}
+
+/* The eigenvector of the largest eigenvalue of a symmetric 4x4 matrix by cyclic
+ * Jacobi rotations.  RotMatToQuaternion calls LAPACK DSYEV for this step; the
+ * largest eigenvalue of its K matrix is isolated (3 against -1, -1, -1 for a
+ * rotation), so any accurate method gives the same unit vector up to sign and
+ * rounding. */
+static void top_eigenvector4(const double* K_in, double* vec) {
+  double a[16], V[16];
+  memcpy(a, K_in, sizeof a);
+  for (int i = 0; i < 16; ++i) V[i] = (i % 5 == 0) ? 1.0 : 0.0;
+#define M4(m, i, j) ((m)[(i) + 4 * (j)])
+  for (int sweep = 0; sweep < 100; ++sweep) {
+    double off = 0.0;
+    for (int p = 0; p < 4; ++p)
+      for (int q = p + 1; q < 4; ++q) off += M4(a, p, q) * M4(a, p, q);
+    if (off == 0.0) break;
+    for (int p = 0; p < 4; ++p)
+      for (int q = p + 1; q < 4; ++q) {
+        double apq = M4(a, p, q);
+        if (apq == 0.0) continue;
+        double th = (M4(a, q, q) - M4(a, p, p)) / (2 * apq);
+        double t = fabs(th) > 1.0e150 ? 0.5 / th : (th >= 0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1));
+        double c = 1 / sqrt(t * t + 1), s = t * c;
+        for (int k = 0; k < 4; ++k) {
+          double akp = M4(a, k, p), akq = M4(a, k, q);
+          M4(a, k, p) = c * akp - s * akq;
+          M4(a, k, q) = s * akp + c * akq;
+        }
+        for (int k = 0; k < 4; ++k) {
+          double apk = M4(a, p, k), aqk = M4(a, q, k);
+          M4(a, p, k) = c * apk - s * aqk;
+          M4(a, q, k) = s * apk + c * aqk;
+        }
+        M4(a, p, q) = 0.0;
+        M4(a, q, p) = 0.0;
+        for (int k = 0; k < 4; ++k) {
+          double vkp = M4(V, k, p), vkq = M4(V, k, q);
+          M4(V, k, p) = c * vkp - s * vkq;
+          M4(V, k, q) = s * vkp + c * vkq;
+        }
+      }
+  }
+  int best = 0;
+  for (int i = 1; i < 4; ++i)
+    if (M4(a, i, i) >= M4(a, best, best)) best = i;
+  for (int k = 0; k < 4; ++k) vec[k] = M4(V, k, best);
+#undef M4
+}
+
+/* RotMatToQuaternion (Lib_Quaternions.f90:246-288): q = (w, x, y, z). */
+void oc_rotmat_to_quaternion(const double* R, double* q) {
+  double K[16] = {0};
+#define K4(i, j) K[((i)-1) + 4 * ((j)-1)]
+  K4(1, 1) = A(R, 1, 1) - A(R, 2, 2) - A(R, 3, 3);
+  K4(2, 1) = A(R, 2, 1) + A(R, 1, 2);
+  K4(3, 1) = A(R, 3, 1) + A(R, 1, 3);
+  K4(4, 1) = A(R, 2, 3) - A(R, 3, 2);
+  K4(2, 2) = A(R, 2, 2) - A(R, 1, 1) - A(R, 3, 3);
+  K4(3, 2) = A(R, 3, 2) + A(R, 2, 3);
+  K4(4, 2) = A(R, 3, 1) - A(R, 1, 3);
+  K4(3, 3) = A(R, 3, 3) - A(R, 1, 1) - A(R, 2, 2);
+  K4(4, 3) = A(R, 1, 2) - A(R, 2, 1);
+  K4(4, 4) = A(R, 1, 1) + A(R, 2, 2) + A(R, 3, 3);
+  for (int j = 1; j <= 4; ++j)
+    for (int i = 1; i < j; ++i) K4(i, j) = K4(j, i); /* DSYEV reads the lower triangle */
+#undef K4
+  double v[4];
+  top_eigenvector4(K, v);
+  if (v[3] > 0)
+    for (int k = 0; k < 4; ++k) v[k] = -v[k];
+  q[1] = v[0];
+  q[2] = v[1];
+  q[3] = v[2];
+  q[0] = -v[3];
+}
+
+/* quaternionToRotMat (Lib_Quaternions.f90:290-321). */
+void oc_quaternion_to_rotmat(const double* q, double* R) {
+  double w = q[0], x = q[1], y = q[2], z = q[3];
+  double ss = (x * x + y * y + z * z + w * w) / 2;
+  A(R, 1, 1) = ss - (y * y + z * z);
+  A(R, 2, 1) = (x * y + z * w);
+  A(R, 3, 1) = (x * z - y * w);
+  A(R, 1, 2) = (x * y - z * w);
+  A(R, 2, 2) = ss - (x * x + z * z);
+  A(R, 3, 2) = (y * z + x * w);
+  A(R, 1, 3) = (x * z + y * w);
+  A(R, 2, 3) = (y * z - x * w);
+  A(R, 3, 3) = ss - (x * x + y * y);
+  ss = 1 / ss;
+  for (int i = 0; i < 9; ++i) R[i] = R[i] * ss;
+}
+
+/* normalise0 (Lib_Quaternions.f90:203-219). */
+static void quaternion_normalise(double* q) {
+  double tt = q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3];
+  if (tt == 0) {
+    q[0] = 1.0;
+    q[1] = q[2] = q[3] = 0.0;
+    return;
+  }
+  tt = 1 / sqrt(tt);
+  for (int k = 0; k < 4; ++k) q[k] = q[k] * tt;
+}
+
+/* slerp (Lib_Quaternions.f90:526-564) with midpoint (:504-524). */
+void oc_slerp(const double* q1, const double* q2, double x, double* qx) {
+  double x1 = q1[0] * q2[0] + q1[1] * q2[1] + q1[2] * q2[2] + q1[3] * q2[3];
+  if (x1 >= 1.0) {
+    memcpy(qx, q1, 4 * sizeof(double));
+    return;
+  }
+  if (x1 <= -1.0) {
+    for (int k = 0; k < 4; ++k) qx[k] = q1[k] + q2[k];
+    double dd = qx[0] * qx[0] + qx[1] * qx[1] + qx[2] * qx[2] + qx[3] * qx[3];
+    if (dd > 0) {
+      dd = 1 / sqrt(dd);
+      for (int k = 0; k < 4; ++k) qx[k] = qx[k] * dd;
+    }
+    return;
+  }
+  double x2 = 2 * x1 * x1 - 1;
+  double omega = acos(x2);
+  x2 = 1 / sin(omega);
+  x1 = sin((1 - x) * omega) * x2;
+  x2 = sin(x * omega) * x2;
+  for (int k = 0; k < 4; ++k) qx[k] = x1 * q1[k] + x2 * q2[k];
+  quaternion_normalise(qx);
+}
+
+/* findFoilThickness (Lib_DynamicalTwoBeamImaging.f90:486-564): the mean and
+ * spread of the foil thickness over columns of about 3 a0.  Returns the
+ * number of columns holding atoms; d receives the cuboid sides. */
+static int find_foil_thickness(oc_d2bi* t, const double* x, int64_t ldx, int64_t nAtoms, const double* RU,
+                               double* d, double* zbar_out, double* zsig_out, int* Nx_out, int* Ny_out) {
+  double dd[3], D[9], a_sup[9];
+  memcpy(dd, t->voxelSupercellDimensions, sizeof dd);
+  super_a(&t->super, a_sup);
+  find_transformed_supercell(a_sup, RU, D, t->delta, t->uvw, &t->nuvw, dd);
+  dd[0] = A(D, 1, 1);
+  dd[1] = A(D, 2, 2);
+  dd[2] = A(D, 3, 3);
+  memcpy(d, dd, sizeof dd);
+  int Nx = (int)lround(dd[0] / (3 * t->a0)), Ny = (int)lround(dd[1] / (3 * t->a0));
+  if (Nx < 1) Nx = 1;
+  if (Ny < 1) Ny = 1;
+  dd[0] = Nx / dd[0];
+  dd[1] = Ny / dd[1];
+  double id3 = 1 / dd[2];
+  double* top = (double*)malloc(sizeof(double) * Nx * Ny);
+  double* thick = (double*)malloc(sizeof(double) * Nx * Ny);
+  for (int i = 0; i < Nx * Ny; ++i) {
+    top[i] = HUGE1;
+    thick[i] = -HUGE1;
+  }
+  for (int nn = 0; nn < t->nuvw; ++nn) {
+    double Ruvw[3];
+    for (int i = 1; i <= 3; ++i)
+      Ruvw[i - 1] = t->uvw[3 * nn] * (A(t->super.a, i, 1) * t->super.Nx) +
+                    t->uvw[3 * nn + 1] * (A(t->super.a, i, 2) * t->super.Ny) +
+                    t->uvw[3 * nn + 2] * (A(t->super.a, i, 3) * t->super.Nz);
+    for (int64_t ii = 0; ii < nAtoms; ++ii) {
+      double xx[3];
+      for (int c = 0; c < 3; ++c) xx[c] = x[ii * ldx + c] + Ruvw[c];
+      mat_vec(RU, xx, xx);
+      for (int c = 0; c < 3; ++c) xx[c] = xx[c] + t->delta[c];
+      int ix = (int)floor(dd[0] * xx[0]);
+      if ((long long)ix * (Nx - 1 - ix) < 0) continue;
+      int iy = (int)floor(dd[1] * xx[1]);
+      if ((long long)iy * (Ny - 1 - iy) < 0) continue;
+      int iz = (int)floor(id3 * xx[2]);
+      if (iz != 0) continue;
+      size_t c = (size_t)ix + (size_t)Nx * iy;
+      if (xx[2] < top[c]) top[c] = xx[2];
+      if (xx[2] > thick[c]) thick[c] = xx[2];
+    }
+  }
+  double zbar = 0.0, z2bar = 0.0;
+  int nn = 0;
+  for (int iy = 0; iy < Ny; ++iy)
+    for (int ix = 0; ix < Nx; ++ix) {
+      size_t c = (size_t)ix + (size_t)Nx * iy;
+      double th = thick[c] > top[c] ? thick[c] - top[c] : 0.0;
+      if (th == 0) continue;
+      zbar = zbar + th;
+      z2bar = z2bar + th * th;
+      nn = nn + 1;
+    }
+  zbar = zbar / nn;
+  z2bar = z2bar / nn;
+  z2bar = z2bar - zbar * zbar;
+  z2bar = sqrt(z2bar > 0.0 ? z2bar : 0.0);
+  *zbar_out = zbar;
+  *zsig_out = z2bar;
+  *Nx_out = Nx;
+  *Ny_out = Ny;
+  free(top);
+  free(thick);
+  return nn;
+}
+
+/* setSupercellTilt1 (Lib_DynamicalTwoBeamImaging.f90:795-939) for integer ng;
+ * x may be NULL (foil thickness from the box). */
+static int set_supercell_tilt1(oc_d2bi* t, int ng, const char* xifile, int latt, double theta_max_deg,
+                               double rho_max, const double* x, int64_t ldx, int64_t nAtoms, oc_tilt_info* info) {
+  int hkl[3];
+  for (int i = 0; i < 3; ++i) hkl[i] = (int)lround(ng * t->g[i]);
+  double zbar;
+  if (x) {
+    double hd[3] = {(double)hkl[0], (double)hkl[1], (double)hkl[2]}, dd[3], zsig;
+    int Nx, Ny;
+    oc_rotate_to_standard_frame(t->k, t->a_cell, hd, t->U);
+    find_foil_thickness(t, x, ldx, nAtoms, t->U, dd, &zbar, &zsig, &Nx, &Ny);
+    if (zbar + 2 * t->a0 > dd[2]) zbar = dd[2];
+    if (info) info->foil_sigma = zsig;
+  } else {
+    zbar = t->voxelSupercellDimensions[2];
+  }
+  t->foilThickness = zbar;
+  double vv = oc_velocity(t->E * 1000);
+  double z = fabs(t->foilThickness);
+  int rc = oc_find_best_rotation(vv, t->k, t->a_cell, latt, hkl, xifile, z, theta_max_deg, rho_max, t->U, t->R,
+                                 info, NULL, NULL);
+  if (rc != OC_OK) return rc;
+  z = fabs(t->foilThickness / A(t->R, 3, 3));
+  int g_int[3] = {(int)lround(t->g[0]), (int)lround(t->g[1]), (int)lround(t->g[2])};
+  double theta;
+  oc_tilt_to_dark_field(oc_velocity(t->E * 1000), t->a_cell, g_int, t->xi0, t->xig, z, theta_max_deg, t->U, t->R,
+                        &theta);
+  if (info) {
+    info->foil = t->foilThickness;
+    info->dark_theta = theta;
+  }
+  t->voxelSupercellDimensions[2] = fabs(t->voxelSupercellDimensions[2] / A(t->R, 3, 3));
+  double RU[9], a_sup[9], D[9], gg[3];
+  mat_mul(t->R, t->U, RU);
+  super_a(&t->super, a_sup);
+  find_transformed_supercell(a_sup, RU, D, t->delta, t->uvw, &t->nuvw, t->voxelSupercellDimensions);
+  build_gksuper(t, D);
+  oc_get_aperture(t, NULL, gg);
+  t->sg = oc_get_deviation_parameter(t, gg);
+  return OC_OK;
+}
+
+/* setSupercellTilt1a (Lib_DynamicalTwoBeamImaging.f90:943-1045). */
+int oc_set_supercell_tilt1a(oc_d2bi* t, double ng, const char* xifile, int latt, double theta_max_deg,
+                            double rho_max, const double* x, int64_t ldx, int64_t nAtoms, oc_tilt_info* info) {
+  double dd[3], q1[4], q2[4], q[4];
+  memcpy(dd, t->voxelSupercellDimensions, sizeof dd);
+  int rc = set_supercell_tilt1(t, (int)floor(ng), xifile, latt, theta_max_deg, rho_max, x, ldx, nAtoms, info);
+  if (rc != OC_OK) return rc;
+  oc_rotmat_to_quaternion(t->R, q1);
+  if (ng - floor(ng) > 1.0e-4) {
+    memcpy(t->voxelSupercellDimensions, dd, sizeof dd);
+    rc = set_supercell_tilt1(t, (int)ceil(ng), xifile, latt, theta_max_deg, rho_max, x, ldx, nAtoms, NULL);
+    if (rc != OC_OK) return rc;
+    oc_rotmat_to_quaternion(t->R, q2);
+  } else {
+    memcpy(q2, q1, sizeof q1);
+  }
+  oc_slerp(q1, q2, ng - floor(ng), q);
+  oc_quaternion_to_rotmat(q, t->R);
+  t->voxelSupercellDimensions[2] = fabs(dd[2] / A(t->R, 3, 3));
+  double RU[9], a_sup[9], D[9], gg[3];
+  mat_mul(t->R, t->U, RU);
+  super_a(&t->super, a_sup);
+  find_transformed_supercell(a_sup, RU, D, t->delta, t->uvw, &t->nuvw, t->voxelSupercellDimensions);
+  build_gksuper(t, D);
+  oc_get_aperture(t, NULL, gg);
+  t->sg = oc_get_deviation_parameter(t, gg);
+  return OC_OK;
+}

@@ -34,6 +34,16 @@ extern "C" {
 #define OC_ERR_CAPACITY 2
 #define OC_ERR_ALLOC 3
 
+/* Lattice types (Lib_Lattices.f90:65-69) and the symmetry of their
+ * extinction-distance tables (Lib_ReadExtinctionDistances.f90:20-22). */
+#define OC_LATTICE_CUSTOM 0
+#define OC_LATTICE_SC 1
+#define OC_LATTICE_BCC 2
+#define OC_LATTICE_FCC 3
+#define OC_LATTICE_HCP 4
+#define OC_SYM_CUBIC 1
+#define OC_SYM_HEX 2
+
 /* SimpleSupercell (Lib_SimpleSupercells.f90:51-55). */
 typedef struct {
   int Nx, Ny, Nz;
@@ -113,7 +123,27 @@ typedef struct {
   int nTomo;          /* -nTomoAngle */
   double tomoAngle;   /* -tomoAngle (deg) */
   int dark;           /* -dark */
+  double ng;          /* -ng (tilt_mode 3) */
+  int lattice;        /* -lattice: OC_LATTICE_* */
+  int surf;           /* -surf: foil thickness from the atoms */
+  double thetaMax;    /* -theta: THETA_MAX (deg) */
+  double rhoMax;      /* RHO_MAX */
+  char xifile[512];   /* -xifile ("" when absent) */
 } oc_args;
+
+/* What the tilt search found (findBestRotationMatrix and setSupercellTilt1). */
+typedef struct {
+  int nk;           /* incident vectors scored */
+  int nn;           /* permitted reflections */
+  int ii_best;      /* 1-based index of the best incident vector */
+  int attempt;      /* 1: THETA_MAX, 2: doubled, 3: no phi limit */
+  int xi_ok;        /* readExtinctionDistance: 1 all found, 0 some missing, -1 no file */
+  double ss_best;   /* its score */
+  double theta, phi;
+  double foil;        /* foil thickness used */
+  double foil_sigma;  /* spread of the column thickness (with -surf) */
+  double dark_theta;  /* tiltToDarkField's tilt about y */
+} oc_tilt_info;
 
 /* --- Lib_SimpleSupercells / Lib_DiffractionConditions / Lib_RelativisticElectrons --- */
 double oc_norm2(const double* v);
@@ -193,6 +223,37 @@ long long oc_format_f12_7(const double* v, long long n, char* out);
  * n_atoms lines read as id, type, x, y, z (strtod-rounded); x(3, n), types(n).  Returns
  * 0, or 1 + the 0-based index of the first line that does not hold five values. */
 long long oc_read_lammps_atoms(const char* path, long long offset, long long n_atoms, double* x, int* types);
+
+/* --- the -ng tilt search --- */
+/* readExtinctionDistance (Lib_ReadExtinctionDistances.f90:29-109): xi_g of the
+ * n reflections hkl(3, n); 1 all found, 0 some missing (xi_g = huge(1.0)),
+ * -1 no file or no header. */
+int oc_read_extinction_distances(const char* path, const int* hkl, int n, int symm, double* xi_g);
+/* permittedReflections (Lib_Lattices.f90:678-735): the number of reflections;
+ * the first cap of them go to hkl(3, cap) when hkl is not NULL. */
+int oc_permitted_reflections(int latt, double rho, int* hkl, int cap);
+/* scoreForIncidentVector1 (Lib_DiffractionConditions.f90:1835-1867). */
+double oc_score_incident_vector(double v, const double* khat, const double* ghkl, const double* xi_g, int nn,
+                                double foil);
+/* findBestRotationMatrix (Lib_DiffractionConditions.f90:129-357). */
+int oc_find_best_rotation(double v, const double* z0, const double* A_cell, int latt, const int* hkl,
+                          const char* xifile, double foil, double theta_max_deg, double rho_max, double* U,
+                          double* R, oc_tilt_info* info, double* scores, double* khat);
+/* The permitted g-vectors (after find_gvectors_permittedReflections' swaps) and their
+ * extinction distances, as findBestRotationMatrix scores them; returns nn. */
+int oc_tilt_reflections(int latt, const double* A_cell, const int* hkl, double rho, const char* xifile,
+                        double* ghkl, double* xi_g, int cap);
+/* tiltToDarkField (Lib_DiffractionConditions.f90:751-927). */
+int oc_tilt_to_dark_field(double v, const double* A_cell, const int* hkl, double xi0, double xig, double foil,
+                          double theta_max_deg, const double* U, double* R, double* theta_out);
+/* Lib_Quaternions.f90:246-288, 290-321, 526-564; q = (w, x, y, z). */
+void oc_rotmat_to_quaternion(const double* R, double* q);
+void oc_quaternion_to_rotmat(const double* q, double* R);
+void oc_slerp(const double* q1, const double* q2, double x, double* qx);
+/* setSupercellTilt1a (Lib_DynamicalTwoBeamImaging.f90:943-1045); x (ldx, nAtoms)
+ * or NULL (foil thickness from the box, no -surf). */
+int oc_set_supercell_tilt1a(oc_d2bi* t, double ng, const char* xifile, int latt, double theta_max_deg,
+                            double rho_max, const double* x, int64_t ldx, int64_t nAtoms, oc_tilt_info* info);
 
 #ifdef __cplusplus
 }

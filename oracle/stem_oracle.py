@@ -49,7 +49,16 @@ class Args(ctypes.Structure):
     _fields_ = [("a_super", _d * 9), ("a0in", _d), ("k", _d * 3), ("g", _d * 3), ("V", _d), ("M", _i * 2),
                 ("tilt_mode", _i), ("sg", _d), ("haveU", _i), ("U", _d * 9), ("R", _d * 9), ("haveD", _i),
                 ("d0", _d * 3), ("xi0", _d), ("xig", _d), ("useDensity", _i), ("nPrec", _i), ("precAngle", _d),
-                ("nTomo", _i), ("tomoAngle", _d), ("dark", _i)]
+                ("nTomo", _i), ("tomoAngle", _d), ("dark", _i), ("ng", _d), ("lattice", _i), ("surf", _i),
+                ("thetaMax", _d), ("rhoMax", _d), ("xifile", ctypes.c_char * 512)]
+
+
+class TiltInfo(ctypes.Structure):
+    _fields_ = [("nk", _i), ("nn", _i), ("ii_best", _i), ("attempt", _i), ("xi_ok", _i), ("ss_best", _d),
+                ("theta", _d), ("phi", _d), ("foil", _d), ("foil_sigma", _d), ("dark_theta", _d)]
+
+
+LATTICES = {"custom": 0, "sc": 1, "bcc": 2, "fcc": 3, "hcp": 4}
 
 
 _lib = None
@@ -72,6 +81,7 @@ def lib():
         L.oc_intensity_at_depth.restype = _d
         L.oc_integrate_column.restype = _d
         L.oc_get_deviation_parameter.restype = _d
+        L.oc_score_incident_vector.restype = _d
         for name in ("oc_image_geometry", "oc_patch_image", "oc_patch_image_rows", "oc_compute_d2bi_img",
                      "oc_neighbour_list", "oc_d2bi_setup"):
             getattr(L, name).restype = _i
@@ -90,7 +100,8 @@ def _mat(m):
 
 
 def make_args(a_super, a0, k, g, V=200.0, M=(4, 4), sg=None, R=None, U=None, d=None, xi0=103.889565,
-              xig=207.533203, density=False, nPrec=1, precAngle=0.005, nTomo=1, tomoAngle=20.0, dark=True):
+              xig=207.533203, density=False, nPrec=1, precAngle=0.005, nTomo=1, tomoAngle=20.0, dark=True, ng=None,
+              xifile=None, lattice="bcc", surf=False, theta_max=5.0, rho_max=10.0):
     """d2bi command-line arguments for one diffraction condition (src/d2bi.f90:48-100 defaults)."""
     a = Args()
     a.a_super[:] = list(np.asarray(a_super, dtype=np.float64).T.reshape(-1))
@@ -99,7 +110,15 @@ def make_args(a_super, a0, k, g, V=200.0, M=(4, 4), sg=None, R=None, U=None, d=N
     a.g[:] = list(map(float, g))
     a.V = V
     a.M[:] = list(M)
-    if R is not None:
+    a.lattice = LATTICES[lattice]
+    a.thetaMax, a.rhoMax = theta_max, rho_max
+    a.surf = int(bool(surf))
+    if xifile:
+        a.xifile = xifile.encode()
+    if ng is not None:
+        a.tilt_mode = 3
+        a.ng = ng
+    elif R is not None:
         a.tilt_mode = 2
         a.R[:] = list(np.asarray(R, dtype=np.float64).T.reshape(-1))
         if U is not None:
@@ -289,3 +308,57 @@ def neighbour_list(a_cell, cells, nmax0, points, query, cutoff):
     if n < 0:
         raise RuntimeError("oracle neighbour list failed: %d" % -n)
     return ids[:n], dx[:n], r2[:n], mc.value
+
+
+def read_extinction_distances(path, hkl, symm=1):
+    """readExtinctionDistance: (xi_g (n,), status 1 / 0 / -1)."""
+    hkl = np.ascontiguousarray(hkl, dtype=np.int32).reshape(-1, 3)
+    xi = np.zeros(len(hkl))
+    rc = lib().oc_read_extinction_distances(path.encode(), hkl.ctypes.data_as(_ip), _i(len(hkl)), _i(symm),
+                                            _dptr(xi))
+    return xi, rc
+
+
+def permitted_reflections(lattice, rho=10.0):
+    L = lib()
+    n = L.oc_permitted_reflections(_i(LATTICES[lattice]), _d(rho), None, _i(0))
+    hkl = np.zeros((n, 3), dtype=np.int32)
+    L.oc_permitted_reflections(_i(LATTICES[lattice]), _d(rho), hkl.ctypes.data_as(_ip), _i(n))
+    return hkl
+
+
+def find_best_rotation(v, z0, a_cell, lattice, hkl, xifile, foil, theta_max=5.0, rho_max=10.0):
+    """findBestRotationMatrix: (U, R, TiltInfo, scores (nk,), khat (nk, 3))."""
+    U, R = (_d * 9)(), (_d * 9)()
+    info = TiltInfo()
+    scores = np.zeros(8000)
+    khat = np.zeros((8000, 3))
+    h = (_i * 3)(*[int(t) for t in hkl])
+    rc = lib().oc_find_best_rotation(_d(v), (_d * 3)(*map(float, z0)), _mat(a_cell), _i(LATTICES[lattice]), h,
+                                     xifile.encode(), _d(foil), _d(theta_max), _d(rho_max), U, R,
+                                     ctypes.byref(info), _dptr(scores), _dptr(khat))
+    if rc != 0:
+        raise RuntimeError("oracle tilt search failed: %d" % rc)
+    cm = lambda m: np.array(list(m)).reshape(3, 3).T
+    return cm(U), cm(R), info, scores[:info.nk].copy(), khat[:info.nk].copy()
+
+
+def quaternion_round_trip(R):
+    """quaternionToRotMat(RotMatToQuaternion(R)) and the quaternion (w, x, y, z)."""
+    q = (_d * 4)()
+    lib().oc_rotmat_to_quaternion(_mat(R), q)
+    out = (_d * 9)()
+    lib().oc_quaternion_to_rotmat(q, out)
+    return np.array(list(out)).reshape(3, 3).T, np.array(list(q))
+
+
+def tilt_reflections(lattice, a_cell, hkl, xifile, rho=10.0):
+    """The scoring inputs of the tilt search: (ghkl (nn, 3), xi_g (nn,))."""
+    h = (_i * 3)(*[int(t) for t in hkl])
+    L = lib()
+    nn = L.oc_tilt_reflections(_i(LATTICES[lattice]), _mat(a_cell), h, _d(rho), xifile.encode(), None, None, _i(0))
+    g = np.zeros((nn, 3))
+    xi = np.zeros(nn)
+    L.oc_tilt_reflections(_i(LATTICES[lattice]), _mat(a_cell), h, _d(rho), xifile.encode(), _dptr(g), _dptr(xi),
+                          _i(nn))
+    return g, xi

@@ -69,6 +69,18 @@ class StLammpsInfo(ctypes.Structure):
                 ("data_offset", _i64), ("file_bytes", _i64)]
 
 
+class StTiltInfo(ctypes.Structure):
+    """st_tilt_info of include/stem_host.h (what a -ng tilt search did)."""
+    _fields_ = [("nk", _i32), ("nn", _i32), ("ii_best", _i32), ("attempt", _i32), ("xi_status", _i32),
+                ("n_recheck", _i32), ("ss_best", _d), ("theta", _d), ("phi", _d), ("foil", _d),
+                ("foil_sigma", _d), ("dark_theta", _d), ("scan_ms", _d), ("foil_ms", _d)]
+
+
+ST_LATTICES = {"sc": 1, "bcc": 2, "fcc": 3, "hcp": 4}
+ST_SYMMETRY_CUBIC = 1
+ST_SYMMETRY_HEXAGONAL = 2
+
+
 class StemError(RuntimeError):
     def __init__(self, code, msg):
         super().__init__("libstem error %d: %s" % (code, msg))
@@ -133,6 +145,19 @@ _PROTOS = {
     "st_tomography_tilt": (_i32, [_d, _i32, _i32, _dp, _dp]),
     "st_wrap_pbc_device": (_i32, [_vp, _dp, _i32, _i32, _i32, _vp, _i64, _i64, _vp]),
     "st_atom_extents_device": (_i32, [_vp, _i32, _dp, _dp, _dp, _vp, _i64, _i64, _dp]),
+    "st_d2bi_set_lattice": (_i32, [_vp, _i32]),
+    "st_d2bi_set_supercell_tilt1a": (_i32, [_vp, _vp, _d, ctypes.c_char_p, _d, _d, _vp, _i64, _i64,
+                                            ctypes.POINTER(StTiltInfo)]),
+    "st_find_best_rotation": (_i32, [_vp, _d, _dp, _dp, _i32, ctypes.POINTER(_i32), ctypes.c_char_p, _d, _d, _d,
+                                     _dp, _dp, ctypes.POINTER(StTiltInfo)]),
+    "st_tilt_scores": (_i32, [_vp, _d, _dp, _i32, _dp, _dp, _i32, _d, _dp]),
+    "st_tilt_to_dark_field": (_i32, [_d, _dp, ctypes.POINTER(_i32), _d, _d, _d, _d, _dp, _dp, _dp]),
+    "st_read_extinction_distances": (_i32, [ctypes.c_char_p, _i32, ctypes.POINTER(_i32), _i32, _dp,
+                                            ctypes.POINTER(_i32)]),
+    "st_permitted_reflections": (_i32, [_i32, _d, ctypes.POINTER(_i32), _i32, ctypes.POINTER(_i32)]),
+    "st_rotmat_to_quaternion": (_i32, [_dp, _dp]),
+    "st_quaternion_to_rotmat": (_i32, [_dp, _dp]),
+    "st_slerp": (_i32, [_dp, _dp, _d, _dp]),
 }
 
 _lib = None

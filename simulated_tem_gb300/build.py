@@ -25,7 +25,7 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall"]
 
 LIB_SOURCES = ["stem_ctx.cu", "k_bin.cu", "k_column.cu", "k_column_v2.cu", "k_blur.cu", "blur_noalloc.cu", "k_output.cu",
-               "k_parse.cu", "k_geom.cu", "host_d2bi.cpp", "host_output.cpp",
+               "k_parse.cu", "k_geom.cu", "k_tilt.cu", "host_d2bi.cpp", "host_tilt.cpp", "host_output.cpp",
                "host_input.cpp"]
 NN_LIB = os.path.join(HERE, "libstem_nn.so")
 NN_SOURCES = ["nn_conv.cu", "nn_ops.cu", "nn_api.cu"]
@@ -63,6 +63,7 @@ def build(verbose=False, ptxas_info=False):
     inc = os.path.join(HERE, "..", "include")
     libs = [
         (LIB, LIB_SOURCES, [os.path.join(CSRC, "internal.h"), os.path.join(CSRC, "parse_number.cuh"),
+                            os.path.join(CSRC, "host_geom.h"),
                             os.path.join(inc, "stem.h"),
                             os.path.join(inc, "stem_host.h")]),
         (NN_LIB, NN_SOURCES, [os.path.join(CSRC, "nn.h"), os.path.join(CSRC, "tc_sm100.cuh"), os.path.join(CSRC, "nn_conv_strip.cuh"),

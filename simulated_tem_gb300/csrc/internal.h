@@ -190,12 +190,45 @@ struct GeomRot {
   int n;
 };
 cudaError_t launch_wrap_pbc(const GeomWrap& w, double* d_x, int64_t ldx, int64_t n, cudaStream_t st);
+// The -ng tilt search (k_tilt.cu).  TiltScores: the constants of the reference's
+// score arithmetic, computed on the host; the launch writes scores[nk] from khat(3, nk),
+// ghkl(3, nn) and bg[nn] = PI / xi_g.
+struct TiltScores {
+  double cst;        // 2 ME v / HBAR
+  double hbar2on2m;  // HBAR^2 / (2 ME)
+  double den;        // 2 PI HBAR v
+  double twopi;      // 2 PI
+  double b0;         // PI / xi_g(1)
+  double foil;       // foil thickness L
+  int nk, nn;
+};
+constexpr int kTiltSlice = 128;  // reflections per task of the score launch
+int tilt_slices(int nn);         // slices per incident vector: the partial sums per score
+// d_part: nk * tilt_slices(nn) partial sums, vector-major
+cudaError_t launch_tilt_scores(const TiltScores& p, const double* d_khat, const double* d_ghkl, const double* d_bg,
+                               double* d_part, cudaStream_t st);
+// findFoilThickness's column grid: the atoms' highest and lowest z per column over the
+// replicas, as order keys (order_key_value turns one back into its double).
+struct FoilGrid {
+  double RU[9];      // column-major
+  double delta[3];
+  double Ruvw[81];   // replica offsets
+  double ddx, ddy;   // Nx / d1, Ny / d2
+  double id3;        // 1 / d3
+  int Nx, Ny, nuvw;
+};
+constexpr size_t kFoilSmemMax = 96 * 1024;  // grids up to 6,144 columns merge in shared memory
+cudaError_t launch_foil_thickness(const FoilGrid& f, const double* d_x, int64_t ldx, int64_t n,
+                                  unsigned long long* d_top, unsigned long long* d_thick, double top0, double thick0,
+                                  cudaStream_t st);
+double order_key_value(unsigned long long k);
 // context accessors for the host translation units (stem_ctx.cu)
 cudaStream_t ctx_stream(st_ctx* c, void* stream);  // stream, or the context's when null; makes its device current
 int ctx_fail(st_ctx* c, int code, const char* msg);
 int ctx_cuda_fail(st_ctx* c, cudaError_t e, const char* where);
 // scratch of the extents pass: *part (kExtentBlocks * kMaxRot * 6 doubles), *out (6 * kMaxRot)
 cudaError_t ctx_geom_scratch(st_ctx* c, double** part, double** out);
+cudaError_t ctx_tilt_scratch(st_ctx* c, size_t n_doubles, double** p);  // device doubles, grown on demand
 // d_part: kExtentBlocks * kMaxRot * 6 doubles; d_out: 6 per rotation (min x, y, z, max x, y, z)
 cudaError_t launch_extents(const GeomRot& rot, const double* d_x, int64_t ldx, int64_t n, double* d_part,
                            double* d_out, cudaStream_t st);

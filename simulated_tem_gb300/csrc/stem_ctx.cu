@@ -76,6 +76,8 @@ struct st_ctx {
   size_t cap_htext = 0;
   double* d_geom = nullptr;  // extents pass: partial and final minima / maxima
   size_t cap_geom = 0;
+  double* d_tilt = nullptr;  // tilt search: incident vectors, reflections, scores; foil-thickness grid
+  size_t cap_tilt = 0;
 };
 
 namespace {
@@ -791,7 +793,7 @@ extern "C" void st_destroy(st_ctx* c) {
                       c->s.counters, c->s.xtab, c->s.xfv, c->s.ytab, c->s.yfv, c->s.ztab, c->s.zfv, c->s.aa,
                       c->s.aaf, c->b.cell_start, c->b.cell_count, c->b.f64, c->b.cs64, c->b.p32, c->b.cs32,
                       c->d_x, c->d_img, c->d_blur, c->d_kern, c->d_binjobs, c->d_coljobs, c->d_work, c->d_bx, c->d_bimg,
-                      c->d_lvaux, c->d_levels, c->d_text, c->d_pseg, c->d_pstart, c->d_pbad, c->d_geom};
+                      c->d_lvaux, c->d_levels, c->d_text, c->d_pseg, c->d_pstart, c->d_pbad, c->d_geom, c->d_tilt};
   for (void* p : dev_ptrs)
     if (p) cudaFree(p);
   if (c->h_counters) cudaFreeHost(c->h_counters);
@@ -1440,6 +1442,11 @@ cudaError_t ctx_geom_scratch(st_ctx* c, double** part, double** out) {
     *part = c->d_geom;
     *out = c->d_geom + np;
   }
+  return e;
+}
+cudaError_t ctx_tilt_scratch(st_ctx* c, size_t n_doubles, double** p) {
+  const cudaError_t e = ensure(c->d_tilt, c->cap_tilt, n_doubles);
+  if (e == cudaSuccess) *p = c->d_tilt;
   return e;
 }
 }  // namespace stem

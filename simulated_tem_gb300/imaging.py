@@ -275,6 +275,20 @@ class DynamicalTwoBeamImaging:
         else:
             check(lib().st_d2bi_set_supercell_tilt2(self.handle, _cm(np.eye(3) if U is None else U), _cm(R)))
 
+    def set_lattice(self, lattice):
+        """type(Lattice) of the crystal: "sc", "bcc" (the default), "fcc" or "hcp"."""
+        check(lib().st_d2bi_set_lattice(self.handle, _lib.ST_LATTICES[lattice]))
+
+    def set_supercell_tilt_ng(self, ctx, ng, xifile, theta_max=5.0, rho_max=10.0, d_x=0, n_atoms=0, ldx=3):
+        """setSupercellTilt1a(ng, xifile [, x]): the -ng tilt search, its scores on the GPU.
+        d_x: 0, or the device pointer of the atoms (ldx, n_atoms) for the foil thickness from
+        the atoms (-surf).  Returns what the search did (a dict)."""
+        info = _lib.StTiltInfo()
+        ctx._check(lib().st_d2bi_set_supercell_tilt1a(self.handle, ctx.handle, float(ng), xifile.encode(),
+                                                      float(theta_max), float(rho_max), ctypes.c_void_p(d_x),
+                                                      int(ldx), int(n_atoms), ctypes.byref(info)))
+        return _tilt_info(info)
+
     def set_extinction_distances(self, xi0, xig):
         check(lib().st_d2bi_set_extinction_distances(self.handle, float(xi0), float(xig)))
 
@@ -429,29 +443,103 @@ def tomography_tilt(tomo_angle, nn, n_tomo, R0):
     return _from_cm(R)
 
 
+def _tilt_info(info):
+    return {name: getattr(info, name) for name, _ in _lib.StTiltInfo._fields_}
+
+
+def read_extinction_distances(path, hkl, lattice="bcc"):
+    """readExtinctionDistance (src/Lib_ReadExtinctionDistances.f90:29-109): (xi_g (n,),
+    status 1 all found / 0 some missing / -1 no file)."""
+    h = np.ascontiguousarray(hkl, dtype=np.int32).reshape(-1, 3)
+    xi = np.zeros(len(h))
+    st = ctypes.c_int32()
+    symm = _lib.ST_SYMMETRY_HEXAGONAL if lattice == "hcp" else _lib.ST_SYMMETRY_CUBIC
+    check(lib().st_read_extinction_distances(path.encode(), len(h), h.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                             symm, _ptr(xi), ctypes.byref(st)))
+    return xi, st.value
+
+
+def permitted_reflections(lattice, rho=10.0):
+    """permittedReflections (src/Lib_Lattices.f90:678-735): (n, 3) int32 in the reference's order."""
+    n = ctypes.c_int32()
+    L = lib()
+    check(L.st_permitted_reflections(_lib.ST_LATTICES[lattice], float(rho), None, 0, ctypes.byref(n)))
+    h = np.zeros((n.value, 3), dtype=np.int32)
+    check(L.st_permitted_reflections(_lib.ST_LATTICES[lattice], float(rho),
+                                     h.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), n.value, ctypes.byref(n)))
+    return h
+
+
+def find_best_rotation(ctx, v, z0, a_cell, lattice, hkl, xifile, foil, theta_max=5.0, rho_max=10.0):
+    """findBestRotationMatrix (src/Lib_DiffractionConditions.f90:129-357) with the scores on
+    the GPU: (U, R, info dict)."""
+    U, R = (_d * 9)(), (_d * 9)()
+    info = _lib.StTiltInfo()
+    h = (ctypes.c_int32 * 3)(*[int(t) for t in hkl])
+    ctx._check(lib().st_find_best_rotation(ctx.handle, float(v), _v3(z0), _cm(a_cell), _lib.ST_LATTICES[lattice], h,
+                                           xifile.encode(), float(foil), float(theta_max), float(rho_max), U, R,
+                                           ctypes.byref(info)))
+    return _from_cm(U), _from_cm(R), _tilt_info(info)
+
+
+def tilt_scores(ctx, v, khat, ghkl, xi_g, foil):
+    """The scores of incident vectors khat (nk, 3) against reflections ghkl (nn, 3) with
+    extinction distances xi_g (nn,), on the GPU (the first two reflections are not scored)."""
+    khat = np.ascontiguousarray(khat, dtype=np.float64)
+    ghkl = np.ascontiguousarray(ghkl, dtype=np.float64)
+    xi_g = np.ascontiguousarray(xi_g, dtype=np.float64)
+    out = np.zeros(len(khat))
+    ctx._check(lib().st_tilt_scores(ctx.handle, float(v), _ptr(khat), len(khat), _ptr(ghkl), _ptr(xi_g), len(ghkl),
+                                    float(foil), _ptr(out)))
+    return out
+
+
 def d2bi_condition(a_super, a0, k, g, x, V=200.0, M=(4, 4), sg=None, R=None, U=None, d=None, xi0=103.889565,
-                   xig=207.533203, density=False, n_tomo=1, tomo_angle=20.0, tomo_step=0):
+                   xig=207.533203, density=False, n_tomo=1, tomo_angle=20.0, tomo_step=0, ng=None, xifile=None,
+                   lattice="bcc", surf=False, theta_max=5.0, rho_max=10.0, ctx=None):
     """One diffraction condition of the d2bi program (src/d2bi.f90:782-991, 1145-1381).
 
     Returns (imaging, wrapped positions (N, 3), aperpx).  ``a0`` is the cubic
     lattice constant (``-a0``); a bcc/fcc/sc conventional cell a0 * I is used.
+    ``ng`` selects the -ng tilt search (needs ``xifile`` and a GPU context ``ctx``;
+    ``surf`` takes the foil thickness from the atoms); with ``xifile`` xi0 and xig are
+    the table's values for [000] and g (:1183-1192).
     """
     a0 = (a0 + a0 + a0) / 3  # a0 = (a0in(1) + a0in(2) + a0in(3)) / 3 (:787-788)
     xw, a_vox, n = wrap_pbc(a_super, M, a0, x)
     a_cell = a0 * np.eye(3)
     if d is None:
         d = atom_extents(k, g, a_cell, xw)
-    t = _condition(a_vox, n, a0, k, g, d, V, M, sg, R, U, xi0, xig, density, n_tomo, tomo_angle, tomo_step)
+    d_x = None
+    if ng is not None and surf:
+        import torch
+        d_x = torch.from_numpy(np.ascontiguousarray(xw)).to("cuda")
+    t = _condition(a_vox, n, a0, k, g, d, V, M, sg, R, U, xi0, xig, density, n_tomo, tomo_angle, tomo_step,
+                   ng=ng, xifile=xifile, lattice=lattice, theta_max=theta_max, rho_max=rho_max, ctx=ctx,
+                   d_x=0 if d_x is None else d_x.data_ptr(), n_atoms=len(xw))
     return t, xw, t.aperpx
 
 
-def _condition(a_vox, n, a0, k, g, d, V, M, sg, R, U, xi0, xig, density, n_tomo, tomo_angle, tomo_step):
+def _condition(a_vox, n, a0, k, g, d, V, M, sg, R, U, xi0, xig, density, n_tomo, tomo_angle, tomo_step, ng=None,
+               xifile=None, lattice="bcc", theta_max=5.0, rho_max=10.0, ctx=None, d_x=0, n_atoms=0):
     """The imaging set-up of one condition on already wrapped atoms with extents d."""
     a_cell = a0 * np.eye(3)
+    if xifile:
+        gi = [int(np.copysign(np.floor(abs(v) + 0.5), v)) for v in g]  # nint: halves away from zero
+        xi, status = read_extinction_distances(xifile, [[0, 0, 0], gi], lattice)
+        if status != 1:
+            raise _lib.StemError(_lib.ST_ERR_ARG, "no xi_g for [000] and g in %s" % xifile)
+        xi0, xig = float(xi[0]), float(xi[1])
     t = DynamicalTwoBeamImaging(a_vox, n, a0, k, g, V, M[0], M[1])
     t.set_conventional_unit_cell(a_cell)
+    t.set_lattice(lattice)
     t.set_voxel_supercell_size(d)
-    if sg is not None:
+    t.tilt = None
+    if ng is not None:
+        if ctx is None or not xifile:
+            raise _lib.StemError(_lib.ST_ERR_ARG, "the -ng tilt search needs xifile and a GPU context")
+        t.tilt = t.set_supercell_tilt_ng(ctx, ng, xifile, theta_max, rho_max, d_x, n_atoms)
+    elif sg is not None:
         t.set_deviation_parameter(sg)
         t.set_supercell_tilt()
     elif R is not None:

@@ -13,6 +13,9 @@ data and writes compact fixtures beside this script:
   line, and its first and last '(1000f12.7)' records (the output-format fixture).
 * ``w_loop_head.lammps`` -- the first 3,000 atom lines of that input with its header
   (the atom count line set to 3000): the reader's fixture.
+* ``w_xi_V200_T300.dat`` -- the extinction-distance table the ``testD2BI`` ctest reads
+  with ``-xifile`` (``Data/ExtinctionDistances/extinctionDistances.W_V200_T300.dat``),
+  copied line for line: the fixture of the ``-ng`` tilt search.
 * ``linkcell_kat.json``  -- the 200 points and the stored neighbour list of
   ``test/testLib_LinkCell3D.f90``.
 * ``electrons_kat.json`` -- the stored wavelength/velocity strings of
@@ -183,6 +186,10 @@ def main(ref):
         f.write(lammps_head(os.path.join(ref, "Data/test/test.i111_loop_W.lammps")))
     with open(os.path.join(HERE, "w_loop_dat_text.json"), "w") as f:
         json.dump(dat_text(os.path.join(ref, dat + ".dat")), f)
+    with open(os.path.join(ref, "Data/ExtinctionDistances/extinctionDistances.W_V200_T300.dat")) as f:
+        xi_table = f.read()
+    with open(os.path.join(HERE, "w_xi_V200_T300.dat"), "w") as f:
+        f.write(xi_table)
     levels = decode_png16(os.path.join(ref, dat + ".png"))
     np.savez_compressed(os.path.join(HERE, "w_loop_png.npz"), levels=levels)
     with open(os.path.join(HERE, "linkcell_kat.json"), "w") as f:
