@@ -1788,6 +1788,24 @@ static void gold_minimise(oc_gold* g, double* xt, double* yt, int* is, int* ok) 
   }
 }
 
+/* The search loop of tiltToDarkField / testLib_GoldenSection.f90 on any function:
+ * nextPoint, f, minimise until converged or out of steps; returns the number of steps. */
+int oc_golden_minimise(double x1, double x3, double (*f)(double, void*), void* arg, double* xt, double* yt) {
+  oc_gold gold;
+  gold_ctor(&gold, x1, x3, f(x1, arg), f(x3, arg));
+  double x2 = 0.0, y2 = 0.0;
+  int conv = 0, ok = 1;
+  while (1) {
+    x2 = gold_next_point(&gold);
+    y2 = f(x2, arg);
+    gold_minimise(&gold, &x2, &y2, &conv, &ok);
+    if (conv || !ok) break;
+  }
+  *xt = x2;
+  *yt = y2;
+  return conv ? gold.step : -gold.step;
+}
+
 /* |phi_g(L')|^2 after a tilt x about y (Lib_DiffractionConditions.f90:831-859). */
 static double dark_field_intensity(double x, const double* gg, double bg, double foil) {
   double cost = cos(x), sint = sin(x);

@@ -246,6 +246,9 @@ int oc_tilt_reflections(int latt, const double* A_cell, const int* hkl, double r
 /* tiltToDarkField (Lib_DiffractionConditions.f90:751-927). */
 int oc_tilt_to_dark_field(double v, const double* A_cell, const int* hkl, double xi0, double xig, double foil,
                           double theta_max_deg, const double* U, double* R, double* theta_out);
+/* The golden-section search (Lib_GoldenSection.f90) of f over the bracket [x1, x3]:
+ * steps when converged, minus the steps when it ran out of them. */
+int oc_golden_minimise(double x1, double x3, double (*f)(double, void*), void* arg, double* xt, double* yt);
 /* Lib_Quaternions.f90:246-288, 290-321, 526-564; q = (w, x, y, z). */
 void oc_rotmat_to_quaternion(const double* R, double* q);
 void oc_quaternion_to_rotmat(const double* q, double* R);

@@ -20,6 +20,12 @@ data and writes compact fixtures beside this script:
   ``test/testLib_LinkCell3D.f90``.
 * ``electrons_kat.json`` -- the stored wavelength/velocity strings of
   ``test/testLib_RelativisticElectrons.f90``.
+* ``quaternion_kat.json`` -- the rotation matrix of ``test/testLib_Quaternions.f90`` and
+  its stored quaternion components (the test's first output line).
+* ``golden_section_kat.json`` -- the brackets of ``test/testLib_GoldenSection.f90`` (each
+  search must end at a local minimum of the test's function).
+* ``tokenizer_kat.json`` -- the real-array string of ``test/testNBAX_StringTokenizers.f90``
+  and its stored '(100g24.12)' output.
 
 Usage: ``python tests/golden/make_fixtures.py /path/to/reference``.
 """
@@ -175,6 +181,32 @@ def electrons_kat(path):
     return {"V": volts, "wavelength": wl, "velocity": v}
 
 
+def quaternion_kat(path):
+    with open(path) as f:
+        text = f.read()
+    body = text[text.index("R1(1:3,1:3) = reshape("):]
+    body = body[:body.index("(/3,3/)")]
+    r1 = [float(v.replace("d0", "")) for v in re.findall(r"-?\d+\.\d+d0", body)]
+    out = re.search(r'output0 = \(/\s*"([^"]*)"', text).group(1).split()
+    return {"R1_column_major": r1, "q_wxyz": out}
+
+
+def golden_section_kat(path):
+    with open(path) as f:
+        text = f.read()
+    pairs = re.findall(r"x1 = (-?[\d.]+)d0 ; x3 = (-?[\d.]+)d0", text)
+    ok = int(re.search(r"passcount==(\d+)", text).group(1))
+    return {"brackets": [[float(a), float(b)] for a, b in pairs], "pass_count": ok}
+
+
+def tokenizer_kat(path):
+    with open(path) as f:
+        text = f.read()
+    src = re.search(r"dummy = '([-0-9.de ]+)'\s*\n\s*output\(10\)", text).group(1)
+    lines = re.findall(r'"(\s+1\.00000000000\s+[^"]*)"', text)
+    return {"string": src, "g24_12": lines[0].split()}
+
+
 def main(ref):
     box, ids, pos = read_lammps(os.path.join(ref, "Data/test/test.i111_loop_W.lammps"))
     np.savez_compressed(os.path.join(HERE, "w_loop_input.npz"), box=box, ids=ids, pos=pos)
@@ -196,6 +228,12 @@ def main(ref):
         json.dump(linkcell_kat(os.path.join(ref, "test/testLib_LinkCell3D.f90")), f, indent=1)
     with open(os.path.join(HERE, "electrons_kat.json"), "w") as f:
         json.dump(electrons_kat(os.path.join(ref, "test/testLib_RelativisticElectrons.f90")), f, indent=1)
+    with open(os.path.join(HERE, "quaternion_kat.json"), "w") as f:
+        json.dump(quaternion_kat(os.path.join(ref, "test/testLib_Quaternions.f90")), f, indent=1)
+    with open(os.path.join(HERE, "golden_section_kat.json"), "w") as f:
+        json.dump(golden_section_kat(os.path.join(ref, "test/testLib_GoldenSection.f90")), f, indent=1)
+    with open(os.path.join(HERE, "tokenizer_kat.json"), "w") as f:
+        json.dump(tokenizer_kat(os.path.join(ref, "test/testNBAX_StringTokenizers.f90")), f, indent=1)
     print("wrote fixtures:", sorted(os.listdir(HERE)))
 
 

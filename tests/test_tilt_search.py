@@ -189,3 +189,40 @@ def test_condition_api_requires_context_for_ng():
     g = golden_data.w_loop()
     with pytest.raises(_lib.StemError):
         I.d2bi_condition(g["a_super"], 3.1652, (0, 0, 1), (2, 0, 0), g["pos"], ng=1.0, xifile=XI)
+
+
+def test_quaternion_kat():
+    """test/testLib_Quaternions.f90: RotMatToQuaternion of its matrix, '(4f16.8)'."""
+    import json
+    with open(os.path.join(golden_data.GOLDEN, "quaternion_kat.json")) as f:
+        k = json.load(f)
+    R = np.array(k["R1_column_major"]).reshape(3, 3).T
+    _, qo = O.quaternion_round_trip(R)
+    assert ["%.8f" % v for v in qo] == k["q_wxyz"]
+    q = (ctypes.c_double * 4)()
+    assert _lib.lib().st_rotmat_to_quaternion(I._cm(R), q) == 0
+    assert ["%.8f" % v for v in q] == k["q_wxyz"]
+
+
+def test_golden_section_kat():
+    """test/testLib_GoldenSection.f90: from each of its brackets the search ends at a local
+    minimum of the test's function (all seven, the test's pass count)."""
+    import json
+    import math
+    with open(os.path.join(golden_data.GOLDEN, "golden_section_kat.json")) as f:
+        k = json.load(f)
+
+    def func(x):  # the test program's function
+        if x < 0:
+            return HUGE1
+        return 1.0 + x * (1.0 + x * (-0.1 + x * 0.2)) * math.sin(3 * x) + math.cos(x) * math.sqrt(x)
+
+    cb = ctypes.CFUNCTYPE(ctypes.c_double, ctypes.c_double, ctypes.c_void_p)(lambda x, _: func(x))
+    passes = 0
+    for x1, x3 in k["brackets"]:
+        xt, yt = ctypes.c_double(), ctypes.c_double()
+        steps = O.lib().oc_golden_minimise(O._d(x1), O._d(x3), cb, None, ctypes.byref(xt), ctypes.byref(yt))
+        assert steps > 0
+        if min(func(xt.value + 0.001), func(xt.value - 0.001)) > func(xt.value):
+            passes += 1
+    assert passes == k["pass_count"]
