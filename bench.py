@@ -468,6 +468,45 @@ def input_leg(ctx, cell, stream, steps, warmup, cpu=True):
             O.read_lammps_atoms(path, info.data_offset, info.n_atoms)
             out["cpu_oracle"] = {"ms": (time.perf_counter() - t0) * 1e3, "cores": 1, "kind": "port",
                                  "note": "oracle reader: fgets + sscanf per atom line, one core"}
+        # the same cell as an extended .xyz file (species, x, y, z; Lattice= on line 2)
+        xpath = os.path.join(tmp, "cell.xyz")
+        synth.write_xyz(xpath, cell.pos, cell.a_super)
+        xi = imaging.xyz_header(xpath)
+        xnb = xi.file_bytes - xi.data_offset
+        walls = []
+        for i in range(warmup + steps):
+            t0 = time.perf_counter()
+            xx, _, species, _ = ctx.read_xyz(xpath, xi)
+            if i >= warmup:
+                walls.append(time.perf_counter() - t0)
+        with open(xpath, "rb") as f:
+            f.seek(xi.data_offset)
+            xtext = np.frombuffer(f.read(), dtype=np.uint8)
+        d_t = torch.from_numpy(xtext.copy()).cuda()
+        d_x3 = torch.empty((xi.n_read, 3), dtype=torch.float64, device="cuda")
+        d_ty = torch.empty(xi.n_read, dtype=torch.int32, device="cuda")
+        ms = []
+        for i in range(warmup + steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            ctx.parse_xyz_device(d_t.data_ptr(), xnb, xi.n_read, xi.n_columns, d_x3.data_ptr(), 3, d_ty.data_ptr(),
+                                 stream=sp)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if i >= warmup:
+                ms.append(e0.elapsed_time(e1))
+        out["xyz"] = {"workload": "extended .xyz file of the same cell (%d atoms, %.1f MB of atom lines)"
+                                  % (xi.n_read, xnb / 1e6),
+                      "read_file_ms": float(np.median(walls)) * 1e3,
+                      "positions_exact": bool(np.array_equal(xx[:, :3], cell.pos)), "species": species,
+                      "gpu_parse_ms": float(np.median(ms)), "gpu_parse_GB_per_s": xnb / float(np.median(ms)) / 1e6,
+                      "note": "read_file: st_read_xyz (header on the host, atom lines and species on the GPU); "
+                              "gpu_parse: st_parse_xyz_device on text resident in HBM, species numbering included"}
+        if cpu:
+            t0 = time.perf_counter()
+            O.read_xyz_atoms(xpath, O.xyz_header(xpath))
+            out["xyz"]["cpu_oracle"] = {"ms": (time.perf_counter() - t0) * 1e3, "cores": 1, "kind": "port",
+                                        "note": "oracle input0: fgets + strtod per atom line, one core"}
     return out
 
 

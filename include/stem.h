@@ -322,6 +322,58 @@ int st_parse_real(const char* text, int64_t len, double* out, int32_t* used);
 int st_read_lammps(st_ctx* ctx, const char* path, const st_lammps_info* info, double* x, int64_t ldx,
                    int32_t* types);
 
+/* ---- Input: the (extended) .xyz files d2bi reads (src/Lib_XYZFiles.f90:507-626, 756-892,
+ * 905-1058) -------------------------------------------------------------------------- */
+#define ST_XYZ_SUPERCELL_NONE 0
+#define ST_XYZ_SUPERCELL_LATTICE 1  /* extended xyz: Lattice="..." on the description line */
+#define ST_XYZ_SUPERCELL_BOXSIZE 2  /* PARCAS: boxsize on the description line */
+#define ST_XYZ_SUPERCELL_HEADER 3   /* a "supercell" comment line and three vector lines */
+#define ST_XYZ_SPECIES_MAX 1000     /* input0's limit on distinct species names */
+#define ST_XYZ_NAME_LEN 6           /* XYZFILE_ATOMNAMELENGTH: names keep 6 characters */
+
+typedef struct st_xyz_info {
+  int64_t n_atoms;             /* the count line's first token (parseInt) */
+  int64_t n_read;              /* the count line read list-directed (input0); -1 if it is not an integer */
+  int32_t n_columns;           /* numbers after the species on the first atom line */
+  int32_t n_header_lines;      /* comment lines (# % !) before the count line */
+  int32_t lammps;              /* 1: the first line starts "LAMMPS" (read with st_lammps_header) */
+  int32_t supercell_kind;      /* ST_XYZ_SUPERCELL_* */
+  int32_t supercell_ok;        /* getSupercell's ok */
+  int32_t repeats[3];          /* the cell repeats of the "supercell" header form (else 1) */
+  double a_super[9];           /* the supercell, column-major (identity when not found) */
+  int64_t data_offset;         /* byte offset of the first atom line */
+  int64_t file_bytes;
+  char column_description[257];  /* the line after the count line (256 characters kept) */
+} st_xyz_info;
+
+/* The header of an .xyz file as readHeader and getSupercell0 read it; the supercell numbers
+ * through the reference's own ParseReal (NBAX_StringTokenizers.f90:303-420), not a correctly
+ * rounded conversion, so that they carry the reference's bits.  Host only.  ST_ERR_ARG for a
+ * missing file, no count line, or fewer than three numbers on the first atom line. */
+int st_xyz_header(const char* path, st_xyz_info* info);
+
+/* The atom lines of an .xyz file in device memory (d_text, n_bytes, from the first atom
+ * line): line i is read list-directed as `species, x(1:n_columns)` (input0): the species
+ * keeps its first 6 characters; the numbers are correctly rounded.  d_x[i ldx + c] for
+ * c < min(ldx, n_columns) (other rows untouched); d_types[i] (may be null) = 1 + the
+ * species' index in order of first appearance; species (may be null) receives the names
+ * (6 characters each, blank padded) of the first species_cap of the *n_species species.
+ * A line with a missing or malformed value returns ST_ERR_ARG with the first such line
+ * (0-based) in *bad_line.  More than ST_XYZ_SPECIES_MAX species is an error, as in input0.
+ * Waits for the parse to finish. */
+int st_parse_xyz_device(st_ctx* ctx, const char* d_text, int64_t n_bytes, int64_t n_atoms, int32_t n_columns,
+                        double* d_x, int64_t ldx, int32_t* d_types, int32_t* n_species, char* species,
+                        int32_t species_cap, int64_t* bad_line, void* stream);
+
+/* An .xyz file into host arrays: x(ldx, n) with n = info->n_read atoms (columns as for
+ * st_parse_xyz_device), types and the species names as there.  info: st_xyz_header. */
+int st_read_xyz(st_ctx* ctx, const char* path, const st_xyz_info* info, double* x, int64_t ldx, int32_t* types,
+                int32_t* n_species, char* species, int32_t species_cap);
+
+/* The reference's ParseReal on the host (the header-value parser of st_xyz_header): the
+ * value of the first number-like run of text (len bytes) and whether one was found. */
+int st_fortran_parse_real(const char* text, int64_t len, double* out, int32_t* ok);
+
 #ifdef __cplusplus
 }
 #endif

@@ -2129,3 +2129,458 @@ int oc_set_supercell_tilt1a(oc_d2bi* t, double ng, const char* xifile, int latt,
   t->sg = oc_get_deviation_parameter(t, gg);
   return OC_OK;
 }
+
+/* ------------------------------------------------------------------------ */
+/* The .xyz reader (Lib_XYZFiles.f90 readHeader, getSupercell0, input0)       */
+/* ------------------------------------------------------------------------ */
+
+/* gfortran's real ** integer (libgcc __powidf2). */
+static double oc_powi(double x, int m) {
+  unsigned n = m < 0 ? 0u - (unsigned)m : (unsigned)m;
+  double y = (n % 2) ? x : 1.0;
+  while (n >>= 1) {
+    x = x * x;
+    if (n % 2) y = y * x;
+  }
+  return m < 0 ? 1 / y : y;
+}
+
+static int is_number_char(char c) { return (c >= '0' && c <= '9') || (c && strchr(".+-eEdD", c) != NULL); }
+
+/* Fortran s(a:b) of a C string of length n into out (cap 33): empty when b < a;
+ * character(len=32) keeps 32. */
+static void fort_substr(const char* s, int n, int a, int b, char* out) {
+  int k = 0;
+  if (a < 1) a = 1;
+  if (b > n) b = n;
+  for (int i = a; i <= b && k < 32; ++i) out[k++] = s[i - 1];
+  out[k] = 0;
+}
+
+/* ParseReal (NBAX_StringTokenizers.f90:303-420) of text[0..len). */
+int oc_fortran_parse_real(const char* text, int len, double* r) {
+  char str[65];
+  int n = 0, in_num = 0;
+  for (int i = 0; i < len; ++i) {
+    char c = text[i];
+    if (!in_num && c == ' ') continue;
+    if (!is_number_char(c)) break;
+    in_num = 1;
+    str[n++] = c;
+    if (n == 64) break;
+  }
+  str[n] = 0;
+  if (n == 0) return 0;
+  for (int i = 0; i < n; ++i)
+    if (str[i] == 'd' || str[i] == 'D' || str[i] == 'E') str[i] = 'e';
+  char* pd = strchr(str, '.');
+  char* pe = strchr(str, 'e');
+  int ii = pd ? (int)(pd - str) + 1 : 0, jj = pe ? (int)(pe - str) + 1 : 0;
+  char a[33] = "0", b[33] = "0", c[33] = "0";
+  if (ii == 1) {
+    if (jj > 1) {
+      fort_substr(str, n, 2, jj - 1, b);
+      fort_substr(str, n, jj + 1, n, c);
+    } else {
+      fort_substr(str, n, 2, n, b);
+    }
+  } else if (ii > 1) {
+    fort_substr(str, n, 1, ii - 1, a);
+    if (jj > 1) {
+      fort_substr(str, n, ii + 1, jj - 1, b);
+      fort_substr(str, n, jj + 1, n, c);
+    } else {
+      fort_substr(str, n, ii + 1, n, b);
+    }
+  } else {
+    if (jj > 1) {
+      fort_substr(str, n, 1, jj - 1, a);
+      fort_substr(str, n, jj + 1, n, c);
+    } else {
+      fort_substr(str, n, 1, n, a);
+    }
+  }
+  double xa = 0.0;
+  for (char* q = a; *q; ++q) {
+    int d = *q - '0';
+    if (d >= 0 && d <= 9) xa = xa * 10 + d;
+  }
+  int ic = 0;
+  for (char* q = c; *q; ++q) {
+    int d = *q - '0';
+    if (d >= 0 && d <= 9) ic = ic * 10 + d;
+  }
+  if (c[0] == '-') ic = -ic;
+  double xx = 1.0, xb = 0.0;
+  for (char* q = b; *q; ++q) {
+    xx = xx * 0.1;
+    xb = xb + xx * (*q - '0');
+  }
+  double rr = (xa + xb) * oc_powi(10.0, ic);
+  if (a[0] == '-') rr = -rr;
+  if (fabs(rr) == 0) rr = 0;
+  *r = rr;
+  return 1;
+}
+
+static int ltrim_len(const char* s) { /* len_trim */
+  int k = (int)strlen(s);
+  while (k > 0 && s[k - 1] == ' ') --k;
+  return k;
+}
+
+/* StringTokenizer over buf (modified in place; blank padded to its length kk). */
+typedef struct {
+  char buf[1025];
+  const char* delims;
+  int ndelims;
+  int max_tok;
+} oc_tok;
+
+static void tok_init(oc_tok* t, const char* s, const char* delims, int ndelims, int max_tok) {
+  int n = ltrim_len(s);
+  if (n > 1024) n = 1024;
+  memcpy(t->buf, s, (size_t)n);
+  t->buf[n] = 0;
+  t->delims = delims;
+  t->ndelims = ndelims;
+  t->max_tok = max_tok;
+}
+
+static int tok_more(const oc_tok* t) { return ltrim_len(t->buf) > 0; }
+
+static int is_delim(const oc_tok* t, char c) {
+  for (int i = 0; i < t->ndelims; ++i)
+    if (t->delims[i] == c) return 1;
+  return 0;
+}
+
+static void tok_next(oc_tok* t, char* out) {
+  for (;;) {
+    int kk = ltrim_len(t->buf);
+    out[0] = 0;
+    if (kk == 0) return;
+    int jj = kk + 1;
+    for (int p = 0; p < kk; ++p)
+      if (is_delim(t, t->buf[p])) {
+        jj = p + 1;
+        break;
+      }
+    int i = jj - 1 < t->max_tok ? jj - 1 : t->max_tok;
+    if (i < 0) i = 0;
+    memcpy(out, t->buf, (size_t)i);
+    out[i] = 0;
+    char rest[1025];
+    int m = 0;
+    for (int p = jj; p < kk; ++p) rest[m++] = t->buf[p];
+    while (m < kk) rest[m++] = ' ';
+    rest[kk] = 0;
+    memcpy(t->buf, rest, (size_t)kk + 1);
+    if (i > 0) return;
+  }
+}
+
+/* ParseRealArray1 (NBAX_StringTokenizers.f90:273-300). */
+static int parse_real_array(const char* s, double* ra, int cap) {
+  static const char delims[6] = {' ', ',', ';', '\t', '\r', '\0'};
+  oc_tok t;
+  char tmp[1025];
+  int n = ltrim_len(s);
+  if (n > 1024) n = 1024;
+  memcpy(tmp, s, (size_t)n);
+  tmp[n] = 0;
+  tok_init(&t, tmp, delims, 6, 32);
+  int cnt = 0;
+  for (int k = 0; k < 1000000 && tok_more(&t); ++k) {
+    char tok[33];
+    tok_next(&t, tok);
+    double r;
+    if (oc_fortran_parse_real(tok, (int)strlen(tok), &r)) {
+      ra[cnt++] = r;
+      if (cnt == cap) break;
+    }
+  }
+  return cnt;
+}
+
+/* parseInt (NBAX_StringTokenizers.f90:534-564). */
+static int fortran_parse_int(const char* s, long long* v) {
+  long long ii = 0;
+  int started = 0, neg = 0;
+  int n = ltrim_len(s);
+  for (int k = 0; k < n; ++k) {
+    char c = s[k];
+    if (c >= '0' && c <= '9') {
+      ii = ii * 10 + (c - '0');
+      started = 1;
+    } else if (started) {
+      break;
+    } else if (c == '-') {
+      neg = 1;
+    }
+  }
+  if (started) *v = neg ? -ii : ii;
+  return started;
+}
+
+/* one record of at most cap - 1 characters (the rest of a longer line is skipped),
+ * without its newline or a trailing CR; offset advanced by the bytes consumed */
+static int read_record(FILE* f, char* out, int cap, long long* offset) {
+  int c, n = 0, any = 0;
+  while ((c = fgetc(f)) != EOF) {
+    any = 1;
+    ++*offset;
+    if (c == '\n') break;
+    if (n < cap - 1) out[n++] = (char)c;
+  }
+  if (n > 0 && out[n - 1] == '\r') --n;
+  out[n] = 0;
+  return any;
+}
+
+static const char* skip_spaces(const char* s) {
+  while (*s == ' ') ++s;
+  return s;
+}
+
+/* readHeader (Lib_XYZFiles.f90:507-626) and getSupercell0 (:905-1058) for a non-LAMMPS file. */
+int oc_xyz_header(const char* path, oc_xyz_info* info) {
+  memset(info, 0, sizeof *info);
+  for (int i = 0; i < 9; ++i) info->a_super[i] = (i % 4 == 0) ? 1.0 : 0.0;
+  info->repeats[0] = info->repeats[1] = info->repeats[2] = 1;
+  info->n_read = -1;
+  FILE* f = fopen(path, "rb");
+  if (!f) return OC_ERR_ARG;
+  static char line[4097];
+  long long off = 0;
+  if (!read_record(f, line, 257, &off)) {
+    fclose(f);
+    return OC_ERR_ARG;
+  }
+  if (strncmp(skip_spaces(line), "LAMMPS", 6) == 0) {
+    fclose(f);
+    info->lammps = 1;
+    return OC_OK;
+  }
+  rewind(f);
+  off = 0;
+  char count[257] = "";
+  int found = 0, nh = 0;
+  for (int ii = 0; ii < 1000 && read_record(f, line, 257, &off); ++ii) {
+    const char* d = skip_spaces(line);
+    if (*d == '#' || *d == '%' || *d == '!') {
+      ++nh;
+      continue;
+    }
+    size_t nd = strlen(d) < sizeof count - 1 ? strlen(d) : sizeof count - 1;
+    memcpy(count, d, nd);
+    count[nd] = 0;
+    found = 1;
+    break;
+  }
+  char desc[257] = "";
+  int ok = found && read_record(f, desc, 257, &off);
+  info->data_offset = off;
+  ok = ok && read_record(f, line, 4097, &off);
+  fseek(f, 0, SEEK_END);
+  info->file_bytes = ftell(f);
+  if (!ok) {
+    fclose(f);
+    return OC_ERR_ARG;
+  }
+  /* the count: the first blank-delimited token through parseInt */
+  oc_tok ct;
+  char tok[1025];
+  tok_init(&ct, count, " ", 1, 256);
+  tok_next(&ct, tok);
+  long long na;
+  if (!fortran_parse_int(tok, &na)) {
+    fclose(f);
+    return OC_ERR_ARG;
+  }
+  /* input0's list-directed integer read of the same line */
+  {
+    const char* p = count;
+    while (*p == ' ' || *p == '\t') ++p;
+    const char* q = p;
+    while (*q && *q != ' ' && *q != '\t' && *q != ',' && *q != '/') ++q;
+    int good = q > p;
+    const char* d = p;
+    if (good && (*d == '+' || *d == '-')) ++d;
+    good = good && d < q;
+    for (const char* e = d; e < q && good; ++e) good = *e >= '0' && *e <= '9';
+    info->n_read = good ? strtoll(p, NULL, 10) : -1;
+  }
+  /* the first atom line: the species, then the numbers of the rest */
+  oc_tok ft;
+  tok_init(&ft, line, " ", 1, 256);
+  tok_next(&ft, tok);
+  double dat[1000];
+  int nc = parse_real_array(ft.buf, dat, 1000);
+  if (nc < 3) {
+    fclose(f);
+    return OC_ERR_ARG;
+  }
+  info->n_atoms = na;
+  info->n_columns = nc;
+  info->n_header_lines = nh;
+  snprintf(info->column_description, sizeof info->column_description, "%s", desc);
+  /* getSupercell0 */
+  double* a = info->a_super;
+  double v[9];
+  char dt[257];
+  snprintf(dt, sizeof dt, "%s", desc);
+  dt[ltrim_len(dt)] = 0;
+  const char* p;
+  if ((p = strstr(dt, "Lattice=\"")) != NULL) {
+    info->supercell_kind = 1;
+    int n = parse_real_array(desc + (p - dt) + 9, v, 9);
+    if (n == 3) {
+      a[0] = v[0];
+      a[4] = v[1];
+      a[8] = v[2];
+      info->supercell_ok = 1;
+    } else if (n == 9) {
+      memcpy(a, v, sizeof v);
+      info->supercell_ok = 1;
+    }
+  } else if ((p = strstr(dt, "boxsize")) != NULL) {
+    info->supercell_kind = 2;
+    int n = parse_real_array(desc + (p - dt) + 8, v, 9);
+    if (n >= 3) {
+      a[0] = v[0];
+      a[4] = v[1];
+      a[8] = v[2];
+      info->supercell_ok = 1;
+    }
+  } else {
+    rewind(f);
+    off = 0;
+    for (int ii = 0; ii < nh; ++ii) {
+      char d[257];
+      read_record(f, d, 257, &off);
+      const char* j1 = strstr(d, "supercell");
+      const char* j2 = strstr(d, "super cell");
+      long long jj1 = j1 ? (j1 - d) + 1 : 0, jj2 = j2 ? (j2 - d) + 1 : 0;
+      long long jj = jj1 > jj2 ? jj1 : jj2;
+      if (jj == 0) continue;
+      info->supercell_kind = 3;
+      double xm[3] = {1.0, 1.0, 1.0};
+      int n = (long long)strlen(d) >= jj + 8 ? parse_real_array(d + jj + 8, v, 9) : 0;
+      if (n == 3) {
+        xm[0] = v[0];
+        xm[1] = v[1];
+        xm[2] = v[2];
+      }
+      int rp[3];
+      for (int k = 0; k < 3; ++k) rp[k] = (int)lround(xm[k]);
+      for (int kk = 0; kk < 3; ++kk) {
+        char v3[257];
+        read_record(f, v3, 257, &off);
+        int m = strlen(v3) > 2 ? parse_real_array(v3 + 2, v, 9) : 0;
+        if (m == 3) {
+          for (int j = 0; j < 3; ++j) a[kk + 3 * j] = v[j];
+          if (kk == 2) {
+            info->supercell_ok = 1;
+            break;
+          }
+        } else if (m == 9) {
+          memcpy(a, v, sizeof v);
+          info->supercell_ok = 1;
+          break;
+        } else {
+          break;
+        }
+      }
+      if (info->supercell_ok)
+        for (int j = 0; j < 3; ++j) {
+          for (int i = 0; i < 3; ++i) a[i + 3 * j] = a[i + 3 * j] * rp[j];
+          info->repeats[j] = rp[j];
+        }
+      break;
+    }
+  }
+  fclose(f);
+  return OC_OK;
+}
+
+/* input0 (Lib_XYZFiles.f90:756-892): n lines from byte offset `offset`, each read as
+ * `atom, dat(1:ncols)` (strtod-rounded); x(ldx, n) receives the first min(ldx, ncols)
+ * values; types the species numbers in order of first appearance; names (6 characters
+ * each, blank padded, cap names) the species.  Returns the number of species, or
+ * -(1 + the 0-based line) that does not read. */
+long long oc_read_xyz_atoms(const char* path, long long offset, long long n, int ncols, double* x, int ldx,
+                            int* types, char* names, int cap) {
+  FILE* f = fopen(path, "rb");
+  if (!f) return -1;
+  fseek(f, offset, SEEK_SET);
+  size_t lcap = 1 << 16;
+  char* line = (char*)malloc(lcap);
+  char (*tab)[7] = (char (*)[7])calloc(1001, 7);
+  int ns = 0;
+  long long rc = 0;
+  int ncopy = ldx < ncols ? ldx : ncols;
+  for (long long i = 0; i < n; ++i) {
+    if (!fgets(line, (int)lcap, f)) {
+      rc = -(i + 1);
+      break;
+    }
+    char* p = line;
+    while (*p == ' ' || *p == '\t' || *p == ',' || *p == '\r') ++p;
+    char* q = p;
+    while (*q && *q != ' ' && *q != '\t' && *q != ',' && *q != '\r' && *q != '\n' && *q != '/') ++q;
+    if (q == p || *p == '\'' || *p == '"') {
+      rc = -(i + 1);
+      break;
+    }
+    char name[7] = "      ";
+    for (int k = 0; k < 6 && p + k < q; ++k) name[k] = p[k];
+    p = q;
+    int bad = 0;
+    for (int c = 0; c < ncols; ++c) {
+      while (*p == ' ' || *p == '\t' || *p == ',' || *p == '\r') ++p;
+      char* e;
+      char buf[128];
+      int m = 0;
+      while (p[m] && p[m] != ' ' && p[m] != '\t' && p[m] != ',' && p[m] != '\r' && p[m] != '\n' && m < 127) {
+        buf[m] = (p[m] == 'd' || p[m] == 'D') ? 'E' : p[m];
+        ++m;
+      }
+      buf[m] = 0;
+      double v = strtod(buf, &e);
+      if (m == 0 || *e) {
+        bad = 1;
+        break;
+      }
+      if (c < ncopy) x[i * ldx + c] = v;
+      p += m;
+    }
+    if (bad) {
+      rc = -(i + 1);
+      break;
+    }
+    int id = -1;
+    for (int k = 0; k < ns; ++k)
+      if (memcmp(tab[k], name, 6) == 0) {
+        id = k;
+        break;
+      }
+    if (id < 0) {
+      if (ns == 1000) {
+        rc = -(i + 1);
+        break;
+      }
+      memcpy(tab[ns], name, 7);
+      id = ns++;
+    }
+    if (types) types[i] = id + 1;
+  }
+  if (rc == 0) {
+    rc = ns;
+    for (int k = 0; k < ns && k < cap; ++k) memcpy(names + 6 * k, tab[k], 6);
+  }
+  free(line);
+  free(tab);
+  fclose(f);
+  return rc;
+}

@@ -258,6 +258,23 @@ void oc_slerp(const double* q1, const double* q2, double x, double* qx);
 int oc_set_supercell_tilt1a(oc_d2bi* t, double ng, const char* xifile, int latt, double theta_max_deg,
                             double rho_max, const double* x, int64_t ldx, int64_t nAtoms, oc_tilt_info* info);
 
+/* --- the .xyz reader --- */
+typedef struct {
+  long long n_atoms, n_read;
+  int n_columns, n_header_lines, lammps, supercell_kind, supercell_ok;
+  int repeats[3];
+  double a_super[9];
+  long long data_offset, file_bytes;
+  char column_description[257];
+} oc_xyz_info;
+/* ParseReal (NBAX_StringTokenizers.f90:303-420): 1 and *r when a number was found. */
+int oc_fortran_parse_real(const char* text, int len, double* r);
+/* readHeader (Lib_XYZFiles.f90:507-626) and getSupercell0 (:905-1058). */
+int oc_xyz_header(const char* path, oc_xyz_info* info);
+/* input0 (Lib_XYZFiles.f90:756-892): the species count, or -(1 + the bad line). */
+long long oc_read_xyz_atoms(const char* path, long long offset, long long n, int ncols, double* x, int ldx,
+                            int* types, char* names, int cap);
+
 #ifdef __cplusplus
 }
 #endif

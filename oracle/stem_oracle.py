@@ -362,3 +362,42 @@ def tilt_reflections(lattice, a_cell, hkl, xifile, rho=10.0):
     L.oc_tilt_reflections(_i(LATTICES[lattice]), _mat(a_cell), h, _d(rho), xifile.encode(), _dptr(g), _dptr(xi),
                           _i(nn))
     return g, xi
+
+
+class XyzInfo(ctypes.Structure):
+    _fields_ = [("n_atoms", ctypes.c_longlong), ("n_read", ctypes.c_longlong), ("n_columns", _i),
+                ("n_header_lines", _i), ("lammps", _i), ("supercell_kind", _i), ("supercell_ok", _i),
+                ("repeats", _i * 3), ("a_super", _d * 9), ("data_offset", ctypes.c_longlong),
+                ("file_bytes", ctypes.c_longlong), ("column_description", ctypes.c_char * 257)]
+
+
+def xyz_header(path):
+    info = XyzInfo()
+    rc = lib().oc_xyz_header(path.encode(), ctypes.byref(info))
+    if rc != 0:
+        raise RuntimeError("oracle xyz header failed: %d" % rc)
+    return info
+
+
+def read_xyz_atoms(path, info, ldx=None):
+    """input0: (x (n, ldx), types (n,), species names)."""
+    n, nc = info.n_read, info.n_columns
+    ldx = nc if ldx is None else ldx
+    x = np.zeros((n, ldx))
+    types = np.zeros(n, dtype=np.int32)
+    names = ctypes.create_string_buffer(6 * 1000)
+    L = lib()
+    L.oc_read_xyz_atoms.restype = ctypes.c_longlong
+    rc = L.oc_read_xyz_atoms(path.encode(), ctypes.c_longlong(info.data_offset), ctypes.c_longlong(n), _i(nc),
+                             _dptr(x), _i(ldx), types.ctypes.data_as(_ip), names, _i(1000))
+    if rc < 0:
+        raise RuntimeError("oracle xyz read failed at line %d" % (-rc - 1))
+    sp = [names.raw[6 * k:6 * k + 6].decode() for k in range(rc)]
+    return x, types, sp
+
+
+def fortran_parse_real(text):
+    r = _d()
+    b = text.encode()
+    ok = lib().oc_fortran_parse_real(b, _i(len(b)), ctypes.byref(r))
+    return (r.value if ok else None)

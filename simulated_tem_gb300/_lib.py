@@ -69,6 +69,14 @@ class StLammpsInfo(ctypes.Structure):
                 ("data_offset", _i64), ("file_bytes", _i64)]
 
 
+class StXyzInfo(ctypes.Structure):
+    """st_xyz_info of include/stem.h (an .xyz file's header)."""
+    _fields_ = [("n_atoms", _i64), ("n_read", _i64), ("n_columns", _i32), ("n_header_lines", _i32),
+                ("lammps", _i32), ("supercell_kind", _i32), ("supercell_ok", _i32), ("repeats", _i32 * 3),
+                ("a_super", _d * 9), ("data_offset", _i64), ("file_bytes", _i64),
+                ("column_description", ctypes.c_char * 257)]
+
+
 class StTiltInfo(ctypes.Structure):
     """st_tilt_info of include/stem_host.h (what a -ng tilt search did)."""
     _fields_ = [("nk", _i32), ("nn", _i32), ("ii_best", _i32), ("attempt", _i32), ("xi_status", _i32),
@@ -77,6 +85,8 @@ class StTiltInfo(ctypes.Structure):
 
 
 ST_LATTICES = {"sc": 1, "bcc": 2, "fcc": 3, "hcp": 4}
+ST_XYZ_SPECIES_MAX = 1000
+ST_XYZ_NAME_LEN = 6
 ST_SYMMETRY_CUBIC = 1
 ST_SYMMETRY_HEXAGONAL = 2
 
@@ -145,6 +155,12 @@ _PROTOS = {
     "st_tomography_tilt": (_i32, [_d, _i32, _i32, _dp, _dp]),
     "st_wrap_pbc_device": (_i32, [_vp, _dp, _i32, _i32, _i32, _vp, _i64, _i64, _vp]),
     "st_atom_extents_device": (_i32, [_vp, _i32, _dp, _dp, _dp, _vp, _i64, _i64, _dp]),
+    "st_xyz_header": (_i32, [ctypes.c_char_p, ctypes.POINTER(StXyzInfo)]),
+    "st_parse_xyz_device": (_i32, [_vp, _vp, _i64, _i64, _i32, _vp, _i64, _vp, ctypes.POINTER(_i32),
+                                   ctypes.c_char_p, _i32, ctypes.POINTER(_i64), _vp]),
+    "st_read_xyz": (_i32, [_vp, ctypes.c_char_p, ctypes.POINTER(StXyzInfo), _dp, _i64, ctypes.POINTER(_i32),
+                           ctypes.POINTER(_i32), ctypes.c_char_p, _i32]),
+    "st_fortran_parse_real": (_i32, [ctypes.c_char_p, _i64, _dp, ctypes.POINTER(_i32)]),
     "st_d2bi_set_lattice": (_i32, [_vp, _i32]),
     "st_d2bi_set_supercell_tilt1a": (_i32, [_vp, _vp, _d, ctypes.c_char_p, _d, _d, _vp, _i64, _i64,
                                             ctypes.POINTER(StTiltInfo)]),

@@ -238,5 +238,16 @@ int64_t parse_segments(int64_t n_bytes);
 cudaError_t launch_parse_atoms(const char* d_text, int64_t n_bytes, int64_t n_atoms, long long* d_seg,
                                long long* d_starts, double* d_x, int64_t ldx, int* d_types,
                                unsigned long long* d_bad, cudaStream_t st);
+// .xyz atom lines (k_parse.cu): species keys (6 bytes) and ncols numbers per line, the first
+// min(ldx, ncols) into d_x; then species numbers in order of first appearance.
+// d_scratch: species_scratch(n) values; the table of first appearances sits at
+// species_table_offset() (1000 keys, then the count; a count of 1001 means too many).
+cudaError_t launch_parse_xyz(const char* d_text, int64_t n_bytes, int64_t n_atoms, int ncols, long long* d_seg,
+                             long long* d_starts, double* d_x, int64_t ldx, unsigned long long* d_keys,
+                             unsigned long long* d_bad, cudaStream_t st);
+int64_t species_scratch(int64_t n_atoms);
+int species_table_offset();
+cudaError_t launch_species(const unsigned long long* d_keys, int64_t n, unsigned long long* d_scratch,
+                           int32_t* d_types, cudaStream_t st);
 
 }  // namespace stem

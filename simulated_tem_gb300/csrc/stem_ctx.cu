@@ -78,6 +78,10 @@ struct st_ctx {
   size_t cap_geom = 0;
   double* d_tilt = nullptr;  // tilt search: incident vectors, reflections, scores; foil-thickness grid
   size_t cap_tilt = 0;
+  unsigned long long* d_keys = nullptr;  // .xyz reader: species key per atom line
+  size_t cap_keys = 0;
+  unsigned long long* d_species = nullptr;  // .xyz reader: species tables
+  size_t cap_species = 0;
 };
 
 namespace {
@@ -793,7 +797,7 @@ extern "C" void st_destroy(st_ctx* c) {
                       c->s.counters, c->s.xtab, c->s.xfv, c->s.ytab, c->s.yfv, c->s.ztab, c->s.zfv, c->s.aa,
                       c->s.aaf, c->b.cell_start, c->b.cell_count, c->b.f64, c->b.cs64, c->b.p32, c->b.cs32,
                       c->d_x, c->d_img, c->d_blur, c->d_kern, c->d_binjobs, c->d_coljobs, c->d_work, c->d_bx, c->d_bimg,
-                      c->d_lvaux, c->d_levels, c->d_text, c->d_pseg, c->d_pstart, c->d_pbad, c->d_geom, c->d_tilt};
+                      c->d_lvaux, c->d_levels, c->d_text, c->d_pseg, c->d_pstart, c->d_pbad, c->d_geom, c->d_tilt, c->d_keys, c->d_species};
   for (void* p : dev_ptrs)
     if (p) cudaFree(p);
   if (c->h_counters) cudaFreeHost(c->h_counters);
@@ -1423,6 +1427,118 @@ extern "C" int st_read_lammps(st_ctx* c, const char* path, const st_lammps_info*
   if (ldx != 3)
     for (int64_t i = 0; i < n; ++i)
       for (int k = 0; k < 3; ++k) x[i * ldx + k] = xs[(size_t)3 * i + k];
+  return ST_OK;
+}
+
+extern "C" int st_parse_xyz_device(st_ctx* c, const char* d_text, int64_t n_bytes, int64_t n_atoms,
+                                   int32_t n_columns, double* d_x, int64_t ldx, int32_t* d_types, int32_t* n_species,
+                                   char* species, int32_t species_cap, int64_t* bad_line, void* stream) {
+  if (!c) return ST_ERR_ARG;
+  if (bad_line) *bad_line = -1;
+  if (n_species) *n_species = 0;
+  if (!d_text || n_bytes < 0 || n_atoms < 0 || !d_x || ldx < 1 || n_columns < 3 || n_columns > 1000 ||
+      species_cap < 0 || (species_cap > 0 && !species))
+    return fail(c, ST_ERR_ARG, "invalid xyz atom-line arguments");
+  if (n_atoms == 0) return ST_OK;
+  if (n_bytes == 0) {
+    if (bad_line) *bad_line = 0;
+    return fail(c, ST_ERR_ARG, "no atom lines");
+  }
+  cudaSetDevice(c->device);
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+  cudaError_t e = ensure(c->d_pseg, c->cap_pseg, (size_t)parse_segments(n_bytes) + 1);
+  if (e == cudaSuccess) e = ensure(c->d_pstart, c->cap_pstart, (size_t)n_atoms);
+  if (e == cudaSuccess) e = ensure(c->d_pbad, c->cap_pbad, 1);
+  if (e == cudaSuccess) e = ensure(c->d_keys, c->cap_keys, (size_t)n_atoms);
+  if (e == cudaSuccess) e = ensure(c->d_species, c->cap_species, (size_t)species_scratch(n_atoms));
+  if (e != cudaSuccess) return cuda_fail(c, e, "allocating parse buffers");
+  e = launch_parse_xyz(d_text, n_bytes, n_atoms, n_columns, c->d_pseg, c->d_pstart, d_x, ldx, c->d_keys, c->d_pbad,
+                       st);
+  unsigned long long bad = ~0ull;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(c->h_counters, c->d_pbad, sizeof bad, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(c, e, "parsing atom lines");
+  bad = c->h_counters[0];
+  if (bad != ~0ull) {
+    if (bad_line) *bad_line = (int64_t)bad;
+    return fail(c, ST_ERR_ARG, "atom line " + std::to_string(bad + 1) +
+                                   " of the .xyz file is missing or malformed (species and " +
+                                   std::to_string(n_columns) + " numbers expected)");
+  }
+  e = launch_species(c->d_keys, n_atoms, c->d_species, d_types, st);
+  std::vector<unsigned long long> table(1001);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(table.data(), c->d_species + species_table_offset(), 1001 * sizeof(unsigned long long),
+                        cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(c, e, "numbering species");
+  const int cnt = (int)table[1000];
+  if (cnt > ST_XYZ_SPECIES_MAX) return fail(c, ST_ERR_ARG, "more than 1000 species names in the .xyz file");
+  if (n_species) *n_species = cnt;
+  for (int k = 0; k < cnt && k < species_cap; ++k)
+    for (int j = 0; j < ST_XYZ_NAME_LEN; ++j) species[k * ST_XYZ_NAME_LEN + j] = (char)((table[k] >> (8 * j)) & 0xFF);
+  return ST_OK;
+}
+
+extern "C" int st_read_xyz(st_ctx* c, const char* path, const st_xyz_info* info, double* x, int64_t ldx,
+                           int32_t* types, int32_t* n_species, char* species, int32_t species_cap) {
+  if (!c) return ST_ERR_ARG;
+  if (!path || !info || !x || ldx < 1 || info->lammps || info->data_offset < 0 || info->n_columns < 3)
+    return fail(c, ST_ERR_ARG, "invalid xyz read arguments");
+  if (info->n_read < 0) return fail(c, ST_ERR_ARG, "the atom count line does not read as an integer");
+  if (info->n_read > info->n_atoms) return fail(c, ST_ERR_ARG, "more atoms on the count line than expected");
+  const int64_t n = info->n_read;
+  if (n_species) *n_species = 0;
+  if (n == 0) return ST_OK;
+  cudaSetDevice(c->device);
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return fail(c, ST_ERR_ARG, std::string("cannot open ") + path);
+  std::fseek(f, 0, SEEK_END);
+  const long long size = std::ftell(f);
+  const long long nb = size - info->data_offset;
+  if (nb <= 0) {
+    std::fclose(f);
+    return fail(c, ST_ERR_ARG, "no atom lines after the header");
+  }
+  const int nc = info->n_columns;
+  const int64_t lx = ldx < nc ? ldx : nc;  // columns kept
+  cudaError_t e = ensure_host(c->h_text, c->cap_htext, (size_t)nb);
+  if (e == cudaSuccess) e = ensure(c->d_text, c->cap_text, (size_t)nb);
+  if (e == cudaSuccess) e = ensure(c->d_x, c->cap_x, (size_t)lx * n);
+  if (e != cudaSuccess) {
+    std::fclose(f);
+    return cuda_fail(c, e, "allocating read buffers");
+  }
+  std::fseek(f, info->data_offset, SEEK_SET);
+  const size_t got = std::fread(c->h_text, 1, (size_t)nb, f);
+  std::fclose(f);
+  if (got != (size_t)nb) return fail(c, ST_ERR_ARG, std::string("reading ") + path + " failed");
+  e = cudaMemcpyAsync(c->d_text, c->h_text, (size_t)nb, cudaMemcpyHostToDevice, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "copying the atom lines");
+  int32_t* d_types = nullptr;
+  if (types) {
+    e = ensure(c->d_bimg, c->cap_bimg, (size_t)(n + 1) / 2);  // n int32 in the batch-image scratch
+    if (e != cudaSuccess) return cuda_fail(c, e, "allocating read buffers");
+    d_types = reinterpret_cast<int32_t*>(c->d_bimg);
+  }
+  int64_t bad = -1;
+  const int rc = st_parse_xyz_device(c, c->d_text, nb, n, nc, c->d_x, lx, d_types, n_species, species, species_cap,
+                                     &bad, c->stream);
+  if (rc != ST_OK) return rc;
+  std::vector<double> xs;
+  double* dst = x;
+  if (ldx != lx) {
+    xs.resize((size_t)lx * n);
+    dst = xs.data();
+  }
+  e = cudaMemcpyAsync(dst, c->d_x, (size_t)lx * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess && types)
+    e = cudaMemcpyAsync(types, d_types, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "copying the positions");
+  if (ldx != lx)
+    for (int64_t i = 0; i < n; ++i)
+      for (int64_t k = 0; k < lx; ++k) x[i * ldx + k] = xs[(size_t)lx * i + k];
   return ST_OK;
 }
 

@@ -183,6 +183,37 @@ class Context:
                                          ctypes.c_void_p(types.ctypes.data)))
         return x, types, info
 
+    def read_xyz(self, path, info=None, ldx=None):
+        """st_read_xyz: (x (N, ldx), types (N,), species names, header) of an .xyz file, the
+        atom lines parsed on the GPU; ldx defaults to the file's number of columns."""
+        info = xyz_header(path) if info is None else info
+        n = max(int(info.n_read), 0)
+        ldx = int(info.n_columns) if ldx is None else int(ldx)
+        x = np.zeros((n, ldx), dtype=np.float64)
+        types = np.zeros(n, dtype=np.int32)
+        ns = ctypes.c_int32()
+        names = ctypes.create_string_buffer(_lib.ST_XYZ_NAME_LEN * _lib.ST_XYZ_SPECIES_MAX)
+        self._check(lib().st_read_xyz(self.handle, os.fsencode(path), ctypes.byref(info), _ptr(x), ldx,
+                                      types.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), ctypes.byref(ns), names,
+                                      _lib.ST_XYZ_SPECIES_MAX))
+        L = _lib.ST_XYZ_NAME_LEN
+        species = [names.raw[L * k:L * k + L].decode("latin-1") for k in range(ns.value)]
+        return x, types, species, info
+
+    def parse_xyz_device(self, text_ptr, n_bytes, n_atoms, n_columns, x_ptr, ldx, types_ptr=0, stream=0):
+        """st_parse_xyz_device on device buffers: (first bad line or -1, species names)."""
+        bad = ctypes.c_int64(-1)
+        ns = ctypes.c_int32()
+        names = ctypes.create_string_buffer(_lib.ST_XYZ_NAME_LEN * _lib.ST_XYZ_SPECIES_MAX)
+        code = lib().st_parse_xyz_device(self.handle, ctypes.c_void_p(text_ptr), int(n_bytes), int(n_atoms),
+                                         int(n_columns), ctypes.c_void_p(x_ptr), int(ldx),
+                                         ctypes.c_void_p(types_ptr) if types_ptr else None, ctypes.byref(ns), names,
+                                         _lib.ST_XYZ_SPECIES_MAX, ctypes.byref(bad), ctypes.c_void_p(stream))
+        if code != _lib.ST_OK and bad.value < 0:
+            self._check(code)
+        L = _lib.ST_XYZ_NAME_LEN
+        return bad.value, [names.raw[L * k:L * k + L].decode("latin-1") for k in range(ns.value)]
+
     def parse_atoms_device(self, text_ptr, n_bytes, n_atoms, x_ptr, types_ptr=0, stream=0):
         """st_parse_atoms_device on device buffers; returns the first bad line or -1."""
         bad = ctypes.c_int64(-1)
@@ -393,6 +424,24 @@ def lammps_header(path):
     if code != _lib.ST_OK:
         raise _lib.StemError(code, "cannot read the LAMMPS header of %s" % path)
     return info
+
+
+def xyz_header(path):
+    """st_xyz_header: the StXyzInfo of an .xyz file (counts, columns, the supercell)."""
+    info = _lib.StXyzInfo()
+    code = lib().st_xyz_header(os.fsencode(path), ctypes.byref(info))
+    if code != _lib.ST_OK:
+        raise _lib.StemError(code, "cannot read the .xyz header of %s" % path)
+    return info
+
+
+def fortran_parse_real(text):
+    """The reference's ParseReal of a string (None when no number is found)."""
+    b = text.encode("latin-1")
+    out = ctypes.c_double()
+    ok = ctypes.c_int32()
+    check(lib().st_fortran_parse_real(b, len(b), ctypes.byref(out), ctypes.byref(ok)))
+    return out.value if ok.value else None
 
 
 def voxel_supercell(a_super, M, a0):

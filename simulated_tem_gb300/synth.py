@@ -125,3 +125,39 @@ def write_lammps(path, pos, box_hi, mass=55.845, box_lo=(0.0, 0.0, 0.0)):
             p = pos[s:s + chunk]
             f.write("".join("%d 1 %r %r %r 0 0 0\n" % (s + i + 1, a, b, c)
                             for i, (a, b, c) in enumerate(p.tolist())))
+
+
+def write_xyz(path, pos, a_super, species=None, extra=None, form="lattice", comments=()):
+    """An .xyz file the reference reads (src/Lib_XYZFiles.f90:507-626, 756-892): optional
+    comment lines, the atom count, a description line carrying the supercell, then one line
+    per atom: species, x, y, z and any extra columns.  form: "lattice" (extended xyz,
+    Lattice="..." with the nine components of the cell vectors), "boxsize" (PARCAS, the
+    three box lengths) or "header" (a "supercell" comment line with 1 1 1 repeats and the
+    three cell vectors, one per line).  Coordinates are written as the shortest decimal
+    strings that read back to the same doubles."""
+    pos = np.asarray(pos, dtype=np.float64)
+    a = np.asarray(a_super, dtype=np.float64)
+    n = len(pos)
+    species = ["Fe"] * n if species is None else list(species)
+    lines = ["# " + c for c in comments]
+    if form == "header":
+        lines.append("# supercell 1 1 1")
+        for k in range(3):
+            lines.append("# " + " ".join(repr(float(v)) for v in a[:, k]))
+        desc = "positions in Angstrom"
+    elif form == "boxsize":
+        desc = "boxsize %r %r %r" % (float(a[0, 0]), float(a[1, 1]), float(a[2, 2]))
+    else:
+        desc = 'Lattice="%s" Properties=species:S:1:pos:R:3' % " ".join(repr(float(v)) for v in a.T.reshape(-1))
+    lines += ["%d" % n, desc]
+    with open(path, "w") as f:
+        f.write("\n".join(lines) + "\n")
+        chunk = 100_000
+        for s in range(0, n, chunk):
+            rows = []
+            for i in range(s, min(n, s + chunk)):
+                vals = [repr(float(v)) for v in pos[i]]
+                if extra is not None:
+                    vals += [repr(float(v)) for v in np.atleast_1d(extra[i])]
+                rows.append("%s %s\n" % (species[i], " ".join(vals)))
+            f.write("".join(rows))
