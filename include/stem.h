@@ -89,6 +89,8 @@ typedef struct st_stats {
   double ms_column;    /* device time of the column kernel (ms) */
   int32_t column_kernel; /* 1 general FP32, 2 slab-ring FP32 (for at least one image), 3 FP64 */
   int32_t ring_variant;  /* occupancy variant of the last slab-ring launch, -1 if none ran */
+  int32_t ring_slab_atoms; /* staging capacity per slab of the last slab-ring launch (0 if none ran) */
+  int32_t pad0;
 } st_stats;
 
 /* Context on CUDA device `device` (made current for the calls). */

@@ -101,6 +101,7 @@ struct ColumnParams {
   int accumulate;   // add into img instead of overwriting
   int use_density;
   int check_cells;  // restrict to the 27 cells around the home cell (needed when a cell is < 3 sigma)
+  int trunc_z;      // the z cells are shorter than 3 sigma (the slab ring applies the 27-cell rule in z)
   int want_stats;
   double a11, a22, a33;  // link-cell sides (cuboid)
   double cut2;           // (3 sigma)^2
@@ -155,11 +156,11 @@ struct ColumnJob {
 };
 int column_tiles(const ColumnParams& p);
 // `variant` selects the register budget (occupancy) of the launch, 0 .. ring_variant_count() - 1;
-// `big_slabs` stages up to 256 atoms per slab instead of 128 (dense footprints).  Every
+// `slab_tier` 0, 1, 2 stages up to 128, 192, 256 atoms per slab (dense footprints).  Every
 // variant computes the same image to the last bit.  `masked`: some jobs carry a tile mask
 // (then max_np must be 1 and stats false).
 cudaError_t launch_column_fp32_ring(const ColumnJob* d_jobs, int n_jobs, int total_tiles, int max_np, bool density,
-                                    bool stats, int variant, bool big_slabs, bool masked, unsigned* work,
+                                    bool stats, int variant, int slab_tier, bool masked, unsigned* work,
                                     const unsigned long long* counters, int64_t cap, cudaStream_t st);
 int ring_variant_count();
 int ring_np_bucket(int max_np);  // the kernel template (angles per pass) serving max_np angles

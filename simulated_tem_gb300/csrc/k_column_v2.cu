@@ -24,11 +24,13 @@
 // * The march does no FP64 arithmetic: the slice depths come from a per-image
 //   table of FP32 values that the host computes in FP64.
 //
-// It needs every link cell to be at least 3 sigma wide (then "within 3 sigma"
-// equals the reference's 27-cell search) and at most CAPS staged atoms per
-// slab (128, or 256 for dense footprints such as coarse voxel grids); otherwise
-// it raises counters[4] and the host retries with the larger capacity, then with
-// k_column_fp32, which handles both cases.  The capacity does not change which
+// It needs link cells at least 3 sigma wide in x and y (the reference's grid always
+// makes them so); in z it applies the 27-cell rule itself, slab by slab, so cells
+// shorter than 3 sigma (a z voxel a little smaller than the in-plane one) give the
+// reference's truncated search.  At most CAPS staged atoms per
+// slab (128, then 192 and 256 for dense footprints such as coarse voxel grids);
+// otherwise it raises counters[4] and the host retries with the next capacity, then
+// with k_column_fp32, which handles both cases.  The capacity does not change which
 // candidates are tested or their order: every instance computes the same image.
 #include <cuda_runtime.h>
 
@@ -346,12 +348,23 @@ __device__ __noinline__ bool column_tile(const ColumnParams& p, WarpSmem<CAPS>& 
       const int slot = u & (kRing - 1);
       const float zoff = G.a33s * (float)(u - hz0);  // cell u's origin relative to hz0's
       const float t0 = zv0 - zoff, t1 = zv1 - zoff;
-      const int b_lo = max(0, min(kBins, (int)floorf((t0 - r3) * inv_bin)));
-      const int b_hi = max(0, min(kBins, (int)ceilf((t1 + r3) * inv_bin)));
+      float w_lo = t0, w_hi = t1;
+      // a missing second slice (odd depth) sits far away and accepts nothing
+      float2 tt = make_float2(-t0, has1 ? -t1 : -1e30f);
+      if (p.trunc_z) {
+        // z cells shorter than 3 sigma: the reference searches only the 27 cells around each
+        // voxel's home cell, so slab u serves a slice only within one cell of its home z cell
+        // (with taller cells nothing farther lies within the cutoff)
+        const bool v0 = u - hz0 >= -1 && u - hz0 <= 1;
+        const bool v1 = has1 && u - hz1 >= -1 && u - hz1 <= 1;
+        w_lo = v0 ? t0 : t1;
+        w_hi = v1 ? t1 : t0;
+        tt = make_float2(v0 ? -t0 : -1e30f, v1 ? -t1 : -1e30f);
+      }
+      const int b_lo = max(0, min(kBins, (int)floorf((w_lo - r3) * inv_bin)));
+      const int b_hi = max(0, min(kBins, (int)ceilf((w_hi + r3) * inv_bin)));
       const int lo = W.bin[slot][b_lo];
       const int hi = W.bin[slot][b_hi];
-      // a missing second slice (odd depth) sits far away and accepts nothing
-      const float2 tt = make_float2(-t0, has1 ? -t1 : -1e30f);
       if (kStats) n_tst += (unsigned long long)(hi - lo);
       const float4* P = W.p[slot];
       const float* S = W.s[slot];
@@ -497,15 +510,17 @@ cudaError_t launch(K kernel, const ColumnJob* jobs, int n_jobs, int total_tiles,
 // base = 5 for up to 8 precession angles per pass (96 registers), 4 for 16 (128).  The
 // arithmetic is the same in every variant; the host's autotuner picks by timing.
 constexpr int kVariants = 2;
-inline int base_blocks(int np) { return np <= 8 ? 5 : 4; }
 
 template <int NP, bool kDensity, bool kStats>
-cudaError_t launch_v(int v, bool big, const ColumnJob* jobs, int n_jobs, int total_tiles, unsigned* work,
+cudaError_t launch_v(int v, int tier, const ColumnJob* jobs, int n_jobs, int total_tiles, unsigned* work,
                      const unsigned long long* counters, int64_t cap, cudaStream_t st) {
   constexpr int B = NP <= 8 ? 5 : 4;
-  if (big)  // 256-atom slabs: 84 KB of shared memory per CTA, two CTAs per SM
+  if (tier >= 2)  // 256-atom slabs: 84 KB of shared memory per CTA, two CTAs per SM
     return launch<256>(k_column_fp32_v2<NP, kDensity, kStats, 2, 256>, jobs, n_jobs, total_tiles, work, counters,
                        cap, 2, st);
+  if (tier == 1)  // 192-atom slabs: 63.6 KB per CTA, three CTAs per SM
+    return launch<192>(k_column_fp32_v2<NP, kDensity, kStats, 3, 192>, jobs, n_jobs, total_tiles, work, counters,
+                       cap, 3, st);
   if constexpr (!kStats) {
     if (v == 1)
       return launch<128>(k_column_fp32_v2<NP, kDensity, kStats, B - 1, 128>, jobs, n_jobs, total_tiles, work, counters,
@@ -516,7 +531,7 @@ cudaError_t launch_v(int v, bool big, const ColumnJob* jobs, int n_jobs, int tot
 }
 
 template <bool kDensity, bool kStats>
-cudaError_t launch_np(int np, int v, bool big, const ColumnJob* jobs, int n_jobs, int total_tiles, unsigned* work,
+cudaError_t launch_np(int np, int v, int big, const ColumnJob* jobs, int n_jobs, int total_tiles, unsigned* work,
                       const unsigned long long* counters, int64_t cap, cudaStream_t st) {
   if (np <= 1) return launch_v<1, kDensity, kStats>(v, big, jobs, n_jobs, total_tiles, work, counters, cap, st);
   if (np <= 2) return launch_v<2, kDensity, kStats>(v, big, jobs, n_jobs, total_tiles, work, counters, cap, st);
@@ -538,24 +553,29 @@ int ring_variant_count() { return kVariants; }
 int ring_np_bucket(int max_np) { return max_np <= 1 ? 1 : max_np <= 2 ? 2 : max_np <= 4 ? 4 : max_np <= 8 ? 8 : 16; }
 
 cudaError_t launch_column_fp32_ring(const ColumnJob* d_jobs, int n_jobs, int total_tiles, int max_np, bool density,
-                                    bool stats, int variant, bool big_slabs, bool masked, unsigned* work,
+                                    bool stats, int variant, int slab_tier, bool masked, unsigned* work,
                                     const unsigned long long* counters, int64_t cap, cudaStream_t st) {
   cudaMemsetAsync(work, 0, sizeof(unsigned), st);
   if (total_tiles <= 0) return cudaSuccess;
   if (masked) {  // tile-masked jobs: one precession angle, no statistics (the host sends others elsewhere)
     if (max_np != 1 || stats) return cudaErrorInvalidValue;
-    if (big_slabs)
+    if (slab_tier >= 2)
       return density ? launch<256>(k_column_fp32_v2<1, true, false, 2, 256, true>, d_jobs, n_jobs, total_tiles, work,
                                    counters, cap, 2, st)
                      : launch<256>(k_column_fp32_v2<1, false, false, 2, 256, true>, d_jobs, n_jobs, total_tiles, work,
                                    counters, cap, 2, st);
+    if (slab_tier == 1)
+      return density ? launch<192>(k_column_fp32_v2<1, true, false, 3, 192, true>, d_jobs, n_jobs, total_tiles, work,
+                                   counters, cap, 3, st)
+                     : launch<192>(k_column_fp32_v2<1, false, false, 3, 192, true>, d_jobs, n_jobs, total_tiles, work,
+                                   counters, cap, 3, st);
     return density ? launch<128>(k_column_fp32_v2<1, true, false, 5, 128, true>, d_jobs, n_jobs, total_tiles, work,
                                  counters, cap, 5, st)
                    : launch<128>(k_column_fp32_v2<1, false, false, 5, 128, true>, d_jobs, n_jobs, total_tiles, work,
                                  counters, cap, 5, st);
   }
   const int v = (variant > 0 && variant < kVariants && !stats) ? variant : 0;  // statistics: variant 0
-  const bool b = big_slabs;
+  const int b = slab_tier;
   if (density)
     return stats ? launch_np<true, true>(max_np, v, b, d_jobs, n_jobs, total_tiles, work, counters, cap, st)
                  : launch_np<true, false>(max_np, v, b, d_jobs, n_jobs, total_tiles, work, counters, cap, st);

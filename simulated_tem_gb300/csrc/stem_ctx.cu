@@ -54,10 +54,11 @@ struct st_ctx {
   st_stats stats{};
   int64_t last_kept = 0;       // kept atoms of the previous call: sizes the next one
   bool fp32_general = false;   // STEM_FP32_KERNEL=general: always use k_column_fp32
+  int min_slab_tier = 0;       // STEM_RING_SLABS=192 or 256: start the slab ring at that capacity
   int last_column_kernel = 0;  // 1 general FP32, 2 slab-ring FP32, 3 FP64
   int tune_mode = ST_TUNE_AUTO;
   std::map<int, int> ring_tuned;  // (angles per pass, density) -> fastest slab-ring variant
-  std::map<uint64_t, int> ring_big;  // (pass kind, image and link-cell shape) needing 256-atom slabs
+  std::map<uint64_t, int> ring_big;  // (pass kind, image and link-cell shape) -> slab tier it needs (1, 2)
   cudaEvent_t tev[3] = {nullptr, nullptr, nullptr};
   int last_ring_variant = -1;
   double* d_lvaux = nullptr;  // PNG levels: partial minima/maxima and the level map
@@ -322,6 +323,7 @@ ColumnParams column_params(st_ctx* c, const Job& j, int64_t cell_base, size_t xo
   // link cells narrower than 3 sigma truncate the search to 27 cells: test the cell offsets too
   const double r3 = 3 * g->sigma * (1.0 + 1e-6) + 1e-6;
   cp.check_cells = (cp.a11 < r3 || cp.a22 < r3 || cp.a33 < r3) ? 1 : 0;
+  cp.trunc_z = cp.a33 < r3 ? 1 : 0;
   cp.cell_start = c->b.cell_start + cell_base;
   point_at_kept(c, cp);
   cp.xtab = c->s.xtab + xoff;
@@ -372,9 +374,15 @@ cudaError_t tune_ring(st_ctx* c, F&& launch_variant, int64_t cap, cudaStream_t s
 
 // The slab-ring FP32 kernel needs cells of at least 3 sigma (no truncated
 // search) and at least one voxel thick in z.
+// The slab ring needs link cells of at least 3 sigma in x and y: then every atom within
+// 3 sigma of a column lies in its 9 cells around it in x-y.  The reference's grid makes them
+// so (Dx + 2 deltaM voxels over floor(Dx / deltaM + 2) cells, deltaM = ceil(3 sigma / the
+// smaller in-plane voxel side)); the margin allows rounding only.  In z the kernel applies
+// the 27-cell rule itself, so cells shorter than 3 sigma qualify.
 bool ring_eligible(const ColumnParams& cp, bool stats) {
   if (cp.tile_mask && (cp.n_prec != 1 || stats)) return false;  // masked ring: one angle, no statistics
-  return !cp.check_cells && cp.Ez <= cp.Mz;
+  const double r3 = 3 * cp.sigma * (1.0 - 1e-9);
+  return cp.a11 >= r3 && cp.a22 >= r3 && cp.Ez <= cp.Mz;
 }
 
 // A recorded call (st_plan): the instantiated graph and what its kernels were recorded with.
@@ -609,8 +617,11 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
     }
     return h;
   };
-  bool big = false;
-  for (int pass = 0; pass < passes; ++pass) big = big || c->ring_big.count(big_key(pass)) > 0;
+  int big = c->min_slab_tier;  // slab tier: 128, 192, 256 atoms
+  for (int pass = 0; pass < passes; ++pass) {
+    auto it = c->ring_big.find(big_key(pass));
+    if (it != c->ring_big.end()) big = std::max(big, it->second);
+  }
   bool masked = false;  // tile-masked ring jobs take the masked kernel instances
   for (int r : ring_jobs) masked = masked || cps[r].tile_mask != nullptr;
   // with_bin false: the column phase only, on the binning already in place
@@ -685,15 +696,16 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
       cap = (int64_t)c->h_counters[0] + (int64_t)c->h_counters[0] / 8 + 1024;  // grow and redo
       continue;
     }
-    if (ring_ok && c->h_counters[4] != 0 && !big) {
-      // a slab held more than 128 atoms: the column phase again with 256-atom slabs, and this
-      // context keeps them for these kinds of pass on images of this shape
-      big = true;
-      for (int pass = 0; pass < passes; ++pass) c->ring_big[big_key(pass)] = 1;
+    while (ring_ok && c->h_counters[4] != 0 && big < 2) {
+      // a slab held more atoms than this tier stages: the column phase again with the next
+      // (192, then 256 atoms), and this context keeps it for these kinds of pass on images
+      // of this shape
+      ++big;
+      for (int pass = 0; pass < passes; ++pass) c->ring_big[big_key(pass)] = big;
       cudaMemsetAsync(c->s.counters + 2, 0, 3 * sizeof(unsigned long long), st);
       e = enqueue(false, false);
       if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-      if (e != cudaSuccess) return cuda_fail(c, e, "image kernels (256-atom slabs)");
+      if (e != cudaSuccess) return cuda_fail(c, e, "image kernels (larger slabs)");
     }
     if (ring_ok && c->h_counters[4] != 0) {
       // a slab held more atoms than the ring kernel stages: recompute every image with the general kernel
@@ -748,6 +760,7 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
   S.ms_column = ms;
   S.column_kernel = c->last_column_kernel;
   S.ring_variant = used_ring ? c->last_ring_variant : -1;
+  S.ring_slab_atoms = used_ring && !ring_jobs.empty() ? (big == 0 ? 128 : big == 1 ? 192 : 256) : 0;
   // the reference stops when a link cell needs more than 16 x nMax0 slots; a batch's
   // largest cell is checked against the smallest nMax0 of its images
   int min_nmax0 = 0;
@@ -785,6 +798,8 @@ extern "C" int st_create(st_ctx** out, int device) {
   }
   const char* kv = std::getenv("STEM_FP32_KERNEL");
   c->fp32_general = kv && std::strcmp(kv, "general") == 0;
+  const char* ks = std::getenv("STEM_RING_SLABS");
+  c->min_slab_tier = !ks ? 0 : std::strcmp(ks, "256") == 0 ? 2 : std::strcmp(ks, "192") == 0 ? 1 : 0;
   *out = c;
   return ST_OK;
 }
@@ -1034,6 +1049,7 @@ void plan_sum_stats(st_plan* p) {
     t.ms_column += S.ms_column;
     t.column_kernel = std::max(t.column_kernel, S.column_kernel);
     t.ring_variant = std::max(t.ring_variant, S.ring_variant);
+    t.ring_slab_atoms = std::max(t.ring_slab_atoms, S.ring_slab_atoms);
   }
   p->stats = t;
 }

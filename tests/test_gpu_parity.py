@@ -6,6 +6,8 @@ path max |dI| <= 1e-4 (the precision target of the FP32 + FP64-phase path);
 binning counts and accepted-pair counts identical; the blur identical to the
 last bit.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -262,3 +264,76 @@ def test_fp32_ring_big_slabs(ctx):
         c.close()
     want, _ = oracle_patch(so, x, 1, 0.005)
     assert np.abs(got - want).max() <= FP32_TOL
+
+
+def _context_with(env):
+    old = {k: os.environ.get(k) for k in env}
+    os.environ.update(env)
+    try:
+        return imaging.Context(0)
+    finally:
+        for k, v in old.items():
+            if v is None:
+                del os.environ[k]
+            else:
+                os.environ[k] = v
+
+
+def test_fp32_ring_slab_capacities_agree(ctx):
+    """The slab ring's staging capacity (128, 192, 256 atoms) changes neither which
+    candidates are tested nor their order: the three give the same image bit for bit;
+    two copies of every atom need the 192-atom tier or more."""
+    cell = synth.small_cell(**CELLS["screw+void"])
+    t, so, x = setup_both(cell, sg=0.01)
+    G, aa = t.image_geometry(len(x), n_prec=2)
+    imgs = {}
+    for slabs in ("128", "192", "256"):
+        c = _context_with({"STEM_RING_SLABS": slabs})
+        try:
+            imgs[slabs] = c.image(G, x, aa, flags=_lib.ST_FLAG_FP32)
+            assert c.stats().column_kernel == 2 and c.stats().ring_slab_atoms == int(slabs)
+        finally:
+            c.close()
+    assert np.array_equal(imgs["128"], imgs["192"]) and np.array_equal(imgs["128"], imgs["256"])
+    dense = synth.Cell(cell.a_super, np.concatenate([cell.pos] * 2))
+    t2, so2, x2 = setup_both(dense, sg=0.01)
+    G2, aa2 = t2.image_geometry(len(x2))
+    c = imaging.Context(0)
+    try:
+        got = c.image(G2, x2, aa2, flags=_lib.ST_FLAG_FP32)
+        assert c.stats().column_kernel == 2 and c.stats().ring_slab_atoms in (192, 256)
+    finally:
+        c.close()
+    want, _ = oracle_patch(so2, x2, 1, 0.005)
+    assert np.abs(got - want).max() <= FP32_TOL
+
+
+@pytest.mark.parametrize("short", [0.9999997, 0.8, 0.55])
+def test_fp32_ring_truncated_z_search(ctx, short):
+    """z link cells shorter than 3 sigma (a z voxel smaller than the in-plane one: deltaM
+    comes from the in-plane side, Lib_DynamicalTwoBeamImaging.f90:1753-1773): the reference
+    searches only the 27 cells around each voxel's home cell.  The slab ring applies that
+    rule slab by slab; it agrees with the general FP32 kernel (which tests cell offsets) and
+    with the FP64 path, which follows the reference's 27-cell search."""
+    cell = synth.small_cell(**CELLS["screw+void"])
+    t, so, x = setup_both(cell, sg=0.01)
+    G, aa = t.image_geometry(len(x))
+    # z voxels `short` x the cell height 3 sigma / 6: six voxels per z cell
+    G.Ez = max(3, G.Ez)
+    G.Mz = 6 * G.Ez
+    G.a_vox[8] = short * G.sigma / 2
+    G.a_col[8] = G.Mz * G.a_vox[8] / G.Ez
+    G.ia_col[8] = 1 / G.a_col[8]
+    G.deltaz = G.a_vox[8]
+    assert G.a_col[8] < 3 * G.sigma
+    ring = ctx.image(G, x, aa, flags=_lib.ST_FLAG_FP32)
+    assert ctx.stats().column_kernel == 2
+    gctx = _general_fp32_context()
+    try:
+        gen = gctx.image(G, x, aa, flags=_lib.ST_FLAG_FP32)
+        assert gctx.stats().column_kernel == 1
+    finally:
+        gctx.close()
+    f64 = ctx.image(G, x, aa, flags=0)
+    assert np.abs(ring - gen).max() <= 2e-5
+    assert np.abs(ring - f64).max() <= FP32_TOL
