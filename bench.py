@@ -550,10 +550,11 @@ def tilt_leg(ctx, cell, steps, warmup, cpu=True):
     out = {"workload": "testD2BI -ng 1 search: 27,847 W atoms, k [001], g [200], %d directions x %d reflections"
                        % (info["nk"], info["nn"]),
            "setup_ms": float(np.median(walls)) * 1e3, "scan_ms": scan, "pairs_per_s": pairs / (scan * 1e-3),
+           "screen_ms": info["screen_ms"], "n_fp64": info["n_fp64"],
            "n_recheck": info["n_recheck"], "ii_best": info["ii_best"], "RU": (R @ U).tolist(),
-           "note": "setup: st_d2bi_set_supercell_tilt1a end to end (reflections, table, directions, GPU scores, "
-                   "exact near-tie re-scoring, dark-field golden section, quaternion round trip); scan: the "
-                   "scoring launch alone"}
+           "note": "setup: st_d2bi_set_supercell_tilt1a end to end (reflections, table, directions, FP32 screen "
+                   "of every direction, FP64 scores of the n_fp64 it leaves open, exact near-tie re-scoring, "
+                   "dark-field golden section, quaternion round trip); scan: the two scoring launches"}
     if cpu:
         from oracle import stem_oracle as O
         args = O.make_args(a_super, 3.1652, (0, 0, 1), (2, 0, 0), V=200.0, M=(4, 4), ng=1.0, xifile=xifile)

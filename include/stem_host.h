@@ -88,10 +88,12 @@ int st_atom_extents_device(st_ctx* ctx, int32_t n_cond, const double* k, const d
 /* ---- the -ng tilt search: setSupercellTilt1a / setSupercellTilt1
  * (Lib_DynamicalTwoBeamImaging.f90:795-1045), findBestRotationMatrix and tiltToDarkField
  * (Lib_DiffractionConditions.f90:129-357, 751-927).  The scores of every candidate beam
- * direction against every permitted reflection are computed on the GPU; the host takes
- * the best, re-scoring in the reference's own arithmetic every candidate whose score
- * lies within the GPU scores' error bound of the best, so that the chosen direction is
- * the one the reference's arithmetic chooses. */
+ * direction against every permitted reflection are computed on the GPU: an FP32 screen of
+ * every direction with a bound on its error, then the reference's FP64 arithmetic for the
+ * directions that can be within that bound of the best; the host takes the best,
+ * re-scoring in the reference's own arithmetic every candidate within the FP64 scores'
+ * error bound of it, so that the chosen direction is the one the reference's arithmetic
+ * chooses. */
 
 /* Lattice types (Lib_Lattices.f90:65-69) and table symmetries (Lib_ReadExtinctionDistances.f90:20-22) */
 #define ST_LATTICE_SC 1
@@ -114,8 +116,11 @@ typedef struct {
   double foil;         /* foil thickness used (A) */
   double foil_sigma;   /* spread of the column thickness with atoms given (A) */
   double dark_theta;   /* tiltToDarkField's tilt about y (rad) */
-  double scan_ms;      /* GPU time of the scoring launch (CUDA events on the context's stream) */
+  double scan_ms;      /* GPU time of the scoring launches, screen and FP64 (CUDA events) */
   double foil_ms;      /* GPU time of the foil-thickness pass (with atoms given) */
+  int32_t n_fp64;      /* directions scored in FP64 after the FP32 screen */
+  int32_t pad0;
+  double screen_ms;    /* GPU time of the FP32 screen alone */
 } st_tilt_info;
 
 /* type(Lattice) of the imaging object (the d2bi -lattice option; default bcc) */
@@ -136,6 +141,10 @@ int st_find_best_rotation(st_ctx* ctx, double v, const double* z0, const double*
  * [hkl] slots) and xi_g[0] is the xi_0 of every term. */
 int st_tilt_scores(st_ctx* ctx, double v, const double* khat, int32_t nk, const double* ghkl, const double* xi_g,
                    int32_t nn, double foil, double* scores);
+/* The FP32 screen of the same scores: scores[nk] and bounds[nk] with |scores - the FP64
+ * scores| <= bounds (the search scores in FP64 only the directions this leaves open). */
+int st_tilt_screen(st_ctx* ctx, double v, const double* khat, int32_t nk, const double* ghkl, const double* xi_g,
+                   int32_t nn, double foil, double* scores, double* bounds);
 /* tiltToDarkField(v, A_cell, hkl, xi0, xig, foil_thickness, U, R): R updated in place;
  * theta (may be NULL) receives the tilt about y. */
 int st_tilt_to_dark_field(double v, const double* a_cell, const int32_t* hkl, double xi0, double xig, double foil,

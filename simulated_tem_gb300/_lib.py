@@ -82,7 +82,8 @@ class StTiltInfo(ctypes.Structure):
     """st_tilt_info of include/stem_host.h (what a -ng tilt search did)."""
     _fields_ = [("nk", _i32), ("nn", _i32), ("ii_best", _i32), ("attempt", _i32), ("xi_status", _i32),
                 ("n_recheck", _i32), ("ss_best", _d), ("theta", _d), ("phi", _d), ("foil", _d),
-                ("foil_sigma", _d), ("dark_theta", _d), ("scan_ms", _d), ("foil_ms", _d)]
+                ("foil_sigma", _d), ("dark_theta", _d), ("scan_ms", _d), ("foil_ms", _d), ("n_fp64", _i32),
+                ("pad0", _i32), ("screen_ms", _d)]
 
 
 ST_LATTICES = {"sc": 1, "bcc": 2, "fcc": 3, "hcp": 4}
@@ -168,6 +169,7 @@ _PROTOS = {
     "st_find_best_rotation": (_i32, [_vp, _d, _dp, _dp, _i32, ctypes.POINTER(_i32), ctypes.c_char_p, _d, _d, _d,
                                      _dp, _dp, ctypes.POINTER(StTiltInfo)]),
     "st_tilt_scores": (_i32, [_vp, _d, _dp, _i32, _dp, _dp, _i32, _d, _dp]),
+    "st_tilt_screen": (_i32, [_vp, _d, _dp, _i32, _dp, _dp, _i32, _d, _dp, _dp]),
     "st_tilt_to_dark_field": (_i32, [_d, _dp, ctypes.POINTER(_i32), _d, _d, _d, _d, _dp, _dp, _dp]),
     "st_read_extinction_distances": (_i32, [ctypes.c_char_p, _i32, ctypes.POINTER(_i32), _i32, _dp,
                                             ctypes.POINTER(_i32)]),

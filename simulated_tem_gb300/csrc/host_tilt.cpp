@@ -345,6 +345,65 @@ int gpu_scores(st_ctx* ctx, double v, const double* khat, int nk, const double* 
   return ST_OK;
 }
 
+// The FP32 screen of every direction: scores and bounds on their errors (summed over the
+// slices in FP64; the warp's FP32 sum of a slice adds a few ulps of it).
+int gpu_screen(st_ctx* ctx, double v, const double* khat, int nk, const double* ghkl, const double* xi_g, int nn,
+               double foil, std::vector<double>& s32, std::vector<double>& b32, double* ms) {
+  const cudaStream_t st = stem::ctx_stream(ctx, nullptr);
+  // FP32 copies of the inputs (the conversions would otherwise run on the FP64 pipe per term)
+  const size_t n_khat = 3 * (size_t)nk, n_g = 3 * (size_t)nn;
+  std::vector<float> in(n_khat + n_g + (size_t)nn);
+  for (size_t i = 0; i < n_khat; ++i) in[i] = (float)khat[i];
+  for (size_t i = 0; i < n_g; ++i) in[n_khat + i] = (float)ghkl[i];
+  for (int j = 0; j < nn; ++j) in[n_khat + n_g + j] = (float)(kPi / xi_g[j]);
+  const int ns = stem::tilt_slices(nn);
+  const size_t n_part = (size_t)nk * ns;  // float pairs: n_part doubles of room
+  double* d = nullptr;
+  cudaError_t e = stem::ctx_tilt_scratch(ctx, (in.size() + 1) / 2 + n_part + 1, &d);
+  if (e != cudaSuccess) return stem::ctx_cuda_fail(ctx, e, "tilt scratch");
+  float* d_khat = reinterpret_cast<float*>(d);
+  float *d_g = d_khat + n_khat, *d_bg = d_g + n_g;
+  float* d_p = reinterpret_cast<float*>(d + (in.size() + 1) / 2 + 1);
+  stem::TiltScores p;
+  p.cst = 2 * kMe * v / kHbar;
+  p.hbar2on2m = kHbar * kHbar / (2 * kMe);
+  p.den = 2 * kPi * kHbar * v;
+  p.twopi = 2 * kPi;
+  p.b0 = kPi / xi_g[0];
+  p.foil = foil;
+  p.nk = nk;
+  p.nn = nn;
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  e = cudaEventCreate(&ev[0]);
+  if (e == cudaSuccess) e = cudaEventCreate(&ev[1]);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_khat, in.data(), in.size() * sizeof(float), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaEventRecord(ev[0], st);
+  if (e == cudaSuccess) e = stem::launch_tilt_screen(p, d_khat, d_g, d_bg, d_p, st);
+  if (e == cudaSuccess) e = cudaEventRecord(ev[1], st);
+  std::vector<float> part(2 * n_part);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(part.data(), d_p, 2 * n_part * sizeof(float), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  float t = 0.0f;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&t, ev[0], ev[1]);
+  for (cudaEvent_t x : ev)
+    if (x) cudaEventDestroy(x);
+  if (e != cudaSuccess) return stem::ctx_cuda_fail(ctx, e, "tilt screen");
+  s32.assign((size_t)nk, 0.0);
+  b32.assign((size_t)nk, 0.0);
+  for (int i = 0; i < nk; ++i) {
+    double s = 0.0, b = 0.0;
+    for (int k = 0; k < ns; ++k) {
+      s += part[2 * ((size_t)i * ns + k)];
+      b += part[2 * ((size_t)i * ns + k) + 1];
+    }
+    s32[i] = s;
+    b32[i] = b + 4.0e-6 * std::fabs(s) + 1e-12;
+  }
+  if (ms) *ms = t;
+  return ST_OK;
+}
+
 // The reference's argmin (first strictly smaller score) from the GPU scores: every
 // candidate whose score can lie within the scores' error bound of the best is re-scored
 // in the reference's arithmetic.  The bound per score: 4e-15 per term for the sine and
@@ -633,14 +692,33 @@ int best_rotation(st_ctx* ctx, double v, const double* z0, const Mat3& A_cell, i
     }
   }
   if (nk == 0) return stem::ctx_fail(ctx, ST_ERR_ARG, "tilt search: no tilt meets the Bragg condition");
-  std::vector<double> scores((size_t)nk);
-  double ms = 0.0;
-  int rc = gpu_scores(ctx, v, khat.data(), nk, ghkl.data(), xi_g.data(), nn, foil, scores.data(), &ms);
+  // FP32 screen of every direction, then the reference's FP64 arithmetic on the directions
+  // whose screened score can be within its error bound of the best
+  std::vector<double> s32, b32;
+  double ms_screen = 0.0, ms = 0.0;
+  int rc = gpu_screen(ctx, v, khat.data(), nk, ghkl.data(), xi_g.data(), nn, foil, s32, b32, &ms_screen);
+  if (rc != ST_OK) return rc;
+  double lim = kHuge1;
+  for (int i = 0; i < nk; ++i) lim = std::min(lim, s32[i] + b32[i]);
+  std::vector<int> cand;
+  for (int i = 0; i < nk; ++i)
+    if (s32[i] - b32[i] <= lim) cand.push_back(i);
+  if (cand.empty() || cand.size() * 4 > (size_t)nk) {  // a flat landscape: score every direction in FP64
+    cand.resize((size_t)nk);
+    for (int i = 0; i < nk; ++i) cand[i] = i;
+  }
+  const int nc = (int)cand.size();
+  std::vector<double> kc(3 * (size_t)nc);
+  for (int c = 0; c < nc; ++c)
+    for (int d = 0; d < 3; ++d) kc[3 * (size_t)c + d] = khat[3 * (size_t)cand[c] + d];
+  std::vector<double> scores((size_t)nc);
+  rc = gpu_scores(ctx, v, kc.data(), nc, ghkl.data(), xi_g.data(), nn, foil, scores.data(), &ms);
   if (rc != ST_OK) return rc;
   double ss_best;
   int n_recheck;
-  const int ib = choose_best(khat.data(), nk, scores.data(), ghkl, xi_g, v, foil, &ss_best, &n_recheck);
-  if (ib < 0) return stem::ctx_fail(ctx, ST_ERR_ARG, "tilt search: no finite score");
+  const int icb = choose_best(kc.data(), nc, scores.data(), ghkl, xi_g, v, foil, &ss_best, &n_recheck);
+  if (icb < 0) return stem::ctx_fail(ctx, ST_ERR_ARG, "tilt search: no finite score");
+  const int ib = cand[icb];
   const double* kb = &khat[3 * (size_t)ib];
   const double phi = -std::asin(kb[0]);
   const double theta = std::acos(kb[2] / std::cos(phi));
@@ -662,7 +740,9 @@ int best_rotation(st_ctx* ctx, double v, const double* z0, const Mat3& A_cell, i
     info->ss_best = ss_best;
     info->theta = theta;
     info->phi = phi;
-    info->scan_ms = ms;
+    info->scan_ms = ms_screen + ms;
+    info->screen_ms = ms_screen;
+    info->n_fp64 = nc;
   }
   return ST_OK;
 }
@@ -828,6 +908,19 @@ int st_tilt_scores(st_ctx* ctx, double v, const double* khat, int32_t nk, const 
   if (!khat || !ghkl || !xi_g || !scores || nk < 1 || nn < 2)
     return stem::ctx_fail(ctx, ST_ERR_ARG, "invalid tilt score arguments");
   return gpu_scores(ctx, v, khat, nk, ghkl, xi_g, nn, foil, scores, nullptr);
+}
+
+int st_tilt_screen(st_ctx* ctx, double v, const double* khat, int32_t nk, const double* ghkl, const double* xi_g,
+                   int32_t nn, double foil, double* scores, double* bounds) {
+  if (!ctx) return ST_ERR_ARG;
+  if (!khat || !ghkl || !xi_g || !scores || !bounds || nk < 1 || nn < 2)
+    return stem::ctx_fail(ctx, ST_ERR_ARG, "invalid tilt screen arguments");
+  std::vector<double> s32, b32;
+  const int rc = gpu_screen(ctx, v, khat, nk, ghkl, xi_g, nn, foil, s32, b32, nullptr);
+  if (rc != ST_OK) return rc;
+  std::copy(s32.begin(), s32.end(), scores);
+  std::copy(b32.begin(), b32.end(), bounds);
+  return ST_OK;
 }
 
 int st_tilt_to_dark_field(double v, const double* a_cell, const int32_t* hkl, double xi0, double xig, double foil,

@@ -208,6 +208,10 @@ int tilt_slices(int nn);         // slices per incident vector: the partial sums
 // d_part: nk * tilt_slices(nn) partial sums, vector-major
 cudaError_t launch_tilt_scores(const TiltScores& p, const double* d_khat, const double* d_ghkl, const double* d_bg,
                                double* d_part, cudaStream_t st);
+// the FP32 screen on FP32 copies of the inputs: d_part2 holds nk * tilt_slices(nn) pairs
+// (partial score, bound on its error)
+cudaError_t launch_tilt_screen(const TiltScores& p, const float* d_khat, const float* d_ghkl, const float* d_bg,
+                               float* d_part2, cudaStream_t st);
 // findFoilThickness's column grid: the atoms' highest and lowest z per column over the
 // replicas, as order keys (order_key_value turns one back into its double).
 struct FoilGrid {

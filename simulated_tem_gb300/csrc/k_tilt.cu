@@ -66,6 +66,57 @@ __global__ void __launch_bounds__(256) k_tilt_scores(TiltScores p, const double*
   }
 }
 
+// The FP32 screen of the same scores, with a bound on each screened score's error.  Per
+// term the phases lambda L carry the FP32 rounding of the energy deviation (a difference
+// of terms up to cst |g| and |g|^2) and of the phase products; a phase error e moves the
+// term by at most 3 e (bg / dd)^2, and the term's own rounding adds a few ulps of it.
+// part2 holds (partial score, partial error bound) per task.
+__global__ void __launch_bounds__(256) k_tilt_screen(TiltScores p, const float* __restrict__ khat,
+                                                     const float* __restrict__ ghkl, const float* __restrict__ bg,
+                                                     float* __restrict__ part2) {
+  const int lane = threadIdx.x & 31;
+  const int n_slices = (p.nn - 2 + kTiltSlice - 1) / kTiltSlice;
+  const int64_t tasks = (int64_t)p.nk * n_slices;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  const float cst = (float)p.cst, h2 = (float)p.hbar2on2m, den = (float)p.den, twopi = (float)p.twopi;
+  const float b0 = (float)p.b0, L = (float)p.foil;
+  const float u = 1.1920929e-07f;  // 2^-23
+  const float k_eps = L * 3.1415927f * (h2 / den) * 16.f * u;  // phase error per unit of |cst k.g| + |g|^2
+  for (int64_t t = (int64_t)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); t < tasks; t += warps) {
+    const int w = (int)(t / n_slices), sl = (int)(t % n_slices);
+    const float k0 = khat[3 * w], k1 = khat[3 * w + 1], k2 = khat[3 * w + 2];
+    const int j1 = min(p.nn, 2 + (sl + 1) * kTiltSlice);
+    float s = 0.f, err = 0.f;
+    for (int j = 2 + sl * kTiltSlice + lane; j < j1; j += 32) {
+      const float g0 = ghkl[3 * j], g1 = ghkl[3 * j + 1], g2 = ghkl[3 * j + 2];
+      const float kg = cst * (k0 * g0 + k1 * g1 + k2 * g2), gg = g0 * g0 + g1 * g1 + g2 * g2;
+      const float aa = twopi * (-((kg + gg) * h2) / den);
+      const float b = bg[j];
+      const float dd = sqrtf(aa * aa * 0.25f + b * b);
+      const float c = b0 + aa * 0.5f;
+      const float ph1 = (c + dd) * L, ph2 = (c - dd) * L;
+      float s1, c1, s2, c2;
+      sincosf(ph1, &s1, &c1);
+      sincosf(ph2, &s2, &c2);
+      const float f = b / (2.f * dd);
+      const float re = (c1 - c2) * f, im = (s1 - s2) * f;
+      const float term = re * re + im * im;
+      s += term;
+      const float e = 8.f * u * (fabsf(ph1) + fabsf(ph2) + 1.f) + k_eps * (fabsf(kg) + gg);
+      err += 3.f * e * (4.f * f * f) + 16.f * u * term;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      s += __shfl_down_sync(0xffffffffu, s, o);
+      err += __shfl_down_sync(0xffffffffu, err, o);
+    }
+    if (lane == 0) {
+      part2[2 * t] = s;
+      part2[2 * t + 1] = err;
+    }
+  }
+}
+
 // order-preserving key of a double (no NaNs on this path)
 __device__ __forceinline__ unsigned long long order_key(double v) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(v);
@@ -175,6 +226,16 @@ cudaError_t launch_tilt_scores(const TiltScores& p, const double* d_khat, const 
   const int64_t want = (tasks + 7) / 8;
   const int blocks = (int)(want < 5 * 152 ? want : 5 * 152);
   k_tilt_scores<<<blocks, 256, 0, st>>>(p, d_khat, d_ghkl, d_bg, d_part);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tilt_screen(const TiltScores& p, const float* d_khat, const float* d_ghkl, const float* d_bg,
+                               float* d_part2, cudaStream_t st) {
+  const int64_t tasks = (int64_t)p.nk * tilt_slices(p.nn);
+  if (tasks <= 0) return cudaSuccess;
+  const int64_t want = (tasks + 7) / 8;
+  const int blocks = (int)(want < 8 * 152 ? want : 8 * 152);
+  k_tilt_screen<<<blocks, 256, 0, st>>>(p, d_khat, d_ghkl, d_bg, d_part2);
   return cudaGetLastError();
 }
 

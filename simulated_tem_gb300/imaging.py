@@ -543,6 +543,17 @@ def tilt_scores(ctx, v, khat, ghkl, xi_g, foil):
     return out
 
 
+def tilt_screen(ctx, v, khat, ghkl, xi_g, foil):
+    """The FP32 screen of tilt_scores: (scores, bounds on their errors)."""
+    khat = np.ascontiguousarray(khat, dtype=np.float64)
+    ghkl = np.ascontiguousarray(ghkl, dtype=np.float64)
+    xi_g = np.ascontiguousarray(xi_g, dtype=np.float64)
+    s, b = np.zeros(len(khat)), np.zeros(len(khat))
+    ctx._check(lib().st_tilt_screen(ctx.handle, float(v), _ptr(khat), len(khat), _ptr(ghkl), _ptr(xi_g), len(ghkl),
+                                    float(foil), _ptr(s), _ptr(b)))
+    return s, b
+
+
 def d2bi_condition(a_super, a0, k, g, x, V=200.0, M=(4, 4), sg=None, R=None, U=None, d=None, xi0=103.889565,
                    xig=207.533203, density=False, n_tomo=1, tomo_angle=20.0, tomo_step=0, ng=None, xifile=None,
                    lattice="bcc", surf=False, theta_max=5.0, rho_max=10.0, ctx=None):

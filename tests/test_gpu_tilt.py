@@ -54,6 +54,21 @@ def test_scores_match_oracle(ctx):
     assert int(np.argmin(gpu)) == info.ii_best - 1
 
 
+@pytest.mark.parametrize("z0,hkl,foil", [((0, 0, 1), (2, 0, 0), FOIL), ((0, 0, 1), (1, 1, 0), 400.0),
+                                         ((1, 1, 1), (1, -1, 0), 60.0), ((0, 0, 1), (4, 0, 0), 1200.0)])
+def test_screen_bounds_hold(ctx, z0, hkl, foil):
+    """The FP32 screen's bound covers its distance from the FP64 score for every direction,
+    and the bound is tight enough to leave few directions to the FP64 pass."""
+    v = _velocity()
+    a_cell = 3.1652 * np.eye(3)
+    _, _, info, scores, khat = O.find_best_rotation(v, z0, a_cell, "bcc", hkl, XI, foil)
+    g, xi = O.tilt_reflections("bcc", a_cell, hkl, XI)
+    s32, b32 = imaging.tilt_screen(ctx, v, khat, g, xi, foil)
+    assert np.all(np.abs(s32 - scores) <= b32)
+    lim = np.min(s32 + b32)
+    assert int(np.sum(s32 - b32 <= lim)) <= len(khat) // 4
+
+
 def test_best_rotation_equals_oracle(ctx):
     v = _velocity()
     a_cell = 3.1652 * np.eye(3)
@@ -65,7 +80,8 @@ def test_best_rotation_equals_oracle(ctx):
         assert (info["nk"], info["nn"], info["ii_best"], info["attempt"]) == (io.nk, io.nn, io.ii_best, io.attempt)
         assert info["ss_best"] == io.ss_best
         assert 1 <= info["n_recheck"] <= 64
-        assert info["scan_ms"] > 0
+        assert 1 <= info["n_fp64"] < info["nk"] // 4
+        assert info["scan_ms"] > 0 and 0 < info["screen_ms"] <= info["scan_ms"]
 
 
 def _product_ng(ctx, cell, a0, k, g, ng, **kw):
