@@ -328,6 +328,11 @@ def cfg5_leg(ctx, stream, flush, steps, warmup, weights=CORRECTOR_WEIGHTS):
 
     ms_fine = timed(fine_step)
     ms_corr = timed(corrected_step)
+    stages = {}  # per-stage GPU time of the same call, untimed passes after the timed ones
+    for i in range(steps):
+        flush.fill_(float(i))
+        imager.image(t2, t8, d_x, len(x), sg, stream=sp, times=stages)
+    stages = {k: v / steps for k, v in stages.items()}
     ref = fine.cpu().numpy()
     got = res["img"].cpu().numpy()
     # the M = 2 image alone, interpolated (the method without the corrector)
@@ -346,7 +351,8 @@ def cfg5_leg(ctx, stream, flush, steps, warmup, weights=CORRECTOR_WEIGHTS):
                                       "fallback_tiles": res["nflag"], "tiles": res["ntiles"],
                                       "fallback_fraction": res["nflag"] / res["ntiles"], "tau": tau,
                                       "max_abs_dI_vs_m8": float(np.abs(d_c).max()),
-                                      "rms_dI_vs_m8": float(np.sqrt((d_c ** 2).mean()))},
+                                      "rms_dI_vs_m8": float(np.sqrt((d_c ** 2).mean())),
+                                      "stages_ms": stages},
             "m2_corrector_no_fallback": {"max_abs_dI_vs_m8": float(np.abs(d_n).max()),
                                          "rms_dI_vs_m8": float(np.sqrt((d_n ** 2).mean()))},
             "m2_interpolated": {"max_abs_dI_vs_m8": float(np.abs(d_u).max()),

@@ -103,8 +103,14 @@ int stn_apply_correction(const float* base, const float* pred, int32_t Cp, int32
 int stn_tile_maxabs(const float* pred, int32_t Cp, int32_t ch, int32_t Mx8, int32_t My8, int32_t Wp, int32_t T,
                     float* tile_max, void* stream);
 
-/* out = fine on every T x T tile whose flag (int32 [ceil(My/T)][ntx]) is nonzero. */
-int stn_merge_tiles(const double* fine, const int32_t* flags, int32_t ntx, int32_t T, int32_t Mx, int32_t My,
+/* The fallback's tile mask, on the device: mask (uint8 [nty][ntx]) = tile_max > thresh, or
+ * the tile on the grid's outer ring when border != 0; *count (device int32) = the flagged
+ * tiles.  The mask feeds st_image_device_masked and stn_merge_tiles directly. */
+int stn_tile_flags(const float* tile_max, int32_t ntx, int32_t nty, float thresh, int32_t border, uint8_t* mask,
+                   int32_t* count, void* stream);
+
+/* out = fine on every T x T tile whose mask byte (uint8 [ceil(My/T)][ntx]) is nonzero. */
+int stn_merge_tiles(const double* fine, const uint8_t* mask, int32_t ntx, int32_t T, int32_t Mx, int32_t My,
                     double* out, void* stream);
 
 /* First failure recorded by a corrector kernel since the last call (0 = none; 1 = a

@@ -372,45 +372,69 @@ class CorrectedImager:
     def __init__(self, model, ctx, tile=16, tau=0.05):
         self.model, self.ctx, self.T, self.tau = model, ctx, tile, tau
 
-    def image(self, t2, t8, x_dev, n_atoms, sg, fallback=True, stream=0, diag=None):
+    def image(self, t2, t8, x_dev, n_atoms, sg, fallback=True, stream=0, diag=None, times=None):
         """Returns (FP64 device image (My8, Mx8), number of fallback tiles, tile count).  A
         dict `diag` receives the tile maxima of the predicted error magnitude (intensity
-        units, host); tiles above tau are recomputed by the plain M = 8 solve."""
+        units, host); tiles above tau are recomputed by the plain M = 8 solve.  The tile
+        mask is made on the device, so nothing waits on the host between the network and
+        the fine solve; the count is read once all of it is queued.  A dict `times`
+        receives the GPU milliseconds of each stage (CUDA events on the current stream)."""
         import torch
 
         from . import _lib
+        ev = []
+
+        def mark():
+            if times is not None:
+                e = torch.cuda.Event(enable_timing=True)
+                e.record()
+                ev.append(e)
+
         G2, aa2 = t2.image_geometry(n_atoms)
         G8, aa8 = t8.image_geometry(n_atoms)
         dev = x_dev.device
+        mark()
         img2 = torch.empty((G2.My, G2.Mx), dtype=torch.float64, device=dev)
         self.ctx.image_device(G2, x_dev.data_ptr(), n_atoms, aa2, _lib.ST_FLAG_FP32, img2.data_ptr(), stream=stream)
+        mark()
         planes = coarse_planes(img2, G2, G8, sg)
         Hp, Wp = planes.shape[1:]
         out = self.model.forward(N.pack(planes[:N_IN].view(N_IN, 1, Hp, Wp), IN_C))
         img = torch.empty((G8.My, G8.Mx), dtype=torch.float64, device=dev)
         N.apply_correction(planes[4], out[0], G8.Mx, G8.My, 1.0 / RES_SCALE, img)
+        mark()
         T = self.T
         ntx, nty = (G8.Mx + T - 1) // T, (G8.My + T - 1) // T
         if not fallback and diag is None:
+            self._times(times, ev, ["m2_solve", "network"])
             return img, 0, ntx * nty
         tmax = torch.empty((nty, ntx), dtype=torch.float32, device=dev)
         N.tile_maxabs(out[0], G8.Mx, G8.My, T, tmax, ch=1)  # the predicted error magnitude
-        tm = tmax.cpu().numpy()
         if diag is not None:
-            diag["tile_max"] = tm / RES_SCALE
+            diag["tile_max"] = tmax.cpu().numpy() / RES_SCALE
         if not fallback:
+            self._times(times, ev, ["m2_solve", "network"])
             return img, 0, ntx * nty
-        flags = (tm > self.tau * RES_SCALE).astype(np.int32)
-        flags[0, :] = flags[-1, :] = 1  # the image's border: the coarse image is clamped there
-        flags[:, 0] = flags[:, -1] = 1
-        nflag = int(flags.sum())
-        if nflag:
-            mask = torch.from_numpy(flags.astype(np.uint8)).to(dev)
-            fine = torch.empty((G8.My, G8.Mx), dtype=torch.float64, device=dev)
-            self.ctx.image_device_masked(G8, x_dev.data_ptr(), n_atoms, aa8, _lib.ST_FLAG_FP32, fine.data_ptr(),
-                                         mask.data_ptr(), T, stream=stream)
-            N.merge_tiles(fine, torch.from_numpy(flags).to(dev), T, G8.Mx, G8.My, img)
+        # every tile above tau, and the image's border, where the coarse image is clamped
+        mask = torch.empty((nty, ntx), dtype=torch.uint8, device=dev)
+        count = torch.empty((), dtype=torch.int32, device=dev)
+        N.tile_flags(tmax, self.tau * RES_SCALE, mask, count, border=True)
+        fine = torch.empty((G8.My, G8.Mx), dtype=torch.float64, device=dev)
+        self.ctx.image_device_masked(G8, x_dev.data_ptr(), n_atoms, aa8, _lib.ST_FLAG_FP32, fine.data_ptr(),
+                                     mask.data_ptr(), T, stream=stream)
+        N.merge_tiles(fine, mask, T, G8.Mx, G8.My, img)
+        mark()
+        nflag = int(count.item())
+        self._times(times, ev, ["m2_solve", "network", "fallback"])
         return img, nflag, ntx * nty
+
+    @staticmethod
+    def _times(times, ev, names):
+        if times is None:
+            return
+        ev[-1].synchronize()
+        for name, a, b in zip(names, ev[:-1], ev[1:]):
+            times[name] = times.get(name, 0.0) + a.elapsed_time(b)
 
 
 

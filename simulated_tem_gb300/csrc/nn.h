@@ -58,7 +58,10 @@ int resample_planes(const double* img2, int Mx2, int My2, int Mx8, int My8, int 
 int apply_correction(const float* base, const float* pred, int Cp, int Mx8, int My8, int Wp, float scale, double* out,
                      cudaStream_t st);
 int tile_maxabs(const float* pred, int Cp, int ch, int Mx8, int My8, int Wp, int T, float* tile_max, cudaStream_t st);
-int merge_tiles(const double* fine, const int* flags, int ntx, int T, int Mx, int My, double* out, cudaStream_t st);
+int tile_flags(const float* tile_max, int ntx, int nty, float thresh, int border, unsigned char* mask, int* count,
+               cudaStream_t st);
+int merge_tiles(const double* fine, const unsigned char* mask, int ntx, int T, int Mx, int My, double* out,
+                cudaStream_t st);
 
 // First failure recorded by a corrector kernel (0 = none), then cleared; synchronises.
 int take_error();

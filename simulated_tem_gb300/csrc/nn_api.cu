@@ -97,8 +97,12 @@ extern "C" int stn_tile_maxabs(const float* pred, int32_t Cp, int32_t ch, int32_
                                int32_t T, float* tile_max, void* stream) {
   return tile_maxabs(pred, Cp, ch, Mx8, My8, Wp, T, tile_max, cs(stream));
 }
-extern "C" int stn_merge_tiles(const double* fine, const int32_t* flags, int32_t ntx, int32_t T, int32_t Mx,
+extern "C" int stn_tile_flags(const float* tile_max, int32_t ntx, int32_t nty, float thresh, int32_t border,
+                              uint8_t* mask, int32_t* count, void* stream) {
+  return tile_flags(tile_max, ntx, nty, thresh, border, mask, count, cs(stream));
+}
+extern "C" int stn_merge_tiles(const double* fine, const uint8_t* mask, int32_t ntx, int32_t T, int32_t Mx,
                                int32_t My, double* out, void* stream) {
-  return merge_tiles(fine, flags, ntx, T, Mx, My, out, cs(stream));
+  return merge_tiles(fine, mask, ntx, T, Mx, My, out, cs(stream));
 }
 extern "C" int stn_last_kernel_error(void) { return take_error(); }

@@ -364,13 +364,38 @@ __global__ void k_tile_maxabs(const float* __restrict__ pred, int Cp, int ch, in
   }
 }
 
-// out[tile] = fine[tile] for every tile with flag != 0 (FP64 images, Mx x My column-major)
-__global__ void k_merge_tiles(const double* __restrict__ fine, const int* __restrict__ flags, int ntx, int T, int Mx,
-                              int My, double* __restrict__ out) {
+// mask[t] = tile_max[t] > thresh, or t on the grid's outer ring when border != 0; *count =
+// the flagged tiles.  One block: a fixed-order count, no atomics, nothing to clear first.
+__global__ void __launch_bounds__(1024) k_tile_flags(const float* __restrict__ tile_max, int ntx, int nty, float thresh,
+                                                     int border, unsigned char* __restrict__ mask, int* __restrict__ count) {
+  const int n = ntx * nty;
+  int c = 0;
+  for (int t = threadIdx.x; t < n; t += blockDim.x) {
+    const int tx = t % ntx, ty = t / ntx;
+    const bool edge = border && (tx == 0 || ty == 0 || tx == ntx - 1 || ty == nty - 1);
+    const unsigned char f = (edge || tile_max[t] > thresh) ? 1 : 0;
+    mask[t] = f;
+    c += f;
+  }
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+  __shared__ int red[32];
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = c;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int t = 0;
+    for (int w = 0; w < (int)(blockDim.x / 32); ++w) t += red[w];
+    *count = t;
+  }
+}
+
+// out[tile] = fine[tile] for every tile whose mask byte is nonzero (FP64 images, Mx x My
+// column-major)
+__global__ void k_merge_tiles(const double* __restrict__ fine, const unsigned char* __restrict__ mask, int ntx, int T,
+                              int Mx, int My, double* __restrict__ out) {
   const long long n = (long long)Mx * My;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     const int x = (int)(i % Mx), y = (int)(i / Mx);
-    if (flags[(y / T) * ntx + x / T]) out[i] = fine[i];
+    if (mask[(y / T) * ntx + x / T]) out[i] = fine[i];
   }
 }
 
@@ -482,9 +507,16 @@ int tile_maxabs(const float* pred, int Cp, int ch, int Mx8, int My8, int Wp, int
   k_tile_maxabs<<<grid, kBlock, 0, st>>>(pred, Cp, ch, Mx8, My8, Wp, T, tile_max);
   return status();
 }
-int merge_tiles(const double* fine, const int* flags, int ntx, int T, int Mx, int My, double* out, cudaStream_t st) {
-  if (!fine || !flags || !out || T < 1) return 1;
-  k_merge_tiles<<<grid_for((long long)Mx * My), kBlock, 0, st>>>(fine, flags, ntx, T, Mx, My, out);
+int tile_flags(const float* tile_max, int ntx, int nty, float thresh, int border, unsigned char* mask, int* count,
+               cudaStream_t st) {
+  if (!tile_max || !mask || !count || ntx < 1 || nty < 1) return 1;
+  k_tile_flags<<<1, 1024, 0, st>>>(tile_max, ntx, nty, thresh, border, mask, count);
+  return status();
+}
+int merge_tiles(const double* fine, const unsigned char* mask, int ntx, int T, int Mx, int My, double* out,
+                cudaStream_t st) {
+  if (!fine || !mask || !out || T < 1 || ntx < (Mx + T - 1) / T) return 1;
+  k_merge_tiles<<<grid_for((long long)Mx * My), kBlock, 0, st>>>(fine, mask, ntx, T, Mx, My, out);
   return status();
 }
 int to_bf16(const float* x, __nv_bfloat16* y, long long n, cudaStream_t st) {

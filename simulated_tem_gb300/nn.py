@@ -35,6 +35,7 @@ _PROTOS = {
     "stn_resample_planes": (_i32, [_vp, _i32, _i32, _i32, _i32, _i32, _i32, _f32, _vp, _f32, _vp, _vp]),
     "stn_apply_correction": (_i32, [_vp, _vp, _i32, _i32, _i32, _i32, _f32, _vp, _vp]),
     "stn_tile_maxabs": (_i32, [_vp, _i32, _i32, _i32, _i32, _i32, _i32, _vp, _vp]),
+    "stn_tile_flags": (_i32, [_vp, _i32, _i32, _f32, _i32, _vp, _vp, _vp]),
     "stn_merge_tiles": (_i32, [_vp, _vp, _i32, _i32, _i32, _i32, _vp, _vp]),
     "stn_last_kernel_error": (_i32, []),
 }
@@ -276,7 +277,16 @@ def tile_maxabs(pred, Mx8, My8, T, out, ch=0):
     return out
 
 
-def merge_tiles(fine, flags, T, Mx, My, out):
-    _check(lib().stn_merge_tiles(_ptr(fine), _ptr(flags), flags.shape[-1], T, Mx, My, _ptr(out), _stream()),
+def tile_flags(tile_max, thresh, mask, count, border=True):
+    """mask (uint8, tile_max's shape) = tile_max > thresh (compared in FP32), or the tile on
+    the outer ring; count (int32 device scalar) = the flagged tiles.  No host round trip."""
+    nty, ntx = tile_max.shape
+    _check(lib().stn_tile_flags(_ptr(tile_max), ntx, nty, float(thresh), int(bool(border)), _ptr(mask), _ptr(count),
+                                _stream()), "stn_tile_flags")
+    return mask
+
+
+def merge_tiles(fine, mask, T, Mx, My, out):
+    _check(lib().stn_merge_tiles(_ptr(fine), _ptr(mask), mask.shape[-1], T, Mx, My, _ptr(out), _stream()),
            "stn_merge_tiles")
     return out

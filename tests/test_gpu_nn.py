@@ -134,3 +134,30 @@ def test_elementwise_layers_match_oracle(nn):
     assert np.allclose(glh[..., 0], NO.bf16_round((2 * d / d.size).astype(np.float32)), rtol=0, atol=1e-7)
     assert np.allclose(glh[..., 1], NO.bf16_round((0.5 * 2 * d1 / d1.size).astype(np.float32)), rtol=0, atol=1e-7)
     assert not glh[..., 2:].any()
+
+
+@pytest.mark.parametrize("nty,ntx,border", [(142, 142, True), (1, 1, True), (3, 37, False), (40, 1, True)])
+def test_tile_flags_and_merge(nn, nty, ntx, border):
+    """The fallback mask made on the device: above the threshold (FP32 compare, ties not
+    flagged) or on the outer ring; its count; the merge of the fine tiles it selects."""
+    rng = np.random.default_rng(nty * 1000 + ntx)
+    tm = rng.random((nty, ntx)).astype(np.float32)
+    thresh = 0.7
+    tm.flat[::7] = np.float32(thresh)  # ties with the threshold
+    want = tm > np.float32(thresh)
+    if border:
+        want[0, :] = want[-1, :] = want[:, 0] = want[:, -1] = True
+    mask = torch.empty((nty, ntx), dtype=torch.uint8, device="cuda")
+    count = torch.empty((), dtype=torch.int32, device="cuda")
+    nn.tile_flags(torch.from_numpy(tm).cuda(), thresh, mask, count, border=border)
+    assert np.array_equal(mask.cpu().numpy(), want.astype(np.uint8))
+    assert count.item() == int(want.sum())
+    T = 8
+    Mx, My = ntx * T - 3, nty * T - 5 if nty * T > 5 else nty * T  # ragged last tiles
+    fine = torch.from_numpy(rng.random((My, Mx))).cuda()
+    out = torch.from_numpy(rng.random((My, Mx))).cuda()
+    exp = out.cpu().numpy().copy()
+    sel = np.repeat(np.repeat(want, T, 0), T, 1)[:My, :Mx]
+    exp[sel] = fine.cpu().numpy()[sel]
+    nn.merge_tiles(fine, mask, T, Mx, My, out)
+    assert np.array_equal(out.cpu().numpy(), exp)
