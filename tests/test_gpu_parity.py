@@ -129,6 +129,28 @@ def test_patches_match_oracle(ctx, nprocs):
     assert np.abs(total - full).max() < 1e-9
 
 
+def test_full_size_workload(ctx):
+    """The benchmark's image at full size: the 1.2M-atom screw + voids cell, g = [110],
+    s_g = 0.01, M = 4 (566 x 566 x 240 voxels).  The FP32 path within 1e-4 of the FP64 path
+    over the whole image; repeated FP32 images identical bit for bit; the FP64 path equal to
+    the oracle on 16 middle rows (the oracle's row range keeps the CPU time to seconds)."""
+    cell = synth.screw_cell_1p2m()
+    t, so, x = setup_both(cell, sg=0.01, xi0=103.9, xig=207.5)
+    G, aa = t.image_geometry(len(x))
+    assert (G.Mx, G.My, G.Mz) == (566, 566, 240)
+    img64 = ctx.image(G, x, aa)
+    img32 = ctx.image(G, x, aa, flags=_lib.ST_FLAG_FP32)
+    again = ctx.image(G, x, aa, flags=_lib.ST_FLAG_FP32)
+    assert np.isfinite(img64).all() and img64.max() > 0
+    assert np.abs(img32 - img64).max() <= FP32_TOL
+    assert np.array_equal(img32, again)
+    Go, aao = O.geometry(so, len(x))
+    lo, hi = 275, 291
+    want, _ = O.patch_image(Go, aao, x, rows=(lo, hi), nthreads=8)
+    assert np.abs(img64[:, lo:hi] - want[:, lo:hi]).max() <= FP64_TOL
+    assert want[:, lo:hi].max() > 0
+
+
 def test_w_loop_golden_on_gpu(ctx):
     g = golden_data.w_loop()
     cell = synth.Cell(g["a_super"], g["pos"])
