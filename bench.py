@@ -57,8 +57,8 @@ def workload():
 
 SWEEP_G = ((1, 1, 0), (2, 0, 0), (2, 1, 1))
 # DRAM bytes (read + write) of one k_column_fp32_v2 launch on the 1.2M-atom image, from an
-# ncu capture of `python bench.py --ncu-case fp32` (61.37 MB read + 2.94 MB written)
-COLUMN_TRAFFIC_BYTES = 6.431e7
+# ncu capture of `python bench.py --ncu-case fp32` (61.15 MB read + 2.89 MB written)
+COLUMN_TRAFFIC_BYTES = 6.405e7
 
 
 def sweep_specs(cell, n_tomo=41, n_prec=16, gs=SWEEP_G):
