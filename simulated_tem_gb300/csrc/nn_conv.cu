@@ -13,7 +13,10 @@
 // bytes further: all nine taps read the same tile through shifted descriptors (LBO =
 // slab pitch between 8-channel groups, SBO = 128 between 8-pixel groups).  Outside the
 // image the TMA box is zero-filled: the padding.  The weights of each (tap, chunk) come
-// by TMA into a ring of B slots ([BN rows][16 bytes] per 8-channel group).
+// into a ring of B slots ([BN rows][16 bytes] per 8-channel group) as one contiguous bulk
+// copy: before the convolution a small kernel writes the weights in exactly that order
+// (per output-channel tile, chunk and tap), so the copy reads whole 32-byte sectors
+// (a tensor box of 16-byte rows 2 x taps x Cin bytes apart used half of each sector).
 //
 // The kernel is persistent: a CTA takes tiles t = blockIdx.x, blockIdx.x + gridDim.x, ...
 // and its rings run on from one tile to the next, so the loads of the next tile overlap
@@ -48,9 +51,13 @@ constexpr uint32_t kWaitLimit = 1u << 20;  // polls of an mbarrier before giving
 constexpr int kTileX = 128;                // output pixels per tile (one image row)
 constexpr int kHalo = kTileX + 2;          // input pixels per halo row
 constexpr int kSlab = 2176;                // bytes per (input row, 8 channels) slab: 130 x 16 rounded to 128
-constexpr int kBSlots = 4;                 // weight ring depth
+// weight ring depth: as many slots as leave room for two CTAs per SM (TMEM allows two at
+// BN = 128); each slot holds KC/16 MMAs of work, and the ring must cover the latency of
+// the TMA loads that refill it
+__host__ __device__ constexpr int b_slots(int BN) { return BN >= 128 ? 7 : BN >= 64 ? 5 : 8; }
 
 struct ConvArgs {
+  const unsigned char* wb;    // blocked weights: [Cout tile][chunk][tap] blocks of one B slot
   const float* bias;          // [Cout] or null
   const __nv_bfloat16* mask;  // [B][H][W][Cout] or null: outputs where mask <= 0 are zeroed
   void* y;                    // [B][H][W][Cout], BF16 or FP32
@@ -61,6 +68,7 @@ struct ConvArgs {
 
 template <int BN, int KC, int NR>
 struct TSmem {
+  static constexpr int kBSlots = b_slots(BN);
   alignas(1024) unsigned char a[2][NR * (KC / 8) * kSlab];
   alignas(1024) unsigned char b[kBSlots][(KC / 8) * BN * 16];
   alignas(8) unsigned long long a_full[2], a_empty[2], b_full[kBSlots], b_empty[kBSlots], acc_full[2],
@@ -95,8 +103,7 @@ __device__ __forceinline__ Tile tile_of(const ConvArgs& a, int t, int BN) {
 
 // NR = 3 input rows for a 3 x 3 convolution, 1 for 1 x 1 (then taps = 1).
 template <int BN, int KC, int NR>
-__global__ void __launch_bounds__(kTileThreads) k_conv_fwd(const ConvArgs a, const __grid_constant__ CUtensorMap tmx,
-                                                           const __grid_constant__ CUtensorMap tmw) {
+__global__ void __launch_bounds__(kTileThreads) k_conv_fwd(const ConvArgs a, const __grid_constant__ CUtensorMap tmx) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   TSmem<BN, KC, NR>& S = *reinterpret_cast<TSmem<BN, KC, NR>*>(
       smem_raw + ((1024 - ((uintptr_t)smem_raw & 1023)) & 1023));
@@ -105,6 +112,7 @@ __global__ void __launch_bounds__(kTileThreads) k_conv_fwd(const ConvArgs a, con
   constexpr uint32_t kBytesA = NR * kG * kHalo * 16;
   constexpr uint32_t kBytesB = kG * BN * 16;
   constexpr uint32_t kCols = 2 * BN;                // two accumulators
+  constexpr int kBSlots = TSmem<BN, KC, NR>::kBSlots;
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
   const int nchunks = a.Cin / KC;
   volatile int* abort = &S.abort;
@@ -133,8 +141,9 @@ __global__ void __launch_bounds__(kTileThreads) k_conv_fwd(const ConvArgs a, con
   if (warp == 4) {
     if (lane == 0) {
       // ---- producer: halo tiles and weight slots, in the order the MMAs consume them
-      int na[2] = {0, 0}, nb[kBSlots] = {0, 0, 0, 0};  // loads armed per stage / slot
-      int ca = 0, jb = 0;                              // chunks and weight loads issued
+      int na[2] = {0, 0}, nb[kBSlots] = {};  // loads armed per stage / slot
+      int ca = 0;                            // chunks issued
+      int sb = 0, rb = 0;                    // weight slot of the next load, and its round
       bool ok = true;
       for (int tt = blockIdx.x; tt < a.n_tiles && ok; tt += gridDim.x) {
         const Tile tl = tile_of(a, tt, BN);
@@ -151,18 +160,20 @@ __global__ void __launch_bounds__(kTileThreads) k_conv_fwd(const ConvArgs a, con
             for (int g = 0; g < kG; ++g)
               tc::tma_load_4d(tc::smem_addr(S.a[sa] + (r * kG + g) * kSlab), &tmx, c * KC + 8 * g,
                               tl.xt * kTileX - 1, tl.y + r - (NR == 3 ? 1 : 0), tl.img, fa);
-          for (int tap = 0; tap < kTaps; ++tap, ++jb) {
-            const int sb = jb % kBSlots;
-            if (jb >= kBSlots &&
-                !wait_or_abort(tc::smem_addr(&S.b_empty[sb]), (jb / kBSlots - 1) & 1, abort)) {
+          for (int tap = 0; tap < kTaps; ++tap) {
+            if (rb >= 1 && !wait_or_abort(tc::smem_addr(&S.b_empty[sb]), (rb - 1) & 1, abort)) {
               ok = false;
               break;
             }
             const uint32_t fb = tc::smem_addr(&S.b_full[sb]);
             tc::mbar_arrive_expect_tx(fb, kBytesB);
             ++nb[sb];
-            for (int g = 0; g < kG; ++g)
-              tc::tma_load_3d(tc::smem_addr(S.b[sb] + g * BN * 16), &tmw, c * KC + 8 * g, tap, tl.n0, fb);
+            tc::bulk_load(tc::smem_addr(S.b[sb]),
+                          a.wb + ((size_t)((tl.n0 / BN) * nchunks + c) * kTaps + tap) * kBytesB, kBytesB, fb);
+            if (++sb == kBSlots) {
+              sb = 0;
+              ++rb;
+            }
           }
         }
       }
@@ -176,7 +187,8 @@ __global__ void __launch_bounds__(kTileThreads) k_conv_fwd(const ConvArgs a, con
     if (lane == 0) {
       // ---- MMA issuer
       constexpr uint32_t idesc = tc::make_idesc_bf16(128, BN);
-      int ca = 0, jb = 0, k = 0;  // chunks, weight slots and tiles consumed
+      int ca = 0, k = 0;   // chunks and tiles consumed
+      int sb = 0, rb = 0;  // weight slot of the next tap, and its round
       bool ok = true;
       for (int tt = blockIdx.x; tt < a.n_tiles && ok; tt += gridDim.x, ++k) {
         const int buf = k & 1;
@@ -193,9 +205,8 @@ __global__ void __launch_bounds__(kTileThreads) k_conv_fwd(const ConvArgs a, con
             break;
           }
           const uint64_t adesc0 = tc::make_desc(tc::smem_addr(S.a[sa]), kSlab, 128);
-          for (int tap = 0; tap < kTaps; ++tap, ++jb) {
-            const int sb = jb % kBSlots;
-            if (!wait_or_abort(tc::smem_addr(&S.b_full[sb]), (jb / kBSlots) & 1, abort)) {
+          for (int tap = 0; tap < kTaps; ++tap) {
+            if (!wait_or_abort(tc::smem_addr(&S.b_full[sb]), rb & 1, abort)) {
               ok = false;
               break;
             }
@@ -211,6 +222,10 @@ __global__ void __launch_bounds__(kTileThreads) k_conv_fwd(const ConvArgs a, con
               bd += 2 * BN;
             }
             tc::mma_commit(tc::smem_addr(&S.b_empty[sb]));
+            if (++sb == kBSlots) {
+              sb = 0;
+              ++rb;
+            }
           }
           if (!ok) break;
           tc::mma_commit(tc::smem_addr(&S.a_empty[sa]));
@@ -311,24 +326,69 @@ bool make_map(CUtensorMap* m, const void* base, int rank, const cuuint64_t* dims
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// Blocked weights: wb[nt][c][tap][g][n][8] = w[nt BN + n][tap][c KC + 8 g + 0..7] (zero for
+// output channels past Cout), one 16-byte vector per thread.
+__global__ void k_block_weights(const uint4* __restrict__ w, int Cout, int taps, int Cin, int BN, int KC,
+                                uint4* __restrict__ wb, long long n_vec) {
+  const int kG = KC / 8, nchunks = Cin / KC;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n_vec;
+       i += (long long)gridDim.x * blockDim.x) {
+    long long r = i;
+    const int n = (int)(r % BN);
+    r /= BN;
+    const int g = (int)(r % kG);
+    r /= kG;
+    const int tap = (int)(r % taps);
+    r /= taps;
+    const int c = (int)(r % nchunks);
+    const int nt = (int)(r / nchunks);
+    const int co = nt * BN + n;
+    wb[i] = co < Cout ? w[((long long)co * taps + tap) * (Cin / 8) + c * kG + g] : make_uint4(0, 0, 0, 0);
+  }
+}
+
+// Device buffer of the blocked weights, grown on demand and kept (calls on one stream
+// reuse it in stream order; growing it synchronises the device).
+unsigned char* g_wb = nullptr;
+size_t g_wb_bytes = 0;
+
+cudaError_t blocked_weights(const __nv_bfloat16* w, int Cout, int taps, int Cin, int BN, int KC, cudaStream_t st,
+                            const unsigned char** out) {
+  const int n_nt = (Cout + BN - 1) / BN;
+  const size_t bytes = (size_t)n_nt * BN * taps * Cin * 2;
+  if (bytes > g_wb_bytes) {
+    if (g_wb) cudaFree(g_wb);
+    g_wb = nullptr;
+    g_wb_bytes = 0;
+    const cudaError_t e = cudaMalloc(&g_wb, bytes);
+    if (e != cudaSuccess) return e;
+    g_wb_bytes = bytes;
+  }
+  const long long n_vec = (long long)(bytes / 16);
+  const int blocks = (int)((n_vec + 255) / 256 < 1024 ? (n_vec + 255) / 256 : 1024);
+  k_block_weights<<<blocks, 256, 0, st>>>(reinterpret_cast<const uint4*>(w), Cout, taps, Cin, BN, KC,
+                                          reinterpret_cast<uint4*>(g_wb), n_vec);
+  *out = g_wb;
+  return cudaGetLastError();
+}
+
 template <int BN, int KC, int NR>
 cudaError_t launch_fwd(const __nv_bfloat16* x, const __nv_bfloat16* w, ConvArgs a, cudaStream_t st) {
-  CUtensorMap tmx, tmw;
+  CUtensorMap tmx;
   const cuuint64_t xd[4] = {(cuuint64_t)a.Cin, (cuuint64_t)a.W, (cuuint64_t)a.H, (cuuint64_t)a.B};
   const cuuint64_t xs[3] = {(cuuint64_t)a.Cin * 2, (cuuint64_t)a.W * a.Cin * 2, (cuuint64_t)a.H * a.W * a.Cin * 2};
   const cuuint32_t xb[4] = {8, kHalo, 1, 1};
-  const cuuint64_t wd[3] = {(cuuint64_t)a.Cin, (cuuint64_t)a.taps, (cuuint64_t)a.Cout};
-  const cuuint64_t ws[2] = {(cuuint64_t)a.Cin * 2, (cuuint64_t)a.taps * a.Cin * 2};
-  const cuuint32_t wb[3] = {8, 1, (cuuint32_t)BN};
-  if (!make_map(&tmx, x, 4, xd, xs, xb) || !make_map(&tmw, w, 3, wd, ws, wb)) return cudaErrorInvalidValue;
+  if (!make_map(&tmx, x, 4, xd, xs, xb)) return cudaErrorInvalidValue;
+  if (a.taps != (NR == 3 ? 9 : 1) || a.Cin % KC != 0) return cudaErrorInvalidValue;
+  cudaError_t e = blocked_weights(w, a.Cout, a.taps, a.Cin, BN, KC, st, &a.wb);
+  if (e != cudaSuccess) return e;
   // CTAs per SM: shared memory, and TMEM (2 BN columns each, 512 per SM)
   const size_t per_sm = 232448, need = sizeof(TSmem<BN, KC, NR>) + 1024;
   int ctas = (int)(per_sm / (need + 1024));
   ctas = ctas < 1 ? 1 : ctas;
   if (ctas * 2 * BN > 512) ctas = 512 / (2 * BN);
   const size_t smem = per_sm / ctas - 1024 > need ? per_sm / ctas - 1024 : need;
-  cudaError_t e =
-      cudaFuncSetAttribute(k_conv_fwd<BN, KC, NR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  e = cudaFuncSetAttribute(k_conv_fwd<BN, KC, NR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   int dev = 0, sms = 148;
   cudaGetDevice(&dev);
@@ -339,7 +399,7 @@ cudaError_t launch_fwd(const __nv_bfloat16* x, const __nv_bfloat16* w, ConvArgs 
   if (tiles >= (1LL << 31)) return cudaErrorInvalidValue;
   a.n_tiles = (int)tiles;
   const int grid = a.n_tiles < ctas * sms ? a.n_tiles : ctas * sms;
-  k_conv_fwd<BN, KC, NR><<<grid, kTileThreads, smem, st>>>(a, tmx, tmw);
+  k_conv_fwd<BN, KC, NR><<<grid, kTileThreads, smem, st>>>(a, tmx);
   return cudaGetLastError();
 }
 
@@ -362,7 +422,7 @@ int conv_fwd(const __nv_bfloat16* x, int B, int H, int W, int Cin, const __nv_bf
   // wide, shallow layers: the strip-persistent kernel (resident weights, rolling input rows)
   const int rs = conv_fwd_strip(x, B, H, W, Cin, w, Cout, taps, bias, relu, mask, y, y_fp32, st);
   if (rs >= 0) return rs;
-  ConvArgs a{bias, mask, y, B, H, W, Cin, Cout, taps, relu, y_fp32, 1, 1, 1};
+  ConvArgs a{nullptr, bias, mask, y, B, H, W, Cin, Cout, taps, relu, y_fp32, 1, 1, 1};
   cudaError_t e;
   if (taps == 9)
     e = Cin % 32 == 0 ? launch_fwd_n<32, 3>(x, w, a, st) : launch_fwd_n<16, 3>(x, w, a, st);
