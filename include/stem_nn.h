@@ -17,7 +17,11 @@ extern "C" {
 
 /* y = relu?(conv(x, w) + bias): "same" padding, stride 1.  Cin a multiple of 16, Cout a
  * multiple of 8; y BF16, or FP32 when y_fp32.  bias and mask may be null; where
- * mask (BF16, y's shape) is <= 0 the output is zeroed (the gradient through a ReLU). */
+ * mask (BF16, y's shape) is <= 0 the output is zeroed (the gradient through a ReLU).
+ * Layers the strip kernel does not take first copy w into a library-owned device buffer
+ * in the order the kernel loads it (one buffer per device, kept and grown to the largest
+ * layer: 1.2 MB for the corrector); calls from several threads or streams take turns on
+ * it, in stream order. */
 int stn_conv2d_fwd(const void* x, int32_t B, int32_t H, int32_t W, int32_t Cin, const void* w, int32_t Cout,
                    int32_t taps, const float* bias, int32_t relu, const void* mask, void* y, int32_t y_fp32,
                    void* stream);

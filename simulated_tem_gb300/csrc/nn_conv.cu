@@ -35,6 +35,8 @@
 #include <cudaTypedefs.h>
 #include <stdint.h>
 
+#include <mutex>
+
 #include "nn.h"
 #include "tc_sm100.cuh"
 
@@ -347,28 +349,42 @@ __global__ void k_block_weights(const uint4* __restrict__ w, int Cout, int taps,
   }
 }
 
-// Device buffer of the blocked weights, grown on demand and kept (calls on one stream
-// reuse it in stream order; growing it synchronises the device).
-unsigned char* g_wb = nullptr;
-size_t g_wb_bytes = 0;
+// Device buffer of the blocked weights, one per device, grown on demand and kept (growing
+// it synchronises the device).  Callers on several host threads or streams take turns:
+// the buffer's mutex is held from the blocking kernel to the convolution's launch, and a
+// new user's stream waits for the event recorded after the last convolution that read it.
+struct BlockedWeights {
+  unsigned char* p = nullptr;
+  size_t bytes = 0;
+  cudaEvent_t done = nullptr;
+};
+constexpr int kMaxDevices = 64;
+BlockedWeights g_wb[kMaxDevices];
+std::mutex g_wb_mu;
 
-cudaError_t blocked_weights(const __nv_bfloat16* w, int Cout, int taps, int Cin, int BN, int KC, cudaStream_t st,
-                            const unsigned char** out) {
+cudaError_t blocked_weights(BlockedWeights& b, const __nv_bfloat16* w, int Cout, int taps, int Cin, int BN, int KC,
+                            cudaStream_t st) {
   const int n_nt = (Cout + BN - 1) / BN;
   const size_t bytes = (size_t)n_nt * BN * taps * Cin * 2;
-  if (bytes > g_wb_bytes) {
-    if (g_wb) cudaFree(g_wb);
-    g_wb = nullptr;
-    g_wb_bytes = 0;
-    const cudaError_t e = cudaMalloc(&g_wb, bytes);
+  cudaError_t e = cudaSuccess;
+  if (!b.done) {
+    e = cudaEventCreateWithFlags(&b.done, cudaEventDisableTiming);
     if (e != cudaSuccess) return e;
-    g_wb_bytes = bytes;
   }
+  if (bytes > b.bytes) {
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.bytes = 0;
+    e = cudaMalloc(&b.p, bytes);
+    if (e != cudaSuccess) return e;
+    b.bytes = bytes;
+  }
+  e = cudaStreamWaitEvent(st, b.done, 0);  // the previous convolution that read the buffer
+  if (e != cudaSuccess) return e;
   const long long n_vec = (long long)(bytes / 16);
   const int blocks = (int)((n_vec + 255) / 256 < 1024 ? (n_vec + 255) / 256 : 1024);
   k_block_weights<<<blocks, 256, 0, st>>>(reinterpret_cast<const uint4*>(w), Cout, taps, Cin, BN, KC,
-                                          reinterpret_cast<uint4*>(g_wb), n_vec);
-  *out = g_wb;
+                                          reinterpret_cast<uint4*>(b.p), n_vec);
   return cudaGetLastError();
 }
 
@@ -380,8 +396,15 @@ cudaError_t launch_fwd(const __nv_bfloat16* x, const __nv_bfloat16* w, ConvArgs 
   const cuuint32_t xb[4] = {8, kHalo, 1, 1};
   if (!make_map(&tmx, x, 4, xd, xs, xb)) return cudaErrorInvalidValue;
   if (a.taps != (NR == 3 ? 9 : 1) || a.Cin % KC != 0) return cudaErrorInvalidValue;
-  cudaError_t e = blocked_weights(w, a.Cout, a.taps, a.Cin, BN, KC, st, &a.wb);
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_wb_mu);
+  BlockedWeights& bw = g_wb[dev];
+  e = blocked_weights(bw, w, a.Cout, a.taps, a.Cin, BN, KC, st);
+  if (e != cudaSuccess) return e;
+  a.wb = bw.p;
   // CTAs per SM: shared memory, and TMEM (2 BN columns each, 512 per SM)
   const size_t per_sm = 232448, need = sizeof(TSmem<BN, KC, NR>) + 1024;
   int ctas = (int)(per_sm / (need + 1024));
@@ -390,8 +413,7 @@ cudaError_t launch_fwd(const __nv_bfloat16* x, const __nv_bfloat16* w, ConvArgs 
   const size_t smem = per_sm / ctas - 1024 > need ? per_sm / ctas - 1024 : need;
   e = cudaFuncSetAttribute(k_conv_fwd<BN, KC, NR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  int dev = 0, sms = 148;
-  cudaGetDevice(&dev);
+  int sms = 148;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   a.n_ntiles = (a.Cout + BN - 1) / BN;
   a.xtiles = (a.W + kTileX - 1) / kTileX;
@@ -400,7 +422,9 @@ cudaError_t launch_fwd(const __nv_bfloat16* x, const __nv_bfloat16* w, ConvArgs 
   a.n_tiles = (int)tiles;
   const int grid = a.n_tiles < ctas * sms ? a.n_tiles : ctas * sms;
   k_conv_fwd<BN, KC, NR><<<grid, kTileThreads, smem, st>>>(a, tmx);
-  return cudaGetLastError();
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  return cudaEventRecord(bw.done, st);
 }
 
 template <int KC, int NR>

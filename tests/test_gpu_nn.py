@@ -161,3 +161,23 @@ def test_tile_flags_and_merge(nn, nty, ntx, border):
     exp[sel] = fine.cpu().numpy()[sel]
     nn.merge_tiles(fine, mask, T, Mx, My, out)
     assert np.array_equal(out.cpu().numpy(), exp)
+
+
+def test_conv_streams_take_turns_on_blocked_weights(nn):
+    """Layers of the halo-tile kernel copy their weights into one library buffer first:
+    convolutions of different weights queued on two streams without synchronising give
+    the results of the same calls made one at a time (bit for bit)."""
+    rng = np.random.default_rng(21)
+    x = _bf16(_rand(rng, 1, 24, 40, 192))
+    ws = [_bf16(_rand(rng, 128, 9, 192, scale=0.02)), _bf16(_rand(rng, 64, 9, 192, scale=0.02))]
+    want = [nn.conv2d(x, w, out_fp32=True) for w in ws]
+    torch.cuda.synchronize()
+    streams = [torch.cuda.Stream(), torch.cuda.Stream()]
+    outs = []
+    for i in range(8):
+        with torch.cuda.stream(streams[i % 2]):
+            outs.append(nn.conv2d(x, ws[i % 2], out_fp32=True))
+    torch.cuda.synchronize()
+    assert nn.last_kernel_error() == 0
+    for i, o in enumerate(outs):
+        assert torch.equal(o, want[i % 2])
