@@ -2,13 +2,15 @@
 //
 // Forward (and input-gradient) convolution, 3 x 3 ("same" padding) or 1 x 1, over NHWC
 // BF16 activations: an implicit GEMM D[p, co] = sum_k A[p, k] B[co, k], p the output
-// pixel, k = (tap, ci).  A tile is 128 consecutive pixels of one image row x BN output
-// channels; its FP32 accumulator lives in TMEM (BN columns).  No thread touches the
-// operands: one thread moves them with TMA, one issues the MMAs, four warps drain TMEM.
+// pixel, k = (tap, ci).  A tile is 128 consecutive pixels of one image row (two adjacent
+// rows for BN <= 64) x BN output channels; each row's FP32 accumulator lives in TMEM (BN
+// columns).  No thread
+// touches the operands: one thread moves them, one issues the MMAs, four warps drain TMEM.
 //
-// Per chunk of KC input channels the producer loads a halo tile: the input rows y - 1,
-// y, y + 1 (one row for 1 x 1), pixels x0 - 1 .. x0 + 128, as (KC / 8) slabs of 130 rows
-// x 16 bytes (8 channels) per input row.  In such a slab the rows are 16 bytes apart, so
+// Per chunk of KC input channels the producer loads a halo tile: the input rows y - 1 ..
+// y + R (R output rows; from y for 1 x 1), pixels x0 - 1 .. x0 + 128, as (KC / 8) slabs
+// of 130 rows x 16 bytes (8 channels) per input row; output row y + q reads the input
+// rows from y - 1 + q, and every row's MMAs read each weight slot.  In such a slab the rows are 16 bytes apart, so
 // the K-major core matrices (8 rows x 16 bytes) of the pixels shifted by dx start 16 dx
 // bytes further: all nine taps read the same tile through shifted descriptors (LBO =
 // slab pitch between 8-channel groups, SBO = 128 between 8-pixel groups).  Outside the
@@ -56,7 +58,10 @@ constexpr int kSlab = 2176;                // bytes per (input row, 8 channels) 
 // weight ring depth: as many slots as leave room for two CTAs per SM (TMEM allows two at
 // BN = 128); each slot holds KC/16 MMAs of work, and the ring must cover the latency of
 // the TMA loads that refill it
-__host__ __device__ constexpr int b_slots(int BN) { return BN >= 128 ? 7 : BN >= 64 ? 5 : 8; }
+__host__ __device__ constexpr int b_slots(int BN) { return BN >= 128 ? 7 : 8; }
+// output rows per tile: two rows read each weight slot and share two halo rows, but need
+// twice the TMEM columns; at BN = 128 that would leave one CTA per SM (measured slower)
+__host__ __device__ constexpr int rows_per_tile(int BN) { return BN >= 128 ? 1 : 2; }
 
 struct ConvArgs {
   const unsigned char* wb;    // blocked weights: [Cout tile][chunk][tap] blocks of one B slot
@@ -65,13 +70,13 @@ struct ConvArgs {
   void* y;                    // [B][H][W][Cout], BF16 or FP32
   int B, H, W, Cin, Cout, taps, relu, y_fp32;
   int n_ntiles;               // output-channel tiles
-  int xtiles, n_tiles;        // tiles: (x tile, row, image, channel tile)
+  int xtiles, n_tiles;        // tiles: (x tile, row group, image, channel tile)
 };
 
 template <int BN, int KC, int NR>
 struct TSmem {
   static constexpr int kBSlots = b_slots(BN);
-  alignas(1024) unsigned char a[2][NR * (KC / 8) * kSlab];
+  alignas(1024) unsigned char a[2][(NR + rows_per_tile(BN) - 1) * (KC / 8) * kSlab];
   alignas(1024) unsigned char b[kBSlots][(KC / 8) * BN * 16];
   alignas(8) unsigned long long a_full[2], a_empty[2], b_full[kBSlots], b_empty[kBSlots], acc_full[2],
       acc_empty[2], done;
@@ -90,14 +95,15 @@ __device__ __forceinline__ bool wait_or_abort(uint32_t mbar, uint32_t parity, vo
 }
 
 struct Tile {
-  int xt, y, img, n0;
+  int xt, y, img, n0;  // y: the first of the tile's rows_per_tile(BN) output rows
 };
 __device__ __forceinline__ Tile tile_of(const ConvArgs& a, int t, int BN) {
   Tile r;
   r.xt = t % a.xtiles;
   int rest = t / a.xtiles;
-  r.y = rest % a.H;
-  rest /= a.H;
+  const int rows = rows_per_tile(BN), groups = (a.H + rows - 1) / rows;
+  r.y = (rest % groups) * rows;
+  rest /= groups;
   r.img = rest % a.B;
   r.n0 = (rest / a.B) * BN;
   return r;
@@ -111,9 +117,11 @@ __global__ void __launch_bounds__(kTileThreads) k_conv_fwd(const ConvArgs a, con
       smem_raw + ((1024 - ((uintptr_t)smem_raw & 1023)) & 1023));
   constexpr int kTaps = NR == 3 ? 9 : 1;
   constexpr int kG = KC / 8;                        // 8-channel groups per chunk
-  constexpr uint32_t kBytesA = NR * kG * kHalo * 16;
+  constexpr int kRowsPerTile = rows_per_tile(BN);
+  constexpr int kInRows = NR + kRowsPerTile - 1;   // halo rows per tile
+  constexpr uint32_t kBytesA = kInRows * kG * kHalo * 16;
   constexpr uint32_t kBytesB = kG * BN * 16;
-  constexpr uint32_t kCols = 2 * BN;                // two accumulators
+  constexpr uint32_t kCols = 2 * kRowsPerTile * BN;  // two buffers of one accumulator per row
   constexpr int kBSlots = TSmem<BN, KC, NR>::kBSlots;
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
   const int nchunks = a.Cin / KC;
@@ -158,7 +166,7 @@ __global__ void __launch_bounds__(kTileThreads) k_conv_fwd(const ConvArgs a, con
           const uint32_t fa = tc::smem_addr(&S.a_full[sa]);
           tc::mbar_arrive_expect_tx(fa, kBytesA);
           ++na[sa];
-          for (int r = 0; r < NR; ++r)
+          for (int r = 0; r < kInRows; ++r)
             for (int g = 0; g < kG; ++g)
               tc::tma_load_4d(tc::smem_addr(S.a[sa] + (r * kG + g) * kSlab), &tmx, c * KC + 8 * g,
                               tl.xt * kTileX - 1, tl.y + r - (NR == 3 ? 1 : 0), tl.img, fa);
@@ -199,7 +207,7 @@ __global__ void __launch_bounds__(kTileThreads) k_conv_fwd(const ConvArgs a, con
           break;
         }
         tc::fence_after_sync();
-        const uint32_t acc = tmem + (uint32_t)(buf * BN);
+        const uint32_t acc = tmem + (uint32_t)(buf * kRowsPerTile * BN);  // row q at + q BN
         for (int c = 0; c < nchunks && ok; ++c, ++ca) {
           const int sa = ca & 1;
           if (!wait_or_abort(tc::smem_addr(&S.a_full[sa]), (ca >> 1) & 1, abort)) {
@@ -214,12 +222,17 @@ __global__ void __launch_bounds__(kTileThreads) k_conv_fwd(const ConvArgs a, con
             }
             tc::fence_after_sync();
             const int dy = NR == 3 ? tap / 3 : 0, dx = NR == 3 ? tap % 3 : 1;  // halo row / column offset
-            // start addresses in 16-byte units (descriptor bits 0-13)
+            // start addresses in 16-byte units (descriptor bits 0-13); output row q reads
+            // halo rows dy + q, one row group (kG slabs) further
             uint64_t ad = adesc0 + (uint64_t)(dy * kG * (kSlab / 16) + dx);
             uint64_t bd = tc::make_desc(tc::smem_addr(S.b[sb]), BN * 16, 128);
+            const uint32_t first = (c == 0 && tap == 0) ? 0u : 1u;
 #pragma unroll
             for (int s = 0; s < KC / 16; ++s) {
-              tc::mma_bf16(acc, ad, bd, idesc, (c == 0 && tap == 0 && s == 0) ? 0u : 1u);
+#pragma unroll
+              for (int q = 0; q < kRowsPerTile; ++q)
+                tc::mma_bf16(acc + (uint32_t)(q * BN), ad + (uint64_t)(q * kG * (kSlab / 16)), bd, idesc,
+                             (s == 0) ? first : 1u);
               ad += 2 * kSlab / 16;
               bd += 2 * BN;
             }
@@ -246,25 +259,30 @@ __global__ void __launch_bounds__(kTileThreads) k_conv_fwd(const ConvArgs a, con
       const int buf = k & 1;
       if (!wait_or_abort(tc::smem_addr(&S.acc_full[buf]), (k >> 1) & 1, abort)) break;
       tc::fence_after_sync();
+#pragma unroll 1
+      for (int q = 0; q < kRowsPerTile; ++q) {
       float v[BN];
       {
         uint32_t reg[BN];
         if constexpr (BN >= 32) {
 #pragma unroll
           for (int col = 0; col < BN; col += 32)
-            tc::tmem_ld32_nowait(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(buf * BN + col), reg + col);
+            tc::tmem_ld32_nowait(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)((buf * kRowsPerTile + q) * BN + col),
+                                 reg + col);
           tc::tmem_wait_ld();
         }
 #pragma unroll
         for (int c2 = 0; c2 < BN; ++c2) v[c2] = __uint_as_float(reg[c2]);
       }
-      tc::fence_before_sync();
-      __syncwarp();
-      if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc::smem_addr(&S.acc_empty[buf]))
-                                  : "memory");
+      if (q == kRowsPerTile - 1) {  // the buffer's last TMEM read: the MMAs may refill it
+        tc::fence_before_sync();
+        __syncwarp();
+        if (lane == 0)
+          asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc::smem_addr(&S.acc_empty[buf])) : "memory");
+      }
       const int xw = tl.xt * kTileX + 32 * warp + lane;
-      if (xw < a.W) {
-        const size_t p = ((size_t)tl.img * a.H + tl.y) * a.W + xw;
+      if (xw < a.W && tl.y + q < a.H) {
+        const size_t p = ((size_t)tl.img * a.H + tl.y + q) * a.W + xw;
 #pragma unroll
         for (int col = 0; col < BN; col += 8) {
           const int n = tl.n0 + col;
@@ -294,6 +312,7 @@ __global__ void __launch_bounds__(kTileThreads) k_conv_fwd(const ConvArgs a, con
                 *reinterpret_cast<const uint4*>(h);
           }
         }
+      }
       }
     }
   }
@@ -405,11 +424,12 @@ cudaError_t launch_fwd(const __nv_bfloat16* x, const __nv_bfloat16* w, ConvArgs 
   e = blocked_weights(bw, w, a.Cout, a.taps, a.Cin, BN, KC, st);
   if (e != cudaSuccess) return e;
   a.wb = bw.p;
-  // CTAs per SM: shared memory, and TMEM (2 BN columns each, 512 per SM)
+  // CTAs per SM: shared memory, and TMEM (2 kRowsPerTile BN columns each, 512 per SM)
+  constexpr int kRowsPerTile = rows_per_tile(BN);
   const size_t per_sm = 232448, need = sizeof(TSmem<BN, KC, NR>) + 1024;
   int ctas = (int)(per_sm / (need + 1024));
   ctas = ctas < 1 ? 1 : ctas;
-  if (ctas * 2 * BN > 512) ctas = 512 / (2 * BN);
+  if (ctas * 2 * kRowsPerTile * BN > 512) ctas = 512 / (2 * kRowsPerTile * BN);
   const size_t smem = per_sm / ctas - 1024 > need ? per_sm / ctas - 1024 : need;
   e = cudaFuncSetAttribute(k_conv_fwd<BN, KC, NR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
@@ -417,7 +437,8 @@ cudaError_t launch_fwd(const __nv_bfloat16* x, const __nv_bfloat16* w, ConvArgs 
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   a.n_ntiles = (a.Cout + BN - 1) / BN;
   a.xtiles = (a.W + kTileX - 1) / kTileX;
-  const long long tiles = (long long)a.xtiles * a.H * a.B * a.n_ntiles;
+  const long long tiles =
+      (long long)a.xtiles * ((a.H + kRowsPerTile - 1) / kRowsPerTile) * a.B * a.n_ntiles;
   if (tiles >= (1LL << 31)) return cudaErrorInvalidValue;
   a.n_tiles = (int)tiles;
   const int grid = a.n_tiles < ctas * sms ? a.n_tiles : ctas * sms;

@@ -36,6 +36,9 @@ def nn():
     (2, 13, 17, 16, 32, 9),     # ragged image, KC = 16
     (1, 24, 20, 64, 128, 9),
     (1, 12, 12, 128, 16, 9),    # Cout 16 in a 32-wide tile
+    (1, 13, 20, 192, 64, 9),    # two-row tiles (BN 64), odd height: the last tile's second row is outside
+    (2, 7, 9, 160, 40, 9),      # two-row tiles, Cout 40 in a 64-wide tile
+    (1, 5, 33, 256, 24, 1),     # two-row tiles of a 1 x 1 convolution
 ])
 def test_conv_fwd_matches_oracle(nn, B, H, W, Cin, Cout, taps):
     rng = np.random.default_rng(B * 1000 + Cin + Cout + taps)
