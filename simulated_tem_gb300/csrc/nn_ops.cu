@@ -271,6 +271,19 @@ __global__ void k_pack(const float* __restrict__ planes, int nplanes, __nv_bfloa
   }
 }
 
+// the same, one thread per pixel: C / 8 vectors of 8 channels (y 16-byte aligned)
+__global__ void k_pack_vec(const float* __restrict__ planes, int nplanes, __nv_bfloat16* __restrict__ y,
+                           long long npix, int C) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npix; p += (long long)gridDim.x * blockDim.x) {
+    for (int c0 = 0; c0 < C; c0 += 8) {
+      __align__(16) __nv_bfloat16 h[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) h[k] = tobf(c0 + k < nplanes ? planes[(long long)(c0 + k) * npix + p] : 0.f);
+      *reinterpret_cast<uint4*>(y + p * C + c0) = *reinterpret_cast<const uint4*>(h);
+    }
+  }
+}
+
 // FP32 -> BF16 copy
 __global__ void k_to_bf16(const float* __restrict__ x, __nv_bfloat16* __restrict__ y, long long n) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
@@ -289,7 +302,16 @@ __global__ void __launch_bounds__(1024) k_image_mean(const double* __restrict__ 
                                                      double* __restrict__ mean) {
   __shared__ double red[32];
   double s = 0.0;
-  for (long long i = threadIdx.x; i < n; i += blockDim.x) s += img[i];
+  // each thread adds img[t], img[t + 1024], ... in that order; eight loads in flight
+  const long long step = blockDim.x;
+  for (long long base = threadIdx.x; base < n; base += 8 * step) {
+    double v[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v[k] = base + k * step < n ? img[base + k * step] : 0.0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+      if (base + k * step < n) s += v[k];
+  }
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
   __syncthreads();
@@ -312,11 +334,15 @@ __global__ void __launch_bounds__(1024) k_image_mean(const double* __restrict__ 
 __global__ void k_resample_planes(const double* __restrict__ img2, int Mx2, int My2, int Mx8, int My8, int Wp, int Hp,
                                   float sg_value, const double* __restrict__ mean, float contrast,
                                   float* __restrict__ planes) {
+  // grid: x over the row's pixels, y over the rows (no 64-bit division per pixel)
   const long long n = (long long)Wp * Hp;
+  const int qx = blockIdx.x * blockDim.x + threadIdx.x, qy = blockIdx.y;
+  if (qx >= Wp || qy >= Hp) return;
+  const long long i = (long long)qy * Wp + qx;
   const double sx = (double)Mx2 / Mx8, sy = (double)My2 / My8;
   const double mu = *mean;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const int px = min((int)(i % Wp), Mx8 - 1), py = min((int)(i / Wp), My8 - 1);
+  {
+    const int px = min(qx, Mx8 - 1), py = min(qy, My8 - 1);
     const double u = px * sx, v = py * sy;
     int i0 = min((int)floor(u), Mx2 - 1), j0 = min((int)floor(v), My2 - 1);
     const double fu = u - i0, fv = v - j0;
@@ -475,7 +501,10 @@ int adam(float* w, float* m, float* v, const float* g, __nv_bfloat16* w16, long 
 }
 int pack(const float* planes, int nplanes, __nv_bfloat16* y, long long npix, int C, cudaStream_t st) {
   if (!planes || !y || nplanes < 1 || nplanes > C) return 1;
-  k_pack<<<grid_for(npix * C), kBlock, 0, st>>>(planes, nplanes, y, npix, C);
+  if (C % 8 == 0 && ((uintptr_t)y & 15) == 0)
+    k_pack_vec<<<grid_for(npix), kBlock, 0, st>>>(planes, nplanes, y, npix, C);
+  else
+    k_pack<<<grid_for(npix * C), kBlock, 0, st>>>(planes, nplanes, y, npix, C);
   return status();
 }
 int add(__nv_bfloat16* a, const __nv_bfloat16* b, long long n, cudaStream_t st) {
@@ -491,8 +520,9 @@ int image_mean(const double* img, long long n, double* mean, cudaStream_t st) {
 int resample_planes(const double* img2, int Mx2, int My2, int Mx8, int My8, int Wp, int Hp, float sg_value,
                     const double* mean, float contrast, float* planes, cudaStream_t st) {
   if (!img2 || !planes || !mean || Mx2 < 1 || My2 < 1 || Mx8 < 1 || My8 < 1 || Wp < Mx8 || Hp < My8) return 1;
-  k_resample_planes<<<grid_for((long long)Wp * Hp), kBlock, 0, st>>>(img2, Mx2, My2, Mx8, My8, Wp, Hp, sg_value,
-                                                                    mean, contrast, planes);
+  if (Hp > 65535) return 1;
+  const dim3 grid((Wp + kBlock - 1) / kBlock, Hp);
+  k_resample_planes<<<grid, kBlock, 0, st>>>(img2, Mx2, My2, Mx8, My8, Wp, Hp, sg_value, mean, contrast, planes);
   return status();
 }
 int apply_correction(const float* base, const float* pred, int Cp, int Mx8, int My8, int Wp, float scale, double* out,

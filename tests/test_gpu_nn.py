@@ -184,3 +184,40 @@ def test_conv_streams_take_turns_on_blocked_weights(nn):
     assert nn.last_kernel_error() == 0
     for i, o in enumerate(outs):
         assert torch.equal(o, want[i % 2])
+
+
+def test_input_planes_mean_and_pack(nn):
+    """The corrector's input path against numpy: the coarse image's mean (one fixed-order
+    FP64 sum), the planes resampled bilinearly onto the fine grid in FP64 (edges clamped,
+    the padding rows and columns repeating the last pixel), and their BF16 NHWC packing
+    (exact: one rounding of each FP32 value, zeros past the planes)."""
+    rng = np.random.default_rng(5)
+    Mx2, My2, Mx8, My8, Wp, Hp = 37, 29, 147, 115, 152, 120
+    img2 = 0.1 + 0.6 * rng.random((My2, Mx2))  # numpy (My2, Mx2) = column-major (Mx2, My2)
+    d_img2 = torch.from_numpy(img2).cuda()
+    mean = torch.empty(1, dtype=torch.float64, device="cuda")
+    nn.image_mean(d_img2, mean)
+    mu = img2.mean()
+    assert abs(mean.item() - mu) <= 1e-14 * mu
+    planes = torch.empty((5, Hp, Wp), dtype=torch.float32, device="cuda")
+    nn.resample_planes(d_img2, Mx2, My2, Mx8, My8, Wp, Hp, 0.25, mean, 20.0, planes)
+    px = np.minimum(np.arange(Wp), Mx8 - 1)
+    py = np.minimum(np.arange(Hp), My8 - 1)
+    u, v = px * (Mx2 / Mx8), py * (My2 / My8)
+    i0 = np.minimum(np.floor(u).astype(int), Mx2 - 1)
+    j0 = np.minimum(np.floor(v).astype(int), My2 - 1)
+    fu, fv = u - i0, v - j0
+    i1, j1 = np.minimum(i0 + 1, Mx2 - 1), np.minimum(j0 + 1, My2 - 1)
+    a, b = img2[j0][:, i0], img2[j0][:, i1]
+    c, d = img2[j1][:, i0], img2[j1][:, i1]
+    df = (1 - fv)[:, None] * ((1 - fu) * a + fu * b) + fv[:, None] * ((1 - fu) * c + fu * d)
+    got = planes.cpu().numpy()
+    m = mean.item()
+    assert np.abs(got[4] - df).max() <= 2e-7
+    assert np.abs(got[0] - (df - m) * 20.0).max() <= 5e-6
+    assert np.array_equal(got[1], -got[0])
+    assert np.all(got[2] == np.float32(0.25)) and np.all(got[3] == np.float32(m))
+    packed = nn.pack(planes[:4].view(4, 1, Hp, Wp), 16).float().cpu().numpy()[0]
+    want = np.zeros((Hp, Wp, 16), dtype=np.float32)
+    want[..., :4] = NO.bf16_round(np.moveaxis(got[:4], 0, -1))
+    assert np.array_equal(packed, want)
