@@ -121,6 +121,21 @@ __global__ void k_upsample2_concat(const __nv_bfloat16* __restrict__ d, const __
   }
 }
 
+// the same on a grid of (vectors of one row, rows): 32-bit index arithmetic in the row
+__global__ void k_upsample2_concat_rows(const __nv_bfloat16* __restrict__ d, const __nv_bfloat16* __restrict__ e,
+                                        __nv_bfloat16* __restrict__ y, int H, int W, int Cd, int Ce) {
+  const int C = Cd + Ce, V = C / 8, Hd = H / 2, Wd = W / 2;
+  const int row = blockIdx.y, b = row / H, yh = row % H;
+  const size_t drow = (size_t)(b * Hd + yh / 2) * Wd;
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < W * V; j += gridDim.x * blockDim.x) {
+    const int c = (j % V) * 8, xw = j / V;
+    const size_t p = (size_t)row * W + xw;
+    const uint4 v = c < Cd ? *reinterpret_cast<const uint4*>(d + (drow + xw / 2) * Cd + c)
+                           : *reinterpret_cast<const uint4*>(e + p * Ce + (c - Cd));
+    *reinterpret_cast<uint4*>(y + p * C + c) = v;
+  }
+}
+
 // gx[b, i, j, c] = sum of gy over the 2 x 2 block it was copied to (FP32 sum, one rounding)
 __global__ void k_upsample2_bwd(const __nv_bfloat16* __restrict__ gy, __nv_bfloat16* __restrict__ gx, int B, int H,
                                 int W, int C) {
@@ -360,12 +375,12 @@ __global__ void k_resample_planes(const double* __restrict__ img2, int Mx2, int 
 
 // out (FP64, Mx8 x My8 column-major) = base + pred[p][0] * scale, p over the Hp x Wp
 // grid's top-left My8 x Mx8 block.
+// grid: (pixels of a row, rows)
 __global__ void k_apply_correction(const float* __restrict__ base, const float* __restrict__ pred, int Cp, int Mx8,
                                    int My8, int Wp, float scale, double* __restrict__ out) {
-  const long long n = (long long)Mx8 * My8;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const int x = (int)(i % Mx8), y = (int)(i / Mx8);
-    const long long p = (long long)y * Wp + x;
+  const int y = blockIdx.y;
+  for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < Mx8; x += gridDim.x * blockDim.x) {
+    const long long i = (long long)y * Mx8 + x, p = (long long)y * Wp + x;
     out[i] = (double)base[p] + (double)pred[p * Cp] * (double)scale;
   }
 }
@@ -416,12 +431,14 @@ __global__ void __launch_bounds__(1024) k_tile_flags(const float* __restrict__ t
 
 // out[tile] = fine[tile] for every tile whose mask byte is nonzero (FP64 images, Mx x My
 // column-major)
+// grid: (pixels of a row, rows)
 __global__ void k_merge_tiles(const double* __restrict__ fine, const unsigned char* __restrict__ mask, int ntx, int T,
                               int Mx, int My, double* __restrict__ out) {
-  const long long n = (long long)Mx * My;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const int x = (int)(i % Mx), y = (int)(i / Mx);
-    if (mask[(y / T) * ntx + x / T]) out[i] = fine[i];
+  const int y = blockIdx.y;
+  const unsigned char* mrow = mask + (y / T) * ntx;
+  for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < Mx; x += gridDim.x * blockDim.x) {
+    const long long i = (long long)y * Mx + x;
+    if (mrow[x / T]) out[i] = fine[i];
   }
 }
 
@@ -450,7 +467,13 @@ int upsample2(const __nv_bfloat16* x, __nv_bfloat16* y, int B, int H, int W, int
 int upsample2_concat(const __nv_bfloat16* d, const __nv_bfloat16* e, __nv_bfloat16* y, int B, int H, int W, int Cd,
                      int Ce, cudaStream_t st) {
   if (!d || !e || !y || H % 2 || W % 2 || Cd % 8 || !pix_ok(B, H, W, Cd + Ce) || Ce < 8 || Ce % 8) return 1;
-  k_upsample2_concat<<<grid_for((long long)B * H * W * (Cd + Ce) / 8), kBlock, 0, st>>>(d, e, y, B, H, W, Cd, Ce);
+  const long long rows = (long long)B * H, per_row = (long long)W * (Cd + Ce) / 8;
+  if (rows <= 65535) {
+    const dim3 grid((unsigned)((per_row + kBlock - 1) / kBlock), (unsigned)rows);
+    k_upsample2_concat_rows<<<grid, kBlock, 0, st>>>(d, e, y, H, W, Cd, Ce);
+  } else {
+    k_upsample2_concat<<<grid_for(rows * per_row), kBlock, 0, st>>>(d, e, y, B, H, W, Cd, Ce);
+  }
   return status();
 }
 int upsample2_bwd(const __nv_bfloat16* gy, __nv_bfloat16* gx, int B, int H, int W, int C, cudaStream_t st) {
@@ -527,8 +550,10 @@ int resample_planes(const double* img2, int Mx2, int My2, int Mx8, int My8, int 
 }
 int apply_correction(const float* base, const float* pred, int Cp, int Mx8, int My8, int Wp, float scale, double* out,
                      cudaStream_t st) {
-  if (!base || !pred || !out || Wp < Mx8) return 1;
-  k_apply_correction<<<grid_for((long long)Mx8 * My8), kBlock, 0, st>>>(base, pred, Cp, Mx8, My8, Wp, scale, out);
+  if (!base || !pred || !out || Wp < Mx8 || My8 > 65535) return 1;
+  if (Mx8 < 1 || My8 < 1) return 0;
+  k_apply_correction<<<dim3((Mx8 + kBlock - 1) / kBlock, My8), kBlock, 0, st>>>(base, pred, Cp, Mx8, My8, Wp, scale,
+                                                                                 out);
   return status();
 }
 int tile_maxabs(const float* pred, int Cp, int ch, int Mx8, int My8, int Wp, int T, float* tile_max, cudaStream_t st) {
@@ -546,7 +571,9 @@ int tile_flags(const float* tile_max, int ntx, int nty, float thresh, int border
 int merge_tiles(const double* fine, const unsigned char* mask, int ntx, int T, int Mx, int My, double* out,
                 cudaStream_t st) {
   if (!fine || !mask || !out || T < 1 || ntx < (Mx + T - 1) / T) return 1;
-  k_merge_tiles<<<grid_for((long long)Mx * My), kBlock, 0, st>>>(fine, mask, ntx, T, Mx, My, out);
+  if (My < 1 || Mx < 1) return 0;
+  if (My > 65535) return 1;
+  k_merge_tiles<<<dim3((Mx + kBlock - 1) / kBlock, My), kBlock, 0, st>>>(fine, mask, ntx, T, Mx, My, out);
   return status();
 }
 int to_bf16(const float* x, __nv_bfloat16* y, long long n, cudaStream_t st) {

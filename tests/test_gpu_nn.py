@@ -221,3 +221,11 @@ def test_input_planes_mean_and_pack(nn):
     want = np.zeros((Hp, Wp, 16), dtype=np.float32)
     want[..., :4] = NO.bf16_round(np.moveaxis(got[:4], 0, -1))
     assert np.array_equal(packed, want)
+    # the corrected image: base + channel 0 of the prediction x scale, FP64, on the image's
+    # My8 x Mx8 block of the padded grid
+    pred = torch.from_numpy(rng.standard_normal((Hp, Wp, 16)).astype(np.float32)).cuda()
+    out = torch.empty((My8, Mx8), dtype=torch.float64, device="cuda")
+    nn.apply_correction(planes[4], pred, Mx8, My8, 0.01, out)
+    want = got[4][:My8, :Mx8].astype(np.float64) + \
+        pred.cpu().numpy()[:My8, :Mx8, 0].astype(np.float64) * np.float64(np.float32(0.01))
+    assert np.abs(out.cpu().numpy() - want).max() <= 1e-15
