@@ -13,17 +13,23 @@ FP64 cell assignment and FP64 g.r reduction.
   e2e    the same through st_image, the C-ABI call a Fortran or C host makes,
          from pinned host buffers: the H2D copy of the atoms and the D2H copy
          of the image are inside the timed region.
-  also   the plain FP64 GPU path (images/s) and max |dI| FP32 vs FP64.
+  also   the plain FP64 GPU path (images/s); accuracy of both paths against the
+         oracle's whole image (max |dI| and RMS), and FP32 vs FP64.
+  roofline  the path roofline of the reference's voxel loop (MUFU, FP32, FP64 and
+         HBM work over the measured peaks; the bound is the largest), as a
+         fraction of the column kernel's time, and of the whole step; the work
+         the kernel executes beside it.
   batched  st_batch_device on (a) the tilt x precession x g sweep of the same
          cell (41 x 16 x 3: 123 images, 1,968 integration passes) and (b) 256
-         independent cells of uneven size; images/s, voxel-slices/s and the
-         FP32-vs-FP64 accuracy of one image of each.  The clock record spans
-         the single-image steps and both batched legs.
+         independent cells of uneven size; images/s, voxel-slices/s, stage
+         times of the timed calls, launches, the path roofline, and accuracy
+         against the oracle (a row band of one image per g; the largest cell
+         whole).  The clock record spans the single-image steps and every leg.
 
 ``--impl reference`` times the reference's algorithm on the host cores: the
 reference (Fortran) cannot be built here, so the oracle's C restatement runs,
-with all host threads, on a bounded band of pixel rows of the same image,
-extrapolated to whole images.
+with all host threads, on whole images of the same workload, one per step.
+Nothing of the product is imported or loaded in that process.
 
 Under torchrun with N > 1 every rank images its own copy of the workload
 (independent images: replicas, no collective on the data path); value is the
@@ -55,6 +61,86 @@ def workload():
     return cell, t, x, aperpx
 
 
+def standalone_synth():
+    """The seeded cell generator (simulated_tem_gb300/synth.py, numpy only) loaded by its file
+    path, without the package: the reference arm must not import or load any product code."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("_bench_synth", os.path.join(ROOT, "simulated_tem_gb300",
+                                                                               "synth.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def oracle_workload_setup(cell, A0):
+    """The oracle's set-up of the 1.2M-atom image (wrapped atoms, geometry, precession)."""
+    from oracle import stem_oracle as O
+    args = O.make_args(cell.a_super, A0, (0, 0, 1), (1, 1, 0), sg=0.01, xi0=103.9, xig=207.5)
+    so, xo, _ = O.setup(args, cell.pos)
+    G, aa = O.geometry(so, len(xo))
+    return G, aa, xo
+
+
+def oracle_workload_image(state, threads):
+    """The 1.2M-atom image computed whole by the oracle (the C restatement of computeD2BI_img,
+    binning included) on `threads` host threads; (image (Mx, My), seconds, stats)."""
+    from oracle import stem_oracle as O
+    G, aa, xo = state
+    t0 = time.perf_counter()
+    img, st = O.patch_image(G, aa, xo, nthreads=threads)
+    return img, time.perf_counter() - t0, st
+
+
+def hbm_peak():
+    """The measured copy bandwidth of the GB300s (GB/s), else the fallback figure."""
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        return float(json.load(open(p))["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs)"
+    return 6800.0, "fallback 6.8 TB/s"
+
+
+# Path roofline of the imaging step (the algorithmic work of the reference's voxel loop,
+# counted from the oracle's and the kernel's identical accept counts):
+#   MUFU   3 per accepted pair (exp, sin, cos of Lib_DynamicalTwoBeamImaging.f90:1877-1892)
+#          + 1 per voxel (the normalisation's rsqrt)
+#   FP32   12 per accepted pair + 6 per voxel (normalisation) + 10 per voxel (density, with
+#          -density) + 90 per voxel and precession angle (the RK4 double step, :2389-2464)
+#   FP64   30 per kept atom (findGdotR's transform, g.r and its reduction)
+#   HBM    24 B per atom + 16 B per kept atom + 8 B per pixel
+# T_roof = max over the four resources of (work / measured peak); frac = T_roof / time.
+def path_roofline(peaks, n_acc, n_kept, n_atoms, voxels, voxel_prec, pixels, density, t_ms):
+    if not peaks:
+        return None
+    hbm_gbs, _ = hbm_peak()
+    ex2, sin = peaks["mufu_ex2_gops"] * 1e9, peaks["mufu_sin_gops"] * 1e9
+    t_mufu = (n_acc + voxels) / ex2 + 2.0 * n_acc / sin
+    w_fp32 = 12.0 * n_acc + (16.0 if density else 6.0) * voxels + 90.0 * voxel_prec
+    t_fp32 = w_fp32 / (peaks["fp32_tflops"] * 1e12)
+    t_fp64 = 30.0 * n_kept / (peaks["fp64_tflops"] * 1e12)
+    w_hbm = 24.0 * n_atoms + 16.0 * n_kept + 8.0 * pixels
+    t_hbm = w_hbm / (hbm_gbs * 1e9)
+    res = {"mufu": t_mufu, "fp32": t_fp32, "fp64": t_fp64, "hbm": t_hbm}
+    bound = max(res, key=res.get)
+    t_roof = res[bound]
+    t = t_ms * 1e-3
+    if bound == "mufu":
+        w, peak, unit = t_mufu * ex2, ex2, "Gop/s (MUFU, ex2-equivalent: sin and cos weighted by the ex2/sin rates)"
+        scale = 1e9
+    elif bound == "fp32":
+        w, peak, unit, scale = w_fp32, peaks["fp32_tflops"] * 1e12, "TFLOP/s", 1e12
+    elif bound == "fp64":
+        w, peak, unit, scale = 30.0 * n_kept, peaks["fp64_tflops"] * 1e12, "TFLOP/s", 1e12
+    else:
+        w, peak, unit, scale = w_hbm, hbm_gbs * 1e9, "GB/s", 1e9
+    return {"bound": bound, "achieved": w / t / scale, "peak": peak / scale, "unit": unit, "frac": t_roof / t,
+            "t_roof_ms": t_roof * 1e3, "t_ms": t_ms,
+            "per_resource_ms": {k: v * 1e3 for k, v in res.items()},
+            "work": {"accepted_pairs": n_acc, "kept_atoms": n_kept, "atoms": n_atoms, "voxels": voxels,
+                     "voxel_precession_passes": voxel_prec, "pixels": pixels, "density": bool(density),
+                     "mufu_ops": 3.0 * n_acc + voxels, "fp32_flop": w_fp32, "fp64_flop": 30.0 * n_kept,
+                     "hbm_bytes": w_hbm}}
+
+
 SWEEP_G = ((1, 1, 0), (2, 0, 0), (2, 1, 1))
 # DRAM bytes (read + write) of one k_column_fp32_v2 launch on the 1.2M-atom image, from an
 # ncu capture of `python bench.py --ncu-case fp32` (61.15 MB read + 2.89 MB written)
@@ -81,12 +167,12 @@ def sweep_specs(cell, n_tomo=41, n_prec=16, gs=SWEEP_G):
     return x0, specs
 
 
-def uneven_specs():
+def uneven_specs(cells=None):
     """256 independent bcc Fe cells, atom counts log-uniform in [10k, 500k] before voids,
     aspect ratios U(0.5, 2), Poisson(10) voids of radius U(4, 20) A, s_g ~ U(-0.02, 0.02)."""
     from simulated_tem_gb300 import imaging, synth
     out = []
-    for cell, sg in synth.uneven_cells():
+    for cell, sg in (cells if cells is not None else synth.uneven_cells()):
         t, x, _ = imaging.d2bi_condition(cell.a_super, synth.A0_FE, (0, 0, 1), (1, 1, 0), cell.pos, sg=sg,
                                          xi0=103.9, xig=207.5, V=200.0, M=(4, 4))
         G, aa = t.image_geometry(len(x))
@@ -95,12 +181,13 @@ def uneven_specs():
 
 
 def time_batch(ctx, jobs, flags, stream, steps, warmup, flush):
-    """CUDA-event time of st_batch_device over `jobs`, L2 flushed before each call."""
+    """CUDA-event time of st_batch_device over `jobs`, L2 flushed before each call; also the
+    library's own per-call stage times (binning, columns) of the same timed calls."""
     import torch
     sptr = stream.cuda_stream
     for _ in range(warmup):
         ctx.batch_device(jobs, flags, sptr)
-    ms = []
+    ms, bins, cols = [], [], []
     for i in range(steps):
         flush.fill_(float(i))
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -109,6 +196,12 @@ def time_batch(ctx, jobs, flags, stream, steps, warmup, flush):
         e1.record(stream)
         torch.cuda.synchronize()
         ms.append(e0.elapsed_time(e1))
+        st = ctx.stats()
+        bins.append(st.ms_bin)
+        cols.append(st.ms_column)
+    time_batch.stages = {"ms_bin": float(np.mean(bins)), "ms_column": float(np.mean(cols)),
+                         "note": "mean over the timed calls of the library's CUDA events around the binning "
+                                 "(with the image clears) and the column phase (column kernels and epilogues)"}
     return ms
 
 
@@ -134,22 +227,53 @@ def time_plan(ctx, jobs, flags, stream, steps, warmup, flush):
     return ms
 
 
-def batched_legs(ctx, cell, stream, flush, steps, warmup):
-    """The two batched workloads through st_batch_device: the tilt x precession x g
-    sweep on the 1.2M-atom cell and the 256-cell uneven batch, FP32 path; for each,
-    one image is recomputed on the plain FP64 path for the accuracy figure."""
+def oracle_band(cell, g, sg, n_prec, rows=None, n_tomo=1, step=0, threads=None):
+    """The oracle's image of one condition (the precession average), whole or on a band of
+    pixel rows, on all host threads: the checker of the batched legs."""
+    from oracle import stem_oracle as O
+    from simulated_tem_gb300 import synth
+    args = O.make_args(cell.a_super, synth.A0_FE, (0, 0, 1), g, sg=sg, xi0=103.9, xig=207.5, nTomo=n_tomo,
+                       tomoAngle=20.0)
+    so, xo, _ = O.setup(args, cell.pos, nn=step)
+    Go, aao = O.geometry(so, len(xo), nPrec=n_prec, precAngle=0.005)
+    img, _ = O.patch_image(Go, aao, xo, rows=rows, nthreads=threads or os.cpu_count() or 1)
+    return img / n_prec
+
+
+def vs_oracle(got, want, rows=None):
+    sl = slice(None) if rows is None else slice(rows[0], rows[1])
+    d = got[:, sl] - want[:, sl]
+    return {"max_abs_dI": float(np.abs(d).max()), "rms_dI": float(np.sqrt((d ** 2).mean())),
+            "pixels": int(d.size), "reference": "oracle (FP64 C restatement of computeD2BI_img)"}
+
+
+def batched_legs(ctx, cell, stream, flush, steps, warmup, peaks=None, cpu=True):
+    """The two batched workloads through st_batch_device: the tilt x precession x g sweep on
+    the 1.2M-atom cell and the 256-cell uneven batch, FP32 path.  Accuracy against the oracle:
+    a band of pixel rows of one mid-series image of each g, and the largest uneven cell whole
+    (without host cores for the oracle: against the plain FP64 GPU path)."""
     import torch
 
     from simulated_tem_gb300 import _lib
     out = {}
     f32 = _lib.ST_FLAG_FP32 | _lib.ST_FLAG_AVERAGE
 
-    def accuracy(G, x_ptr, n, aa, img):
+    def fp64_gpu(G, x_ptr, n, aa):
         ref = torch.empty((G.My, G.Mx), dtype=torch.float64, device="cuda")
         ctx.image_device(G, x_ptr, n, aa, _lib.ST_FLAG_AVERAGE, ref.data_ptr(), stream=stream.cuda_stream)
         torch.cuda.synchronize()
-        d = (img - ref).abs()
-        return {"max_abs_dI_fp32_vs_fp64": float(d.max()), "rms_dI_fp32_vs_fp64": float(d.pow(2).mean().sqrt())}
+        return ref.cpu().numpy().T
+
+    def roof(st, specs_g, t_col, t_batch, n_atoms):
+        vox = sum((G.ix1 - G.ix0) * (G.iy1 - G.iy0) * G.Mz for G in specs_g[0])
+        vp = sum((G.ix1 - G.ix0) * (G.iy1 - G.iy0) * G.Mz * n for G, n in zip(*specs_g))
+        pix = sum((G.ix1 - G.ix0) * (G.iy1 - G.iy0) for G in specs_g[0])
+        r = path_roofline(peaks, st.n_accepted, st.n_kept, n_atoms, vox, vp, pix, False, t_col)
+        if r:
+            r["kernel"] = "k_column_fp32_v2 (every column launch of the batch)"
+            r["frac_batch"] = r["t_roof_ms"] / t_batch
+            r["executed"] = {"tests": st.n_tests, "tests_per_voxel": st.n_tests / max(vox, 1)}
+        return r
 
     # tilt x precession x g sweep: set up on the host condition by condition (the atoms
     # wrapped and their extents taken for every image), and on the GPU (wrapped once, the
@@ -168,22 +292,38 @@ def batched_legs(ctx, cell, stream, flush, steps, warmup):
     same = same and bool(np.array_equal(d_x.cpu().numpy(), x))
     imgs = [torch.empty((G.My, G.Mx), dtype=torch.float64, device="cuda") for G, _ in specs]
     jobs = [(G, d_x.data_ptr(), len(x), aa, im.data_ptr()) for (G, aa), im in zip(specs, imgs)]
-    ms = time_batch(ctx, jobs, f32 | _lib.ST_FLAG_STATS, stream, 1, 0, flush)  # statistics
+    time_batch(ctx, jobs, f32 | _lib.ST_FLAG_STATS, stream, 1, 0, flush)  # counts for the roofline
     st = ctx.stats()
     ms = time_batch(ctx, jobs, f32, stream, steps, warmup, flush)
+    stages = dict(time_batch.stages)
+    launches = ctx.stats().n_launches
     t = float(np.mean(ms)) * 1e-3
     n_img, n_pass = len(specs), sum(len(aa) for _, aa in specs)
     vs = sum((G.ix1 - G.ix0) * (G.iy1 - G.iy0) * G.Mz * len(aa) for G, aa in specs)
-    k = len(specs) // (2 * len(SWEEP_G))  # a mid-series tilt of g = 110
-    G, aa = specs[k]
+    # one mid-series tilt of each g against the oracle (a band of rows; FP32 bar 1e-4)
+    acc = {}
+    for gi, g in enumerate(SWEEP_G):
+        k = gi * 41 + 20
+        G, aa = specs[k]
+        got = imgs[k].cpu().numpy().T
+        if cpu:
+            mid = (G.iy0 + G.iy1) // 2
+            rows = (mid - 8, mid + 8)
+            want = oracle_band(cell, g, 0.01, 16, rows=rows, n_tomo=41, step=20)
+            acc["g%d%d%d" % g] = vs_oracle(got, want, rows)
+        else:
+            acc["g%d%d%d" % g] = vs_oracle(got, fp64_gpu(G, d_x.data_ptr(), len(x), aa))
+            acc["g%d%d%d" % g]["reference"] = "plain FP64 GPU path"
     out["sweep"] = {"workload": "1.2M-atom cell: 41 tilts over +-20 deg x 16 precession angles (5 mrad) x "
                                 "g in {110, 200, 211}, FP32, images averaged over precession",
                     "images": n_img, "integration_passes": n_pass, "images_per_s": n_img / t,
                     "passes_per_s": n_pass / t, "voxel_slices_per_s": vs / t, "ms_per_batch": t * 1e3,
                     "steps": steps, "image_sizes": sorted({(G_.Mx, G_.My, G_.Mz) for G_, _ in specs}),
-                    "kept_atoms": st.n_kept, "column_kernel": st.column_kernel,
-                    "ms_bin": st.ms_bin, "ms_column": st.ms_column,
-                    "accuracy_one_image": accuracy(G, d_x.data_ptr(), len(x), aa, imgs[k]),
+                    "kept_atoms": st.n_kept, "column_kernel": st.column_kernel, "stages": stages,
+                    "launches_per_batch": launches,
+                    "roofline": roof(st, ([G_ for G_, _ in specs], [len(aa_) for _, aa_ in specs]),
+                                     stages["ms_column"], t * 1e3, len(x) * n_img),
+                    "accuracy_tilt20_per_g": acc,
                     "setup": {"host_s": setup_host, "device_s": setup_dev, "same_geometry": same,
                               "images_per_s_with_device_setup": n_img / (t + setup_dev),
                               "note": "set-up of the 123 geometries: host (wrap and extents per image) vs "
@@ -195,24 +335,36 @@ def batched_legs(ctx, cell, stream, flush, steps, warmup):
     del imgs, jobs
 
     # 256 independent cells of uneven size
-    specs = uneven_specs()
+    cells = synth.uneven_cells()
+    specs = uneven_specs(cells)
     d_xs = [torch.from_numpy(np.ascontiguousarray(x_)).cuda() for _, _, x_ in specs]
     imgs = [torch.empty((G.My, G.Mx), dtype=torch.float64, device="cuda") for G, _, _ in specs]
     jobs = [(G, dx.data_ptr(), len(x_), aa, im.data_ptr()) for (G, aa, x_), dx, im in zip(specs, d_xs, imgs)]
     time_batch(ctx, jobs, f32 | _lib.ST_FLAG_STATS, stream, 1, 0, flush)
     st = ctx.stats()
     ms = time_batch(ctx, jobs, f32, stream, steps, warmup, flush)
+    stages = dict(time_batch.stages)
+    launches = ctx.stats().n_launches
     t = float(np.mean(ms)) * 1e-3
     vs = sum((G.ix1 - G.ix0) * (G.iy1 - G.iy0) * G.Mz for G, _, _ in specs)
     k = int(np.argmax([len(x_) for _, _, x_ in specs]))
     G, aa, x_ = specs[k]
+    got = imgs[k].cpu().numpy().T
+    if cpu:
+        cell_k, sg_k = cells[k]
+        acc = vs_oracle(got, oracle_band(cell_k, (1, 1, 0), sg_k, 1))
+    else:
+        acc = vs_oracle(got, fp64_gpu(G, d_xs[k].data_ptr(), len(x_), aa))
+        acc["reference"] = "plain FP64 GPU path"
     out["uneven"] = {"workload": "256 bcc Fe cells, atoms log-uniform in [10k, 500k] before voids, aspect U(0.5, 2), "
                                  "Poisson(10) voids of radius U(4, 20) A, s_g U(-0.02, 0.02), FP32",
                      "images": len(specs), "atoms": int(sum(len(x_) for _, _, x_ in specs)),
                      "images_per_s": len(specs) / t, "voxel_slices_per_s": vs / t, "ms_per_batch": t * 1e3,
-                     "steps": steps, "kept_atoms": st.n_kept, "column_kernel": st.column_kernel,
-                     "ms_bin": st.ms_bin, "ms_column": st.ms_column,
-                     "accuracy_largest_cell": accuracy(G, d_xs[k].data_ptr(), len(x_), aa, imgs[k])}
+                     "steps": steps, "kept_atoms": st.n_kept, "column_kernel": st.column_kernel, "stages": stages,
+                     "launches_per_batch": launches,
+                     "roofline": roof(st, ([G_ for G_, _, _ in specs], [1] * len(specs)), stages["ms_column"],
+                                      t * 1e3, sum(len(x_) for _, _, x_ in specs)),
+                     "accuracy_largest_cell": acc}
     return out
 
 
@@ -690,7 +842,7 @@ def run_gpu(args):
     if ws > 1:
         torch.distributed.barrier()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    col_ms = []
+    col_ms, launches = [], 0
     with ClockSampler(local) as clk:
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -699,11 +851,15 @@ def run_gpu(args):
             ev[i][0].record(stream)
             step()
             ev[i][1].record(stream)
-            col_ms.append(ctx.stats().ms_column)
+            st_i = ctx.stats()
+            col_ms.append(st_i.ms_column)
+            launches += st_i.n_launches
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
+        peaks = measure_fp32_peak()
         batched = None if args.no_batched else batched_legs(ctx, cell, stream, flush, args.batch_steps,
-                                                             args.warmup)
+                                                             args.warmup, peaks=peaks,
+                                                             cpu=(rank == 0 and not args.no_cpu))
         cfg1 = None if args.no_batched else cfg1_leg(ctx, stream, flush, 5, args.warmup,
                                                       cpu=(rank == 0 and not args.no_cpu))
         cfg5 = None if args.no_batched else cfg5_leg(ctx, stream, flush, 3, args.warmup)
@@ -759,23 +915,29 @@ def run_gpu(args):
     img64 = d_img.cpu().numpy().T.copy()
     d = img32 - img64
 
-    peaks = measure_fp32_peak()
     V = (G.ix1 - G.ix0) * (G.iy1 - G.iy0) * G.Mz
-    c_tests = reference_candidate_tests(ctx, G, x)
-    flops = 8.0 * c_tests + 6.0 * n_acc + 20.0 * V + 165.0 * (G.Mz // 2) * (G.Mx * G.My) * n_prec
     col_avg = float(np.mean(col_ms))
-    achieved = flops / (col_avg * 1e-3) / 1e12
-    roof = {"bound": "fp32", "kernel": "k_column_fp32_v2", "achieved": achieved,
-            "peak": peaks["fp32_tflops"] if peaks else None, "unit": "TFLOP/s",
-            "frac": achieved / peaks["fp32_tflops"] if peaks else None,
-            "peak_source": "measured live: FP32 FMA-pipe microbenchmark (libstem_peaks.so) on this GPU",
-            "traffic": COLUMN_TRAFFIC_BYTES, "traffic_unit": "bytes per launch",
-            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_column_fp32_v2 on this "
-                              "image (profiles/k_column_fp32_v2_1p2m_screw.md)",
-            "algorithmic": {"flops_per_image": flops, "c_tests": c_tests, "accepted_pairs": n_acc,
-                            "voxels": V, "kept_atoms": n_kept, "kernel_ms": col_avg,
-                            "kernel_tests_per_voxel": n_tst / V, "reference_tests_per_voxel": c_tests / V,
-                            "formula": "8*C_tests + 6*accepted + 20*V + 165*(Mz/2)*Mx*My*nPrec"}}
+    pix = (G.ix1 - G.ix0) * (G.iy1 - G.iy0)
+    roof = path_roofline(peaks, n_acc, n_kept, len(x), V, V * n_prec, pix, False, col_avg)
+    if roof:
+        c_tests = reference_candidate_tests(ctx, G, x)
+        roof.update({"kernel": "k_column_fp32_v2",
+                     "peak_source": "measured live in this run by the project's pipe microbenchmarks "
+                                    "(libstem_peaks.so: FP32 FMA, FP64 FMA, MUFU ex2 and sin); HBM from "
+                                    + hbm_peak()[1],
+                     "traffic": COLUMN_TRAFFIC_BYTES, "traffic_unit": "bytes per launch",
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_column_fp32_v2 on "
+                                       "this image (profiles/k_column_fp32_v2_1p2m_screw.md)",
+                     "frac_step": roof["t_roof_ms"] / ms,
+                     "executed": {"tests": n_tst, "tests_per_voxel": n_tst / V,
+                                  "reference_tests_per_voxel": c_tests / V,
+                                  "accepted_per_voxel": n_acc / V,
+                                  "ex2_issued": n_tst, "ex2_frac_of_peak":
+                                      n_tst / (col_avg * 1e-3) / (peaks["mufu_ex2_gops"] * 1e9),
+                                  "note": "work the kernel executes: every candidate test (a slab-ring slice "
+                                          "pair counts two) issues one ex2; the reference's own 27-cell search "
+                                          "tests reference_tests_per_voxel candidates per voxel"}})
+    acc = {"max_abs_dI_fp32_vs_fp64": float(np.abs(d).max()), "rms_dI_fp32_vs_fp64": float(np.sqrt((d ** 2).mean()))}
     line = {"metric": METRIC, "value": value, "unit": "images/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded bcc Fe cell, no dataset)",
@@ -787,24 +949,24 @@ def run_gpu(args):
             "fp64": {"value": 1000.0 / fp64_ms, "unit": "images/s", "ms": fp64_ms},
             "plan": {"value": plan_value, "unit": "images/s",
                      "note": "the same step recorded once as a CUDA graph (st_plan) and replayed"},
-            "accuracy": {"max_abs_dI_fp32_vs_fp64": float(np.abs(d).max()),
-                         "rms_dI_fp32_vs_fp64": float(np.sqrt((d ** 2).mean()))},
-            "gpu_launches": args.steps * launches_per_image(n_prec, fp32=True, average=True),
+            "accuracy": acc,
+            "gpu_launches": launches,
             "roofline": roof, "peaks": peaks, "wall_s": wall, "clocks": clk.summary(), "batched": batched, "cfg1_128k": cfg1, "cfg5_corrector": cfg5,
             "output_files": io, "input_file": inp, "tilt_search": tilt}
     if rank == 0:
         if ws == 1 and not args.no_cpu:
-            line["cpu_baseline"] = cpu_baseline(x_state=(cell, t, x), rows=args.cpu_rows)
+            from simulated_tem_gb300 import synth
+            cb, want = cpu_baseline(cell, synth.A0_FE)
+            line["cpu_baseline"] = cb
+            for name, img in (("fp32", img32), ("fp64", img64)):
+                r = vs_oracle(img, want)
+                acc["max_abs_dI_%s_vs_oracle" % name] = r["max_abs_dI"]
+                acc["rms_dI_%s_vs_oracle" % name] = r["rms_dI"]
+            acc["reference"] = "oracle (FP64 C restatement of computeD2BI_img), whole image, %d pixels" % want.size
         print(json.dumps(line), flush=True)
     ctx.close()
     if ws > 1:
         torch.distributed.destroy_process_group()
-
-
-def launches_per_image(n_prec, fp32, average):
-    width = 16 if fp32 else 4
-    passes = (n_prec + width - 1) // width
-    return 6 + passes + (1 if average else 0)  # transform, 3 scans, place, finalize; columns; epilogue
 
 
 def reference_candidate_tests(ctx, G, x):
@@ -849,53 +1011,46 @@ def _bin_counts(G, x):
     return counts
 
 
-def cpu_baseline(x_state=None, rows=48, threads=None):
-    """The oracle (C restatement of the reference) on all host cores, on a band of
-    pixel rows of the same image; extrapolated to whole images."""
-    from oracle import stem_oracle as O
-    from simulated_tem_gb300 import synth
-    cell, _, _ = x_state if x_state else (synth.screw_cell_1p2m(), None, None)
+def cpu_baseline(cell, A0, threads=None):
+    """The oracle (C restatement of the reference's computeD2BI_img) on all host cores, one
+    whole image, binning included; also returns the image (the accuracy reference)."""
     threads = threads or os.cpu_count() or 1
-    args = O.make_args(cell.a_super, synth.A0_FE, (0, 0, 1), (1, 1, 0), sg=0.01, xi0=103.9, xig=207.5)
-    so, xo, _ = O.setup(args, cell.pos)
-    G, aa = O.geometry(so, len(xo))
-    mid = (G.iy0 + G.iy1) // 2
-    r1 = max(1, rows // 4)
-    t0 = time.perf_counter()
-    O.patch_image(G, aa, xo, rows=(mid, mid + r1), nthreads=threads)
-    ta = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    O.patch_image(G, aa, xo, rows=(mid, mid + rows), nthreads=threads)
-    tb = time.perf_counter() - t0
-    per_row = max((tb - ta) / (rows - r1), 1e-9)
-    t_bin = max(ta - r1 * per_row, 0.0)
-    t_img = t_bin + per_row * (G.iy1 - G.iy0)
-    return {"value": 1.0 / t_img, "unit": "images/s", "cores": threads, "kind": "port",
-            "sample": "oracle C restatement of computeD2BI_img, binning + %d pixel rows of %d (566 columns each, "
-                      "240 voxels deep), extrapolated: %.2f s per image (binning %.2f s)" % (rows, G.iy1 - G.iy0,
-                                                                                            t_img, t_bin),
-            "seconds_measured": ta + tb}
+    img, s, st = oracle_workload_image(oracle_workload_setup(cell, A0), threads)
+    return {"value": 1.0 / s, "unit": "images/s", "cores": threads, "kind": "port",
+            "sample": "one whole 1.2M-atom image (566 x 566 x 240 voxels, binning included) by the oracle's C "
+                      "restatement of computeD2BI_img on %d host threads: %.2f s" % (threads, s),
+            "seconds_measured": s, "accepted_pairs": st.n_accepted}, img
 
 
 def run_reference(args):
+    """The reference's algorithm on the host cores (the reference's Fortran cannot be built on
+    either machine, so the oracle's C restatement of it runs), whole images, all host threads.
+    Nothing of the product is imported or loaded: the cell comes from the generator module
+    loaded by its file path, the geometry and the image from the oracle."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return
     from oracle import stem_oracle as O
     O.build() if not os.path.exists(O.LIB_PATH) else None
-    cell, t, x, _ = workload()
-    vals = []
+    synth = standalone_synth()
+    cell = synth.screw_cell_1p2m()
+    threads = os.cpu_count() or 1
+    state = oracle_workload_setup(cell, synth.A0_FE)
+    secs = []
     for i in range(args.warmup + args.steps):
-        cb = cpu_baseline(x_state=(cell, t, x), rows=args.cpu_rows)
+        _, s, _ = oracle_workload_image(state, threads)
         if i >= args.warmup:
-            vals.append(1.0 / cb["value"])
-    s_per_img = float(np.mean(vals))
+            secs.append(s)
+    s_per_img = float(np.mean(secs))
     value = 1.0 / s_per_img
-    cb["value"] = value
+    cb = {"value": value, "unit": "images/s", "cores": threads, "kind": "port",
+          "sample": "whole 1.2M-atom images (566 x 566 x 240 voxels, binning included), one per step, by the "
+                    "oracle's C restatement of computeD2BI_img on %d host threads; min %.2f s, max %.2f s"
+                    % (threads, min(secs), max(secs))}
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "images/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": s_per_img * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded bcc Fe cell)",
-            "config": {"workload": WORKLOAD, "atoms": len(x),
+            "config": {"workload": WORKLOAD, "atoms": len(cell.pos),
                        "note": "reference Fortran is not buildable here (no Fortran compiler on either machine); "
                                "the oracle C restatement of its algorithm runs on all host cores"},
             "cpu_baseline": cb,
@@ -963,7 +1118,6 @@ def main():
     ap.add_argument("--steps", type=int, default=60)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--cpu-rows", type=int, default=48)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched sweep and uneven-cell legs")
     ap.add_argument("--batch-steps", type=int, default=3)

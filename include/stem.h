@@ -90,7 +90,7 @@ typedef struct st_stats {
   int32_t column_kernel; /* 1 general FP32, 2 slab-ring FP32 (for at least one image), 3 FP64 */
   int32_t ring_variant;  /* occupancy variant of the last slab-ring launch, -1 if none ran */
   int32_t ring_slab_atoms; /* staging capacity per slab of the last slab-ring launch (0 if none ran) */
-  int32_t pad0;
+  int32_t n_launches;    /* kernels the call launched (all attempts; autotuning trials included) */
 } st_stats;
 
 /* Context on CUDA device `device` (made current for the calls). */

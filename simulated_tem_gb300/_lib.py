@@ -48,7 +48,7 @@ class StStats(ctypes.Structure):
     _fields_ = [("n_atoms", _i64), ("n_kept", _i64), ("n_tests", _i64), ("n_accepted", _i64),
                 ("n_voxels", _i64), ("max_cell_count", _i32), ("n_prec", _i32), ("ms_bin", _d),
                 ("ms_column", _d), ("column_kernel", _i32), ("ring_variant", _i32), ("ring_slab_atoms", _i32),
-                ("pad0", _i32)]
+                ("n_launches", _i32)]
 
 
 class StJob(ctypes.Structure):

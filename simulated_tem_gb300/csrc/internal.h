@@ -141,6 +141,13 @@ __device__ __forceinline__ bool tile_wanted(const ColumnParams& p, int tx, int t
 // candidates [0, total_cand) and cells [0, total_cells) concatenated in job order.
 // fp32: the FP32 path's records (Rec32); else the FP64 path's, in the reference's rounded
 // arithmetic.
+// Kernels the imaging path has launched on this host thread; run_images resets it per
+// call and reports the count in st_stats.n_launches.
+inline int& launch_count() {
+  static thread_local int n = 0;
+  return n;
+}
+
 cudaError_t launch_bin(const BinParams* d_jobs, int n_jobs, int64_t total_atoms, int64_t total_cand,
                        int64_t total_cells, int64_t cap, Scratch& s, BinnedAtoms& b, bool fp32, cudaStream_t st);
 cudaError_t launch_bin_finalize(const BinParams* d_jobs, int n_jobs, int64_t total_cells, int64_t cap, Scratch& s,

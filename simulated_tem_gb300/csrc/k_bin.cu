@@ -462,6 +462,7 @@ cudaError_t launch_bin(const BinParams* d_jobs, int n_jobs, int64_t total_atoms,
     k_bin_transform_exact<<<grid_for(total_cand, 256, sms * 16), 256, 0, st>>>(
         d_jobs, n_jobs, total_cand, cap, b.cell_count, s.tmp_key, s.tmp_cell, s.tmp_slot, s.tmp_f, s.counters);
   const int nb = (int)((total_cells + kScanBlock - 1) / kScanBlock);
+  launch_count() += 5;  // the kernel above, three scans and the placement
   k_scan_blocks<<<nb, 256, 0, st>>>(b.cell_count, total_cells, s.block_sums, s.counters);
   k_scan_top<<<1, 1024, 0, st>>>(s.block_sums, nb);
   k_scan_final<<<nb, 256, 0, st>>>(b.cell_count, total_cells, s.block_sums, b.cell_start);
@@ -476,6 +477,7 @@ cudaError_t launch_bin_finalize(const BinParams* d_jobs, int n_jobs, int64_t tot
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int grid = grid_for(cap, 256, sms * 8);  // the kernel reads the kept count on the device
+  ++launch_count();
   if (fp32)
     k_bin_finalize<true><<<grid, 256, 0, st>>>(d_jobs, n_jobs, b.cell_start, b.cell_count, s.perm, s.tmp_key,
                                                s.tmp_cell, s.tmp_f, b, s.counters, cap);

@@ -619,6 +619,7 @@ cudaError_t launch_cols(K kernel, const ColumnParams& p, size_t smem, cudaStream
   const int grid = (tiles + kWarps - 1) / kWarps;
   cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
+  ++launch_count();
   kernel<<<grid, kWarps * 32, smem, st>>>(p);
   return cudaGetLastError();
 }
@@ -663,6 +664,7 @@ __global__ void k_epilogue(double* img, int Mx, int ix0, int ix1, int iy0, int i
 cudaError_t launch_epilogue(double* img, int Mx, int My, int ix0, int ix1, int iy0, int iy1, double scale,
                             int bright, cudaStream_t st) {
   (void)My;
+  ++launch_count();
   k_epilogue<<<256, 256, 0, st>>>(img, Mx, ix0, ix1, iy0, iy1, scale, bright);
   return cudaGetLastError();
 }

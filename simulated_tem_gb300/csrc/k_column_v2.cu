@@ -502,6 +502,7 @@ cudaError_t launch(K kernel, const ColumnJob* jobs, int n_jobs, int total_tiles,
   const int need = (total_tiles + kWarps - 1) / kWarps;
   if (grid > need) grid = need;
   if (grid < 1) grid = 1;
+  ++launch_count();
   kernel<<<grid, kWarps * 32, smem, st>>>(jobs, n_jobs, total_tiles, work, counters, cap);
   return cudaGetLastError();
 }

@@ -396,6 +396,7 @@ struct GraphOut {
 int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStream_t st, GraphOut* gout = nullptr) {
   const int n = (int)jobs.size();
   const bool fp32 = (flags & ST_FLAG_FP32) != 0;
+  launch_count() = 0;
   // concatenation offsets
   std::vector<int64_t> cand_base(n + 1, 0), cell_base(n + 1, 0), atom_base(n + 1, 0);
   std::vector<size_t> xoff(n + 1, 0), yoff(n + 1, 0), zoff(n + 1, 0), aoff(n + 1, 0);
@@ -724,6 +725,7 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
     break;
   }
   const bool used_ring = ring_ok;
+  const int n_launches = launch_count();  // before the graph recording, which launches nothing now
   if (gout) {
     // record the same work as a CUDA graph for replay (st_plan)
     if (gout->exec) cudaGraphExecDestroy(gout->exec);
@@ -761,6 +763,7 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
   S.column_kernel = c->last_column_kernel;
   S.ring_variant = used_ring ? c->last_ring_variant : -1;
   S.ring_slab_atoms = used_ring && !ring_jobs.empty() ? (big == 0 ? 128 : big == 1 ? 192 : 256) : 0;
+  S.n_launches = n_launches;
   // the reference stops when a link cell needs more than 16 x nMax0 slots; a batch's
   // largest cell is checked against the smallest nMax0 of its images
   int min_nmax0 = 0;
@@ -906,6 +909,7 @@ int run_batch(st_ctx* c, const std::vector<Job>& js, int32_t flags, cudaStream_t
     total.ms_bin += S.ms_bin;
     total.ms_column += S.ms_column;
     total.column_kernel = std::max(total.column_kernel, S.column_kernel);
+    total.n_launches += S.n_launches;
     first = last;
   }
   c->stats = total;
@@ -1050,6 +1054,7 @@ void plan_sum_stats(st_plan* p) {
     t.column_kernel = std::max(t.column_kernel, S.column_kernel);
     t.ring_variant = std::max(t.ring_variant, S.ring_variant);
     t.ring_slab_atoms = std::max(t.ring_slab_atoms, S.ring_slab_atoms);
+    t.n_launches += S.n_launches;
   }
   p->stats = t;
 }
