@@ -154,23 +154,53 @@ cudaError_t launch_bin_finalize(const BinParams* d_jobs, int n_jobs, int64_t tot
                                 BinnedAtoms& b, bool fp32, cudaStream_t st);
 cudaError_t launch_column_fp32(const ColumnParams& p, cudaStream_t st);
 
-// A job of the persistent slab-ring FP32 column kernel: an image and the first
-// warp tile it owns in the batch's tile sequence.
+// A job of the persistent slab-ring FP32 column kernels: an image and the first warp
+// tile it owns in the batch's tile sequence, for each tile shape (8 x 4, 4 x 8, 16 x 2).
+constexpr int kRingShapes = 3;
 struct ColumnJob {
   ColumnParams p;
-  int tile_base;
+  int tile_base[kRingShapes];
   int pad;
 };
-int column_tiles(const ColumnParams& p);
-// `variant` selects the register budget (occupancy) of the launch, 0 .. ring_variant_count() - 1;
-// `slab_tier` 0, 1, 2 stages up to 128, 192, 256 atoms per slab (dense footprints).  Every
-// variant computes the same image to the last bit.  `masked`: some jobs carry a tile mask
+int column_tiles(const ColumnParams& p, int shape = 0);  // warp tiles of one image in `shape`
+// The slab-ring launch.  `tiles`: the pass's warp tiles in each shape (host array).
+// `variant` 0 .. ring_variant_count() - 1 selects the kernel, its tile shape, slab
+// capacity and CTAs per SM (ring_variant_name); the images of different variants agree to
+// FP32 rounding, those of one variant (at any tier) to the last bit.  `slab_tier` 1, 2:
+// 192, 256 atoms per slab (dense footprints).  `masked`: some jobs carry a tile mask
 // (then max_np must be 1 and stats false).
-cudaError_t launch_column_fp32_ring(const ColumnJob* d_jobs, int n_jobs, int total_tiles, int max_np, bool density,
+cudaError_t launch_column_fp32_ring(const ColumnJob* d_jobs, int n_jobs, const int* tiles, int max_np, bool density,
                                     bool stats, int variant, int slab_tier, bool masked, unsigned* work,
                                     const unsigned long long* counters, int64_t cap, cudaStream_t st);
 int ring_variant_count();
+const char* ring_variant_name(int variant);
+int ring_variant_slab(int variant);  // atoms per slab of the variant's first tier
 int ring_np_bucket(int max_np);  // the kernel template (angles per pass) serving max_np angles
+// second-generation slab ring (k_column_v2.cu): occupancy variant v2 (0, 1), 8 x 4 tiles
+cudaError_t launch_column_fp32_ring_v2(const ColumnJob* d_jobs, int n_jobs, int total_tiles, int max_np, bool density,
+                                       bool stats, int v2, int slab_tier, bool masked, unsigned* work,
+                                       const unsigned long long* counters, int64_t cap, cudaStream_t st);
+namespace ring3 {
+// third generation (k_column_v3.cuh), one instance set per angle bucket NP
+struct Ring3Args {
+  const ColumnJob* jobs;
+  int n_jobs;
+  const int* tiles;  // per shape
+  bool density, stats, masked;
+  int variant, tier;
+  unsigned* work;
+  const unsigned long long* counters;
+  int64_t cap;
+  cudaStream_t st;
+};
+template <int NP>
+cudaError_t ring3_launch_np(const Ring3Args& a);
+extern template cudaError_t ring3_launch_np<1>(const Ring3Args&);
+extern template cudaError_t ring3_launch_np<2>(const Ring3Args&);
+extern template cudaError_t ring3_launch_np<4>(const Ring3Args&);
+extern template cudaError_t ring3_launch_np<8>(const Ring3Args&);
+extern template cudaError_t ring3_launch_np<16>(const Ring3Args&);
+}  // namespace ring3
 cudaError_t launch_column_fp64(const ColumnParams& p, cudaStream_t st);
 cudaError_t launch_epilogue(double* img, int Mx, int My, int ix0, int ix1, int iy0, int iy1, double scale,
                             int bright, cudaStream_t st);

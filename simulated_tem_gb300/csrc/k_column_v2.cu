@@ -474,18 +474,18 @@ __global__ void __launch_bounds__(kWarps * 32, kMinBlocks)
     int lo = 0, hi = n_jobs - 1;  // job of this tile
     while (lo < hi) {
       const int mid = (lo + hi + 1) >> 1;
-      if (jobs[mid].tile_base <= tile)
+      if (jobs[mid].tile_base[0] <= tile)
         lo = mid;
       else
         hi = mid - 1;
     }
     if constexpr (kMasked) {
       const ColumnParams& P = jobs[lo].p;
-      const int local = tile - jobs[lo].tile_base;
+      const int local = tile - jobs[lo].tile_base[0];
       const int tiles_x = (P.ix1 - P.ix0 + kTileX - 1) / kTileX;
       if (!tile_wanted(P, local % tiles_x, local / tiles_x, kTileX, kTileY)) continue;
     }
-    if (!column_tile<NP, kDensity, kStats, CAPS>(jobs[lo].p, W, tile - jobs[lo].tile_base, lane)) break;
+    if (!column_tile<NP, kDensity, kStats, CAPS>(jobs[lo].p, W, tile - jobs[lo].tile_base[0], lane)) break;
   }
 }
 
@@ -543,19 +543,9 @@ cudaError_t launch_np(int np, int v, int big, const ColumnJob* jobs, int n_jobs,
 
 }  // namespace
 
-int column_tiles(const ColumnParams& p) {
-  const int Wd = p.ix1 - p.ix0, Hd = p.iy1 - p.iy0;
-  if (Wd <= 0 || Hd <= 0) return 0;
-  return ((Wd + kTileX - 1) / kTileX) * ((Hd + kTileY - 1) / kTileY);
-}
-
-int ring_variant_count() { return kVariants; }
-
-int ring_np_bucket(int max_np) { return max_np <= 1 ? 1 : max_np <= 2 ? 2 : max_np <= 4 ? 4 : max_np <= 8 ? 8 : 16; }
-
-cudaError_t launch_column_fp32_ring(const ColumnJob* d_jobs, int n_jobs, int total_tiles, int max_np, bool density,
-                                    bool stats, int variant, int slab_tier, bool masked, unsigned* work,
-                                    const unsigned long long* counters, int64_t cap, cudaStream_t st) {
+cudaError_t launch_column_fp32_ring_v2(const ColumnJob* d_jobs, int n_jobs, int total_tiles, int max_np, bool density,
+                                       bool stats, int variant, int slab_tier, bool masked, unsigned* work,
+                                       const unsigned long long* counters, int64_t cap, cudaStream_t st) {
   cudaMemsetAsync(work, 0, sizeof(unsigned), st);
   if (total_tiles <= 0) return cudaSuccess;
   if (masked) {  // tile-masked jobs: one precession angle, no statistics (the host sends others elsewhere)

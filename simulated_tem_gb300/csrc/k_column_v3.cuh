@@ -1,0 +1,672 @@
+// K2+K3, FP32, third generation: separable weights and a per-step candidate buffer.
+//
+// Same computation as k_column_fp32 / k_column_fp32_v2 (the pixel loop of
+// computeD2BI_img, Lib_DynamicalTwoBeamImaging.f90:1870-1900, with the neighbour
+// search of Lib_LinkCell3D.f90:1515-1605 and the integrator of :2316-2480).
+//
+// The slab ring of the second generation stays: one warp owns a patch of 32 pixel
+// columns (8 x 4, 4 x 8 or 16 x 2), one lane per column, advancing two depth slices
+// per step; the atoms of the link-cell slabs the march needs are staged in
+// warp-private shared memory, prefiltered to 3 sigma of the patch and ordered by z
+// bin.  What changes is how a step visits them:
+//
+// * Every column of a patch samples the same two depths, so everything that depends
+//   only on an atom and the depth is the same in all 32 lanes.  A cooperative pass
+//   (one candidate per lane) computes it once per atom and step: the z distances,
+//   the largest in-plane r^2 each slice still accepts (hmax_k = (3 sigma)^2 - dz_k^2,
+//   or -1 where the reference's 27-cell rule excludes the slab for that slice), and
+//   the z factor of the Gaussian times the atom's phasor, ex2(-dz_k^2) (cos, sin).
+// * The Gaussian is separable, exp(-r^2/2s^2) = exp(-dxy^2/2s^2) exp(-dz^2/2s^2), so a
+//   lane needs one ex2 per atom (its in-plane factor) for both slices, and the
+//   inclusive cutoff r^2 <= (3 sigma)^2 becomes dxy^2 <= hmax_k.
+// * The same pass drops atoms that no column of the patch accepts at either slice
+//   (distance to the patch's sample rectangle beyond sqrt(hmax)), so the lanes test
+//   the patch's sphere-dilated box instead of its cylinder-dilated one, and compacts
+//   the rest into a small per-warp buffer (ballot + popc, order kept) that all lanes
+//   then read with two 16-byte loads per atom.
+//
+// Per atom and lane: two loads, the in-plane distance (3 FP32 ops), one ex2, two
+// compares and two predicated FP32x2 multiply-adds (both slices' cos and sin).
+//
+// Precision: FP32 throughout the march, as in the second generation; the weight is the
+// product of two ex2 values (a few ulp), and the cutoff test compares dxy^2 with
+// (3 sigma)^2 - dz^2 instead of dxy^2 + dz^2 with (3 sigma)^2, so an atom within
+// rounding of the cutoff may be taken or left differently (as with any FP32 distance).
+// The images stay within the FP32 path's bar of the FP64 oracle.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cfloat>
+#include <type_traits>
+
+#include "internal.h"
+
+namespace stem {
+namespace ring3 {
+
+constexpr int kWarps = 4;
+constexpr int kRing = 4;    // resident slabs (unwrapped z cells u, slot u & 3)
+constexpr int kBins = 32;   // z bins per slab for the window lookup
+constexpr int kBuf = 64;    // per-step candidate buffer (flushed at 32)
+constexpr float kHuge = FLT_MAX;
+
+template <int CAPS>  // staged atoms per slab
+struct WarpSmem3 {
+  float4 p[kRing][CAPS];      // X', Y' (warp frame), z (own cell), cos -- lengths scaled by s
+  float s[kRing][CAPS];       // sin
+  int bin[kRing][kBins + 1];  // bin[b]: first atom of z bin b; bin[kBins] = count
+  int count[kRing];
+  float4 ba[kBuf];            // step buffer: X', Y', hmax_0, hmax_1
+  float4 be[kBuf];            // ex2(-dz_0^2) (cos, sin), ex2(-dz_1^2) (cos, sin)
+};
+
+__device__ __forceinline__ float ex2_approx(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+__device__ __forceinline__ int pos_mod(int a, int n) {
+  const int r = a % n;
+  return r < 0 ? r + n : r;
+}
+
+__device__ __forceinline__ int floor_div(int a, int n) { return (a >= 0) ? a / n : -((-a + n - 1) / n); }
+
+// Lengths inside the kernel are scaled by s = sqrt(log2(e) / (2 sigma^2)), so that the
+// Gaussian weight exp(-r^2 / (2 sigma^2)) is ex2(-r'^2) of the scaled distance r'.
+struct Geo {
+  int ux_lo, ux_hi, uy_lo, uy_hi, ux_ref, uy_ref;
+  float xmin, xmax, ymin, ymax, pre2;
+  float a11s, a22s, a33s, scale;
+};
+
+// Gather slab u (its cells in the patch footprint, atoms within 3 sigma of the
+// patch rectangle) into its ring slot and order it by z bin in place; false
+// when it holds more than CAPS atoms.
+template <int CAPS>
+__device__ bool load_slab3(const ColumnParams& p, const Geo& G, int u, WarpSmem3<CAPS>& W, int lane) {
+  const int cz = pos_mod(u, p.Ez);
+  const int slot = u & (kRing - 1);
+  float4* P = W.p[slot];
+  float* S = W.s[slot];
+  int n = 0;
+  for (int uy = G.uy_lo; uy <= G.uy_hi; ++uy) {
+    const int cy = pos_mod(uy, p.Ey);
+    const int64_t row_base = (int64_t)p.Ex * (cy + (int64_t)p.Ey * cz);
+    const float yoff = G.a22s * (float)(uy - G.uy_ref);
+    for (int ux = G.ux_lo; ux <= G.ux_hi;) {
+      const int k = floor_div(ux, p.Ex);
+      const int run_hi = min(G.ux_hi, (k + 1) * p.Ex - 1);
+      const int shift = k * p.Ex;
+      const int a_lo = p.cell_start[row_base + (ux - shift)];
+      const int a_hi = p.cell_start[row_base + (run_hi - shift) + 1];
+      for (int b = a_lo; b < a_hi; b += 32) {
+        const int j = b + lane;
+        bool keep = false;
+        float4 rec = make_float4(0.f, 0.f, 0.f, 0.f);
+        float sn = 0.f;
+        if (j < a_hi) {
+          const float4 r = p.p32[j];
+          const int packed = __float_as_int(r.w);
+          const int cxu = (packed & 1023) + shift;
+          const float X = fmaf(r.x, G.scale, G.a11s * (float)(cxu - G.ux_ref));
+          const float Y = fmaf(r.y, G.scale, yoff);
+          const float dx = fmaxf(0.f, fmaxf(G.xmin - X, X - G.xmax));
+          const float dy = fmaxf(0.f, fmaxf(G.ymin - Y, Y - G.ymax));
+          keep = dx * dx + dy * dy <= G.pre2;
+          const float2 cs = p.cs32[j];
+          rec = make_float4(X, Y, r.z * G.scale, cs.x);
+          sn = cs.y;
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, keep);
+        const int cnt = __popc(m);
+        if (n + cnt > CAPS) return false;
+        if (keep) {
+          const int d = n + __popc(m & ((1u << lane) - 1));
+          P[d] = rec;
+          S[d] = sn;
+        }
+        n += cnt;
+      }
+      ux = run_hi + 1;
+    }
+  }
+  __syncwarp();
+  // counting sort by z bin, in place: every lane first holds its atoms in registers;
+  // within a bin the gather order is kept (deterministic)
+  constexpr int kPer = CAPS / 32;
+  const float inv_bin = kBins / G.a33s;
+  int* hist = W.bin[slot];
+  for (int b = lane; b <= kBins; b += 32) hist[b] = 0;
+  __syncwarp();
+  float4 e[kPer];
+  float es[kPer];
+  int eb[kPer], er[kPer];
+  const unsigned lt = (1u << lane) - 1;
+#pragma unroll
+  for (int k = 0; k < kPer; ++k) {
+    const int i = lane + 32 * k;
+    const bool valid = i < n;
+    e[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+    es[k] = 0.f;
+    eb[k] = 0;
+    er[k] = 0;
+    const unsigned act = __ballot_sync(0xffffffffu, valid);
+    if (valid) {
+      e[k] = P[i];
+      es[k] = S[i];
+      eb[k] = min(kBins - 1, max(0, (int)floorf(e[k].z * inv_bin)));
+      const unsigned m = __match_any_sync(act, eb[k]);
+      er[k] = hist[eb[k]] + __popc(m & lt);
+      __syncwarp(act);
+      if ((m & lt) == 0) hist[eb[k]] += __popc(m);  // the group's first lane counts it
+    }
+    __syncwarp();
+  }
+  // exclusive scan of the 32 bin counts: bin starts, bin[kBins] = n
+  {
+    const int v = hist[lane];
+    int incl = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += t;
+    }
+    __syncwarp();
+    hist[lane] = incl - v;
+    if (lane == 0) hist[kBins] = n;
+  }
+  __syncwarp();
+#pragma unroll
+  for (int k = 0; k < kPer; ++k) {
+    if (lane + 32 * k < n) {
+      const int d = hist[eb[k]] + er[k];
+      P[d] = e[k];
+      S[d] = es[k];
+    }
+  }
+  __syncwarp();
+  if (lane == 0) W.count[slot] = n;
+  __syncwarp();
+  return true;
+}
+
+// The RK4 double step in explicitly rounded operations, on one precession angle
+// (float) or two (float2: .x angle k, .y angle k + 1, one FP32x2 instruction per
+// operation).  Both forms round every operation the same way, so an angle's result
+// does not depend on how many angles share the pass.
+__device__ __forceinline__ float fma_(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ float2 fma_(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float mul_(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float2 mul_(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float add_(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float2 add_(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float neg_(float a) { return -a; }
+__device__ __forceinline__ float2 neg_(float2 a) { return make_float2(-a.x, -a.y); }
+template <typename T>
+__device__ __forceinline__ T bc(float v);
+template <>
+__device__ __forceinline__ float bc<float>(float v) { return v; }
+template <>
+__device__ __forceinline__ float2 bc<float2>(float v) { return make_float2(v, v); }
+__device__ __forceinline__ float rsq_(float a) { return rsqrtf(a); }
+__device__ __forceinline__ float2 rsq_(float2 a) { return make_float2(rsqrtf(a.x), rsqrtf(a.y)); }
+
+struct Sample {
+  float c0, cgr, cgi;
+};
+
+template <typename T>
+struct SampleT {
+  T c0, cgr, cgi;
+};
+
+template <typename T>
+__device__ __forceinline__ SampleT<T> widen(const Sample& s) {
+  return SampleT<T>{bc<T>(s.c0), bc<T>(s.cgr), bc<T>(s.cgi)};
+}
+
+// d/dz (phi_0, phi_g) of the reference's two-beam equations (:2375-2380), phases as
+// (Re phi_0, Im phi_0, Re phi_g, Im phi_g)
+template <typename T>
+__device__ __forceinline__ void deriv(const SampleT<T>& s, T a, const T* ph, T* d) {
+  const T ca = add_(s.c0, a);
+  d[0] = fma_(neg_(s.cgr), ph[3], fma_(neg_(s.cgi), ph[2], mul_(neg_(s.c0), ph[1])));
+  d[1] = fma_(neg_(s.cgi), ph[3], fma_(s.cgr, ph[2], mul_(s.c0, ph[0])));
+  d[2] = fma_(neg_(ca), ph[3], fma_(neg_(s.cgr), ph[1], mul_(s.cgi, ph[0])));
+  d[3] = fma_(ca, ph[2], fma_(s.cgi, ph[1], mul_(s.cgr, ph[0])));
+}
+
+// One RK4 double step over samples (z-2, z-1, z) with weights dz/3, 2dz/3 (:2389-2464)
+// and the renormalisation of the phases (:2466-2472).
+template <typename T>
+__device__ __forceinline__ void rk4(const SampleT<T>& s0, const SampleT<T>& s1, const SampleT<T>& s2, T a, float dzf,
+                                    T* ph) {
+  T d[4], p1[4], q[4];
+  const T dz = bc<T>(dzf), dz3 = bc<T>(dzf / 3.f), dz23 = bc<T>(2.f * dzf / 3.f), dz2 = bc<T>(2.f * dzf);
+  deriv(s0, a, ph, d);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    p1[i] = fma_(d[i], dz3, ph[i]);
+    q[i] = fma_(d[i], dz, ph[i]);
+  }
+  deriv(s1, a, q, d);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    q[i] = fma_(d[i], dz, ph[i]);
+    p1[i] = fma_(d[i], dz23, p1[i]);
+  }
+  deriv(s1, a, q, d);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    q[i] = fma_(d[i], dz2, ph[i]);
+    p1[i] = fma_(d[i], dz23, p1[i]);
+  }
+  deriv(s2, a, q, d);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) ph[i] = fma_(d[i], dz3, p1[i]);
+  const T inv = rsq_(fma_(ph[3], ph[3], fma_(ph[2], ph[2], fma_(ph[1], ph[1], mul_(ph[0], ph[0])))));
+#pragma unroll
+  for (int i = 0; i < 4; ++i) ph[i] = mul_(ph[i], inv);
+}
+
+__device__ __forceinline__ float rho_of(float r2min, float sig) {
+  if (r2min < sig * sig) return 1.f;
+  if (r2min > 4.f * sig * sig) return 0.f;
+  const float xx = sqrtf(r2min) / sig - 1.f;
+  return 1.f - xx * xx * xx * (10.f - 15.f * xx + 6.f * xx * xx);
+}
+
+template <bool kDensity>
+__device__ __forceinline__ Sample make_sample(float sr, float si, float r2min, float b0, float bg, float sig,
+                                              bool use_density) {
+  const float inv = rsqrtf(fmaxf(fmaf(sr, sr, si * si), 1e-32f));  // x = S / max(1e-16, |S|)
+  const float rho = (kDensity && use_density) ? rho_of(r2min, sig) : 1.f;
+  return Sample{b0 * rho, bg * rho * (sr * inv), bg * rho * (si * inv)};
+}
+
+// The lanes' half of a step: every buffered atom against the lane's column at both
+// slices.  Two accumulator sets (even and odd atoms) for instruction-level
+// parallelism; a*.x / a*.y are the real / imaginary sums, a0 slice z0, a1 slice z0 + 1.
+// r2 minima (density) are kept as min(dxy^2 - hmax_k) = r^2 - (3 sigma)^2.
+template <bool kDensity, bool kStats>
+__device__ __forceinline__ void consume(const float4* __restrict__ BA, const float4* __restrict__ BE, int n, float Xv,
+                                        float Yv, float2& a0A, float2& a1A, float2& a0B, float2& a1B, float2& rmA,
+                                        float2& rmB, unsigned& n_acc) {
+  int i = 0;
+  for (; i + 1 < n; i += 2) {
+    const float4 qa = BA[i], qb = BA[i + 1];
+    const float4 ea = BE[i], eb = BE[i + 1];
+    const float dxa = qa.x - Xv, dya = qa.y - Yv, dxb = qb.x - Xv, dyb = qb.y - Yv;
+    const float ha = fmaf(dxa, dxa, dya * dya), hb = fmaf(dxb, dxb, dyb * dyb);
+    const float wa = ex2_approx(-ha), wb = ex2_approx(-hb);
+    const float2 wa2 = make_float2(wa, wa), wb2 = make_float2(wb, wb);
+    if (ha <= qa.z) a0A = __ffma2_rn(wa2, make_float2(ea.x, ea.y), a0A);
+    if (ha <= qa.w) a1A = __ffma2_rn(wa2, make_float2(ea.z, ea.w), a1A);
+    if (hb <= qb.z) a0B = __ffma2_rn(wb2, make_float2(eb.x, eb.y), a0B);
+    if (hb <= qb.w) a1B = __ffma2_rn(wb2, make_float2(eb.z, eb.w), a1B);
+    if (kDensity) {
+      rmA.x = fminf(rmA.x, ha - qa.z);
+      rmA.y = fminf(rmA.y, ha - qa.w);
+      rmB.x = fminf(rmB.x, hb - qb.z);
+      rmB.y = fminf(rmB.y, hb - qb.w);
+    }
+    if (kStats) n_acc += (ha <= qa.z) + (ha <= qa.w) + (hb <= qb.z) + (hb <= qb.w);
+  }
+  if (i < n) {
+    const float4 qa = BA[i];
+    const float4 ea = BE[i];
+    const float dxa = qa.x - Xv, dya = qa.y - Yv;
+    const float ha = fmaf(dxa, dxa, dya * dya);
+    const float wa = ex2_approx(-ha);
+    const float2 wa2 = make_float2(wa, wa);
+    if (ha <= qa.z) a0A = __ffma2_rn(wa2, make_float2(ea.x, ea.y), a0A);
+    if (ha <= qa.w) a1A = __ffma2_rn(wa2, make_float2(ea.z, ea.w), a1A);
+    if (kDensity) {
+      rmA.x = fminf(rmA.x, ha - qa.z);
+      rmA.y = fminf(rmA.y, ha - qa.w);
+    }
+    if (kStats) n_acc += (ha <= qa.z) + (ha <= qa.w);
+  }
+}
+
+// Precession coefficient (pair) k: from registers, or from the table (L1).  The table of
+// a pass holds aa(prec_offset ...) and is read in pairs only below np, whose odd last
+// angle pairs with a zero the host appends.
+template <typename T, bool kReg>
+__device__ __forceinline__ T aa_at(const T* aa, const float* __restrict__ aag, int k) {
+  if constexpr (kReg) {
+    return aa[k];
+  } else if constexpr (std::is_same<T, float>::value) {
+    return __ldg(aag + k);
+  } else {
+    return make_float2(__ldg(aag + 2 * k), __ldg(aag + 2 * k + 1));
+  }
+}
+
+// One warp tile of one image: the TX x (32 / TX) columns of tile `tile` marched through
+// the depth.  Returns false when a slab overflows its staging (counters[4]).
+template <int NP, bool kDensity, bool kStats, int CAPS, int TX, bool kMasked>
+__device__ __noinline__ bool column_tile3(const ColumnParams& p, WarpSmem3<CAPS>& W, int tile, int lane) {
+  constexpr int TY = 32 / TX;
+  // one precession angle: scalar phases; more: pairs of angles in FP32x2 registers
+  using T = typename std::conditional<NP == 1, float, float2>::type;
+  constexpr int NH = NP == 1 ? 1 : NP / 2;
+  const int Wd = p.ix1 - p.ix0;
+  const int tiles_x = (Wd + TX - 1) / TX;
+  const int tx = tile % tiles_x, ty = tile / tiles_x;
+  const int ix = p.ix0 + tx * TX + (lane % TX);
+  const int iy = p.iy0 + ty * TY + lane / TX;
+  const bool active = ix < p.ix1 && iy < p.iy1;
+  // tile mask: a column is written only when its mask tile is wanted; the warp marches
+  // when any of its columns is (a warp tile may straddle mask tiles in any shape)
+  bool wanted = true;
+  if constexpr (kMasked) {
+    if (p.tile_mask) wanted = active && p.tile_mask[(iy / p.mask_T) * p.mask_ntx + ix / p.mask_T] != 0;
+    if (!__any_sync(0xffffffffu, wanted)) return true;
+  }
+
+  // s = sqrt(log2(e) / (2 sigma^2)): exp(-r^2 / (2 sigma^2)) = ex2(-(s r)^2)
+  const double sd = sqrt(p.i2s2 * 1.4426950408889634);
+  Geo G;
+  G.scale = (float)sd;
+  const int ixc = min(ix, p.ix1 - 1), iyc = min(iy, p.iy1 - 1);
+  const int hx = p.xtab[ixc].x, hy = p.ytab[iyc].x;
+  const double fvx = p.xfv[ixc], fvy = p.yfv[iyc];
+  {
+    const int big = 1 << 29;
+    const int mnx = __reduce_min_sync(0xffffffffu, active ? hx : big);
+    const int mxx = __reduce_max_sync(0xffffffffu, active ? hx : -big);
+    const int mny = __reduce_min_sync(0xffffffffu, active ? hy : big);
+    const int mxy = __reduce_max_sync(0xffffffffu, active ? hy : -big);
+    G.ux_lo = mnx - 1;
+    G.ux_hi = mxx + 1;
+    G.uy_lo = mny - 1;
+    G.uy_hi = mxy + 1;
+    G.ux_ref = mnx;
+    G.uy_ref = mny;
+  }
+  G.a11s = (float)(p.a11 * sd);
+  G.a22s = (float)(p.a22 * sd);
+  G.a33s = (float)(p.a33 * sd);
+  const float Xv = (float)(p.a11 * (fvx + (double)(hx - G.ux_ref)) * sd);
+  const float Yv = (float)(p.a22 * (fvy + (double)(hy - G.uy_ref)) * sd);
+  {
+    const float big = 1e30f;
+    float v = active ? Xv : big, w = active ? -Xv : big, y = active ? Yv : big, z = active ? -Yv : big;
+    for (int o = 16; o > 0; o >>= 1) {
+      v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+      w = fminf(w, __shfl_xor_sync(0xffffffffu, w, o));
+      y = fminf(y, __shfl_xor_sync(0xffffffffu, y, o));
+      z = fminf(z, __shfl_xor_sync(0xffffffffu, z, o));
+    }
+    G.xmin = v;
+    G.xmax = -w;
+    G.ymin = y;
+    G.ymax = -z;
+  }
+  const float cut2 = (float)(p.cut2 * sd * sd);        // (3 sigma)^2 in scaled units
+  const float r3 = sqrtf(cut2) * 1.0001f + 1e-4f;      // z-window half width, rounded up
+  G.pre2 = cut2 * 1.0002f + 1e-3f;
+  const float inv_bin = kBins / G.a33s;
+  const float sig = (float)p.sigma, b0 = (float)p.b0, bg = (float)p.bg, dzs = (float)p.dz;
+  const float r2_to_A2 = (float)(1.0 / (sd * sd));    // scaled r^2 back to A^2 (density)
+  const unsigned lt = (1u << lane) - 1;
+
+  const int np = min(NP, p.n_prec - p.prec_offset);
+  const float* __restrict__ aag = p.aaf + p.prec_offset;
+  // the precession coefficients a_k stay in registers for few angles; for many they are
+  // read from L1 at each step (pairs: the host pads the table to an even count), which
+  // leaves the registers to the phases
+  constexpr bool kAaReg = NP <= 4;
+  T aa[kAaReg ? NH : 1], ph[NH][4];
+#pragma unroll
+  for (int k = 0; k < NH; ++k) {
+    if constexpr (kAaReg) {
+      if constexpr (NP == 1) {
+        aa[k] = aag[0];
+      } else {
+        aa[k] = make_float2(2 * k < np ? aag[2 * k] : 0.f, 2 * k + 1 < np ? aag[2 * k + 1] : 0.f);
+      }
+    }
+    ph[k][0] = bc<T>(1.f);
+    ph[k][1] = ph[k][2] = ph[k][3] = bc<T>(0.f);
+  }
+  const int nh = NP == 1 ? 1 : (np + 1) / 2;  // angle pairs in use
+  Sample s_first{0.f, 0.f, 0.f}, s_prev{0.f, 0.f, 0.f}, s_mid{0.f, 0.f, 0.f};
+  int ring_lo = 1 << 30, ring_hi = (1 << 30) - 1;  // empty
+  unsigned n_acc = 0;
+  unsigned long long n_tst = 0;
+
+  for (int z0 = 0; z0 < p.Mz; z0 += 2) {
+    const bool has1 = z0 + 1 < p.Mz;
+    // home cells and slice depths (scaled, relative to the origin of home cell hz0)
+    const int2 e0 = p.ztab[z0];
+    const int2 e1 = has1 ? p.ztab[z0 + 1] : e0;
+    const int hz0 = e0.x, hz1 = e1.x;
+    const float zv0 = __int_as_float(e0.y), zv1 = __int_as_float(e1.y);
+    const int need_lo = hz0 - 1, need_hi = hz1 + 1;
+    if (need_lo > ring_hi || need_hi < ring_lo) {
+      ring_lo = need_lo;
+      ring_hi = need_lo - 1;
+    }
+    if (ring_lo < need_lo) ring_lo = need_lo;
+    bool ok = true;
+    while (ring_hi < need_hi && ok) {
+      ++ring_hi;
+      ok = load_slab3<CAPS>(p, G, ring_hi, W, lane);
+    }
+    if (!ok) {
+      if (lane == 0) atomicExch(&p.counters[4], 1ull);
+      return false;  // the host recomputes with larger slabs, or the general kernel
+    }
+    float2 a0A = make_float2(0.f, 0.f), a1A = a0A, a0B = a0A, a1B = a0A;
+    float2 rmA = make_float2(kHuge, kHuge), rmB = rmA;
+    int nb = 0;  // atoms in the step buffer
+    for (int u = need_lo; u <= need_hi; ++u) {
+      const int slot = u & (kRing - 1);
+      const float zoff = G.a33s * (float)(u - hz0);  // cell u's origin relative to hz0's
+      const float t0 = zv0 - zoff, t1 = zv1 - zoff;
+      // slab u serves slice k within the cutoff; with z cells shorter than 3 sigma the
+      // reference searches only the 27 cells around each voxel's home cell, so it serves
+      // a slice only within one cell of that slice's home z cell
+      bool v0 = true, v1 = has1;
+      if (p.trunc_z) {
+        v0 = u - hz0 >= -1 && u - hz0 <= 1;
+        v1 = has1 && u - hz1 >= -1 && u - hz1 <= 1;
+      }
+      if (!v0 && !v1) continue;
+      const float w_lo = v0 ? t0 : t1, w_hi = v1 ? t1 : t0;
+      const int b_lo = max(0, min(kBins, (int)floorf((w_lo - r3) * inv_bin)));
+      const int b_hi = max(0, min(kBins, (int)ceilf((w_hi + r3) * inv_bin)));
+      const int lo = W.bin[slot][b_lo];
+      const int hi = W.bin[slot][b_hi];
+      const float4* P = W.p[slot];
+      const float* S = W.s[slot];
+      for (int b = lo; b < hi; b += 32) {
+        // cooperative pass: one atom per lane, its depth-only terms, kept if some column
+        // of the patch can accept it at some slice
+        const int j = b + lane;
+        bool keep = false;
+        float4 A, E;
+        if (j < hi) {
+          const float4 q = P[j];
+          const float sn = S[j];
+          const float dz0 = q.z - t0, dz1 = q.z - t1;
+          const float hm0 = v0 ? cut2 - dz0 * dz0 : -1.f;
+          const float hm1 = v1 ? cut2 - dz1 * dz1 : -1.f;
+          const float dxr = fmaxf(0.f, fmaxf(G.xmin - q.x, q.x - G.xmax));
+          const float dyr = fmaxf(0.f, fmaxf(G.ymin - q.y, q.y - G.ymax));
+          // margin: the lanes' own rounding of dxy^2 must not reach below the rectangle's
+          keep = fmaf(dxr, dxr, dyr * dyr) <= fmaxf(hm0, hm1) * 1.0001f + 1e-4f;
+          const float wz0 = ex2_approx(-dz0 * dz0), wz1 = ex2_approx(-dz1 * dz1);
+          A = make_float4(q.x, q.y, hm0, hm1);
+          E = make_float4(wz0 * q.w, wz0 * sn, wz1 * q.w, wz1 * sn);
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, keep);
+        if (keep) {
+          const int d = nb + __popc(m & lt);
+          W.ba[d] = A;
+          W.be[d] = E;
+        }
+        nb += __popc(m);
+        if (nb >= 32) {
+          __syncwarp();
+          consume<kDensity, kStats>(W.ba, W.be, nb, Xv, Yv, a0A, a1A, a0B, a1B, rmA, rmB, n_acc);
+          if (kStats) n_tst += (unsigned long long)nb;
+          __syncwarp();
+          nb = 0;
+        }
+      }
+    }
+    if (nb > 0) {
+      __syncwarp();
+      consume<kDensity, kStats>(W.ba, W.be, nb, Xv, Yv, a0A, a1A, a0B, a1B, rmA, rmB, n_acc);
+      if (kStats) n_tst += (unsigned long long)nb;
+      __syncwarp();
+    }
+    const float2 a0 = __fadd2_rn(a0A, a0B), a1 = __fadd2_rn(a1A, a1B);
+    const float rm0 = (cut2 + fminf(rmA.x, rmB.x)) * r2_to_A2, rm1 = (cut2 + fminf(rmA.y, rmB.y)) * r2_to_A2;
+    // field samples z0 (even) and z0 + 1 (odd), then the RK4 double step (z0-2, z0-1, z0)
+    const Sample s0 = make_sample<kDensity>(a0.x, a0.y, rm0, b0, bg, sig, p.use_density != 0);
+    if (z0 == 0) {
+      s_first = s0;
+    } else {
+      const SampleT<T> w0 = widen<T>(s_prev), w1 = widen<T>(s_mid), w2 = widen<T>(s0);
+#pragma unroll
+      for (int k = 0; k < NH; ++k)
+        if (k < nh) rk4<T>(w0, w1, w2, aa_at<T, kAaReg>(aa, aag, k), dzs, ph[k]);
+    }
+    s_prev = s0;
+    if (has1) s_mid = make_sample<kDensity>(a1.x, a1.y, rm1, b0, bg, sig, p.use_density != 0);
+  }
+  if ((p.Mz & 1) == 0) {  // closure x(Mz) = x(0)
+    const SampleT<T> w0 = widen<T>(s_prev), w1 = widen<T>(s_mid), w2 = widen<T>(s_first);
+#pragma unroll
+    for (int k = 0; k < NH; ++k)
+      if (k < nh) rk4<T>(w0, w1, w2, aa_at<T, kAaReg>(aa, aag, k), dzs, ph[k]);
+  }
+  // |phi_g|^2 summed over the angles in order, rounded the same way for either form
+  float acc = 0.f;
+#pragma unroll
+  for (int k = 0; k < NH; ++k) {
+    if constexpr (NP == 1) {
+      acc = __fadd_rn(acc, __fmaf_rn(ph[k][2], ph[k][2], __fmul_rn(ph[k][3], ph[k][3])));
+    } else {
+      if (2 * k < np) acc = __fadd_rn(acc, __fmaf_rn(ph[k][2].x, ph[k][2].x, __fmul_rn(ph[k][3].x, ph[k][3].x)));
+      if (2 * k + 1 < np)
+        acc = __fadd_rn(acc, __fmaf_rn(ph[k][2].y, ph[k][2].y, __fmul_rn(ph[k][3].y, ph[k][3].y)));
+    }
+  }
+  if (active && wanted) {
+    double* o = p.img + ix + (int64_t)p.Mx * iy;
+    *o = p.accumulate ? *o + (double)acc : (double)acc;
+  }
+  if (kStats) {
+    unsigned long long acc_w = active ? n_acc : 0u, tst_w = active ? 2 * n_tst : 0u;
+    for (int o = 16; o > 0; o >>= 1) {
+      acc_w += __shfl_xor_sync(0xffffffffu, acc_w, o);
+      tst_w += __shfl_xor_sync(0xffffffffu, tst_w, o);
+    }
+    if (lane == 0) {
+      atomicAdd(&p.counters[2], tst_w);
+      atomicAdd(&p.counters[3], acc_w);
+    }
+  }
+  return true;
+}
+
+// Persistent launch over the warp tiles of every job of a batch: each warp takes the
+// next tile from a global counter, so images of uneven size share the GPU without a tail
+// per image.  kMasked: jobs may carry a tile mask (columns outside it are not written).
+template <int NP, bool kDensity, bool kStats, int kMinBlocks, int CAPS, int TX, bool kMasked>
+__global__ void __launch_bounds__(kWarps * 32, kMinBlocks)
+    k_column_fp32_v3(const ColumnJob* __restrict__ jobs, int n_jobs, int total_tiles, unsigned* __restrict__ work,
+                     const unsigned long long* __restrict__ counters, int64_t cap) {
+  constexpr int kShape = TX == 8 ? 0 : TX == 4 ? 1 : 2;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  WarpSmem3<CAPS>& W = reinterpret_cast<WarpSmem3<CAPS>*>(smem_raw)[warp];
+  if ((int64_t)counters[0] > cap) return;  // the binning overflowed: the host retries
+  for (;;) {
+    int tile = 0;
+    if (lane == 0) tile = (int)atomicAdd(work, 1u);
+    tile = __shfl_sync(0xffffffffu, tile, 0);
+    if (tile >= total_tiles) break;
+    if (counters[4] != 0) break;  // a slab overflowed: the host recomputes with larger slabs
+    int lo = 0, hi = n_jobs - 1;  // job of this tile
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (jobs[mid].tile_base[kShape] <= tile)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    const int local = tile - jobs[lo].tile_base[kShape];
+    if (!column_tile3<NP, kDensity, kStats, CAPS, TX, kMasked>(jobs[lo].p, W, local, lane)) break;
+  }
+}
+
+template <int CAPS, typename K>
+cudaError_t launch3(K kernel, const Ring3Args& a, int tiles, int blocks_per_sm) {
+  const size_t smem = sizeof(WarpSmem3<CAPS>) * kWarps;
+  cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  int dev = 0, sms = 148;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int grid = sms * blocks_per_sm;
+  const int need = (tiles + kWarps - 1) / kWarps;
+  if (grid > need) grid = need;
+  if (grid < 1) grid = 1;
+  ++launch_count();
+  kernel<<<grid, kWarps * 32, smem, a.st>>>(a.jobs, a.n_jobs, tiles, a.work, a.counters, a.cap);
+  return cudaGetLastError();
+}
+
+// Instances of one angle bucket NP.  Tuning variants (tier 0, no statistics, no mask):
+// the tile shape (8 x 4, 4 x 8, 16 x 2 columns) and the slab capacity of the first tier
+// (128 atoms, four CTAs per SM; 96 atoms, five -- three with 16 angles, whose phases
+// need more registers than four CTAs leave: the tuner weighs the spills against the
+// occupancy).  Tiers 1 and 2 (192 and 256 atoms per slab, three and two CTAs
+// per SM), the statistics and the tile-masked instances use 8 x 4 tiles.
+template <int NP, bool kDensity>
+cudaError_t ring3_dispatch(const Ring3Args& a) {
+  constexpr int B96 = NP >= 16 ? 3 : 5;
+  const int* T = a.tiles;
+  if (a.masked) {  // the variant's tile shape, so that a masked image equals the plain one on its tiles
+    if constexpr (NP == 1) {
+      if (a.tier >= 2) return launch3<256>(k_column_fp32_v3<1, kDensity, false, 2, 256, 8, true>, a, T[0], 2);
+      if (a.tier == 1) return launch3<192>(k_column_fp32_v3<1, kDensity, false, 3, 192, 8, true>, a, T[0], 3);
+      if (a.variant == 2 || a.variant == 3)
+        return launch3<128>(k_column_fp32_v3<1, kDensity, false, 4, 128, 4, true>, a, T[1], 4);
+      if (a.variant == 4 || a.variant == 5)
+        return launch3<128>(k_column_fp32_v3<1, kDensity, false, 4, 128, 16, true>, a, T[2], 4);
+      return launch3<128>(k_column_fp32_v3<1, kDensity, false, 4, 128, 8, true>, a, T[0], 4);
+    }
+    return cudaErrorInvalidValue;
+  }
+  if (a.stats) {
+    if (a.tier >= 2) return launch3<256>(k_column_fp32_v3<NP, kDensity, true, 2, 256, 8, false>, a, T[0], 2);
+    if (a.tier == 1) return launch3<192>(k_column_fp32_v3<NP, kDensity, true, 3, 192, 8, false>, a, T[0], 3);
+    return launch3<128>(k_column_fp32_v3<NP, kDensity, true, 4, 128, 8, false>, a, T[0], 4);
+  }
+  if (a.tier >= 2) return launch3<256>(k_column_fp32_v3<NP, kDensity, false, 2, 256, 8, false>, a, T[0], 2);
+  if (a.tier == 1) return launch3<192>(k_column_fp32_v3<NP, kDensity, false, 3, 192, 8, false>, a, T[0], 3);
+  switch (a.variant) {
+    case 1: return launch3<96>(k_column_fp32_v3<NP, kDensity, false, B96, 96, 8, false>, a, T[0], B96);
+    case 2: return launch3<128>(k_column_fp32_v3<NP, kDensity, false, 4, 128, 4, false>, a, T[1], 4);
+    case 3: return launch3<96>(k_column_fp32_v3<NP, kDensity, false, B96, 96, 4, false>, a, T[1], B96);
+    case 4: return launch3<128>(k_column_fp32_v3<NP, kDensity, false, 4, 128, 16, false>, a, T[2], 4);
+    case 5: return launch3<96>(k_column_fp32_v3<NP, kDensity, false, B96, 96, 16, false>, a, T[2], B96);
+    default: return launch3<128>(k_column_fp32_v3<NP, kDensity, false, 4, 128, 8, false>, a, T[0], 4);
+  }
+}
+
+template <int NP>
+cudaError_t ring3_launch_np(const Ring3Args& a) {
+  return a.density ? ring3_dispatch<NP, true>(a) : ring3_dispatch<NP, false>(a);
+}
+
+}  // namespace ring3
+}  // namespace stem

@@ -343,8 +343,10 @@ ColumnParams column_params(st_ctx* c, const Job& j, int64_t cell_base, size_t xo
 }
 
 // Times every slab-ring variant once on the same pass (each overwrites the pass's
-// images with the same values) and returns the fastest in `best`, or -1 when a
-// trial found the binning or a slab overflowed (the timings mean nothing then).
+// images) and returns the fastest in `best`, or -1 when the binning overflowed (the
+// timings mean nothing then).  A variant whose slabs overflowed its staging is left out
+// (its counter is cleared for the next trial).  The variants' images agree to FP32
+// rounding, not to the bit, so the pass ends with the chosen variant's own output.
 template <typename F>
 cudaError_t tune_ring(st_ctx* c, F&& launch_variant, int64_t cap, cudaStream_t st, int& best) {
   best = -1;
@@ -353,23 +355,31 @@ cudaError_t tune_ring(st_ctx* c, F&& launch_variant, int64_t cap, cudaStream_t s
     if (!c->tev[i]) e = cudaEventCreate(&c->tev[i]);
   const int nv = ring_variant_count();
   std::vector<float> ms(nv, 0.f);
+  std::vector<char> valid(nv, 0);
+  unsigned long long h[5];
+  int last = -1;
   for (int v = 0; v < nv && e == cudaSuccess; ++v) {
     cudaEventRecord(c->tev[0], st);
     e = launch_variant(v);
     cudaEventRecord(c->tev[1], st);
     if (e == cudaSuccess) e = cudaEventSynchronize(c->tev[1]);
     if (e == cudaSuccess) e = cudaEventElapsedTime(&ms[v], c->tev[0], c->tev[1]);
+    if (e == cudaSuccess) e = cudaMemcpy(h, c->s.counters, sizeof h, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) break;
+    if ((int64_t)h[0] > cap) return cudaSuccess;
+    if (h[4] != 0) {
+      e = cudaMemsetAsync(c->s.counters + 4, 0, sizeof(unsigned long long), st);
+      continue;
+    }
+    valid[v] = 1;
+    last = v;
   }
   if (e != cudaSuccess) return e;
-  unsigned long long h[5];
-  e = cudaMemcpy(h, c->s.counters, sizeof h, cudaMemcpyDeviceToHost);
-  if (e != cudaSuccess) return e;
-  if (h[4] != 0 || (int64_t)h[0] > cap) return cudaSuccess;
-  best = 0;
-  for (int v = 1; v < nv; ++v)
-    if (ms[v] < ms[best]) best = v;
-  c->last_ring_variant = best;
-  return cudaSuccess;
+  for (int v = 0; v < nv; ++v)
+    if (valid[v] && (best < 0 || ms[v] < ms[best])) best = v;
+  if (best >= 0 && best != last) e = launch_variant(best);  // the pass's images from the chosen variant
+  if (best >= 0) c->last_ring_variant = best;
+  return e;
 }
 
 // The slab-ring FP32 kernel needs cells of at least 3 sigma (no truncated
@@ -408,7 +418,7 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
     xoff[i + 1] = xoff[i] + g->Mx;
     yoff[i + 1] = yoff[i] + g->My;
     zoff[i + 1] = zoff[i] + g->Mz;
-    aoff[i + 1] = aoff[i] + jobs[i].n_prec;
+    aoff[i + 1] = aoff[i] + ((jobs[i].n_prec + 1) & ~1);  // even: the FP32 ring reads angle pairs
   }
   const int64_t total_cand = cand_base[n], total_cells = cell_base[n];
   // kept atoms are indexed by int (cell starts, permutation): at most total_cand of them
@@ -498,23 +508,25 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
   const int width = fp32 ? 16 : 4;
   const int passes = (ring_np + width - 1) / width;
   std::vector<ColumnJob> cj;
-  std::vector<int> pass_tiles(passes, 0);
+  std::vector<int> pass_tiles((size_t)passes * kRingShapes, 0);  // per pass, per tile shape
   if (ring) {
     // the density variant of the kernel serves every image of the launch when any image uses it;
     // an image without the density field then gets rho = 1 from use_density = 0 in the sample
     cj.resize((size_t)n_ring * passes);
     for (int pass = 0; pass < passes; ++pass) {
-      int tiles = 0;
+      int tiles[kRingShapes] = {0, 0, 0};
       for (int r = 0; r < n_ring; ++r) {
         ColumnJob& J = cj[(size_t)pass * n_ring + r];
         J.p = cps[ring_jobs[r]];
         J.p.prec_offset = pass * width;
         J.p.accumulate = pass > 0 ? 1 : 0;
-        J.tile_base = tiles;
         J.pad = 0;
-        if (J.p.prec_offset < J.p.n_prec) tiles += column_tiles(J.p);  // fewer angles: no tiles this pass
+        for (int sh = 0; sh < kRingShapes; ++sh) {
+          J.tile_base[sh] = tiles[sh];
+          if (J.p.prec_offset < J.p.n_prec) tiles[sh] += column_tiles(J.p, sh);  // fewer angles: none this pass
+        }
       }
-      pass_tiles[pass] = tiles;
+      for (int sh = 0; sh < kRingShapes; ++sh) pass_tiles[(size_t)pass * kRingShapes + sh] = tiles[sh];
     }
   }
 
@@ -547,6 +559,10 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
     for (int k = 0; k < jobs[i].n_prec; ++k) {
       haa[aoff[i] + k] = jobs[i].aa[k];
       haaf[aoff[i] + k] = (float)jobs[i].aa[k];
+    }
+    for (size_t k = aoff[i] + jobs[i].n_prec; k < aoff[i + 1]; ++k) {  // pad to a pair
+      haa[k] = 0.0;
+      haaf[k] = 0.f;
     }
     hbp[i] = bin_params(jobs[i], cand_base[i], cell_base[i], atom_base[i]);
   }
@@ -638,7 +654,8 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
     for (int pass = 0; ring_ok && pass < passes && ce == cudaSuccess; ++pass) {
       const int np_pass = std::min(width, ring_np - pass * width);
       auto ring_launch = [&](int v) {
-        return launch_column_fp32_ring(c->d_coljobs + (size_t)pass * n_ring, n_ring, pass_tiles[pass], np_pass,
+        return launch_column_fp32_ring(c->d_coljobs + (size_t)pass * n_ring, n_ring,
+                                       pass_tiles.data() + (size_t)pass * kRingShapes, np_pass,
                                        dens, stats, v, big, masked, c->d_work, c->s.counters, cap, st);
       };
       if (capturing) {
@@ -654,13 +671,13 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
         if (it != c->ring_tuned.end()) {
           v = it->second;
         } else if (pass == 0 && pass_tiles[0] >= 4096 && !big && !masked) {
-          // autotune on the real work: the first pass overwrites its images, so every trial
-          // leaves the same result; keep the fastest for the later calls of this context
+          // autotune on the real work: the first pass overwrites its images, and the tuner
+          // ends with the chosen variant's output; keep it for the later calls of this context
           ce = tune_ring(c, ring_launch, cap, st, v);
           if (ce == cudaSuccess && v >= 0) {
             c->ring_tuned[key] = v;
             pass_variant[pass] = v;
-            continue;  // the last trial's output is the pass's result
+            continue;
           }
           v = 0;
         }
@@ -762,7 +779,8 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
   S.ms_column = ms;
   S.column_kernel = c->last_column_kernel;
   S.ring_variant = used_ring ? c->last_ring_variant : -1;
-  S.ring_slab_atoms = used_ring && !ring_jobs.empty() ? (big == 0 ? 128 : big == 1 ? 192 : 256) : 0;
+  S.ring_slab_atoms =
+      used_ring && !ring_jobs.empty() ? (big == 0 ? ring_variant_slab(S.ring_variant) : big == 1 ? 192 : 256) : 0;
   S.n_launches = n_launches;
   // the reference stops when a link cell needs more than 16 x nMax0 slots; a batch's
   // largest cell is checked against the smallest nMax0 of its images
