@@ -58,13 +58,14 @@ struct BinnedAtoms {
   // FP32 records
   float4* p32;         // a_col11*fx, a_col22*fy, a_col33*fz, bits(packed cell)
   float2* cs32;        // cos, sin of the FP64-reduced phase
+  uint4* fr32;         // 2^-32 units of the cell fractions (x, y, z, -): the cutoff's exact recheck
 };
 
 // A kept atom's record of the FP32 path as the binning makes it (same size as double4_32a).
 struct alignas(16) Rec32 {
-  float4 p;   // a_col11*fx, a_col22*fy, a_col33*fz, bits(packed cell)
-  float2 cs;  // cos, sin of the phase
-  float2 pad;
+  float4 p;          // a_col11*fx, a_col22*fy, a_col33*fz, bits(packed cell)
+  float tc;          // phase g.y / 2 pi, reduced to [-1/2, 1/2) cycles
+  unsigned frac[3];  // 2^-32 units of the cell fractions fx, fy, fz (the fixed point's top 32 bits)
 };
 
 struct Scratch {
@@ -113,6 +114,7 @@ struct ColumnParams {
   const double2* cs64;
   const float4* p32;
   const float2* cs32;
+  const uint4* fr32;
   const int2* xtab;
   const double* xfv;
   const int2* ytab;
@@ -176,10 +178,6 @@ int ring_variant_count();
 const char* ring_variant_name(int variant);
 int ring_variant_slab(int variant);  // atoms per slab of the variant's first tier
 int ring_np_bucket(int max_np);  // the kernel template (angles per pass) serving max_np angles
-// second-generation slab ring (k_column_v2.cu): occupancy variant v2 (0, 1), 8 x 4 tiles
-cudaError_t launch_column_fp32_ring_v2(const ColumnJob* d_jobs, int n_jobs, int total_tiles, int max_np, bool density,
-                                       bool stats, int v2, int slab_tier, bool masked, unsigned* work,
-                                       const unsigned long long* counters, int64_t cap, cudaStream_t st);
 namespace ring3 {
 // third generation (k_column_v3.cuh), one instance set per angle bucket NP
 struct Ring3Args {

@@ -274,8 +274,6 @@ __global__ void __launch_bounds__(256) k_bin_atoms_fp32(const BinParams* __restr
             // phase: g.y / 2 pi reduced to [-1/2, 1/2) cycles (sign-extended 36-bit fraction)
             const long long r = (long long)((unsigned long long)gt << (64 - kFixBits)) >> (64 - kFixBits);
             const float tc = (float)(int)(r >> 4) * 2.3283064365386963e-10f;
-            float sf, cf;
-            sincospif(2.0f * tc, &sf, &cf);
             tmp_key[idx] = (int)((int64_t)nn * p.n_atoms + jj);
             tmp_cell[idx] = cell;
             tmp_slot[idx] = slot;
@@ -285,7 +283,9 @@ __global__ void __launch_bounds__(256) k_bin_atoms_fp32(const BinParams* __restr
                                  p.a_colf[1] * fix_frac_to_float(c[1] & kFracMask),
                                  p.a_colf[2] * fix_frac_to_float(c[2] & kFracMask),
                                  __int_as_float(pack_cell(k0, k1, k2)));
-            rec[1] = make_float4(cf, sf, 0.0f, 0.0f);
+            rec[1] = make_float4(tc, __uint_as_float((unsigned)((c[0] & kFracMask) >> 4)),
+                                 __uint_as_float((unsigned)((c[1] & kFracMask) >> 4)),
+                                 __uint_as_float((unsigned)((c[2] & kFracMask) >> 4)));
           }
         }
       }
@@ -421,11 +421,15 @@ __global__ void __launch_bounds__(256) k_bin_finalize(const BinParams* __restric
     int r = 0;
     for (int j = 0; j < n; ++j) r += (tmp_key[perm[s + j]] < key);
     if constexpr (kFp32) {
-      // the binning wrote the records; they move to their place
+      // the binning wrote the records; they move to their place, with the phasor of the
+      // FP64-reduced phase and the cell fractions for the column kernels' cutoff recheck
       const float4* rec = reinterpret_cast<const float4*>(tmp_f + t);
       const float4 hi = rec[1];
+      float sf, cf;
+      sincospif(2.0f * hi.x, &sf, &cf);
       b.p32[s + r] = rec[0];
-      b.cs32[s + r] = make_float2(hi.x, hi.y);
+      b.cs32[s + r] = make_float2(cf, sf);
+      b.fr32[s + r] = make_uint4(__float_as_uint(hi.y), __float_as_uint(hi.z), __float_as_uint(hi.w), 0u);
     } else {
       const int job = n_jobs == 1 ? 0 : find_job(n_jobs, cell, [&](int k) { return jobs[k].cell_base; });
       const BinParams& p = jobs[job];

@@ -1,30 +1,26 @@
-// The slab-ring FP32 column launch: the tuning variants of the second- and
-// third-generation kernels behind one entry point.
+// The slab-ring FP32 column launch: the tuning variants of the slab-ring kernel
+// (k_column_v3.cuh) behind one entry point.
 //
 // Variants (st_tune, the autotuner's candidates), all computing the pixel loop of
 // computeD2BI_img (Lib_DynamicalTwoBeamImaging.f90:1870-1900) on the slab ring:
-//   0  third generation, 8 x 4 columns per warp, 128-atom slabs, 4 CTAs per SM
-//   1  third generation, 8 x 4, 96-atom slabs, 5 CTAs per SM (3 with 16 angles)
-//   2  third generation, 4 x 8, 128-atom slabs
-//   3  third generation, 4 x 8, 96-atom slabs
-//   4  third generation, 16 x 2, 128-atom slabs
-//   5  third generation, 16 x 2, 96-atom slabs
-//   6  second generation, 8 x 4, 128-atom slabs, 5 CTAs per SM (4 with 16 angles)
-//   7  second generation, 8 x 4, 128-atom slabs, one CTA per SM fewer
-// Slab tiers 1 and 2 (192 and 256 atoms) keep the variant's kernel generation with 8 x 4
-// tiles.  Statistics use variant 0's kernel (6's for the second generation); a tile-masked
-// launch uses its variant's kernel and tile shape, so the masked columns equal the plain
-// image's bit for bit.
+//   0  8 x 4 columns per warp, 128-atom slabs, 4 CTAs per SM
+//   1  8 x 4, 96-atom slabs, 5 CTAs per SM (3 with 16 angles)
+//   2  4 x 8, 128-atom slabs
+//   3  4 x 8, 96-atom slabs
+//   4  16 x 2, 128-atom slabs
+//   5  16 x 2, 96-atom slabs
+// Slab tiers 1 and 2 (192 and 256 atoms) use 8 x 4 tiles.  Statistics use variant 0's
+// kernel; a tile-masked launch uses its variant's tile shape, so the masked columns equal
+// the plain image's bit for bit.
 #include "internal.h"
 
 namespace stem {
 
 namespace {
 constexpr int kShapeTX[kRingShapes] = {8, 4, 16};
-constexpr int kVariants = 8;
-const char* const kNames[kVariants] = {"v3 8x4 slab128", "v3 8x4 slab96", "v3 4x8 slab128", "v3 4x8 slab96",
-                                       "v3 16x2 slab128", "v3 16x2 slab96", "v2 8x4 slab128 occupancy+1",
-                                       "v2 8x4 slab128"};
+constexpr int kVariants = 6;
+const char* const kNames[kVariants] = {"8x4 slab128", "8x4 slab96", "4x8 slab128", "4x8 slab96", "16x2 slab128",
+                                       "16x2 slab96"};
 }  // namespace
 
 int column_tiles(const ColumnParams& p, int shape) {
@@ -48,9 +44,6 @@ cudaError_t launch_column_fp32_ring(const ColumnJob* d_jobs, int n_jobs, const i
                                     bool stats, int variant, int slab_tier, bool masked, unsigned* work,
                                     const unsigned long long* counters, int64_t cap, cudaStream_t st) {
   if (variant < 0 || variant >= kVariants) variant = 0;
-  if (variant >= 6)
-    return launch_column_fp32_ring_v2(d_jobs, n_jobs, tiles[0], max_np, density, stats, variant - 6, slab_tier, masked,
-                                      work, counters, cap, st);
   cudaError_t e = cudaMemsetAsync(work, 0, sizeof(unsigned), st);
   if (e != cudaSuccess) return e;
   if (tiles[0] <= 0) return cudaSuccess;

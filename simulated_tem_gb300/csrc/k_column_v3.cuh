@@ -1,14 +1,16 @@
-// K2+K3, FP32, third generation: separable weights and a per-step candidate buffer.
+// K2+K3, FP32: the slab-ring column kernel with separable weights and a per-step
+// candidate buffer.
 //
-// Same computation as k_column_fp32 / k_column_fp32_v2 (the pixel loop of
-// computeD2BI_img, Lib_DynamicalTwoBeamImaging.f90:1870-1900, with the neighbour
-// search of Lib_LinkCell3D.f90:1515-1605 and the integrator of :2316-2480).
+// The pixel loop of computeD2BI_img (Lib_DynamicalTwoBeamImaging.f90:1870-1900), with the
+// neighbour search of Lib_LinkCell3D.f90:1515-1605 and the integrator of :2316-2480, for
+// the FP32 path (k_column_fp32 in k_column.cu is the general form, for any cell size and
+// slab occupancy).
 //
-// The slab ring of the second generation stays: one warp owns a patch of 32 pixel
-// columns (8 x 4, 4 x 8 or 16 x 2), one lane per column, advancing two depth slices
-// per step; the atoms of the link-cell slabs the march needs are staged in
-// warp-private shared memory, prefiltered to 3 sigma of the patch and ordered by z
-// bin.  What changes is how a step visits them:
+// One warp owns a patch of 32 pixel columns (8 x 4, 4 x 8 or 16 x 2), one lane per
+// column, advancing two depth slices per step.  The atoms of the link-cell slabs the
+// march needs (one slab per z cell, a ring of four) are staged in warp-private shared
+// memory once, prefiltered to 3 sigma of the patch and ordered by z bin, so that a step
+// visits only the bins overlapping its depth window.  Within a step:
 //
 // * Every column of a patch samples the same two depths, so everything that depends
 //   only on an atom and the depth is the same in all 32 lanes.  A cooperative pass
@@ -28,11 +30,10 @@
 // Per atom and lane: two loads, the in-plane distance (3 FP32 ops), one ex2, two
 // compares and two predicated FP32x2 multiply-adds (both slices' cos and sin).
 //
-// Precision: FP32 throughout the march, as in the second generation; the weight is the
-// product of two ex2 values (a few ulp), and the cutoff test compares dxy^2 with
-// (3 sigma)^2 - dz^2 instead of dxy^2 + dz^2 with (3 sigma)^2, so an atom within
-// rounding of the cutoff may be taken or left differently (as with any FP32 distance).
-// The images stay within the FP32 path's bar of the FP64 oracle.
+// Precision: FP32 throughout the march; the weight is the product of two ex2 values (a
+// few ulp).  The FP32 cutoff test may decide an atom within rounding of the cutoff
+// differently from the reference; columns whose field sum is small enough for that to
+// matter re-decide those atoms in the reference's FP64 arithmetic (exact_fix below).
 #pragma once
 #include <cuda_runtime.h>
 
@@ -94,7 +95,7 @@ __device__ bool load_slab3(const ColumnParams& p, const Geo& G, int u, WarpSmem3
   for (int uy = G.uy_lo; uy <= G.uy_hi; ++uy) {
     const int cy = pos_mod(uy, p.Ey);
     const int64_t row_base = (int64_t)p.Ex * (cy + (int64_t)p.Ey * cz);
-    const float yoff = G.a22s * (float)(uy - G.uy_ref);
+    const float yoff = __fmul_rn(G.a22s, (float)(uy - G.uy_ref));
     for (int ux = G.ux_lo; ux <= G.ux_hi;) {
       const int k = floor_div(ux, p.Ex);
       const int run_hi = min(G.ux_hi, (k + 1) * p.Ex - 1);
@@ -110,13 +111,13 @@ __device__ bool load_slab3(const ColumnParams& p, const Geo& G, int u, WarpSmem3
           const float4 r = p.p32[j];
           const int packed = __float_as_int(r.w);
           const int cxu = (packed & 1023) + shift;
-          const float X = fmaf(r.x, G.scale, G.a11s * (float)(cxu - G.ux_ref));
-          const float Y = fmaf(r.y, G.scale, yoff);
+          const float X = __fmaf_rn(r.x, G.scale, __fmul_rn(G.a11s, (float)(cxu - G.ux_ref)));
+          const float Y = __fmaf_rn(r.y, G.scale, yoff);
           const float dx = fmaxf(0.f, fmaxf(G.xmin - X, X - G.xmax));
           const float dy = fmaxf(0.f, fmaxf(G.ymin - Y, Y - G.ymax));
           keep = dx * dx + dy * dy <= G.pre2;
           const float2 cs = p.cs32[j];
-          rec = make_float4(X, Y, r.z * G.scale, cs.x);
+          rec = make_float4(X, Y, __fmul_rn(r.z, G.scale), cs.x);
           sn = cs.y;
         }
         const unsigned m = __ballot_sync(0xffffffffu, keep);
@@ -297,8 +298,9 @@ __device__ __forceinline__ void consume(const float4* __restrict__ BA, const flo
   for (; i + 1 < n; i += 2) {
     const float4 qa = BA[i], qb = BA[i + 1];
     const float4 ea = BE[i], eb = BE[i + 1];
-    const float dxa = qa.x - Xv, dya = qa.y - Yv, dxb = qb.x - Xv, dyb = qb.y - Yv;
-    const float ha = fmaf(dxa, dxa, dya * dya), hb = fmaf(dxb, dxb, dyb * dyb);
+    const float dxa = __fsub_rn(qa.x, Xv), dya = __fsub_rn(qa.y, Yv), dxb = __fsub_rn(qb.x, Xv),
+                dyb = __fsub_rn(qb.y, Yv);
+    const float ha = __fmaf_rn(dxa, dxa, __fmul_rn(dya, dya)), hb = __fmaf_rn(dxb, dxb, __fmul_rn(dyb, dyb));
     const float wa = ex2_approx(-ha), wb = ex2_approx(-hb);
     const float2 wa2 = make_float2(wa, wa), wb2 = make_float2(wb, wb);
     if (ha <= qa.z) a0A = __ffma2_rn(wa2, make_float2(ea.x, ea.y), a0A);
@@ -316,8 +318,8 @@ __device__ __forceinline__ void consume(const float4* __restrict__ BA, const flo
   if (i < n) {
     const float4 qa = BA[i];
     const float4 ea = BE[i];
-    const float dxa = qa.x - Xv, dya = qa.y - Yv;
-    const float ha = fmaf(dxa, dxa, dya * dya);
+    const float dxa = __fsub_rn(qa.x, Xv), dya = __fsub_rn(qa.y, Yv);
+    const float ha = __fmaf_rn(dxa, dxa, __fmul_rn(dya, dya));
     const float wa = ex2_approx(-ha);
     const float2 wa2 = make_float2(wa, wa);
     if (ha <= qa.z) a0A = __ffma2_rn(wa2, make_float2(ea.x, ea.y), a0A);
@@ -342,6 +344,85 @@ __device__ __forceinline__ T aa_at(const T* aa, const float* __restrict__ aag, i
   } else {
     return make_float2(__ldg(aag + 2 * k), __ldg(aag + 2 * k + 1));
   }
+}
+
+// The cutoff in the reference is an FP64 comparison, d.d <= (3 sigma)^2
+// (Lib_LinkCell3D.f90:1594), and the phase field is discontinuous there: a voxel whose only
+// neighbour lies at the cutoff has x = 0 on one side and a unit phasor on the other
+// (S / max(1e-16, |S|), Lib_DynamicalTwoBeamImaging.f90:1877-1892).  The FP32 test may
+// decide an atom within about 3e-5 (scaled r^2) of the cutoff differently.  That changes
+// a voxel with many neighbours by a few 1e-6 in I at most, but a sparse one (a void's rim,
+// or neighbours whose phases cancel) by up to 1e-2.  So after each step the columns whose
+// field sum is small re-decide, in the reference's FP64 arithmetic, every candidate of
+// their 27 cells that the FP32 test placed within kGuard of the cutoff, and correct the sum
+// for each decision that changes.  The FP32 values are recomputed in the same rounded
+// operations as the march, so the candidates and their FP32 decisions are the ones the
+// march made; the FP64 distance uses the cell fractions the binning kept (2^-32 cells).
+constexpr float kGuard = 1e-4f;    // scaled r^2; the FP32 test's error is below 3e-5
+constexpr float kSparse2 = 4.0f;   // |S|^2 below which a column re-decides its near-cutoff atoms
+
+struct Fix {
+  float2 d0, d1;  // corrections of the two slices' sums
+  int dn;         // change of the accepted count
+};
+
+static __device__ __noinline__ Fix exact_fix(const ColumnParams& p, const Geo G, int hx, int hy, double fvx, double fvy,
+                                      float Xv, float Yv, int hz0, int hza, int hzb, float zva, float zvb, double fza,
+                                      double fzb, bool fa, bool fb, float cut2) {
+  Fix r{make_float2(0.f, 0.f), make_float2(0.f, 0.f), 0};
+  const int u_lo = min(fa ? hza : hzb, fb ? hzb : hza) - 1;
+  const int u_hi = max(fa ? hza : hzb, fb ? hzb : hza) + 1;
+  for (int u = u_lo; u <= u_hi; ++u) {
+    const bool oka = fa && u - hza >= -1 && u - hza <= 1;
+    const bool okb = fb && u - hzb >= -1 && u - hzb <= 1;
+    if (!oka && !okb) continue;
+    const int cz = pos_mod(u, p.Ez);
+    const float zoff = __fmul_rn(G.a33s, (float)(u - hz0));
+    const float ta = __fsub_rn(zva, zoff), tb = __fsub_rn(zvb, zoff);
+    for (int ky = -1; ky <= 1; ++ky) {
+      const int uy = hy + ky, cy = pos_mod(uy, p.Ey);
+      const float yoff = __fmul_rn(G.a22s, (float)(uy - G.uy_ref));
+      for (int kx = -1; kx <= 1; ++kx) {
+        const int ux = hx + kx, cx = pos_mod(ux, p.Ex);
+        const float xoff = __fmul_rn(G.a11s, (float)(ux - G.ux_ref));
+        const int64_t cell = cx + (int64_t)p.Ex * (cy + (int64_t)p.Ey * cz);
+        const int j0 = p.cell_start[cell], j1 = p.cell_start[cell + 1];
+        for (int j = j0; j < j1; ++j) {
+          const float4 q = p.p32[j];
+          const float X = __fmaf_rn(q.x, G.scale, xoff), Y = __fmaf_rn(q.y, G.scale, yoff);
+          const float qz = __fmul_rn(q.z, G.scale);
+          const float dx = __fsub_rn(X, Xv), dy = __fsub_rn(Y, Yv);
+          const float h = __fmaf_rn(dx, dx, __fmul_rn(dy, dy));
+#pragma unroll
+          for (int k = 0; k < 2; ++k) {
+            if (!(k == 0 ? oka : okb)) continue;
+            const float dz = __fsub_rn(qz, k == 0 ? ta : tb);
+            const float hm = __fmaf_rn(-dz, dz, cut2);
+            if (!(fabsf(h - hm) <= kGuard)) continue;
+            const bool acc32 = h <= hm;
+            // the reference's distance (:1576-1594): d = a (f + (k - zi_frac)), rounded alike
+            const uint4 fr = p.fr32[j];
+            const double fx = (double)fr.x * 2.3283064365386963e-10, fy = (double)fr.y * 2.3283064365386963e-10,
+                         fz = (double)fr.z * 2.3283064365386963e-10;
+            const int kz = u - (k == 0 ? hza : hzb);
+            const double d0 = __dmul_rn(p.a11, __dadd_rn(fx, __dsub_rn((double)kx, fvx)));
+            const double d1 = __dmul_rn(p.a22, __dadd_rn(fy, __dsub_rn((double)ky, fvy)));
+            const double d2 = __dmul_rn(p.a33, __dadd_rn(fz, __dsub_rn((double)kz, k == 0 ? fza : fzb)));
+            const double dd = __dadd_rn(__dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1)), __dmul_rn(d2, d2));
+            const bool acc64 = dd <= p.cut2;
+            if (acc64 == acc32) continue;
+            const float2 cs = p.cs32[j];
+            const float w = ex2_approx(-h) * ex2_approx(-dz * dz) * (acc64 ? 1.f : -1.f);
+            float2& d = k == 0 ? r.d0 : r.d1;
+            d.x = fmaf(w, cs.x, d.x);
+            d.y = fmaf(w, cs.y, d.y);
+            r.dn += acc64 ? 1 : -1;
+          }
+        }
+      }
+    }
+  }
+  return r;
 }
 
 // One warp tile of one image: the TX x (32 / TX) columns of tile `tile` marched through
@@ -462,11 +543,12 @@ __device__ __noinline__ bool column_tile3(const ColumnParams& p, WarpSmem3<CAPS>
     }
     float2 a0A = make_float2(0.f, 0.f), a1A = a0A, a0B = a0A, a1B = a0A;
     float2 rmA = make_float2(kHuge, kHuge), rmB = rmA;
-    int nb = 0;  // atoms in the step buffer
+    int nb = 0;       // atoms in the step buffer
+    int n_step = 0;   // atoms buffered in this step (warp-uniform)
     for (int u = need_lo; u <= need_hi; ++u) {
       const int slot = u & (kRing - 1);
-      const float zoff = G.a33s * (float)(u - hz0);  // cell u's origin relative to hz0's
-      const float t0 = zv0 - zoff, t1 = zv1 - zoff;
+      const float zoff = __fmul_rn(G.a33s, (float)(u - hz0));  // cell u's origin relative to hz0's
+      const float t0 = __fsub_rn(zv0, zoff), t1 = __fsub_rn(zv1, zoff);
       // slab u serves slice k within the cutoff; with z cells shorter than 3 sigma the
       // reference searches only the 27 cells around each voxel's home cell, so it serves
       // a slice only within one cell of that slice's home z cell
@@ -492,9 +574,9 @@ __device__ __noinline__ bool column_tile3(const ColumnParams& p, WarpSmem3<CAPS>
         if (j < hi) {
           const float4 q = P[j];
           const float sn = S[j];
-          const float dz0 = q.z - t0, dz1 = q.z - t1;
-          const float hm0 = v0 ? cut2 - dz0 * dz0 : -1.f;
-          const float hm1 = v1 ? cut2 - dz1 * dz1 : -1.f;
+          const float dz0 = __fsub_rn(q.z, t0), dz1 = __fsub_rn(q.z, t1);
+          const float hm0 = v0 ? __fmaf_rn(-dz0, dz0, cut2) : -1.f;
+          const float hm1 = v1 ? __fmaf_rn(-dz1, dz1, cut2) : -1.f;
           const float dxr = fmaxf(0.f, fmaxf(G.xmin - q.x, q.x - G.xmax));
           const float dyr = fmaxf(0.f, fmaxf(G.ymin - q.y, q.y - G.ymax));
           // margin: the lanes' own rounding of dxy^2 must not reach below the rectangle's
@@ -515,6 +597,7 @@ __device__ __noinline__ bool column_tile3(const ColumnParams& p, WarpSmem3<CAPS>
           consume<kDensity, kStats>(W.ba, W.be, nb, Xv, Yv, a0A, a1A, a0B, a1B, rmA, rmB, n_acc);
           if (kStats) n_tst += (unsigned long long)nb;
           __syncwarp();
+          n_step += nb;
           nb = 0;
         }
       }
@@ -524,8 +607,26 @@ __device__ __noinline__ bool column_tile3(const ColumnParams& p, WarpSmem3<CAPS>
       consume<kDensity, kStats>(W.ba, W.be, nb, Xv, Yv, a0A, a1A, a0B, a1B, rmA, rmB, n_acc);
       if (kStats) n_tst += (unsigned long long)nb;
       __syncwarp();
+      n_step += nb;
     }
-    const float2 a0 = __fadd2_rn(a0A, a0B), a1 = __fadd2_rn(a1A, a1B);
+    float2 a0 = __fadd2_rn(a0A, a0B), a1 = __fadd2_rn(a1A, a1B);
+    {
+      // sparse or cancelling sums: re-decide the near-cutoff atoms exactly (see exact_fix)
+      const bool f0 = active && n_step > 0 && fmaf(a0.x, a0.x, a0.y * a0.y) < kSparse2;
+      const bool f1 = active && n_step > 0 && has1 && fmaf(a1.x, a1.x, a1.y * a1.y) < kSparse2;
+      if (__any_sync(0xffffffffu, f0 || f1)) {
+        if (f0 || f1) {
+          const Fix fx = exact_fix(p, G, hx, hy, fvx, fvy, Xv, Yv, hz0, hz0, hz1, zv0, zv1, p.zfv[z0],
+                                   has1 ? p.zfv[z0 + 1] : 0.0, f0, f1, cut2);
+          a0.x += fx.d0.x;
+          a0.y += fx.d0.y;
+          a1.x += fx.d1.x;
+          a1.y += fx.d1.y;
+          if (kStats) n_acc += (unsigned)fx.dn;
+        }
+        __syncwarp();
+      }
+    }
     const float rm0 = (cut2 + fminf(rmA.x, rmB.x)) * r2_to_A2, rm1 = (cut2 + fminf(rmA.y, rmB.y)) * r2_to_A2;
     // field samples z0 (even) and z0 + 1 (odd), then the RK4 double step (z0-2, z0-1, z0)
     const Sample s0 = make_sample<kDensity>(a0.x, a0.y, rm0, b0, bg, sig, p.use_density != 0);

@@ -214,7 +214,7 @@ def test_host_batch_equals_device_batch(ctx, fp32):
 
 
 def test_ring_variants_agree_and_autotuned():
-    """The slab-ring variants (kernel generation, tile shape 8 x 4 / 4 x 8 / 16 x 2, slab
+    """The slab-ring variants (tile shape 8 x 4 / 4 x 8 / 16 x 2, slab
     capacity 96 / 128, CTAs per SM): every variant within the FP32 bar of the oracle;
     variants that differ only in slab capacity or occupancy compute the same image to the
     last bit.  With ST_TUNE_AUTO a context times them all on its first large pass, keeps
@@ -224,7 +224,7 @@ def test_ring_variants_agree_and_autotuned():
     G, aa = t.image_geometry(len(x), n_prec=3)
     flags = _lib.ST_FLAG_FP32 | _lib.ST_FLAG_AVERAGE
     n_var = _lib.lib().st_tune_variants()
-    assert n_var == 8
+    assert n_var == 6
     imgs = []
     c = imaging.Context(0)
     try:
@@ -243,7 +243,7 @@ def test_ring_variants_agree_and_autotuned():
             c.tune(n_var)
     finally:
         c.close()
-    for a_, b_ in ((0, 1), (2, 3), (4, 5), (6, 7)):
+    for a_, b_ in ((0, 1), (2, 3), (4, 5)):
         assert np.array_equal(imgs[a_], imgs[b_])
     assert np.array_equal(auto, imgs[chosen]) and np.array_equal(again, imgs[chosen])
     Go, aao = O.geometry(so, len(x), nPrec=3, precAngle=0.005)
