@@ -59,6 +59,7 @@ struct BinnedAtoms {
   float4* p32;         // a_col11*fx, a_col22*fy, a_col33*fz, bits(packed cell)
   float2* cs32;        // cos, sin of the FP64-reduced phase
   uint4* fr32;         // 2^-32 units of the cell fractions (x, y, z, -): the cutoff's exact recheck
+  float* ph32;         // the FP64-reduced phase in cycles, [-1/2, 1/2)
 };
 
 // A kept atom's record of the FP32 path as the binning makes it (same size as double4_32a).
@@ -115,6 +116,7 @@ struct ColumnParams {
   const float4* p32;
   const float2* cs32;
   const uint4* fr32;
+  const float* ph32;
   const int2* xtab;
   const double* xfv;
   const int2* ytab;

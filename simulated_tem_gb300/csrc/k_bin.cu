@@ -430,6 +430,7 @@ __global__ void __launch_bounds__(256) k_bin_finalize(const BinParams* __restric
       b.p32[s + r] = rec[0];
       b.cs32[s + r] = make_float2(cf, sf);
       b.fr32[s + r] = make_uint4(__float_as_uint(hi.y), __float_as_uint(hi.z), __float_as_uint(hi.w), 0u);
+      b.ph32[s + r] = hi.x;
     } else {
       const int job = n_jobs == 1 ? 0 : find_job(n_jobs, cell, [&](int k) { return jobs[k].cell_base; });
       const BinParams& p = jobs[job];

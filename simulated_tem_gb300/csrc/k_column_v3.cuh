@@ -53,8 +53,8 @@ constexpr float kHuge = FLT_MAX;
 
 template <int CAPS>  // staged atoms per slab
 struct WarpSmem3 {
-  float4 p[kRing][CAPS];      // X', Y' (warp frame), z (own cell), cos -- lengths scaled by s
-  float s[kRing][CAPS];       // sin
+  float4 p[kRing][CAPS];      // X', Y' (warp frame), z (own cell), phase (cycles) -- lengths scaled by s
+  int gi[kRing][CAPS];        // index of the kept atom (its records in global memory)
   int bin[kRing][kBins + 1];  // bin[b]: first atom of z bin b; bin[kBins] = count
   int count[kRing];
   float4 ba[kBuf];            // step buffer: X', Y', hmax_0, hmax_1
@@ -90,7 +90,7 @@ __device__ bool load_slab3(const ColumnParams& p, const Geo& G, int u, WarpSmem3
   const int cz = pos_mod(u, p.Ez);
   const int slot = u & (kRing - 1);
   float4* P = W.p[slot];
-  float* S = W.s[slot];
+  int* GI = W.gi[slot];
   int n = 0;
   for (int uy = G.uy_lo; uy <= G.uy_hi; ++uy) {
     const int cy = pos_mod(uy, p.Ey);
@@ -106,7 +106,6 @@ __device__ bool load_slab3(const ColumnParams& p, const Geo& G, int u, WarpSmem3
         const int j = b + lane;
         bool keep = false;
         float4 rec = make_float4(0.f, 0.f, 0.f, 0.f);
-        float sn = 0.f;
         if (j < a_hi) {
           const float4 r = p.p32[j];
           const int packed = __float_as_int(r.w);
@@ -116,9 +115,7 @@ __device__ bool load_slab3(const ColumnParams& p, const Geo& G, int u, WarpSmem3
           const float dx = fmaxf(0.f, fmaxf(G.xmin - X, X - G.xmax));
           const float dy = fmaxf(0.f, fmaxf(G.ymin - Y, Y - G.ymax));
           keep = dx * dx + dy * dy <= G.pre2;
-          const float2 cs = p.cs32[j];
-          rec = make_float4(X, Y, __fmul_rn(r.z, G.scale), cs.x);
-          sn = cs.y;
+          rec = make_float4(X, Y, __fmul_rn(r.z, G.scale), p.ph32[j]);
         }
         const unsigned m = __ballot_sync(0xffffffffu, keep);
         const int cnt = __popc(m);
@@ -126,7 +123,7 @@ __device__ bool load_slab3(const ColumnParams& p, const Geo& G, int u, WarpSmem3
         if (keep) {
           const int d = n + __popc(m & ((1u << lane) - 1));
           P[d] = rec;
-          S[d] = sn;
+          GI[d] = j;
         }
         n += cnt;
       }
@@ -142,7 +139,7 @@ __device__ bool load_slab3(const ColumnParams& p, const Geo& G, int u, WarpSmem3
   for (int b = lane; b <= kBins; b += 32) hist[b] = 0;
   __syncwarp();
   float4 e[kPer];
-  float es[kPer];
+  int es[kPer];
   int eb[kPer], er[kPer];
   const unsigned lt = (1u << lane) - 1;
 #pragma unroll
@@ -150,13 +147,13 @@ __device__ bool load_slab3(const ColumnParams& p, const Geo& G, int u, WarpSmem3
     const int i = lane + 32 * k;
     const bool valid = i < n;
     e[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-    es[k] = 0.f;
+    es[k] = 0;
     eb[k] = 0;
     er[k] = 0;
     const unsigned act = __ballot_sync(0xffffffffu, valid);
     if (valid) {
       e[k] = P[i];
-      es[k] = S[i];
+      es[k] = GI[i];
       eb[k] = min(kBins - 1, max(0, (int)floorf(e[k].z * inv_bin)));
       const unsigned m = __match_any_sync(act, eb[k]);
       er[k] = hist[eb[k]] + __popc(m & lt);
@@ -183,7 +180,7 @@ __device__ bool load_slab3(const ColumnParams& p, const Geo& G, int u, WarpSmem3
     if (lane + 32 * k < n) {
       const int d = hist[eb[k]] + er[k];
       P[d] = e[k];
-      S[d] = es[k];
+      GI[d] = es[k];
     }
   }
   __syncwarp();
@@ -353,72 +350,95 @@ __device__ __forceinline__ T aa_at(const T* aa, const float* __restrict__ aag, i
 // decide an atom within about 3e-5 (scaled r^2) of the cutoff differently.  That changes
 // a voxel with many neighbours by a few 1e-6 in I at most, but a sparse one (a void's rim,
 // or neighbours whose phases cancel) by up to 1e-2.  So after each step the columns whose
-// field sum is small re-decide, in the reference's FP64 arithmetic, every candidate of
-// their 27 cells that the FP32 test placed within kGuard of the cutoff, and correct the sum
-// for each decision that changes.  The FP32 values are recomputed in the same rounded
-// operations as the march, so the candidates and their FP32 decisions are the ones the
-// march made; the FP64 distance uses the cell fractions the binning kept (2^-32 cells).
-constexpr float kGuard = 1e-4f;    // scaled r^2; the FP32 test's error is below 3e-5
-constexpr float kSparse2 = 4.0f;   // |S|^2 below which a column re-decides its near-cutoff atoms
+// field sum is small rescan the step's resident slabs, re-decide in the reference's FP64
+// arithmetic every atom the FP32 test placed within kGuard of the cutoff, and correct the
+// sum for each decision that changes.  The rescan repeats the march's FP32 operations on
+// the same staged values, so it meets the same decisions; the FP64 distance uses the cell
+// fractions the binning kept (2^-32 cells) and the reference's per-axis form
+// d = a (f + (k - zi_frac)).
+constexpr float kGuard = 1e-4f;  // scaled r^2; the FP32 test's error is below 3e-5
+// |S|^2 below which a column re-decides its near-cutoff atoms.  A flipped atom weighs
+// exp(-9/2) = 0.011 and moves x = S / |S| by at most 0.011 |e^(i phi) - x| / |S|; above
+// |S| = 1/2, with the few-tenths-of-a-radian phase spread of neighbouring atoms, that
+// changes I by a few 1e-5 at most.
+constexpr float kSparse2 = 0.25f;
+
+__device__ __forceinline__ int wrap_diff(int c, int h, int n) {  // c - h in -(n/2) .. n/2, periodic
+  int d = c - h;
+  if (d > n / 2) d -= n;
+  else if (d < -(n / 2)) d += n;
+  return d;
+}
+
+struct Slice {
+  int hz;       // home z cell
+  float zv;     // scaled depth from the origin of the step's even home cell
+  double fz;    // fractional position in the home cell (FP64)
+  bool want;    // this lane re-decides this slice
+};
+
+// One lane's exact re-decision of slice sl against staged atom j of `slot` (cell u).
+template <int CAPS>
+__device__ __forceinline__ void exact_one(const ColumnParams& p, const WarpSmem3<CAPS>& W, int slot, int j, float h,
+                                          float dz, bool acc32, int hx, int hy, double fvx, double fvy,
+                                          const Slice& sl, float2& S, int& dn) {
+  const int gi = W.gi[slot][j];
+  const int packed = __float_as_int(p.p32[gi].w);
+  const int kx = wrap_diff(packed & 1023, hx, p.Ex), ky = wrap_diff((packed >> 10) & 1023, hy, p.Ey);
+  const int kz = wrap_diff(packed >> 20, sl.hz, p.Ez);
+  const uint4 fr = p.fr32[gi];
+  const double fx = (double)fr.x * 2.3283064365386963e-10, fy = (double)fr.y * 2.3283064365386963e-10,
+               fz = (double)fr.z * 2.3283064365386963e-10;
+  const double d0 = __dmul_rn(p.a11, __dadd_rn(fx, __dsub_rn((double)kx, fvx)));
+  const double d1 = __dmul_rn(p.a22, __dadd_rn(fy, __dsub_rn((double)ky, fvy)));
+  const double d2 = __dmul_rn(p.a33, __dadd_rn(fz, __dsub_rn((double)kz, sl.fz)));
+  const double dd = __dadd_rn(__dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1)), __dmul_rn(d2, d2));
+  const bool acc64 = dd <= p.cut2;
+  if (acc64 == acc32) return;
+  float sn, cs;
+  __sincosf(6.28318531f * W.p[slot][j].w, &sn, &cs);
+  const float w = ex2_approx(-h) * ex2_approx(-dz * dz) * (acc64 ? 1.f : -1.f);
+  S.x = fmaf(w, cs, S.x);
+  S.y = fmaf(w, sn, S.y);
+  dn += acc64 ? 1 : -1;
+}
 
 struct Fix {
   float2 d0, d1;  // corrections of the two slices' sums
   int dn;         // change of the accepted count
 };
 
-static __device__ __noinline__ Fix exact_fix(const ColumnParams& p, const Geo G, int hx, int hy, double fvx, double fvy,
-                                      float Xv, float Yv, int hz0, int hza, int hzb, float zva, float zvb, double fza,
-                                      double fzb, bool fa, bool fb, float cut2) {
+// The rescan of one step (slabs need_lo .. need_hi of the ring) for the lanes that want it.
+template <int CAPS>
+__device__ __noinline__ Fix exact_fix(const ColumnParams& p, const WarpSmem3<CAPS>& W, int need_lo, int need_hi,
+                                      int hz0, float a33s, float cut2, float r3, float inv_bin, float Xv, float Yv,
+                                      int hx, int hy, double fvx, double fvy, Slice s0, Slice s1, bool has1) {
   Fix r{make_float2(0.f, 0.f), make_float2(0.f, 0.f), 0};
-  const int u_lo = min(fa ? hza : hzb, fb ? hzb : hza) - 1;
-  const int u_hi = max(fa ? hza : hzb, fb ? hzb : hza) + 1;
-  for (int u = u_lo; u <= u_hi; ++u) {
-    const bool oka = fa && u - hza >= -1 && u - hza <= 1;
-    const bool okb = fb && u - hzb >= -1 && u - hzb <= 1;
-    if (!oka && !okb) continue;
-    const int cz = pos_mod(u, p.Ez);
-    const float zoff = __fmul_rn(G.a33s, (float)(u - hz0));
-    const float ta = __fsub_rn(zva, zoff), tb = __fsub_rn(zvb, zoff);
-    for (int ky = -1; ky <= 1; ++ky) {
-      const int uy = hy + ky, cy = pos_mod(uy, p.Ey);
-      const float yoff = __fmul_rn(G.a22s, (float)(uy - G.uy_ref));
-      for (int kx = -1; kx <= 1; ++kx) {
-        const int ux = hx + kx, cx = pos_mod(ux, p.Ex);
-        const float xoff = __fmul_rn(G.a11s, (float)(ux - G.ux_ref));
-        const int64_t cell = cx + (int64_t)p.Ex * (cy + (int64_t)p.Ey * cz);
-        const int j0 = p.cell_start[cell], j1 = p.cell_start[cell + 1];
-        for (int j = j0; j < j1; ++j) {
-          const float4 q = p.p32[j];
-          const float X = __fmaf_rn(q.x, G.scale, xoff), Y = __fmaf_rn(q.y, G.scale, yoff);
-          const float qz = __fmul_rn(q.z, G.scale);
-          const float dx = __fsub_rn(X, Xv), dy = __fsub_rn(Y, Yv);
-          const float h = __fmaf_rn(dx, dx, __fmul_rn(dy, dy));
-#pragma unroll
-          for (int k = 0; k < 2; ++k) {
-            if (!(k == 0 ? oka : okb)) continue;
-            const float dz = __fsub_rn(qz, k == 0 ? ta : tb);
-            const float hm = __fmaf_rn(-dz, dz, cut2);
-            if (!(fabsf(h - hm) <= kGuard)) continue;
-            const bool acc32 = h <= hm;
-            // the reference's distance (:1576-1594): d = a (f + (k - zi_frac)), rounded alike
-            const uint4 fr = p.fr32[j];
-            const double fx = (double)fr.x * 2.3283064365386963e-10, fy = (double)fr.y * 2.3283064365386963e-10,
-                         fz = (double)fr.z * 2.3283064365386963e-10;
-            const int kz = u - (k == 0 ? hza : hzb);
-            const double d0 = __dmul_rn(p.a11, __dadd_rn(fx, __dsub_rn((double)kx, fvx)));
-            const double d1 = __dmul_rn(p.a22, __dadd_rn(fy, __dsub_rn((double)ky, fvy)));
-            const double d2 = __dmul_rn(p.a33, __dadd_rn(fz, __dsub_rn((double)kz, k == 0 ? fza : fzb)));
-            const double dd = __dadd_rn(__dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1)), __dmul_rn(d2, d2));
-            const bool acc64 = dd <= p.cut2;
-            if (acc64 == acc32) continue;
-            const float2 cs = p.cs32[j];
-            const float w = ex2_approx(-h) * ex2_approx(-dz * dz) * (acc64 ? 1.f : -1.f);
-            float2& d = k == 0 ? r.d0 : r.d1;
-            d.x = fmaf(w, cs.x, d.x);
-            d.y = fmaf(w, cs.y, d.y);
-            r.dn += acc64 ? 1 : -1;
-          }
-        }
+  for (int u = need_lo; u <= need_hi; ++u) {
+    const int slot = u & (kRing - 1);
+    const float zoff = __fmul_rn(a33s, (float)(u - hz0));
+    const float t0 = __fsub_rn(s0.zv, zoff), t1 = __fsub_rn(s1.zv, zoff);
+    bool v0 = true, v1 = has1;  // the march's slab rule (27 cells in z for short cells)
+    if (p.trunc_z) {
+      v0 = u - s0.hz >= -1 && u - s0.hz <= 1;
+      v1 = has1 && u - s1.hz >= -1 && u - s1.hz <= 1;
+    }
+    if (!v0 && !v1) continue;
+    const float w_lo = v0 ? t0 : t1, w_hi = v1 ? t1 : t0;
+    const int b_lo = max(0, min(kBins, (int)floorf((w_lo - r3) * inv_bin)));
+    const int b_hi = max(0, min(kBins, (int)ceilf((w_hi + r3) * inv_bin)));
+    const int lo = W.bin[slot][b_lo], hi = W.bin[slot][b_hi];
+    for (int j = lo; j < hi; ++j) {
+      const float4 q = W.p[slot][j];
+      const float dx = __fsub_rn(q.x, Xv), dy = __fsub_rn(q.y, Yv);
+      const float h = __fmaf_rn(dx, dx, __fmul_rn(dy, dy));
+      if (s0.want && v0) {
+        const float dz = __fsub_rn(q.z, t0), hm = __fmaf_rn(-dz, dz, cut2);
+        if (fabsf(h - hm) <= kGuard) exact_one(p, W, slot, j, h, dz, h <= hm, hx, hy, fvx, fvy, s0, r.d0, r.dn);
+      }
+      if (s1.want && v1) {
+        const float dz = __fsub_rn(q.z, t1), hm = __fmaf_rn(-dz, dz, cut2);
+        if (fabsf(h - hm) <= kGuard) exact_one(p, W, slot, j, h, dz, h <= hm, hx, hy, fvx, fvy, s1, r.d1, r.dn);
       }
     }
   }
@@ -564,7 +584,6 @@ __device__ __noinline__ bool column_tile3(const ColumnParams& p, WarpSmem3<CAPS>
       const int lo = W.bin[slot][b_lo];
       const int hi = W.bin[slot][b_hi];
       const float4* P = W.p[slot];
-      const float* S = W.s[slot];
       for (int b = lo; b < hi; b += 32) {
         // cooperative pass: one atom per lane, its depth-only terms, kept if some column
         // of the patch can accept it at some slice
@@ -573,7 +592,8 @@ __device__ __noinline__ bool column_tile3(const ColumnParams& p, WarpSmem3<CAPS>
         float4 A, E;
         if (j < hi) {
           const float4 q = P[j];
-          const float sn = S[j];
+          float sn, cs;
+          __sincosf(6.28318531f * q.w, &sn, &cs);  // the phase lies in [-1/2, 1/2) cycles
           const float dz0 = __fsub_rn(q.z, t0), dz1 = __fsub_rn(q.z, t1);
           const float hm0 = v0 ? __fmaf_rn(-dz0, dz0, cut2) : -1.f;
           const float hm1 = v1 ? __fmaf_rn(-dz1, dz1, cut2) : -1.f;
@@ -583,7 +603,7 @@ __device__ __noinline__ bool column_tile3(const ColumnParams& p, WarpSmem3<CAPS>
           keep = fmaf(dxr, dxr, dyr * dyr) <= fmaxf(hm0, hm1) * 1.0001f + 1e-4f;
           const float wz0 = ex2_approx(-dz0 * dz0), wz1 = ex2_approx(-dz1 * dz1);
           A = make_float4(q.x, q.y, hm0, hm1);
-          E = make_float4(wz0 * q.w, wz0 * sn, wz1 * q.w, wz1 * sn);
+          E = make_float4(wz0 * cs, wz0 * sn, wz1 * cs, wz1 * sn);
         }
         const unsigned m = __ballot_sync(0xffffffffu, keep);
         if (keep) {
@@ -616,8 +636,9 @@ __device__ __noinline__ bool column_tile3(const ColumnParams& p, WarpSmem3<CAPS>
       const bool f1 = active && n_step > 0 && has1 && fmaf(a1.x, a1.x, a1.y * a1.y) < kSparse2;
       if (__any_sync(0xffffffffu, f0 || f1)) {
         if (f0 || f1) {
-          const Fix fx = exact_fix(p, G, hx, hy, fvx, fvy, Xv, Yv, hz0, hz0, hz1, zv0, zv1, p.zfv[z0],
-                                   has1 ? p.zfv[z0 + 1] : 0.0, f0, f1, cut2);
+          const Slice sl0{hz0, zv0, p.zfv[z0], f0}, sl1{hz1, zv1, has1 ? p.zfv[z0 + 1] : 0.0, f1};
+          const Fix fx = exact_fix<CAPS>(p, W, need_lo, need_hi, hz0, G.a33s, cut2, r3, inv_bin, Xv, Yv, hx, hy,
+                                         fvx, fvy, sl0, sl1, has1);
           a0.x += fx.d0.x;
           a0.y += fx.d0.y;
           a1.x += fx.d1.x;

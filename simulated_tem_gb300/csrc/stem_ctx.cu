@@ -139,6 +139,7 @@ bool alloc_kept(st_ctx* c, size_t need) {
   grow(c->b.p32);
   grow(c->b.cs32);
   grow(c->b.fr32);
+  grow(c->b.ph32);
   if (e != cudaSuccess) return false;
   c->cap_kept = k;
   c->s.cap_candidates = k;
@@ -293,6 +294,7 @@ void point_at_kept(const st_ctx* c, ColumnParams& cp) {
   cp.p32 = c->b.p32;
   cp.cs32 = c->b.cs32;
   cp.fr32 = c->b.fr32;
+  cp.ph32 = c->b.ph32;
 }
 
 ColumnParams column_params(st_ctx* c, const Job& j, int64_t cell_base, size_t xoff, size_t yoff, size_t zoff,
@@ -834,7 +836,7 @@ extern "C" void st_destroy(st_ctx* c) {
   void* dev_ptrs[] = {c->s.tmp_key, c->s.tmp_cell, c->s.tmp_slot, c->s.tmp_f, c->s.perm, c->s.block_sums,
                       c->s.counters, c->s.xtab, c->s.xfv, c->s.ytab, c->s.yfv, c->s.ztab, c->s.zfv, c->s.aa,
                       c->s.aaf, c->b.cell_start, c->b.cell_count, c->b.f64, c->b.cs64, c->b.p32, c->b.cs32,
-                      c->b.fr32, c->d_x, c->d_img, c->d_blur, c->d_kern, c->d_binjobs, c->d_coljobs, c->d_work, c->d_bx, c->d_bimg,
+                      c->b.fr32, c->b.ph32, c->d_x, c->d_img, c->d_blur, c->d_kern, c->d_binjobs, c->d_coljobs, c->d_work, c->d_bx, c->d_bimg,
                       c->d_lvaux, c->d_levels, c->d_text, c->d_pseg, c->d_pstart, c->d_pbad, c->d_geom, c->d_tilt, c->d_keys, c->d_species};
   for (void* p : dev_ptrs)
     if (p) cudaFree(p);
