@@ -216,7 +216,8 @@ int st_get_stats(const st_ctx* ctx, st_stats* out);
  * intermediate (the x-pass image and its column weights) lives in a fixed
  * file-scope device array that every GPU loading the library holds until the
  * process exits; larger images than the limits above return ST_ERR_ARG with
- * the reason in err.  The first call on each device looks that array's device
+ * the reason in err.  The first call in each CUDA context (per device, and again
+ * after a device reset or under another context) looks that array's device
  * address up (cudaGetSymbolAddress, which may load the library's GPU module):
  * make that first call outside any stream capture.  Calls share the array and
  * it keeps the last call's contents; every entry is rewritten before it is

@@ -13,6 +13,7 @@
 // the weights are computed on the host exactly as st_blur computes them and
 // passed by value to the kernels, and the sums run in the same order, so the
 // output is identical to st_blur's.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -24,17 +25,49 @@
 
 namespace {
 
-constexpr int kMaxDevices = 64;
+constexpr int kMaxContexts = 64;
 constexpr int64_t kScratchDoubles = (int64_t)ST_BLUR_NOALLOC_MAX_PIXELS + ST_BLUR_NOALLOC_MAX_NX;
 
 // The scratch: x-pass image (nx * ny doubles) followed by w_stripe (nx doubles).
 static __device__ __align__(256) double g_blur_scratch[kScratchDoubles];
 
-// Device addresses of g_blur_scratch, one per device, looked up once.  In
-// host code the name g_blur_scratch is only a host-side stand-in for the
-// device array, so the kernels receive the looked-up address.
-double* g_scratch_addr[kMaxDevices] = {nullptr};
+// Device addresses of g_blur_scratch, looked up once per CUDA context (the module, and so
+// the array, is loaded per context).  In host code the name g_blur_scratch is only a
+// host-side stand-in for the device array, so the kernels receive the looked-up address.
+// The cache is keyed on the context's unique ID (cuCtxGetId), not on the device ordinal or
+// the context handle: after a device reset, or under another context of the same device,
+// the first call looks the address up again.
+struct ScratchAddr {
+  unsigned long long ctx_id;
+  double* addr;
+};
+ScratchAddr g_scratch_addr[kMaxContexts] = {};
+int g_scratch_next = 0;
 std::mutex g_setup_mutex;
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
+
+// The unique ID of the calling thread's current context (driver entry points fetched through
+// the runtime, so the library does not link the driver library itself); 0 on failure.
+unsigned long long current_context_id() {
+  if (!g_ctx_get_current || !g_ctx_get_id) {
+    void* f0 = nullptr;
+    void* f1 = nullptr;
+    cudaDriverEntryPointQueryResult q0, q1;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f0, 12000, cudaEnableDefault, &q0) != cudaSuccess ||
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &f1, 12000, cudaEnableDefault, &q1) != cudaSuccess ||
+        q0 != cudaDriverEntryPointSuccess || q1 != cudaDriverEntryPointSuccess)
+      return 0;
+    g_ctx_get_current = reinterpret_cast<CtxGetCurrentFn>(f0);
+    g_ctx_get_id = reinterpret_cast<CtxGetIdFn>(f1);
+  }
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (g_ctx_get_current(&ctx) != CUDA_SUCCESS || !ctx || g_ctx_get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
 
 struct BlurWeights {
   int nk;
@@ -108,21 +141,25 @@ extern "C" int st_blur_noalloc(const double* d_in, int32_t nx, int32_t ny, doubl
   w.k[0] = 1.0;
   for (int i = 1; i <= w.nk; ++i) w.k[i] = std::exp(-(i * i * i2s2));
 
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return report(err, err_len, ST_ERR_CUDA, cudaGetErrorString(e));
-  if (dev < 0 || dev >= kMaxDevices) return report(err, err_len, ST_ERR_ARG, "st_blur_noalloc: device index too large");
+  cudaError_t e = cudaSuccess;
   double* scratch = nullptr;
   {
-    // once per device, with that device current: the device address of the scratch array
+    // once per context, with it current: the device address of the scratch array (a thread
+    // without a current context gets the device's primary context from this first lookup)
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_addr[dev]) {
+    unsigned long long id = current_context_id();
+    for (const ScratchAddr& a : g_scratch_addr)
+      if (id != 0 && a.ctx_id == id) scratch = a.addr;
+    if (!scratch) {
       void* p = nullptr;
       e = cudaGetSymbolAddress(&p, g_blur_scratch);
       if (e != cudaSuccess) return report(err, err_len, ST_ERR_CUDA, cudaGetErrorString(e));
-      g_scratch_addr[dev] = static_cast<double*>(p);
+      scratch = static_cast<double*>(p);
+      if (id == 0) id = current_context_id();
+      if (id == 0) return report(err, err_len, ST_ERR_CUDA, "st_blur_noalloc: no current CUDA context");
+      g_scratch_addr[g_scratch_next] = ScratchAddr{id, scratch};
+      g_scratch_next = (g_scratch_next + 1) % kMaxContexts;
     }
-    scratch = g_scratch_addr[dev];
   }
   const int64_t n = (int64_t)nx * ny;
   int blocks = (int)((n + 255) / 256);

@@ -105,6 +105,9 @@ struct ColumnParams {
   int check_cells;  // restrict to the 27 cells around the home cell (needed when a cell is < 3 sigma)
   int trunc_z;      // the z cells are shorter than 3 sigma (the slab ring applies the 27-cell rule in z)
   int want_stats;
+  int finalize;          // the slab ring's last pass: write (sum) / fin_scale, or 1 - that when fin_bright
+  int fin_bright;
+  double fin_scale;
   double a11, a22, a33;  // link-cell sides (cuboid)
   double cut2;           // (3 sigma)^2
   double i2s2;           // 1 / (2 sigma^2)

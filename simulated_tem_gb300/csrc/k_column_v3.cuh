@@ -681,8 +681,15 @@ __device__ __noinline__ bool column_tile3(const ColumnParams& p, WarpSmem3<CAPS>
     }
   }
   if (active && wanted) {
+    // the precession average and the bright-field flip fold into the last pass's store,
+    // in the separate epilogue's arithmetic (k_epilogue)
     double* o = p.img + ix + (int64_t)p.Mx * iy;
-    *o = p.accumulate ? *o + (double)acc : (double)acc;
+    double v = p.accumulate ? *o + (double)acc : (double)acc;
+    if (p.finalize) {
+      v = __ddiv_rn(v, p.fin_scale);
+      if (p.fin_bright) v = __dsub_rn(1.0, v);
+    }
+    *o = v;
   }
   if (kStats) {
     unsigned long long acc_w = active ? n_acc : 0u, tst_w = active ? 2 * n_tst : 0u;

@@ -349,14 +349,15 @@ __global__ void __launch_bounds__(1024) k_image_mean(const double* __restrict__ 
 __global__ void k_resample_planes(const double* __restrict__ img2, int Mx2, int My2, int Mx8, int My8, int Wp, int Hp,
                                   float sg_value, const double* __restrict__ mean, float contrast,
                                   float* __restrict__ planes) {
-  // grid: x over the row's pixels, y over the rows (no 64-bit division per pixel)
+  // grid: x over the row's pixels, y over the rows, striding by the grid's height (at most
+  // 65,535 rows per launch) -- no 64-bit division per pixel
   const long long n = (long long)Wp * Hp;
-  const int qx = blockIdx.x * blockDim.x + threadIdx.x, qy = blockIdx.y;
-  if (qx >= Wp || qy >= Hp) return;
-  const long long i = (long long)qy * Wp + qx;
+  const int qx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (qx >= Wp) return;
   const double sx = (double)Mx2 / Mx8, sy = (double)My2 / My8;
   const double mu = *mean;
-  {
+  for (int qy = blockIdx.y; qy < Hp; qy += gridDim.y) {
+    const long long i = (long long)qy * Wp + qx;
     const int px = min(qx, Mx8 - 1), py = min(qy, My8 - 1);
     const double u = px * sx, v = py * sy;
     int i0 = min((int)floor(u), Mx2 - 1), j0 = min((int)floor(v), My2 - 1);
@@ -375,14 +376,14 @@ __global__ void k_resample_planes(const double* __restrict__ img2, int Mx2, int 
 
 // out (FP64, Mx8 x My8 column-major) = base + pred[p][0] * scale, p over the Hp x Wp
 // grid's top-left My8 x Mx8 block.
-// grid: (pixels of a row, rows)
+// grid: (pixels of a row, rows), the rows striding by the grid's height
 __global__ void k_apply_correction(const float* __restrict__ base, const float* __restrict__ pred, int Cp, int Mx8,
                                    int My8, int Wp, float scale, double* __restrict__ out) {
-  const int y = blockIdx.y;
-  for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < Mx8; x += gridDim.x * blockDim.x) {
-    const long long i = (long long)y * Mx8 + x, p = (long long)y * Wp + x;
-    out[i] = (double)base[p] + (double)pred[p * Cp] * (double)scale;
-  }
+  for (int y = blockIdx.y; y < My8; y += gridDim.y)
+    for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < Mx8; x += gridDim.x * blockDim.x) {
+      const long long i = (long long)y * Mx8 + x, p = (long long)y * Wp + x;
+      out[i] = (double)base[p] + (double)pred[p * Cp] * (double)scale;
+    }
 }
 
 // tile_max[ty][tx] = max |pred[p][ch]| over the T x T tile (inside Mx8 x My8); one block per tile
@@ -431,14 +432,15 @@ __global__ void __launch_bounds__(1024) k_tile_flags(const float* __restrict__ t
 
 // out[tile] = fine[tile] for every tile whose mask byte is nonzero (FP64 images, Mx x My
 // column-major)
-// grid: (pixels of a row, rows)
+// grid: (pixels of a row, rows), the rows striding by the grid's height
 __global__ void k_merge_tiles(const double* __restrict__ fine, const unsigned char* __restrict__ mask, int ntx, int T,
                               int Mx, int My, double* __restrict__ out) {
-  const int y = blockIdx.y;
-  const unsigned char* mrow = mask + (y / T) * ntx;
-  for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < Mx; x += gridDim.x * blockDim.x) {
-    const long long i = (long long)y * Mx + x;
-    if (mrow[x / T]) out[i] = fine[i];
+  for (int y = blockIdx.y; y < My; y += gridDim.y) {
+    const unsigned char* mrow = mask + (y / T) * ntx;
+    for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < Mx; x += gridDim.x * blockDim.x) {
+      const long long i = (long long)y * Mx + x;
+      if (mrow[x / T]) out[i] = fine[i];
+    }
   }
 }
 
@@ -543,17 +545,16 @@ int image_mean(const double* img, long long n, double* mean, cudaStream_t st) {
 int resample_planes(const double* img2, int Mx2, int My2, int Mx8, int My8, int Wp, int Hp, float sg_value,
                     const double* mean, float contrast, float* planes, cudaStream_t st) {
   if (!img2 || !planes || !mean || Mx2 < 1 || My2 < 1 || Mx8 < 1 || My8 < 1 || Wp < Mx8 || Hp < My8) return 1;
-  if (Hp > 65535) return 1;
-  const dim3 grid((Wp + kBlock - 1) / kBlock, Hp);
+  const dim3 grid((Wp + kBlock - 1) / kBlock, Hp < 65535 ? Hp : 65535);
   k_resample_planes<<<grid, kBlock, 0, st>>>(img2, Mx2, My2, Mx8, My8, Wp, Hp, sg_value, mean, contrast, planes);
   return status();
 }
 int apply_correction(const float* base, const float* pred, int Cp, int Mx8, int My8, int Wp, float scale, double* out,
                      cudaStream_t st) {
-  if (!base || !pred || !out || Wp < Mx8 || My8 > 65535) return 1;
+  if (!base || !pred || !out || Wp < Mx8) return 1;
   if (Mx8 < 1 || My8 < 1) return 0;
-  k_apply_correction<<<dim3((Mx8 + kBlock - 1) / kBlock, My8), kBlock, 0, st>>>(base, pred, Cp, Mx8, My8, Wp, scale,
-                                                                                 out);
+  k_apply_correction<<<dim3((Mx8 + kBlock - 1) / kBlock, My8 < 65535 ? My8 : 65535), kBlock, 0, st>>>(
+      base, pred, Cp, Mx8, My8, Wp, scale, out);
   return status();
 }
 int tile_maxabs(const float* pred, int Cp, int ch, int Mx8, int My8, int Wp, int T, float* tile_max, cudaStream_t st) {
@@ -572,8 +573,8 @@ int merge_tiles(const double* fine, const unsigned char* mask, int ntx, int T, i
                 cudaStream_t st) {
   if (!fine || !mask || !out || T < 1 || ntx < (Mx + T - 1) / T) return 1;
   if (My < 1 || Mx < 1) return 0;
-  if (My > 65535) return 1;
-  k_merge_tiles<<<dim3((Mx + kBlock - 1) / kBlock, My), kBlock, 0, st>>>(fine, mask, ntx, T, Mx, My, out);
+  k_merge_tiles<<<dim3((Mx + kBlock - 1) / kBlock, My < 65535 ? My : 65535), kBlock, 0, st>>>(fine, mask, ntx, T, Mx,
+                                                                                            My, out);
   return status();
 }
 int to_bf16(const float* x, __nv_bfloat16* y, long long n, cudaStream_t st) {

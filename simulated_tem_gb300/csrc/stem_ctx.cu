@@ -524,6 +524,12 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
         J.p = cps[ring_jobs[r]];
         J.p.prec_offset = pass * width;
         J.p.accumulate = pass > 0 ? 1 : 0;
+        // the average (and bright-field flip) in the store of the image's last pass, unless
+        // the image is tile-masked (its epilogue also covers the columns the mask leaves)
+        J.p.finalize = (flags & ST_FLAG_AVERAGE) && !J.p.tile_mask && J.p.prec_offset < J.p.n_prec &&
+                       J.p.prec_offset + width >= J.p.n_prec;
+        J.p.fin_scale = (double)J.p.n_prec;
+        J.p.fin_bright = (flags & ST_FLAG_BRIGHT) ? 1 : 0;
         J.pad = 0;
         for (int sh = 0; sh < kRingShapes; ++sh) {
           J.tile_base[sh] = tiles[sh];
@@ -598,12 +604,14 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
     }
     return ce;
   };
+  bool ring_ok = ring;  // false once a slab overflowed even 256-atom staging: the general kernel
   auto epilogues = [&]() -> cudaError_t {
     cudaError_t ce = cudaSuccess;
     if (!(flags & ST_FLAG_AVERAGE)) return ce;
     for (int i = 0; i < n && ce == cudaSuccess; ++i) {
       const st_geom* g = jobs[i].g;
       if (g->ix1 <= g->ix0 || g->iy1 <= g->iy0) continue;
+      if (ring_ok && on_ring[i] && !cps[i].tile_mask) continue;  // finished by the ring's last pass
       ce = launch_epilogue(jobs[i].d_img, g->Mx, g->My, g->ix0, g->ix1, g->iy0, g->iy1, (double)jobs[i].n_prec,
                            (flags & ST_FLAG_BRIGHT) ? 1 : 0, st);
     }
@@ -624,7 +632,6 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
   // Everything a call enqueues after the tables: binning, clearing, column kernels,
   // epilogues and the read-back of the counters.  `capturing`: no events, no tuning
   // (the variants and the kernel choice of the eager run are replayed).
-  bool ring_ok = ring;  // false once a slab overflowed even 256-atom staging: the general kernel
   const bool stats = (flags & ST_FLAG_STATS) != 0;
   std::vector<int> pass_variant(passes, 0);
   // big slabs when an earlier call of this context needed them for the same kind of pass on

@@ -65,3 +65,38 @@ def test_sweep_set_up_on_device_equals_host(ctx, cell):
             assert bytes(G) == bytes(Gd) and np.array_equal(aa, aad), (g, step)
             i += 1
     assert np.array_equal(d_x.cpu().numpy(), x)
+
+
+def _oracle_sweep_geometry(cell, g, n_tomo, step, n_prec):
+    from oracle import stem_oracle as O
+    args = O.make_args(cell.a_super, synth.A0_FE, (0, 0, 1), g, sg=0.01, xi0=103.9, xig=207.5, nTomo=n_tomo,
+                       tomoAngle=20.0)
+    so, xo, _ = O.setup(args, cell.pos, nn=step)
+    Go, aao = O.geometry(so, len(xo), nPrec=n_prec, precAngle=0.005)
+    return xo, Go, aao
+
+
+@pytest.mark.parametrize("which", ["small", "1p2m"])
+def test_sweep_geometry_matches_oracle(ctx, cell, which):
+    """d2bi_sweep (the wrap and the extents of every g on the GPU, the scalar set-up per tilt
+    on the host) against the oracle's own set-up of each condition, tilt by tilt and g by g:
+    the wrapped atoms, every field of the geometry the kernels receive, and the precession
+    coefficients, all to the last bit.  The small cell: every one of 3 g x 9 tilts; the
+    1.2M-atom cell of the benchmark's sweep (41 tilts): the first, middle and last tilt of
+    each g."""
+    from tests.test_host_geometry import assert_geom_equal
+    gs = ((1, 1, 0), (2, 0, 0), (2, 1, 1))
+    if which == "small":
+        c, n_tomo, steps = cell, 9, range(9)
+    else:
+        c, n_tomo, steps = synth.screw_cell_1p2m(), 41, (0, 20, 40)
+    d_x, specs, _ = imaging.d2bi_sweep(ctx, c.a_super, synth.A0_FE, (0, 0, 1), gs, c.pos, n_tomo=n_tomo,
+                                       tomo_angle=20.0, prec_angle=0.005, n_prec=16, sg=0.01, xi0=103.9,
+                                       xig=207.5)
+    x_dev = d_x.cpu().numpy()
+    for gi, g in enumerate(gs):
+        for step in steps:
+            xo, Go, aao = _oracle_sweep_geometry(c, g, n_tomo, step, 16)
+            assert np.array_equal(xo, x_dev)
+            G, aa = specs[gi * n_tomo + step]
+            assert_geom_equal(G, aa, Go, aao)

@@ -37,8 +37,12 @@ def test_blur_noalloc_matches_st_blur_on_consecutive_calls():
     stream = torch.cuda.current_stream().cuda_stream
     rng = np.random.default_rng(2024)
     try:
-        # a large image, then a smaller one that reuses the array the first call left behind
-        for nx, ny, t in ((566, 566, 3.1446), (94, 131, 2.5)):
+        # a large image, then a smaller one that reuses the array the first call left behind;
+        # then the limits: the widest weight table (t near 204.6 px, an 8 KB kernel argument)
+        # and the widest and largest image the scratch takes (nx = 4096, nx * ny = 2^21)
+        for nx, ny, t in ((566, 566, 3.1446), (94, 131, 2.5), (300, 220, 204.0),
+                          (_lib.ST_BLUR_NOALLOC_MAX_NX, _lib.ST_BLUR_NOALLOC_MAX_PIXELS // _lib.ST_BLUR_NOALLOC_MAX_NX,
+                           4.7)):
             img = rng.random((nx, ny))
             want = ctx.blur(img, t)
             rc, msg, got = _noalloc(L, img, t, stream)
