@@ -87,7 +87,8 @@ typedef struct st_stats {
   int32_t n_prec;
   double ms_bin;       /* device time of the binning kernels (ms) */
   double ms_column;    /* device time of the column kernel (ms) */
-  int32_t column_kernel; /* 1 general FP32, 2 slab-ring FP32 (for at least one image), 3 FP64 */
+  int32_t column_kernel; /* 1 general FP32, 2 slab-ring FP32, 3 general FP64, 4 slab-ring FP64 (the
+                            slab ring for at least one image) */
   int32_t ring_variant;  /* occupancy variant of the last slab-ring launch, -1 if none ran */
   int32_t ring_slab_atoms; /* staging capacity per slab of the last slab-ring launch (0 if none ran) */
   int32_t n_launches;    /* kernels the call launched (all attempts; autotuning trials included) */

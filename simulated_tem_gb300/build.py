@@ -24,7 +24,7 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp
                      "--expt-relaxed-constexpr"]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall"]
 
-LIB_SOURCES = ["stem_ctx.cu", "k_bin.cu", "k_column.cu", "k_column_ring.cu", "k_column_v3_np1.cu",
+LIB_SOURCES = ["stem_ctx.cu", "k_bin.cu", "k_column.cu", "k_column_ring.cu", "k_column_f64ring.cu", "k_column_v3_np1.cu",
                "k_column_v3_np2.cu", "k_column_v3_np4.cu", "k_column_v3_np8.cu", "k_column_v3_np16.cu", "k_blur.cu", "blur_noalloc.cu", "k_output.cu",
                "k_parse.cu", "k_geom.cu", "k_tilt.cu", "host_d2bi.cpp", "host_tilt.cpp", "host_output.cpp",
                "host_input.cpp"]
@@ -64,7 +64,7 @@ def build(verbose=False, ptxas_info=False):
     inc = os.path.join(HERE, "..", "include")
     libs = [
         (LIB, LIB_SOURCES, [os.path.join(CSRC, "internal.h"), os.path.join(CSRC, "parse_number.cuh"),
-                            os.path.join(CSRC, "k_column_v3.cuh"),
+                            os.path.join(CSRC, "k_column_v3.cuh"), os.path.join(CSRC, "fp64_column.cuh"),
                             os.path.join(CSRC, "host_geom.h"),
                             os.path.join(inc, "stem.h"),
                             os.path.join(inc, "stem_host.h")]),

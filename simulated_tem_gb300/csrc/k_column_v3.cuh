@@ -85,8 +85,12 @@ struct Geo {
 // Gather slab u (its cells in the patch footprint, atoms within 3 sigma of the
 // patch rectangle) into its ring slot and order it by z bin in place; false
 // when it holds more than CAPS atoms.
-template <int CAPS>
-__device__ bool load_slab3(const ColumnParams& p, const Geo& G, int u, WarpSmem3<CAPS>& W, int lane) {
+// kCellCode: the fourth float of an entry holds the atom's unwrapped cell relative to the warp's
+// reference cells, (ux - ux_ref + 8) | (uy - uy_ref + 8) << 8 (the FP64 kernel's exact
+// distances need it), instead of its phase.  WS: any warp-memory layout with the slab
+// arrays p, gi, bin and count.
+template <int CAPS, bool kCellCode = false, typename WS>
+__device__ bool load_slab3(const ColumnParams& p, const Geo& G, int u, WS& W, int lane) {
   const int cz = pos_mod(u, p.Ez);
   const int slot = u & (kRing - 1);
   float4* P = W.p[slot];
@@ -115,7 +119,8 @@ __device__ bool load_slab3(const ColumnParams& p, const Geo& G, int u, WarpSmem3
           const float dx = fmaxf(0.f, fmaxf(G.xmin - X, X - G.xmax));
           const float dy = fmaxf(0.f, fmaxf(G.ymin - Y, Y - G.ymax));
           keep = dx * dx + dy * dy <= G.pre2;
-          rec = make_float4(X, Y, __fmul_rn(r.z, G.scale), p.ph32[j]);
+          const float w4 = kCellCode ? __int_as_float((cxu - G.ux_ref + 8) | ((uy - G.uy_ref + 8) << 8)) : p.ph32[j];
+          rec = make_float4(X, Y, __fmul_rn(r.z, G.scale), w4);
         }
         const unsigned m = __ballot_sync(0xffffffffu, keep);
         const int cnt = __popc(m);

@@ -54,8 +54,9 @@ struct st_ctx {
   st_stats stats{};
   int64_t last_kept = 0;       // kept atoms of the previous call: sizes the next one
   bool fp32_general = false;   // STEM_FP32_KERNEL=general: always use k_column_fp32
+  bool fp64_general = false;   // STEM_FP64_KERNEL=general: always use k_column_fp64
   int min_slab_tier = 0;       // STEM_RING_SLABS=192 or 256: start the slab ring at that capacity
-  int last_column_kernel = 0;  // 1 general FP32, 2 slab-ring FP32, 3 FP64
+  int last_column_kernel = 0;  // 1 general FP32, 2 slab-ring FP32, 3 general FP64, 4 slab-ring FP64
   int tune_mode = ST_TUNE_AUTO;
   std::map<int, int> ring_tuned;  // (angles per pass, density) -> fastest slab-ring variant
   std::map<uint64_t, int> ring_big;  // (pass kind, image and link-cell shape) -> slab tier it needs (1, 2)
@@ -488,7 +489,7 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
   for (int i = 0; i < n; ++i) {
     cps[i] = column_params(c, jobs[i], cell_base[i], xoff[i], yoff[i], zoff[i], aoff[i], flags);
     max_np = std::max(max_np, jobs[i].n_prec);
-    if (fp32 && !c->fp32_general && ring_eligible(cps[i], (flags & ST_FLAG_STATS) != 0)) {
+    if (!(fp32 ? c->fp32_general : c->fp64_general) && ring_eligible(cps[i], (flags & ST_FLAG_STATS) != 0)) {
       on_ring[i] = 1;
       ring_jobs.push_back(i);
       dens = dens || cps[i].use_density;
@@ -637,7 +638,8 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
   // big slabs when an earlier call of this context needed them for the same kind of pass on
   // images of the same shape (the first ring image's image and link-cell dimensions)
   auto big_key = [&](int pass) -> uint64_t {
-    uint64_t h = (uint64_t)(ring_np_bucket(std::min(width, ring_np - pass * width)) * 2 + (dens ? 1 : 0));
+    uint64_t h = (uint64_t)(ring_np_bucket(std::min(width, ring_np - pass * width)) * 2 + (dens ? 1 : 0)) +
+                 (fp32 ? 0u : 1000u);
     if (!ring_jobs.empty()) {
       const st_geom* g = jobs[ring_jobs[0]].g;
       const int dims[6] = {g->Mx, g->My, g->Mz, g->Ex, g->Ey, g->Ez};
@@ -665,6 +667,10 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
     for (int pass = 0; ring_ok && pass < passes && ce == cudaSuccess; ++pass) {
       const int np_pass = std::min(width, ring_np - pass * width);
       auto ring_launch = [&](int v) {
+        if (!fp32)
+          return launch_column_fp64_ring(c->d_coljobs + (size_t)pass * n_ring, n_ring,
+                                         pass_tiles[(size_t)pass * kRingShapes], np_pass, big, masked, c->d_work,
+                                         c->s.counters, cap, st);
         return launch_column_fp32_ring(c->d_coljobs + (size_t)pass * n_ring, n_ring,
                                        pass_tiles.data() + (size_t)pass * kRingShapes, np_pass,
                                        dens, stats, v, big, masked, c->d_work, c->s.counters, cap, st);
@@ -675,9 +681,9 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
       }
       const int key = ring_np_bucket(np_pass) * 2 + (dens ? 1 : 0);
       int v = 0;
-      if (c->tune_mode >= 0) {
+      if (c->tune_mode >= 0 && fp32) {
         v = c->tune_mode;
-      } else if (c->tune_mode == ST_TUNE_AUTO && !stats) {
+      } else if (c->tune_mode == ST_TUNE_AUTO && !stats && fp32) {  // the FP64 ring has one variant
         auto it = c->ring_tuned.find(key);
         if (it != c->ring_tuned.end()) {
           v = it->second;
@@ -772,7 +778,7 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
     gout->ring = used_ring;
   }
   c->last_kept = (int64_t)c->h_counters[0];
-  c->last_column_kernel = !fp32 ? 3 : (used_ring ? 2 : 1);
+  c->last_column_kernel = !fp32 ? (used_ring && !ring_jobs.empty() ? 4 : 3) : (used_ring ? 2 : 1);
 
   st_stats& S = c->stats;
   memset(&S, 0, sizeof S);
@@ -830,6 +836,8 @@ extern "C" int st_create(st_ctx** out, int device) {
   }
   const char* kv = std::getenv("STEM_FP32_KERNEL");
   c->fp32_general = kv && std::strcmp(kv, "general") == 0;
+  const char* kv64 = std::getenv("STEM_FP64_KERNEL");
+  c->fp64_general = kv64 && std::strcmp(kv64, "general") == 0;
   const char* ks = std::getenv("STEM_RING_SLABS");
   c->min_slab_tier = !ks ? 0 : std::strcmp(ks, "256") == 0 ? 2 : std::strcmp(ks, "192") == 0 ? 1 : 0;
   *out = c;
@@ -1130,6 +1138,7 @@ extern "C" int st_plan_create(st_ctx* c, int32_t n_jobs, const st_job* jobs, int
     G.c->tune_mode = c->tune_mode;
     G.c->ring_tuned = c->ring_tuned;
     G.c->fp32_general = c->fp32_general;
+    G.c->fp64_general = c->fp64_general;
     G.jobs.assign(js.begin() + first, js.begin() + last);
     p->groups.push_back(G);
     first = last;
