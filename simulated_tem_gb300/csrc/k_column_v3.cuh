@@ -47,7 +47,7 @@ namespace ring3 {
 
 constexpr int kWarps = 4;
 constexpr int kRing = 4;    // resident slabs (unwrapped z cells u, slot u & 3)
-constexpr int kBins = 32;   // z bins per slab for the window lookup
+constexpr int kBins = 32;   // z bins per slab for the window lookup (at most 32: one lane each)
 constexpr int kBuf = 64;    // per-step candidate buffer (flushed at 32)
 constexpr float kHuge = FLT_MAX;
 
@@ -169,14 +169,14 @@ __device__ bool load_slab3(const ColumnParams& p, const Geo& G, int u, WS& W, in
   }
   // exclusive scan of the 32 bin counts: bin starts, bin[kBins] = n
   {
-    const int v = hist[lane];
+    const int v = lane < kBins ? hist[lane] : 0;
     int incl = v;
-    for (int o = 1; o < 32; o <<= 1) {
+    for (int o = 1; o < kBins; o <<= 1) {
       const int t = __shfl_up_sync(0xffffffffu, incl, o);
       if (lane >= o) incl += t;
     }
     __syncwarp();
-    hist[lane] = incl - v;
+    if (lane < kBins) hist[lane] = incl - v;
     if (lane == 0) hist[kBins] = n;
   }
   __syncwarp();
