@@ -142,9 +142,9 @@ def path_roofline(peaks, n_acc, n_kept, n_atoms, voxels, voxel_prec, pixels, den
 
 
 SWEEP_G = ((1, 1, 0), (2, 0, 0), (2, 1, 1))
-# DRAM bytes (read + write) of one k_column_fp32_v2 launch on the 1.2M-atom image, from an
-# ncu capture of `python bench.py --ncu-case fp32` (61.15 MB read + 2.89 MB written)
-COLUMN_TRAFFIC_BYTES = 6.405e7
+# DRAM bytes (read + write) of one k_column_fp32_v3 launch on the 1.2M-atom image, from an
+# ncu capture of `python bench.py --ncu-case fp32` (51.53 MB read + 1.77 MB written)
+COLUMN_TRAFFIC_BYTES = 5.330e7
 
 
 def sweep_specs(cell, n_tomo=41, n_prec=16, gs=SWEEP_G):
@@ -270,7 +270,7 @@ def batched_legs(ctx, cell, stream, flush, steps, warmup, peaks=None, cpu=True):
         pix = sum((G.ix1 - G.ix0) * (G.iy1 - G.iy0) for G in specs_g[0])
         r = path_roofline(peaks, st.n_accepted, st.n_kept, n_atoms, vox, vp, pix, False, t_col)
         if r:
-            r["kernel"] = "k_column_fp32_v2 (every column launch of the batch)"
+            r["kernel"] = "k_column_fp32_v3 (every column launch of the batch)"
             r["frac_batch"] = r["t_roof_ms"] / t_batch
             r["executed"] = {"tests": st.n_tests, "tests_per_voxel": st.n_tests / max(vox, 1)}
         return r
@@ -297,6 +297,7 @@ def batched_legs(ctx, cell, stream, flush, steps, warmup, peaks=None, cpu=True):
     ms = time_batch(ctx, jobs, f32, stream, steps, warmup, flush)
     stages = dict(time_batch.stages)
     launches = ctx.stats().n_launches
+    variant = _lib.lib().st_tune_variant_name(ctx.stats().ring_variant).decode()
     t = float(np.mean(ms)) * 1e-3
     n_img, n_pass = len(specs), sum(len(aa) for _, aa in specs)
     vs = sum((G.ix1 - G.ix0) * (G.iy1 - G.iy0) * G.Mz * len(aa) for G, aa in specs)
@@ -320,7 +321,7 @@ def batched_legs(ctx, cell, stream, flush, steps, warmup, peaks=None, cpu=True):
                     "passes_per_s": n_pass / t, "voxel_slices_per_s": vs / t, "ms_per_batch": t * 1e3,
                     "steps": steps, "image_sizes": sorted({(G_.Mx, G_.My, G_.Mz) for G_, _ in specs}),
                     "kept_atoms": st.n_kept, "column_kernel": st.column_kernel, "stages": stages,
-                    "launches_per_batch": launches,
+                    "launches_per_batch": launches, "ring_variant": variant,
                     "roofline": roof(st, ([G_ for G_, _ in specs], [len(aa_) for _, aa_ in specs]),
                                      stages["ms_column"], t * 1e3, len(x) * n_img),
                     "accuracy_tilt20_per_g": acc,
@@ -345,6 +346,7 @@ def batched_legs(ctx, cell, stream, flush, steps, warmup, peaks=None, cpu=True):
     ms = time_batch(ctx, jobs, f32, stream, steps, warmup, flush)
     stages = dict(time_batch.stages)
     launches = ctx.stats().n_launches
+    variant = _lib.lib().st_tune_variant_name(ctx.stats().ring_variant).decode()
     t = float(np.mean(ms)) * 1e-3
     vs = sum((G.ix1 - G.ix0) * (G.iy1 - G.iy0) * G.Mz for G, _, _ in specs)
     k = int(np.argmax([len(x_) for _, _, x_ in specs]))
@@ -361,7 +363,7 @@ def batched_legs(ctx, cell, stream, flush, steps, warmup, peaks=None, cpu=True):
                      "images": len(specs), "atoms": int(sum(len(x_) for _, _, x_ in specs)),
                      "images_per_s": len(specs) / t, "voxel_slices_per_s": vs / t, "ms_per_batch": t * 1e3,
                      "steps": steps, "kept_atoms": st.n_kept, "column_kernel": st.column_kernel, "stages": stages,
-                     "launches_per_batch": launches,
+                     "launches_per_batch": launches, "ring_variant": variant,
                      "roofline": roof(st, ([G_ for G_, _, _ in specs], [1] * len(specs)), stages["ms_column"],
                                       t * 1e3, sum(len(x_) for _, _, x_ in specs)),
                      "accuracy_largest_cell": acc}
@@ -842,7 +844,7 @@ def run_gpu(args):
     if ws > 1:
         torch.distributed.barrier()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    col_ms, launches = [], 0
+    col_ms, launches, variant = [], 0, 0
     with ClockSampler(local) as clk:
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -854,6 +856,7 @@ def run_gpu(args):
             st_i = ctx.stats()
             col_ms.append(st_i.ms_column)
             launches += st_i.n_launches
+            variant = st_i.ring_variant
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
         peaks = measure_fp32_peak()
@@ -921,21 +924,23 @@ def run_gpu(args):
     roof = path_roofline(peaks, n_acc, n_kept, len(x), V, V * n_prec, pix, False, col_avg)
     if roof:
         c_tests = reference_candidate_tests(ctx, G, x)
-        roof.update({"kernel": "k_column_fp32_v2",
+        roof.update({"kernel": "k_column_fp32_v3",
                      "peak_source": "measured live in this run by the project's pipe microbenchmarks "
                                     "(libstem_peaks.so: FP32 FMA, FP64 FMA, MUFU ex2 and sin); HBM from "
                                     + hbm_peak()[1],
                      "traffic": COLUMN_TRAFFIC_BYTES, "traffic_unit": "bytes per launch",
-                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_column_fp32_v2 on "
-                                       "this image (profiles/k_column_fp32_v2_1p2m_screw.md)",
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_column_fp32_v3 on "
+                                       "this image (profiles/k_column_fp32_v3_1p2m_screw.md)",
                      "frac_step": roof["t_roof_ms"] / ms,
                      "executed": {"tests": n_tst, "tests_per_voxel": n_tst / V,
                                   "reference_tests_per_voxel": c_tests / V,
                                   "accepted_per_voxel": n_acc / V,
-                                  "ex2_issued": n_tst, "ex2_frac_of_peak":
-                                      n_tst / (col_avg * 1e-3) / (peaks["mufu_ex2_gops"] * 1e9),
-                                  "note": "work the kernel executes: every candidate test (a slab-ring slice "
-                                          "pair counts two) issues one ex2; the reference's own 27-cell search "
+                                  "ex2_issued": n_tst / 2, "ex2_frac_of_peak":
+                                      n_tst / 2 / (col_avg * 1e-3) / (peaks["mufu_ex2_gops"] * 1e9),
+                                  "note": "work the kernel executes: tests counts each buffered atom once per "
+                                          "column and slice; the in-plane weight is one ex2 per atom and column "
+                                          "for both slices of a step (ex2_issued), the depth factor one per atom "
+                                          "and slice for the whole warp; the reference's own 27-cell search "
                                           "tests reference_tests_per_voxel candidates per voxel"}})
     acc = {"max_abs_dI_fp32_vs_fp64": float(np.abs(d).max()), "rms_dI_fp32_vs_fp64": float(np.sqrt((d ** 2).mean()))}
     line = {"metric": METRIC, "value": value, "unit": "images/s", "n_gpus": ws, "steps": args.steps,
@@ -943,7 +948,8 @@ def run_gpu(args):
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded bcc Fe cell, no dataset)",
             "config": {"workload": WORKLOAD, "atoms": len(x), "image": [G.Mx, G.My, G.Mz], "n_prec": n_prec,
                        "path": "FP32 deposition + integration, FP64 binning and g.r mod 1",
-                       "l2": "flushed between steps (512 MB write)", "parallelism": "replicas%d" % ws},
+                       "l2": "flushed between steps (512 MB write)", "parallelism": "replicas%d" % ws,
+                       "ring_variant": _lib.lib().st_tune_variant_name(variant).decode()},
             "e2e": {"value": e2e_value, "unit": "images/s", "h2d_bytes_per_step": int(x.nbytes),
                     "d2h_bytes_per_step": int(G.Mx * G.My * 8)},
             "fp64": {"value": 1000.0 / fp64_ms, "unit": "images/s", "ms": fp64_ms},

@@ -113,17 +113,23 @@ int st_image(st_ctx* ctx, const st_geom* geom, const double* x, int64_t ldx, int
 int st_image_device(st_ctx* ctx, const st_geom* geom, const double* d_x, int64_t ldx, int64_t nAtoms,
                     const double* aa, int32_t nPrec, int32_t flags, double* d_img, void* stream);
 
-/* Launch tuning of the slab-ring FP32 kernel.  Its variants differ only in the
- * register budget per thread (CTAs per SM) and compute identical images.
+/* Launch tuning of the slab-ring FP32 kernel.  Its variants differ in the warp
+ * tile's shape (8 x 4, 4 x 8 or 16 x 2 pixel columns), the slab capacity of
+ * the first staging tier (128 or 96 atoms) and with it the CTAs per SM; the
+ * images of variants of one tile shape are identical, those of different
+ * shapes agree to FP32 rounding (their atoms are summed in different orders).
  * ST_TUNE_AUTO (the default): the first pass of each (angles per pass,
- * density) kind in a context times every variant on the real work and keeps
- * the fastest for the context's later calls.  ST_TUNE_OFF: variant 0 always.
+ * density) kind in a context with at least 4,096 warp tiles times every
+ * variant on the real work, keeps the fastest for the context's later calls,
+ * and leaves that variant's own images.  ST_TUNE_OFF: variant 0 always.
  * mode >= 0: that variant always.  No counterpart in the reference. */
 #define ST_TUNE_AUTO (-1)
 #define ST_TUNE_OFF (-2)
 int st_tune(st_ctx* ctx, int32_t mode);
 /* Number of slab-ring variants (valid forced modes are 0 .. count - 1). */
 int st_tune_variants(void);
+/* A variant's name ("8x4 slab96" ...); "invalid" out of range. */
+const char* st_tune_variant_name(int32_t variant);
 
 /* st_image_device restricted to chosen tiles: d_tile_mask (device, one byte per mask_T x
  * mask_T pixel tile, ceil(Mx / mask_T) tiles per row, row-major) selects the tiles whose

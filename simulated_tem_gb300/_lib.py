@@ -122,6 +122,7 @@ _PROTOS = {
     "st_plan_last_error": (ctypes.c_char_p, [_vp]),
     "st_plan_destroy": (None, [_vp]),
     "st_tune_variants": (_i32, []),
+    "st_tune_variant_name": (ctypes.c_char_p, [_i32]),
     "st_format_dat_header": (_i32, [ctypes.POINTER(StDatHeader), _i32, _i32, ctypes.c_char_p, _i64,
                                     ctypes.POINTER(_i64)]),
     "st_dat_text_bytes": (_i64, [_i64]),

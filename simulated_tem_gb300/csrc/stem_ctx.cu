@@ -876,6 +876,8 @@ extern "C" int st_tune(st_ctx* c, int32_t mode) {
 
 extern "C" int st_tune_variants(void) { return ring_variant_count(); }
 
+extern "C" const char* st_tune_variant_name(int32_t variant) { return ring_variant_name(variant); }
+
 extern "C" const char* st_last_error(const st_ctx* c) { return c ? c->err.c_str() : "null context"; }
 
 extern "C" int st_get_stats(const st_ctx* c, st_stats* out) {
