@@ -273,8 +273,12 @@ def make_pairs(ctx, cell, sgs, crop, per_image, rng, fp32=True):
         if G8.My < crop or G8.Mx < crop:
             continue
         for _ in range(per_image):
-            y0 = int(rng.integers(0, G8.My - crop + 1))
-            x0 = int(rng.integers(0, G8.Mx - crop + 1))
+            # half the crops touch an image edge in x, half in y (the network sees the edges,
+            # where the coarse image extrapolates, as often as the interior)
+            def corner(n):
+                r = rng.random()
+                return 0 if r < 0.25 else n - crop if r < 0.5 else int(rng.integers(0, n - crop + 1))
+            y0, x0 = corner(G8.My), corner(G8.Mx)
             pin = planes[:, y0:y0 + crop, x0:x0 + crop]
             ins.append(pin[:N_IN])
             tgs.append((fine[y0:y0 + crop, x0:x0 + crop] - pin[4]) * RES_SCALE)
@@ -369,8 +373,13 @@ class CorrectedImager:
     """M = 8 images from the M = 2 solve and the corrector, with the plain fine-grid solve
     as the fallback on T x T tiles whose predicted correction exceeds `tau`."""
 
-    def __init__(self, model, ctx, tile=16, tau=0.05):
+    def __init__(self, model, ctx, tile=16, tau=0.05, border=None):
+        """border: recompute the image's outer ring of tiles whatever their predicted error
+        (default: as the model was calibrated, model.meta["border"], else True)."""
         self.model, self.ctx, self.T, self.tau = model, ctx, tile, tau
+        if border is None:
+            border = bool(int(getattr(model, "meta", {}).get("border", 1)))
+        self.border = border
 
     def image(self, t2, t8, x_dev, n_atoms, sg, fallback=True, stream=0, diag=None, times=None):
         """Returns (FP64 device image (My8, Mx8), number of fallback tiles, tile count).  A
@@ -415,10 +424,10 @@ class CorrectedImager:
         if not fallback:
             self._times(times, ev, ["m2_solve", "network"])
             return img, 0, ntx * nty
-        # every tile above tau, and the image's border, where the coarse image is clamped
+        # every tile above tau, and the image's outer ring if the model was calibrated so
         mask = torch.empty((nty, ntx), dtype=torch.uint8, device=dev)
         count = torch.empty((), dtype=torch.int32, device=dev)
-        N.tile_flags(tmax, self.tau * RES_SCALE, mask, count, border=True)
+        N.tile_flags(tmax, self.tau * RES_SCALE, mask, count, border=self.border)
         fine = torch.empty((G8.My, G8.Mx), dtype=torch.float64, device=dev)
         self.ctx.image_device_masked(G8, x_dev.data_ptr(), n_atoms, aa8, _lib.ST_FLAG_FP32, fine.data_ptr(),
                                      mask.data_ptr(), T, stream=stream)
@@ -472,15 +481,16 @@ def build_dataset(ctx, n_pairs, crop, seed, conds_per_cell=10, crops_per_image=5
 
 
 def calibrate(model, ctx, conditions, tile=16, target=1e-2):
-    """The fallback threshold: over whole validation images (cell, s_g), the largest tau for
-    which every interior tile whose corrected error exceeds `target` has a predicted local
-    error above tau (so it falls back; the border ring of tiles always does).  Returns
-    (tau, report)."""
+    """The fallback threshold over whole validation images (cell, s_g): the largest tau for
+    which every tile whose corrected error exceeds `target` has a predicted local error
+    above tau (so it falls back).  Two rules are calibrated: every tile judged by its
+    prediction, and the image's outer ring of tiles always recomputed with the interior
+    judged; the one that recomputes fewer tiles is kept.  Returns (tau, border, report)."""
     import torch
 
     from . import _lib
-    imager = CorrectedImager(model, ctx, tile=tile, tau=np.inf)
-    bad_pred, all_pred, worst, n_border = [], [], 0.0, 0
+    imager = CorrectedImager(model, ctx, tile=tile, tau=np.inf, border=False)
+    ring_pred, ring_bad, in_pred, in_bad, worst = [], [], [], [], 0.0
     for cell, sg in conditions:
         t2, x = condition(cell, 2, sg)
         t8, _ = condition(cell, 8, sg)
@@ -492,20 +502,31 @@ def calibrate(model, ctx, conditions, tile=16, target=1e-2):
         worst = max(worst, float(err.max()))
         tm = diag["tile_max"]
         ny, nx = tm.shape
-        n_border += 2 * (nx + ny) - 4
-        for ty in range(1, ny - 1):  # the border ring always falls back
-            for tx in range(1, nx - 1):
+        for ty in range(ny):
+            for tx in range(nx):
                 e = err[ty * tile:(ty + 1) * tile, tx * tile:(tx + 1) * tile].max()
-                all_pred.append(tm[ty, tx])
+                ring = ty == 0 or tx == 0 or ty == ny - 1 or tx == nx - 1
+                (ring_pred if ring else in_pred).append(tm[ty, tx])
                 if e > target:
-                    bad_pred.append(tm[ty, tx])
-    all_pred = np.array(all_pred)
-    tau = 0.9 * float(min(bad_pred)) if bad_pred else float(all_pred.max()) * 1.1 + 1e-6
-    n_tiles = all_pred.size + n_border
-    frac = float(((all_pred > tau).sum() + n_border) / n_tiles)
-    return tau, {"tiles": int(n_tiles), "interior_tiles_above_target": len(bad_pred), "fallback_fraction": frac,
-                 "interior_fallback_fraction": float((all_pred > tau).mean()),
-                 "max_error_without_fallback": worst}
+                    (ring_bad if ring else in_bad).append(tm[ty, tx])
+    ring_pred, in_pred = np.array(ring_pred), np.array(in_pred)
+    n_tiles = ring_pred.size + in_pred.size
+
+    def tau_of(bad, pred):
+        return 0.9 * float(min(bad)) if bad else float(pred.max()) * 1.1 + 1e-6
+
+    tau_all = tau_of(ring_bad + in_bad, np.concatenate([ring_pred, in_pred]))
+    frac_all = float(((ring_pred > tau_all).sum() + (in_pred > tau_all).sum()) / n_tiles)
+    tau_in = tau_of(in_bad, in_pred)
+    frac_ring = float((ring_pred.size + (in_pred > tau_in).sum()) / n_tiles)
+    border = frac_ring < frac_all
+    tau = tau_in if border else tau_all
+    return tau, border, {"tiles": int(n_tiles), "ring_tiles": int(ring_pred.size),
+                         "tiles_above_target": len(ring_bad) + len(in_bad), "ring_tiles_above_target": len(ring_bad),
+                         "fallback_fraction": frac_ring if border else frac_all,
+                         "fallback_fraction_every_tile_judged": frac_all,
+                         "fallback_fraction_ring_always": frac_ring, "border": bool(border),
+                         "max_error_without_fallback": worst}
 
 
 def train_main(argv=None):
@@ -550,11 +571,11 @@ def train_main(argv=None):
     t_train = time.time() - t0
     rng = np.random.default_rng(args.seed + 2)
     conds = [(random_cell(rng), float(rng.uniform(-0.02, 0.02))) for _ in range(args.val_cells)]
-    tau, report = calibrate(model, ctx, conds)
+    tau, border, report = calibrate(model, ctx, conds)
     report.update({"tau": tau, "validation": ev, "train_seconds": t_train, "data_seconds": t_data,
                    "pairs": args.pairs, "crop": args.crop, "steps": args.steps, "batch": args.batch})
     print(json.dumps(report), flush=True)
-    model.save(args.out, tau=tau, report=json.dumps(report))
+    model.save(args.out, tau=tau, border=int(border), report=json.dumps(report))
     return report
 
 

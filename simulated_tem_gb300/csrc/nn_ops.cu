@@ -340,8 +340,9 @@ __global__ void __launch_bounds__(1024) k_image_mean(const double* __restrict__ 
 // The corrector's planes on the fine (M = 8) pixel grid, Hp x Wp (the image My8 x Mx8,
 // extended by its last row and column).  DF is the coarse (M = 2) image interpolated
 // bilinearly at the fine pixels' positions (pixel i of an N-pixel axis sits at i d / N on
-// both grids), clamped at the image's edges: the tilted crystal makes the image
-// non-periodic.  mu is the coarse image's mean.  Planes (FP32 [5][Hp][Wp]):
+// both grids); the fine pixels past the last coarse pixel extrapolate from the last two
+// (the tilted crystal makes the image non-periodic, and a clamped edge would be a step
+// the network must learn).  mu is the coarse image's mean.  Planes (FP32 [5][Hp][Wp]):
 // 0: (DF - mu) * contrast, 1: (BF - (1 - mu)) * contrast with BF = 1 - DF, 2: sg_value,
 // 3: mu, 4: DF (the base the correction is added to).  Planes 0-3 are the network's input:
 // the contrast, a few 1e-3 on a level near 0.1-0.7, would not survive BF16 unshifted.
@@ -358,9 +359,11 @@ __global__ void k_resample_planes(const double* __restrict__ img2, int Mx2, int 
   const double mu = *mean;
   for (int qy = blockIdx.y; qy < Hp; qy += gridDim.y) {
     const long long i = (long long)qy * Wp + qx;
+    // bilinear between the two nearest coarse pixels; past the last coarse pixel (the
+    // fine grid's last quarter pixel-row and column) the last two extrapolate linearly
     const int px = min(qx, Mx8 - 1), py = min(qy, My8 - 1);
     const double u = px * sx, v = py * sy;
-    int i0 = min((int)floor(u), Mx2 - 1), j0 = min((int)floor(v), My2 - 1);
+    const int i0 = max(0, min((int)floor(u), Mx2 - 2)), j0 = max(0, min((int)floor(v), My2 - 2));
     const double fu = u - i0, fv = v - j0;
     const int i1 = min(i0 + 1, Mx2 - 1), j1 = min(j0 + 1, My2 - 1);
     const double a = img2[i0 + (long long)Mx2 * j0], b = img2[i1 + (long long)Mx2 * j0];

@@ -132,7 +132,7 @@ def test_training_beats_interpolation(ctx, C):
 
 def test_fallback_reproduces_the_fine_solve(ctx, C):
     """With tau = 0 every tile falls back: the image is the plain M = 8 solve exactly; with an
-    infinite tau only the border ring of tiles does (the coarse image is clamped there)."""
+    infinite tau only the border ring of tiles does (with the ring always recomputed)."""
     cell = _cells(1, 9, nxy=16, nz=12)[0]
     t2, x = C.condition(cell, 2, 0.01)
     t8, _ = C.condition(cell, 8, 0.01)

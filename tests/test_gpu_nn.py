@@ -188,8 +188,9 @@ def test_conv_streams_take_turns_on_blocked_weights(nn):
 
 def test_input_planes_mean_and_pack(nn):
     """The corrector's input path against numpy: the coarse image's mean (one fixed-order
-    FP64 sum), the planes resampled bilinearly onto the fine grid in FP64 (edges clamped,
-    the padding rows and columns repeating the last pixel), and their BF16 NHWC packing
+    FP64 sum), the planes resampled bilinearly onto the fine grid in FP64 (past the last
+    coarse pixel the last two extrapolate, the padding rows and columns repeat the last
+    pixel), and their BF16 NHWC packing
     (exact: one rounding of each FP32 value, zeros past the planes)."""
     rng = np.random.default_rng(5)
     Mx2, My2, Mx8, My8, Wp, Hp = 37, 29, 147, 115, 152, 120
@@ -204,8 +205,8 @@ def test_input_planes_mean_and_pack(nn):
     px = np.minimum(np.arange(Wp), Mx8 - 1)
     py = np.minimum(np.arange(Hp), My8 - 1)
     u, v = px * (Mx2 / Mx8), py * (My2 / My8)
-    i0 = np.minimum(np.floor(u).astype(int), Mx2 - 1)
-    j0 = np.minimum(np.floor(v).astype(int), My2 - 1)
+    i0 = np.maximum(0, np.minimum(np.floor(u).astype(int), Mx2 - 2))
+    j0 = np.maximum(0, np.minimum(np.floor(v).astype(int), My2 - 2))
     fu, fv = u - i0, v - j0
     i1, j1 = np.minimum(i0 + 1, Mx2 - 1), np.minimum(j0 + 1, My2 - 1)
     a, b = img2[j0][:, i0], img2[j0][:, i1]
