@@ -173,9 +173,10 @@ int column_tiles(const ColumnParams& p, int shape = 0);  // warp tiles of one im
 // The slab-ring launch.  `tiles`: the pass's warp tiles in each shape (host array).
 // `variant` 0 .. ring_variant_count() - 1 selects the kernel, its tile shape, slab
 // capacity and CTAs per SM (ring_variant_name); the images of different variants agree to
-// FP32 rounding, those of one variant (at any tier) to the last bit.  `slab_tier` 1, 2:
-// 192, 256 atoms per slab (dense footprints).  `masked`: some jobs carry a tile mask
-// (then max_np must be 1 and stats false).
+// FP32 rounding, those of one variant to the last bit.  `slab_tier` 1, 2: 192, 256 atoms
+// per slab (dense footprints), with variant 0's 8 x 4 tiles, so at those tiers every
+// variant gives variant 0's bits.  `masked`: some jobs carry a tile mask (then max_np must
+// be 1 and stats false).
 cudaError_t launch_column_fp32_ring(const ColumnJob* d_jobs, int n_jobs, const int* tiles, int max_np, bool density,
                                     bool stats, int variant, int slab_tier, bool masked, unsigned* work,
                                     const unsigned long long* counters, int64_t cap, cudaStream_t st);
