@@ -51,6 +51,14 @@ constexpr int kBins = 32;   // z bins per slab for the window lookup (at most 32
 constexpr int kBuf = 64;    // per-step candidate buffer (flushed at 32)
 constexpr float kHuge = FLT_MAX;
 
+// Lengths inside the kernel are scaled by s = sqrt(log2(e) / (2 sigma^2)), so that the
+// Gaussian weight exp(-r^2 / (2 sigma^2)) is ex2(-r'^2) of the scaled distance r'.
+struct Geo {
+  int ux_lo, ux_hi, uy_lo, uy_hi, ux_ref, uy_ref;
+  float xmin, xmax, ymin, ymax, pre2;
+  float a11s, a22s, a33s, scale;
+};
+
 template <int CAPS>  // staged atoms per slab
 struct WarpSmem3 {
   float4 p[kRing][CAPS];      // X', Y' (warp frame), z (own cell), phase (cycles) -- lengths scaled by s
@@ -59,6 +67,7 @@ struct WarpSmem3 {
   int count[kRing];
   float4 ba[kBuf];            // step buffer: X', Y', hmax_0, hmax_1
   float4 be[kBuf];            // ex2(-dz_0^2) (cos, sin), ex2(-dz_1^2) (cos, sin)
+  Geo geo;                    // the tile's footprint and frame (warp-uniform: here, not in registers)
 };
 
 __device__ __forceinline__ float ex2_approx(float x) {
@@ -74,13 +83,6 @@ __device__ __forceinline__ int pos_mod(int a, int n) {
 
 __device__ __forceinline__ int floor_div(int a, int n) { return (a >= 0) ? a / n : -((-a + n - 1) / n); }
 
-// Lengths inside the kernel are scaled by s = sqrt(log2(e) / (2 sigma^2)), so that the
-// Gaussian weight exp(-r^2 / (2 sigma^2)) is ex2(-r'^2) of the scaled distance r'.
-struct Geo {
-  int ux_lo, ux_hi, uy_lo, uy_hi, ux_ref, uy_ref;
-  float xmin, xmax, ymin, ymax, pre2;
-  float a11s, a22s, a33s, scale;
-};
 
 // Gather slab u (its cells in the patch footprint, atoms within 3 sigma of the
 // patch rectangle) into its ring slot and order it by z bin in place; false
@@ -89,50 +91,138 @@ struct Geo {
 // reference cells, (ux - ux_ref + 8) | (uy - uy_ref + 8) << 8 (the FP64 kernel's exact
 // distances need it), instead of its phase.  WS: any warp-memory layout with the slab
 // arrays p, gi, bin and count.
+// One gathered candidate: atom j of a cell in row uy, x cells shifted by `shift` (an
+// unwrapped run), in the warp's scaled frame; keep when within 3 sigma of the patch.
+template <bool kCellCode>
+__device__ __forceinline__ bool slab_candidate(const ColumnParams& p, const Geo& G, int j, int shift, int uy,
+                                               float4& rec) {
+  const float4 r = p.p32[j];
+  const int packed = __float_as_int(r.w);
+  const int cxu = (packed & 1023) + shift;
+  const float X = __fmaf_rn(r.x, G.scale, __fmul_rn(G.a11s, (float)(cxu - G.ux_ref)));
+  const float Y = __fmaf_rn(r.y, G.scale, __fmul_rn(G.a22s, (float)(uy - G.uy_ref)));
+  const float dx = fmaxf(0.f, fmaxf(G.xmin - X, X - G.xmax));
+  const float dy = fmaxf(0.f, fmaxf(G.ymin - Y, Y - G.ymax));
+  const float w4 = kCellCode ? __int_as_float((cxu - G.ux_ref + 8) | ((uy - G.uy_ref + 8) << 8)) : p.ph32[j];
+  rec = make_float4(X, Y, __fmul_rn(r.z, G.scale), w4);
+  return dx * dx + dy * dy <= G.pre2;
+}
+
+// Appends the kept candidates of one 32-lane round (ballot + popc, order kept); false
+// when the slab would exceed CAPS.
+template <int CAPS>
+__device__ __forceinline__ bool slab_append(float4* P, int* GI, int& n, bool keep, const float4& rec, int j,
+                                            int lane) {
+  const unsigned m = __ballot_sync(0xffffffffu, keep);
+  const int cnt = __popc(m);
+  if (n + cnt > CAPS) return false;
+  if (keep) {
+    const int d = n + __popc(m & ((1u << lane) - 1));
+    P[d] = rec;
+    GI[d] = j;
+  }
+  n += cnt;
+  return true;
+}
+
+// Gather slab u (its cells in the patch footprint, atoms within 3 sigma of the
+// patch rectangle) into its ring slot and order it by z bin in place; false
+// when it holds more than CAPS atoms.
+// kCellCode: the fourth float of an entry holds the atom's unwrapped cell relative to the warp's
+// reference cells, (ux - ux_ref + 8) | (uy - uy_ref + 8) << 8 (the FP64 kernel's exact
+// distances need it), instead of its phase.  WS: any warp-memory layout with the slab
+// arrays p, gi, bin and count.
+//
+// The footprint is rows uy of x runs (a run ends where x wraps): segments of consecutive
+// atoms.  Where a thread has 128 registers or more and there are up to 8 segments, the
+// lanes look up all segment ranges at once, join them into one index space (the slot's
+// bin array, free until the sort, holds the table) and gather two 32-lane rounds at a
+// time; otherwise (and in the five-CTA variants, whose 96 registers it would overflow)
+// row by row, one round at a time.  Both routes visit the atoms in the same order (rows,
+// runs, atoms), so the slab's contents and order do not depend on the route.
 template <int CAPS, bool kCellCode = false, typename WS>
 __device__ bool load_slab3(const ColumnParams& p, const Geo& G, int u, WS& W, int lane) {
+  constexpr bool kJoined = CAPS >= 128;  // 128 registers or more per thread
   const int cz = pos_mod(u, p.Ez);
   const int slot = u & (kRing - 1);
   float4* P = W.p[slot];
   int* GI = W.gi[slot];
   int n = 0;
-  for (int uy = G.uy_lo; uy <= G.uy_hi; ++uy) {
-    const int cy = pos_mod(uy, p.Ey);
-    const int64_t row_base = (int64_t)p.Ex * (cy + (int64_t)p.Ey * cz);
-    const float yoff = __fmul_rn(G.a22s, (float)(uy - G.uy_ref));
-    for (int ux = G.ux_lo; ux <= G.ux_hi;) {
-      const int k = floor_div(ux, p.Ex);
-      const int run_hi = min(G.ux_hi, (k + 1) * p.Ex - 1);
-      const int shift = k * p.Ex;
-      const int a_lo = p.cell_start[row_base + (ux - shift)];
-      const int a_hi = p.cell_start[row_base + (run_hi - shift) + 1];
-      for (int b = a_lo; b < a_hi; b += 32) {
-        const int j = b + lane;
-        bool keep = false;
-        float4 rec = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (j < a_hi) {
-          const float4 r = p.p32[j];
-          const int packed = __float_as_int(r.w);
-          const int cxu = (packed & 1023) + shift;
-          const float X = __fmaf_rn(r.x, G.scale, __fmul_rn(G.a11s, (float)(cxu - G.ux_ref)));
-          const float Y = __fmaf_rn(r.y, G.scale, yoff);
-          const float dx = fmaxf(0.f, fmaxf(G.xmin - X, X - G.xmax));
-          const float dy = fmaxf(0.f, fmaxf(G.ymin - Y, Y - G.ymax));
-          keep = dx * dx + dy * dy <= G.pre2;
-          const float w4 = kCellCode ? __int_as_float((cxu - G.ux_ref + 8) | ((uy - G.uy_ref + 8) << 8)) : p.ph32[j];
-          rec = make_float4(X, Y, __fmul_rn(r.z, G.scale), w4);
+  constexpr int kMaxSeg = 8;
+  static_assert(4 * kMaxSeg + 1 <= kBins + 1, "the segment table lives in a slot's bin array");
+  const int k_lo = floor_div(G.ux_lo, p.Ex), k_hi = floor_div(G.ux_hi, p.Ex);
+  const int n_run = max(0, k_hi - k_lo + 1), n_seg = max(0, G.uy_hi - G.uy_lo + 1) * n_run;
+  if (kJoined && n_seg >= 1 && n_seg <= kMaxSeg) {
+    int* seg = W.bin[slot];  // per segment: first index, first atom, x shift, row; then the total
+    int len = 0, a_lo = 0, shift = 0, uy = 0;
+    if (lane < n_seg) {
+      const int k = k_lo + lane % n_run;
+      uy = G.uy_lo + lane / n_run;
+      shift = k * p.Ex;
+      const int x0 = max(G.ux_lo, shift), x1 = min(G.ux_hi, shift + p.Ex - 1);
+      const int64_t row_base = (int64_t)p.Ex * (pos_mod(uy, p.Ey) + (int64_t)p.Ey * cz);
+      a_lo = p.cell_start[row_base + (x0 - shift)];
+      len = p.cell_start[row_base + (x1 - shift) + 1] - a_lo;
+    }
+    int incl = len;
+#pragma unroll
+    for (int o = 1; o < kMaxSeg; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += t;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, kMaxSeg - 1);
+    if (lane < n_seg) {
+      seg[4 * lane] = incl - len;
+      seg[4 * lane + 1] = a_lo;
+      seg[4 * lane + 2] = shift;
+      seg[4 * lane + 3] = uy;
+    }
+    if (lane == 0) seg[4 * n_seg] = total;
+    __syncwarp();
+    int sg = 0;  // this lane's segment (its indices only grow)
+    auto locate = [&](int i, int& j, int& sh, int& y) {
+      while (i >= seg[4 * (sg + 1)]) ++sg;
+      j = seg[4 * sg + 1] + (i - seg[4 * sg]);
+      sh = seg[4 * sg + 2];
+      y = seg[4 * sg + 3];
+    };
+    constexpr int kRounds = 2;
+    for (int b = 0; b < total; b += 32 * kRounds) {
+      int j[kRounds];
+      bool keep[kRounds];
+      float4 rec[kRounds];
+#pragma unroll
+      for (int r = 0; r < kRounds; ++r) {
+        const int i = b + 32 * r + lane;
+        int sh = 0, y = 0;
+        j[r] = 0;
+        keep[r] = false;
+        rec[r] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (i < total) {
+          locate(i, j[r], sh, y);
+          keep[r] = slab_candidate<kCellCode>(p, G, j[r], sh, y, rec[r]);
         }
-        const unsigned m = __ballot_sync(0xffffffffu, keep);
-        const int cnt = __popc(m);
-        if (n + cnt > CAPS) return false;
-        if (keep) {
-          const int d = n + __popc(m & ((1u << lane) - 1));
-          P[d] = rec;
-          GI[d] = j;
-        }
-        n += cnt;
       }
-      ux = run_hi + 1;
+#pragma unroll
+      for (int r = 0; r < kRounds; ++r)
+        if (b + 32 * r < total && !slab_append<CAPS>(P, GI, n, keep[r], rec[r], j[r], lane)) return false;
+    }
+  } else {
+    for (int uy = G.uy_lo; uy <= G.uy_hi; ++uy) {
+      const int64_t row_base = (int64_t)p.Ex * (pos_mod(uy, p.Ey) + (int64_t)p.Ey * cz);
+      for (int k = k_lo; k <= k_hi; ++k) {
+        const int shift = k * p.Ex;
+        const int x0 = max(G.ux_lo, shift), x1 = min(G.ux_hi, shift + p.Ex - 1);
+        const int a_lo = p.cell_start[row_base + (x0 - shift)];
+        const int a_hi = p.cell_start[row_base + (x1 - shift) + 1];
+        for (int b = a_lo; b < a_hi; b += 32) {
+          const int j = b + lane;
+          bool keep = false;
+          float4 rec = make_float4(0.f, 0.f, 0.f, 0.f);
+          if (j < a_hi) keep = slab_candidate<kCellCode>(p, G, j, shift, uy, rec);
+          if (!slab_append<CAPS>(P, GI, n, keep, rec, j, lane)) return false;
+        }
+      }
     }
   }
   __syncwarp();
@@ -474,12 +564,17 @@ __device__ __noinline__ bool column_tile3(const ColumnParams& p, WarpSmem3<CAPS>
 
   // s = sqrt(log2(e) / (2 sigma^2)): exp(-r^2 / (2 sigma^2)) = ex2(-(s r)^2)
   const double sd = sqrt(p.i2s2 * 1.4426950408889634);
-  Geo G;
-  G.scale = (float)sd;
   const int ixc = min(ix, p.ix1 - 1), iyc = min(iy, p.iy1 - 1);
   const int hx = p.xtab[ixc].x, hy = p.ytab[iyc].x;
   const double fvx = p.xfv[ixc], fvy = p.yfv[iyc];
+  const float cut2 = (float)(p.cut2 * sd * sd);        // (3 sigma)^2 in scaled units
+  const float r3 = sqrtf(cut2) * 1.0001f + 1e-4f;      // z-window half width, rounded up
+  float Xv, Yv;
   {
+    // the tile's frame and footprint, warp-uniform: built here, then read from the warp's
+    // shared memory by the march, which leaves its registers to the per-column state
+    Geo G;
+    G.scale = (float)sd;
     const int big = 1 << 29;
     const int mnx = __reduce_min_sync(0xffffffffu, active ? hx : big);
     const int mxx = __reduce_max_sync(0xffffffffu, active ? hx : -big);
@@ -491,15 +586,13 @@ __device__ __noinline__ bool column_tile3(const ColumnParams& p, WarpSmem3<CAPS>
     G.uy_hi = mxy + 1;
     G.ux_ref = mnx;
     G.uy_ref = mny;
-  }
-  G.a11s = (float)(p.a11 * sd);
-  G.a22s = (float)(p.a22 * sd);
-  G.a33s = (float)(p.a33 * sd);
-  const float Xv = (float)(p.a11 * (fvx + (double)(hx - G.ux_ref)) * sd);
-  const float Yv = (float)(p.a22 * (fvy + (double)(hy - G.uy_ref)) * sd);
-  {
-    const float big = 1e30f;
-    float v = active ? Xv : big, w = active ? -Xv : big, y = active ? Yv : big, z = active ? -Yv : big;
+    G.a11s = (float)(p.a11 * sd);
+    G.a22s = (float)(p.a22 * sd);
+    G.a33s = (float)(p.a33 * sd);
+    Xv = (float)(p.a11 * (fvx + (double)(hx - G.ux_ref)) * sd);
+    Yv = (float)(p.a22 * (fvy + (double)(hy - G.uy_ref)) * sd);
+    const float fbig = 1e30f;
+    float v = active ? Xv : fbig, w = active ? -Xv : fbig, y = active ? Yv : fbig, z = active ? -Yv : fbig;
     for (int o = 16; o > 0; o >>= 1) {
       v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
       w = fminf(w, __shfl_xor_sync(0xffffffffu, w, o));
@@ -510,10 +603,12 @@ __device__ __noinline__ bool column_tile3(const ColumnParams& p, WarpSmem3<CAPS>
     G.xmax = -w;
     G.ymin = y;
     G.ymax = -z;
+    G.pre2 = cut2 * 1.0002f + 1e-3f;
+    __syncwarp();  // a previous tile's march has finished reading the warp's copy
+    if (lane == 0) W.geo = G;
+    __syncwarp();
   }
-  const float cut2 = (float)(p.cut2 * sd * sd);        // (3 sigma)^2 in scaled units
-  const float r3 = sqrtf(cut2) * 1.0001f + 1e-4f;      // z-window half width, rounded up
-  G.pre2 = cut2 * 1.0002f + 1e-3f;
+  const Geo& G = W.geo;
   const float inv_bin = kBins / G.a33s;
   const float sig = (float)p.sigma, b0 = (float)p.b0, bg = (float)p.bg, dzs = (float)p.dz;
   const float r2_to_A2 = (float)(1.0 / (sd * sd));    // scaled r^2 back to A^2 (density)
