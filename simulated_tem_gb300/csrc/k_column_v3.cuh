@@ -59,6 +59,15 @@ struct Geo {
   float a11s, a22s, a33s, scale;
 };
 
+// Scalars of a tile's march, the same in every lane (scaled units where lengths).
+struct TileConst {
+  float cut2;      // (3 sigma)^2
+  float r3;        // z-window half width, rounded up
+  float inv_bin;   // z bins per scaled length
+  float b0, bg, sig, dzs;
+  float r2_to_A2;  // scaled r^2 back to A^2 (density)
+};
+
 template <int CAPS>  // staged atoms per slab
 struct WarpSmem3 {
   float4 p[kRing][CAPS];      // X', Y' (warp frame), z (own cell), phase (cycles) -- lengths scaled by s
@@ -68,6 +77,7 @@ struct WarpSmem3 {
   float4 ba[kBuf];            // step buffer: X', Y', hmax_0, hmax_1
   float4 be[kBuf];            // ex2(-dz_0^2) (cos, sin), ex2(-dz_1^2) (cos, sin)
   Geo geo;                    // the tile's footprint and frame (warp-uniform: here, not in registers)
+  TileConst tc;               // the tile's scalar constants (likewise)
 };
 
 __device__ __forceinline__ float ex2_approx(float x) {
@@ -134,15 +144,13 @@ __device__ __forceinline__ bool slab_append(float4* P, int* GI, int& n, bool kee
 // arrays p, gi, bin and count.
 //
 // The footprint is rows uy of x runs (a run ends where x wraps): segments of consecutive
-// atoms.  Where a thread has 128 registers or more and there are up to 8 segments, the
-// lanes look up all segment ranges at once, join them into one index space (the slot's
-// bin array, free until the sort, holds the table) and gather two 32-lane rounds at a
-// time; otherwise (and in the five-CTA variants, whose 96 registers it would overflow)
-// row by row, one round at a time.  Both routes visit the atoms in the same order (rows,
-// runs, atoms), so the slab's contents and order do not depend on the route.
+// atoms.  With up to 8 segments, the lanes look up all segment ranges at once, join them
+// into one index space (the slot's bin array, free until the sort, holds the table) and
+// gather two 32-lane rounds at a time; otherwise row by row, one round at a time.  Both
+// routes visit the atoms in the same order (rows, runs, atoms), so the slab's contents
+// and order do not depend on the route.
 template <int CAPS, bool kCellCode = false, typename WS>
 __device__ bool load_slab3(const ColumnParams& p, const Geo& G, int u, WS& W, int lane) {
-  constexpr bool kJoined = CAPS >= 128;  // 128 registers or more per thread
   const int cz = pos_mod(u, p.Ez);
   const int slot = u & (kRing - 1);
   float4* P = W.p[slot];
@@ -152,7 +160,7 @@ __device__ bool load_slab3(const ColumnParams& p, const Geo& G, int u, WS& W, in
   static_assert(4 * kMaxSeg + 1 <= kBins + 1, "the segment table lives in a slot's bin array");
   const int k_lo = floor_div(G.ux_lo, p.Ex), k_hi = floor_div(G.ux_hi, p.Ex);
   const int n_run = max(0, k_hi - k_lo + 1), n_seg = max(0, G.uy_hi - G.uy_lo + 1) * n_run;
-  if (kJoined && n_seg >= 1 && n_seg <= kMaxSeg) {
+  if (n_seg >= 1 && n_seg <= kMaxSeg) {
     int* seg = W.bin[slot];  // per segment: first index, first atom, x shift, row; then the total
     int len = 0, a_lo = 0, shift = 0, uy = 0;
     if (lane < n_seg) {
@@ -567,8 +575,6 @@ __device__ __noinline__ bool column_tile3(const ColumnParams& p, WarpSmem3<CAPS>
   const int ixc = min(ix, p.ix1 - 1), iyc = min(iy, p.iy1 - 1);
   const int hx = p.xtab[ixc].x, hy = p.ytab[iyc].x;
   const double fvx = p.xfv[ixc], fvy = p.yfv[iyc];
-  const float cut2 = (float)(p.cut2 * sd * sd);        // (3 sigma)^2 in scaled units
-  const float r3 = sqrtf(cut2) * 1.0001f + 1e-4f;      // z-window half width, rounded up
   float Xv, Yv;
   {
     // the tile's frame and footprint, warp-uniform: built here, then read from the warp's
@@ -603,15 +609,25 @@ __device__ __noinline__ bool column_tile3(const ColumnParams& p, WarpSmem3<CAPS>
     G.xmax = -w;
     G.ymin = y;
     G.ymax = -z;
-    G.pre2 = cut2 * 1.0002f + 1e-3f;
-    __syncwarp();  // a previous tile's march has finished reading the warp's copy
-    if (lane == 0) W.geo = G;
+    TileConst C;
+    C.cut2 = (float)(p.cut2 * sd * sd);
+    C.r3 = sqrtf(C.cut2) * 1.0001f + 1e-4f;
+    C.inv_bin = kBins / G.a33s;
+    C.b0 = (float)p.b0;
+    C.bg = (float)p.bg;
+    C.sig = (float)p.sigma;
+    C.dzs = (float)p.dz;
+    C.r2_to_A2 = (float)(1.0 / (sd * sd));
+    G.pre2 = C.cut2 * 1.0002f + 1e-3f;
+    __syncwarp();  // a previous tile's march has finished reading the warp's copies
+    if (lane == 0) {
+      W.geo = G;
+      W.tc = C;
+    }
     __syncwarp();
   }
   const Geo& G = W.geo;
-  const float inv_bin = kBins / G.a33s;
-  const float sig = (float)p.sigma, b0 = (float)p.b0, bg = (float)p.bg, dzs = (float)p.dz;
-  const float r2_to_A2 = (float)(1.0 / (sd * sd));    // scaled r^2 back to A^2 (density)
+  const TileConst& C = W.tc;
   const unsigned lt = (1u << lane) - 1;
 
   const int np = min(NP, p.n_prec - p.prec_offset);
@@ -679,8 +695,8 @@ __device__ __noinline__ bool column_tile3(const ColumnParams& p, WarpSmem3<CAPS>
       }
       if (!v0 && !v1) continue;
       const float w_lo = v0 ? t0 : t1, w_hi = v1 ? t1 : t0;
-      const int b_lo = max(0, min(kBins, (int)floorf((w_lo - r3) * inv_bin)));
-      const int b_hi = max(0, min(kBins, (int)ceilf((w_hi + r3) * inv_bin)));
+      const int b_lo = max(0, min(kBins, (int)floorf((w_lo - C.r3) * C.inv_bin)));
+      const int b_hi = max(0, min(kBins, (int)ceilf((w_hi + C.r3) * C.inv_bin)));
       const int lo = W.bin[slot][b_lo];
       const int hi = W.bin[slot][b_hi];
       const float4* P = W.p[slot];
@@ -695,8 +711,8 @@ __device__ __noinline__ bool column_tile3(const ColumnParams& p, WarpSmem3<CAPS>
           float sn, cs;
           __sincosf(6.28318531f * q.w, &sn, &cs);  // the phase lies in [-1/2, 1/2) cycles
           const float dz0 = __fsub_rn(q.z, t0), dz1 = __fsub_rn(q.z, t1);
-          const float hm0 = v0 ? __fmaf_rn(-dz0, dz0, cut2) : -1.f;
-          const float hm1 = v1 ? __fmaf_rn(-dz1, dz1, cut2) : -1.f;
+          const float hm0 = v0 ? __fmaf_rn(-dz0, dz0, C.cut2) : -1.f;
+          const float hm1 = v1 ? __fmaf_rn(-dz1, dz1, C.cut2) : -1.f;
           const float dxr = fmaxf(0.f, fmaxf(G.xmin - q.x, q.x - G.xmax));
           const float dyr = fmaxf(0.f, fmaxf(G.ymin - q.y, q.y - G.ymax));
           // margin: the lanes' own rounding of dxy^2 must not reach below the rectangle's
@@ -737,7 +753,7 @@ __device__ __noinline__ bool column_tile3(const ColumnParams& p, WarpSmem3<CAPS>
       if (__any_sync(0xffffffffu, f0 || f1)) {
         if (f0 || f1) {
           const Slice sl0{hz0, zv0, p.zfv[z0], f0}, sl1{hz1, zv1, has1 ? p.zfv[z0 + 1] : 0.0, f1};
-          const Fix fx = exact_fix<CAPS>(p, W, need_lo, need_hi, hz0, G.a33s, cut2, r3, inv_bin, Xv, Yv, hx, hy,
+          const Fix fx = exact_fix<CAPS>(p, W, need_lo, need_hi, hz0, G.a33s, C.cut2, C.r3, C.inv_bin, Xv, Yv, hx, hy,
                                          fvx, fvy, sl0, sl1, has1);
           a0.x += fx.d0.x;
           a0.y += fx.d0.y;
@@ -748,25 +764,26 @@ __device__ __noinline__ bool column_tile3(const ColumnParams& p, WarpSmem3<CAPS>
         __syncwarp();
       }
     }
-    const float rm0 = (cut2 + fminf(rmA.x, rmB.x)) * r2_to_A2, rm1 = (cut2 + fminf(rmA.y, rmB.y)) * r2_to_A2;
+    const float rm0 = (C.cut2 + fminf(rmA.x, rmB.x)) * C.r2_to_A2;
+    const float rm1 = (C.cut2 + fminf(rmA.y, rmB.y)) * C.r2_to_A2;
     // field samples z0 (even) and z0 + 1 (odd), then the RK4 double step (z0-2, z0-1, z0)
-    const Sample s0 = make_sample<kDensity>(a0.x, a0.y, rm0, b0, bg, sig, p.use_density != 0);
+    const Sample s0 = make_sample<kDensity>(a0.x, a0.y, rm0, C.b0, C.bg, C.sig, p.use_density != 0);
     if (z0 == 0) {
       s_first = s0;
     } else {
       const SampleT<T> w0 = widen<T>(s_prev), w1 = widen<T>(s_mid), w2 = widen<T>(s0);
 #pragma unroll
       for (int k = 0; k < NH; ++k)
-        if (k < nh) rk4<T>(w0, w1, w2, aa_at<T, kAaReg>(aa, aag, k), dzs, ph[k]);
+        if (k < nh) rk4<T>(w0, w1, w2, aa_at<T, kAaReg>(aa, aag, k), C.dzs, ph[k]);
     }
     s_prev = s0;
-    if (has1) s_mid = make_sample<kDensity>(a1.x, a1.y, rm1, b0, bg, sig, p.use_density != 0);
+    if (has1) s_mid = make_sample<kDensity>(a1.x, a1.y, rm1, C.b0, C.bg, C.sig, p.use_density != 0);
   }
   if ((p.Mz & 1) == 0) {  // closure x(Mz) = x(0)
     const SampleT<T> w0 = widen<T>(s_prev), w1 = widen<T>(s_mid), w2 = widen<T>(s_first);
 #pragma unroll
     for (int k = 0; k < NH; ++k)
-      if (k < nh) rk4<T>(w0, w1, w2, aa_at<T, kAaReg>(aa, aag, k), dzs, ph[k]);
+      if (k < nh) rk4<T>(w0, w1, w2, aa_at<T, kAaReg>(aa, aag, k), C.dzs, ph[k]);
   }
   // |phi_g|^2 summed over the angles in order, rounded the same way for either form
   float acc = 0.f;
