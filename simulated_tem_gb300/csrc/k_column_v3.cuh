@@ -76,7 +76,7 @@ struct WarpSmem3 {
   int count[kRing];
   float4 ba[kBuf];            // step buffer: X', Y', hmax_0, hmax_1
   float4 be[kBuf];            // ex2(-dz_0^2) (cos, sin), ex2(-dz_1^2) (cos, sin)
-  Geo geo;                    // the tile's footprint and frame (warp-uniform: here, not in registers)
+  Geo geo;                    // the tile's footprint and frame (one angle per pass: here, not in registers)
   TileConst tc;               // the tile's scalar constants (likewise)
 };
 
@@ -144,12 +144,14 @@ __device__ __forceinline__ bool slab_append(float4* P, int* GI, int& n, bool kee
 // arrays p, gi, bin and count.
 //
 // The footprint is rows uy of x runs (a run ends where x wraps): segments of consecutive
-// atoms.  With up to 8 segments, the lanes look up all segment ranges at once, join them
-// into one index space (the slot's bin array, free until the sort, holds the table) and
-// gather two 32-lane rounds at a time; otherwise row by row, one round at a time.  Both
+// atoms.  With kJoined and up to 8 segments, the lanes look up all segment ranges at once,
+// join them into one index space (the slot's bin array, free until the sort, holds the
+// table) and gather two 32-lane rounds at a time; otherwise row by row, one round at a
+// time (with more than one angle per pass the march's phases leave no registers for a
+// second round: measured, 16 angles spilled more and ran 10 % slower).  Both
 // routes visit the atoms in the same order (rows, runs, atoms), so the slab's contents
 // and order do not depend on the route.
-template <int CAPS, bool kCellCode = false, typename WS>
+template <int CAPS, bool kCellCode = false, bool kJoined = true, typename WS>
 __device__ bool load_slab3(const ColumnParams& p, const Geo& G, int u, WS& W, int lane) {
   const int cz = pos_mod(u, p.Ez);
   const int slot = u & (kRing - 1);
@@ -160,7 +162,7 @@ __device__ bool load_slab3(const ColumnParams& p, const Geo& G, int u, WS& W, in
   static_assert(4 * kMaxSeg + 1 <= kBins + 1, "the segment table lives in a slot's bin array");
   const int k_lo = floor_div(G.ux_lo, p.Ex), k_hi = floor_div(G.ux_hi, p.Ex);
   const int n_run = max(0, k_hi - k_lo + 1), n_seg = max(0, G.uy_hi - G.uy_lo + 1) * n_run;
-  if (n_seg >= 1 && n_seg <= kMaxSeg) {
+  if (kJoined && n_seg >= 1 && n_seg <= kMaxSeg) {
     int* seg = W.bin[slot];  // per segment: first index, first atom, x shift, row; then the total
     int len = 0, a_lo = 0, shift = 0, uy = 0;
     if (lane < n_seg) {
@@ -576,10 +578,16 @@ __device__ __noinline__ bool column_tile3(const ColumnParams& p, WarpSmem3<CAPS>
   const int hx = p.xtab[ixc].x, hy = p.ytab[iyc].x;
   const double fvx = p.xfv[ixc], fvy = p.yfv[iyc];
   float Xv, Yv;
+  // the tile's frame, footprint and scalars, warp-uniform: with one angle per pass the march
+  // reads them from the warp's shared memory, which leaves its registers to the per-column
+  // state (measured: 3.26 -> 3.06 ms on the 1.2M-atom image); with more angles the phases
+  // take those registers anyway and the shared-memory reads cost (16 angles: 8 % slower),
+  // so they stay in registers
+  constexpr bool kSmemTile = NP == 1;
+  Geo Gr;
+  TileConst Cr;
   {
-    // the tile's frame and footprint, warp-uniform: built here, then read from the warp's
-    // shared memory by the march, which leaves its registers to the per-column state
-    Geo G;
+    Geo& G = Gr;
     G.scale = (float)sd;
     const int big = 1 << 29;
     const int mnx = __reduce_min_sync(0xffffffffu, active ? hx : big);
@@ -609,7 +617,7 @@ __device__ __noinline__ bool column_tile3(const ColumnParams& p, WarpSmem3<CAPS>
     G.xmax = -w;
     G.ymin = y;
     G.ymax = -z;
-    TileConst C;
+    TileConst& C = Cr;
     C.cut2 = (float)(p.cut2 * sd * sd);
     C.r3 = sqrtf(C.cut2) * 1.0001f + 1e-4f;
     C.inv_bin = kBins / G.a33s;
@@ -619,15 +627,17 @@ __device__ __noinline__ bool column_tile3(const ColumnParams& p, WarpSmem3<CAPS>
     C.dzs = (float)p.dz;
     C.r2_to_A2 = (float)(1.0 / (sd * sd));
     G.pre2 = C.cut2 * 1.0002f + 1e-3f;
-    __syncwarp();  // a previous tile's march has finished reading the warp's copies
-    if (lane == 0) {
-      W.geo = G;
-      W.tc = C;
+    if constexpr (kSmemTile) {
+      __syncwarp();  // a previous tile's march has finished reading the warp's copies
+      if (lane == 0) {
+        W.geo = G;
+        W.tc = C;
+      }
+      __syncwarp();
     }
-    __syncwarp();
   }
-  const Geo& G = W.geo;
-  const TileConst& C = W.tc;
+  const Geo& G = kSmemTile ? W.geo : Gr;
+  const TileConst& C = kSmemTile ? W.tc : Cr;
   const unsigned lt = (1u << lane) - 1;
 
   const int np = min(NP, p.n_prec - p.prec_offset);
@@ -671,7 +681,7 @@ __device__ __noinline__ bool column_tile3(const ColumnParams& p, WarpSmem3<CAPS>
     bool ok = true;
     while (ring_hi < need_hi && ok) {
       ++ring_hi;
-      ok = load_slab3<CAPS>(p, G, ring_hi, W, lane);
+      ok = load_slab3<CAPS, false, (NP == 1)>(p, G, ring_hi, W, lane);
     }
     if (!ok) {
       if (lane == 0) atomicExch(&p.counters[4], 1ull);
