@@ -143,8 +143,8 @@ def path_roofline(peaks, n_acc, n_kept, n_atoms, voxels, voxel_prec, pixels, den
 
 SWEEP_G = ((1, 1, 0), (2, 0, 0), (2, 1, 1))
 # DRAM bytes (read + write) of one k_column_fp32_v3 launch on the 1.2M-atom image, from an
-# ncu capture of `python bench.py --ncu-case fp32` (51.53 MB read + 1.77 MB written)
-COLUMN_TRAFFIC_BYTES = 5.330e7
+# ncu capture of `python bench.py --ncu-case fp32` (51.58 MB read + 2.60 MB written)
+COLUMN_TRAFFIC_BYTES = 5.418e7
 
 
 def sweep_specs(cell, n_tomo=41, n_prec=16, gs=SWEEP_G):
@@ -801,11 +801,14 @@ class ClockSampler:
 
 def measure_fp32_peak():
     from simulated_tem_gb300 import _lib
-    out = (ctypes.c_double * 4)()
+    out = (ctypes.c_double * 5)()
     rc = _lib.peaks_lib().stp_measure_peaks(out)
     if rc != 0:
         return None
-    return {"fp32_tflops": out[0], "fp64_tflops": out[1], "mufu_ex2_gops": out[2], "mufu_sin_gops": out[3]}
+    # the FP32 peak is the larger of the scalar and the packed FP32x2 FMA rates (the
+    # integrator issues FP32x2 instructions)
+    return {"fp32_tflops": max(out[0], out[4]), "fp32_scalar_tflops": out[0], "fp32x2_tflops": out[4],
+            "fp64_tflops": out[1], "mufu_ex2_gops": out[2], "mufu_sin_gops": out[3]}
 
 
 def run_gpu(args):

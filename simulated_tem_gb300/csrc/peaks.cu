@@ -32,6 +32,23 @@ __global__ void fp32_fma_kernel(float* out, float b, float c) {
   if (s == 1234.5f) out[blockIdx.x] = s;  // keeps the chains alive
 }
 
+// The same on packed FP32x2 multiply-adds (two FMAs per instruction), the form the
+// column integrator uses.
+__global__ void fp32x2_fma_kernel(float* out, float b, float c) {
+  float2 a[kChains];
+#pragma unroll
+  for (int i = 0; i < kChains; ++i) a[i] = make_float2(threadIdx.x * 1e-3f + i, threadIdx.x * 2e-3f + i);
+  const float2 b2 = make_float2(b, b), c2 = make_float2(c, c);
+  for (int it = 0; it < kIters; ++it) {
+#pragma unroll
+    for (int i = 0; i < kChains; ++i) a[i] = __ffma2_rn(a[i], b2, c2);
+  }
+  float s = 0.f;
+#pragma unroll
+  for (int i = 0; i < kChains; ++i) s += a[i].x + a[i].y;
+  if (s == 1234.5f) out[blockIdx.x] = s;
+}
+
 __global__ void fp64_fma_kernel(double* out, double b, double c) {
   double a[kChains];
 #pragma unroll
@@ -98,8 +115,9 @@ double time_ms(F&& launch, cudaStream_t st) {
 
 }  // namespace
 
-// out[0] FP32 FMA-pipe TFLOP/s (2 flops per FMA), out[1] FP64 TFLOP/s,
-// out[2] MUFU ex2 Gop/s, out[3] MUFU sin Gop/s.  Returns 0 or a CUDA error code.
+// out[0] FP32 FMA-pipe TFLOP/s on scalar FMAs (2 flops per FMA), out[1] FP64 TFLOP/s,
+// out[2] MUFU ex2 Gop/s, out[3] MUFU sin Gop/s, out[4] FP32 TFLOP/s on packed FP32x2
+// FMAs (4 flops per instruction).  Returns 0 or a CUDA error code.
 extern "C" int stp_measure_peaks(double* out) {
   int dev = 0, sms = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return 1;
@@ -119,6 +137,9 @@ extern "C" int stp_measure_peaks(double* out) {
   out[2] = double(kChains) * (kIters / 4) * threads / (ms * 1e-3) / 1e9;
   ms = time_ms([&] { mufu_kernel<1><<<blocks, kThreads, 0, st>>>((float*)scratch); }, st);
   out[3] = double(kChains) * (kIters / 4) * threads / (ms * 1e-3) / 1e9;
+
+  ms = time_ms([&] { fp32x2_fma_kernel<<<blocks, kThreads, 0, st>>>((float*)scratch, 0.999f, 1e-3f); }, st);
+  out[4] = 4.0 * kChains * kIters * threads / (ms * 1e-3) / 1e12;
 
   cudaError_t err = cudaStreamSynchronize(st);
   cudaStreamDestroy(st);
