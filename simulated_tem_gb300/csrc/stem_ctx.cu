@@ -49,6 +49,7 @@ struct st_ctx {
   size_t cap_bimg = 0;
   unsigned long long* h_counters = nullptr;  // pinned
   void* h_stage = nullptr;                   // pinned staging for tables and job descriptors
+  cudaEvent_t ev_stage = nullptr;            // recorded after the last copy out of h_stage
   size_t cap_stage = 0;
   cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
   st_stats stats{};
@@ -544,11 +545,15 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
   // ---- per-image tables and job descriptors, staged through pinned memory
   const size_t tab_bytes = (xoff[n] + yoff[n] + zoff[n]) * (sizeof(int2) + sizeof(double)) + aoff[n] * 12;
   const size_t job_bytes = (size_t)n * sizeof(BinParams) + cj.size() * sizeof(ColumnJob);
+  // the staging buffer may still feed a previous call's copies (a call that failed before
+  // its final synchronisation), and growing it frees it: wait for those copies alone, not
+  // for the stream, so that the host builds the tables while work already queued (st_image's
+  // atom upload) runs
+  if (c->ev_stage) cudaEventSynchronize(c->ev_stage);
   e = ensure_host(c->h_stage, c->cap_stage, tab_bytes + job_bytes + 256);
   if (e == cudaSuccess) e = ensure(c->d_binjobs, c->cap_binjobs, (size_t)n);
   if (e == cudaSuccess && !cj.empty()) e = ensure(c->d_coljobs, c->cap_coljobs, cj.size());
   if (e != cudaSuccess) return cuda_fail(c, e, "allocating job descriptors");
-  cudaStreamSynchronize(st);  // the staging buffer may still feed a previous call's copies
   unsigned char* hp = (unsigned char*)c->h_stage;
   int2* hxt = (int2*)hp;
   int2* hyt = hxt + xoff[n];
@@ -588,6 +593,8 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
   cudaMemcpyAsync(c->s.aaf, haaf, aoff[n] * sizeof(float), cudaMemcpyHostToDevice, st);
   cudaMemcpyAsync(c->d_binjobs, hbp, (size_t)n * sizeof(BinParams), cudaMemcpyHostToDevice, st);
   if (!cj.empty()) cudaMemcpyAsync(c->d_coljobs, hcj, cj.size() * sizeof(ColumnJob), cudaMemcpyHostToDevice, st);
+  if (!c->ev_stage) cudaEventCreateWithFlags(&c->ev_stage, cudaEventDisableTiming);
+  if (c->ev_stage) cudaEventRecord(c->ev_stage, st);
 
   // ---- per-image column launches (general FP32 or FP64 kernel), epilogues, image clearing
   auto columns_per_image = [&](int64_t kept_cap, bool all) -> cudaError_t {
@@ -721,6 +728,7 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
       if (!cj.empty()) {
         e = cudaMemcpyAsync(c->d_coljobs, hcj, cj.size() * sizeof(ColumnJob), cudaMemcpyHostToDevice, st);
         if (e != cudaSuccess) return cuda_fail(c, e, "copying column jobs");
+        if (c->ev_stage) cudaEventRecord(c->ev_stage, st);
       }
     }
     e = enqueue(false, true);
@@ -862,6 +870,7 @@ extern "C" void st_destroy(st_ctx* c) {
     if (e) cudaEventDestroy(e);
   for (auto& e : c->tev)
     if (e) cudaEventDestroy(e);
+  if (c->ev_stage) cudaEventDestroy(c->ev_stage);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
