@@ -143,8 +143,8 @@ def path_roofline(peaks, n_acc, n_kept, n_atoms, voxels, voxel_prec, pixels, den
 
 SWEEP_G = ((1, 1, 0), (2, 0, 0), (2, 1, 1))
 # DRAM bytes (read + write) of one k_column_fp32_v3 launch on the 1.2M-atom image, from an
-# ncu capture of `python bench.py --ncu-case fp32` (51.58 MB read + 2.60 MB written)
-COLUMN_TRAFFIC_BYTES = 5.418e7
+# ncu capture of `python bench.py --ncu-case fp32` (51.59 MB read + 2.36 MB written)
+COLUMN_TRAFFIC_BYTES = 5.395e7
 
 
 def sweep_specs(cell, n_tomo=41, n_prec=16, gs=SWEEP_G):
