@@ -28,7 +28,10 @@
 //   then read with two 16-byte loads per atom.
 //
 // Per atom and lane: two loads, the in-plane distance (3 FP32 ops), one ex2, two
-// compares and two predicated FP32x2 multiply-adds (both slices' cos and sin).
+// compares and two predicated FP32x2 multiply-adds (both slices' cos and sin); the loop
+// runs four atom pairs per iteration, because at the 18-20 warps per SM that the
+// registers and shared memory allow, the kernel is bound by dependent-instruction
+// latency rather than by any pipe.
 //
 // Precision: FP32 throughout the march; the weight is the product of two ex2 values (a
 // few ulp).  The FP32 cutoff test may decide an atom within rounding of the cutoff
@@ -93,14 +96,6 @@ __device__ __forceinline__ int pos_mod(int a, int n) {
 
 __device__ __forceinline__ int floor_div(int a, int n) { return (a >= 0) ? a / n : -((-a + n - 1) / n); }
 
-
-// Gather slab u (its cells in the patch footprint, atoms within 3 sigma of the
-// patch rectangle) into its ring slot and order it by z bin in place; false
-// when it holds more than CAPS atoms.
-// kCellCode: the fourth float of an entry holds the atom's unwrapped cell relative to the warp's
-// reference cells, (ux - ux_ref + 8) | (uy - uy_ref + 8) << 8 (the FP64 kernel's exact
-// distances need it), instead of its phase.  WS: any warp-memory layout with the slab
-// arrays p, gi, bin and count.
 // One gathered candidate: atom j of a cell in row uy, x cells shifted by `shift` (an
 // unwrapped run), in the warp's scaled frame; keep when within 3 sigma of the patch.
 template <bool kCellCode>
