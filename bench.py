@@ -298,6 +298,7 @@ def batched_legs(ctx, cell, stream, flush, steps, warmup, peaks=None, cpu=True):
     stages = dict(time_batch.stages)
     launches = ctx.stats().n_launches
     variant = _lib.lib().st_tune_variant_name(ctx.stats().ring_variant).decode()
+    slab_atoms = ctx.stats().ring_slab_atoms  # 192 or 256: the larger staging tiers ran
     t = float(np.mean(ms)) * 1e-3
     n_img, n_pass = len(specs), sum(len(aa) for _, aa in specs)
     vs = sum((G.ix1 - G.ix0) * (G.iy1 - G.iy0) * G.Mz * len(aa) for G, aa in specs)
@@ -321,7 +322,7 @@ def batched_legs(ctx, cell, stream, flush, steps, warmup, peaks=None, cpu=True):
                     "passes_per_s": n_pass / t, "voxel_slices_per_s": vs / t, "ms_per_batch": t * 1e3,
                     "steps": steps, "image_sizes": sorted({(G_.Mx, G_.My, G_.Mz) for G_, _ in specs}),
                     "kept_atoms": st.n_kept, "column_kernel": st.column_kernel, "stages": stages,
-                    "launches_per_batch": launches, "ring_variant": variant,
+                    "launches_per_batch": launches, "ring_variant": variant, "ring_slab_atoms": slab_atoms,
                     "roofline": roof(st, ([G_ for G_, _ in specs], [len(aa_) for _, aa_ in specs]),
                                      stages["ms_column"], t * 1e3, len(x) * n_img),
                     "accuracy_tilt20_per_g": acc,
@@ -347,6 +348,7 @@ def batched_legs(ctx, cell, stream, flush, steps, warmup, peaks=None, cpu=True):
     stages = dict(time_batch.stages)
     launches = ctx.stats().n_launches
     variant = _lib.lib().st_tune_variant_name(ctx.stats().ring_variant).decode()
+    slab_atoms = ctx.stats().ring_slab_atoms  # 192 or 256: the larger staging tiers ran
     t = float(np.mean(ms)) * 1e-3
     vs = sum((G.ix1 - G.ix0) * (G.iy1 - G.iy0) * G.Mz for G, _, _ in specs)
     k = int(np.argmax([len(x_) for _, _, x_ in specs]))
@@ -363,7 +365,7 @@ def batched_legs(ctx, cell, stream, flush, steps, warmup, peaks=None, cpu=True):
                      "images": len(specs), "atoms": int(sum(len(x_) for _, _, x_ in specs)),
                      "images_per_s": len(specs) / t, "voxel_slices_per_s": vs / t, "ms_per_batch": t * 1e3,
                      "steps": steps, "kept_atoms": st.n_kept, "column_kernel": st.column_kernel, "stages": stages,
-                     "launches_per_batch": launches, "ring_variant": variant,
+                     "launches_per_batch": launches, "ring_variant": variant, "ring_slab_atoms": slab_atoms,
                      "roofline": roof(st, ([G_ for G_, _, _ in specs], [1] * len(specs)), stages["ms_column"],
                                       t * 1e3, sum(len(x_) for _, _, x_ in specs)),
                      "accuracy_largest_cell": acc}

@@ -881,13 +881,14 @@ cudaError_t launch3(K kernel, const Ring3Args& a, int tiles, int blocks_per_sm) 
 
 // Instances of one angle bucket NP.  Tuning variants (tier 0, no statistics, no mask):
 // the tile shape (8 x 4, 4 x 8, 16 x 2 columns) and the slab capacity of the first tier
-// (128 atoms, four CTAs per SM; 96 atoms, five -- three with 16 angles, whose phases
-// need more registers than four CTAs leave: the tuner weighs the spills against the
-// occupancy).  Tiers 1 and 2 (192 and 256 atoms per slab, three and two CTAs
-// per SM), the statistics and the tile-masked instances use 8 x 4 tiles.
+// (128 atoms, four CTAs per SM; 96 atoms, five -- both three with 16 angles, whose phases
+// need more registers than four CTAs leave).  Tiers 1 and 2 (192 and 256 atoms per slab,
+// three and two CTAs per SM), the statistics and the tile-masked instances use 8 x 4
+// tiles.
 template <int NP, bool kDensity>
 cudaError_t ring3_dispatch(const Ring3Args& a) {
   constexpr int B96 = NP >= 16 ? 3 : 5;
+  constexpr int B128 = NP >= 16 ? 3 : 4;  // 16 angles: 168 registers, no spills (at four CTAs they spill)
   const int* T = a.tiles;
   if (a.masked) {  // the variant's tile shape, so that a masked image equals the plain one on its tiles
     if constexpr (NP == 1) {
@@ -910,11 +911,11 @@ cudaError_t ring3_dispatch(const Ring3Args& a) {
   if (a.tier == 1) return launch3<192>(k_column_fp32_v3<NP, kDensity, false, 3, 192, 8, false>, a, T[0], 3);
   switch (a.variant) {
     case 1: return launch3<96>(k_column_fp32_v3<NP, kDensity, false, B96, 96, 8, false>, a, T[0], B96);
-    case 2: return launch3<128>(k_column_fp32_v3<NP, kDensity, false, 4, 128, 4, false>, a, T[1], 4);
+    case 2: return launch3<128>(k_column_fp32_v3<NP, kDensity, false, B128, 128, 4, false>, a, T[1], B128);
     case 3: return launch3<96>(k_column_fp32_v3<NP, kDensity, false, B96, 96, 4, false>, a, T[1], B96);
-    case 4: return launch3<128>(k_column_fp32_v3<NP, kDensity, false, 4, 128, 16, false>, a, T[2], 4);
+    case 4: return launch3<128>(k_column_fp32_v3<NP, kDensity, false, B128, 128, 16, false>, a, T[2], B128);
     case 5: return launch3<96>(k_column_fp32_v3<NP, kDensity, false, B96, 96, 16, false>, a, T[2], B96);
-    default: return launch3<128>(k_column_fp32_v3<NP, kDensity, false, 4, 128, 8, false>, a, T[0], 4);
+    default: return launch3<128>(k_column_fp32_v3<NP, kDensity, false, B128, 128, 8, false>, a, T[0], B128);
   }
 }
 
