@@ -44,6 +44,7 @@ constexpr float kPreMargin = 1e-3f;      // scaled r^2: the FP32 prefilter's mar
 
 template <int CAPS>
 struct WarpSmem64 {
+  static_assert(CAPS % 32 == 0, "the z sort holds CAPS / 32 atoms per lane");
   float4 p[kRing][CAPS];  // X', Y', z (scaled FP32, for the prefilter), cell code
   int gi[kRing][CAPS];    // index of the kept atom
   int bin[kRing][kBins + 1];

@@ -73,6 +73,7 @@ struct TileConst {
 
 template <int CAPS>  // staged atoms per slab
 struct WarpSmem3 {
+  static_assert(CAPS % 32 == 0, "the z sort holds CAPS / 32 atoms per lane");
   float4 p[kRing][CAPS];      // X', Y' (warp frame), z (own cell), phase (cycles) -- lengths scaled by s
   int gi[kRing][CAPS];        // index of the kept atom (its records in global memory)
   int bin[kRing][kBins + 1];  // bin[b]: first atom of z bin b; bin[kBins] = count
