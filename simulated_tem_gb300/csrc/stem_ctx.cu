@@ -933,6 +933,7 @@ int collect_jobs(st_ctx* c, int32_t n_jobs, const st_job* jobs, std::vector<Job>
 int run_batch(st_ctx* c, const std::vector<Job>& js, int32_t flags, cudaStream_t st) {
   const int n_jobs = (int)js.size();
   st_stats total{};
+  total.ring_variant = -1;  // none ran
   int first = 0;
   while (first < n_jobs) {
     int last = first;
@@ -957,6 +958,8 @@ int run_batch(st_ctx* c, const std::vector<Job>& js, int32_t flags, cudaStream_t
     total.ms_bin += S.ms_bin;
     total.ms_column += S.ms_column;
     total.column_kernel = std::max(total.column_kernel, S.column_kernel);
+    total.ring_variant = std::max(total.ring_variant, S.ring_variant);
+    total.ring_slab_atoms = std::max(total.ring_slab_atoms, S.ring_slab_atoms);
     total.n_launches += S.n_launches;
     first = last;
   }

@@ -355,3 +355,19 @@ def test_plan_recovers_from_slab_overflow(ctx):
         assert np.abs(imgs[0].cpu().numpy().T - ref).max() <= FP32_TOL
     finally:
         plan.close()
+
+
+def test_batch_stats_report_the_variant():
+    """A batch's statistics (its binning groups merged) name the slab-ring variant that ran
+    and its staging capacity, as a single image's do."""
+    specs, _ = _mixed_specs(True)
+    c = imaging.Context(0)
+    try:
+        c.tune(3)
+        _batch(c, specs, _lib.ST_FLAG_FP32 | _lib.ST_FLAG_AVERAGE)
+        st = c.stats()
+        assert st.column_kernel == 2
+        assert st.ring_variant == 3
+        assert st.ring_slab_atoms in (96, 192, 256)  # the variant's tier, or a larger one after an overflow
+    finally:
+        c.close()
