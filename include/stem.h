@@ -118,10 +118,11 @@ int st_image_device(st_ctx* ctx, const st_geom* geom, const double* d_x, int64_t
  * the first staging tier (128 or 96 atoms) and with it the CTAs per SM; the
  * images of variants of one tile shape are identical, those of different
  * shapes agree to FP32 rounding (their atoms are summed in different orders).
- * ST_TUNE_AUTO (the default): the first pass of each (angles per pass,
- * density) kind in a context with at least 4,096 warp tiles times every
- * variant on the real work, keeps the fastest for the context's later calls,
- * and leaves that variant's own images.  ST_TUNE_OFF: variant 0 always.
+ * ST_TUNE_AUTO (the default): the first pass of each kind (angles per pass,
+ * density) on images of each shape (image and link-cell dimensions) in a
+ * context, with at least 4,096 warp tiles, times every variant on the real
+ * work, keeps the fastest for the context's later calls on that kind and
+ * shape, and leaves that variant's own images.  ST_TUNE_OFF: variant 0 always.
  * mode >= 0: that variant always.  No counterpart in the reference. */
 #define ST_TUNE_AUTO (-1)
 #define ST_TUNE_OFF (-2)

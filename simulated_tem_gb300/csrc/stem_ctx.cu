@@ -59,7 +59,7 @@ struct st_ctx {
   int min_slab_tier = 0;       // STEM_RING_SLABS=192 or 256: start the slab ring at that capacity
   int last_column_kernel = 0;  // 1 general FP32, 2 slab-ring FP32, 3 general FP64, 4 slab-ring FP64
   int tune_mode = ST_TUNE_AUTO;
-  std::map<int, int> ring_tuned;  // (angles per pass, density) -> fastest slab-ring variant
+  std::map<uint64_t, int> ring_tuned;  // (pass kind, image and link-cell shape) -> fastest slab-ring variant
   std::map<uint64_t, int> ring_big;  // (pass kind, image and link-cell shape) -> slab tier it needs (1, 2)
   cudaEvent_t tev[3] = {nullptr, nullptr, nullptr};
   int last_ring_variant = -1;
@@ -642,8 +642,9 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
   // (the variants and the kernel choice of the eager run are replayed).
   const bool stats = (flags & ST_FLAG_STATS) != 0;
   std::vector<int> pass_variant(passes, 0);
-  // big slabs when an earlier call of this context needed them for the same kind of pass on
-  // images of the same shape (the first ring image's image and link-cell dimensions)
+  // a pass's kind (angles per pass, density, precision) and the shape of its images (the first
+  // ring image's image and link-cell dimensions): the key of the slab tier an earlier call of
+  // this context needed, and of the variant it tuned
   auto big_key = [&](int pass) -> uint64_t {
     uint64_t h = (uint64_t)(ring_np_bucket(std::min(width, ring_np - pass * width)) * 2 + (dens ? 1 : 0)) +
                  (fp32 ? 0u : 1000u);
@@ -686,7 +687,8 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
         ce = ring_launch(pass_variant[pass]);
         continue;
       }
-      const int key = ring_np_bucket(np_pass) * 2 + (dens ? 1 : 0);
+      // the variant tuned for this kind of pass (angles, density) on images of this shape
+      const uint64_t key = big_key(pass);
       int v = 0;
       if (c->tune_mode >= 0 && fp32) {
         v = c->tune_mode;

@@ -371,3 +371,27 @@ def test_batch_stats_report_the_variant():
         assert st.ring_slab_atoms in (96, 192, 256)  # the variant's tier, or a larger one after an overflow
     finally:
         c.close()
+
+
+def test_autotuner_keys_on_image_shape():
+    """With ST_TUNE_AUTO the first large image of each shape in a context times the variants
+    (more kernel launches than a plain call); the next image of that shape reuses the choice."""
+    cell = synth.make_cell(100, 100, 8, 13, n_voids=2, void_radius=(5.0, 8.0), with_screw=True)
+    jobs = []
+    for M in ((4, 4), (5, 5)):
+        t, x, _ = imaging.d2bi_condition(cell.a_super, synth.A0_FE, (0, 0, 1), (1, 1, 0), cell.pos, sg=0.01, M=M)
+        G, aa = t.image_geometry(len(x))
+        assert ((G.ix1 - G.ix0 + 7) // 8) * ((G.iy1 - G.iy0 + 3) // 4) >= 4096  # large enough to tune
+        jobs.append((G, x, aa))
+    assert (jobs[0][0].Mx, jobs[0][0].My) != (jobs[1][0].Mx, jobs[1][0].My)
+    c = imaging.Context(0)
+    try:
+        launches, variants = [], []
+        for G, x, aa in jobs + jobs:
+            c.image(G, x, aa, flags=_lib.ST_FLAG_FP32)
+            launches.append(c.stats().n_launches)
+            variants.append(c.stats().ring_variant)
+    finally:
+        c.close()
+    assert launches[0] > launches[2] and launches[1] > launches[3]
+    assert variants[2] == variants[0] and variants[3] == variants[1]
