@@ -207,10 +207,15 @@ extern template cudaError_t ring3_launch_np<16>(const Ring3Args&);
 }  // namespace ring3
 cudaError_t launch_column_fp64(const ColumnParams& p, cudaStream_t st);
 // The FP64 slab-ring launch (k_column_f64ring.cu) over the jobs of one pass of at most 4
-// precession angles; slab tiers 0, 1, 2 stage 128, 192, 256 atoms.
+// precession angles; slab tiers 0, 1, 2 stage 128, 192, 256 atoms; `four`: every job's
+// steps of four slices fit the ring (four_slices_fit).
 cudaError_t launch_column_fp64_ring(const ColumnJob* d_jobs, int n_jobs, int tiles, int max_np, int slab_tier,
-                                    bool masked, unsigned* work, const unsigned long long* counters, int64_t cap,
-                                    cudaStream_t st);
+                                    bool masked, bool four, unsigned* work, const unsigned long long* counters,
+                                    int64_t cap, cudaStream_t st);
+// Whether every step of four slices (z = 0, 4, 8 ...) of an image has home z cells that
+// rise by at most one cell without wrapping, so that the cells the step needs (one more on
+// either side) fit the slab ring's four slots.
+bool four_slices_fit(const st_geom* g);
 cudaError_t launch_epilogue(double* img, int Mx, int My, int ix0, int ix1, int iy0, int iy1, double scale,
                             int bright, cudaStream_t st);
 cudaError_t launch_blur(const double* d_in, double* d_tmp, double* d_out, int nx, int ny, const double* d_kernel,

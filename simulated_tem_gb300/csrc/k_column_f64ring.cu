@@ -39,66 +39,69 @@ using ring3::load_slab3;
 using ring3::pos_mod;
 
 constexpr int kWarps = 4;
-constexpr int kBuf64 = 64;               // step buffer (flushed at 32)
 constexpr float kPreMargin = 1e-3f;      // scaled r^2: the FP32 prefilter's margin over its error
 
-template <int CAPS>
+// SL slices per step (2, or 4 where every image's steps of four slices fit the ring); the
+// step buffer holds kN atoms and is flushed at kN - 32, before a round of 32 may add more.
+template <int CAPS, int SL>
 struct WarpSmem64 {
   static_assert(CAPS % 32 == 0, "the z sort holds CAPS / 32 atoms per lane");
+  static constexpr int kN = SL == 4 ? 48 : 64;
+  static constexpr int kFlush = kN - 32;
   float4 p[kRing][CAPS];  // X', Y', z (scaled FP32, for the prefilter), cell code
   int gi[kRing][CAPS];    // index of the kept atom
   int bin[kRing][kBins + 1];
   int count[kRing];
-  float4 ba[kBuf64];      // X', Y', hmax_0 + margin, hmax_1 + margin (FP32 prefilter)
-  double2 bf[kBuf64];     // f_x, f_y (the reference's cell fractions)
-  double2 bz[kBuf64];     // d_z^2 for slice 0, 1 (+inf where the slab does not serve the slice)
-  double2 be0[kBuf64];    // exp(-d_z0^2 / 2 sigma^2) (cos, sin)
-  double2 be1[kBuf64];    // exp(-d_z1^2 / 2 sigma^2) (cos, sin)
-  int bc[kBuf64];         // cell code (unwrapped x, y cell relative to the warp's reference cells)
+  float4 ba[kN];          // X', Y', the largest hmax of the step's slices + margin (FP32 prefilter), 0
+  double2 bf[kN];         // f_x, f_y (the reference's cell fractions)
+  double2 be[kN][SL];     // per slice: exp(-d_z^2 / 2 sigma^2) (cos, sin)
+  double bz[kN][SL];      // per slice: d_z^2 (+inf where the slab does not serve the slice)
+  int bc[kN];             // cell code (unwrapped x, y cell relative to the warp's reference cells)
 };
 
+template <int SL>
 struct Acc64 {
-  double sr0, si0, sr1, si1, rm0, rm1;
+  double sr[SL], si[SL], rm[SL];
   unsigned n_acc;
 };
 
-// Every buffered atom against this lane's column at both slices.
-__device__ __forceinline__ void consume64(const float4* __restrict__ BA, const double2* __restrict__ BF,
-                                          const double2* __restrict__ BZ, const double2* __restrict__ BE0,
-                                          const double2* __restrict__ BE1, const int* __restrict__ BC, int n,
-                                          float Xv, float Yv, int hxo, int hyo, const double* dzx,
-                                          const double* dzy, double a11, double a22, double cut2, double i2s2,
-                                          Acc64& A) {
+// Every buffered atom against this lane's column at the step's SL slices.  One in-plane
+// exp per accepted atom serves all of them.
+template <int CAPS, int SL>
+__device__ __forceinline__ void consume64(const WarpSmem64<CAPS, SL>& W, int n, float Xv, float Yv, int hxo, int hyo,
+                                          const double* dzx, const double* dzy, double a11, double a22, double cut2,
+                                          double i2s2, Acc64<SL>& A) {
   for (int i = 0; i < n; ++i) {
-    const float4 q = BA[i];
+    const float4 q = W.ba[i];
     const float dx = q.x - Xv, dy = q.y - Yv;
     const float h = fmaf(dx, dx, dy * dy);
-    if (!(h <= fmaxf(q.z, q.w))) continue;  // beyond the cutoff at both slices, with margin
-    const int code = BC[i];
+    if (!(h <= q.z)) continue;  // beyond the cutoff at every slice, with margin
+    const int code = W.bc[i];
     const int kx = (code & 255) - hxo, ky = ((code >> 8) & 255) - hyo;
     if (kx < -1 || kx > 1 || ky < -1 || ky > 1) continue;  // outside the lane's 27 cells
-    const double2 f = BF[i];
+    const double2 f = W.bf[i];
     const double d0 = DM(a11, DA(f.x, dzx[kx + 1]));
     const double d1 = DM(a22, DA(f.y, dzy[ky + 1]));
     const double dxy = DA(DM(d0, d0), DM(d1, d1));
-    const double2 z = BZ[i];
-    const double dd0 = DA(dxy, z.x), dd1 = DA(dxy, z.y);
-    const bool acc0 = dd0 <= cut2, acc1 = dd1 <= cut2;
-    if (!acc0 && !acc1) continue;
-    const double wxy = exp(DM(-dxy, i2s2));
-    if (acc0) {
-      const double2 e = BE0[i];
-      A.sr0 = DA(A.sr0, DM(wxy, e.x));
-      A.si0 = DA(A.si0, DM(wxy, e.y));
-      A.rm0 = fmin(A.rm0, dd0);
-      ++A.n_acc;
+    double dd[SL];
+    bool acc[SL], any = false;
+#pragma unroll
+    for (int k = 0; k < SL; ++k) {
+      dd[k] = DA(dxy, W.bz[i][k]);
+      acc[k] = dd[k] <= cut2;
+      any = any || acc[k];
     }
-    if (acc1) {
-      const double2 e = BE1[i];
-      A.sr1 = DA(A.sr1, DM(wxy, e.x));
-      A.si1 = DA(A.si1, DM(wxy, e.y));
-      A.rm1 = fmin(A.rm1, dd1);
-      ++A.n_acc;
+    if (!any) continue;
+    const double wxy = exp(DM(-dxy, i2s2));
+#pragma unroll
+    for (int k = 0; k < SL; ++k) {
+      if (acc[k]) {
+        const double2 e = W.be[i][k];
+        A.sr[k] = DA(A.sr[k], DM(wxy, e.x));
+        A.si[k] = DA(A.si[k], DM(wxy, e.y));
+        A.rm[k] = fmin(A.rm[k], dd[k]);
+        ++A.n_acc;
+      }
     }
   }
 }
@@ -113,8 +116,8 @@ __device__ __forceinline__ Sample64 sample64(const ColumnParams& p, double sr, d
   return Sample64{DM(p.b0, rho), DM(p.b0, rho), DM(bgr, xr), DM(bgr, xi)};
 }
 
-template <int NP, int CAPS, bool kMasked>
-__device__ __noinline__ bool column_tile64(const ColumnParams& p, WarpSmem64<CAPS>& W, int tile, int lane) {
+template <int NP, int CAPS, bool kMasked, int SL>
+__device__ __noinline__ bool column_tile64(const ColumnParams& p, WarpSmem64<CAPS, SL>& W, int tile, int lane) {
   constexpr int TX = 8, TY = 4;
   const int Wd = p.ix1 - p.ix0;
   const int tiles_x = (Wd + TX - 1) / TX;
@@ -193,14 +196,34 @@ __device__ __noinline__ bool column_tile64(const ColumnParams& p, WarpSmem64<CAP
   unsigned n_acc = 0;
   unsigned long long n_tst = 0;
 
-  for (int z0 = 0; z0 < p.Mz; z0 += 2) {
-    const bool has1 = z0 + 1 < p.Mz;
-    const int2 e0 = p.ztab[z0];
-    const int2 e1 = has1 ? p.ztab[z0 + 1] : e0;
-    const int hz0 = e0.x, hz1 = e1.x;
-    const float zv0 = __int_as_float(e0.y), zv1 = __int_as_float(e1.y);
-    const double fz0 = p.zfv[z0], fz1 = has1 ? p.zfv[z0 + 1] : 0.0;
-    const int need_lo = hz0 - 1, need_hi = hz1 + 1;
+  using WS = WarpSmem64<CAPS, SL>;
+  for (int z0 = 0; z0 < p.Mz; z0 += SL) {
+    // the step's slices: home z cells, FP32 depths in the frame of home cell hz[0] (the
+    // table gives each pair's from its even slice's home cell), FP64 fractions
+    int hz[SL];
+    float zv[SL];
+    double fz[SL];
+    bool has[SL];
+#pragma unroll
+    for (int k = 0; k < SL; ++k) {
+      has[k] = z0 + k < p.Mz;
+      const int2 e = p.ztab[has[k] ? z0 + k : z0];
+      hz[k] = has[k] ? e.x : hz[0];
+      zv[k] = has[k] ? __int_as_float(e.y) : 0.f;
+      fz[k] = has[k] ? p.zfv[z0 + k] : 0.0;
+    }
+#pragma unroll
+    for (int k = 2; k < SL; ++k)
+      if (has[k]) zv[k] = __fadd_rn(zv[k], __fmul_rn(G.a33s, (float)(hz[k & ~1] - hz[0])));
+    int hz_last = hz[0];
+#pragma unroll
+    for (int k = 1; k < SL; ++k)
+      if (has[k]) hz_last = hz[k];
+    const int need_lo = hz[0] - 1, need_hi = hz_last + 1;
+    if (need_hi - need_lo + 1 > kRing) {  // the host takes four slices only where they fit
+      if (lane == 0) atomicExch(&p.counters[4], 1ull);
+      return false;
+    }
     if (need_lo > ring_hi || need_hi < ring_lo) {
       ring_lo = need_lo;
       ring_hi = need_lo - 1;
@@ -215,50 +238,67 @@ __device__ __noinline__ bool column_tile64(const ColumnParams& p, WarpSmem64<CAP
       if (lane == 0) atomicExch(&p.counters[4], 1ull);
       return false;
     }
-    Acc64 A{0.0, 0.0, 0.0, 0.0, (double)FLT_MAX, (double)FLT_MAX, 0u};
+    Acc64<SL> A;
+#pragma unroll
+    for (int k = 0; k < SL; ++k) {
+      A.sr[k] = A.si[k] = 0.0;
+      A.rm[k] = (double)FLT_MAX;
+    }
+    A.n_acc = 0u;
     int nb = 0;
     for (int u = need_lo; u <= need_hi; ++u) {
       const int slot = u & (kRing - 1);
-      const float zoff = __fmul_rn(G.a33s, (float)(u - hz0));
-      const float t0 = __fsub_rn(zv0, zoff), t1 = __fsub_rn(zv1, zoff);
+      const float zoff = __fmul_rn(G.a33s, (float)(u - hz[0]));
       // the reference's 27 cells in z: slab u serves slice k within one cell of its home cell
-      const bool v0 = u - hz0 >= -1 && u - hz0 <= 1;
-      const bool v1 = has1 && u - hz1 >= -1 && u - hz1 <= 1;
-      if (!v0 && !v1) continue;
-      const float w_lo = v0 ? t0 : t1, w_hi = v1 ? t1 : t0;
+      float t[SL];
+      bool v[SL];
+      float w_lo = 1e30f, w_hi = -1e30f;
+#pragma unroll
+      for (int k = 0; k < SL; ++k) {
+        t[k] = __fsub_rn(zv[k], zoff);
+        v[k] = has[k] && u - hz[k] >= -1 && u - hz[k] <= 1;
+        if (v[k]) {
+          w_lo = fminf(w_lo, t[k]);
+          w_hi = fmaxf(w_hi, t[k]);
+        }
+      }
+      if (w_lo > w_hi) continue;
       const int b_lo = max(0, min(kBins, (int)floorf((w_lo - r3) * inv_bin)));
       const int b_hi = max(0, min(kBins, (int)ceilf((w_hi + r3) * inv_bin)));
       const int lo = W.bin[slot][b_lo];
       const int hi = W.bin[slot][b_hi];
       for (int b = lo; b < hi; b += 32) {
-        // one atom per lane: the FP32 prefilter bounds, the z distance and z factor in FP64
+        // one atom per lane: the FP32 prefilter bound, the z distances and z factors in FP64
         const int j = b + lane;
         bool keep = false;
         float4 A4;
-        double2 F, Z, E0, E1;
+        double2 F, E[SL];
+        double Z[SL];
         int code = 0;
         if (j < hi) {
           const float4 q = W.p[slot][j];
-          const float dz0 = q.z - t0, dz1 = q.z - t1;
-          const float hm0 = v0 ? cut2f - dz0 * dz0 + kPreMargin : -1.f;
-          const float hm1 = v1 ? cut2f - dz1 * dz1 + kPreMargin : -1.f;
+          float hmax = -1.f;
+#pragma unroll
+          for (int k = 0; k < SL; ++k) {
+            const float dz = q.z - t[k];
+            hmax = fmaxf(hmax, v[k] ? cut2f - dz * dz + kPreMargin : -1.f);
+          }
           const float dxr = fmaxf(0.f, fmaxf(G.xmin - q.x, q.x - G.xmax));
           const float dyr = fmaxf(0.f, fmaxf(G.ymin - q.y, q.y - G.ymax));
-          keep = fmaf(dxr, dxr, dyr * dyr) <= fmaxf(hm0, hm1) + kPreMargin;
+          keep = fmaf(dxr, dxr, dyr * dyr) <= hmax + kPreMargin;
           if (keep) {
             const int gi = W.gi[slot][j];
             const double4_32a f = p.f64[gi];
             const double2 cs = p.cs64[gi];
-            const double d20 = DM(p.a33, DA(f.z, DS((double)(u - hz0), fz0)));
-            const double d21 = DM(p.a33, DA(f.z, DS((double)(u - hz1), fz1)));
-            const double q0 = v0 ? DM(d20, d20) : (double)INFINITY;
-            const double q1 = v1 ? DM(d21, d21) : (double)INFINITY;
-            const double ez0 = v0 ? exp(DM(-q0, p.i2s2)) : 0.0, ez1 = v1 ? exp(DM(-q1, p.i2s2)) : 0.0;
-            A4 = make_float4(q.x, q.y, hm0, hm1);
+#pragma unroll
+            for (int k = 0; k < SL; ++k) {
+              const double d2 = DM(p.a33, DA(f.z, DS((double)(u - hz[k]), fz[k])));
+              Z[k] = v[k] ? DM(d2, d2) : (double)INFINITY;
+              const double ez = v[k] ? exp(DM(-Z[k], p.i2s2)) : 0.0;
+              E[k] = make_double2(DM(ez, cs.x), DM(ez, cs.y));
+            }
+            A4 = make_float4(q.x, q.y, hmax, 0.f);
             F = make_double2(f.x, f.y);
-            Z = make_double2(q0, q1);
-            E0 = make_double2(DM(ez0, cs.x), DM(ez0, cs.y));
-            E1 = make_double2(DM(ez1, cs.x), DM(ez1, cs.y));
             code = __float_as_int(q.w);
           }
         }
@@ -267,16 +307,17 @@ __device__ __noinline__ bool column_tile64(const ColumnParams& p, WarpSmem64<CAP
           const int d = nb + __popc(m & lt);
           W.ba[d] = A4;
           W.bf[d] = F;
-          W.bz[d] = Z;
-          W.be0[d] = E0;
-          W.be1[d] = E1;
+#pragma unroll
+          for (int k = 0; k < SL; ++k) {
+            W.bz[d][k] = Z[k];
+            W.be[d][k] = E[k];
+          }
           W.bc[d] = code;
         }
         nb += __popc(m);
-        if (nb >= 32) {
+        if (nb >= WS::kFlush) {
           __syncwarp();
-          consume64(W.ba, W.bf, W.bz, W.be0, W.be1, W.bc, nb, Xv, Yv, hxo, hyo, dzx, dzy, p.a11, p.a22, p.cut2,
-                    p.i2s2, A);
+          consume64<CAPS, SL>(W, nb, Xv, Yv, hxo, hyo, dzx, dzy, p.a11, p.a22, p.cut2, p.i2s2, A);
           n_tst += (unsigned long long)nb;
           __syncwarp();
           nb = 0;
@@ -285,22 +326,27 @@ __device__ __noinline__ bool column_tile64(const ColumnParams& p, WarpSmem64<CAP
     }
     if (nb > 0) {
       __syncwarp();
-      consume64(W.ba, W.bf, W.bz, W.be0, W.be1, W.bc, nb, Xv, Yv, hxo, hyo, dzx, dzy, p.a11, p.a22, p.cut2, p.i2s2,
-                A);
+      consume64<CAPS, SL>(W, nb, Xv, Yv, hxo, hyo, dzx, dzy, p.a11, p.a22, p.cut2, p.i2s2, A);
       n_tst += (unsigned long long)nb;
       __syncwarp();
     }
     n_acc += A.n_acc;
-    const Sample64 s0 = sample64(p, A.sr0, A.si0, A.rm0);
-    if (z0 == 0) {
-      s_first = s0;
-    } else {
+    // the RK4 double steps: pair (z, z + 1) closes the double step (z - 2, z - 1, z) at z
 #pragma unroll
-      for (int k = 0; k < NP; ++k)
-        if (k < np) rk4_64(s_prev, s_mid, s0, aa[k], p.dz, ph[k]);
+    for (int pr = 0; pr < SL / 2; ++pr) {
+      const int z = z0 + 2 * pr;
+      if (z >= p.Mz) break;
+      const Sample64 se = sample64(p, A.sr[2 * pr], A.si[2 * pr], A.rm[2 * pr]);
+      if (z == 0) {
+        s_first = se;
+      } else {
+#pragma unroll
+        for (int k = 0; k < NP; ++k)
+          if (k < np) rk4_64(s_prev, s_mid, se, aa[k], p.dz, ph[k]);
+      }
+      s_prev = se;
+      if (z + 1 < p.Mz) s_mid = sample64(p, A.sr[2 * pr + 1], A.si[2 * pr + 1], A.rm[2 * pr + 1]);
     }
-    s_prev = s0;
-    if (has1) s_mid = sample64(p, A.sr1, A.si1, A.rm1);
   }
   if ((p.Mz & 1) == 0) {
 #pragma unroll
@@ -320,7 +366,7 @@ __device__ __noinline__ bool column_tile64(const ColumnParams& p, WarpSmem64<CAP
     *o = acc;
   }
   if (p.want_stats) {
-    unsigned long long acc_w = active ? n_acc : 0u, tst_w = active ? 2 * n_tst : 0u;
+    unsigned long long acc_w = active ? n_acc : 0u, tst_w = active ? (unsigned long long)SL * n_tst : 0u;
     for (int o = 16; o > 0; o >>= 1) {
       acc_w += __shfl_xor_sync(0xffffffffu, acc_w, o);
       tst_w += __shfl_xor_sync(0xffffffffu, tst_w, o);
@@ -333,13 +379,13 @@ __device__ __noinline__ bool column_tile64(const ColumnParams& p, WarpSmem64<CAP
   return true;
 }
 
-template <int NP, int CAPS, bool kMasked, int kMinBlocks>
+template <int NP, int CAPS, bool kMasked, int kMinBlocks, int SL>
 __global__ void __launch_bounds__(kWarps * 32, kMinBlocks)
     k_column_fp64_ring(const ColumnJob* __restrict__ jobs, int n_jobs, int total_tiles, unsigned* __restrict__ work,
                        const unsigned long long* __restrict__ counters, int64_t cap) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  WarpSmem64<CAPS>& W = reinterpret_cast<WarpSmem64<CAPS>*>(smem_raw)[warp];
+  WarpSmem64<CAPS, SL>& W = reinterpret_cast<WarpSmem64<CAPS, SL>*>(smem_raw)[warp];
   if ((int64_t)counters[0] > cap) return;
   for (;;) {
     int tile = 0;
@@ -355,14 +401,14 @@ __global__ void __launch_bounds__(kWarps * 32, kMinBlocks)
       else
         hi = mid - 1;
     }
-    if (!column_tile64<NP, CAPS, kMasked>(jobs[lo].p, W, tile - jobs[lo].tile_base[0], lane)) break;
+    if (!column_tile64<NP, CAPS, kMasked, SL>(jobs[lo].p, W, tile - jobs[lo].tile_base[0], lane)) break;
   }
 }
 
-template <int CAPS, typename K>
+template <int CAPS, int SL, typename K>
 cudaError_t launch64(K kernel, const ColumnJob* jobs, int n_jobs, int tiles, unsigned* work,
                      const unsigned long long* counters, int64_t cap, int blocks_per_sm, cudaStream_t st) {
-  const size_t smem = sizeof(WarpSmem64<CAPS>) * kWarps;
+  const size_t smem = sizeof(WarpSmem64<CAPS, SL>) * kWarps;
   cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   int dev = 0, sms = 148;
@@ -377,31 +423,42 @@ cudaError_t launch64(K kernel, const ColumnJob* jobs, int n_jobs, int tiles, uns
   return cudaGetLastError();
 }
 
-template <int NP, bool kMasked>
+template <int NP, bool kMasked, int SL>
 cudaError_t launch_tier(int tier, const ColumnJob* jobs, int n_jobs, int tiles, unsigned* work,
                         const unsigned long long* counters, int64_t cap, cudaStream_t st) {
   if (tier >= 2)
-    return launch64<256>(k_column_fp64_ring<NP, 256, kMasked, 1>, jobs, n_jobs, tiles, work, counters, cap, 1, st);
+    return launch64<256, SL>(k_column_fp64_ring<NP, 256, kMasked, 1, SL>, jobs, n_jobs, tiles, work, counters, cap, 1,
+                             st);
   if (tier == 1)
-    return launch64<192>(k_column_fp64_ring<NP, 192, kMasked, 2>, jobs, n_jobs, tiles, work, counters, cap, 2, st);
-  return launch64<128>(k_column_fp64_ring<NP, 128, kMasked, 3>, jobs, n_jobs, tiles, work, counters, cap, 3, st);
+    return launch64<192, SL>(k_column_fp64_ring<NP, 192, kMasked, 2, SL>, jobs, n_jobs, tiles, work, counters, cap, 2,
+                             st);
+  return launch64<128, SL>(k_column_fp64_ring<NP, 128, kMasked, 3, SL>, jobs, n_jobs, tiles, work, counters, cap, 3,
+                           st);
 }
 
 }  // namespace ring64
 
 // The FP64 slab-ring launch over the jobs of one pass (at most 4 precession angles).
+// `four`: every job's steps of four slices fit the ring (four_slices_fit), so a launch of
+// one angle per pass marches four slices per step: each in-plane exp then serves four
+// slices instead of two, and the images are the two-slice march's to the bit (each slice's
+// sum takes the same accepted atoms in the same order).  Tile-masked launches march two.
 cudaError_t launch_column_fp64_ring(const ColumnJob* d_jobs, int n_jobs, int tiles, int max_np, int slab_tier,
-                                    bool masked, unsigned* work, const unsigned long long* counters, int64_t cap,
-                                    cudaStream_t st) {
+                                    bool masked, bool four, unsigned* work, const unsigned long long* counters,
+                                    int64_t cap, cudaStream_t st) {
   cudaError_t e = cudaMemsetAsync(work, 0, sizeof(unsigned), st);
   if (e != cudaSuccess || tiles <= 0) return e;
   if (masked) {
     if (max_np != 1) return cudaErrorInvalidValue;
-    return ring64::launch_tier<1, true>(slab_tier, d_jobs, n_jobs, tiles, work, counters, cap, st);
+    return ring64::launch_tier<1, true, 2>(slab_tier, d_jobs, n_jobs, tiles, work, counters, cap, st);
   }
-  if (max_np <= 1) return ring64::launch_tier<1, false>(slab_tier, d_jobs, n_jobs, tiles, work, counters, cap, st);
-  if (max_np <= 2) return ring64::launch_tier<2, false>(slab_tier, d_jobs, n_jobs, tiles, work, counters, cap, st);
-  return ring64::launch_tier<4, false>(slab_tier, d_jobs, n_jobs, tiles, work, counters, cap, st);
+  // four slices with one angle per pass (with more, the phases leave no registers for the
+  // four slices' sums)
+  if (four && max_np <= 1)
+    return ring64::launch_tier<1, false, 4>(slab_tier, d_jobs, n_jobs, tiles, work, counters, cap, st);
+  if (max_np <= 1) return ring64::launch_tier<1, false, 2>(slab_tier, d_jobs, n_jobs, tiles, work, counters, cap, st);
+  if (max_np <= 2) return ring64::launch_tier<2, false, 2>(slab_tier, d_jobs, n_jobs, tiles, work, counters, cap, st);
+  return ring64::launch_tier<4, false, 2>(slab_tier, d_jobs, n_jobs, tiles, work, counters, cap, st);
 }
 
 }  // namespace stem

@@ -188,6 +188,19 @@ void depth_table(const st_geom* g, int2* tab, const double* fv) {
   }
 }
 
+bool four_slices_fit(const st_geom* g) {
+  std::vector<int2> tab((size_t)g->Mz);
+  std::vector<double> fv((size_t)g->Mz);
+  axis_table(g->Mz, g->a_vox[8], g->lc_delta[2], g->ia_col[8], g->Ez, tab.data(), fv.data());
+  for (int z0 = 0; z0 < g->Mz; z0 += 4) {
+    const int last = std::min(z0 + 3, g->Mz - 1);
+    for (int z = z0 + 1; z <= last; ++z)
+      if (tab[z].x < tab[z - 1].x) return false;  // wrapped
+    if (tab[last].x - tab[z0].x > 1) return false;
+  }
+  return true;
+}
+
 int validate(st_ctx* c, const st_geom* g, int64_t ldx, int64_t nAtoms, int32_t nPrec) {
   if (!g) return fail(c, ST_ERR_ARG, "geometry is null");
   if (ldx < 3) return fail(c, ST_ERR_ARG, "ldx must be >= 3");
@@ -662,6 +675,8 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
   }
   bool masked = false;  // tile-masked ring jobs take the masked kernel instances
   for (int r : ring_jobs) masked = masked || cps[r].tile_mask != nullptr;
+  bool four64 = !fp32 && !ring_jobs.empty();  // the FP64 ring marches four slices per step where all fit
+  for (int r : ring_jobs) four64 = four64 && four_slices_fit(jobs[r].g);
   // with_bin false: the column phase only, on the binning already in place
   auto enqueue = [&](bool capturing, bool with_bin) -> cudaError_t {
     cudaError_t ce = cudaSuccess;
@@ -677,8 +692,8 @@ int run_images(st_ctx* c, const std::vector<Job>& jobs, int32_t flags, cudaStrea
       auto ring_launch = [&](int v) {
         if (!fp32)
           return launch_column_fp64_ring(c->d_coljobs + (size_t)pass * n_ring, n_ring,
-                                         pass_tiles[(size_t)pass * kRingShapes], np_pass, big, masked, c->d_work,
-                                         c->s.counters, cap, st);
+                                         pass_tiles[(size_t)pass * kRingShapes], np_pass, big, masked, four64,
+                                         c->d_work, c->s.counters, cap, st);
         return launch_column_fp32_ring(c->d_coljobs + (size_t)pass * n_ring, n_ring,
                                        pass_tiles.data() + (size_t)pass * kRingShapes, np_pass,
                                        dens, stats, v, big, masked, c->d_work, c->s.counters, cap, st);
