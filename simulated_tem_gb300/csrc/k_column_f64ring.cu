@@ -3,8 +3,9 @@
 // The pixel loop of computeD2BI_img (Lib_DynamicalTwoBeamImaging.f90:1870-1900) with the
 // neighbour search of Lib_LinkCell3D.f90:1515-1605 and the integrator of :2316-2480, in
 // the reference's FP64 arithmetic, on the FP32 path's slab ring (k_column_v3.cuh): one
-// warp per 8 x 4 pixel columns, two depth slices per step, the atoms of the link-cell
-// slabs staged once in warp-private shared memory and ordered by z bin.
+// warp per 8 x 4 pixel columns, two depth slices per step (four with one angle per pass
+// where every image's steps of four slices fit the ring), the atoms of the link-cell slabs
+// staged once in warp-private shared memory and ordered by z bin.
 //
 // What is exact, and how:
 // * The accept decision is the reference's: d_a = a_aa (f_a + (k_a - zi_frac_a)) for
@@ -13,9 +14,11 @@
 //   and the unwrapped 27-cell offsets k.  An FP32 test with a margin only skips atoms far
 //   from the cutoff, so the accepted set and count equal the reference's.
 // * The weight: the reference evaluates exp(-d.d / 2 sigma^2) per pair.  Here the Gaussian
-//   is split, exp(-(d_x^2 + d_y^2) / 2 sigma^2) per atom and column for both slices of a
+//   is split, exp(-(d_x^2 + d_y^2) / 2 sigma^2) per atom and column for all slices of a
 //   step, times exp(-d_z^2 / 2 sigma^2) per atom and slice, formed once by the warp: the
-//   product differs from the reference's weight by a few ulp.
+//   product differs from the reference's weight by a few ulp.  Each slice's sum takes the
+//   same accepted atoms in the same order at two or four slices per step, so both give the
+//   same image to the bit.
 // * The sums S run in the step buffer's order rather than the 27-cell loop's; both are
 //   FP64 sums of the same terms.
 // The field sample, the density and the RK4 double step are fp64_column.cuh's, the
