@@ -50,3 +50,14 @@ def test_errors_without_context():
     assert L.st_blur(None, None, 1, 1, 1.0, None) == _lib.ST_ERR_ARG
     h = ctypes.c_void_p()
     assert L.st_d2bi_create(ctypes.byref(h), None, 1, 1, 1, 1.0, None, None, 200.0, 4, 4) == _lib.ST_ERR_ARG
+
+
+def test_tuning_variants_are_named_without_gpu():
+    """st_tune_variants / st_tune_variant_name are host-only: six slab-ring variants, the
+    tile shape and slab capacity in each name, "invalid" out of range."""
+    L = _lib.lib()
+    n = L.st_tune_variants()
+    assert n == 6
+    names = [L.st_tune_variant_name(v).decode() for v in range(n)]
+    assert names == ["8x4 slab128", "8x4 slab96", "4x8 slab128", "4x8 slab96", "16x2 slab128", "16x2 slab96"]
+    assert L.st_tune_variant_name(-1).decode() == "invalid" and L.st_tune_variant_name(n).decode() == "invalid"
