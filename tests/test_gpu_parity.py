@@ -359,3 +359,23 @@ def test_fp32_ring_truncated_z_search(ctx, short):
     f64 = ctx.image(G, x, aa, flags=0)
     assert np.abs(ring - gen).max() <= 2e-5
     assert np.abs(ring - f64).max() <= FP32_TOL
+
+
+@pytest.mark.parametrize("n,M", [((10, 10, 7), (4, 5)), ((10, 10, 6), (4, 3)), ((10, 10, 7), (4, 3))])
+def test_fp64_uneven_slice_counts_match_oracle(ctx, n, M):
+    """The plain FP64 path with 35, 18 and 21 slices per column (3, 2 and 1 past a multiple
+    of four: the four-slice march ends on a partial step; odd counts also leave the last
+    interval to the integrator's rule) against the oracle, counts included."""
+    cell = synth.small_cell(n=n, seed=7, n_voids=1, radius=(3.0, 5.0), with_screw=True)
+    t, xw, _ = imaging.d2bi_condition(cell.a_super, synth.A0_FE, (0, 0, 1), (1, 1, 0), cell.pos, sg=0.01, M=M)
+    args = O.make_args(cell.a_super, synth.A0_FE, (0, 0, 1), (1, 1, 0), sg=0.01, M=M)
+    so, xo, _ = O.setup(args, cell.pos)
+    assert np.array_equal(xw, xo)
+    G, aa = t.image_geometry(len(xw))
+    assert G.Mz % 4 != 0
+    got = ctx.image(G, xw, aa, flags=_lib.ST_FLAG_STATS)
+    st = ctx.stats()
+    assert st.column_kernel == 4  # the FP64 slab ring
+    want, ost = oracle_patch(so, xw, 1, 0.005)
+    assert np.abs(got - want).max() <= FP64_TOL
+    assert st.n_kept == ost.n_kept and st.n_accepted == ost.n_accepted
